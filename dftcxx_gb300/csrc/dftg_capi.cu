@@ -1,0 +1,508 @@
+// dftg_capi.cu -- extern "C" entry points of include/dftg.h.
+//
+// Owns the context (device buffers, stream, call-order state) and sequences the
+// kernels of one grid Fock build:
+//   set_density      K3 rho = 2 phi^T P phi              (gridpoint.cpp:82-84)
+//   correct_density  K6 c = sum Z / int w rho, rho *= c   (moleculargrid.cpp:132-146)
+//   xc points        LDA point kernel, cxc = w v_xc, E_xc (dft.cpp:394-424)
+//   hartree          K5a-e, cj = w V / 2                  (moleculargrid.cpp:336-380)
+//   contraction      K4 XC and J in one pass over phi     (dft.cpp:426-432, atomicgrid.cpp:471-488)
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+#include "dftg_internal.cuh"
+#include "lebedev_data.h"
+
+namespace dftg {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line)
+{
+    set_error("CUDA error %s (%s) at %s:%d in %s", cudaGetErrorName(e), cudaGetErrorString(e), file, line, what);
+    return e == cudaErrorMemoryAllocation ? DFTG_ERR_NOMEM : DFTG_ERR_CUDA;
+}
+
+static double dfact(int n) { double r = 1.0; for (int k = n; k > 1; k -= 2) r *= k; return r; }
+
+// GTO normalisation constant, cgf.cpp:102-114 (truncated pi of cgf.cpp:103)
+double gto_norm(double alpha, int l, int m, int n)
+{
+    double nom = std::pow(2.0, 2.0 * (l + m + n) + 3.0 / 2.0) * std::pow(alpha, (l + m + n) + 3.0 / 2.0);
+    double denom = (l < 1 ? 1 : dfact(2 * l - 1)) * (m < 1 ? 1 : dfact(2 * m - 1)) * (n < 1 ? 1 : dfact(2 * n - 1)) *
+                   std::pow(kPiTrunc, 3.0 / 2.0);
+    return std::sqrt(nom / denom);
+}
+
+template <typename T>
+static int dalloc(T **p, size_t n)
+{
+    if (n == 0) n = 1;
+    DFTG_CUDA(cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T)));
+    return DFTG_OK;
+}
+
+#define DFTG_TRY(x) do { int rc_ = (x); if (rc_ != DFTG_OK) return rc_; } while (0)
+
+static void free_ctx(dftg_ctx *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    void *bufs[] = {c->d_atoms, c->d_rab, c->d_rn, c->d_wrad, c->d_leb, c->d_bf_lmn, c->d_bf_off, c->d_bf_atom,
+                    c->d_pa, c->d_pcn, c->d_x, c->d_y, c->d_z, c->d_w, c->d_wb, c->d_rho, c->d_V, c->d_Vown,
+                    c->d_cxc, c->d_cj, c->d_cxc32, c->d_cj32, c->d_phi, c->d_phi32, c->d_P, c->d_P32, c->d_J,
+                    c->d_XC, c->d_part, c->d_red, c->d_scal, c->d_Y, c->d_Yw, c->d_pre, c->d_pre32, c->d_rec,
+                    c->d_rec32, c->d_rholm, c->d_U, c->d_LU, c->d_piv, c->d_sx, c->d_spl, c->d_spl32, c->d_tiles,
+                    c->d_ints_work};
+    for (void *b : bufs)
+        if (b) cudaFree(b);
+    if (c->h_scal) cudaFreeHost(c->h_scal);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+}
+
+static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *basis, const dftg_grid_params *g)
+{
+    c->device = g->device;
+    DFTG_CUDA(cudaSetDevice(c->device));
+    DFTG_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+    c->stream = c->own_stream;
+
+    // molecule and basis
+    c->natoms = mol->natoms;
+    c->Z.assign(mol->Z, mol->Z + mol->natoms);
+    c->xyz.assign(mol->xyz, mol->xyz + 3 * mol->natoms);
+    c->nbf = basis->nbf;
+    c->bf_atom.assign(basis->bf_atom, basis->bf_atom + c->nbf);
+    c->bf_lmn.assign(basis->bf_lmn, basis->bf_lmn + 3 * c->nbf);
+    c->bf_off.assign(c->nbf + 1, 0);
+    for (int i = 0; i < c->nbf; ++i) c->bf_off[i + 1] = c->bf_off[i] + basis->bf_nprim[i];
+    c->nprim = c->bf_off[c->nbf];
+    c->alpha.assign(basis->prim_alpha, basis->prim_alpha + c->nprim);
+    c->coef.assign(basis->prim_coef, basis->prim_coef + c->nprim);
+    c->norm.resize(c->nprim);
+    std::vector<double> pcn(c->nprim);
+    for (int i = 0; i < c->nbf; ++i)
+        for (int k = c->bf_off[i]; k < c->bf_off[i + 1]; ++k) {
+            c->norm[k] = gto_norm(c->alpha[k], c->bf_lmn[3 * i], c->bf_lmn[3 * i + 1], c->bf_lmn[3 * i + 2]);
+            pcn[k] = c->coef[k] * c->norm[k];
+        }
+
+    // radial grid, atomicgrid.cpp:44-63
+    c->nrad = g->radial_points;
+    c->leb = g->lebedev_order;
+    c->nang = dftg_lebedev_npts[c->leb];
+    c->lmax = g->lmax;
+    c->nlm = (c->lmax + 1) * (c->lmax + 1);
+    c->npts = (size_t)c->natoms * c->nrad * c->nang;
+    c->npad = (c->npts + kPtsAlign - 1) / kPtsAlign * kPtsAlign;
+    c->r_n.resize(c->nrad);
+    c->w_rad.resize(c->nrad);
+    const double f = kPi / (double)(c->nrad + 1);
+    for (int p = 1; p <= c->nrad; ++p) {
+        double w = f * std::pow(std::sin(f * (double)p), 2.0);
+        const double x = std::cos(f * (double)p);
+        c->r_n[p - 1] = (1.0 + x) / (1.0 - x);
+        w = w / std::sqrt(1.0 - std::pow(x, 2.0)) * 2.0 / std::pow(1.0 - x, 2.0);
+        c->w_rad[p - 1] = w;
+    }
+
+    const size_t np = c->npad, nn = (size_t)c->nbf * c->nbf, nlm = c->nlm, N = c->nrad;
+    DFTG_TRY(dalloc(&c->d_atoms, 4 * (size_t)c->natoms));
+    DFTG_TRY(dalloc(&c->d_rab, (size_t)c->natoms * c->natoms));
+    DFTG_TRY(dalloc(&c->d_rn, N));
+    DFTG_TRY(dalloc(&c->d_wrad, N));
+    DFTG_TRY(dalloc(&c->d_leb, 4 * (size_t)c->nang));
+    DFTG_TRY(dalloc(&c->d_bf_lmn, 3 * (size_t)c->nbf));
+    DFTG_TRY(dalloc(&c->d_bf_off, (size_t)c->nbf + 1));
+    DFTG_TRY(dalloc(&c->d_bf_atom, (size_t)c->nbf));
+    DFTG_TRY(dalloc(&c->d_pa, (size_t)c->nprim));
+    DFTG_TRY(dalloc(&c->d_pcn, (size_t)c->nprim));
+    DFTG_TRY(dalloc(&c->d_x, np));
+    DFTG_TRY(dalloc(&c->d_y, np));
+    DFTG_TRY(dalloc(&c->d_z, np));
+    DFTG_TRY(dalloc(&c->d_w, np));
+    DFTG_TRY(dalloc(&c->d_wb, np));
+    DFTG_TRY(dalloc(&c->d_rho, np));
+    DFTG_TRY(dalloc(&c->d_V, np));
+    DFTG_TRY(dalloc(&c->d_Vown, np));
+    DFTG_TRY(dalloc(&c->d_cxc, np));
+    DFTG_TRY(dalloc(&c->d_cj, np));
+    DFTG_TRY(dalloc(&c->d_cxc32, np));
+    DFTG_TRY(dalloc(&c->d_cj32, np));
+    DFTG_TRY(dalloc(&c->d_phi, np * c->nbf));
+    DFTG_TRY(dalloc(&c->d_phi32, np * c->nbf));
+    DFTG_TRY(dalloc(&c->d_P, nn));
+    DFTG_TRY(dalloc(&c->d_P32, nn));
+    DFTG_TRY(dalloc(&c->d_J, nn));
+    DFTG_TRY(dalloc(&c->d_XC, nn));
+    size_t part = contract_part_elems(c->nbf, c->npad);
+    const size_t spline_work = 3 * (size_t)c->natoms * nlm * N;
+    c->part_elems = part > spline_work ? part : spline_work;
+    DFTG_TRY(dalloc(&c->d_part, c->part_elems));
+    c->red_elems = reduction_elems(c->npad, c->natoms, c->nrad, c->nang) + 64;
+    DFTG_TRY(dalloc(&c->d_red, c->red_elems));
+    DFTG_TRY(dalloc(&c->d_scal, scal_elems(c->natoms)));
+    DFTG_CUDA(cudaMallocHost(&c->h_scal, sizeof(double) * scal_elems(c->natoms)));
+    DFTG_TRY(dalloc(&c->d_Y, nlm * c->nang));
+    DFTG_TRY(dalloc(&c->d_Yw, nlm * c->nang));
+    DFTG_TRY(dalloc(&c->d_pre, nlm));
+    DFTG_TRY(dalloc(&c->d_pre32, nlm));
+    DFTG_TRY(dalloc(&c->d_rec, 2 * nlm));
+    DFTG_TRY(dalloc(&c->d_rec32, 2 * nlm));
+    DFTG_TRY(dalloc(&c->d_rholm, (size_t)c->natoms * nlm * N));
+    DFTG_TRY(dalloc(&c->d_U, (size_t)c->natoms * nlm * N));
+    DFTG_TRY(dalloc(&c->d_LU, (size_t)(c->lmax + 1) * (N + 2) * (N + 2)));
+    DFTG_TRY(dalloc(&c->d_piv, (size_t)(c->lmax + 1) * (N + 2)));
+    DFTG_TRY(dalloc(&c->d_sx, N));
+    DFTG_TRY(dalloc(&c->d_spl, (size_t)c->natoms * nlm * N * 4));
+    DFTG_TRY(dalloc(&c->d_spl32, (size_t)c->natoms * nlm * N * 4));
+    DFTG_CUDA(cudaMemset(c->d_scal, 0, sizeof(double) * scal_elems(c->natoms)));
+
+    std::vector<double> atoms(4 * (size_t)c->natoms), rab((size_t)c->natoms * c->natoms);
+    for (int a = 0; a < c->natoms; ++a) {
+        for (int d = 0; d < 3; ++d) atoms[4 * a + d] = c->xyz[3 * a + d];
+        atoms[4 * a + 3] = (double)c->Z[a];
+    }
+    for (int a = 0; a < c->natoms; ++a)
+        for (int b = 0; b < c->natoms; ++b) {
+            double dx = c->xyz[3 * b] - c->xyz[3 * a], dy = c->xyz[3 * b + 1] - c->xyz[3 * a + 1],
+                   dz = c->xyz[3 * b + 2] - c->xyz[3 * a + 2];
+            rab[(size_t)a * c->natoms + b] = std::sqrt(dx * dx + dy * dy + dz * dz);
+        }
+    DFTG_CUDA(cudaMemcpy(c->d_atoms, atoms.data(), sizeof(double) * atoms.size(), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_rab, rab.data(), sizeof(double) * rab.size(), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_rn, c->r_n.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_wrad, c->w_rad.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_leb, dftg_lebedev_table[dftg_lebedev_offset[c->leb]], sizeof(double) * 4 * c->nang,
+                         cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_bf_lmn, c->bf_lmn.data(), sizeof(int) * 3 * c->nbf, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_bf_off, c->bf_off.data(), sizeof(int) * (c->nbf + 1), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_bf_atom, c->bf_atom.data(), sizeof(int) * c->nbf, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_pa, c->alpha.data(), sizeof(double) * c->nprim, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_pcn, pcn.data(), sizeof(double) * c->nprim, cudaMemcpyHostToDevice));
+
+    DFTG_TRY(launch_grid(c));
+    DFTG_TRY(launch_amplitudes(c));
+    DFTG_TRY(hartree_setup(c));
+    DFTG_TRY(contract_setup(c));
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    return DFTG_OK;
+}
+
+static int check_matrix(const double *P, int n)
+{
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            const double a = P[i + (size_t)j * n];
+            if (!std::isfinite(a)) {
+                set_error("P(%d,%d) is not finite", i, j);
+                return DFTG_ERR_NONFINITE;
+            }
+            const double b = P[j + (size_t)i * n];
+            if (std::fabs(a - b) > 1e-10 * (1.0 + std::fabs(a))) {
+                set_error("P is not symmetric at (%d,%d): %g vs %g", i, j, a, b);
+                return DFTG_ERR_NONFINITE;
+            }
+        }
+    return DFTG_OK;
+}
+
+static int sync_scalars(dftg_ctx *c)
+{
+    DFTG_CUDA(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(double) * scal_elems(c->natoms), cudaMemcpyDeviceToHost,
+                              c->stream));
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    return DFTG_OK;
+}
+
+// device part of one Fock build; P already in c->d_P
+static int fock_pipeline(dftg_ctx *c, bool want_xc, bool want_j)
+{
+    if (c->precision != DFTG_PREC_FP64) DFTG_TRY(launch_convert_P(c));
+    DFTG_TRY(launch_density(c));
+    DFTG_TRY(launch_atom_sums(c, true));
+    if (want_xc) DFTG_TRY(launch_xc_points(c));
+    if (want_j) DFTG_TRY(launch_hartree(c));
+    DFTG_TRY(launch_contract(c, want_xc, want_j));
+    return DFTG_OK;
+}
+
+}  // namespace dftg
+
+using namespace dftg;
+
+#define CHECK_CTX(c)                                                   \
+    do {                                                               \
+        if (!(c)) { set_error("null context"); return DFTG_ERR_ARG; }  \
+    } while (0)
+
+extern "C" {
+
+const char *dftg_last_error(void) { return g_err; }
+
+int dftg_create(const dftg_molecule *mol, const dftg_basis *basis, const dftg_grid_params *g, dftg_ctx **out)
+{
+    if (!out) { set_error("out is NULL"); return DFTG_ERR_ARG; }
+    *out = nullptr;
+    if (!mol || !basis || !g || !mol->Z || !mol->xyz || !basis->bf_atom || !basis->bf_lmn || !basis->bf_nprim ||
+        !basis->prim_alpha || !basis->prim_coef) {
+        set_error("NULL argument");
+        return DFTG_ERR_ARG;
+    }
+    if (mol->natoms < 1 || mol->natoms > kMaxAtoms) { set_error("natoms %d out of [1,%d]", mol->natoms, kMaxAtoms); return DFTG_ERR_ARG; }
+    if (basis->nbf < 1) { set_error("nbf %d < 1", basis->nbf); return DFTG_ERR_ARG; }
+    if (g->radial_points < 8 || g->radial_points > 2000) { set_error("radial_points %d out of [8,2000]", g->radial_points); return DFTG_ERR_ARG; }
+    if (g->lebedev_order < 0 || g->lebedev_order >= DFTG_NUM_LEBEDEV_ORDERS) { set_error("lebedev_order %d out of [0,%d]", g->lebedev_order, DFTG_NUM_LEBEDEV_ORDERS - 1); return DFTG_ERR_ARG; }
+    if (g->lmax < 0 || g->lmax > kLmaxCap) { set_error("lmax %d out of [0,%d]", g->lmax, kLmaxCap); return DFTG_ERR_ARG; }
+    for (int a = 0; a < mol->natoms; ++a) {
+        if (mol->Z[a] < 1 || mol->Z[a] > 18) { set_error("Z[%d] = %d out of [1,18]", a, mol->Z[a]); return DFTG_ERR_ARG; }
+        for (int d = 0; d < 3; ++d)
+            if (!std::isfinite(mol->xyz[3 * a + d])) { set_error("atom %d coordinate not finite", a); return DFTG_ERR_NONFINITE; }
+        for (int b = 0; b < a; ++b) {
+            double dx = mol->xyz[3 * a] - mol->xyz[3 * b], dy = mol->xyz[3 * a + 1] - mol->xyz[3 * b + 1],
+                   dz = mol->xyz[3 * a + 2] - mol->xyz[3 * b + 2];
+            if (dx * dx + dy * dy + dz * dz < 1e-12) { set_error("atoms %d and %d coincide", b, a); return DFTG_ERR_ARG; }
+        }
+    }
+    long long np = 0;
+    for (int i = 0; i < basis->nbf; ++i) {
+        if (basis->bf_atom[i] < 0 || basis->bf_atom[i] >= mol->natoms) { set_error("bf_atom[%d] out of range", i); return DFTG_ERR_ARG; }
+        if (basis->bf_nprim[i] < 1) { set_error("bf_nprim[%d] < 1", i); return DFTG_ERR_ARG; }
+        int L = 0;
+        for (int d = 0; d < 3; ++d) {
+            if (basis->bf_lmn[3 * i + d] < 0) { set_error("bf_lmn[%d] negative", i); return DFTG_ERR_ARG; }
+            L += basis->bf_lmn[3 * i + d];
+        }
+        if (L > 4) { set_error("bf %d: angular momentum %d > 4", i, L); return DFTG_ERR_ARG; }
+        np += basis->bf_nprim[i];
+    }
+    for (long long k = 0; k < np; ++k)
+        if (!(basis->prim_alpha[k] > 0.0) || !std::isfinite(basis->prim_coef[k])) {
+            set_error("primitive %lld: bad exponent or coefficient", k);
+            return DFTG_ERR_ARG;
+        }
+    dftg_ctx *c = new (std::nothrow) dftg_ctx();
+    if (!c) { set_error("host allocation failed"); return DFTG_ERR_NOMEM; }
+    int rc = build_ctx(c, mol, basis, g);
+    if (rc != DFTG_OK) { free_ctx(c); return rc; }
+    *out = c;
+    return DFTG_OK;
+}
+
+int dftg_destroy(dftg_ctx *c)
+{
+    free_ctx(c);
+    return DFTG_OK;
+}
+
+int dftg_grid_size(const dftg_ctx *c, size_t *npts)
+{
+    CHECK_CTX(c);
+    if (!npts) { set_error("npts NULL"); return DFTG_ERR_ARG; }
+    *npts = c->npts;
+    return DFTG_OK;
+}
+
+int dftg_nbf(const dftg_ctx *c, int *nbf)
+{
+    CHECK_CTX(c);
+    if (!nbf) { set_error("nbf NULL"); return DFTG_ERR_ARG; }
+    *nbf = c->nbf;
+    return DFTG_OK;
+}
+
+int dftg_set_precision(dftg_ctx *c, int precision)
+{
+    CHECK_CTX(c);
+    if (precision != DFTG_PREC_FP64 && precision != DFTG_PREC_MIXED) { set_error("unknown precision %d", precision); return DFTG_ERR_ARG; }
+    c->precision = precision;
+    return DFTG_OK;
+}
+
+int dftg_set_stream(dftg_ctx *c, void *s)
+{
+    CHECK_CTX(c);
+    c->stream = s ? reinterpret_cast<cudaStream_t>(s) : c->own_stream;
+    return DFTG_OK;
+}
+
+int dftg_set_density(dftg_ctx *c, const double *P)
+{
+    CHECK_CTX(c);
+    if (!P) { set_error("P NULL"); return DFTG_ERR_ARG; }
+    DFTG_TRY(check_matrix(P, c->nbf));
+    DFTG_CUDA(cudaSetDevice(c->device));
+    DFTG_CUDA(cudaMemcpyAsync(c->d_P, P, sizeof(double) * c->nbf * c->nbf, cudaMemcpyHostToDevice, c->stream));
+    if (c->precision != DFTG_PREC_FP64) DFTG_TRY(launch_convert_P(c));
+    DFTG_TRY(launch_density(c));
+    DFTG_TRY(launch_atom_sums(c, false));
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    c->have_density = true;
+    c->have_hartree = false;
+    return DFTG_OK;
+}
+
+int dftg_correct_densities(dftg_ctx *c, double *scale)
+{
+    CHECK_CTX(c);
+    if (!c->have_density) { set_error("correct_densities before set_density"); return DFTG_ERR_STATE; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    DFTG_TRY(launch_atom_sums(c, true));
+    DFTG_TRY(sync_scalars(c));
+    if (scale) *scale = c->h_scal[kScalScale];
+    return DFTG_OK;
+}
+
+int dftg_calculate_density(dftg_ctx *c, double *nelec)
+{
+    CHECK_CTX(c);
+    if (!nelec) { set_error("nelec NULL"); return DFTG_ERR_ARG; }
+    if (!c->have_density) { set_error("calculate_density before set_density"); return DFTG_ERR_STATE; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    DFTG_TRY(launch_atom_sums(c, false));
+    DFTG_TRY(sync_scalars(c));
+    *nelec = c->h_scal[kScalNelec];
+    return DFTG_OK;
+}
+
+int dftg_calculate_hartree_potential(dftg_ctx *c, double *J)
+{
+    CHECK_CTX(c);
+    if (!c->have_density) { set_error("calculate_hartree_potential before set_density"); return DFTG_ERR_STATE; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    DFTG_TRY(launch_atom_sums(c, false));   // per-atom charges of the current rho
+    DFTG_TRY(launch_hartree(c));
+    DFTG_TRY(launch_contract(c, false, true));
+    if (J) DFTG_CUDA(cudaMemcpyAsync(J, c->d_J, sizeof(double) * c->nbf * c->nbf, cudaMemcpyDeviceToHost, c->stream));
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    c->have_hartree = true;
+    return DFTG_OK;
+}
+
+int dftg_calculate_xc(dftg_ctx *c, double *XC, double *exc)
+{
+    CHECK_CTX(c);
+    if (!c->have_density) { set_error("calculate_xc before set_density"); return DFTG_ERR_STATE; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    DFTG_TRY(launch_xc_points(c));
+    DFTG_TRY(launch_contract(c, true, false));
+    if (XC) DFTG_CUDA(cudaMemcpyAsync(XC, c->d_XC, sizeof(double) * c->nbf * c->nbf, cudaMemcpyDeviceToHost, c->stream));
+    DFTG_TRY(sync_scalars(c));
+    if (exc) *exc = c->h_scal[kScalExc];
+    return DFTG_OK;
+}
+
+int dftg_fock_build_device(dftg_ctx *c, const double *P_dev, double *J_dev, double *XC_dev, double *scalars_dev)
+{
+    CHECK_CTX(c);
+    if (!P_dev) { set_error("P_dev NULL"); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    if (P_dev != c->d_P) DFTG_CUDA(cudaMemcpyAsync(c->d_P, P_dev, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
+    DFTG_TRY(fock_pipeline(c, true, true));
+    if (J_dev) DFTG_CUDA(cudaMemcpyAsync(J_dev, c->d_J, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
+    if (XC_dev) DFTG_CUDA(cudaMemcpyAsync(XC_dev, c->d_XC, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
+    if (scalars_dev) {
+        DFTG_CUDA(cudaMemcpyAsync(scalars_dev, c->d_scal + kScalExc, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        DFTG_CUDA(cudaMemcpyAsync(scalars_dev + 1, c->d_scal + kScalNelec, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    c->have_density = true;
+    c->have_hartree = true;
+    return DFTG_OK;
+}
+
+int dftg_fock_build(dftg_ctx *c, const double *P, double *J, double *XC, double *exc, double *nelec)
+{
+    CHECK_CTX(c);
+    if (!P) { set_error("P NULL"); return DFTG_ERR_ARG; }
+    DFTG_TRY(check_matrix(P, c->nbf));
+    DFTG_CUDA(cudaSetDevice(c->device));
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    DFTG_CUDA(cudaMemcpyAsync(c->d_P, P, sizeof(double) * nn, cudaMemcpyHostToDevice, c->stream));
+    DFTG_TRY(fock_pipeline(c, true, true));
+    if (J) DFTG_CUDA(cudaMemcpyAsync(J, c->d_J, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream));
+    if (XC) DFTG_CUDA(cudaMemcpyAsync(XC, c->d_XC, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream));
+    DFTG_TRY(sync_scalars(c));
+    if (exc) *exc = c->h_scal[kScalExc];
+    if (nelec) *nelec = c->h_scal[kScalNelec];
+    c->have_density = true;
+    c->have_hartree = true;
+    return DFTG_OK;
+}
+
+static int get_points(const dftg_ctx *c, const double *src, double *out, size_t cap, size_t mult)
+{
+    CHECK_CTX(c);
+    if (!out) { set_error("out NULL"); return DFTG_ERR_ARG; }
+    if (cap < c->npts * mult) { set_error("capacity %zu < %zu", cap, c->npts * mult); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    DFTG_CUDA(cudaMemcpy(out, src, sizeof(double) * c->npts, cudaMemcpyDeviceToHost));
+    return DFTG_OK;
+}
+
+int dftg_get_weights(const dftg_ctx *c, double *out, size_t cap) { return get_points(c, c ? c->d_w : nullptr, out, cap, 1); }
+int dftg_get_becke_weights(const dftg_ctx *c, double *out, size_t cap) { return get_points(c, c ? c->d_wb : nullptr, out, cap, 1); }
+int dftg_get_densities(const dftg_ctx *c, double *out, size_t cap) { return get_points(c, c ? c->d_rho : nullptr, out, cap, 1); }
+int dftg_get_potential(const dftg_ctx *c, double *out, size_t cap) { return get_points(c, c ? c->d_V : nullptr, out, cap, 1); }
+
+int dftg_get_positions(const dftg_ctx *c, double *out, size_t cap)
+{
+    CHECK_CTX(c);
+    if (!out) { set_error("out NULL"); return DFTG_ERR_ARG; }
+    if (cap < 3 * c->npts) { set_error("capacity %zu < %zu", cap, 3 * c->npts); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<double> t(c->npts);
+    const double *src[3] = {c->d_x, c->d_y, c->d_z};
+    for (int d = 0; d < 3; ++d) {
+        DFTG_CUDA(cudaMemcpy(t.data(), src[d], sizeof(double) * c->npts, cudaMemcpyDeviceToHost));
+        for (size_t p = 0; p < c->npts; ++p) out[3 * p + d] = t[p];
+    }
+    return DFTG_OK;
+}
+
+int dftg_get_amplitudes(const dftg_ctx *c, double *out, size_t cap)
+{
+    CHECK_CTX(c);
+    if (!out) { set_error("out NULL"); return DFTG_ERR_ARG; }
+    const size_t need = c->npts * (size_t)c->nbf;
+    if (cap < need) { set_error("capacity %zu < %zu", cap, need); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<double> t(c->npts);
+    for (int mu = 0; mu < c->nbf; ++mu) {
+        DFTG_CUDA(cudaMemcpy(t.data(), c->d_phi + (size_t)mu * c->npad, sizeof(double) * c->npts, cudaMemcpyDeviceToHost));
+        for (size_t p = 0; p < c->npts; ++p) out[mu + p * (size_t)c->nbf] = t[p];
+    }
+    return DFTG_OK;
+}
+
+int dftg_nuclear_repulsion(const dftg_ctx *c, double *enuc)
+{
+    CHECK_CTX(c);
+    if (!enuc) { set_error("enuc NULL"); return DFTG_ERR_ARG; }
+    double e = 0.0;   // dft.cpp:235-246
+    for (int i = 0; i < c->natoms; ++i)
+        for (int j = i + 1; j < c->natoms; ++j) {
+            double dx = c->xyz[3 * i] - c->xyz[3 * j], dy = c->xyz[3 * i + 1] - c->xyz[3 * j + 1],
+                   dz = c->xyz[3 * i + 2] - c->xyz[3 * j + 2];
+            e += c->Z[i] * c->Z[j] / std::sqrt(dx * dx + dy * dy + dz * dz);
+        }
+    *enuc = e;
+    return DFTG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,166 @@
+// k_contract.cu -- K4: XC = phi^T diag(w v_xc) phi and J = phi^T diag(w V / 2) phi
+// in one pass over the amplitudes (dft.cpp:424-432, atomicgrid.cpp:471-488).
+//
+// CUDA-core form.  The nbf x nbf output is cut into TILE x TILE blocks
+// (TILE = 16 R); only blocks on or above the diagonal are computed, the rest is
+// mirrored.  The point dimension is split into nchunk contiguous chunks (split-K):
+// CTA (tile, chunk) accumulates its chunk in registers (R x R outputs of each
+// matrix per thread) and stores an FP64 partial; a second kernel sums the
+// partials of each element in chunk order (deterministic FP64 reduction).
+// T = double for the FP64 path, float for the mixed path (FP32 products and
+// in-chunk accumulation, FP64 across chunks).
+#include <vector>
+#include "dftg_internal.cuh"
+
+namespace dftg {
+
+constexpr int kKB = 32;   // points per shared-memory stage
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_contract(int nbf, int pts_per_chunk, size_t npad, const T *__restrict__ phi,
+                                                  const T *__restrict__ cxc, const T *__restrict__ cj, int want_xc,
+                                                  int want_j, const int2 *__restrict__ tiles,
+                                                  double *__restrict__ part)
+{
+    constexpr int TILE = 16 * R;
+    constexpr int LD = TILE + 1;
+    __shared__ T sm_m[kKB * LD];
+    __shared__ T sm_n[kKB * LD];
+    __shared__ T sa[kKB], sb[kKB];
+    const int2 tl = tiles[blockIdx.x];
+    const int m0 = tl.x * TILE, n0 = tl.y * TILE;
+    const int chunk = blockIdx.y;
+    const size_t pb = (size_t)chunk * pts_per_chunk;
+    const size_t pe = min(npad, pb + (size_t)pts_per_chunk);
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    T ax[R][R], aj[R][R];
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+        for (int j = 0; j < R; ++j) { ax[i][j] = 0; aj[i][j] = 0; }
+
+    for (size_t kb = pb; kb < pe; kb += kKB) {
+        __syncthreads();
+        for (int e = tid; e < TILE * kKB; e += 256) {
+            const int row = e / kKB, k = e % kKB;
+            const int mu = m0 + row, nu = n0 + row;
+            sm_m[k * LD + row] = (mu < nbf) ? phi[(size_t)mu * npad + kb + k] : T(0);
+            sm_n[k * LD + row] = (nu < nbf) ? phi[(size_t)nu * npad + kb + k] : T(0);
+        }
+        if (tid < kKB) {
+            sa[tid] = want_xc ? cxc[kb + tid] : T(0);
+            sb[tid] = want_j ? cj[kb + tid] : T(0);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int k = 0; k < kKB; ++k) {
+            T fm[R], fn[R];
+#pragma unroll
+            for (int i = 0; i < R; ++i) fm[i] = sm_m[k * LD + ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < R; ++j) fn[j] = sm_n[k * LD + tx + 16 * j];
+            const T a = sa[k], b = sb[k];
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+                const T u = a * fm[i], s = b * fm[i];
+#pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    ax[i][j] += u * fn[j];
+                    aj[i][j] += s * fn[j];
+                }
+            }
+        }
+    }
+    const size_t nn = (size_t)nbf * nbf;
+    double *px = part + (size_t)chunk * 2 * nn, *pj = px + nn;
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            const int mu = m0 + ty + 16 * i, nu = n0 + tx + 16 * j;
+            if (mu < nbf && nu < nbf) {
+                px[(size_t)mu * nbf + nu] = (double)ax[i][j];
+                pj[(size_t)mu * nbf + nu] = (double)aj[i][j];
+            }
+        }
+}
+
+// sum partials of every computed element in chunk order; mirror below the
+// diagonal blocks.  out matrices are column-major == row-major (symmetric).
+__global__ void k_contract_reduce(int nbf, int tile, int nchunk, int want_xc, int want_j,
+                                  const double *__restrict__ part, double *__restrict__ XC, double *__restrict__ J)
+{
+    const size_t nn = (size_t)nbf * nbf;
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nn) return;
+    const int mu = (int)(e / nbf), nu = (int)(e % nbf);
+    const int tm = mu / tile, tn = nu / tile;
+    if (tm > tn) return;   // written by the mirror of (nu, mu)
+    double sx = 0.0, sj = 0.0;
+    for (int c = 0; c < nchunk; ++c) {
+        const double *p = part + (size_t)c * 2 * nn;
+        sx += p[e];
+        sj += p[nn + e];
+    }
+    // column-major element (row mu, col nu) sits at mu + nu*nbf
+    if (want_xc) {
+        XC[(size_t)nu * nbf + mu] = sx;
+        if (tm < tn) XC[(size_t)mu * nbf + nu] = sx;
+    }
+    if (want_j) {
+        J[(size_t)nu * nbf + mu] = sj;
+        if (tm < tn) J[(size_t)mu * nbf + nu] = sj;
+    }
+}
+
+static int tile_R(int nbf) { return nbf <= 80 ? 5 : 4; }
+
+size_t contract_part_elems(int nbf, size_t npad)
+{
+    const int R = tile_R(nbf), tile = 16 * R;
+    const int nt = (nbf + tile - 1) / tile;
+    const int npairs = nt * (nt + 1) / 2;
+    int nchunk = (2 * 152 + npairs - 1) / npairs;
+    const size_t max_chunks = npad / (4 * kKB);
+    if ((size_t)nchunk > max_chunks) nchunk = (int)(max_chunks > 0 ? max_chunks : 1);
+    return (size_t)nchunk * 2 * nbf * nbf;
+}
+
+int contract_setup(dftg_ctx *c)
+{
+    const int R = tile_R(c->nbf), tile = 16 * R;
+    const int nt = (c->nbf + tile - 1) / tile;
+    std::vector<int2> tl;
+    for (int a = 0; a < nt; ++a)
+        for (int b = a; b < nt; ++b) tl.push_back(make_int2(a, b));
+    c->ntiles = (int)tl.size();
+    c->nchunk = (int)(contract_part_elems(c->nbf, c->npad) / (2 * (size_t)c->nbf * c->nbf));
+    DFTG_CUDA(cudaMalloc(&c->d_tiles, sizeof(int2) * tl.size()));
+    DFTG_CUDA(cudaMemcpy(c->d_tiles, tl.data(), sizeof(int2) * tl.size(), cudaMemcpyHostToDevice));
+    return DFTG_OK;
+}
+
+int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
+{
+    const int R = tile_R(c->nbf), tile = 16 * R;
+    const int2 *d_tiles = reinterpret_cast<const int2 *>(c->d_tiles);
+    size_t per = (c->npad + c->nchunk - 1) / c->nchunk;
+    per = (per + kKB - 1) / kKB * kKB;
+    dim3 grid((unsigned)c->ntiles, (unsigned)c->nchunk);
+    const int wx = want_xc ? 1 : 0, wj = want_j ? 1 : 0;
+    if (c->precision == DFTG_PREC_FP64) {
+        if (R == 5) k_contract<double, 5><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
+        else k_contract<double, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
+    } else {
+        if (R == 5) k_contract<float, 5><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, c->d_cj32, wx, wj, d_tiles, c->d_part);
+        else k_contract<float, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, c->d_cj32, wx, wj, d_tiles, c->d_part);
+    }
+    DFTG_LAUNCH_CHECK();
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    k_contract_reduce<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->nbf, tile, c->nchunk, wx, wj, c->d_part,
+                                                                          c->d_XC, c->d_J);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+}  // namespace dftg

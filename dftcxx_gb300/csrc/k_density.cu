@@ -1,0 +1,284 @@
+// k_density.cu -- density on the grid, charge reductions, LDA point kernel.
+//
+// K3  rho_p = 2 phi_p^T P phi_p (gridpoint.cpp:82-84).  One thread per point,
+//     P staged in shared memory 32 columns at a time; T = double (FP64 path)
+//     or float (mixed path, FP32 phi and P).  HBM traffic: nbf*npad*sizeof(T)
+//     read once per 32-column block (the re-reads after the first hit L1/L2).
+// K6  per-atom integrals q_a = sum_p w rho (atomicgrid.cpp:520-530), the
+//     correction factor c = sum Z / sum q (moleculargrid.cpp:132-146) and the
+//     rescaling rho <- c rho.  Deterministic two-stage FP64 reductions.
+// LDA Slater exchange (functionals.cpp:24-63) + VWN correlation
+//     (functionals.cpp:65-158), closed shell, fused with the weight: writes
+//     cxc_p = w_p * v_p and block partials of E_xc = sum w (e_x + e_c).
+#include "dftg_internal.cuh"
+
+namespace dftg {
+
+constexpr int kRedBlock = 256;
+constexpr int kRedChunk = 4096;   // points per stage-1 reduction block
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_density(int nbf, size_t npad, const T *__restrict__ phi,
+                                                 const T *__restrict__ P, double *__restrict__ rho)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *Ps = reinterpret_cast<T *>(smem_raw);   // [nbf][32]
+    const size_t p = (size_t)blockIdx.x * 128 + threadIdx.x;
+    T r = 0;
+    for (int n0 = 0; n0 < nbf; n0 += 32) {
+        const int nc = min(32, nbf - n0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < nbf * 32; e += 128) {
+            const int mu = e >> 5, j = e & 31;
+            Ps[e] = (j < nc) ? P[(size_t)mu * nbf + n0 + j] : T(0);
+        }
+        __syncthreads();
+        T acc[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) acc[j] = 0;
+        for (int mu = 0; mu < nbf; ++mu) {
+            const T f = phi[(size_t)mu * npad + p];
+            const T *pr = Ps + mu * 32;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) acc[j] += f * pr[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if (j < nc) r += acc[j] * phi[(size_t)(n0 + j) * npad + p];
+    }
+    rho[p] = 2.0 * (double)r;
+}
+
+// stage 1: partial sums of w*rho over chunks that never straddle two atoms
+__global__ void k_atom_partials(size_t per_atom, int chunks_per_atom, const double *__restrict__ w,
+                                const double *__restrict__ rho, double *__restrict__ part)
+{
+    __shared__ double sh[kRedBlock];
+    const int b = blockIdx.x;
+    const int a = b / chunks_per_atom, ch = b % chunks_per_atom;
+    const size_t base = (size_t)a * per_atom;
+    const size_t lo = (size_t)ch * kRedChunk, hi = min(per_atom, lo + kRedChunk);
+    double s = 0.0;
+    for (size_t i = lo + threadIdx.x; i < hi; i += kRedBlock) s += w[base + i] * rho[base + i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = kRedBlock / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[b] = sh[0];
+}
+
+// stage 2 (one warp): per-atom sums, total, correction factor
+__global__ void k_atom_final(int natoms, int chunks_per_atom, const double *__restrict__ part,
+                             const double *__restrict__ atoms, double *scal, int mode)
+{
+    if (threadIdx.x != 0) return;
+    double total = 0.0, charge = 0.0;
+    for (int a = 0; a < natoms; ++a) {
+        double q = 0.0;
+        for (int ch = 0; ch < chunks_per_atom; ++ch) q += part[a * chunks_per_atom + ch];
+        scal[kScalAtomQ + a] = q;
+        total += q;
+        charge += atoms[4 * a + 3];
+    }
+    if (mode == 0) {           // before correction
+        scal[kScalSum] = total;
+        scal[kScalScale] = charge / total;
+    } else {                   // after correction
+        scal[kScalNelec] = total;
+    }
+}
+
+__global__ void k_scale(size_t npts, const double *__restrict__ scal, double *rho)
+{
+    size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < npts) rho[p] *= scal[kScalScale];
+}
+
+// ---------------------------------------------------------------- LDA
+
+template <typename T> struct LdaMath;
+template <> struct LdaMath<double> {
+    static __device__ double pw(double x, double y) { return pow(x, y); }
+    static __device__ double lg(double x) { return log(x); }
+    static __device__ double at(double x) { return atan(x); }
+    static __device__ double sq(double x) { return sqrt(x); }
+};
+template <> struct LdaMath<float> {
+    static __device__ float pw(float x, float y) { return powf(x, y); }
+    static __device__ float lg(float x) { return logf(x); }
+    static __device__ float at(float x) { return atanf(x); }
+    static __device__ float sq(float x) { return sqrtf(x); }
+};
+
+template <typename T>
+__device__ __forceinline__ T vwn_xx(T x, T b, T c) { return x * x + b * x + c; }
+
+template <typename T>
+__device__ T vwn_eps(T x, T a, T x0, T b, T c)
+{
+    using M = LdaMath<T>;
+    const T q = M::sq(T(4) * c - b * b);
+    return a * (M::lg(x * x / vwn_xx(x, b, c))
+                - b * (x0 / vwn_xx(x0, b, c)) * M::lg((x - x0) * (x - x0) / vwn_xx(x, b, c))
+                + (T(2) * b / q) * (T(1) - (x0 * (T(2) * x0 + b) / vwn_xx(x0, b, c))) * M::at(q / (T(2) * x + b)));
+}
+
+template <typename T>
+__device__ T vwn_deps(T x, T a, T x0, T b, T c)
+{
+    using M = LdaMath<T>;
+    const T q = M::sq(T(4) * c - b * b);
+    const T t = (T(2) * x + b) * (T(2) * x + b) + q * q;
+    return a * (T(2) / x - (T(2) * x + b) / vwn_xx(x, b, c) - T(4) * b / t
+                - (b * x0 / vwn_xx(x0, b, c)) * (T(2) / (x - x0) - (T(2) * x + b) / vwn_xx(x, b, c)
+                                                 - T(4) * (T(2) * x0 + b) / t));
+}
+
+// closed-shell point kernel: e_x + e_c and 0.5 * (vxa + vxb + vca + vcb)
+template <typename T>
+__device__ void lda_point(double rho_d, T &e, T &v)
+{
+    using M = LdaMath<T>;
+    const T tol = T(1e-10);
+    const T fac = T(-2.25 * (2.0 / 3.0)) * M::pw(T(3.0 / 4.0 / kPi), T(1.0 / 3.0));
+    const T da = T(rho_d * 0.5);
+    T ex = 0, vxa = 0;
+    if (!(da < tol)) {
+        const T r3 = M::pw(da, T(1.0 / 3.0));
+        ex = fac * da * r3;
+        vxa = T(4.0 / 3.0) * fac * r3;
+    }
+    // rho_b == rho_a: identical second spin channel
+    ex = ex + ex;
+    const T vx = vxa;   // (vxa + vxb) / 2
+    T ec = 0, vc = 0;
+    const T dens = da + da;
+    if (!(dens < tol)) {
+        const T x = M::pw(T(3.0 / 4.0 / kPi) / dens, T(1.0 / 6.0));
+        const T epsp = vwn_eps<T>(x, T(0.0310907), T(-0.10498), T(3.72744), T(12.9352));
+        const T depsp = vwn_deps<T>(x, T(0.0310907), T(-0.10498), T(3.72744), T(12.9352));
+        // zeta = 0 gives g = 0 < tol: paramagnetic branch (functionals.cpp:94-99)
+        ec = epsp * dens;
+        vc = epsp - (x / T(6)) * depsp;
+    }
+    e = ex + ec;
+    v = vx + vc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, const double *__restrict__ rho,
+                                                   const double *__restrict__ w, double *__restrict__ cxc,
+                                                   float *__restrict__ cxc32, double *__restrict__ part)
+{
+    __shared__ double sh[kRedBlock];
+    const size_t p = (size_t)blockIdx.x * kRedBlock + threadIdx.x;
+    double ew = 0.0;
+    if (p < npad) {
+        T e, v;
+        lda_point<T>(rho[p], e, v);
+        const double wp = w[p];
+        ew = wp * (double)e;
+        const double c = wp * (double)v;
+        cxc[p] = c;
+        cxc32[p] = (float)c;
+    }
+    sh[threadIdx.x] = ew;
+    __syncthreads();
+    for (int o = kRedBlock / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void k_sum_to_scalar(int n, const double *__restrict__ part, double *scal, int slot)
+{
+    __shared__ double sh[kRedBlock];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += kRedBlock) s += part[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = kRedBlock / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) scal[slot] = sh[0];
+}
+
+__global__ void k_convert_P(int n, const double *__restrict__ P, float *__restrict__ P32)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) P32[i] = (float)P[i];
+}
+
+// ---------------------------------------------------------------- launchers
+
+int launch_convert_P(dftg_ctx *c)
+{
+    const int n = c->nbf * c->nbf;
+    k_convert_P<<<(n + 255) / 256, 256, 0, c->stream>>>(n, c->d_P, c->d_P32);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+int launch_density(dftg_ctx *c)
+{
+    const unsigned nb = (unsigned)(c->npad / 128);
+    if (c->precision == DFTG_PREC_FP64) {
+        const size_t sm = (size_t)c->nbf * 32 * sizeof(double);
+        if (sm > 48 * 1024) DFTG_CUDA(cudaFuncSetAttribute(k_density<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_density<double><<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi, c->d_P, c->d_rho);
+    } else {
+        const size_t sm = (size_t)c->nbf * 32 * sizeof(float);
+        if (sm > 48 * 1024) DFTG_CUDA(cudaFuncSetAttribute(k_density<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_density<float><<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi32, c->d_P32, c->d_rho);
+    }
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+// apply_scale: compute c and rescale rho, then recompute the per-atom charges
+int launch_atom_sums(dftg_ctx *c, bool apply_scale)
+{
+    const size_t per_atom = (size_t)c->nrad * c->nang;
+    const int cpa = (int)((per_atom + kRedChunk - 1) / kRedChunk);
+    const int nb = cpa * c->natoms;
+    k_atom_partials<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, c->d_w, c->d_rho, c->d_red);
+    DFTG_LAUNCH_CHECK();
+    k_atom_final<<<1, 32, 0, c->stream>>>(c->natoms, cpa, c->d_red, c->d_atoms, c->d_scal, apply_scale ? 0 : 1);
+    DFTG_LAUNCH_CHECK();
+    if (apply_scale) {
+        k_scale<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, c->d_scal, c->d_rho);
+        DFTG_LAUNCH_CHECK();
+        k_atom_partials<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, c->d_w, c->d_rho, c->d_red);
+        DFTG_LAUNCH_CHECK();
+        k_atom_final<<<1, 32, 0, c->stream>>>(c->natoms, cpa, c->d_red, c->d_atoms, c->d_scal, 1);
+        DFTG_LAUNCH_CHECK();
+    }
+    return DFTG_OK;
+}
+
+int launch_xc_points(dftg_ctx *c)
+{
+    const unsigned nb = (unsigned)((c->npad + kRedBlock - 1) / kRedBlock);
+    if (c->precision == DFTG_PREC_FP64)
+        k_lda<double><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_cxc, c->d_cxc32, c->d_red);
+    else
+        k_lda<float><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_cxc, c->d_cxc32, c->d_red);
+    DFTG_LAUNCH_CHECK();
+    k_sum_to_scalar<<<1, kRedBlock, 0, c->stream>>>((int)nb, c->d_red, c->d_scal, kScalExc);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+size_t reduction_elems(size_t npad, int natoms, int nrad, int nang)
+{
+    size_t a = (npad + kRedBlock - 1) / kRedBlock;
+    size_t per_atom = (size_t)nrad * nang;
+    size_t b = (size_t)natoms * ((per_atom + kRedChunk - 1) / kRedChunk);
+    return a > b ? a : b;
+}
+
+}  // namespace dftg

@@ -1,0 +1,207 @@
+"""Python mirror of DFTCXX's MolecularGrid / DFT call surface over the C ABI.
+
+``MolecularGrid`` keeps the reference's method names and argument meanings
+(moleculargrid.h:84-167); ``DFT`` keeps ``scf()`` and the energy bookkeeping
+(dft.h:83-91, dft.cpp:84-142, 300-366, 441-447).  Every grid operation runs in
+``libdftg.so``; the host side only moves nbf x nbf matrices and runs the small
+eigen-solves of the SCF driver.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+class MolecularGrid:
+    """Becke-partitioned Gauss-Chebyshev x Lebedev grid on one GPU.
+
+    ``precision``: "fp64" (every step in FP64) or "mixed" (split-precision
+    contractions, FP64 reductions)."""
+
+    def __init__(self, mol, radial_points=15, lebedev_order=7, lmax=8, precision="fp64", device=0):
+        L = _lib.load()
+        self.mol = mol
+        self._arrays = [np.ascontiguousarray(mol.Z, dtype=np.int32),
+                        np.ascontiguousarray(mol.xyz, dtype=np.float64),
+                        np.ascontiguousarray(mol.bf_atom, dtype=np.int32),
+                        np.ascontiguousarray(mol.bf_lmn, dtype=np.int32),
+                        np.ascontiguousarray(mol.bf_nprim, dtype=np.int32),
+                        np.ascontiguousarray(mol.prim_alpha, dtype=np.float64),
+                        np.ascontiguousarray(mol.prim_coef, dtype=np.float64)]
+        Z, xyz, ba, bl, bn, pa, pc = self._arrays
+        ip = ctypes.POINTER(ctypes.c_int)
+        m = _lib.Molecule(mol.natoms, Z.ctypes.data_as(ip), _ptr(xyz))
+        b = _lib.Basis(mol.nbf, ba.ctypes.data_as(ip), bl.ctypes.data_as(ip), bn.ctypes.data_as(ip), _ptr(pa), _ptr(pc))
+        g = _lib.GridParams(radial_points, lebedev_order, lmax, device)
+        h = ctypes.c_void_p()
+        check(L.dftg_create(ctypes.byref(m), ctypes.byref(b), ctypes.byref(g), ctypes.byref(h)))
+        self._h = h
+        n = ctypes.c_size_t()
+        check(L.dftg_grid_size(h, ctypes.byref(n)))
+        self.grid_size = int(n.value)
+        self.nbf = mol.nbf
+        self.radial_points, self.lebedev_order, self.lmax = radial_points, lebedev_order, lmax
+        self.set_precision(precision)
+
+    # ------------------------------------------------------------ lifetime
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().dftg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_precision(self, precision):
+        code = {"fp64": _lib.DFTG_PREC_FP64, "mixed": _lib.DFTG_PREC_MIXED}[precision]
+        check(_lib.load().dftg_set_precision(self._h, code))
+        self.precision = precision
+
+    def set_stream(self, stream_ptr):
+        check(_lib.load().dftg_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
+
+    # ------------------------------------------------- reference interface
+    def set_density(self, P):
+        P = np.asfortranarray(P, dtype=np.float64)
+        check(_lib.load().dftg_set_density(self._h, _ptr(P)))
+
+    def correct_densities(self):
+        c = ctypes.c_double()
+        check(_lib.load().dftg_correct_densities(self._h, ctypes.byref(c)))
+        return c.value
+
+    def calculate_density(self):
+        n = ctypes.c_double()
+        check(_lib.load().dftg_calculate_density(self._h, ctypes.byref(n)))
+        return n.value
+
+    def calculate_hartree_potential(self):
+        J = np.zeros((self.nbf, self.nbf), order="F")
+        check(_lib.load().dftg_calculate_hartree_potential(self._h, _ptr(J)))
+        return np.ascontiguousarray(J)
+
+    def calculate_xc(self):
+        XC = np.zeros((self.nbf, self.nbf), order="F")
+        e = ctypes.c_double()
+        check(_lib.load().dftg_calculate_xc(self._h, _ptr(XC), ctypes.byref(e)))
+        return np.ascontiguousarray(XC), e.value
+
+    def fock_build(self, P):
+        """One grid Fock build at fixed P; returns J, XC, E_xc and the
+        integrated (corrected) density."""
+        P = np.asfortranarray(P, dtype=np.float64)
+        J = np.zeros((self.nbf, self.nbf), order="F")
+        XC = np.zeros((self.nbf, self.nbf), order="F")
+        e, n = ctypes.c_double(), ctypes.c_double()
+        check(_lib.load().dftg_fock_build(self._h, _ptr(P), _ptr(J), _ptr(XC), ctypes.byref(e), ctypes.byref(n)))
+        return {"J": np.ascontiguousarray(J), "XC": np.ascontiguousarray(XC), "Exc": e.value, "nelec": n.value}
+
+    def _points(self, name, mult=1):
+        out = np.empty(self.grid_size * mult)
+        check(getattr(_lib.load(), name)(self._h, _ptr(out), out.size))
+        return out
+
+    def get_weights(self):
+        return self._points("dftg_get_weights")
+
+    def get_becke_weights(self):
+        return self._points("dftg_get_becke_weights")
+
+    def get_densities(self):
+        return self._points("dftg_get_densities")
+
+    def get_potential(self):
+        return self._points("dftg_get_potential")
+
+    def get_positions(self):
+        return self._points("dftg_get_positions", 3).reshape(-1, 3)
+
+    def get_amplitudes(self):
+        """nbf x npts (the reference's orientation)."""
+        out = np.empty(self.grid_size * self.nbf)
+        check(_lib.load().dftg_get_amplitudes(self._h, _ptr(out), out.size))
+        return out.reshape(self.grid_size, self.nbf).T
+
+    def one_electron(self):
+        n = self.nbf
+        S, T, V = (np.zeros((n, n), order="F") for _ in range(3))
+        check(_lib.load().dftg_one_electron(self._h, _ptr(S), _ptr(T), _ptr(V)))
+        return np.ascontiguousarray(S), np.ascontiguousarray(T), np.ascontiguousarray(V)
+
+    def nuclear_repulsion(self):
+        e = ctypes.c_double()
+        check(_lib.load().dftg_nuclear_repulsion(self._h, ctypes.byref(e)))
+        return e.value
+
+
+class DFT:
+    """Closed-shell LDA SCF driver with the reference's iteration
+    (dft.cpp:84-142): F = H + 2J + XC, canonical orthogonalisation,
+    P = C_occ C_occ^T, linear damping 0.5 after the first density."""
+
+    def __init__(self, mol, radial_points=15, lebedev_order=7, lmax=8, precision="fp64", device=0):
+        self.mol = mol
+        self.molgrid = MolecularGrid(mol, radial_points, lebedev_order, lmax, precision, device)
+        S, T, V = self.molgrid.one_electron()
+        self.S, self.T, self.V = S, T, V
+        self.H = T + V
+        self.enuc = self.molgrid.nuclear_repulsion()
+        lam, U = np.linalg.eigh(S)
+        self.X = U @ np.diag(1.0 / np.sqrt(lam))
+        n = mol.nbf
+        self.J = np.zeros((n, n))
+        self.XC = np.zeros((n, n))
+        self.P = None
+        self.exc = 0.0
+        self.history = []
+        # construct_matrices: first density from H, then J and the energy (dft.cpp:216-226)
+        self._density_matrix()
+        self.molgrid.set_density(self.P)
+        self.molgrid.correct_densities()
+        self.J = self.molgrid.calculate_hartree_potential()
+        self.et = self._energy()
+
+    def _density_matrix(self, alpha=0.5):
+        F = self.H + 2.0 * self.J + self.XC
+        _, Cp = np.linalg.eigh(self.X.T @ F @ self.X)
+        C = self.X @ Cp
+        nocc = self.mol.nelec // 2
+        Pn = C[:, :nocc] @ C[:, :nocc].T
+        self.P = Pn if self.P is None else (1.0 - alpha) * Pn + alpha * self.P
+
+    def _energy(self):
+        self.e_one = 2.0 * np.trace(self.P @ self.H)
+        self.e_j = 2.0 * np.trace(self.P @ self.J)
+        return self.e_one + self.e_j + self.enuc + self.exc
+
+    def scf(self, tol=1e-4, max_iter=100, min_iter=3):
+        old = self.et
+        diff = 1.0
+        it = 0
+        while diff > tol or it < min_iter:
+            it += 1
+            self._density_matrix()
+            r = self.molgrid.fock_build(self.P)
+            self.J, self.XC, self.exc = r["J"], r["XC"], r["Exc"]
+            self.et = self._energy()
+            self.history.append({"iter": it, "E": self.et, "Exc": self.exc, "EJ": self.e_j, "nelec": r["nelec"]})
+            diff = abs(self.et - old)
+            old = self.et
+            if it >= max_iter:
+                break
+        return self.et

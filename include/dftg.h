@@ -1,0 +1,144 @@
+/*
+ * dftg.h -- C ABI of the GB300-native grid Fock build (DFTCXX drop-in).
+ *
+ * Replaces the grid part of DFTCXX's MolecularGrid / AtomicGrid / DFT call
+ * surface (ifilot/dftcxx, src/moleculargrid.h:84-167, src/atomicgrid.h:75-241,
+ * src/dft.cpp:394-447).  Plain C types only: counts, host pointers and sizes.
+ *
+ * Conventions (identical to the reference):
+ *   - lengths in bohr, energies in Hartree;
+ *   - P is the closed-shell *half* density matrix: rho = 2 phi^T P phi
+ *     (gridpoint.cpp:82-84);
+ *   - J is returned such that F = H + 2 J + XC (dft.cpp:334); the 1/2 of
+ *     atomicgrid.cpp:485 is inside J;
+ *   - nbf x nbf matrices are column-major (Eigen's default); the matrices are
+ *     symmetric, so row-major callers may pass them unchanged;
+ *   - per-point arrays are ordered atom by atom, radial shell by shell
+ *     (largest radius first), Lebedev point by point (atomicgrid.cpp:48-81).
+ *
+ * Errors: every call returns DFTG_OK (0) or a DFTG_ERR_* code; nothing throws
+ * across the ABI.  dftg_last_error() gives a message for the calling thread.
+ * Threading: one context per CUDA stream; calls on one context must be
+ * serialised by the caller.  Different contexts may be used concurrently.
+ * Ownership: the context owns all device memory; the caller owns every host
+ * array it passes; no pointer is retained after a call returns.
+ */
+#ifndef DFTG_H
+#define DFTG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DFTG_OK 0
+#define DFTG_ERR_ARG 1        /* invalid argument or size */
+#define DFTG_ERR_CUDA 2       /* CUDA runtime error (message has details) */
+#define DFTG_ERR_NONFINITE 3  /* non-finite or asymmetric input matrix */
+#define DFTG_ERR_STATE 4      /* call order violated (e.g. XC before density) */
+#define DFTG_ERR_NOMEM 5      /* device allocation failed */
+#define DFTG_ERR_TIMEOUT 6    /* a bounded device wait gave up */
+
+/* arithmetic of the per-iteration build */
+#define DFTG_PREC_FP64 0      /* every step in FP64 on the CUDA cores */
+#define DFTG_PREC_MIXED 1     /* contractions split-precision, FP64 reductions */
+
+/* Lebedev orders: 0..10 are the reference's enum (settings.h:64-78:
+ * 6,14,26,38,50,74,86,110,146,170,194 points); 11 is the 302-point rule, an
+ * extension generated from the published Lebedev-Laikov data. */
+#define DFTG_LEBEDEV_302 11
+
+typedef struct dftg_ctx dftg_ctx;
+
+/* Atoms: replaces Molecule's atom list (molecule.h:41-81, molecule.cpp:97-101). */
+typedef struct {
+    int natoms;
+    const int *Z;          /* [natoms] nuclear charges (1..18) */
+    const double *xyz;     /* [natoms][3] bohr */
+} dftg_molecule;
+
+/* Contracted Cartesian Gaussians: replaces Molecule's CGF list (cgf.h:152-287,
+ * molecule.cpp:135-238).  Function i sits on atom bf_atom[i] with powers
+ * bf_lmn[3i..3i+2] and bf_nprim[i] primitives taken in order from prim_alpha /
+ * prim_coef.  Primitive normalisation follows cgf.cpp:102-114. */
+typedef struct {
+    int nbf;
+    const int *bf_atom;       /* [nbf] */
+    const int *bf_lmn;        /* [nbf][3] */
+    const int *bf_nprim;      /* [nbf] */
+    const double *prim_alpha; /* [sum(bf_nprim)] */
+    const double *prim_coef;  /* [sum(bf_nprim)] */
+} dftg_basis;
+
+/* MolecularGrid::set_grid_parameters (moleculargrid.cpp:175-179). */
+typedef struct {
+    int radial_points;     /* Gauss-Chebyshev radial points per atom, >= 8 */
+    int lebedev_order;     /* 0..11, see above */
+    int lmax;              /* spherical-harmonic cut-off of the Hartree solve, 0..16 */
+    int device;            /* CUDA device ordinal */
+} dftg_grid_params;
+
+/* Build molecule, basis and grid: MolecularGrid(mol) + create_grid()
+ * (moleculargrid.cpp:31-34, 193-261).  Computes grid points, Becke weights and
+ * the basis amplitudes on the device. */
+int dftg_create(const dftg_molecule *mol, const dftg_basis *basis,
+                const dftg_grid_params *grid, dftg_ctx **out);
+int dftg_destroy(dftg_ctx *ctx);
+const char *dftg_last_error(void);
+
+/* Sizes. */
+int dftg_grid_size(const dftg_ctx *ctx, size_t *npts);   /* grid_size, moleculargrid.h:76 */
+int dftg_nbf(const dftg_ctx *ctx, int *nbf);             /* Molecule::get_nr_bfs */
+
+/* Precision of the per-iteration build (default DFTG_PREC_FP64). */
+int dftg_set_precision(dftg_ctx *ctx, int precision);
+/* Run on a caller-owned cudaStream_t (NULL restores the context's stream). */
+int dftg_set_stream(dftg_ctx *ctx, void *cuda_stream);
+
+/* MolecularGrid::set_density(P) (moleculargrid.cpp:48-53): rho = 2 phi^T P phi
+ * on every point.  P: nbf x nbf host array. */
+int dftg_set_density(dftg_ctx *ctx, const double *P);
+/* MolecularGrid::correct_densities (moleculargrid.cpp:132-146): scales rho by
+ * sum(Z) / integral(w rho); the factor is written to *scale (may be NULL). */
+int dftg_correct_densities(dftg_ctx *ctx, double *scale);
+/* MolecularGrid::calculate_density (moleculargrid.cpp:157-166). */
+int dftg_calculate_density(dftg_ctx *ctx, double *nelec);
+/* MolecularGrid::calculate_hartree_potential (moleculargrid.cpp:336-389):
+ * Becke-Poisson Hartree potential on every point and J (nbf x nbf). */
+int dftg_calculate_hartree_potential(dftg_ctx *ctx, double *J);
+/* DFT::calculate_exchange_correlation_matrix (dft.cpp:394-433): Slater +
+ * VWN point kernel, XC (nbf x nbf) and E_xc. */
+int dftg_calculate_xc(dftg_ctx *ctx, double *XC, double *exc);
+
+/* One whole grid Fock build at fixed P (dft.cpp:361-365, 377-433): the four
+ * calls above in one, with host buffers.  Any output pointer may be NULL. */
+int dftg_fock_build(dftg_ctx *ctx, const double *P, double *J, double *XC,
+                    double *exc, double *nelec);
+/* The same with DEVICE pointers on the context's stream and no host
+ * synchronisation (P: nbf*nbf doubles; J, XC: nbf*nbf; scalars: exc, nelec as
+ * a 2-double device array).  For callers whose P is already in HBM. */
+int dftg_fock_build_device(dftg_ctx *ctx, const double *P_dev, double *J_dev,
+                           double *XC_dev, double *scalars_dev);
+
+/* Getters (copies): MolecularGrid::get_weights / get_densities /
+ * get_amplitudes (moleculargrid.cpp:61-127).  cap is the element capacity of
+ * out.  Amplitudes are nbf x npts column-major (the reference's layout). */
+int dftg_get_weights(const dftg_ctx *ctx, double *out, size_t cap);
+int dftg_get_becke_weights(const dftg_ctx *ctx, double *out, size_t cap);
+int dftg_get_densities(const dftg_ctx *ctx, double *out, size_t cap);
+int dftg_get_amplitudes(const dftg_ctx *ctx, double *out, size_t cap);
+int dftg_get_positions(const dftg_ctx *ctx, double *out, size_t cap);   /* [npts][3] */
+int dftg_get_potential(const dftg_ctx *ctx, double *out, size_t cap);   /* Hartree V */
+
+/* One-electron matrices S, T, V (sum over nuclei) and E_nuc, computed on the
+ * device in FP64 (DFT::construct_matrices dft.cpp:184-199, integrals.cpp:43-387,
+ * gamma.cpp:41-229).  Any pointer may be NULL. */
+int dftg_one_electron(dftg_ctx *ctx, double *S, double *T, double *V);
+int dftg_nuclear_repulsion(const dftg_ctx *ctx, double *enuc);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DFTG_H */

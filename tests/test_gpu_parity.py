@@ -1,0 +1,131 @@
+"""FP64 CUDA path vs the CPU oracle, through the C ABI (libdftg.so).
+
+Tolerances: the plain FP64 GPU build must reproduce the oracle's J, XC, E_xc
+and the per-point arrays to 1e-10 (absolute for matrix elements and energies,
+relative for point arrays)."""
+import numpy as np
+import pytest
+
+from dftcxx_gb300.molecule import Molecule, h2o, benzene, small_molecule
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def _pair(gpu_lib, oracle_mod, mol, nrad, leb, lmax, precision="fp64"):
+    from dftcxx_gb300.grid import MolecularGrid
+    g = MolecularGrid(mol, nrad, leb, lmax, precision=precision)
+    o = oracle_mod.OracleGrid(mol, nrad, leb, lmax)
+    return g, o
+
+
+def _density(mol, seed=0):
+    rng = np.random.default_rng(seed)
+    C = rng.normal(0, 0.3, size=(mol.nbf, max(1, mol.nelec // 2)))
+    return C @ C.T
+
+
+@pytest.mark.parametrize("name,basis,nrad,leb,lmax", [
+    ("H2O", "sto3g", 32, 7, 8),
+    ("LiH", "p631", 20, 5, 6),
+    ("NH3", "p631", 16, 8, 8),
+])
+def test_grid_and_amplitudes(gpu_lib, oracle_mod, name, basis, nrad, leb, lmax):
+    Z, xyz = small_molecule(name)
+    mol = Molecule(Z, xyz, basis)
+    g, o = _pair(gpu_lib, oracle_mod, mol, nrad, leb, lmax)
+    assert g.grid_size == o.npts
+    np.testing.assert_allclose(g.get_positions(), o.positions(), rtol=0, atol=1e-12)
+    # Becke weights lie in [0, 1]: compare absolutely (tiny weights come from
+    # cancelling distance differences and carry 1e-16 absolute noise)
+    wb_o = o.becke_weights()
+    assert np.abs(g.get_becke_weights() - wb_o).max() < 1e-13
+    w_o = o.weights()
+    w_geom = np.where(wb_o > 0, w_o / np.where(wb_o > 0, wb_o, 1.0), 0.0)
+    assert np.all(np.abs(g.get_weights() - w_o) <= 1e-12 * w_geom + 1e-300)
+    A = g.get_amplitudes()                       # nbf x npts
+    np.testing.assert_allclose(A.T, o.amplitudes(), rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("name,basis,nrad,leb,lmax", [
+    ("H2O", "sto3g", 32, 7, 8),
+    ("CH4", "p631", 20, 8, 6),
+    ("CO", "sto3g", 24, 10, 10),
+])
+def test_fock_build_fp64_matches_oracle(gpu_lib, oracle_mod, name, basis, nrad, leb, lmax):
+    Z, xyz = small_molecule(name)
+    mol = Molecule(Z, xyz, basis)
+    g, o = _pair(gpu_lib, oracle_mod, mol, nrad, leb, lmax)
+    P = _density(mol)
+    ref = o.fock_build(P)
+    out = g.fock_build(P)
+    assert abs(out["nelec"] - ref["nelec"]) < TOL
+    rho_o = o.densities()
+    assert np.abs(g.get_densities() - rho_o).max() <= 1e-12 * np.abs(rho_o).max()
+    np.testing.assert_allclose(g.get_potential(), o.potential(), rtol=1e-11, atol=1e-12)
+    assert np.abs(out["J"] - ref["J"]).max() < TOL
+    assert np.abs(out["XC"] - ref["XC"]).max() < TOL
+    assert abs(out["Exc"] - ref["Exc"]) < TOL
+
+
+def test_reference_call_sequence(gpu_lib, oracle_mod):
+    """set_density -> correct_densities -> hartree -> xc, as DFT::scf calls them."""
+    Z, xyz = h2o()
+    mol = Molecule(Z, xyz, "sto3g")
+    g, o = _pair(gpu_lib, oracle_mod, mol, 20, 7, 8)
+    P = _density(mol, 3)
+    g.set_density(P)
+    o.set_density(P)
+    assert abs(g.calculate_density() - o.calculate_density()) < TOL
+    assert abs(g.correct_densities() - o.correct_densities()) < 1e-12
+    assert abs(g.calculate_density() - mol.nelec) < 1e-9
+    J = g.calculate_hartree_potential()
+    assert np.abs(J - o.hartree()).max() < TOL
+    XC, exc = g.calculate_xc()
+    XCo, exco = o.xc()
+    assert np.abs(XC - XCo).max() < TOL
+    assert abs(exc - exco) < TOL
+
+
+def test_one_electron_matches_oracle(gpu_lib, oracle_mod):
+    for name, basis in (("H2O", "sto3g"), ("CO", "p631"), ("NH3", "p631")):
+        Z, xyz = small_molecule(name)
+        mol = Molecule(Z, xyz, basis)
+        g, o = _pair(gpu_lib, oracle_mod, mol, 8, 0, 0)
+        S, T, V = g.one_electron()
+        So, To, Vo = o.one_electron()
+        assert np.abs(S - So).max() < 1e-12
+        assert np.abs(T - To).max() < 1e-11
+        assert np.abs(V - Vo).max() < 1e-10
+        assert abs(g.nuclear_repulsion() - o.nuclear_repulsion()) < 1e-12
+
+
+def test_scf_h2o_fp64_matches_oracle(gpu_lib, oracle_mod):
+    """H2O / STO-3G / 32 x 110, SCF from the core guess to dE < 1e-8."""
+    from dftcxx_gb300.grid import DFT
+    Z, xyz = h2o()
+    mol = Molecule(Z, xyz, "sto3g")
+    d = DFT(mol, 32, 7, 8, precision="fp64")
+    e = d.scf(tol=1e-8)
+    og = oracle_mod.OracleGrid(mol, 32, 7, 8)
+    hist, _ = oracle_mod.scf(og, tol=1e-8)
+    assert len(d.history) == len(hist)
+    for a, b in zip(d.history, hist):
+        assert abs(a["E"] - b["E"]) < TOL
+        assert abs(a["Exc"] - b["Exc"]) < TOL
+    assert abs(e - hist[-1]["E"]) < TOL
+
+
+def test_mixed_precision_error_small(gpu_lib, oracle_mod):
+    Z, xyz = h2o()
+    mol = Molecule(Z, xyz, "sto3g")
+    from dftcxx_gb300.grid import MolecularGrid
+    g64 = MolecularGrid(mol, 32, 7, 8, precision="fp64")
+    gmx = MolecularGrid(mol, 32, 7, 8, precision="mixed")
+    P = _density(mol, 5)
+    a = g64.fock_build(P)
+    b = gmx.fock_build(P)
+    assert np.abs(a["J"] - b["J"]).max() < 1e-5
+    assert np.abs(a["XC"] - b["XC"]).max() < 1e-5
+    assert abs(a["Exc"] - b["Exc"]) < 1e-5
