@@ -1,0 +1,397 @@
+#!/usr/bin/env python3
+"""Benchmark: ms per SCF grid Fock build on one GB300, mixed vs FP64.
+
+Workload (the headline configuration): benzene D6h (C-C 2.640, C-H 2.040
+bohr), 6-31G (66 basis functions), 75 radial x 302 Lebedev points per atom,
+lmax 8: 271,800 grid points.  A step is one grid Fock build at a fixed density
+matrix P (the converged FP64 SCF density): rho on the grid, density
+correction, Slater+VWN point kernel, Becke-Poisson Hartree potential, J and XC.
+
+  value     ms per build in mixed precision, P already in HBM, device-timed with
+            CUDA events on the library's stream, L2 flushed before every step
+  e2e       the same metric through dftg_fock_build (host buffers: P copied in,
+            J, XC, E_xc, N copied out, all inside the timed region)
+  fp64      the same build with every step in FP64 (the metric's comparison)
+  accuracy  |dE_tot| between mixed and FP64 SCF energies at convergence, and
+            max|dJ|, max|dXC| at the converged P
+  roofline  dominant kernel of the mixed build, algorithmic bytes / measured
+            duration, against the measured HBM copy bandwidth
+
+--impl reference times the reference algorithm on the host cores (the C port
+under oracle/, OpenMP on all cores) for the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {"workload": "benzene/6-31G grid Fock build", "molecule": "C6H6 D6h", "basis": "6-31G", "nbf": 66,
+            "radial_points": 75, "lebedev_points": 302, "lmax": 8, "grid_points": 271800}
+
+# kernels launched per build, by profile phase (see dftcxx_gb300/csrc)
+KERNELS_PER_PHASE = {"convert_P": 1, "density": 1, "charge": 5, "lda": 2, "rholm": 1, "poisson": 1, "vown": 1,
+                     "splines": 1, "vcross": 1, "contract": 1, "contract_reduce": 1}
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    p = [x.strip() for x in line.split(",")]
+                    if len(p) >= 9:
+                        rows.append(p)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def _benzene_mol():
+    from dftcxx_gb300.molecule import Molecule, benzene
+    Z, xyz = benzene()
+    return Molecule(Z, xyz, "p631", "benzene")
+
+
+def run_reference(args, rank):
+    """Reference algorithm (C port, oracle/) on all host cores."""
+    if rank != 0:
+        return None
+    from oracle import oracle
+    oracle.build()
+    mol = _benzene_mol()
+    g = oracle.OracleGrid(mol, 75, 11, 8)
+    rng = np.random.default_rng(0)
+    C = rng.normal(0, 0.1, size=(mol.nbf, mol.nelec // 2))
+    P = C @ C.T
+    stride = 4
+    g.set_sample_stride(stride)
+    cores = oracle.lib().orc_num_threads()
+
+    def step():
+        t0 = time.perf_counter()
+        g.set_density(P)
+        g.correct_densities()
+        g.hartree()
+        t1 = time.perf_counter()
+        g.xc()
+        t2 = time.perf_counter()
+        tm = g.timings()     # [multipole+Poisson, cross-V, J, XC matrix] (sampled: cross-V, J, XC)
+        fixed = (t1 - t0) - tm[1] - tm[2] + (t2 - t1) - tm[3]
+        return (fixed + stride * (tm[1] + tm[2] + tm[3])) * 1e3
+
+    for _ in range(args.warmup):
+        step()
+    times = [step() for _ in range(args.steps)]
+    ms = float(np.mean(times))
+    sample = ("benzene/6-31G/75x302 Fock build per step; cross-atom potential, J and XC point loops "
+              "on every %d-th point, their wall time scaled by %d" % (stride, stride))
+    return {"metric": "ms per SCF grid Fock build", "value": ms, "unit": "ms", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic geometry (no dataset)",
+            "config": dict(WORKLOAD, parallelism="host OpenMP"), "impl": "reference",
+            "cpu_baseline": {"value": ms, "unit": "ms", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def _scf(grid, mol, S, H, enuc, precision, tol=1e-8, max_iter=200):
+    """Reference SCF iteration (dft.cpp:84-142) on one context."""
+    grid.set_precision(precision)
+    lam, U = np.linalg.eigh(S)
+    X = U @ np.diag(1.0 / np.sqrt(lam))
+    nocc = mol.nelec // 2
+    n = mol.nbf
+    J = np.zeros((n, n))
+    XC = np.zeros((n, n))
+    P = None
+
+    def dens(P):
+        _, Cp = np.linalg.eigh(X.T @ (H + 2 * J + XC) @ X)
+        C = X @ Cp
+        Pn = C[:, :nocc] @ C[:, :nocc].T
+        return Pn if P is None else 0.5 * Pn + 0.5 * P
+
+    P = dens(P)
+    grid.set_density(P)
+    grid.correct_densities()
+    J = grid.calculate_hartree_potential()
+    exc = 0.0
+    E = 2 * np.trace(P @ H) + 2 * np.trace(P @ J) + enuc + exc
+    old, it = E, 0
+    while True:
+        it += 1
+        P = dens(P)
+        r = grid.fock_build(P)
+        J, XC, exc = r["J"], r["XC"], r["Exc"]
+        E = 2 * np.trace(P @ H) + 2 * np.trace(P @ J) + enuc + exc
+        if (abs(E - old) < tol and it >= 3) or it >= max_iter:
+            return E, P, it
+        old = E
+
+
+def run_ours(args, rank, world):
+    import torch
+    from dftcxx_gb300 import build as b
+    from dftcxx_gb300 import _lib
+    from dftcxx_gb300.grid import MolecularGrid
+    b.build()
+    L = _lib.load()
+    dev = _env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(dev)
+    mol = _benzene_mol()
+    grid = MolecularGrid(mol, 75, 11, 8, precision="mixed", device=dev)
+    S, T, V = grid.one_electron()
+    H = T + V
+    enuc = grid.nuclear_repulsion()
+
+    # accuracy: converged SCF in both precisions (outside the timed region)
+    t0 = time.perf_counter()
+    E64, P64, it64 = _scf(grid, mol, S, H, enuc, "fp64")
+    Emx, Pmx, itmx = _scf(grid, mol, S, H, enuc, "mixed")
+    scf_s = time.perf_counter() - t0
+    grid.set_precision("fp64")
+    r64 = grid.fock_build(P64)
+    grid.set_precision("mixed")
+    rmx = grid.fock_build(P64)
+    dE_fixedP = abs(2 * np.trace(P64 @ (rmx["J"] - r64["J"])) + rmx["Exc"] - r64["Exc"])
+    accuracy = {"dE_tot_scf_Ha": abs(E64 - Emx), "E_tot_fp64_Ha": E64, "E_tot_mixed_Ha": Emx,
+                "scf_iterations": [it64, itmx], "dE_tot_fixed_P_Ha": dE_fixedP,
+                "max_dJ": float(np.abs(rmx["J"] - r64["J"]).max()),
+                "max_dXC": float(np.abs(rmx["XC"] - r64["XC"]).max()),
+                "dExc_Ha": abs(rmx["Exc"] - r64["Exc"])}
+
+    stream = torch.cuda.Stream(device=dev)
+    grid.set_stream(stream.cuda_stream)
+    nn = mol.nbf * mol.nbf
+    dP = torch.from_numpy(np.asfortranarray(P64).ravel(order="F").copy()).to(f"cuda:{dev}")
+    dJ = torch.zeros(nn, dtype=torch.float64, device=f"cuda:{dev}")
+    dXC = torch.zeros_like(dJ)
+    dS = torch.zeros(2, dtype=torch.float64, device=f"cuda:{dev}")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")   # > 129 MB L2
+
+    def dev_step():
+        rc = L.dftg_fock_build_device(grid.handle, ctypes.c_void_p(dP.data_ptr()), ctypes.c_void_p(dJ.data_ptr()),
+                                      ctypes.c_void_p(dXC.data_ptr()), ctypes.c_void_p(dS.data_ptr()))
+        _lib.check(rc)
+
+    def timed(precision, steps, warmup):
+        grid.set_precision(precision)
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                flush.zero_()
+                dev_step()
+            torch.cuda.synchronize(dev)
+            if world > 1:
+                torch.distributed.barrier()
+            evs = []
+            torch.cuda.nvtx.range_push("timed_" + precision)
+            for _ in range(steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                dev_step()
+                e1.record(stream)
+                evs.append((e0, e1))
+            torch.cuda.nvtx.range_pop()
+            torch.cuda.synchronize(dev)
+        return [a.elapsed_time(b) for a, b in evs]
+
+    def profile(precision, reps=5):
+        grid.set_precision(precision)
+        acc = {}
+        ms = (ctypes.c_double * 24)()
+        names = (ctypes.c_char_p * 24)()
+        n = ctypes.c_int()
+        for _ in range(reps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            _lib.check(L.dftg_fock_build_profile(grid.handle, ctypes.c_void_p(dP.data_ptr()), ms, names, 24,
+                                                 ctypes.byref(n)))
+            for i in range(n.value):
+                k = names[i].decode()
+                acc.setdefault(k, []).append(ms[i])
+        return {k: float(np.mean(v)) for k, v in acc.items()}
+
+    with ClockSampler(dev) as clk:
+        t_mx = timed("mixed", args.steps, args.warmup)
+        t_64 = timed("fp64", max(3, min(args.steps, 10)), 3)
+    clocks = clk.summary()
+    ms_mx = float(np.mean(t_mx))
+    ms_64 = float(np.mean(t_64))
+    prof_mx = profile("mixed")
+    prof_64 = profile("fp64")
+
+    # end to end through the public host-buffer call
+    grid.set_precision("mixed")
+    grid.set_stream(0)
+    hP = torch.from_numpy(np.asfortranarray(P64).ravel(order="F").copy()).pin_memory()
+    hJ = torch.zeros(nn, dtype=torch.float64).pin_memory()
+    hXC = torch.zeros(nn, dtype=torch.float64).pin_memory()
+    e_, n_ = ctypes.c_double(), ctypes.c_double()
+    dp = ctypes.POINTER(ctypes.c_double)
+
+    def e2e_step():
+        _lib.check(L.dftg_fock_build(grid.handle, ctypes.cast(hP.data_ptr(), dp), ctypes.cast(hJ.data_ptr(), dp),
+                                     ctypes.cast(hXC.data_ptr(), dp), ctypes.byref(e_), ctypes.byref(n_)))
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        e2e_step()
+    e2e = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    ms_e2e = float(np.mean(e2e))
+
+    # max over ranks
+    if world > 1:
+        t = torch.tensor([ms_mx, ms_e2e, ms_64], dtype=torch.float64, device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_mx, ms_e2e, ms_64 = (float(x) for x in t.tolist())
+
+    # roofline of the dominant mixed-precision kernel
+    hbm, _, peak_src = _peaks()
+    npts, nbf = grid.grid_size, mol.nbf
+    npad = (npts + 127) // 128 * 128
+    alg_bytes = {
+        "density": npad * nbf * 4 + 8 * npad + 4 * nbf * nbf,          # phi32 read, rho written, P read
+        "contract": npad * nbf * 4 + 2 * 4 * npad,                      # phi32 + two coefficient planes
+        "vcross": npad * (3 * 8 + 8 + 8 + 16),                          # xyz, w, V_own in; V, cj out
+        "lda": npad * (8 + 8) + npad * (8 + 4),
+    }
+    dom = max(prof_mx, key=lambda k: prof_mx[k])
+    dom_ms = prof_mx[dom]
+    roof = {"kernel": dom, "bound": "hbm", "unit": "GB/s", "peak": hbm, "peak_source": peak_src,
+            "traffic": None}
+    if dom in alg_bytes:
+        ach = alg_bytes[dom] / (dom_ms * 1e-3) / 1e9
+        roof.update(achieved=ach, frac=ach / hbm, bytes_per_launch=alg_bytes[dom])
+    else:
+        roof.update(achieved=None, frac=None)
+    launches_per_step = sum(KERNELS_PER_PHASE.get(k, 1) for k in prof_mx)
+
+    # CPU baseline: reference algorithm on the host cores, bounded sample
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        ref_args = argparse.Namespace(**vars(args))
+        ref_args.steps, ref_args.warmup = 1, 0
+        r = run_reference(ref_args, 0)
+        cpu = r["cpu_baseline"]
+
+    return {"metric": "ms per SCF grid Fock build (mixed precision)", "value": ms_mx, "unit": "ms",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mx,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32-split/f64",
+            "data": "synthetic geometry (no dataset)",
+            "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single GPU",
+                           l2="flushed (256 MB write) before every step"),
+            "fp64_ms_per_step": ms_64, "speedup_vs_fp64": ms_64 / ms_mx, "accuracy": accuracy,
+            "phases_ms_mixed": prof_mx, "phases_ms_fp64": prof_64,
+            "e2e": {"value": ms_e2e, "unit": "ms", "h2d_bytes_per_step": 8 * nn,
+                    "d2h_bytes_per_step": 2 * 8 * nn + 2 * 8},
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": launches_per_step * args.steps,
+            "scf_seconds_outside_timing": scf_s}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    world = _env_int("WORLD_SIZE", 1)
+    rank = _env_int("RANK", 0)
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        out = run_reference(args, rank)
+    else:
+        out = run_ours(args, rank, world)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -61,6 +61,8 @@ SIGNATURES = {
     "dftg_calculate_xc": [ctypes.c_void_p, _dp, _dp],
     "dftg_fock_build": [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp],
     "dftg_fock_build_device": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    "dftg_fock_build_profile": [ctypes.c_void_p, ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_char_p), ctypes.c_int,
+                                ctypes.POINTER(ctypes.c_int)],
     "dftg_get_weights": [ctypes.c_void_p, _dp, ctypes.c_size_t],
     "dftg_get_becke_weights": [ctypes.c_void_p, _dp, ctypes.c_size_t],
     "dftg_get_densities": [ctypes.c_void_p, _dp, ctypes.c_size_t],

@@ -34,6 +34,17 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line)
     return e == cudaErrorMemoryAllocation ? DFTG_ERR_NOMEM : DFTG_ERR_CUDA;
 }
 
+int mark(dftg_ctx *c, const char *name)
+{
+    if (c->prof_n >= dftg_ctx::kMaxMarks) return DFTG_OK;
+    cudaEvent_t &ev = c->prof_ev[c->prof_n];
+    if (!ev) DFTG_CUDA(cudaEventCreate(&ev));
+    DFTG_CUDA(cudaEventRecord(ev, c->stream));
+    c->prof_name[c->prof_n] = name;
+    ++c->prof_n;
+    return DFTG_OK;
+}
+
 static double dfact(int n) { double r = 1.0; for (int k = n; k > 1; k -= 2) r *= k; return r; }
 
 // GTO normalisation constant, cgf.cpp:102-114 (truncated pi of cgf.cpp:103)
@@ -68,6 +79,8 @@ static void free_ctx(dftg_ctx *c)
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
+    for (cudaEvent_t ev : c->prof_ev)
+        if (ev) cudaEventDestroy(ev);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }
@@ -418,6 +431,37 @@ int dftg_fock_build_device(dftg_ctx *c, const double *P_dev, double *J_dev, doub
         DFTG_CUDA(cudaMemcpyAsync(scalars_dev, c->d_scal + kScalExc, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
         DFTG_CUDA(cudaMemcpyAsync(scalars_dev + 1, c->d_scal + kScalNelec, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     }
+    c->have_density = true;
+    c->have_hartree = true;
+    return DFTG_OK;
+}
+
+int dftg_fock_build_profile(dftg_ctx *c, const double *P_dev, double *phase_ms, const char **names, int cap,
+                            int *nphase)
+{
+    CHECK_CTX(c);
+    if (!P_dev || !phase_ms || !nphase) { set_error("NULL argument"); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    c->prof_n = 0;
+    c->prof_on = true;
+    int rc = mark(c, "start");
+    if (rc == DFTG_OK && P_dev != c->d_P) {
+        cudaError_t e = cudaMemcpyAsync(c->d_P, P_dev, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "copy P", __FILE__, __LINE__);
+    }
+    if (rc == DFTG_OK) rc = fock_pipeline(c, true, true);
+    c->prof_on = false;
+    if (rc != DFTG_OK) return rc;
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    const int n = c->prof_n - 1 < cap ? c->prof_n - 1 : cap;
+    for (int i = 0; i < n; ++i) {
+        float ms = 0.f;
+        DFTG_CUDA(cudaEventElapsedTime(&ms, c->prof_ev[i], c->prof_ev[i + 1]));
+        phase_ms[i] = ms;
+        if (names) names[i] = c->prof_name[i + 1];
+    }
+    *nphase = n;
     c->have_density = true;
     c->have_hartree = true;
     return DFTG_OK;

@@ -110,6 +110,13 @@ struct dftg_ctx {
     // call-order state
     bool have_density = false;
     bool have_hartree = false;
+
+    // per-phase CUDA-event timing (dftg_fock_build_profile)
+    static constexpr int kMaxMarks = 24;
+    cudaEvent_t prof_ev[kMaxMarks] = {};
+    const char *prof_name[kMaxMarks] = {};
+    int prof_n = 0;
+    bool prof_on = false;
 };
 
 namespace dftg {
@@ -123,6 +130,10 @@ enum {
     kScalAtomQ = 8,    // [natoms] per-atom integral of rho (after correction)
 };
 inline size_t scal_elems(int natoms) { return 8 + (size_t)natoms; }
+
+// records a named event after the preceding launch when profiling is on
+int mark(dftg_ctx *c, const char *name);
+#define DFTG_MARK(c, name) do { if ((c)->prof_on) { int rc_m_ = ::dftg::mark((c), (name)); if (rc_m_) return rc_m_; } } while (0)
 
 // k_grid.cu
 int launch_grid(dftg_ctx *c);

@@ -156,10 +156,12 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
         else k_contract<float, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, c->d_cj32, wx, wj, d_tiles, c->d_part);
     }
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "contract");
     const size_t nn = (size_t)c->nbf * c->nbf;
     k_contract_reduce<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->nbf, tile, c->nchunk, wx, wj, c->d_part,
                                                                           c->d_XC, c->d_J);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "contract_reduce");
     return DFTG_OK;
 }
 

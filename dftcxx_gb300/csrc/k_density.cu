@@ -220,6 +220,7 @@ int launch_convert_P(dftg_ctx *c)
     const int n = c->nbf * c->nbf;
     k_convert_P<<<(n + 255) / 256, 256, 0, c->stream>>>(n, c->d_P, c->d_P32);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "convert_P");
     return DFTG_OK;
 }
 
@@ -236,6 +237,7 @@ int launch_density(dftg_ctx *c)
         k_density<float><<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi32, c->d_P32, c->d_rho);
     }
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "density");
     return DFTG_OK;
 }
 
@@ -257,6 +259,7 @@ int launch_atom_sums(dftg_ctx *c, bool apply_scale)
         k_atom_final<<<1, 32, 0, c->stream>>>(c->natoms, cpa, c->d_red, c->d_atoms, c->d_scal, 1);
         DFTG_LAUNCH_CHECK();
     }
+    DFTG_MARK(c, "charge");
     return DFTG_OK;
 }
 
@@ -270,6 +273,7 @@ int launch_xc_points(dftg_ctx *c)
     DFTG_LAUNCH_CHECK();
     k_sum_to_scalar<<<1, kRedBlock, 0, c->stream>>>((int)nb, c->d_red, c->d_scal, kScalExc);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "lda");
     return DFTG_OK;
 }
 

@@ -421,19 +421,23 @@ int launch_hartree(dftg_ctx *c)
     k_rholm<<<c->natoms * N, 128, sizeof(double) * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho, c->d_wb, c->d_Yw,
                                                                          c->d_rholm);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "rholm");
     const int nrhs = c->natoms * nlm;
     const size_t sm = sizeof(double) * S * 32;
     if (sm > 48 * 1024) DFTG_CUDA(cudaFuncSetAttribute(k_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_poisson<<<(nrhs + 31) / 32, 32, sm, c->stream>>>(c->natoms, N, c->lmax, c->d_rn, c->d_LU, c->d_piv, c->d_rholm,
                                                        c->d_scal, c->d_U);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "poisson");
     k_vown<<<(unsigned)((c->npts + 127) / 128), 128, 0, c->stream>>>(c->npts, N, c->nang, nlm, c->d_rn, c->d_leb,
                                                                      c->d_Y, c->d_U, c->d_Vown);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "vown");
     // the spline work area reuses the contraction partial buffer (3 * nrhs * N doubles)
     k_splines<<<(nrhs + 63) / 64, 64, 0, c->stream>>>(c->natoms, N, nlm, c->d_sx, c->d_U, c->d_spl, c->d_spl32,
                                                       c->d_part);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "splines");
     const unsigned nb = (unsigned)(c->npad / 128);
     if (c->precision == DFTG_PREC_FP64)
         k_vcross<double><<<nb, 128, 0, c->stream>>>(c->npts, c->npad, c->natoms, N, c->nang, c->lmax, c->d_atoms,
@@ -444,6 +448,7 @@ int launch_hartree(dftg_ctx *c)
                                                    c->d_x, c->d_y, c->d_z, c->d_w, c->d_sx, c->d_spl32, c->d_pre32,
                                                    c->d_rec32, c->d_Vown, c->d_V, c->d_cj, c->d_cj32);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "vcross");
     return DFTG_OK;
 }
 

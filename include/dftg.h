@@ -121,6 +121,13 @@ int dftg_fock_build(dftg_ctx *ctx, const double *P, double *J, double *XC,
 int dftg_fock_build_device(dftg_ctx *ctx, const double *P_dev, double *J_dev,
                            double *XC_dev, double *scalars_dev);
 
+/* Diagnostic variant of dftg_fock_build_device (no counterpart in the
+ * reference, which only prints wall-clock totals, dft.cpp:98-119): runs one
+ * build with CUDA events between the kernel phases and returns up to cap
+ * per-phase durations in milliseconds with their names (static strings). */
+int dftg_fock_build_profile(dftg_ctx *ctx, const double *P_dev, double *phase_ms,
+                            const char **names, int cap, int *nphase);
+
 /* Getters (copies): MolecularGrid::get_weights / get_densities /
  * get_amplitudes (moleculargrid.cpp:61-127).  cap is the element capacity of
  * out.  Amplitudes are nbf x npts column-major (the reference's layout). */

@@ -58,7 +58,23 @@ typedef struct {
     double *sx;              /* [nrad] increasing spline abscissae */
     double *sy;              /* [natoms][nlm][nrad] spline ordinates */
     double *sc;              /* [natoms][nlm][nrad-1][4] spline coefficients */
+    int stride;              /* timing sample: point loops visit every stride-th point */
+    double tm[4];            /* wall times: multipole+Poisson, cross-atom V, J, XC */
 } orc_t;
+
+static double orc_now(void)
+{
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+}
+
+/* Bounded-sample timing mode (CPU baseline only): the cross-atom potential,
+ * the J assembly and the XC matrix visit every stride-th point; the caller
+ * scales their wall times (orc_get_timings) by stride.  Results are then not
+ * the full build and must not be used as values. */
 
 /* ---------------------------------------------------------------- basis */
 
@@ -293,6 +309,7 @@ orc_t *orc_create(int natoms, const int *Z, const double *xyz,
     o->sx = malloc(sizeof(double) * nrad);
     o->sy = malloc(sizeof(double) * (size_t)natoms * o->nlm * nrad);
     o->sc = malloc(sizeof(double) * (size_t)natoms * o->nlm * (nrad - 1) * 4);
+    o->stride = 1;
 
     const int off = dftg_lebedev_offset[leb];
     const double f = ORC_PI / (double)(nrad + 1);
@@ -358,6 +375,8 @@ void orc_destroy(orc_t *o)
 }
 
 long orc_grid_size(const orc_t *o) { return (long)o->npts; }
+void orc_set_sample_stride(orc_t *o, int s) { o->stride = s < 1 ? 1 : s; }
+void orc_get_timings(const orc_t *o, double *out) { memcpy(out, o->tm, sizeof(o->tm)); }
 int orc_nang(const orc_t *o) { return o->nang; }
 
 void orc_get_weights(const orc_t *o, double *out) { memcpy(out, o->w, sizeof(double) * o->npts); }
@@ -511,12 +530,15 @@ double orc_xc(orc_t *o, double *XC, double *vxc_out)
     double exc = 0.0;
     for (size_t i = 0; i < n; ++i) exc += o->w[i] * e[i];
     /* nbf^2 dot products over the grid, serial as in dft.cpp:426-432 */
+    const size_t st = (size_t)o->stride;
+    double t0 = orc_now();
     for (int i = 0; i < nbf; ++i)
         for (int j = 0; j < nbf; ++j) {
             double s = 0.0;
-            for (size_t p = 0; p < n; ++p) s += wva[p] * o->phi[p * nbf + i] * o->phi[p * nbf + j];
+            for (size_t p = 0; p < n; p += st) s += wva[p] * o->phi[p * nbf + i] * o->phi[p * nbf + j];
             XC[i + (size_t)j * nbf] = s;
         }
+    o->tm[3] = orc_now() - t0;
     free(wva);
     free(e);
     return exc;
@@ -701,14 +723,17 @@ static void calc_U_lm(orc_t *o, int a)
 void orc_hartree(orc_t *o, double *J)
 {
     const int N = o->nrad, nlm = o->nlm, nang = o->nang, nbf = o->nbf;
+    const long st = o->stride;
+    double t0 = orc_now();
     for (int a = 0; a < o->natoms; ++a) {
         calc_rho_lm(o, a);
         calc_U_lm(o, a);
     }
+    double t1 = orc_now();
     for (int i = 0; i < o->natoms; ++i) {
         size_t base = (size_t)i * N * nang;
         #pragma omp parallel for schedule(static)
-        for (long j = 0; j < (long)N * nang; ++j) {
+        for (long j = 0; j < (long)N * nang; j += st) {
             double V = 0.0;
             const double *pp = o->pos + 3 * (base + j);
             for (int k = 0; k < o->natoms; ++k) {
@@ -728,6 +753,7 @@ void orc_hartree(orc_t *o, double *J)
             o->V[base + j] = V;
         }
     }
+    double t2 = orc_now();
     memset(J, 0, sizeof(double) * nbf * nbf);
     double *Jj = malloc(sizeof(double) * nbf * nbf);
     for (int a = 0; a < o->natoms; ++a) {
@@ -736,7 +762,7 @@ void orc_hartree(orc_t *o, double *J)
         for (int i = 0; i < nbf; ++i)
             for (int j = i; j < nbf; ++j) {
                 double s = 0.0;
-                for (size_t p = 0; p < cnt; ++p) {
+                for (size_t p = 0; p < cnt; p += (size_t)st) {
                     size_t q = base + p;
                     s += o->w[q] * o->V[q] * o->phi[q * nbf + i] * o->phi[q * nbf + j];
                 }
@@ -745,6 +771,9 @@ void orc_hartree(orc_t *o, double *J)
         for (int t = 0; t < nbf * nbf; ++t) J[t] += Jj[t];
     }
     free(Jj);
+    o->tm[0] = t1 - t0;
+    o->tm[1] = t2 - t1;
+    o->tm[2] = orc_now() - t2;
 }
 
 /* ------------------------------------------------- one-electron integrals */

@@ -67,6 +67,8 @@ def lib():
         L.orc_gto_norm.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.orc_poisson_matrix.argtypes = [ctypes.c_int, _dp, _dp]
         L.orc_num_threads.restype = ctypes.c_int
+        L.orc_set_sample_stride.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_get_timings.argtypes = [ctypes.c_void_p, _dp]
         _lib = L
     return _lib
 
@@ -179,6 +181,15 @@ class OracleGrid:
 
     def nuclear_repulsion(self):
         return lib().orc_nuclear_repulsion(self.h)
+
+    def set_sample_stride(self, stride):
+        """Timing-only mode: point loops of the cross-atom potential, J and XC
+        visit every stride-th point (results are then NOT the full build)."""
+        lib().orc_set_sample_stride(self.h, int(stride))
+
+    def timings(self):
+        """Wall times of the last build: [multipole+Poisson, cross-atom V, J, XC]."""
+        return self._get("orc_get_timings", 4)
 
     def fock_build(self, P):
         """One grid Fock build at fixed P: set_density, correct_densities,
