@@ -70,6 +70,8 @@ SIGNATURES = {
     "dftg_get_positions": [ctypes.c_void_p, _dp, ctypes.c_size_t],
     "dftg_get_potential": [ctypes.c_void_p, _dp, ctypes.c_size_t],
     "dftg_one_electron": [ctypes.c_void_p, _dp, _dp, _dp],
+    "dftg_contract_noalloc": [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     "dftg_nuclear_repulsion": [ctypes.c_void_p, _dp],
 }
 

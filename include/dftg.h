@@ -144,6 +144,26 @@ int dftg_get_potential(const dftg_ctx *ctx, double *out, size_t cap);   /* Hartr
 int dftg_one_electron(dftg_ctx *ctx, double *S, double *T, double *V);
 int dftg_nuclear_repulsion(const dftg_ctx *ctx, double *enuc);
 
+/* XC and J contraction that allocates nothing.  No counterpart in the
+ * reference: it exists for callers that may not call cudaMalloc / cudaFree
+ * while serving (their framework owns all device memory, or they run under a
+ * fixed device-memory budget).  Computes, in FP64,
+ *   XC = phi^T diag(cxc) phi,   J = phi^T diag(cj) phi
+ * from caller-owned device buffers on the current device: phi is nbf rows of
+ * npts amplitudes, row stride ld (>= npts) doubles; cxc, cj hold npts point
+ * coefficients; XC and J (nbf x nbf, either may be NULL) are written.  Its
+ * scratch is a static device array of DFTG_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading the library holds until exit; nbf above DFTG_NOALLOC_MAX_NBF is
+ * rejected with DFTG_ERR_ARG.  The first call on a device looks up that array
+ * (make it before any stream capture).  Calls that overlap on the GPU race on
+ * the shared array.  stream: a cudaStream_t, NULL for the legacy stream; the
+ * call returns without synchronising. */
+#define DFTG_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+#define DFTG_NOALLOC_MAX_NBF 1024
+int dftg_contract_noalloc(const double *phi, size_t ld, size_t npts, int nbf,
+                          const double *cxc, const double *cj, double *XC,
+                          double *J, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
