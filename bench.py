@@ -194,7 +194,7 @@ def _scf(grid, mol, S, H, enuc, precision, tol=1e-8, max_iter=200):
         P = dens(P)
         r = grid.fock_build(P)
         J, XC, exc = r["J"], r["XC"], r["Exc"]
-        E = 2 * np.trace(P @ H) + 2 * np.trace(P @ J) + enuc + exc
+        E = 2 * np.trace(P @ H) + r["EJ"] + enuc + exc     # E_J = 2 tr(P J) summed on the grid
         if (abs(E - old) < tol and it >= 3) or it >= max_iter:
             return E, P, it
         old = E
@@ -224,12 +224,24 @@ def run_ours(args, rank, world):
     r64 = grid.fock_build(P64)
     grid.set_precision("mixed")
     rmx = grid.fock_build(P64)
-    dE_fixedP = abs(2 * np.trace(P64 @ (rmx["J"] - r64["J"])) + rmx["Exc"] - r64["Exc"])
+    dE_fixedP = abs(rmx["EJ"] - r64["EJ"] + rmx["Exc"] - r64["Exc"])
+    dE_Jmatrix = abs(2 * np.trace(P64 @ (rmx["J"] - r64["J"])))
+    # error budget: each step alone in its mixed form, at the converged FP64 density
+    ablation = {}
+    for name, bit in grid.MIX_BITS.items():
+        grid.set_precision_mask(bit)
+        rb = grid.fock_build(P64)
+        ablation[name] = {"dE_tot_Ha": float(rb["EJ"] - r64["EJ"] + rb["Exc"] - r64["Exc"]),
+                          "dE_2trPdJ_Ha": float(2 * np.trace(P64 @ (rb["J"] - r64["J"]))),
+                          "max_dJ": float(np.abs(rb["J"] - r64["J"]).max()),
+                          "max_dXC": float(np.abs(rb["XC"] - r64["XC"]).max())}
     accuracy = {"dE_tot_scf_Ha": abs(E64 - Emx), "E_tot_fp64_Ha": E64, "E_tot_mixed_Ha": Emx,
                 "scf_iterations": [it64, itmx], "dE_tot_fixed_P_Ha": dE_fixedP,
                 "max_dJ": float(np.abs(rmx["J"] - r64["J"]).max()),
                 "max_dXC": float(np.abs(rmx["XC"] - r64["XC"]).max()),
-                "dExc_Ha": abs(rmx["Exc"] - r64["Exc"])}
+                "dExc_Ha": abs(rmx["Exc"] - r64["Exc"]), "dE_2trPdJ_Ha": dE_Jmatrix,
+                "dE_J_grid_fp64_vs_2trPJ_Ha": abs(r64["EJ"] - 2 * np.trace(P64 @ r64["J"])),
+                "per_step": ablation}
 
     stream = torch.cuda.Stream(device=dev)
     grid.set_stream(stream.cuda_stream)

@@ -54,6 +54,7 @@ SIGNATURES = {
     "dftg_nbf": [ctypes.c_void_p, _ip],
     "dftg_set_precision": [ctypes.c_void_p, ctypes.c_int],
     "dftg_set_stream": [ctypes.c_void_p, ctypes.c_void_p],
+    "dftg_set_precision_mask": [ctypes.c_void_p, ctypes.c_uint],
     "dftg_set_density": [ctypes.c_void_p, _dp],
     "dftg_correct_densities": [ctypes.c_void_p, _dp],
     "dftg_calculate_density": [ctypes.c_void_p, _dp],
@@ -73,6 +74,7 @@ SIGNATURES = {
     "dftg_contract_noalloc": [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     "dftg_nuclear_repulsion": [ctypes.c_void_p, _dp],
+    "dftg_get_energies": [ctypes.c_void_p, _dp, _dp, _dp],
 }
 
 _lib = None

@@ -74,8 +74,9 @@ static void free_ctx(dftg_ctx *c)
                     c->d_pa, c->d_pcn, c->d_x, c->d_y, c->d_z, c->d_w, c->d_wb, c->d_rho, c->d_V, c->d_Vown,
                     c->d_cxc, c->d_cj, c->d_cxc32, c->d_cj32, c->d_phi, c->d_phi32, c->d_P, c->d_P32, c->d_J,
                     c->d_XC, c->d_part, c->d_red, c->d_scal, c->d_Y, c->d_Yw, c->d_pre, c->d_pre32, c->d_rec,
-                    c->d_rec32, c->d_rholm, c->d_U, c->d_LU, c->d_piv, c->d_sx, c->d_spl, c->d_spl32, c->d_tiles,
-                    c->d_ints_work};
+                    c->d_rec32, c->d_rholm, c->d_U, c->d_U32, c->d_Y32, c->d_Ywt32, c->d_fold, c->d_Gt,
+                    c->d_Gb, c->d_Kt, c->d_sx, c->d_splf, c->d_spl, c->d_splm, c->d_tiles,
+                    c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_flag};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -161,7 +162,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(dalloc(&c->d_J, nn));
     DFTG_TRY(dalloc(&c->d_XC, nn));
     size_t part = contract_part_elems(c->nbf, c->npad);
-    const size_t spline_work = 3 * (size_t)c->natoms * nlm * N;
+    const size_t spline_work = 2 * (size_t)c->natoms * nlm * N;
     c->part_elems = part > spline_work ? part : spline_work;
     DFTG_TRY(dalloc(&c->d_part, c->part_elems));
     c->red_elems = reduction_elems(c->npad, c->natoms, c->nrad, c->nang) + 64;
@@ -176,11 +177,14 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(dalloc(&c->d_rec32, 2 * nlm));
     DFTG_TRY(dalloc(&c->d_rholm, (size_t)c->natoms * nlm * N));
     DFTG_TRY(dalloc(&c->d_U, (size_t)c->natoms * nlm * N));
-    DFTG_TRY(dalloc(&c->d_LU, (size_t)(c->lmax + 1) * (N + 2) * (N + 2)));
-    DFTG_TRY(dalloc(&c->d_piv, (size_t)(c->lmax + 1) * (N + 2)));
+    DFTG_TRY(dalloc(&c->d_U32, 2 * (size_t)c->natoms * nlm * N));
+    DFTG_TRY(dalloc(&c->d_Y32, 2 * nlm * c->nang));
+    DFTG_TRY(dalloc(&c->d_Ywt32, 2 * nlm * c->nang));
+    DFTG_TRY(dalloc(&c->d_fold, nlm));
     DFTG_TRY(dalloc(&c->d_sx, N));
+    DFTG_TRY(dalloc(&c->d_splf, hartree_splf_elems(c->nrad)));
     DFTG_TRY(dalloc(&c->d_spl, (size_t)c->natoms * nlm * N * 4));
-    DFTG_TRY(dalloc(&c->d_spl32, (size_t)c->natoms * nlm * N * 4));
+    DFTG_TRY(dalloc(&c->d_splm, (size_t)c->natoms * nlm * N * 8));
     DFTG_CUDA(cudaMemset(c->d_scal, 0, sizeof(double) * scal_elems(c->natoms)));
 
     std::vector<double> atoms(4 * (size_t)c->natoms), rab((size_t)c->natoms * c->natoms);
@@ -210,6 +214,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(launch_amplitudes(c));
     DFTG_TRY(hartree_setup(c));
     DFTG_TRY(contract_setup(c));
+    DFTG_TRY(density_tc_setup(c));
     DFTG_CUDA(cudaStreamSynchronize(c->stream));
     return DFTG_OK;
 }
@@ -237,18 +242,27 @@ static int sync_scalars(dftg_ctx *c)
     DFTG_CUDA(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(double) * scal_elems(c->natoms), cudaMemcpyDeviceToHost,
                               c->stream));
     DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->d_flag) {   // a bounded wait inside a kernel gave up
+        int flag = 0;
+        DFTG_CUDA(cudaMemcpy(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+        if (flag) {
+            DFTG_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
+            set_error("a bounded device wait expired (code %d); results of this build are invalid", flag);
+            return DFTG_ERR_TIMEOUT;
+        }
+    }
     return DFTG_OK;
 }
 
 // device part of one Fock build; P already in c->d_P
-static int fock_pipeline(dftg_ctx *c, bool want_xc, bool want_j)
+static int fock_pipeline(dftg_ctx *c)
 {
-    if (c->precision != DFTG_PREC_FP64) DFTG_TRY(launch_convert_P(c));
     DFTG_TRY(launch_density(c));
-    DFTG_TRY(launch_atom_sums(c, true));
-    if (want_xc) DFTG_TRY(launch_xc_points(c));
-    if (want_j) DFTG_TRY(launch_hartree(c));
-    DFTG_TRY(launch_contract(c, want_xc, want_j));
+    DFTG_TRY(launch_atom_sums(c, kSumsFactor));
+    DFTG_TRY(launch_xc_points(c, true));    // rescales rho by the correction factor
+    c->rho_scaled = true;
+    DFTG_TRY(launch_hartree(c));
+    DFTG_TRY(launch_contract(c, true, true));
     return DFTG_OK;
 }
 
@@ -341,6 +355,16 @@ int dftg_set_precision(dftg_ctx *c, int precision)
     CHECK_CTX(c);
     if (precision != DFTG_PREC_FP64 && precision != DFTG_PREC_MIXED) { set_error("unknown precision %d", precision); return DFTG_ERR_ARG; }
     c->precision = precision;
+    c->prec_mask = precision == DFTG_PREC_MIXED ? (unsigned)kPrecAll : 0u;
+    return DFTG_OK;
+}
+
+int dftg_set_precision_mask(dftg_ctx *c, unsigned mask)
+{
+    CHECK_CTX(c);
+    if (mask & ~(unsigned)kPrecAll) { set_error("unknown precision bits 0x%x", mask); return DFTG_ERR_ARG; }
+    c->prec_mask = mask;
+    c->precision = mask ? DFTG_PREC_MIXED : DFTG_PREC_FP64;
     return DFTG_OK;
 }
 
@@ -358,12 +382,12 @@ int dftg_set_density(dftg_ctx *c, const double *P)
     DFTG_TRY(check_matrix(P, c->nbf));
     DFTG_CUDA(cudaSetDevice(c->device));
     DFTG_CUDA(cudaMemcpyAsync(c->d_P, P, sizeof(double) * c->nbf * c->nbf, cudaMemcpyHostToDevice, c->stream));
-    if (c->precision != DFTG_PREC_FP64) DFTG_TRY(launch_convert_P(c));
     DFTG_TRY(launch_density(c));
-    DFTG_TRY(launch_atom_sums(c, false));
+    DFTG_TRY(launch_atom_sums(c, kSumsOnly));
     DFTG_CUDA(cudaStreamSynchronize(c->stream));
     c->have_density = true;
     c->have_hartree = false;
+    c->rho_scaled = false;
     return DFTG_OK;
 }
 
@@ -372,7 +396,8 @@ int dftg_correct_densities(dftg_ctx *c, double *scale)
     CHECK_CTX(c);
     if (!c->have_density) { set_error("correct_densities before set_density"); return DFTG_ERR_STATE; }
     DFTG_CUDA(cudaSetDevice(c->device));
-    DFTG_TRY(launch_atom_sums(c, true));
+    DFTG_TRY(launch_atom_sums(c, kSumsCorrect));
+    c->rho_scaled = true;
     DFTG_TRY(sync_scalars(c));
     if (scale) *scale = c->h_scal[kScalScale];
     return DFTG_OK;
@@ -384,7 +409,7 @@ int dftg_calculate_density(dftg_ctx *c, double *nelec)
     if (!nelec) { set_error("nelec NULL"); return DFTG_ERR_ARG; }
     if (!c->have_density) { set_error("calculate_density before set_density"); return DFTG_ERR_STATE; }
     DFTG_CUDA(cudaSetDevice(c->device));
-    DFTG_TRY(launch_atom_sums(c, false));
+    DFTG_TRY(launch_atom_sums(c, kSumsOnly));
     DFTG_TRY(sync_scalars(c));
     *nelec = c->h_scal[kScalNelec];
     return DFTG_OK;
@@ -395,7 +420,7 @@ int dftg_calculate_hartree_potential(dftg_ctx *c, double *J)
     CHECK_CTX(c);
     if (!c->have_density) { set_error("calculate_hartree_potential before set_density"); return DFTG_ERR_STATE; }
     DFTG_CUDA(cudaSetDevice(c->device));
-    DFTG_TRY(launch_atom_sums(c, false));   // per-atom charges of the current rho
+    DFTG_TRY(launch_atom_sums(c, kSumsOnly));   // per-atom charges of the current rho
     DFTG_TRY(launch_hartree(c));
     DFTG_TRY(launch_contract(c, false, true));
     if (J) DFTG_CUDA(cudaMemcpyAsync(J, c->d_J, sizeof(double) * c->nbf * c->nbf, cudaMemcpyDeviceToHost, c->stream));
@@ -409,7 +434,7 @@ int dftg_calculate_xc(dftg_ctx *c, double *XC, double *exc)
     CHECK_CTX(c);
     if (!c->have_density) { set_error("calculate_xc before set_density"); return DFTG_ERR_STATE; }
     DFTG_CUDA(cudaSetDevice(c->device));
-    DFTG_TRY(launch_xc_points(c));
+    DFTG_TRY(launch_xc_points(c, false));
     DFTG_TRY(launch_contract(c, true, false));
     if (XC) DFTG_CUDA(cudaMemcpyAsync(XC, c->d_XC, sizeof(double) * c->nbf * c->nbf, cudaMemcpyDeviceToHost, c->stream));
     DFTG_TRY(sync_scalars(c));
@@ -424,12 +449,13 @@ int dftg_fock_build_device(dftg_ctx *c, const double *P_dev, double *J_dev, doub
     DFTG_CUDA(cudaSetDevice(c->device));
     const size_t nn = (size_t)c->nbf * c->nbf;
     if (P_dev != c->d_P) DFTG_CUDA(cudaMemcpyAsync(c->d_P, P_dev, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
-    DFTG_TRY(fock_pipeline(c, true, true));
+    DFTG_TRY(fock_pipeline(c));
     if (J_dev) DFTG_CUDA(cudaMemcpyAsync(J_dev, c->d_J, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
     if (XC_dev) DFTG_CUDA(cudaMemcpyAsync(XC_dev, c->d_XC, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
     if (scalars_dev) {
         DFTG_CUDA(cudaMemcpyAsync(scalars_dev, c->d_scal + kScalExc, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
         DFTG_CUDA(cudaMemcpyAsync(scalars_dev + 1, c->d_scal + kScalNelec, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        DFTG_CUDA(cudaMemcpyAsync(scalars_dev + 2, c->d_scal + kScalEJ, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     }
     c->have_density = true;
     c->have_hartree = true;
@@ -450,7 +476,7 @@ int dftg_fock_build_profile(dftg_ctx *c, const double *P_dev, double *phase_ms, 
         cudaError_t e = cudaMemcpyAsync(c->d_P, P_dev, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream);
         if (e != cudaSuccess) rc = cuda_fail(e, "copy P", __FILE__, __LINE__);
     }
-    if (rc == DFTG_OK) rc = fock_pipeline(c, true, true);
+    if (rc == DFTG_OK) rc = fock_pipeline(c);
     c->prof_on = false;
     if (rc != DFTG_OK) return rc;
     DFTG_CUDA(cudaStreamSynchronize(c->stream));
@@ -475,7 +501,7 @@ int dftg_fock_build(dftg_ctx *c, const double *P, double *J, double *XC, double 
     DFTG_CUDA(cudaSetDevice(c->device));
     const size_t nn = (size_t)c->nbf * c->nbf;
     DFTG_CUDA(cudaMemcpyAsync(c->d_P, P, sizeof(double) * nn, cudaMemcpyHostToDevice, c->stream));
-    DFTG_TRY(fock_pipeline(c, true, true));
+    DFTG_TRY(fock_pipeline(c));
     if (J) DFTG_CUDA(cudaMemcpyAsync(J, c->d_J, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream));
     if (XC) DFTG_CUDA(cudaMemcpyAsync(XC, c->d_XC, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream));
     DFTG_TRY(sync_scalars(c));
@@ -531,6 +557,17 @@ int dftg_get_amplitudes(const dftg_ctx *c, double *out, size_t cap)
         DFTG_CUDA(cudaMemcpy(t.data(), c->d_phi + (size_t)mu * c->npad, sizeof(double) * c->npts, cudaMemcpyDeviceToHost));
         for (size_t p = 0; p < c->npts; ++p) out[mu + p * (size_t)c->nbf] = t[p];
     }
+    return DFTG_OK;
+}
+
+int dftg_get_energies(dftg_ctx *c, double *exc, double *ej, double *nelec)
+{
+    CHECK_CTX(c);
+    DFTG_CUDA(cudaSetDevice(c->device));
+    DFTG_TRY(sync_scalars(c));
+    if (exc) *exc = c->h_scal[kScalExc];
+    if (ej) *ej = c->h_scal[kScalEJ];
+    if (nelec) *nelec = c->h_scal[kScalNelec];
     return DFTG_OK;
 }
 

@@ -7,7 +7,8 @@
 //               phi32 [nbf][npad] FP32      (mixed-precision copy)
 //   point coefficients  cxc = w*v_xc, cj = w*V/2   [npad] FP64 and FP32
 //   Hartree     Y [nlm][nang], rholm/U [natoms][nlm][nrad], LU factors per l,
-//               spline coefficients [natoms][nlm][nrad][4] (last interval = clamp)
+//               spline coefficients [natoms][nlm][nrad][4] (last interval = clamp),
+//               FP64 and, for the mixed path, normalised and split into FP32 hi/lo
 #pragma once
 #include <cuda_runtime.h>
 #include <cstddef>
@@ -33,6 +34,16 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
     } while (0)
 
 #define DFTG_LAUNCH_CHECK() DFTG_CUDA(cudaGetLastError())
+#define DFTG_TRY_L(x) do { int rc_l_ = (x); if (rc_l_ != DFTG_OK) return rc_l_; } while (0)
+
+// compensated FP32 accumulation (Knuth's TwoSum): s + e is the running sum
+__device__ __forceinline__ void two_sum_acc(float &s, float &e, float x)
+{
+    const float t = s + x;
+    const float bp = t - s;
+    e += (s - (t - bp)) + (x - bp);
+    s = t;
+}
 
 }  // namespace dftg
 
@@ -41,6 +52,7 @@ struct dftg_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     int precision = DFTG_PREC_FP64;
+    unsigned prec_mask = 0;       // kPrec* bits: steps run in reduced precision
 
     // molecule and basis (host copies)
     int natoms = 0, nbf = 0, nprim = 0;
@@ -98,11 +110,26 @@ struct dftg_ctx {
     float *d_rec32 = nullptr;
     double *d_rholm = nullptr;    // [natoms][nlm][nrad]
     double *d_U = nullptr;        // [natoms][nlm][nrad]
-    double *d_LU = nullptr;       // [lmax+1][S][S] packed LU factors, S = nrad+2
-    int *d_piv = nullptr;         // [lmax+1][S]
+    float *d_U32 = nullptr;       // [2][natoms][nlm][nrad] U split into FP32 hi, lo
+    float *d_Y32 = nullptr;       // [2][nlm][nang] Y_lm split into FP32 hi, lo
+    float *d_Ywt32 = nullptr;     // [2][nang][nlm] w_leb Y_lm split, transposed
+    double *d_fold = nullptr;     // [nlm] Y_lm normalisation of the integer recursion
+    double *d_Gt = nullptr;       // [lmax+1][nrad (k)][nrad (i)] radial Poisson solution map
+    double *d_Gb = nullptr;       // [nrad] boundary column of the l = 0 map (times q_a)
+    double *d_Kt = nullptr;       // [nrad (j)][nrad (i)] spline derivative map
     double *d_sx = nullptr;       // [nrad] increasing spline abscissae
-    double *d_spl = nullptr;      // [natoms][nrad-1][nlm][4]
-    float *d_spl32 = nullptr;     // same in FP32
+    double *d_splf = nullptr;     // spline factorisation (x only)
+    double *d_spl = nullptr;      // [natoms][nlm][nrad][4] FP64 spline coefficients
+    float *d_splm = nullptr;      // [natoms][nlm][nrad][8] normalised coefficients, FP32 hi + lo
+
+    // device: tensor-core density (integer-slice split of phi and P)
+    bool tc_ready = false;
+    int tc_KP = 0, tc_NP = 0, tc_grid = 0;
+    void *d_tcA = nullptr;        // [4][tiles][128 x KP] BF16 slices of phi
+    void *d_tcB = nullptr;        // [4][NP x KP] BF16 slices of P
+    int *d_tc_rowexp = nullptr;   // [npad] per-point scale exponents
+    int *d_tc_colexp = nullptr;   // [NP] per-column scale exponents of P
+    int *d_flag = nullptr;        // device error flag (bounded waits that expired)
 
     // device: one-electron integrals output (allocated on first use)
     double *d_ints_work = nullptr;
@@ -110,6 +137,7 @@ struct dftg_ctx {
     // call-order state
     bool have_density = false;
     bool have_hartree = false;
+    bool rho_scaled = false;      // rho on the device carries the correction factor
 
     // per-phase CUDA-event timing (dftg_fock_build_profile)
     static constexpr int kMaxMarks = 24;
@@ -121,12 +149,23 @@ struct dftg_ctx {
 
 namespace dftg {
 
+// steps of the build that the mixed path runs in split / single precision
+enum {
+    kPrecDensity = 1,     // rho = 2 phi^T P phi
+    kPrecLda = 2,         // point kernel
+    kPrecMultipole = 4,   // rho_lm projection and own-cell potential
+    kPrecCross = 8,       // cross-atom potential
+    kPrecContract = 16,   // XC and J contractions
+    kPrecAll = 31,
+};
+
 // scalar slots in d_scal
 enum {
     kScalSum = 0,      // sum_p w rho (before correction)
     kScalScale = 1,    // correction factor
     kScalExc = 2,      // E_xc
     kScalNelec = 3,    // integral of corrected rho
+    kScalEJ = 4,       // E_J = 2 tr(P J) = sum_p (w V / 2) rho_raw, FP64 on the grid
     kScalAtomQ = 8,    // [natoms] per-atom integral of rho (after correction)
 };
 inline size_t scal_elems(int natoms) { return 8 + (size_t)natoms; }
@@ -140,11 +179,15 @@ int launch_grid(dftg_ctx *c);
 int launch_amplitudes(dftg_ctx *c);
 // k_density.cu
 int launch_density(dftg_ctx *c);
-int launch_atom_sums(dftg_ctx *c, bool apply_scale);
-int launch_xc_points(dftg_ctx *c);
-int launch_convert_P(dftg_ctx *c);
+enum { kSumsOnly = 0, kSumsCorrect = 1, kSumsFactor = 2 };
+// k_density_tc.cu
+int density_tc_setup(dftg_ctx *c);
+int launch_density_tc(dftg_ctx *c);
+int launch_atom_sums(dftg_ctx *c, int mode);
+int launch_xc_points(dftg_ctx *c, bool apply_scale);
 // k_hartree.cu
 int hartree_setup(dftg_ctx *c);
+size_t hartree_splf_elems(int nrad);
 int launch_hartree(dftg_ctx *c);
 // k_integrals.cu
 int launch_one_electron(dftg_ctx *c, double *dS, double *dT, double *dV);

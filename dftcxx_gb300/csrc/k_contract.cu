@@ -87,20 +87,39 @@ __global__ void __launch_bounds__(256) k_contract(int nbf, int pts_per_chunk, si
 
 // sum partials of every computed element in chunk order; mirror below the
 // diagonal blocks.  out matrices are column-major == row-major (symmetric).
-__global__ void k_contract_reduce(int nbf, int tile, int nchunk, int want_xc, int want_j,
-                                  const double *__restrict__ part, double *__restrict__ XC, double *__restrict__ J)
+// Block (32 elements x 8 chunk groups): group g sums chunks g, g+8, ... of its
+// element (coalesced over the 32 elements), the 8 group sums are added in a
+// fixed order, so the result does not depend on scheduling.
+__global__ void __launch_bounds__(256) k_contract_reduce(int nbf, int tile, int nchunk, int want_xc, int want_j,
+                                                         const double *__restrict__ part, double *__restrict__ XC,
+                                                         double *__restrict__ J)
 {
+    __shared__ double shx[8][33], shj[8][33];
     const size_t nn = (size_t)nbf * nbf;
-    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nn) return;
+    const int lx = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const size_t e = (size_t)blockIdx.x * 32 + lx;
+    double sx = 0.0, sj = 0.0;
+    if (e < nn) {
+        const int mu = (int)(e / nbf), nu = (int)(e % nbf);
+        if (mu / tile <= nu / tile)
+            for (int c = g; c < nchunk; c += 8) {
+                const double *p = part + (size_t)c * 2 * nn;
+                sx += p[e];
+                sj += p[nn + e];
+            }
+    }
+    shx[g][lx] = sx;
+    shj[g][lx] = sj;
+    __syncthreads();
+    if (g != 0 || e >= nn) return;
     const int mu = (int)(e / nbf), nu = (int)(e % nbf);
     const int tm = mu / tile, tn = nu / tile;
     if (tm > tn) return;   // written by the mirror of (nu, mu)
-    double sx = 0.0, sj = 0.0;
-    for (int c = 0; c < nchunk; ++c) {
-        const double *p = part + (size_t)c * 2 * nn;
-        sx += p[e];
-        sj += p[nn + e];
+    sx = shx[0][lx];
+    sj = shj[0][lx];
+    for (int k = 1; k < 8; ++k) {
+        sx += shx[k][lx];
+        sj += shj[k][lx];
     }
     // column-major element (row mu, col nu) sits at mu + nu*nbf
     if (want_xc) {
@@ -148,7 +167,7 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
     per = (per + kKB - 1) / kKB * kKB;
     dim3 grid((unsigned)c->ntiles, (unsigned)c->nchunk);
     const int wx = want_xc ? 1 : 0, wj = want_j ? 1 : 0;
-    if (c->precision == DFTG_PREC_FP64) {
+    if (!(c->prec_mask & kPrecContract)) {
         if (R == 5) k_contract<double, 5><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
         else k_contract<double, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
     } else {
@@ -158,8 +177,8 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "contract");
     const size_t nn = (size_t)c->nbf * c->nbf;
-    k_contract_reduce<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->nbf, tile, c->nchunk, wx, wj, c->d_part,
-                                                                          c->d_XC, c->d_J);
+    k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, tile, c->nchunk, wx, wj, c->d_part,
+                                                                        c->d_XC, c->d_J);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "contract_reduce");
     return DFTG_OK;

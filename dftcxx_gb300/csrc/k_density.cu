@@ -49,6 +49,64 @@ __global__ void __launch_bounds__(128) k_density(int nbf, size_t npad, const T *
     rho[p] = 2.0 * (double)r;
 }
 
+// Mixed path of K3.  P enters as an FP32 hi/lo pair with separate accumulators
+// (the FP32 rounding of P is common to every point and would bias the energy;
+// the roundings of phi and of the accumulation differ point by point).  Each
+// thread owns two points, so every P element read from shared memory feeds
+// four FMAs.
+__global__ void __launch_bounds__(128) k_density_split(int nbf, size_t npad, const float *__restrict__ phi,
+                                                       const double *__restrict__ P, double *__restrict__ rho)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *Ps = reinterpret_cast<float2 *>(smem_raw);   // [nbf][16] (hi, lo)
+    const size_t p0 = (size_t)blockIdx.x * 256 + threadIdx.x, p1 = p0 + 128;
+    const bool v1 = p1 < npad;
+    float rh0 = 0.f, rl0 = 0.f, rh1 = 0.f, rl1 = 0.f;
+    for (int n0 = 0; n0 < nbf; n0 += 16) {
+        const int nc = min(16, nbf - n0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < nbf * 16; e += 128) {
+            const int mu = e >> 4, j = e & 15;
+            float2 v = make_float2(0.f, 0.f);
+            if (j < nc) {
+                const double d = P[(size_t)mu * nbf + n0 + j];
+                v.x = (float)d;
+                v.y = (float)(d - (double)v.x);
+            }
+            Ps[e] = v;
+        }
+        __syncthreads();
+        float ah0[16], al0[16], ah1[16], al1[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) { ah0[j] = 0.f; al0[j] = 0.f; ah1[j] = 0.f; al1[j] = 0.f; }
+        for (int mu = 0; mu < nbf; ++mu) {
+            const float f0 = phi[(size_t)mu * npad + p0];
+            const float f1 = v1 ? phi[(size_t)mu * npad + p1] : 0.f;
+            const float2 *pr = Ps + mu * 16;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float2 q = pr[j];
+                ah0[j] = fmaf(f0, q.x, ah0[j]);
+                al0[j] = fmaf(f0, q.y, al0[j]);
+                ah1[j] = fmaf(f1, q.x, ah1[j]);
+                al1[j] = fmaf(f1, q.y, al1[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            if (j < nc) {
+                const float g0 = phi[(size_t)(n0 + j) * npad + p0];
+                const float g1 = v1 ? phi[(size_t)(n0 + j) * npad + p1] : 0.f;
+                rh0 = fmaf(ah0[j], g0, rh0);
+                rl0 = fmaf(al0[j], g0, rl0);
+                rh1 = fmaf(ah1[j], g1, rh1);
+                rl1 = fmaf(al1[j], g1, rl1);
+            }
+    }
+    rho[p0] = 2.0 * ((double)rh0 + (double)rl0);
+    if (v1) rho[p1] = 2.0 * ((double)rh1 + (double)rl1);
+}
+
 // stage 1: partial sums of w*rho over chunks that never straddle two atoms
 __global__ void k_atom_partials(size_t per_atom, int chunks_per_atom, const double *__restrict__ w,
                                 const double *__restrict__ rho, double *__restrict__ part)
@@ -82,9 +140,16 @@ __global__ void k_atom_final(int natoms, int chunks_per_atom, const double *__re
         total += q;
         charge += atoms[4 * a + 3];
     }
-    if (mode == 0) {           // before correction
+    if (mode == 0) {           // before correction; charges scaled to the corrected density
         scal[kScalSum] = total;
-        scal[kScalScale] = charge / total;
+        const double cf = charge / total;
+        scal[kScalScale] = cf;
+        double n = 0.0;
+        for (int a = 0; a < natoms; ++a) {
+            scal[kScalAtomQ + a] *= cf;
+            n += scal[kScalAtomQ + a];
+        }
+        scal[kScalNelec] = n;
     } else {                   // after correction
         scal[kScalNelec] = total;
     }
@@ -167,20 +232,75 @@ __device__ void lda_point(double rho_d, T &e, T &v)
     v = vx + vc;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, const double *__restrict__ rho,
-                                                   const double *__restrict__ w, double *__restrict__ cxc,
+// Mixed-path point kernel.  The transcendental functions run in FP32 on
+// per-point arguments (their errors differ point by point); every constant and
+// the energy density are combined in FP64, so no rounding is shared by all
+// points.  The potential (which enters the Fock matrix, not the energy) stays
+// FP32.  Constants: fac = -9/4 (2/3) (3/4pi)^(1/3); VWN paramagnetic
+// A = 0.0310907, x0 = -0.10498, b = 3.72744, c = 12.9352 (functionals.cpp:120),
+// Q = sqrt(4c - b^2), X0 = x0^2 + b x0 + c, K1 = b x0 / X0,
+// K2 = 2b/Q (1 - x0 (2 x0 + b) / X0).
+__device__ void lda_point_mixed(double rho, double &e, float &v)
+{
+    constexpr double FAC = -0.93052573634910019, K34PI = 0.238732414637843;
+    constexpr double A = 0.0310907, K1 = -0.031167608678943783, K2 = 1.2474243062431216;
+    constexpr float Af = 0.0310907f, X0f = -0.10498f, Bf = 3.72744f, Cf = 12.9352f, Qf = 6.1519908197590798f,
+                    Q2f = 37.846991046399992f, K1f = -0.031167608678943783f, VXf = -1.2407009817988002f;
+    const double da = rho * 0.5;
+    double ex = 0.0;
+    float vx = 0.f;
+    if (!(da < 1e-10)) {
+        const float r3 = cbrtf((float)da);
+        ex = 2.0 * (FAC * da) * (double)r3;
+        vx = VXf * r3;
+    }
+    double ec = 0.0;
+    float vc = 0.f;
+    if (!(rho < 1e-10)) {
+        const float x = sqrtf(cbrtf((float)(K34PI / rho)));
+        const float X = fmaf(x, x + Bf, Cf);
+        const float L1 = logf(x * x / X);
+        const float L2 = logf((x - X0f) * (x - X0f) / X);
+        const float tb = 2.f * x + Bf;
+        const float T = atanf(Qf / tb);
+        const double eps = A * ((double)L1 - K1 * (double)L2 + K2 * (double)T);
+        ec = eps * rho;
+        const float den = tb * tb + Q2f;
+        const float deps = Af * (2.f / x - tb / X - 4.f * Bf / den -
+                                 K1f * (2.f / (x - X0f) - tb / X - 4.f * (2.f * X0f + Bf) / den));
+        vc = (float)eps - (x / 6.f) * deps;
+    }
+    e = ex + ec;
+    v = vx + vc;
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restrict__ rho,
+                                                   const double *__restrict__ w, const double *__restrict__ scal,
+                                                   int apply_scale, double *__restrict__ cxc,
                                                    float *__restrict__ cxc32, double *__restrict__ part)
 {
     __shared__ double sh[kRedBlock];
     const size_t p = (size_t)blockIdx.x * kRedBlock + threadIdx.x;
     double ew = 0.0;
     if (p < npad) {
-        T e, v;
-        lda_point<T>(rho[p], e, v);
+        double r = rho[p];
+        if (apply_scale) {        // density correction fused into the point kernel
+            r *= scal[kScalScale];
+            rho[p] = r;
+        }
+        double e;
+        double vd;
+        if (MIXED) {
+            float v;
+            lda_point_mixed(r, e, v);
+            vd = (double)v;
+        } else {
+            lda_point<double>(r, e, vd);
+        }
         const double wp = w[p];
-        ew = wp * (double)e;
-        const double c = wp * (double)v;
+        ew = wp * e;
+        const double c = wp * vd;
         cxc[p] = c;
         cxc32[p] = (float)c;
     }
@@ -207,51 +327,41 @@ __global__ void k_sum_to_scalar(int n, const double *__restrict__ part, double *
     if (threadIdx.x == 0) scal[slot] = sh[0];
 }
 
-__global__ void k_convert_P(int n, const double *__restrict__ P, float *__restrict__ P32)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) P32[i] = (float)P[i];
-}
-
 // ---------------------------------------------------------------- launchers
-
-int launch_convert_P(dftg_ctx *c)
-{
-    const int n = c->nbf * c->nbf;
-    k_convert_P<<<(n + 255) / 256, 256, 0, c->stream>>>(n, c->d_P, c->d_P32);
-    DFTG_LAUNCH_CHECK();
-    DFTG_MARK(c, "convert_P");
-    return DFTG_OK;
-}
 
 int launch_density(dftg_ctx *c)
 {
-    const unsigned nb = (unsigned)(c->npad / 128);
-    if (c->precision == DFTG_PREC_FP64) {
+    if (!(c->prec_mask & kPrecDensity)) {
+        const unsigned nb = (unsigned)(c->npad / 128);
         const size_t sm = (size_t)c->nbf * 32 * sizeof(double);
         if (sm > 48 * 1024) DFTG_CUDA(cudaFuncSetAttribute(k_density<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         k_density<double><<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi, c->d_P, c->d_rho);
+    } else if (c->tc_ready) {
+        DFTG_TRY_L(launch_density_tc(c));
     } else {
-        const size_t sm = (size_t)c->nbf * 32 * sizeof(float);
-        if (sm > 48 * 1024) DFTG_CUDA(cudaFuncSetAttribute(k_density<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_density<float><<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi32, c->d_P32, c->d_rho);
+        const unsigned nb = (unsigned)((c->npad + 255) / 256);
+        const size_t sm = (size_t)c->nbf * 16 * sizeof(float2);
+        if (sm > 48 * 1024) DFTG_CUDA(cudaFuncSetAttribute(k_density_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_density_split<<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi32, c->d_P, c->d_rho);
     }
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "density");
     return DFTG_OK;
 }
 
-// apply_scale: compute c and rescale rho, then recompute the per-atom charges
-int launch_atom_sums(dftg_ctx *c, bool apply_scale)
+// kSumsOnly: per-atom charges of the current rho.  kSumsCorrect: correction
+// factor, rho rescaled, charges recomputed (correct_densities).  kSumsFactor:
+// correction factor and rescaled charges only; the LDA kernel rescales rho.
+int launch_atom_sums(dftg_ctx *c, int mode)
 {
     const size_t per_atom = (size_t)c->nrad * c->nang;
     const int cpa = (int)((per_atom + kRedChunk - 1) / kRedChunk);
     const int nb = cpa * c->natoms;
     k_atom_partials<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, c->d_w, c->d_rho, c->d_red);
     DFTG_LAUNCH_CHECK();
-    k_atom_final<<<1, 32, 0, c->stream>>>(c->natoms, cpa, c->d_red, c->d_atoms, c->d_scal, apply_scale ? 0 : 1);
+    k_atom_final<<<1, 32, 0, c->stream>>>(c->natoms, cpa, c->d_red, c->d_atoms, c->d_scal, mode == kSumsOnly ? 1 : 0);
     DFTG_LAUNCH_CHECK();
-    if (apply_scale) {
+    if (mode == kSumsCorrect) {
         k_scale<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, c->d_scal, c->d_rho);
         DFTG_LAUNCH_CHECK();
         k_atom_partials<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, c->d_w, c->d_rho, c->d_red);
@@ -263,13 +373,16 @@ int launch_atom_sums(dftg_ctx *c, bool apply_scale)
     return DFTG_OK;
 }
 
-int launch_xc_points(dftg_ctx *c)
+int launch_xc_points(dftg_ctx *c, bool apply_scale)
 {
     const unsigned nb = (unsigned)((c->npad + kRedBlock - 1) / kRedBlock);
-    if (c->precision == DFTG_PREC_FP64)
-        k_lda<double><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_cxc, c->d_cxc32, c->d_red);
+    const int sc = apply_scale ? 1 : 0;
+    if (c->prec_mask & kPrecLda)
+        k_lda<true><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_scal, sc, c->d_cxc, c->d_cxc32,
+                                                     c->d_red);
     else
-        k_lda<float><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_cxc, c->d_cxc32, c->d_red);
+        k_lda<false><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_scal, sc, c->d_cxc,
+                                                      c->d_cxc32, c->d_red);
     DFTG_LAUNCH_CHECK();
     k_sum_to_scalar<<<1, kRedBlock, 0, c->stream>>>((int)nb, c->d_red, c->d_scal, kScalExc);
     DFTG_LAUNCH_CHECK();

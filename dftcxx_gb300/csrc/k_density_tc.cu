@@ -1,0 +1,416 @@
+// k_density_tc.cu -- mixed-path density rho_p = 2 phi_p^T P phi_p on the tcgen05
+// tensor cores, accurate to ~1e-10 relative (gridpoint.cpp:82-84).
+//
+// The energy depends on rho at first order, so rho must carry near-FP64
+// accuracy; FP32 or 3xTF32 arithmetic leaves ~1e-7 random errors per point,
+// about 3e-6 Ha on benzene.  The GEMM T = Phi P is therefore done as an exact
+// integer-slice product (Ozaki's error-free splitting) on the BF16 tensor cores:
+//
+//   Phi[p, mu] = 2^e_p  sum_{i=1..4} A_i[p, mu] 2^(-8 i)      (per point e_p)
+//   P[mu, nu]  = 2^t_nu sum_{j=1..4} B_j[mu, nu] 2^(-8 j)     (per column t_nu)
+//
+// with integer slices |A_1|, |B_1| <= 256 and |A_i|, |B_j| <= 128 (exact in
+// BF16).  Each slice product summed over mu <= 80 stays below 2^24, so the
+// FP32 accumulation in TMEM is exact; the 10 pairs with i + j <= 5 go to four
+// accumulators, one per level L = i + j (weight 2^(-8 L)).  The dropped levels
+// are below 2^-40 of the row/column scales.  The epilogue combines the levels
+// with TwoSum into an FP32 pair and forms rho = 2 sum_nu T_nu phi_nu in
+// compensated FP32, phi rebuilt exactly from the slices in shared memory.
+//
+// Layouts (canonical no-swizzle K-major core matrices, 8 rows x 16 bytes):
+//   A slices in HBM: [slice][tile][128/8][KP/8][8][8] BF16, one contiguous
+//     128 x KP block per slice and tile, copied with cp.async.bulk;
+//   B slices: [slice][NP/8][KP/8][8][8] BF16 (rows nu, K = mu).
+// CTA: warp 0 producer (bulk copies), warp 1 TMEM owner + MMA issuer,
+// warps 2-5 epilogue (TMEM lanes 32 (w % 4) ...).  Persistent over tiles, two
+// A stages.  Every mbarrier wait is bounded: on expiry the CTA records an error
+// code, drains its copies, frees TMEM and exits.
+#include <cuda_bf16.h>
+#include <cstdint>
+#include "dftg_internal.cuh"
+
+namespace dftg {
+
+constexpr int kTcSlices = 4;
+constexpr int kTcTile = 128;
+constexpr int kTcMaxK = 80;                   // nbf <= 80 for this kernel
+constexpr int kTcThreads = 192;
+constexpr uint32_t kTcTmemCols = 512;
+constexpr unsigned long long kWaitLimit = 1ull << 27;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// bounded wait for the phase of the given parity; false on expiry
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    const uint32_t a = smem_u32(bar);
+    for (unsigned long long it = 0; it < kWaitLimit; ++it) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(a), "r"(parity)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// shared-memory matrix descriptor, no swizzle, K-major core matrices
+__device__ __forceinline__ uint64_t smem_desc(const void *base, uint32_t lbo, uint32_t sbo)
+{
+    const uint64_t a = (uint64_t)((smem_u32(base) >> 4) & 0x3FFF);
+    return a | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+// instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                 "l"(a), "l"(b), "r"(idesc), "r"(acc)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void epi_bar_sync()   // named barrier of the 4 epilogue warps
+{
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+}
+
+// byte offset of element (row, k) inside a K-major no-swizzle block whose K
+// extent holds `kcores` core matrices: cores ordered row group by row group,
+// so LBO (next core along K) = 128 B and SBO (next row group) = kcores * 128 B;
+// every address the MMA forms stays inside the block
+__host__ __device__ __forceinline__ uint32_t core_off(int row, int k, int kcores)
+{
+    return (uint32_t)(((row >> 3) * kcores + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+struct TcShared {
+    uint64_t full[2], empty[2], tmem_full, tmem_empty;
+    uint32_t tmem_base;
+};
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restrict__ Aslices,
+             const int *__restrict__ row_exp, const unsigned char *__restrict__ Bslices,
+             const int *__restrict__ col_exp, double *__restrict__ rho, int *__restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const uint32_t a_slice_bytes = (uint32_t)kTcTile * KP * 2;
+    const uint32_t a_stage_bytes = kTcSlices * a_slice_bytes;
+    const uint32_t b_slice_bytes = (uint32_t)NP * KP * 2;
+    unsigned char *sA = smem;                                   // [2][slices][tile block]
+    unsigned char *sB = smem + 2 * a_stage_bytes;                // [slices][B block]
+    TcShared *sh = reinterpret_cast<TcShared *>(sB + kTcSlices * b_slice_bytes);
+    __shared__ int s_texp[kTcMaxK];
+    __shared__ int s_fail;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        mbar_init(&sh->full[0], 1);
+        mbar_init(&sh->full[1], 1);
+        mbar_init(&sh->empty[0], 1);
+        mbar_init(&sh->empty[1], 1);
+        mbar_init(&sh->tmem_full, 1);
+        mbar_init(&sh->tmem_empty, 1);
+        s_fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // B slices and column exponents: plain copies, then made visible to the tensor core
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(Bslices);
+        uint4 *dst = reinterpret_cast<uint4 *>(sB);
+        const int n16 = (int)(kTcSlices * b_slice_bytes / 16);
+        for (int i = threadIdx.x; i < n16; i += kTcThreads) dst[i] = src[i];
+        for (int i = threadIdx.x; i < NP && i < kTcMaxK; i += kTcThreads) s_texp[i] = i < nbf ? col_exp[i] : 0;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem_base)),
+                     "r"(kTcTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sh->tmem_base;
+    const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+
+    if (warp == 0) {
+        // ------------------------------------------------------------ producer
+        int issued = 0;
+        if (lane == 0) {
+            for (int it = 0; it < my_tiles; ++it) {
+                const int s = it & 1, n = it >> 1;
+                if (!mbar_wait(&sh->empty[s], (uint32_t)((n & 1) ^ 1))) { atomicExch(err, 1); s_fail = 1; break; }
+                if (s_fail) break;
+                const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+                mbar_arrive_expect_tx(&sh->full[s], a_stage_bytes);
+                for (int i = 0; i < kTcSlices; ++i)
+                    bulk_g2s(sA + (size_t)s * a_stage_bytes + (size_t)i * a_slice_bytes,
+                             Aslices + ((size_t)i * ntiles + tile) * a_slice_bytes, a_slice_bytes, &sh->full[s]);
+                issued = it + 1;
+            }
+            // drain: every issued stage must have landed before the CTA exits
+            for (int it = (issued > 2 ? issued - 2 : 0); it < issued; ++it)
+                mbar_wait(&sh->full[it & 1], (uint32_t)((it >> 1) & 1));
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ------------------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(kTcTile, NP);
+            const uint32_t lbo = 128, sbo = (uint32_t)(KP / 8) * 128;
+            for (int it = 0; it < my_tiles; ++it) {
+                const int s = it & 1, n = it >> 1;
+                if (!mbar_wait(&sh->full[s], (uint32_t)(n & 1))) { atomicExch(err, 2); s_fail = 1; break; }
+                if (!mbar_wait(&sh->tmem_empty, (uint32_t)((it & 1) ^ 1))) { atomicExch(err, 3); s_fail = 1; break; }
+                if (s_fail) break;
+                tc_fence_after();
+                const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
+                for (int L = 2; L <= 5; ++L) {
+                    const uint32_t d = tmem + (uint32_t)((L - 2) * 128);
+                    int first = 1;
+                    for (int i = 1; i <= 4; ++i) {
+                        const int j = L - i;
+                        if (j < 1 || j > 4) continue;
+                        const unsigned char *ai = a0 + (size_t)(i - 1) * a_slice_bytes;
+                        const unsigned char *bj = sB + (size_t)(j - 1) * b_slice_bytes;
+                        for (int kk = 0; kk < KP / 16; ++kk) {
+                            const uint64_t ad = smem_desc(ai + (size_t)kk * 2 * lbo, lbo, sbo);
+                            const uint64_t bd = smem_desc(bj + (size_t)kk * 2 * lbo, lbo, sbo);
+                            mma_bf16(d, ad, bd, idesc, first ? 0u : 1u);
+                            first = 0;
+                        }
+                    }
+                }
+                mma_commit(&sh->tmem_full);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ------------------------------------------------------------ epilogue
+        const int q = warp & 3;                 // TMEM lane quarter of this warp
+        const int r = q * 32 + lane;            // row of the tile = TMEM lane
+        for (int it = 0; it < my_tiles; ++it) {
+            const int s = it & 1;
+            bool ok = mbar_wait(&sh->tmem_full, (uint32_t)(it & 1));
+            if (!ok) { atomicExch(err, 4); s_fail = 1; }
+            epi_bar_sync();
+            if (s_fail) break;
+            tc_fence_after();
+            const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+            const size_t p = (size_t)tile * kTcTile + r;
+            const int ep = row_exp[p];
+            const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
+            float S = 0.f, E = 0.f;
+            for (int c0 = 0; c0 < NP; c0 += 16) {
+                float d2[16], d3[16], d4[16], d5[16];
+                const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+                tmem_ld16(ta, d2);
+                tmem_ld16(ta + 128u, d3);
+                tmem_ld16(ta + 256u, d4);
+                tmem_ld16(ta + 384u, d5);
+                tmem_wait_ld();
+#pragma unroll
+                for (int k = 0; k < 16; ++k) {
+                    const int nu = c0 + k;
+                    if (nu >= nbf) continue;
+                    // T~_nu = sum_L D_L 2^(-8L): exact head via TwoSum, small tail
+                    float t = d2[k] * 0x1p-16f;
+                    const float x3 = d3[k] * 0x1p-24f;
+                    const float u = t + x3;
+                    const float bp = u - t;
+                    float te = (t - (u - bp)) + (x3 - bp);
+                    t = u;
+                    te += d4[k] * 0x1p-32f + d5[k] * 0x1p-40f;
+                    const float sc = __int_as_float((127 + s_texp[nu]) << 23);
+                    t *= sc;
+                    te *= sc;
+                    // phi~ from the slices of this row (exact FP32 pair)
+                    const uint32_t off = core_off(r, nu, KP / 8);
+                    const float m1 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + off));
+                    const float m2 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + a_slice_bytes + off));
+                    const float m3 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + 2 * a_slice_bytes + off));
+                    const float m4 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + 3 * a_slice_bytes + off));
+                    const float fh = fmaf(m2, 0x1p-16f, m1 * 0x1p-8f);
+                    const float fl = fmaf(m4, 0x1p-32f, m3 * 0x1p-24f);
+                    // S + E += (t + te)(fh + fl)
+                    const float pr = t * fh;
+                    const float pe = fmaf(t, fh, -pr);
+                    const float w = S + pr;
+                    const float bq = w - S;
+                    E += (S - (w - bq)) + (pr - bq) + pe + fmaf(t, fl, te * fh);
+                    S = w;
+                }
+            }
+            tc_fence_before();
+            epi_bar_sync();                      // all TMEM reads and A-stage reads of this tile are done
+            if (threadIdx.x == 64) {
+                mbar_arrive(&sh->tmem_empty);
+                mbar_arrive(&sh->empty[s]);
+            }
+            rho[p] = 2.0 * ((double)S + (double)E) * ldexp(1.0, 2 * ep);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
+    }
+}
+
+// ------------------------------------------------------------------ slicing
+
+// Phi (FP64, [nbf][npad]) -> 4 integer slices per element in the tile layout
+__global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const double *__restrict__ phi,
+                            __nv_bfloat16 *__restrict__ A, int *__restrict__ row_exp)
+{
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npad) return;
+    double mx = 0.0;
+    for (int mu = 0; mu < nbf; ++mu) mx = fmax(mx, fabs(phi[(size_t)mu * npad + p]));
+    int e = 0;
+    if (mx > 0.0) frexp(mx, &e);                 // mx < 2^e
+    row_exp[p] = e;
+    const int tile = (int)(p / kTcTile), r = (int)(p % kTcTile);
+    const size_t slice = (size_t)ntiles * kTcTile * KP;
+    for (int mu = 0; mu < KP; ++mu) {
+        double x = mu < nbf ? ldexp(phi[(size_t)mu * npad + p], -e) : 0.0;
+        const size_t o = (size_t)tile * kTcTile * KP + core_off(r, mu, KP / 8) / 2;
+        for (int i = 0; i < kTcSlices; ++i) {
+            x *= 256.0;
+            const double m = rint(x);
+            x -= m;
+            A[(size_t)i * slice + o] = __float2bfloat16_rn((float)m);
+        }
+    }
+}
+
+// P (FP64, nbf x nbf, symmetric) -> 4 integer slices per column in the B layout
+__global__ void k_slice_P(int nbf, int KP, int NP, const double *__restrict__ P, __nv_bfloat16 *__restrict__ B,
+                          int *__restrict__ col_exp)
+{
+    const int nu = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nu >= NP) return;
+    double mx = 0.0;
+    if (nu < nbf)
+        for (int mu = 0; mu < nbf; ++mu) mx = fmax(mx, fabs(P[(size_t)nu * nbf + mu]));
+    int e = 0;
+    if (mx > 0.0) frexp(mx, &e);
+    if (nu < nbf) col_exp[nu] = e;
+    const size_t slice = (size_t)NP * KP;
+    for (int mu = 0; mu < KP; ++mu) {
+        double x = (nu < nbf && mu < nbf) ? ldexp(P[(size_t)nu * nbf + mu], -e) : 0.0;
+        const size_t o = core_off(nu, mu, KP / 8) / 2;
+        for (int i = 0; i < kTcSlices; ++i) {
+            x *= 256.0;
+            const double m = rint(x);
+            x -= m;
+            B[(size_t)i * slice + o] = __float2bfloat16_rn((float)m);
+        }
+    }
+}
+
+size_t density_tc_smem(int KP, int NP)
+{
+    return 2 * (size_t)kTcSlices * kTcTile * KP * 2 + (size_t)kTcSlices * NP * KP * 2 + sizeof(TcShared) + 64;
+}
+
+bool density_tc_supported(int nbf) { return nbf <= kTcMaxK; }
+
+int density_tc_setup(dftg_ctx *c)
+{
+    if (!density_tc_supported(c->nbf)) return DFTG_OK;
+    c->tc_KP = (c->nbf + 15) / 16 * 16;
+    c->tc_NP = c->tc_KP;
+    const int ntiles = (int)(c->npad / kTcTile);
+    const size_t aslice = (size_t)ntiles * kTcTile * c->tc_KP;
+    DFTG_CUDA(cudaMalloc(&c->d_tcA, sizeof(__nv_bfloat16) * kTcSlices * aslice));
+    DFTG_CUDA(cudaMalloc(&c->d_tc_rowexp, sizeof(int) * c->npad));
+    DFTG_CUDA(cudaMalloc(&c->d_tcB, sizeof(__nv_bfloat16) * kTcSlices * c->tc_NP * c->tc_KP));
+    DFTG_CUDA(cudaMalloc(&c->d_tc_colexp, sizeof(int) * c->tc_NP));
+    DFTG_CUDA(cudaMalloc(&c->d_flag, sizeof(int)));
+    DFTG_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
+    k_slice_phi<<<(unsigned)((c->npad + 127) / 128), 128, 0, c->stream>>>(
+        c->nbf, c->tc_KP, c->npad, ntiles, c->d_phi, reinterpret_cast<__nv_bfloat16 *>(c->d_tcA), c->d_tc_rowexp);
+    DFTG_LAUNCH_CHECK();
+    const size_t sm = density_tc_smem(c->tc_KP, c->tc_NP);
+    DFTG_CUDA(cudaFuncSetAttribute(k_density_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    int nsm = 0;
+    DFTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+    c->tc_grid = nsm < ntiles ? nsm : ntiles;
+    c->tc_ready = true;
+    return DFTG_OK;
+}
+
+int launch_density_tc(dftg_ctx *c)
+{
+    k_slice_P<<<1, 128, 0, c->stream>>>(c->nbf, c->tc_KP, c->tc_NP, c->d_P,
+                                        reinterpret_cast<__nv_bfloat16 *>(c->d_tcB), c->d_tc_colexp);
+    DFTG_LAUNCH_CHECK();
+    const int ntiles = (int)(c->npad / kTcTile);
+    k_density_tc<<<c->tc_grid, kTcThreads, density_tc_smem(c->tc_KP, c->tc_NP), c->stream>>>(
+        c->nbf, c->tc_KP, c->tc_NP, ntiles, reinterpret_cast<const unsigned char *>(c->d_tcA), c->d_tc_rowexp,
+        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+}  // namespace dftg

@@ -5,18 +5,24 @@
 // K5a rho_lm[a][lm][i] = 4 pi sum_j rho w_becke w_leb,j Y_lm(dir_j): one CTA per
 //     (atom, radial shell); Y_lm of the Lebedev directions precomputed once.
 // K5b radial Poisson solve per (atom, lm): the finite-difference operator
-//     depends only on (nrad, l), so it is LU-factored once per l on the host
-//     (partial pivoting, same elimination order as the reference's dense LU)
-//     and every right-hand side is swept on the device.
+//     depends only on (nrad, l), so its solution map is built once per grid
+//     (columns of the inverse from a partial-pivot LU, as the reference's dense
+//     LU) and applied on the device as a matrix-vector product per (atom, lm):
+//     no sequential sweeps on the slow FP64 pipe.
 // K5c own-cell potential V_n(p) = sum_lm U_lm(r_i) / r Y_lm (atomicgrid.cpp:439-462).
-// K5d cubic splines of U_lm over increasing r (cspline.cpp:66-142), one thread
-//     per (atom, lm), stored [atom][lm][interval][4] (interval nrad-1 holds the
-//     clamp value of the last knot).
+// K5d cubic splines of U_lm over increasing r (cspline.cpp:66-142): the
+//     derivatives are a fixed linear map of the ordinates (the tridiagonal
+//     system depends on the abscissae only), applied per (atom, lm).  Stored
+//     [atom][lm][interval][4] (interval nrad-1 holds the clamp value of the
+//     last knot).
 // K5e cross-atom potential: for every point and every other atom k,
 //     sum_lm U^k_lm(r)/r Y_lm with Y_lm by Cartesian recursion (no atan2/acos)
 //     and an O(1) spline-interval lookup from the analytic radial map
 //     r = (1+x)/(1-x), x = cos(pi p/(N+1)) (moleculargrid.cpp:342-380).
-//     T = double (FP64 path) or float (mixed path); V accumulates in FP64.
+//     FP64 path, or the mixed path: FP32 arithmetic per point with every
+//     constant shared by many points carried as a split FP32 pair.
+// Mixed path of K5a/K5c: split-FP32 products (hi*hi + hi*lo + lo*hi), FP32
+//     partial sums of 16 terms added in FP64.
 #include <cmath>
 #include <vector>
 #include "dftg_internal.cuh"
@@ -119,6 +125,56 @@ static void poisson_matrix(int N, const double *r_n, double *A)
 
 // in-place LU with partial pivoting: multipliers below the diagonal, U above,
 // piv[k] = row exchanged with k at step k
+static void lu_factor(int S, double *M, int *piv);
+
+// solve M x = b with the factors of lu_factor: row interchanges first (the rows
+// were exchanged whole), then the unit-lower and upper sweeps
+static void lu_apply(int S, const double *F, const int *piv, double *b)
+{
+    for (int k = 0; k < S; ++k)
+        if (piv[k] != k) std::swap(b[k], b[piv[k]]);
+    for (int i = 1; i < S; ++i) {
+        double s = b[i];
+        for (int k = 0; k < i; ++k) s -= F[(size_t)i * S + k] * b[k];
+        b[i] = s;
+    }
+    for (int i = S - 1; i >= 0; --i) {
+        double s = b[i];
+        for (int j = i + 1; j < S; ++j) s -= F[(size_t)i * S + j] * b[j];
+        b[i] = s / F[(size_t)i * S + i];
+    }
+}
+
+// spline derivatives D of cspline.cpp:66-130 (x increasing, n >= 3)
+static void spline_derivatives(int n, const double *x, const double *y, double *D)
+{
+    std::vector<double> A(n, 0.0), B(n, 0.0), C(n, 0.0), Y(n, 0.0);
+    double h0 = x[1] - x[0], h1 = x[2] - x[1];
+    double r0 = (y[1] - y[0]) / h0, r1 = (y[2] - y[1]) / h1;
+    B[0] = h1 * (h0 + h1);
+    C[0] = (h0 + h1) * (h0 + h1);
+    Y[0] = r0 * (3 * h0 * h1 + 2 * h1 * h1) + r1 * h0 * h0;
+    for (int i = 1; i < n - 1; ++i) {
+        h0 = x[i] - x[i - 1];
+        h1 = x[i + 1] - x[i];
+        r0 = (y[i] - y[i - 1]) / h0;
+        r1 = (y[i + 1] - y[i]) / h1;
+        A[i] = h1;
+        B[i] = 2 * (h0 + h1);
+        C[i] = h0;
+        Y[i] = 3 * (r0 * h1 + r1 * h0);
+    }
+    A[n - 1] = (h0 + h1) * (h0 + h1);
+    B[n - 1] = h0 * (h0 + h1);
+    Y[n - 1] = r0 * h1 * h1 + r1 * (3 * h0 * h1 + 2 * h0 * h0);
+    C[0] = C[0] / B[0];
+    for (int i = 1; i < n - 1; ++i) C[i] = C[i] / (B[i] - A[i] * C[i - 1]);
+    Y[0] = Y[0] / B[0];
+    for (int i = 1; i < n; ++i) Y[i] = (Y[i] - A[i] * Y[i - 1]) / (B[i] - A[i] * C[i - 1]);
+    D[n - 1] = Y[n - 1];
+    for (int i = n - 1; i > 0; --i) D[i - 1] = Y[i - 1] - C[i - 1] * D[i];
+}
+
 static void lu_factor(int S, double *M, int *piv)
 {
     for (int k = 0; k < S; ++k) {
@@ -141,31 +197,75 @@ static void lu_factor(int S, double *M, int *piv)
     }
 }
 
+static double dfact_h(int n) { double r = 1.0; for (int k = n; k > 1; k -= 2) r *= k; return r; }
+
+// spline factor layout: inv_h, h, A, C', 1/den (each nrad) and 4 end-row constants
+size_t hartree_splf_elems(int nrad) { return (size_t)5 * nrad + 4; }
+
+static void split_f32(double v, float &hi, float &lo)
+{
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
 int hartree_setup(dftg_ctx *c)
 {
     const int nang = c->nang, nlm = c->nlm, N = c->nrad, S = N + 2;
-    std::vector<double> Y((size_t)nlm * nang), Yw((size_t)nlm * nang), pre(nlm);
+    std::vector<double> Y((size_t)nlm * nang), Yw((size_t)nlm * nang), pre(nlm), fold(nlm);
+    std::vector<float> Y32(2 * (size_t)nlm * nang), Ywt32(2 * (size_t)nlm * nang);
     std::vector<double> leb((size_t)nang * 4);
     DFTG_CUDA(cudaMemcpy(leb.data(), c->d_leb, sizeof(double) * nang * 4, cudaMemcpyDeviceToHost));
+    const size_t half = (size_t)nlm * nang;
     for (int l = 0; l <= c->lmax; ++l)
         for (int m = -l; m <= l; ++m) {
-            int lm = l * l + l + m;
+            const int lm = l * l + l + m, am = m < 0 ? -m : m;
             pre[lm] = sh_prefactor(l, m);
+            // Y_lm = fold_lm * R_l^|m|(z) * {Re, Im}((x + i y)^|m|) with the integer recursion
+            // R_l = (2l-1) z R_{l-1} - (l+m-1)(l-m-1) R_{l-2}, R_m = 1
+            fold[lm] = pre[lm] * ((am & 1) ? -1.0 : 1.0) * dfact_h(2 * am - 1) / fact(l - am);
             for (int j = 0; j < nang; ++j) {
-                double y = ylm_host(l, m, leb[4 * j], leb[4 * j + 1], leb[4 * j + 2]);
+                const double y = ylm_host(l, m, leb[4 * j], leb[4 * j + 1], leb[4 * j + 2]);
+                const double yw = y * leb[4 * j + 3];
                 Y[(size_t)lm * nang + j] = y;
-                Yw[(size_t)lm * nang + j] = y * leb[4 * j + 3];
+                Yw[(size_t)lm * nang + j] = yw;
+                split_f32(y, Y32[(size_t)lm * nang + j], Y32[half + (size_t)lm * nang + j]);
+                split_f32(yw, Ywt32[(size_t)j * nlm + lm], Ywt32[half + (size_t)j * nlm + lm]);
             }
         }
-    std::vector<double> A((size_t)S * S), LU((size_t)(c->lmax + 1) * S * S);
-    std::vector<int> piv((size_t)(c->lmax + 1) * S);
+    // Radial Poisson operator per l (atomicgrid.cpp:316-425) as an explicit
+    // linear map: U[i] = sum_k Gt[l][k][i] rho_lm[k] + [lm = 0] Gb[i] q_a, from
+    // the columns of the inverse obtained with the partial-pivot LU factors.
+    std::vector<double> A((size_t)S * S), M((size_t)S * S), e(S);
+    std::vector<int> piv(S);
+    std::vector<double> Gt((size_t)(c->lmax + 1) * N * N), Gb(N);
     poisson_matrix(N, c->r_n.data(), A.data());
     for (int l = 0; l <= c->lmax; ++l) {
-        double *M = LU.data() + (size_t)l * S * S;
-        for (size_t t = 0; t < (size_t)S * S; ++t) M[t] = A[t];
+        M = A;
         for (int i = 1; i < N + 1; ++i)
             M[(size_t)i * S + i] -= (double)l * (double)(l + 1) / (c->r_n[i - 1] * c->r_n[i - 1]);
-        lu_factor(S, M, piv.data() + (size_t)l * S);
+        lu_factor(S, M.data(), piv.data());
+        for (int k = 0; k <= N; ++k) {      // column k of the inverse
+            for (int i = 0; i < S; ++i) e[i] = (i == k) ? 1.0 : 0.0;
+            lu_apply(S, M.data(), piv.data(), e.data());
+            for (int i = 1; i < N + 1; ++i) {
+                if (k == 0) {
+                    if (l == 0) Gb[i - 1] = std::sqrt(4.0 * kPi) * e[i];
+                } else {
+                    Gt[((size_t)l * N + (k - 1)) * N + (i - 1)] = -4.0 * kPi * c->r_n[k - 1] * e[i];
+                }
+            }
+        }
+    }
+    // spline derivatives as a linear map of the ordinates: D = K y (cspline.cpp:66-130)
+    std::vector<double> Kt((size_t)N * N);
+    {
+        std::vector<double> sxv(N), yv(N), D(N);
+        for (int i = 0; i < N; ++i) sxv[i] = c->r_n[N - 1 - i];
+        for (int j = 0; j < N; ++j) {
+            for (int i = 0; i < N; ++i) yv[i] = (i == j) ? 1.0 : 0.0;
+            spline_derivatives(N, sxv.data(), yv.data(), D.data());
+            for (int i = 0; i < N; ++i) Kt[(size_t)j * N + i] = D[i];
+        }
     }
     std::vector<double> rec((size_t)2 * nlm, 0.0);
     for (int l = 0; l <= c->lmax; ++l)
@@ -173,24 +273,54 @@ int hartree_setup(dftg_ctx *c)
             rec[2 * (l * l + l + m)] = (double)(2 * l - 1) / (double)(l - m);
             rec[2 * (l * l + l + m) + 1] = (double)(l + m - 1) / (double)(l - m);
         }
-    std::vector<float> pre32(pre.begin(), pre.end()), rec32(rec.begin(), rec.end());
-    DFTG_CUDA(cudaMemcpy(c->d_rec, rec.data(), sizeof(double) * rec.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_rec32, rec32.data(), sizeof(float) * rec32.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_pre32, pre32.data(), sizeof(float) * pre32.size(), cudaMemcpyHostToDevice));
-    std::vector<double> sx(N);
+    // spline factorisation: the tridiagonal matrix of cspline.cpp:83-118 depends on x only
+    std::vector<double> sx(N), f(hartree_splf_elems(N), 0.0);
     for (int i = 0; i < N; ++i) sx[i] = c->r_n[N - 1 - i];
+    double *inv_h = f.data(), *h = inv_h + N, *Aa = h + N, *Cp = Aa + N, *inv_den = Cp + N, *k4 = inv_den + N;
+    for (int i = 0; i < N - 1; ++i) { h[i] = sx[i + 1] - sx[i]; inv_h[i] = 1.0 / h[i]; }
+    {
+        const double h0 = h[0], h1 = h[1];
+        const double B0 = h1 * (h0 + h1);
+        Cp[0] = (h0 + h1) * (h0 + h1) / B0;
+        inv_den[0] = 1.0 / B0;
+        k4[0] = 3 * h0 * h1 + 2 * h1 * h1;   // Y_0 = r_0 k4[0] + r_1 k4[1]
+        k4[1] = h0 * h0;
+        for (int i = 1; i < N - 1; ++i) {
+            Aa[i] = h[i];
+            const double den = 2 * (h[i - 1] + h[i]) - Aa[i] * Cp[i - 1];
+            Cp[i] = h[i - 1] / den;
+            inv_den[i] = 1.0 / den;
+        }
+        const double g0 = h[N - 3], g1 = h[N - 2];
+        Aa[N - 1] = (g0 + g1) * (g0 + g1);
+        inv_den[N - 1] = 1.0 / (g0 * (g0 + g1) - Aa[N - 1] * Cp[N - 2]);
+        k4[2] = g1 * g1;                      // Y_{n-1} = r_{n-3} k4[2] + r_{n-2} k4[3]
+        k4[3] = 3 * g0 * g1 + 2 * g0 * g0;
+    }
+    std::vector<float> pre32(pre.begin(), pre.end()), rec32(rec.begin(), rec.end());
+    DFTG_CUDA(cudaMalloc(&c->d_Gt, sizeof(double) * Gt.size()));
+    DFTG_CUDA(cudaMalloc(&c->d_Gb, sizeof(double) * Gb.size()));
+    DFTG_CUDA(cudaMalloc(&c->d_Kt, sizeof(double) * Kt.size()));
+    DFTG_CUDA(cudaMemcpy(c->d_Gt, Gt.data(), sizeof(double) * Gt.size(), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_Gb, Gb.data(), sizeof(double) * Gb.size(), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_Kt, Kt.data(), sizeof(double) * Kt.size(), cudaMemcpyHostToDevice));
     DFTG_CUDA(cudaMemcpy(c->d_Y, Y.data(), sizeof(double) * Y.size(), cudaMemcpyHostToDevice));
     DFTG_CUDA(cudaMemcpy(c->d_Yw, Yw.data(), sizeof(double) * Yw.size(), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_Y32, Y32.data(), sizeof(float) * Y32.size(), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_Ywt32, Ywt32.data(), sizeof(float) * Ywt32.size(), cudaMemcpyHostToDevice));
     DFTG_CUDA(cudaMemcpy(c->d_pre, pre.data(), sizeof(double) * pre.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_LU, LU.data(), sizeof(double) * LU.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_piv, piv.data(), sizeof(int) * piv.size(), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_fold, fold.data(), sizeof(double) * fold.size(), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_rec, rec.data(), sizeof(double) * rec.size(), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_pre32, pre32.data(), sizeof(float) * pre32.size(), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_rec32, rec32.data(), sizeof(float) * rec32.size(), cudaMemcpyHostToDevice));
     DFTG_CUDA(cudaMemcpy(c->d_sx, sx.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_splf, f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice));
     return DFTG_OK;
 }
 
 // ------------------------------------------------------------------ kernels
 
-// K5a: CTA per (atom, shell)
+// K5a (FP64): CTA per (atom, shell)
 __global__ void k_rholm(int nrad, int nang, int nlm, const double *__restrict__ rho, const double *__restrict__ wb,
                         const double *__restrict__ Yw, double *__restrict__ rholm)
 {
@@ -207,51 +337,70 @@ __global__ void k_rholm(int nrad, int nang, int nlm, const double *__restrict__ 
     }
 }
 
-// K5b: one thread per (atom, lm); g in shared memory [S][32]
-__global__ void k_poisson(int natoms, int nrad, int lmax, const double *__restrict__ rn,
-                          const double *__restrict__ LU, const int *__restrict__ piv,
-                          const double *__restrict__ rholm, const double *__restrict__ scal,
-                          double *__restrict__ U)
+// K5a (mixed): split-FP32 products (hi*hi + hi*lo + lo*hi), FP32 partial sums of
+// 16 terms added in FP64
+__global__ void k_rholm_split(int nrad, int nang, int nlm, const double *__restrict__ rho,
+                              const double *__restrict__ wb, const float *__restrict__ Ywt, double *__restrict__ rholm)
 {
-    extern __shared__ double s_g[];
-    const int nlm = (lmax + 1) * (lmax + 1);
-    const int t = threadIdx.x;
-    const int id = blockIdx.x * 32 + t;
-    const int N = nrad, S = N + 2;
-    if (id >= natoms * nlm) return;
-    const int a = id / nlm, lm = id % nlm;
-    int l = 0;
-    while ((l + 1) * (l + 1) <= lm) ++l;
-    const double *F = LU + (size_t)l * S * S;
-    const int *pv = piv + (size_t)l * S;
-    const double *R = rholm + ((size_t)a * nlm + lm) * N;
-    double *g = s_g;   // g[i*32 + t]
-    g[t] = (lm == 0) ? sqrt(4.0 * kPi) * scal[kScalAtomQ + a] : 0.0;
-    for (int i = 1; i < N + 1; ++i) g[i * 32 + t] = -4.0 * kPi * rn[i - 1] * R[i - 1];
-    g[(N + 1) * 32 + t] = 0.0;
-    // the factor rows were exchanged whole (multipliers included), so the
-    // interchanges are applied to g first, then the unit-lower sweep
-    for (int k = 0; k < S; ++k) {
-        const int p = pv[k];
-        if (p != k) { double tmp = g[k * 32 + t]; g[k * 32 + t] = g[p * 32 + t]; g[p * 32 + t] = tmp; }
+    extern __shared__ float s_sp[];    // [2][nang]
+    const int a = blockIdx.x / nrad, i = blockIdx.x % nrad;
+    const size_t base = ((size_t)a * nrad + i) * nang;
+    for (int j = threadIdx.x; j < nang; j += blockDim.x) {
+        const double v = rho[base + j] * wb[base + j];
+        const float hi = (float)v;
+        s_sp[j] = hi;
+        s_sp[nang + j] = (float)(v - (double)hi);
     }
-    for (int k = 0; k < S; ++k) {
-        const double gk = g[k * 32 + t];
-        for (int i = k + 1; i < S; ++i) {
-            const double f = F[(size_t)i * S + k];
-            if (f != 0.0) g[i * 32 + t] -= f * gk;
+    __syncthreads();
+    const size_t half = (size_t)nlm * nang;
+    for (int lm = threadIdx.x; lm < nlm; lm += blockDim.x) {
+        float s = 0.f, e = 0.f;
+        for (int j = 0; j < nang; ++j) {
+            const float yh = Ywt[(size_t)j * nlm + lm], yl = Ywt[half + (size_t)j * nlm + lm];
+            const float sh = s_sp[j], sl = s_sp[nang + j];
+            two_sum_acc(s, e, fmaf(sh, yh, fmaf(sh, yl, sl * yh)));
         }
+        rholm[((size_t)a * nlm + lm) * nrad + i] = ((double)s + (double)e) * 4.0 * kPi;
     }
-    for (int i = S - 1; i >= 0; --i) {
-        double s = g[i * 32 + t];
-        for (int j = i + 1; j < S; ++j) s -= F[(size_t)i * S + j] * g[j * 32 + t];
-        g[i * 32 + t] = s / F[(size_t)i * S + i];
-    }
-    double *u = U + ((size_t)a * nlm + lm) * N;
-    for (int i = 1; i < N + 1; ++i) u[i - 1] = g[i * 32 + t];
 }
 
-// K5c: own-cell potential for every point
+// K5b: U_lm = G_l rho_lm (+ the l = 0 boundary column times q_a): one block per
+// (atom, lm), one thread per radial point, four partial sums per dot product.
+// Writes U (FP64) and its hi/lo FP32 split.
+__global__ void k_poisson(int natoms, int nrad, int lmax, const double *__restrict__ Gt,
+                          const double *__restrict__ Gb, const double *__restrict__ rholm,
+                          const double *__restrict__ scal, double *__restrict__ U, float *__restrict__ U32)
+{
+    extern __shared__ double s_r[];     // [nrad]
+    const int nlm = (lmax + 1) * (lmax + 1);
+    const int id = blockIdx.x, a = id / nlm, lm = id % nlm, N = nrad;
+    int l = 0;
+    while ((l + 1) * (l + 1) <= lm) ++l;
+    const double *R = rholm + (size_t)id * N;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) s_r[k] = R[k];
+    __syncthreads();
+    const double *G = Gt + (size_t)l * N * N;
+    const double q = (lm == 0) ? scal[kScalAtomQ + a] : 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        int k = 0;
+        for (; k + 3 < N; k += 4) {
+            s0 += G[(size_t)k * N + i] * s_r[k];
+            s1 += G[(size_t)(k + 1) * N + i] * s_r[k + 1];
+            s2 += G[(size_t)(k + 2) * N + i] * s_r[k + 2];
+            s3 += G[(size_t)(k + 3) * N + i] * s_r[k + 3];
+        }
+        for (; k < N; ++k) s0 += G[(size_t)k * N + i] * s_r[k];
+        double v = (s0 + s1) + (s2 + s3);
+        if (lm == 0) v += Gb[i] * q;
+        U[(size_t)id * N + i] = v;
+        const float hi = (float)v;
+        U32[(size_t)id * N + i] = hi;
+        U32[(size_t)natoms * nlm * N + (size_t)id * N + i] = (float)(v - (double)hi);
+    }
+}
+
+// K5c (FP64): own-cell potential for every point
 __global__ void k_vown(size_t npts, int nrad, int nang, int nlm, const double *__restrict__ rn,
                        const double *__restrict__ leb, const double *__restrict__ Y, const double *__restrict__ U,
                        double *__restrict__ Vown)
@@ -269,79 +418,107 @@ __global__ void k_vown(size_t npts, int nrad, int nang, int nlm, const double *_
     Vown[p] = v;
 }
 
-// K5d: spline coefficients, thread per (atom, lm)
-__global__ void k_splines(int natoms, int nrad, int nlm, const double *__restrict__ sx, const double *__restrict__ U,
-                          double *__restrict__ spl, float *__restrict__ spl32, double *__restrict__ work)
+// K5c (mixed): split-FP32 products, 16-term FP32 partials added in FP64
+__global__ void k_vown_split(size_t npts, int natoms, int nrad, int nang, int nlm, const double *__restrict__ rn,
+                             const double *__restrict__ leb, const float *__restrict__ Y32,
+                             const float *__restrict__ U32, double *__restrict__ Vown)
 {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= natoms * nlm) return;
-    const int n = nrad;
-    const double *u = U + (size_t)id * n;      // u[i] at r_n[i] (decreasing r)
-    double *Bc = work + (size_t)id * 3 * n, *Cc = Bc + n, *Yc = Cc + n;
-#define YV(i) u[n - 1 - (i)]
-    double h0 = sx[1] - sx[0], h1 = sx[2] - sx[1];
-    double r0 = (YV(1) - YV(0)) / h0, r1 = (YV(2) - YV(1)) / h1;
-    double B0 = h1 * (h0 + h1);
-    Cc[0] = (h0 + h1) * (h0 + h1);
-    Yc[0] = r0 * (3 * h0 * h1 + 2 * h1 * h1) + r1 * h0 * h0;
-    Bc[0] = B0;
-    // forward sweep fused with the system assembly (cspline.cpp:83-128)
-    Cc[0] = Cc[0] / B0;
-    Yc[0] = Yc[0] / B0;
-    for (int i = 1; i < n - 1; ++i) {
-        h0 = sx[i] - sx[i - 1];
-        h1 = sx[i + 1] - sx[i];
-        r0 = (YV(i) - YV(i - 1)) / h0;
-        r1 = (YV(i + 1) - YV(i)) / h1;
-        const double A = h1, B = 2 * (h0 + h1), C = h0, Yv = 3 * (r0 * h1 + r1 * h0);
-        const double den = B - A * Cc[i - 1];
-        Cc[i] = C / den;
-        Yc[i] = (Yv - A * Yc[i - 1]) / den;
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npts) return;
+    const int per_atom = nrad * nang;
+    const int a = (int)(p / per_atom), rem = (int)(p % per_atom), i = rem / nang, j = rem % nang;
+    const double ri = rn[i];
+    const double px = leb[4 * j] * ri, py = leb[4 * j + 1] * ri, pz = leb[4 * j + 2] * ri;
+    const double inv_r = 1.0 / sqrt(px * px + py * py + pz * pz);
+    const size_t uhalf = (size_t)natoms * nlm * nrad, yhalf = (size_t)nlm * nang;
+    const float *uh = U32 + (size_t)a * nlm * nrad + i, *ul = uh + uhalf;
+    float s = 0.f, e = 0.f;
+    for (int lm = 0; lm < nlm; ++lm) {
+        const float yh = Y32[(size_t)lm * nang + j], yl = Y32[yhalf + (size_t)lm * nang + j];
+        const float h = uh[(size_t)lm * nrad], lo = ul[(size_t)lm * nrad];
+        two_sum_acc(s, e, fmaf(h, yh, fmaf(h, yl, lo * yh)));
     }
-    {
-        const int i = n - 1;
-        const double A = (h0 + h1) * (h0 + h1), B = h0 * (h0 + h1);
-        const double Yv = r0 * h1 * h1 + r1 * (3 * h0 * h1 + 2 * h0 * h0);
-        Yc[i] = (Yv - A * Yc[i - 1]) / (B - A * Cc[i - 1]);
-    }
-    // back substitution: derivatives D (stored in Bc)
-    double *D = Bc;
-    D[n - 1] = Yc[n - 1];
-    for (int i = n - 1; i > 0; --i) D[i - 1] = Yc[i - 1] - Cc[i - 1] * D[i];
-    const int a = id / nlm, lm = id % nlm;
-    double *out = spl + (((size_t)a * nlm + lm) * n) * 4;
-    float *out32 = spl32 + (((size_t)a * nlm + lm) * n) * 4;
-    for (int i = 0; i < n - 1; ++i) {
-        const double dx = 1.0 / (sx[i + 1] - sx[i]);
-        const double dy = (YV(i + 1) - YV(i)) * dx;
-        const double c0 = YV(i), c1 = D[i], c2 = dx * (3 * dy - 2 * D[i] - D[i + 1]),
-                     c3 = dx * dx * (-2 * dy + D[i] + D[i + 1]);
-        out[4 * i] = c0; out[4 * i + 1] = c1; out[4 * i + 2] = c2; out[4 * i + 3] = c3;
-        out32[4 * i] = (float)c0; out32[4 * i + 1] = (float)c1; out32[4 * i + 2] = (float)c2; out32[4 * i + 3] = (float)c3;
-    }
-    // interval n-1: clamp value of the last knot
-    out[4 * (n - 1)] = YV(n - 1); out[4 * (n - 1) + 1] = 0.0; out[4 * (n - 1) + 2] = 0.0; out[4 * (n - 1) + 3] = 0.0;
-    out32[4 * (n - 1)] = (float)YV(n - 1); out32[4 * (n - 1) + 1] = 0.f; out32[4 * (n - 1) + 2] = 0.f; out32[4 * (n - 1) + 3] = 0.f;
-#undef YV
+    Vown[p] = inv_r * ((double)s + (double)e);
 }
 
-template <typename T> __device__ __forceinline__ T tsqrt(T x);
-template <> __device__ __forceinline__ double tsqrt<double>(double x) { return sqrt(x); }
-template <> __device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
-template <typename T> __device__ __forceinline__ T tacos(T x);
-template <> __device__ __forceinline__ double tacos<double>(double x) { return acos(x); }
-template <> __device__ __forceinline__ float tacos<float>(float x) { return acosf(x); }
+// K5d: spline coefficients of U_lm over increasing r (cspline.cpp:66-142):
+// derivatives D = K y with the precomputed x-only map K, then the per-interval
+// cubic coefficients.  One block per (atom, lm).  Writes the FP64 table
+// [atom][lm][interval][4] and the mixed table [atom][lm][interval][8] =
+// fold_lm * (c0..c3) split into FP32 hi and lo.
+__global__ void k_splines(int natoms, int nrad, int nlm, const double *__restrict__ splf,
+                          const double *__restrict__ Kt, const double *__restrict__ U,
+                          const double *__restrict__ fold, double *__restrict__ spl, float *__restrict__ splm)
+{
+    extern __shared__ double s_spl[];   // y [n], D [n]
+    const int id = blockIdx.x, n = nrad;
+    double *y = s_spl, *D = s_spl + n;
+    const double *u = U + (size_t)id * n;      // u[i] at r_n[i] (decreasing r)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = u[n - 1 - i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double s0 = 0.0, s1 = 0.0;
+        int j = 0;
+        for (; j + 1 < n; j += 2) {
+            s0 += Kt[(size_t)j * n + i] * y[j];
+            s1 += Kt[(size_t)(j + 1) * n + i] * y[j + 1];
+        }
+        if (j < n) s0 += Kt[(size_t)j * n + i] * y[j];
+        D[i] = s0 + s1;
+    }
+    __syncthreads();
+    const double *inv_h = splf;
+    const int lm = id % nlm;
+    const double F = fold[lm];
+    double *out = spl + (size_t)id * n * 4;
+    float *o32 = splm + (size_t)id * n * 8;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double cc[4];
+        if (i < n - 1) {
+            const double dx = inv_h[i];
+            const double dy = (y[i + 1] - y[i]) * dx;
+            cc[0] = y[i];
+            cc[1] = D[i];
+            cc[2] = dx * (3 * dy - 2 * D[i] - D[i + 1]);
+            cc[3] = dx * dx * (-2 * dy + D[i] + D[i + 1]);
+        } else {                     // clamp value of the last knot
+            cc[0] = y[n - 1]; cc[1] = 0.0; cc[2] = 0.0; cc[3] = 0.0;
+        }
+        for (int k = 0; k < 4; ++k) {
+            out[4 * i + k] = cc[k];
+            const double v = F * cc[k];
+            const float hi = (float)v;
+            o32[8 * i + k] = hi;
+            o32[8 * i + 4 + k] = (float)(v - (double)hi);
+        }
+    }
+}
 
-// K5e: total potential on every point; writes V and cj = w V / 2
-template <typename T>
-__global__ void __launch_bounds__(128) k_vcross(size_t npts, size_t npad, int natoms, int nrad, int nang, int lmax,
-                                                const double *__restrict__ atoms, const double *__restrict__ X,
-                                                const double *__restrict__ Yc, const double *__restrict__ Zc,
-                                                const double *__restrict__ W, const double *__restrict__ sx,
-                                                const T *__restrict__ spl, const T *__restrict__ pre,
-                                                const T *__restrict__ rec, const double *__restrict__ Vown,
-                                                double *__restrict__ V, double *__restrict__ cj,
-                                                float *__restrict__ cj32)
+// spline interval of r: smallest i >= 1 with r <= sx[i] (cspline.cpp:163-170),
+// from the analytic inverse of the radial map and an exact comparison fix-up
+__device__ __forceinline__ void spline_interval(double rd, const double *__restrict__ sx, int N, double fscale,
+                                                int &iv, double &t)
+{
+    if (rd < sx[0]) { iv = 0; t = 0.0; return; }
+    if (rd >= sx[N - 1]) { iv = N - 1; t = 0.0; return; }
+    const float pr = acosf((float)((rd - 1.0) / (rd + 1.0))) * (float)fscale;
+    int i = (int)ceilf((float)N - pr);
+    i = max(1, min(N - 1, i));
+    while (i < N - 1 && rd > sx[i]) ++i;
+    while (i > 1 && rd <= sx[i - 1]) --i;
+    iv = i - 1;
+    t = rd - sx[iv];
+}
+
+// K5e (FP64): total potential on every point; writes V and cj = w V / 2
+__global__ void __launch_bounds__(128) k_vcross64(size_t npts, size_t npad, int natoms, int nrad, int nang, int lmax,
+                                                  const double *__restrict__ atoms, const double *__restrict__ X,
+                                                  const double *__restrict__ Yc, const double *__restrict__ Zc,
+                                                  const double *__restrict__ W, const double *__restrict__ sx,
+                                                  const double *__restrict__ spl, const double *__restrict__ pre,
+                                                  const double *__restrict__ rec, const double *__restrict__ Vown,
+                                                  double *__restrict__ V, double *__restrict__ cj,
+                                                  float *__restrict__ cj32)
 {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npad) return;
@@ -350,39 +527,23 @@ __global__ void __launch_bounds__(128) k_vcross(size_t npts, size_t npad, int na
     const int N = nrad;
     const int a = (int)(p / ((size_t)nrad * nang));
     const double px = X[p], py = Yc[p], pz = Zc[p];
-    const double sx0 = sx[0], sxN = sx[N - 1];
-    const T fscale = T((double)(N + 1) / kPi);
+    const double fscale = (double)(N + 1) / kPi;
     double Vt = 0.0;
     for (int k = 0; k < natoms; ++k) {
         if (k == a) { Vt += Vown[p]; continue; }
-        const double dxd = px - atoms[4 * k], dyd = py - atoms[4 * k + 1], dzd = pz - atoms[4 * k + 2];
-        const T dx = T(dxd), dy = T(dyd), dz = T(dzd);
-        const T r = tsqrt<T>(dx * dx + dy * dy + dz * dz);
-        const double rd = double(r);
+        const double dx = px - atoms[4 * k], dy = py - atoms[4 * k + 1], dz = pz - atoms[4 * k + 2];
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
         int iv;
-        T t;
-        if (rd < sx0) { iv = 0; t = T(0); }
-        else if (rd >= sxN) { iv = N - 1; t = T(0); }
-        else {
-            // r <= sx[i] <=> radial index p(r) >= N - i, p(r) = acos((r-1)/(r+1)) (N+1)/pi
-            const T pr = tacos<T>((r - T(1)) / (r + T(1))) * fscale;
-            int i = (int)ceil(double(N) - double(pr));
-            i = max(1, min(N - 1, i));
-            while (i < N - 1 && rd > sx[i]) ++i;
-            while (i > 1 && rd <= sx[i - 1]) --i;
-            iv = i - 1;
-            t = T(rd - sx[iv]);
-        }
-        const T inv_r = T(1) / r;
-        const T ux = dx * inv_r, uy = dy * inv_r, uz = dz * inv_r;
-        const T *cf = spl + ((size_t)k * nlm * N + iv) * 4;   // + lm*N*4
-        T acc = T(0);
-        T cm = T(1), sm = T(0);     // Re / Im of (ux + i uy)^m
-        T qmm = T(1);               // Q_m^m = (-1)^m (2m-1)!!
+        double t;
+        spline_interval(r, sx, N, fscale, iv, t);
+        const double inv_r = 1.0 / r;
+        const double ux = dx * inv_r, uy = dy * inv_r, uz = dz * inv_r;
+        const double *cf = spl + ((size_t)k * nlm * N + iv) * 4;
+        double acc = 0.0, cm = 1.0, sm = 0.0, qmm = 1.0;
         for (int m = 0; m <= lmax; ++m) {
-            T q2 = T(0), q1 = qmm;
+            double q2 = 0.0, q1 = qmm;
             for (int l = m; l <= lmax; ++l) {
-                T q;
+                double q;
                 if (l == m) q = qmm;
                 else {
                     const int lmi = l * l + l + m;
@@ -391,23 +552,23 @@ __global__ void __launch_bounds__(128) k_vcross(size_t npts, size_t npad, int na
                     q1 = q;
                 }
                 const int lp = l * l + l + m;
-                const T *c0 = cf + (size_t)lp * N * 4;
-                const T sp = c0[0] + t * (c0[1] + t * (c0[2] + t * c0[3]));
+                const double *c0 = cf + (size_t)lp * N * 4;
+                const double sp = c0[0] + t * (c0[1] + t * (c0[2] + t * c0[3]));
                 if (m == 0) {
                     acc += pre[lp] * q * sp;
                 } else {
                     const int ln = l * l + l - m;
-                    const T *c1 = cf + (size_t)ln * N * 4;
-                    const T sn = c1[0] + t * (c1[1] + t * (c1[2] + t * c1[3]));
+                    const double *c1 = cf + (size_t)ln * N * 4;
+                    const double sn = c1[0] + t * (c1[1] + t * (c1[2] + t * c1[3]));
                     acc += pre[lp] * q * cm * sp + pre[ln] * q * sm * sn;
                 }
-                if (l == m) { q2 = T(0); q1 = qmm; }
             }
-            const T cn = cm * ux - sm * uy, sn2 = cm * uy + sm * ux;
-            cm = cn; sm = sn2;
-            qmm = -T(2 * m + 1) * qmm;
+            const double cn = cm * ux - sm * uy, sn2 = cm * uy + sm * ux;
+            cm = cn;
+            sm = sn2;
+            qmm = -(double)(2 * m + 1) * qmm;
         }
-        Vt += double(inv_r * acc);
+        Vt += inv_r * acc;
     }
     V[p] = Vt;
     const double c = 0.5 * (W[p] * Vt);
@@ -415,40 +576,158 @@ __global__ void __launch_bounds__(128) k_vcross(size_t npts, size_t npad, int na
     cj32[p] = (float)c;
 }
 
+// K5e (mixed): FP32 recursion with exact integer coefficients; every constant
+// shared by many points (Y_lm normalisation, spline coefficients) enters as a
+// split FP32 pair so no rounding is common to all points.  Per atom pair the
+// sums are carried in FP32 (hi and lo parts) and added to V in FP64.
+__global__ void __launch_bounds__(128) k_vcross_mixed(size_t npts, size_t npad, int natoms, int nrad, int nang,
+                                                      int lmax, const double *__restrict__ atoms,
+                                                      const double *__restrict__ X, const double *__restrict__ Yc,
+                                                      const double *__restrict__ Zc, const double *__restrict__ W,
+                                                      const double *__restrict__ sx, const float *__restrict__ splm,
+                                                      const double *__restrict__ Vown, double *__restrict__ V,
+                                                      double *__restrict__ cj, float *__restrict__ cj32)
+{
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npad) return;
+    if (p >= npts) { V[p] = 0.0; cj[p] = 0.0; cj32[p] = 0.f; return; }
+    const int nlm = (lmax + 1) * (lmax + 1);
+    const int N = nrad;
+    const int a = (int)(p / ((size_t)nrad * nang));
+    const double px = X[p], py = Yc[p], pz = Zc[p];
+    const double fscale = (double)(N + 1) / kPi;
+    double Vt = 0.0;
+    for (int k = 0; k < natoms; ++k) {
+        if (k == a) { Vt += Vown[p]; continue; }
+        const float dx = (float)(px - atoms[4 * k]), dy = (float)(py - atoms[4 * k + 1]),
+                    dz = (float)(pz - atoms[4 * k + 2]);
+        const float r = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+        int iv;
+        double td;
+        spline_interval((double)r, sx, N, fscale, iv, td);
+        const float t = (float)td;
+        const float inv_r = 1.0f / r;
+        const float ux = dx * inv_r, uy = dy * inv_r, uz = dz * inv_r;
+        const float4 *cf = reinterpret_cast<const float4 *>(splm + ((size_t)k * nlm * N + iv) * 8);
+        const size_t lstride = (size_t)N * 2;   // float4 units per lm
+        float ah = 0.f, al = 0.f, cm = 1.f, sm = 0.f;
+        for (int m = 0; m <= lmax; ++m) {
+            float r2 = 0.f, r1 = 1.f;
+            for (int l = m; l <= lmax; ++l) {
+                float q;
+                if (l == m) q = 1.f;
+                else {
+                    q = (float)(2 * l - 1) * uz * r1 - (float)((l + m - 1) * (l - m - 1)) * r2;
+                    r2 = r1;
+                    r1 = q;
+                }
+                const int lp = l * l + l + m;
+                const float4 ch = cf[(size_t)lp * lstride], cl = cf[(size_t)lp * lstride + 1];
+                const float sh = fmaf(t, fmaf(t, fmaf(t, ch.w, ch.z), ch.y), ch.x);
+                const float sl = fmaf(t, fmaf(t, fmaf(t, cl.w, cl.z), cl.y), cl.x);
+                if (m == 0) {
+                    ah = fmaf(q, sh, ah);
+                    al = fmaf(q, sl, al);
+                } else {
+                    const int ln = l * l + l - m;
+                    const float4 dh = cf[(size_t)ln * lstride], dl = cf[(size_t)ln * lstride + 1];
+                    const float nh = fmaf(t, fmaf(t, fmaf(t, dh.w, dh.z), dh.y), dh.x);
+                    const float nl = fmaf(t, fmaf(t, fmaf(t, dl.w, dl.z), dl.y), dl.x);
+                    const float qc = q * cm, qs = q * sm;
+                    ah = fmaf(qc, sh, fmaf(qs, nh, ah));
+                    al = fmaf(qc, sl, fmaf(qs, nl, al));
+                }
+            }
+            const float cn = cm * ux - sm * uy, sn2 = cm * uy + sm * ux;
+            cm = cn;
+            sm = sn2;
+        }
+        Vt += (double)inv_r * ((double)ah + (double)al);
+    }
+    V[p] = Vt;
+    const double c = 0.5 * (W[p] * Vt);
+    cj[p] = c;
+    cj32[p] = (float)c;
+}
+
+// E_J = 2 tr(P J) = sum_p (w V / 2) rho_raw (the J assembly contracted with P,
+// evaluated directly on the grid in FP64): deterministic block partials...
+__global__ void __launch_bounds__(256) k_ej_partials(size_t npad, const double *__restrict__ cj,
+                                                     const double *__restrict__ rho, double *__restrict__ part)
+{
+    __shared__ double sh[256];
+    const size_t p = (size_t)blockIdx.x * 256 + threadIdx.x;
+    sh[threadIdx.x] = p < npad ? cj[p] * rho[p] : 0.0;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// ...summed in order; rho on the device carries the correction factor when scaled
+__global__ void __launch_bounds__(256) k_ej_final(int n, const double *__restrict__ part, int scaled, double *scal)
+{
+    __shared__ double sh[256];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += 256) s += part[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) scal[kScalEJ] = scaled ? sh[0] / scal[kScalScale] : sh[0];
+}
+
 int launch_hartree(dftg_ctx *c)
 {
     const int N = c->nrad, S = N + 2, nlm = c->nlm;
-    k_rholm<<<c->natoms * N, 128, sizeof(double) * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho, c->d_wb, c->d_Yw,
-                                                                         c->d_rholm);
+    const bool mp = (c->prec_mask & kPrecMultipole) != 0;
+    if (mp)
+        k_rholm_split<<<c->natoms * N, 96, sizeof(float) * 2 * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho,
+                                                                                     c->d_wb, c->d_Ywt32, c->d_rholm);
+    else
+        k_rholm<<<c->natoms * N, 96, sizeof(double) * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho, c->d_wb,
+                                                                            c->d_Yw, c->d_rholm);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "rholm");
     const int nrhs = c->natoms * nlm;
-    const size_t sm = sizeof(double) * S * 32;
-    if (sm > 48 * 1024) DFTG_CUDA(cudaFuncSetAttribute(k_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_poisson<<<(nrhs + 31) / 32, 32, sm, c->stream>>>(c->natoms, N, c->lmax, c->d_rn, c->d_LU, c->d_piv, c->d_rholm,
-                                                       c->d_scal, c->d_U);
+    (void)S;
+    k_poisson<<<nrhs, 128, sizeof(double) * N, c->stream>>>(c->natoms, N, c->lmax, c->d_Gt, c->d_Gb, c->d_rholm,
+                                                            c->d_scal, c->d_U, c->d_U32);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "poisson");
-    k_vown<<<(unsigned)((c->npts + 127) / 128), 128, 0, c->stream>>>(c->npts, N, c->nang, nlm, c->d_rn, c->d_leb,
-                                                                     c->d_Y, c->d_U, c->d_Vown);
+    const unsigned npb = (unsigned)((c->npts + 127) / 128);
+    if (mp)
+        k_vown_split<<<npb, 128, 0, c->stream>>>(c->npts, c->natoms, N, c->nang, nlm, c->d_rn, c->d_leb, c->d_Y32,
+                                                 c->d_U32, c->d_Vown);
+    else
+        k_vown<<<npb, 128, 0, c->stream>>>(c->npts, N, c->nang, nlm, c->d_rn, c->d_leb, c->d_Y, c->d_U, c->d_Vown);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "vown");
-    // the spline work area reuses the contraction partial buffer (3 * nrhs * N doubles)
-    k_splines<<<(nrhs + 63) / 64, 64, 0, c->stream>>>(c->natoms, N, nlm, c->d_sx, c->d_U, c->d_spl, c->d_spl32,
-                                                      c->d_part);
+    k_splines<<<nrhs, 128, sizeof(double) * 2 * N, c->stream>>>(c->natoms, N, nlm, c->d_splf, c->d_Kt, c->d_U,
+                                                                c->d_fold, c->d_spl, c->d_splm);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "splines");
     const unsigned nb = (unsigned)(c->npad / 128);
-    if (c->precision == DFTG_PREC_FP64)
-        k_vcross<double><<<nb, 128, 0, c->stream>>>(c->npts, c->npad, c->natoms, N, c->nang, c->lmax, c->d_atoms,
-                                                    c->d_x, c->d_y, c->d_z, c->d_w, c->d_sx, c->d_spl, c->d_pre,
-                                                    c->d_rec, c->d_Vown, c->d_V, c->d_cj, c->d_cj32);
+    if (c->prec_mask & kPrecCross)
+        k_vcross_mixed<<<nb, 128, 0, c->stream>>>(c->npts, c->npad, c->natoms, N, c->nang, c->lmax, c->d_atoms,
+                                                  c->d_x, c->d_y, c->d_z, c->d_w, c->d_sx, c->d_splm, c->d_Vown,
+                                                  c->d_V, c->d_cj, c->d_cj32);
     else
-        k_vcross<float><<<nb, 128, 0, c->stream>>>(c->npts, c->npad, c->natoms, N, c->nang, c->lmax, c->d_atoms,
-                                                   c->d_x, c->d_y, c->d_z, c->d_w, c->d_sx, c->d_spl32, c->d_pre32,
-                                                   c->d_rec32, c->d_Vown, c->d_V, c->d_cj, c->d_cj32);
+        k_vcross64<<<nb, 128, 0, c->stream>>>(c->npts, c->npad, c->natoms, N, c->nang, c->lmax, c->d_atoms, c->d_x,
+                                              c->d_y, c->d_z, c->d_w, c->d_sx, c->d_spl, c->d_pre, c->d_rec,
+                                              c->d_Vown, c->d_V, c->d_cj, c->d_cj32);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "vcross");
+    const unsigned ne = (unsigned)((c->npad + 255) / 256);
+    k_ej_partials<<<ne, 256, 0, c->stream>>>(c->npad, c->d_cj, c->d_rho, c->d_red);
+    DFTG_LAUNCH_CHECK();
+    k_ej_final<<<1, 256, 0, c->stream>>>((int)ne, c->d_red, c->rho_scaled ? 1 : 0, c->d_scal);
+    DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "hartree_energy");
     return DFTG_OK;
 }
 

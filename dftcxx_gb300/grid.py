@@ -72,6 +72,13 @@ class MolecularGrid:
         check(_lib.load().dftg_set_precision(self._h, code))
         self.precision = precision
 
+    MIX_BITS = {"density": 1, "lda": 2, "multipole": 4, "cross": 8, "contract": 16}
+
+    def set_precision_mask(self, mask):
+        """Run the steps whose bits are set (MIX_BITS) in the mixed form."""
+        check(_lib.load().dftg_set_precision_mask(self._h, int(mask)))
+        self.precision = "mixed" if mask else "fp64"
+
     def set_stream(self, stream_ptr):
         check(_lib.load().dftg_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
 
@@ -109,7 +116,15 @@ class MolecularGrid:
         XC = np.zeros((self.nbf, self.nbf), order="F")
         e, n = ctypes.c_double(), ctypes.c_double()
         check(_lib.load().dftg_fock_build(self._h, _ptr(P), _ptr(J), _ptr(XC), ctypes.byref(e), ctypes.byref(n)))
-        return {"J": np.ascontiguousarray(J), "XC": np.ascontiguousarray(XC), "Exc": e.value, "nelec": n.value}
+        return {"J": np.ascontiguousarray(J), "XC": np.ascontiguousarray(XC), "Exc": e.value, "nelec": n.value,
+                "EJ": self.energies()["EJ"]}
+
+    def energies(self):
+        """E_xc, E_J = 2 tr(P J) summed on the grid in FP64, integrated density
+        of the last build."""
+        e, j, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(_lib.load().dftg_get_energies(self._h, ctypes.byref(e), ctypes.byref(j), ctypes.byref(n)))
+        return {"Exc": e.value, "EJ": j.value, "nelec": n.value}
 
     def _points(self, name, mult=1):
         out = np.empty(self.grid_size * mult)
@@ -185,8 +200,13 @@ class DFT:
         self.P = Pn if self.P is None else (1.0 - alpha) * Pn + alpha * self.P
 
     def _energy(self):
+        """dft.cpp:441-447.  In the mixed build the Hartree term is the grid sum
+        of the library (the same 2 tr(P J), accumulated in FP64)."""
         self.e_one = 2.0 * np.trace(self.P @ self.H)
-        self.e_j = 2.0 * np.trace(self.P @ self.J)
+        if self.molgrid.precision == "mixed" and getattr(self, "e_j_grid", None) is not None:
+            self.e_j = self.e_j_grid
+        else:
+            self.e_j = 2.0 * np.trace(self.P @ self.J)
         return self.e_one + self.e_j + self.enuc + self.exc
 
     def scf(self, tol=1e-4, max_iter=100, min_iter=3):
@@ -198,6 +218,7 @@ class DFT:
             self._density_matrix()
             r = self.molgrid.fock_build(self.P)
             self.J, self.XC, self.exc = r["J"], r["XC"], r["Exc"]
+            self.e_j_grid = r["EJ"]
             self.et = self._energy()
             self.history.append({"iter": it, "E": self.et, "Exc": self.exc, "EJ": self.e_j, "nelec": r["nelec"]})
             diff = abs(self.et - old)

@@ -93,6 +93,15 @@ int dftg_nbf(const dftg_ctx *ctx, int *nbf);             /* Molecule::get_nr_bfs
 
 /* Precision of the per-iteration build (default DFTG_PREC_FP64). */
 int dftg_set_precision(dftg_ctx *ctx, int precision);
+/* Finer control for error budgets (no counterpart in the reference): each set
+ * bit runs one step of the build in the mixed form, the others in FP64.
+ * DFTG_PREC_MIXED is all bits; 0 is DFTG_PREC_FP64. */
+#define DFTG_MIX_DENSITY 1u     /* rho = 2 phi^T P phi */
+#define DFTG_MIX_LDA 2u         /* Slater + VWN point kernel */
+#define DFTG_MIX_MULTIPOLE 4u   /* rho_lm projection and own-cell potential */
+#define DFTG_MIX_CROSS 8u       /* cross-atom Hartree potential */
+#define DFTG_MIX_CONTRACT 16u   /* XC and J contractions */
+int dftg_set_precision_mask(dftg_ctx *ctx, unsigned mask);
 /* Run on a caller-owned cudaStream_t (NULL restores the context's stream). */
 int dftg_set_stream(dftg_ctx *ctx, void *cuda_stream);
 
@@ -116,10 +125,18 @@ int dftg_calculate_xc(dftg_ctx *ctx, double *XC, double *exc);
 int dftg_fock_build(dftg_ctx *ctx, const double *P, double *J, double *XC,
                     double *exc, double *nelec);
 /* The same with DEVICE pointers on the context's stream and no host
- * synchronisation (P: nbf*nbf doubles; J, XC: nbf*nbf; scalars: exc, nelec as
- * a 2-double device array).  For callers whose P is already in HBM. */
+ * synchronisation (P: nbf*nbf doubles; J, XC: nbf*nbf; scalars: a 3-double
+ * device array receiving E_xc, the integrated density and E_J).  For callers
+ * whose P is already in HBM. */
 int dftg_fock_build_device(dftg_ctx *ctx, const double *P_dev, double *J_dev,
                            double *XC_dev, double *scalars_dev);
+
+/* Energies of the last build: E_xc, E_J and the integrated density.  E_J is
+ * the Hartree term of DFT::calculate_energy, 2 tr(P J) (dft.cpp:443), which
+ * equals sum_p (w_p V_p / 2) rho_p over the grid with rho = 2 phi^T P phi
+ * before correction; it is summed on the grid in FP64 in both precisions, so
+ * the energy does not inherit the split-precision rounding of the J matrix. */
+int dftg_get_energies(dftg_ctx *ctx, double *exc, double *ej, double *nelec);
 
 /* Diagnostic variant of dftg_fock_build_device (no counterpart in the
  * reference, which only prints wall-clock totals, dft.cpp:98-119): runs one

@@ -133,3 +133,27 @@ def test_mixed_precision_error_small(gpu_lib, oracle_mod):
     assert np.abs(a["J"] - b["J"]).max() < 1e-5
     assert np.abs(a["XC"] - b["XC"]).max() < 1e-5
     assert abs(a["Exc"] - b["Exc"]) < 1e-5
+
+
+@pytest.mark.parametrize("name,basis,nrad,leb", [("H2O", "sto3g", 32, 7), ("C6H6", "p631", 20, 8)])
+def test_mixed_density_tensor_core_accuracy(gpu_lib, name, basis, nrad, leb):
+    """The mixed-path density (integer-slice BF16 products on the tensor cores)
+    reproduces the FP64 density to ~1e-10 relative."""
+    from dftcxx_gb300.grid import MolecularGrid
+    Z, xyz = small_molecule(name)
+    mol = Molecule(Z, xyz, basis)
+    g64 = MolecularGrid(mol, nrad, leb, 6, precision="fp64")
+    gmx = MolecularGrid(mol, nrad, leb, 6, precision="mixed")
+    P = _density(mol, 7)
+    g64.set_density(P)
+    gmx.set_density(P)
+    r64, rmx = g64.get_densities(), gmx.get_densities()
+    # four 8-bit slices per operand: 2^-33 of the row and column scales per
+    # element, summed over nbf products (worst case ~1e-8 at the nuclei)
+    d = np.abs(rmx - r64)
+    tol = 3e-8 * np.abs(r64) + 1e-12 * np.abs(r64).max()
+    bad = np.argmax(d - tol)
+    assert np.all(d <= tol), (float(d[bad]), float(r64[bad]), float(d.max()), float((d / np.maximum(r64, 1e-300)).max()))
+    a, b = g64.fock_build(P), gmx.fock_build(P)
+    assert abs(a["Exc"] - b["Exc"]) < 2e-7
+    assert abs(a["EJ"] - b["EJ"]) < 2e-6
