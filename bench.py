@@ -40,8 +40,9 @@ WORKLOAD = {"workload": "benzene/6-31G grid Fock build", "molecule": "C6H6 D6h",
             "radial_points": 75, "lebedev_points": 302, "lmax": 8, "grid_points": 271800}
 
 # kernels launched per build, by profile phase (see dftcxx_gb300/csrc)
-KERNELS_PER_PHASE = {"convert_P": 1, "density": 1, "charge": 5, "lda": 2, "rholm": 1, "poisson": 1, "vown": 1,
-                     "splines": 1, "vcross": 1, "contract": 1, "contract_reduce": 1}
+# kernels launched per phase of one mixed-precision build (dftg_fock_build_device)
+KERNELS_PER_PHASE = {"density": 2, "charge": 2, "lda": 2, "rholm": 1, "poisson": 1, "vown": 1,
+                     "splines": 1, "vcross": 2, "hartree_energy": 2, "contract": 1, "contract_reduce": 1}
 
 
 def _env_int(name, default):

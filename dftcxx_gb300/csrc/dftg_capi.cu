@@ -76,7 +76,8 @@ static void free_ctx(dftg_ctx *c)
                     c->d_XC, c->d_part, c->d_red, c->d_scal, c->d_Y, c->d_Yw, c->d_pre, c->d_pre32, c->d_rec,
                     c->d_rec32, c->d_rholm, c->d_U, c->d_U32, c->d_Y32, c->d_Ywt32, c->d_fold, c->d_Gt,
                     c->d_Gb, c->d_Kt, c->d_sx, c->d_splf, c->d_spl, c->d_splm, c->d_tiles,
-                    c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_flag};
+                    c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_flag,
+                    c->d_pairs, c->d_pairpos, c->d_pairv};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -215,6 +216,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(hartree_setup(c));
     DFTG_TRY(contract_setup(c));
     DFTG_TRY(density_tc_setup(c));
+    DFTG_TRY(cross_pairs_setup(c));
     DFTG_CUDA(cudaStreamSynchronize(c->stream));
     return DFTG_OK;
 }

@@ -117,6 +117,11 @@ struct dftg_ctx {
     double *d_Gt = nullptr;       // [lmax+1][nrad (k)][nrad (i)] radial Poisson solution map
     double *d_Gb = nullptr;       // [nrad] boundary column of the l = 0 map (times q_a)
     double *d_Kt = nullptr;       // [nrad (j)][nrad (i)] spline derivative map
+    size_t npairs = 0;            // (point, other atom) pairs of the cross-atom potential
+    void *d_pairs = nullptr;      // [npairs] float4 (unit vector, 1/r) then [npairs] float2 (t, k << 16 | interval),
+                                  // ordered by (atom, spline interval)
+    int *d_pairpos = nullptr;     // [npts][natoms] place of pair (p, k) in d_pairs
+    void *d_pairv = nullptr;      // [npairs] float2 contributions
     double *d_sx = nullptr;       // [nrad] increasing spline abscissae
     double *d_splf = nullptr;     // spline factorisation (x only)
     double *d_spl = nullptr;      // [natoms][nlm][nrad][4] FP64 spline coefficients
@@ -187,6 +192,7 @@ int launch_atom_sums(dftg_ctx *c, int mode);
 int launch_xc_points(dftg_ctx *c, bool apply_scale);
 // k_hartree.cu
 int hartree_setup(dftg_ctx *c);
+int cross_pairs_setup(dftg_ctx *c);
 size_t hartree_splf_elems(int nrad);
 int launch_hartree(dftg_ctx *c);
 // k_integrals.cu

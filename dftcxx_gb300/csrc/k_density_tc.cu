@@ -1,30 +1,33 @@
 // k_density_tc.cu -- mixed-path density rho_p = 2 phi_p^T P phi_p on the tcgen05
-// tensor cores, accurate to ~1e-10 relative (gridpoint.cpp:82-84).
+// tensor cores, accurate to ~1e-8 relative (gridpoint.cpp:82-84).
 //
 // The energy depends on rho at first order, so rho must carry near-FP64
 // accuracy; FP32 or 3xTF32 arithmetic leaves ~1e-7 random errors per point,
-// about 3e-6 Ha on benzene.  The GEMM T = Phi P is therefore done as an exact
+// about 3e-6 Ha on benzene.  The GEMM T = Phi P is therefore done as an
 // integer-slice product (Ozaki's error-free splitting) on the BF16 tensor cores:
 //
-//   Phi[p, mu] = 2^e_p  sum_{i=1..4} A_i[p, mu] 2^(-8 i)      (per point e_p)
-//   P[mu, nu]  = 2^t_nu sum_{j=1..4} B_j[mu, nu] 2^(-8 j)     (per column t_nu)
+//   Phi[p, mu] = 2^e_p  sum_{i=1..4} a_i[p, mu] 2^(-8 i)      (per point e_p)
+//   P[mu, nu]  = 2^t_nu sum_{j=1..4} b_j[mu, nu] 2^(-8 j)     (per column t_nu)
 //
-// with integer slices |A_1|, |B_1| <= 256 and |A_i|, |B_j| <= 128 (exact in
-// BF16).  Each slice product summed over mu <= 80 stays below 2^24, so the
-// FP32 accumulation in TMEM is exact; the 10 pairs with i + j <= 5 go to four
-// accumulators, one per level L = i + j (weight 2^(-8 L)).  The dropped levels
-// are below 2^-40 of the row/column scales.  The epilogue combines the levels
-// with TwoSum into an FP32 pair and forms rho = 2 sum_nu T_nu phi_nu in
-// compensated FP32, phi rebuilt exactly from the slices in shared memory.
+// with integers |a_1|, |b_1| <= 256 and |a_i|, |b_j| <= 128.  Slice i is
+// stored pre-scaled, A_i = a_i 2^(-8(i-1)) (exact in BF16), so every pair
+// (i, j) contributes A_i B_j with the same weight 2^-16 2^(e_p + t_nu):
+//   D_hi = A_1 B_1           integer products, exact in the FP32 accumulator
+//   D_lo = the other 9 pairs with i + j <= 5, about 2^-8 of D_hi; its FP32
+//          rounding stays near 2^-32 of D_hi, the size of the dropped pairs.
+// The epilogue forms T = D_hi + D_lo with TwoSum and rho = 2 sum_nu T_nu phi_nu
+// in compensated FP32, phi rebuilt exactly from the slices in shared memory.
 //
-// Layouts (canonical no-swizzle K-major core matrices, 8 rows x 16 bytes):
+// Layouts (canonical no-swizzle K-major core matrices, 8 rows x 16 bytes,
+// cores ordered row group by row group: LBO 128 B, SBO (KP/8) 128 B):
 //   A slices in HBM: [slice][tile][128/8][KP/8][8][8] BF16, one contiguous
 //     128 x KP block per slice and tile, copied with cp.async.bulk;
 //   B slices: [slice][NP/8][KP/8][8][8] BF16 (rows nu, K = mu).
 // CTA: warp 0 producer (bulk copies), warp 1 TMEM owner + MMA issuer,
 // warps 2-5 epilogue (TMEM lanes 32 (w % 4) ...).  Persistent over tiles, two
-// A stages.  Every mbarrier wait is bounded: on expiry the CTA records an error
-// code, drains its copies, frees TMEM and exits.
+// A stages and two TMEM accumulator pairs, so the MMAs of one tile overlap the
+// epilogue of the previous one.  Every mbarrier wait is bounded: on expiry the
+// CTA records an error code, drains its copies, frees TMEM and exits.
 #include <cuda_bf16.h>
 #include <cstdint>
 #include "dftg_internal.cuh"
@@ -140,7 +143,7 @@ __host__ __device__ __forceinline__ uint32_t core_off(int row, int k, int kcores
 }
 
 struct TcShared {
-    uint64_t full[2], empty[2], tmem_full, tmem_empty;
+    uint64_t full[2], empty[2], tmem_full[2], tmem_empty[2];
     uint32_t tmem_base;
 };
 
@@ -161,12 +164,12 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
-        mbar_init(&sh->full[0], 1);
-        mbar_init(&sh->full[1], 1);
-        mbar_init(&sh->empty[0], 1);
-        mbar_init(&sh->empty[1], 1);
-        mbar_init(&sh->tmem_full, 1);
-        mbar_init(&sh->tmem_empty, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&sh->full[b], 1);
+            mbar_init(&sh->empty[b], 1);
+            mbar_init(&sh->tmem_full[b], 1);
+            mbar_init(&sh->tmem_empty[b], 1);
+        }
         s_fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -217,29 +220,31 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
             const uint32_t idesc = idesc_bf16(kTcTile, NP);
             const uint32_t lbo = 128, sbo = (uint32_t)(KP / 8) * 128;
             for (int it = 0; it < my_tiles; ++it) {
-                const int s = it & 1, n = it >> 1;
+                const int s = it & 1, n = it >> 1;   // A stage and TMEM buffer share the index
                 if (!mbar_wait(&sh->full[s], (uint32_t)(n & 1))) { atomicExch(err, 2); s_fail = 1; break; }
-                if (!mbar_wait(&sh->tmem_empty, (uint32_t)((it & 1) ^ 1))) { atomicExch(err, 3); s_fail = 1; break; }
+                if (!mbar_wait(&sh->tmem_empty[s], (uint32_t)((n & 1) ^ 1))) { atomicExch(err, 3); s_fail = 1; break; }
                 if (s_fail) break;
                 tc_fence_after();
                 const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
-                for (int L = 2; L <= 5; ++L) {
-                    const uint32_t d = tmem + (uint32_t)((L - 2) * 128);
-                    int first = 1;
-                    for (int i = 1; i <= 4; ++i) {
-                        const int j = L - i;
-                        if (j < 1 || j > 4) continue;
+                const uint32_t d_hi = tmem + (uint32_t)(s * 256), d_lo = d_hi + 128;
+                int first_lo = 1;
+                for (int i = 1; i <= 4; ++i)
+                    for (int j = 1; i + j <= 5; ++j) {
                         const unsigned char *ai = a0 + (size_t)(i - 1) * a_slice_bytes;
                         const unsigned char *bj = sB + (size_t)(j - 1) * b_slice_bytes;
+                        const bool hi = (i == 1 && j == 1);
                         for (int kk = 0; kk < KP / 16; ++kk) {
                             const uint64_t ad = smem_desc(ai + (size_t)kk * 2 * lbo, lbo, sbo);
                             const uint64_t bd = smem_desc(bj + (size_t)kk * 2 * lbo, lbo, sbo);
-                            mma_bf16(d, ad, bd, idesc, first ? 0u : 1u);
-                            first = 0;
+                            if (hi) {
+                                mma_bf16(d_hi, ad, bd, idesc, kk > 0 ? 1u : 0u);
+                            } else {
+                                mma_bf16(d_lo, ad, bd, idesc, first_lo ? 0u : 1u);
+                                first_lo = 0;
+                            }
                         }
                     }
-                }
-                mma_commit(&sh->tmem_full);
+                mma_commit(&sh->tmem_full[s]);
             }
         }
         __syncwarp();
@@ -247,9 +252,10 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3;                 // TMEM lane quarter of this warp
         const int r = q * 32 + lane;            // row of the tile = TMEM lane
+        const int kc = KP / 8;
         for (int it = 0; it < my_tiles; ++it) {
-            const int s = it & 1;
-            bool ok = mbar_wait(&sh->tmem_full, (uint32_t)(it & 1));
+            const int s = it & 1, n = it >> 1;
+            bool ok = mbar_wait(&sh->tmem_full[s], (uint32_t)(n & 1));
             if (!ok) { atomicExch(err, 4); s_fail = 1; }
             epi_bar_sync();
             if (s_fail) break;
@@ -258,38 +264,32 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
             const size_t p = (size_t)tile * kTcTile + r;
             const int ep = row_exp[p];
             const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
+            const uint32_t ta0 = tmem + (uint32_t)(s * 256) + ((uint32_t)(q * 32) << 16);
             float S = 0.f, E = 0.f;
             for (int c0 = 0; c0 < NP; c0 += 16) {
-                float d2[16], d3[16], d4[16], d5[16];
-                const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
-                tmem_ld16(ta, d2);
-                tmem_ld16(ta + 128u, d3);
-                tmem_ld16(ta + 256u, d4);
-                tmem_ld16(ta + 384u, d5);
+                float dh[16], dl[16];
+                tmem_ld16(ta0 + (uint32_t)c0, dh);
+                tmem_ld16(ta0 + 128u + (uint32_t)c0, dl);
                 tmem_wait_ld();
 #pragma unroll
                 for (int k = 0; k < 16; ++k) {
                     const int nu = c0 + k;
                     if (nu >= nbf) continue;
-                    // T~_nu = sum_L D_L 2^(-8L): exact head via TwoSum, small tail
-                    float t = d2[k] * 0x1p-16f;
-                    const float x3 = d3[k] * 0x1p-24f;
-                    const float u = t + x3;
-                    const float bp = u - t;
-                    float te = (t - (u - bp)) + (x3 - bp);
-                    t = u;
-                    te += d4[k] * 0x1p-32f + d5[k] * 0x1p-40f;
-                    const float sc = __int_as_float((127 + s_texp[nu]) << 23);
-                    t *= sc;
+                    // T~_nu 2^16 = D_hi + D_lo: exact head by TwoSum
+                    const float u = dh[k] + dl[k];
+                    const float bp = u - dh[k];
+                    float te = (dh[k] - (u - bp)) + (dl[k] - bp);
+                    const float sc = __int_as_float((127 - 16 + s_texp[nu]) << 23);
+                    const float t = u * sc;
                     te *= sc;
-                    // phi~ from the slices of this row (exact FP32 pair)
-                    const uint32_t off = core_off(r, nu, KP / 8);
+                    // phi~ 2^8 from the pre-scaled slices of this row (exact FP32 pair)
+                    const uint32_t off = core_off(r, nu, kc);
                     const float m1 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + off));
                     const float m2 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + a_slice_bytes + off));
                     const float m3 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + 2 * a_slice_bytes + off));
                     const float m4 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + 3 * a_slice_bytes + off));
-                    const float fh = fmaf(m2, 0x1p-16f, m1 * 0x1p-8f);
-                    const float fl = fmaf(m4, 0x1p-32f, m3 * 0x1p-24f);
+                    const float fh = (m1 + m2) * 0x1p-8f;
+                    const float fl = (m3 + m4) * 0x1p-8f;
                     // S + E += (t + te)(fh + fl)
                     const float pr = t * fh;
                     const float pe = fmaf(t, fh, -pr);
@@ -302,7 +302,7 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
             tc_fence_before();
             epi_bar_sync();                      // all TMEM reads and A-stage reads of this tile are done
             if (threadIdx.x == 64) {
-                mbar_arrive(&sh->tmem_empty);
+                mbar_arrive(&sh->tmem_empty[s]);
                 mbar_arrive(&sh->empty[s]);
             }
             rho[p] = 2.0 * ((double)S + (double)E) * ldexp(1.0, 2 * ep);
@@ -318,7 +318,7 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
 
 // ------------------------------------------------------------------ slicing
 
-// Phi (FP64, [nbf][npad]) -> 4 integer slices per element in the tile layout
+// Phi (FP64, [nbf][npad]) -> 4 pre-scaled integer slices per element in the tile layout
 __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const double *__restrict__ phi,
                             __nv_bfloat16 *__restrict__ A, int *__restrict__ row_exp)
 {
@@ -338,32 +338,34 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
             x *= 256.0;
             const double m = rint(x);
             x -= m;
-            A[(size_t)i * slice + o] = __float2bfloat16_rn((float)m);
+            A[(size_t)i * slice + o] = __float2bfloat16_rn((float)ldexp(m, -8 * i));
         }
     }
 }
 
-// P (FP64, nbf x nbf, symmetric) -> 4 integer slices per column in the B layout
+// P (FP64, nbf x nbf, symmetric) -> 4 pre-scaled integer slices per column in
+// the B layout: one warp per column, lanes over the rows
 __global__ void k_slice_P(int nbf, int KP, int NP, const double *__restrict__ P, __nv_bfloat16 *__restrict__ B,
                           int *__restrict__ col_exp)
 {
-    const int nu = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nu = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (nu >= NP) return;
     double mx = 0.0;
     if (nu < nbf)
-        for (int mu = 0; mu < nbf; ++mu) mx = fmax(mx, fabs(P[(size_t)nu * nbf + mu]));
+        for (int mu = lane; mu < nbf; mu += 32) mx = fmax(mx, fabs(P[(size_t)nu * nbf + mu]));
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     int e = 0;
     if (mx > 0.0) frexp(mx, &e);
-    if (nu < nbf) col_exp[nu] = e;
+    if (nu < nbf && lane == 0) col_exp[nu] = e;
     const size_t slice = (size_t)NP * KP;
-    for (int mu = 0; mu < KP; ++mu) {
+    for (int mu = lane; mu < KP; mu += 32) {
         double x = (nu < nbf && mu < nbf) ? ldexp(P[(size_t)nu * nbf + mu], -e) : 0.0;
         const size_t o = core_off(nu, mu, KP / 8) / 2;
         for (int i = 0; i < kTcSlices; ++i) {
             x *= 256.0;
             const double m = rint(x);
             x -= m;
-            B[(size_t)i * slice + o] = __float2bfloat16_rn((float)m);
+            B[(size_t)i * slice + o] = __float2bfloat16_rn((float)ldexp(m, -8 * i));
         }
     }
 }
@@ -402,8 +404,8 @@ int density_tc_setup(dftg_ctx *c)
 
 int launch_density_tc(dftg_ctx *c)
 {
-    k_slice_P<<<1, 128, 0, c->stream>>>(c->nbf, c->tc_KP, c->tc_NP, c->d_P,
-                                        reinterpret_cast<__nv_bfloat16 *>(c->d_tcB), c->d_tc_colexp);
+    k_slice_P<<<(c->tc_NP + 3) / 4, 128, 0, c->stream>>>(c->nbf, c->tc_KP, c->tc_NP, c->d_P,
+                                                         reinterpret_cast<__nv_bfloat16 *>(c->d_tcB), c->d_tc_colexp);
     DFTG_LAUNCH_CHECK();
     const int ntiles = (int)(c->npad / kTcTile);
     k_density_tc<<<c->tc_grid, kTcThreads, density_tc_smem(c->tc_KP, c->tc_NP), c->stream>>>(

@@ -23,7 +23,10 @@
 //     constant shared by many points carried as a split FP32 pair.
 // Mixed path of K5a/K5c: split-FP32 products (hi*hi + hi*lo + lo*hi), FP32
 //     partial sums of 16 terms added in FP64.
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
+#include <cstring>
 #include <vector>
 #include "dftg_internal.cuh"
 
@@ -576,78 +579,170 @@ __global__ void __launch_bounds__(128) k_vcross64(size_t npts, size_t npad, int 
     cj32[p] = (float)c;
 }
 
-// K5e (mixed): FP32 recursion with exact integer coefficients; every constant
-// shared by many points (Y_lm normalisation, spline coefficients) enters as a
-// split FP32 pair so no rounding is common to all points.  Per atom pair the
-// sums are carried in FP32 (hi and lo parts) and added to V in FP64.
-__global__ void __launch_bounds__(128) k_vcross_mixed(size_t npts, size_t npad, int natoms, int nrad, int nang,
-                                                      int lmax, const double *__restrict__ atoms,
-                                                      const double *__restrict__ X, const double *__restrict__ Yc,
-                                                      const double *__restrict__ Zc, const double *__restrict__ W,
-                                                      const double *__restrict__ sx, const float *__restrict__ splm,
-                                                      const double *__restrict__ Vown, double *__restrict__ V,
-                                                      double *__restrict__ cj, float *__restrict__ cj32)
+// K5e (mixed): FP32 recursion with exact integer coefficients; the spline
+// coefficients (which carry the Y_lm normalisation) enter as split FP32 hi/lo
+// pairs so no rounding is common to all points.  No FP64 work in the pair
+// loop: the per-atom contributions accumulate in an FP32 TwoSum pair and meet
+// the FP64 own-cell part once per point.
+// One thread per (point, other atom) pair.  The pairs are ordered by (atom,
+// spline interval) once per grid, so the lanes of a warp read the same spline
+// coefficients.  Writes the pair's contribution as an FP32 (hi, lo) pair.
+__global__ void __launch_bounds__(128) k_vcross_pairs(size_t npairs, int nrad, int lmax,
+                                                      const float4 *__restrict__ pgeo,
+                                                      const float2 *__restrict__ ptk,
+                                                      const float *__restrict__ splm, float2 *__restrict__ out)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= npairs) return;
+    const float4 g = pgeo[e];            // unit vector from atom k to the point, 1/r
+    const float2 tk = ptk[e];            // spline offset t, (k << 16 | interval)
+    const int nlm = (lmax + 1) * (lmax + 1);
+    const int N = nrad;
+    const uint32_t kv = __float_as_uint(tk.y);
+    const int k = (int)(kv >> 16), iv = (int)(kv & 0xffffu);
+    const float t = tk.x, inv_r = g.w;
+    const float ux = g.x, uy = g.y, uz = g.z;
+    const float4 *cf = reinterpret_cast<const float4 *>(splm + ((size_t)k * nlm * N + iv) * 8);
+    const size_t lstride = (size_t)N * 2;   // float4 units per lm
+    float ah = 0.f, al = 0.f, cm = 1.f, sm = 0.f;
+    for (int m = 0; m <= lmax; ++m) {
+        float r2 = 0.f, r1 = 1.f;
+        for (int l = m; l <= lmax; ++l) {
+            float q;
+            if (l == m) q = 1.f;
+            else {
+                q = (float)(2 * l - 1) * uz * r1 - (float)((l + m - 1) * (l - m - 1)) * r2;
+                r2 = r1;
+                r1 = q;
+            }
+            const int lp = l * l + l + m;
+            const float4 ch = cf[(size_t)lp * lstride];
+            const float4 cl = cf[(size_t)lp * lstride + 1];
+            const float sh = fmaf(t, fmaf(t, fmaf(t, ch.w, ch.z), ch.y), ch.x);
+            const float sl = fmaf(t, fmaf(t, fmaf(t, cl.w, cl.z), cl.y), cl.x);
+            if (m == 0) {
+                ah = fmaf(q, sh, ah);
+                al = fmaf(q, sl, al);
+            } else {
+                const int ln = l * l + l - m;
+                const float4 dh = cf[(size_t)ln * lstride];
+                const float4 dl = cf[(size_t)ln * lstride + 1];
+                const float nh = fmaf(t, fmaf(t, fmaf(t, dh.w, dh.z), dh.y), dh.x);
+                const float nl = fmaf(t, fmaf(t, fmaf(t, dl.w, dl.z), dl.y), dl.x);
+                const float qc = q * cm, qs = q * sm;
+                ah = fmaf(qc, sh, fmaf(qs, nh, ah));
+                al = fmaf(qc, sl, fmaf(qs, nl, al));
+            }
+        }
+        const float cn = cm * ux - sm * uy, sn2 = cm * uy + sm * ux;
+        cm = cn;
+        sm = sn2;
+    }
+    const float vh = inv_r * ah;
+    const float vl = fmaf(inv_r, ah, -vh) + inv_r * al;
+    out[e] = make_float2(vh, vl);
+}
+
+// total potential per point: own cell (FP64) plus the pair contributions in
+// atom order, summed with TwoSum; writes V and cj = w V / 2
+__global__ void k_vcross_gather(size_t npts, size_t npad, int natoms, int nrad, int nang,
+                                const int *__restrict__ pos, const float2 *__restrict__ pairv,
+                                const double *__restrict__ Vown, const double *__restrict__ W,
+                                double *__restrict__ V, double *__restrict__ cj, float *__restrict__ cj32)
 {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npad) return;
     if (p >= npts) { V[p] = 0.0; cj[p] = 0.0; cj32[p] = 0.f; return; }
-    const int nlm = (lmax + 1) * (lmax + 1);
-    const int N = nrad;
     const int a = (int)(p / ((size_t)nrad * nang));
-    const double px = X[p], py = Yc[p], pz = Zc[p];
-    const double fscale = (double)(N + 1) / kPi;
-    double Vt = 0.0;
+    float vh = 0.f, vl = 0.f;
     for (int k = 0; k < natoms; ++k) {
-        if (k == a) { Vt += Vown[p]; continue; }
-        const float dx = (float)(px - atoms[4 * k]), dy = (float)(py - atoms[4 * k + 1]),
-                    dz = (float)(pz - atoms[4 * k + 2]);
-        const float r = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-        int iv;
-        double td;
-        spline_interval((double)r, sx, N, fscale, iv, td);
-        const float t = (float)td;
-        const float inv_r = 1.0f / r;
-        const float ux = dx * inv_r, uy = dy * inv_r, uz = dz * inv_r;
-        const float4 *cf = reinterpret_cast<const float4 *>(splm + ((size_t)k * nlm * N + iv) * 8);
-        const size_t lstride = (size_t)N * 2;   // float4 units per lm
-        float ah = 0.f, al = 0.f, cm = 1.f, sm = 0.f;
-        for (int m = 0; m <= lmax; ++m) {
-            float r2 = 0.f, r1 = 1.f;
-            for (int l = m; l <= lmax; ++l) {
-                float q;
-                if (l == m) q = 1.f;
-                else {
-                    q = (float)(2 * l - 1) * uz * r1 - (float)((l + m - 1) * (l - m - 1)) * r2;
-                    r2 = r1;
-                    r1 = q;
-                }
-                const int lp = l * l + l + m;
-                const float4 ch = cf[(size_t)lp * lstride], cl = cf[(size_t)lp * lstride + 1];
-                const float sh = fmaf(t, fmaf(t, fmaf(t, ch.w, ch.z), ch.y), ch.x);
-                const float sl = fmaf(t, fmaf(t, fmaf(t, cl.w, cl.z), cl.y), cl.x);
-                if (m == 0) {
-                    ah = fmaf(q, sh, ah);
-                    al = fmaf(q, sl, al);
-                } else {
-                    const int ln = l * l + l - m;
-                    const float4 dh = cf[(size_t)ln * lstride], dl = cf[(size_t)ln * lstride + 1];
-                    const float nh = fmaf(t, fmaf(t, fmaf(t, dh.w, dh.z), dh.y), dh.x);
-                    const float nl = fmaf(t, fmaf(t, fmaf(t, dl.w, dl.z), dl.y), dl.x);
-                    const float qc = q * cm, qs = q * sm;
-                    ah = fmaf(qc, sh, fmaf(qs, nh, ah));
-                    al = fmaf(qc, sl, fmaf(qs, nl, al));
-                }
-            }
-            const float cn = cm * ux - sm * uy, sn2 = cm * uy + sm * ux;
-            cm = cn;
-            sm = sn2;
-        }
-        Vt += (double)inv_r * ((double)ah + (double)al);
+        if (k == a) continue;
+        const float2 v = pairv[pos[p * natoms + k]];
+        two_sum_acc(vh, vl, v.x);
+        vl += v.y;
     }
+    const double Vt = Vown[p] + ((double)vh + (double)vl);
     V[p] = Vt;
     const double c = 0.5 * (W[p] * Vt);
     cj[p] = c;
     cj32[p] = (float)c;
+}
+
+// Order the (point, other atom) pairs by (atom, spline interval of their
+// distance) with a counting sort; pos[p][k] is the place of pair (p, k).
+int cross_pairs_setup(dftg_ctx *c)
+{
+    const size_t n = c->npts;
+    const int na = c->natoms, N = c->nrad, per_atom = c->nrad * c->nang;
+    if (na < 2) { c->npairs = 0; return DFTG_OK; }
+    std::vector<double> X(n), Y(n), Z(n);
+    DFTG_CUDA(cudaMemcpy(X.data(), c->d_x, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    DFTG_CUDA(cudaMemcpy(Y.data(), c->d_y, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    DFTG_CUDA(cudaMemcpy(Z.data(), c->d_z, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    std::vector<double> sx(N);
+    for (int i = 0; i < N; ++i) sx[i] = c->r_n[N - 1 - i];
+    // interval and offset of the spline evaluation at distance r, the same
+    // rule as spline_interval(): clamp below the first and beyond the last knot
+    auto interval = [&](double r, int &iv, double &t) {
+        if (r < sx[0]) { iv = 0; t = 0.0; return; }
+        if (r >= sx[N - 1]) { iv = N - 1; t = 0.0; return; }
+        int i = (int)(std::lower_bound(sx.begin(), sx.end(), r) - sx.begin());
+        i = std::max(1, std::min(N - 1, i));
+        iv = i - 1;
+        t = r - sx[iv];
+    };
+    const size_t npairs = n * (size_t)(na - 1);
+    const int nkeys = na * N;
+    std::vector<int> key(npairs);
+    std::vector<size_t> count((size_t)nkeys + 1, 0);
+    size_t e = 0;
+    for (size_t p = 0; p < n; ++p) {
+        const int a = (int)(p / per_atom);
+        for (int k = 0; k < na; ++k) {
+            if (k == a) continue;
+            const double dx = X[p] - c->xyz[3 * k], dy = Y[p] - c->xyz[3 * k + 1], dz = Z[p] - c->xyz[3 * k + 2];
+            int iv;
+            double t;
+            interval(std::sqrt(dx * dx + dy * dy + dz * dz), iv, t);
+            key[e] = k * N + iv;
+            ++count[(size_t)key[e] + 1];
+            ++e;
+        }
+    }
+    for (int i = 0; i < nkeys; ++i) count[i + 1] += count[i];
+    // the geometry of a pair is fixed for the grid: direction, 1/r and the
+    // spline offset are formed in FP64 and rounded once to FP32
+    std::vector<float4> geo(npairs);
+    std::vector<float2> tk(npairs);
+    std::vector<int> pos(n * (size_t)na, 0);
+    e = 0;
+    for (size_t p = 0; p < n; ++p) {
+        const int a = (int)(p / per_atom);
+        for (int k = 0; k < na; ++k) {
+            if (k == a) continue;
+            const size_t dst = count[key[e++]]++;
+            const double dx = X[p] - c->xyz[3 * k], dy = Y[p] - c->xyz[3 * k + 1], dz = Z[p] - c->xyz[3 * k + 2];
+            const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+            int iv;
+            double t;
+            interval(r, iv, t);
+            geo[dst] = make_float4((float)(dx / r), (float)(dy / r), (float)(dz / r), (float)(1.0 / r));
+            uint32_t kv = ((uint32_t)k << 16) | (uint32_t)iv;
+            float kvf;
+            std::memcpy(&kvf, &kv, sizeof(kvf));
+            tk[dst] = make_float2((float)t, kvf);
+            pos[p * na + k] = (int)dst;
+        }
+    }
+    c->npairs = npairs;
+    DFTG_CUDA(cudaMalloc(&c->d_pairs, (sizeof(float4) + sizeof(float2)) * npairs));
+    DFTG_CUDA(cudaMalloc(&c->d_pairpos, sizeof(int) * pos.size()));
+    DFTG_CUDA(cudaMalloc(&c->d_pairv, sizeof(float2) * npairs));
+    char *base = static_cast<char *>(c->d_pairs);
+    DFTG_CUDA(cudaMemcpy(base, geo.data(), sizeof(float4) * npairs, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(base + sizeof(float4) * npairs, tk.data(), sizeof(float2) * npairs, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_pairpos, pos.data(), sizeof(int) * pos.size(), cudaMemcpyHostToDevice));
+    return DFTG_OK;
 }
 
 // E_J = 2 tr(P J) = sum_p (w V / 2) rho_raw (the J assembly contracted with P,
@@ -712,11 +807,18 @@ int launch_hartree(dftg_ctx *c)
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "splines");
     const unsigned nb = (unsigned)(c->npad / 128);
-    if (c->prec_mask & kPrecCross)
-        k_vcross_mixed<<<nb, 128, 0, c->stream>>>(c->npts, c->npad, c->natoms, N, c->nang, c->lmax, c->d_atoms,
-                                                  c->d_x, c->d_y, c->d_z, c->d_w, c->d_sx, c->d_splm, c->d_Vown,
-                                                  c->d_V, c->d_cj, c->d_cj32);
-    else
+    if (c->prec_mask & kPrecCross) {
+        if (c->npairs > 0) {
+            k_vcross_pairs<<<(unsigned)((c->npairs + 127) / 128), 128, 0, c->stream>>>(
+                c->npairs, N, c->lmax, reinterpret_cast<const float4 *>(c->d_pairs),
+                reinterpret_cast<const float2 *>(static_cast<const char *>(c->d_pairs) + sizeof(float4) * c->npairs),
+                c->d_splm, reinterpret_cast<float2 *>(c->d_pairv));
+            DFTG_LAUNCH_CHECK();
+        }
+        k_vcross_gather<<<(unsigned)((c->npad + 127) / 128), 128, 0, c->stream>>>(
+            c->npts, c->npad, c->natoms, N, c->nang, c->d_pairpos, reinterpret_cast<const float2 *>(c->d_pairv),
+            c->d_Vown, c->d_w, c->d_V, c->d_cj, c->d_cj32);
+    } else
         k_vcross64<<<nb, 128, 0, c->stream>>>(c->npts, c->npad, c->natoms, N, c->nang, c->lmax, c->d_atoms, c->d_x,
                                               c->d_y, c->d_z, c->d_w, c->d_sx, c->d_spl, c->d_pre, c->d_rec,
                                               c->d_Vown, c->d_V, c->d_cj, c->d_cj32);

@@ -149,11 +149,12 @@ def test_mixed_density_tensor_core_accuracy(gpu_lib, name, basis, nrad, leb):
     gmx.set_density(P)
     r64, rmx = g64.get_densities(), gmx.get_densities()
     # four 8-bit slices per operand: 2^-33 of the row and column scales per
-    # element, summed over nbf products (worst case ~1e-8 at the nuclei)
+    # element, summed over nbf products, plus the FP32 rounding of the low-order
+    # pairs (worst case a few 1e-8 at the nuclei)
     d = np.abs(rmx - r64)
-    tol = 3e-8 * np.abs(r64) + 1e-12 * np.abs(r64).max()
+    tol = 1e-7 * np.abs(r64) + 1e-12 * np.abs(r64).max()
     bad = np.argmax(d - tol)
     assert np.all(d <= tol), (float(d[bad]), float(r64[bad]), float(d.max()), float((d / np.maximum(r64, 1e-300)).max()))
     a, b = g64.fock_build(P), gmx.fock_build(P)
     assert abs(a["Exc"] - b["Exc"]) < 2e-7
-    assert abs(a["EJ"] - b["EJ"]) < 2e-6
+    assert abs(a["EJ"] - b["EJ"]) < 2e-9 * abs(a["EJ"])
