@@ -36,10 +36,10 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = "ms per SCF grid Fock build, mixed vs FP64 on one GB300 at |\u0394E_tot|\u22641e-6 Ha"
 WORKLOAD = {"workload": "benzene/6-31G grid Fock build", "molecule": "C6H6 D6h", "basis": "6-31G", "nbf": 66,
             "radial_points": 75, "lebedev_points": 302, "lmax": 8, "grid_points": 271800}
 
-# kernels launched per build, by profile phase (see dftcxx_gb300/csrc)
 # kernels launched per phase of one mixed-precision build (dftg_fock_build_device)
 KERNELS_PER_PHASE = {"density": 2, "charge": 2, "lda": 2, "rholm": 1, "poisson": 1, "vown": 1,
                      "splines": 1, "vcross": 2, "hartree_energy": 2, "contract": 1, "contract_reduce": 1}
@@ -119,6 +119,14 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def max_over_ranks(values, device="cpu"):
+    """Element-wise maximum of a list of floats over all ranks of the default group."""
+    import torch
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
 def _benzene_mol():
     from dftcxx_gb300.molecule import Molecule, benzene
     Z, xyz = benzene()
@@ -158,7 +166,7 @@ def run_reference(args, rank):
     ms = float(np.mean(times))
     sample = ("benzene/6-31G/75x302 Fock build per step; cross-atom potential, J and XC point loops "
               "on every %d-th point, their wall time scaled by %d" % (stride, stride))
-    return {"metric": "ms per SCF grid Fock build", "value": ms, "unit": "ms", "n_gpus": args.gpus,
+    return {"metric": METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic geometry (no dataset)",
             "config": dict(WORKLOAD, parallelism="host OpenMP"), "impl": "reference",
@@ -333,9 +341,7 @@ def run_ours(args, rank, world):
 
     # max over ranks
     if world > 1:
-        t = torch.tensor([ms_mx, ms_e2e, ms_64], dtype=torch.float64, device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_mx, ms_e2e, ms_64 = (float(x) for x in t.tolist())
+        ms_mx, ms_e2e, ms_64 = max_over_ranks([ms_mx, ms_e2e, ms_64], f"cuda:{dev}")
 
     # roofline of the dominant mixed-precision kernel
     hbm, _, peak_src = _peaks()
@@ -366,7 +372,7 @@ def run_ours(args, rank, world):
         r = run_reference(ref_args, 0)
         cpu = r["cpu_baseline"]
 
-    return {"metric": "ms per SCF grid Fock build (mixed precision)", "value": ms_mx, "unit": "ms",
+    return {"metric": METRIC, "value": ms_mx, "unit": "ms",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mx,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32-split/f64",
             "data": "synthetic geometry (no dataset)",

@@ -20,6 +20,8 @@ DFTG_ERR_TIMEOUT = 6
 DFTG_PREC_FP64 = 0
 DFTG_PREC_MIXED = 1
 DFTG_LEBEDEV_302 = 11
+NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
+NOALLOC_MAX_NBF = 1024
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)

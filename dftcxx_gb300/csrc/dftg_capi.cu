@@ -162,7 +162,11 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(dalloc(&c->d_P32, nn));
     DFTG_TRY(dalloc(&c->d_J, nn));
     DFTG_TRY(dalloc(&c->d_XC, nn));
+    int nsm = 0;
+    DFTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     size_t part = contract_part_elems(c->nbf, c->npad);
+    const size_t part_tc = contract_tc_part_elems(c->nbf, c->npad, nsm);
+    if (part_tc > part) part = part_tc;
     const size_t spline_work = 2 * (size_t)c->natoms * nlm * N;
     c->part_elems = part > spline_work ? part : spline_work;
     DFTG_TRY(dalloc(&c->d_part, c->part_elems));
@@ -215,6 +219,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(launch_amplitudes(c));
     DFTG_TRY(hartree_setup(c));
     DFTG_TRY(contract_setup(c));
+    DFTG_TRY(contract_tc_setup(c));
     DFTG_TRY(density_tc_setup(c));
     DFTG_TRY(cross_pairs_setup(c));
     DFTG_CUDA(cudaStreamSynchronize(c->stream));

@@ -136,6 +136,10 @@ struct dftg_ctx {
     int *d_tc_colexp = nullptr;   // [NP] per-column scale exponents of P
     int *d_flag = nullptr;        // device error flag (bounded waits that expired)
 
+    // device: tensor-core XC / J contraction (split-K over point chunks)
+    bool ct_ready = false;
+    int ct_NP = 0, ct_nst = 0, ct_nkb = 0, ct_kbpc = 0, ct_nchunk = 0, ct_grid = 0;
+
     // device: one-electron integrals output (allocated on first use)
     double *d_ints_work = nullptr;
 
@@ -202,5 +206,9 @@ int contract_setup(dftg_ctx *c);
 size_t contract_part_elems(int nbf, size_t npad);
 size_t reduction_elems(size_t npad, int natoms, int nrad, int nang);
 int launch_contract(dftg_ctx *c, bool want_xc, bool want_j);
+// k_contract_tc.cu
+size_t contract_tc_part_elems(int nbf, size_t npad, int nsm);
+int contract_tc_setup(dftg_ctx *c);
+int launch_contract_tc(dftg_ctx *c);
 
 }  // namespace dftg

@@ -161,12 +161,23 @@ int contract_setup(dftg_ctx *c)
 
 int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
 {
+    const int wx = want_xc ? 1 : 0, wj = want_j ? 1 : 0;
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    if ((c->prec_mask & kPrecContract) && c->ct_ready) {
+        // tensor-core form: full nbf x nbf partials per point chunk, upper triangle kept
+        DFTG_TRY_L(launch_contract_tc(c));
+        DFTG_MARK(c, "contract");
+        k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, 1, c->ct_nchunk, wx, wj,
+                                                                            c->d_part, c->d_XC, c->d_J);
+        DFTG_LAUNCH_CHECK();
+        DFTG_MARK(c, "contract_reduce");
+        return DFTG_OK;
+    }
     const int R = tile_R(c->nbf), tile = 16 * R;
     const int2 *d_tiles = reinterpret_cast<const int2 *>(c->d_tiles);
     size_t per = (c->npad + c->nchunk - 1) / c->nchunk;
     per = (per + kKB - 1) / kKB * kKB;
     dim3 grid((unsigned)c->ntiles, (unsigned)c->nchunk);
-    const int wx = want_xc ? 1 : 0, wj = want_j ? 1 : 0;
     if (!(c->prec_mask & kPrecContract)) {
         if (R == 5) k_contract<double, 5><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
         else k_contract<double, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
@@ -176,7 +187,6 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
     }
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "contract");
-    const size_t nn = (size_t)c->nbf * c->nbf;
     k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, tile, c->nchunk, wx, wj, c->d_part,
                                                                         c->d_XC, c->d_J);
     DFTG_LAUNCH_CHECK();

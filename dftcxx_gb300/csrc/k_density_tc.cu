@@ -31,6 +31,7 @@
 #include <cuda_bf16.h>
 #include <cstdint>
 #include "dftg_internal.cuh"
+#include "tc_common.cuh"
 
 namespace dftg {
 
@@ -39,109 +40,6 @@ constexpr int kTcTile = 128;
 constexpr int kTcMaxK = 80;                   // nbf <= 80 for this kernel
 constexpr int kTcThreads = 192;
 constexpr uint32_t kTcTmemCols = 512;
-constexpr unsigned long long kWaitLimit = 1ull << 27;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
-{
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
-{
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-// bounded wait for the phase of the given parity; false on expiry
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
-{
-    const uint32_t a = smem_u32(bar);
-    for (unsigned long long it = 0; it < kWaitLimit; ++it) {
-        uint32_t done;
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-                     : "=r"(done)
-                     : "r"(a), "r"(parity)
-                     : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-
-// shared-memory matrix descriptor, no swizzle, K-major core matrices
-__device__ __forceinline__ uint64_t smem_desc(const void *base, uint32_t lbo, uint32_t sbo)
-{
-    const uint64_t a = (uint64_t)((smem_u32(base) >> 4) & 0x3FFF);
-    return a | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
-}
-
-// instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
-{
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
-{
-    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-                 "l"(a), "l"(b), "r"(idesc), "r"(acc)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t *bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
-{
-    uint32_t r[16];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-                 : "r"(taddr));
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void epi_bar_sync()   // named barrier of the 4 epilogue warps
-{
-    asm volatile("bar.sync 1, 128;" ::: "memory");
-}
-
-// byte offset of element (row, k) inside a K-major no-swizzle block whose K
-// extent holds `kcores` core matrices: cores ordered row group by row group,
-// so LBO (next core along K) = 128 B and SBO (next row group) = kcores * 128 B;
-// every address the MMA forms stays inside the block
-__host__ __device__ __forceinline__ uint32_t core_off(int row, int k, int kcores)
-{
-    return (uint32_t)(((row >> 3) * kcores + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
-}
-
 struct TcShared {
     uint64_t full[2], empty[2], tmem_full[2], tmem_empty[2];
     uint32_t tmem_base;
@@ -388,8 +286,10 @@ int density_tc_setup(dftg_ctx *c)
     DFTG_CUDA(cudaMalloc(&c->d_tc_rowexp, sizeof(int) * c->npad));
     DFTG_CUDA(cudaMalloc(&c->d_tcB, sizeof(__nv_bfloat16) * kTcSlices * c->tc_NP * c->tc_KP));
     DFTG_CUDA(cudaMalloc(&c->d_tc_colexp, sizeof(int) * c->tc_NP));
-    DFTG_CUDA(cudaMalloc(&c->d_flag, sizeof(int)));
-    DFTG_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
+    if (!c->d_flag) {
+        DFTG_CUDA(cudaMalloc(&c->d_flag, sizeof(int)));
+        DFTG_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
+    }
     k_slice_phi<<<(unsigned)((c->npad + 127) / 128), 128, 0, c->stream>>>(
         c->nbf, c->tc_KP, c->npad, ntiles, c->d_phi, reinterpret_cast<__nv_bfloat16 *>(c->d_tcA), c->d_tc_rowexp);
     DFTG_LAUNCH_CHECK();
