@@ -77,7 +77,7 @@ static void free_ctx(dftg_ctx *c)
                     c->d_rec32, c->d_rholm, c->d_U, c->d_U32, c->d_Y32, c->d_Ywt32, c->d_fold, c->d_Gt,
                     c->d_Gb, c->d_Kt, c->d_sx, c->d_splf, c->d_spl, c->d_splm, c->d_tiles,
                     c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_flag,
-                    c->d_pairs, c->d_pairpos, c->d_pairv};
+                    c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);

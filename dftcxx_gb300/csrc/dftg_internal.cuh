@@ -120,6 +120,8 @@ struct dftg_ctx {
     size_t npairs = 0;            // (point, other atom) pairs of the cross-atom potential
     void *d_pairs = nullptr;      // [npairs] float4 (unit vector, 1/r) then [npairs] float2 (t, k << 16 | interval),
                                   // ordered by (atom, spline interval)
+    void *d_cross_tasks = nullptr; // [ncross_tasks] int4 (first pair, pairs, atom, interval)
+    int ncross_tasks = 0;
     int *d_pairpos = nullptr;     // [npts][natoms] place of pair (p, k) in d_pairs
     void *d_pairv = nullptr;      // [npairs] float2 contributions
     double *d_sx = nullptr;       // [nrad] increasing spline abscissae
@@ -138,7 +140,10 @@ struct dftg_ctx {
 
     // device: tensor-core XC / J contraction (split-K over point chunks)
     bool ct_ready = false;
-    int ct_NP = 0, ct_nst = 0, ct_nkb = 0, ct_kbpc = 0, ct_nchunk = 0, ct_grid = 0;
+    int ct_NP = 0, ct_AR = 0, ct_nst = 0, ct_spart = 0, ct_nkb = 0, ct_kbpc = 0, ct_nchunk = 0, ct_grid = 0;
+    int *d_ct_rowexp = nullptr;   // [2][nchunk][nbf] exponent bounds of |phi| and |w phi| per point chunk
+    float *d_ct_winv = nullptr;   // [npad] 1 / w (0 where w vanishes)
+    void *d_ct_A = nullptr;       // [nkb][3][AR x 32] BF16 slices of phi, shared-memory operand layout
 
     // device: one-electron integrals output (allocated on first use)
     double *d_ints_work = nullptr;
@@ -210,5 +215,6 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j);
 size_t contract_tc_part_elems(int nbf, size_t npad, int nsm);
 int contract_tc_setup(dftg_ctx *c);
 int launch_contract_tc(dftg_ctx *c);
+int launch_contract_tc_reduce(dftg_ctx *c, bool want_xc, bool want_j);
 
 }  // namespace dftg

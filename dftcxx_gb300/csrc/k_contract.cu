@@ -164,12 +164,10 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
     const int wx = want_xc ? 1 : 0, wj = want_j ? 1 : 0;
     const size_t nn = (size_t)c->nbf * c->nbf;
     if ((c->prec_mask & kPrecContract) && c->ct_ready) {
-        // tensor-core form: full nbf x nbf partials per point chunk, upper triangle kept
+        // tensor-core form: full nbf x nbf partials per CTA, upper triangle kept
         DFTG_TRY_L(launch_contract_tc(c));
         DFTG_MARK(c, "contract");
-        k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, 1, c->ct_nchunk, wx, wj,
-                                                                            c->d_part, c->d_XC, c->d_J);
-        DFTG_LAUNCH_CHECK();
+        DFTG_TRY_L(launch_contract_tc_reduce(c, want_xc, want_j));
         DFTG_MARK(c, "contract_reduce");
         return DFTG_OK;
     }

@@ -3,25 +3,36 @@
 //
 //   XC = phi^T diag(c_xc) phi,   J = phi^T diag(c_j) phi,   c_xc = w v_xc, c_j = w V / 2
 //
-// as one GEMM per point chunk, D[mu][n] = sum_p A[mu][p] B[n][p], with
-//   A = phi (rows mu < nbf of M = 128),
-//   B = [c_xc o phi ; c_j o phi] (rows n < 2 nbf of N = NP, NP = 2 nbf rounded up to 16),
-// K = points.  Both operands are split into NS BF16 slices, x = x_1 + x_2 (+ x_3),
-// x_{i+1} = bf16(x - x_1 - ... - x_i), so the FP32 inputs are carried to 16 (NS = 2)
-// or 24 (NS = 3) bits.  The products are accumulated in two TMEM accumulators:
-//   D_hi = A_1 B_1                          (the leading term)
-//   D_lo = A_1 B_2 + A_2 B_1 (+ A_1 B_3 + A_2 B_2 + A_3 B_1)
-// so the rounding of the small terms is not charged to the leading sum.  The point
-// dimension is cut into nchunk chunks; each chunk's D_hi + D_lo is written as an
-// FP64 partial and the partials are summed in a fixed order by k_contract_reduce,
-// which also symmetrises the result.
+// as one GEMM per point chunk, D[mu][n] = sum_p A[mu][p] B[n][p], K = points:
+//   A = phi                         rows mu < nbf of M = 128
+//   B = [c_xc o phi ; c_j o phi]    rows n < 2 nbf of N = NP (2 nbf rounded up to 16)
 //
-// CTA (persistent over chunks): warps 0-3 produce operand stages from the FP32
-// amplitudes and point coefficients (coalesced loads, BF16 slicing, canonical
-// no-swizzle K-major core matrices in shared memory, then a proxy fence); warp 4
-// owns TMEM and issues the MMAs from one thread; warps 5-8 drain the accumulators.
+// Number format (per point chunk of at most 256 points).  Row mu of A is scaled
+// by 2^(7 - e_mu), e_mu the exponent bound of max |phi_mu| over the chunk, and
+// split into three BF16 slices: a_1 = rint(x) (an integer, |a_1| <= 128),
+// a_2 = bf16(x - a_1), a_3 = bf16(x - a_1 - a_2).  B row nu is scaled by
+// 2^(7 - s_nu - v), s_nu the bound of max |w phi_nu| over the chunk (fixed for
+// the grid) and v the bound of max |c / w| (per build), and split likewise.  The
+// leading products a_1 b_1 are integers below 2^14, so their sum over a chunk
+// (< 2^22) is exact in the FP32 accumulator whatever the accumulator's
+// rounding; the five correction products (a_1 b_2, a_2 b_1, a_1 b_3, a_2 b_2,
+// a_3 b_1) go to a second accumulator, about 2^-8 of the first.  The epilogue
+// scales D_hi and D_lo back by exact powers of two and adds them to the CTA's
+// partial, a double-float (FP32 hi + lo, TwoSum) matrix in shared memory, so
+// no FP64 arithmetic (slow on this GPU) runs per chunk; k_contract_tc_reduce
+// sums the CTA partials in FP64 in a fixed order and symmetrises.  A (phi is fixed for the grid) is sliced once at setup into HBM
+// in the shared-memory operand layout; B is formed every build from A and c.
+//
+// CTA (persistent over chunks, 448 threads):
+//   warps 0-3  producers: warp w builds the B slices of the stages in ring slots
+//              w, w + 4, ... from the A slices and c values of the stage (shared
+//              memory), then a proxy fence and an mbarrier arrive;
+//   warp 4     TMEM owner and MMA issuer (one thread);
+//   warps 5-12 epilogue: TMEM -> FP64 partial (TMEM lane quarter = warp % 4,
+//              alternate 16-column blocks for the two warps of a quarter);
+//   warp 13    loader: bulk copies of the A slices and c values of each stage.
 // Every mbarrier wait is bounded: on expiry the CTA records an error code, lets
-// its MMAs complete, frees TMEM and exits.
+// its copies and MMAs complete, frees TMEM and exits.
 #include <cuda_bf16.h>
 #include <cstdint>
 #include "dftg_internal.cuh"
@@ -33,67 +44,121 @@ constexpr int kCtKS = 32;                  // points per stage
 constexpr int kCtKcores = kCtKS / 8;       // core matrices along K per stage
 constexpr int kCtM = 128;
 constexpr int kCtMaxNbf = 128;             // 2 nbf <= 256 columns per accumulator
-constexpr int kCtThreads = 288;
+constexpr int kCtThreads = 448;
+constexpr int kCtLoaderWarp = 13;
 constexpr int kCtMaxStages = 8;
-constexpr int kCtMaxKbPerChunk = 32;       // at most 1024 points per FP32 accumulation
+constexpr int kCtMaxKbPerChunk = 8;        // <= 256 points per exact integer accumulation
 constexpr uint32_t kCtTmemCols = 512;      // D_hi at column 0, D_lo at column 256
 constexpr int kCtSlices = 3;
+constexpr int kCtExpMin = -100;            // exponent bounds are clamped to [-100, 100]
+constexpr int kCtExpMax = 100;
 
 struct CtShared {
-    uint64_t full[kCtMaxStages], empty[kCtMaxStages];
+    uint64_t a_full[kCtMaxStages];         // A slices and c values landed (bulk copies)
+    uint64_t full[kCtMaxStages];           // B slices written (producer warp)
+    uint64_t empty[kCtMaxStages];          // MMAs done with the stage
     uint64_t tmem_full, tmem_empty, drain;
     uint32_t tmem_base;
     int fail;
 };
 
-__device__ __forceinline__ void ct_epi_bar()
+__device__ __forceinline__ void ct_epi_bar()   // named barrier 1 over the 8 epilogue warps
 {
-    asm volatile("bar.sync 1, 128;" ::: "memory");
+    asm volatile("bar.sync 1, 256;" ::: "memory");
 }
 
-// eight consecutive K values -> NS packed BF16 slices (16 bytes each)
-template <int NS>
-__device__ __forceinline__ void slice8(const float (&v)[8], uint4 (&out)[NS])
+__device__ __forceinline__ float pow2f(int k)   // 2^k, -126 <= k <= 127
 {
-    uint32_t w[NS][4];
+    return __int_as_float((127 + k) << 23);
+}
+
+// exponent e with |x| < 2^e for the largest |x| given as FP32 bits, clamped
+__device__ __forceinline__ int exp_bound(uint32_t absbits)
+{
+    const int e = (int)(absbits >> 23) - 126;
+    return e < kCtExpMin ? kCtExpMin : (e > kCtExpMax ? kCtExpMax : e);
+}
+
+// eight consecutive K values (scaled, |x| < 128) -> three BF16 slices, the
+// first an integer
+__device__ __forceinline__ void slice8_fixed(const float (&v)[8], uint4 (&out)[kCtSlices])
+{
+    uint32_t w[kCtSlices][4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         float x0 = v[2 * j], x1 = v[2 * j + 1];
-#pragma unroll
-        for (int i = 0; i < NS; ++i) {
-            const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);   // .x (low half) = x0
-            w[i][j] = *reinterpret_cast<const uint32_t *>(&h);
-            if (i + 1 < NS) {
-                const float2 f = __bfloat1622float2(h);
-                x0 -= f.x;                                             // exact in FP32
-                x1 -= f.y;
-            }
-        }
+        const float i0 = rintf(x0), i1 = rintf(x1);
+        const __nv_bfloat162 h1 = __floats2bfloat162_rn(i0, i1);   // exact: integers <= 128
+        x0 -= i0;                                                  // exact
+        x1 -= i1;
+        const __nv_bfloat162 h2 = __floats2bfloat162_rn(x0, x1);
+        const float2 f2 = __bfloat1622float2(h2);
+        const __nv_bfloat162 h3 = __floats2bfloat162_rn(x0 - f2.x, x1 - f2.y);
+        w[0][j] = *reinterpret_cast<const uint32_t *>(&h1);
+        w[1][j] = *reinterpret_cast<const uint32_t *>(&h2);
+        w[2][j] = *reinterpret_cast<const uint32_t *>(&h3);
     }
 #pragma unroll
-    for (int i = 0; i < NS; ++i) out[i] = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+    for (int i = 0; i < kCtSlices; ++i) out[i] = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+}
+
+__device__ __forceinline__ void unpack8(uint4 u, float (&v)[8])
+{
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        v[2 * j] = __uint_as_float(w[j] << 16);
+        v[2 * j + 1] = __uint_as_float(w[j] & 0xffff0000u);
+    }
+}
+
+// warp-wide exponent bounds of max |c_xc / w| and max |c_j / w| over points [p0, p1)
+__device__ __forceinline__ void chunk_v_exps(const float *__restrict__ cxc, const float *__restrict__ cj,
+                                             const float *__restrict__ winv, size_t p0, size_t p1, int lane,
+                                             int &ex, int &ej)
+{
+    float mx = 0.f, mj = 0.f;
+    for (size_t p = p0 + 4 * lane; p < p1; p += 128) {
+        const float4 a = *reinterpret_cast<const float4 *>(cxc + p);
+        const float4 b = *reinterpret_cast<const float4 *>(cj + p);
+        const float4 u = *reinterpret_cast<const float4 *>(winv + p);
+        mx = fmaxf(mx, fmaxf(fmaxf(fabsf(a.x) * u.x, fabsf(a.y) * u.y), fmaxf(fabsf(a.z) * u.z, fabsf(a.w) * u.w)));
+        mj = fmaxf(mj, fmaxf(fmaxf(fabsf(b.x) * u.x, fabsf(b.y) * u.y), fmaxf(fabsf(b.z) * u.z, fabsf(b.w) * u.w)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mj = fmaxf(mj, __shfl_xor_sync(0xffffffffu, mj, o));
+    }
+    ex = exp_bound(__float_as_uint(mx));
+    ej = exp_bound(__float_as_uint(mj));
 }
 
 __host__ __device__ constexpr uint32_t ct_a_slice_bytes() { return (uint32_t)kCtM * kCtKS * 2; }
 __host__ __device__ constexpr uint32_t ct_b_slice_bytes(int NP) { return (uint32_t)NP * kCtKS * 2; }
-__host__ __device__ constexpr uint32_t ct_stage_bytes(int NS, int NP)
+__host__ __device__ constexpr uint32_t ct_stage_bytes(int NP)
 {
-    return (uint32_t)NS * (ct_a_slice_bytes() + ct_b_slice_bytes(NP));
+    return (uint32_t)kCtSlices * (ct_a_slice_bytes() + ct_b_slice_bytes(NP)) + 2 * kCtKS * 4;
 }
 
-template <int NS>
 __global__ void __launch_bounds__(kCtThreads, 1)
-k_contract_tc(int nbf, int NP, int nst, int nkb, int kb_per_chunk, int nchunk, size_t npad,
-              const float *__restrict__ phi, const float *__restrict__ cxc, const float *__restrict__ cj,
-              double *__restrict__ part, int *__restrict__ err)
+k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_chunk, int nchunk,
+              const unsigned char *__restrict__ aslices, const int *__restrict__ rowexp,
+              const int *__restrict__ swexp, const float *__restrict__ winv, const float *__restrict__ cxc,
+              const float *__restrict__ cj, float2 *__restrict__ part, int *__restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const uint32_t a_slice = ct_a_slice_bytes(), b_slice = ct_b_slice_bytes(NP);
-    const uint32_t stage = ct_stage_bytes(NS, NP);
-    CtShared *sh = reinterpret_cast<CtShared *>(smem + (size_t)nst * stage);
+    const uint32_t stage = ct_stage_bytes(NP);
+    const uint32_t c_off = kCtSlices * (a_slice + b_slice);     // c_xc[32], c_j[32] of the stage
+    const uint32_t a_hbm = (uint32_t)AR * kCtKS * 2;           // bytes of one A slice block in HBM
+    // CTA partial [2][nbf][nbf] double-float in shared memory when spart (else in HBM / L2)
+    float2 *s_part = reinterpret_cast<float2 *>(smem + (size_t)nst * stage);
+    CtShared *sh = reinterpret_cast<CtShared *>(smem + (size_t)nst * stage +
+                                                (spart ? 2 * (size_t)nbf * nbf * sizeof(float2) : 0));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    // zero the operand stages once: rows >= nbf of A and >= 2 nbf of B are never written
+    // zero the operand stages once: rows >= AR of A and >= 2 nbf of B are never written
     {
         uint4 *z = reinterpret_cast<uint4 *>(smem);
         const int n16 = (int)((size_t)nst * stage / 16);
@@ -102,8 +167,9 @@ k_contract_tc(int nbf, int NP, int nst, int nkb, int kb_per_chunk, int nchunk, s
     }
     if (threadIdx.x == 0) {
         for (int s = 0; s < nst; ++s) {
-            mbar_init(&sh->full[s], 1);          // the producing warp
-            mbar_init(&sh->empty[s], 1);         // MMA commit
+            mbar_init(&sh->a_full[s], 1);
+            mbar_init(&sh->full[s], 1);
+            mbar_init(&sh->empty[s], 1);
         }
         mbar_init(&sh->tmem_full, 1);
         mbar_init(&sh->tmem_empty, 1);
@@ -124,71 +190,63 @@ k_contract_tc(int nbf, int NP, int nst, int nkb, int kb_per_chunk, int nchunk, s
 
     if (warp < 4) {
         // ------------------------------------------------------------ producers
-        // warp w fills stages w, w + 4, ... of this CTA's sequence, so four
-        // stages are in preparation at once; lane = (row group of 8 mu) x (8-point group g)
-        const int g = lane & 3, mrow = lane >> 2;
+        const int g = lane & 3, mrow = lane >> 2;      // 8-point group, row within a group of 8 rows
         int it = 0;
         bool ok = true;
         for (int ch = blockIdx.x; ch < nchunk && ok; ch += gridDim.x) {
             const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
+            int ex, ej;
+            chunk_v_exps(cxc, cj, winv, (size_t)kb0 * kCtKS, (size_t)kb1 * kCtKS, lane, ex, ej);
+            const float sx = pow2f(-ex), sj = pow2f(-ej);
+            const int *ea = rowexp + (size_t)ch * nbf, *es = swexp + (size_t)ch * nbf;
             for (int kb = kb0; kb < kb1; ++kb, ++it) {
-                if ((it & 3) != warp) continue;
+                // each ring slot has exactly one producer warp (slot % 4), which
+                // therefore waits on the slot's phases strictly in order
                 const int s = it % nst, n = it / nst;
+                if ((s & 3) != warp) continue;
                 int w_ok = 1;
-                if (lane == 0) w_ok = mbar_wait(&sh->empty[s], (uint32_t)((n & 1) ^ 1)) ? 1 : 0;
+                if (lane == 0) w_ok = mbar_wait(&sh->a_full[s], (uint32_t)(n & 1)) ? 1 : 0;
                 w_ok = __shfl_sync(0xffffffffu, w_ok, 0);
                 if (!w_ok || sh->fail) {
                     if (lane == 0 && !w_ok) { atomicExch(err, 11); sh->fail = 1; }
                     ok = false;
                     break;
                 }
-                const size_t p = (size_t)kb * kCtKS + 8 * g;
-                const float4 x0 = *reinterpret_cast<const float4 *>(cxc + p);
-                const float4 x1 = *reinterpret_cast<const float4 *>(cxc + p + 4);
-                const float4 j0 = *reinterpret_cast<const float4 *>(cj + p);
-                const float4 j1 = *reinterpret_cast<const float4 *>(cj + p + 4);
-                const float cx[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
-                const float cy[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
                 unsigned char *sA = smem + (size_t)s * stage;
-                unsigned char *sB = sA + NS * a_slice;
-                constexpr int U = 3;
-                for (int base = 0; base < nbf; base += 8 * U) {
-                    float4 f[U][2];
+                unsigned char *sB = sA + kCtSlices * a_slice;
+                const float *sc = reinterpret_cast<const float *>(sA + c_off);
+                float cx[8], cy[8];
 #pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        const int mu = base + 8 * u + mrow;
-                        if (mu < nbf) {
-                            f[u][0] = *reinterpret_cast<const float4 *>(phi + (size_t)mu * npad + p);
-                            f[u][1] = *reinterpret_cast<const float4 *>(phi + (size_t)mu * npad + p + 4);
-                        } else {
-                            f[u][0] = make_float4(0.f, 0.f, 0.f, 0.f);
-                            f[u][1] = f[u][0];
-                        }
+                for (int k = 0; k < 8; ++k) {
+                    cx[k] = sc[8 * g + k] * sx;
+                    cy[k] = sc[kCtKS + 8 * g + k] * sj;
+                }
+                for (int mu = mrow; mu < nbf; mu += 8) {
+                    const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
+                    // B row scale: phi 2^(7 - e_mu) -> phi 2^(7 - s_mu)
+                    const float rf = pow2f(max(-126, min(127, ea[mu] - es[mu])));
+                    float v[8], t[8];
+                    unpack8(*reinterpret_cast<const uint4 *>(sA + oa), v);
+                    unpack8(*reinterpret_cast<const uint4 *>(sA + a_slice + oa), t);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) v[k] += t[k];
+                    unpack8(*reinterpret_cast<const uint4 *>(sA + 2 * a_slice + oa), t);
+                    float bx[8], by[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        v[k] += t[k];                          // phi 2^(7 - e_mu), |v| < 128
+                        const float u = v[k] * rf;
+                        bx[k] = cx[k] * u;                     // c phi 2^(7 - s_mu - v), |bx| < 128
+                        by[k] = cy[k] * u;
                     }
+                    uint4 sbx[kCtSlices], sby[kCtSlices];
+                    slice8_fixed(bx, sbx);
+                    slice8_fixed(by, sby);
+                    const uint32_t oj = core_off(nbf + mu, 8 * g, kCtKcores);
 #pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        const int mu = base + 8 * u + mrow;
-                        if (mu >= nbf) continue;
-                        const float v[8] = {f[u][0].x, f[u][0].y, f[u][0].z, f[u][0].w,
-                                            f[u][1].x, f[u][1].y, f[u][1].z, f[u][1].w};
-                        float bx[8], by[8];
-#pragma unroll
-                        for (int k = 0; k < 8; ++k) {
-                            bx[k] = cx[k] * v[k];
-                            by[k] = cy[k] * v[k];
-                        }
-                        uint4 sa[NS], sbx[NS], sby[NS];
-                        slice8<NS>(v, sa);
-                        slice8<NS>(bx, sbx);
-                        slice8<NS>(by, sby);
-                        const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
-                        const uint32_t oj = core_off(nbf + mu, 8 * g, kCtKcores);
-#pragma unroll
-                        for (int i = 0; i < NS; ++i) {
-                            *reinterpret_cast<uint4 *>(sA + i * a_slice + oa) = sa[i];
-                            *reinterpret_cast<uint4 *>(sB + i * b_slice + oa) = sbx[i];
-                            *reinterpret_cast<uint4 *>(sB + i * b_slice + oj) = sby[i];
-                        }
+                    for (int i = 0; i < kCtSlices; ++i) {
+                        *reinterpret_cast<uint4 *>(sB + i * b_slice + oa) = sbx[i];
+                        *reinterpret_cast<uint4 *>(sB + i * b_slice + oj) = sby[i];
                     }
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -219,14 +277,14 @@ k_contract_tc(int nbf, int NP, int nst, int nkb, int kb_per_chunk, int nchunk, s
                     }
                     tc_fence_after();
                     const unsigned char *sA = smem + (size_t)s * stage;
-                    const unsigned char *sB = sA + NS * a_slice;
+                    const unsigned char *sB = sA + kCtSlices * a_slice;
 #pragma unroll
                     for (int kk = 0; kk < kCtKS / 16; ++kk) {
                         const uint32_t ko = (uint32_t)kk * 2 * lbo;
 #pragma unroll
-                        for (int i = 0; i < NS; ++i)
+                        for (int i = 0; i < kCtSlices; ++i)
 #pragma unroll
-                            for (int j = 0; i + j < NS; ++j) {
+                            for (int j = 0; i + j < kCtSlices; ++j) {
                                 const uint64_t ad = smem_desc(sA + i * a_slice + ko, lbo, sbo);
                                 const uint64_t bd = smem_desc(sB + j * b_slice + ko, lbo, sbo);
                                 if (i == 0 && j == 0) {
@@ -248,32 +306,61 @@ k_contract_tc(int nbf, int NP, int nst, int nkb, int kb_per_chunk, int nchunk, s
             mbar_wait(&sh->drain, 0);
         }
         __syncwarp();
-    } else {
+    } else if (warp < kCtLoaderWarp) {
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3;                  // TMEM lane quarter of this warp
+        const int h = (warp - 5) >> 2;           // column blocks h, h + 2, ...
         const int r = q * 32 + lane;             // accumulator row = basis function mu
         const size_t nn = (size_t)nbf * nbf;
+        float2 *gpart = part + (size_t)blockIdx.x * 2 * nn;   // this CTA's partial in HBM
+        float2 *px = spart ? s_part : gpart;
         int cc = 0;
         for (int ch = blockIdx.x; ch < nchunk; ch += gridDim.x, ++cc) {
+            const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
+            int ex, ej;
+            chunk_v_exps(cxc, cj, winv, (size_t)kb0 * kCtKS, (size_t)kb1 * kCtKS, lane, ex, ej);
+            const int *ea = rowexp + (size_t)ch * nbf, *es = swexp + (size_t)ch * nbf;
+            const int er = r < nbf ? ea[r] : 0;
             const bool ok = mbar_wait(&sh->tmem_full, (uint32_t)(cc & 1));
             if (!ok) { atomicExch(err, 14); sh->fail = 1; }
             ct_epi_bar();
             if (sh->fail) break;
             tc_fence_after();
             const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16);
-            double *px = part + (size_t)ch * 2 * nn;
-            for (int c0 = 0; c0 < NP; c0 += 16) {
+            for (int c0 = 16 * h; c0 < NP; c0 += 32) {
                 float dh[16], dl[16];
                 tmem_ld16(ta + (uint32_t)c0, dh);
                 tmem_ld16(ta + 256u + (uint32_t)c0, dl);
                 tmem_wait_ld();
                 if (r < nbf) {
+                    // all loads of the block before its stores, so they are in flight together
+                    float2 old[16];
 #pragma unroll
                     for (int k = 0; k < 16; ++k) {
-                        const int nu = c0 + k;
-                        const double v = (double)dh[k] + (double)dl[k];
-                        if (nu < nbf) px[(size_t)nu * nbf + r] = v;
-                        else if (nu < 2 * nbf) px[nn + (size_t)(nu - nbf) * nbf + r] = v;
+                        const int n = c0 + k;
+                        old[k] = make_float2(0.f, 0.f);
+                        if (cc > 0 && n < 2 * nbf)
+                            old[k] = px[(n < nbf ? 0 : nn) + (size_t)(n < nbf ? n : n - nbf) * nbf + r];
+                    }
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        const int n = c0 + k;
+                        if (n >= 2 * nbf) continue;
+                        const bool xc = n < nbf;
+                        const int nu = xc ? n : n - nbf;
+                        // exact power-of-two scaling (two factors cover the clamped exponent range)
+                        const int sc = er + es[nu] + (xc ? ex : ej) - 14;
+                        const int sc1 = max(-126, min(127, sc));
+                        const float f = pow2f(sc1) * pow2f(max(-126, min(127, sc - sc1)));
+                        const float vh = dh[k] * f, vl = dl[k] * f;
+                        // (s, e) += vh + vl, then renormalise so |e| <= ulp(s) / 2
+                        float s2 = old[k].x, e2 = old[k].y;
+                        const float t = s2 + vh;
+                        const float bp = t - s2;
+                        e2 += (s2 - (t - bp)) + (vh - bp) + vl;
+                        s2 = t + e2;
+                        e2 = e2 - (s2 - t);
+                        px[(xc ? 0 : nn) + (size_t)nu * nbf + r] = make_float2(s2, e2);
                     }
                 }
             }
@@ -281,6 +368,40 @@ k_contract_tc(int nbf, int NP, int nst, int nkb, int kb_per_chunk, int nchunk, s
             ct_epi_bar();                        // all TMEM reads of this chunk are done
             if (threadIdx.x == 160) mbar_arrive(&sh->tmem_empty);
         }
+        if (spart && !sh->fail) {
+            for (size_t i = threadIdx.x - 160; i < 2 * nn; i += 256) gpart[i] = s_part[i];
+        }
+    } else {
+        // ------------------------------------------------------------ loader
+        if (lane == 0) {
+            const uint32_t tx = kCtSlices * a_hbm + 2 * kCtKS * 4;
+            int it = 0, issued = 0;
+            for (int ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+                const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
+                bool ok = true;
+                for (int kb = kb0; kb < kb1; ++kb, ++it) {
+                    const int s = it % nst, n = it / nst;
+                    if (!mbar_wait(&sh->empty[s], (uint32_t)((n & 1) ^ 1)) || sh->fail) {
+                        atomicExch(err, 15);
+                        sh->fail = 1;
+                        ok = false;
+                        break;
+                    }
+                    unsigned char *sA = smem + (size_t)s * stage;
+                    mbar_arrive_expect_tx(&sh->a_full[s], tx);
+                    for (int i = 0; i < kCtSlices; ++i)
+                        bulk_g2s(sA + i * a_slice, aslices + ((size_t)kb * kCtSlices + i) * a_hbm, a_hbm, &sh->a_full[s]);
+                    bulk_g2s(sA + c_off, cxc + (size_t)kb * kCtKS, kCtKS * 4, &sh->a_full[s]);
+                    bulk_g2s(sA + c_off + kCtKS * 4, cj + (size_t)kb * kCtKS, kCtKS * 4, &sh->a_full[s]);
+                    issued = it + 1;
+                }
+                if (!ok) break;
+            }
+            // drain: the copies of the last nst stages must land before the CTA exits
+            for (int j = (issued > nst ? issued - nst : 0); j < issued; ++j)
+                mbar_wait(&sh->a_full[j % nst], (uint32_t)((j / nst) & 1));
+        }
+        __syncwarp();
     }
     tc_fence_before();
     __syncthreads();
@@ -290,9 +411,117 @@ k_contract_tc(int nbf, int NP, int nst, int nkb, int kb_per_chunk, int nchunk, s
     }
 }
 
-// ------------------------------------------------------------------ host side
+// ------------------------------------------------------------------ setup
 
-static size_t ct_smem(int nst, int NP) { return (size_t)nst * ct_stage_bytes(kCtSlices, NP) + sizeof(CtShared); }
+// exponent bounds of max |phi_mu| and max |w phi_mu| over each chunk: block
+// per chunk, warp per row
+__global__ void k_ct_rowexp(int nbf, size_t npad, int nkb, int kb_per_chunk, const float *__restrict__ phi,
+                            const double *__restrict__ W, int *__restrict__ rowexp, int *__restrict__ swexp)
+{
+    const int ch = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t p0 = (size_t)ch * kb_per_chunk * kCtKS;
+    const size_t p1 = (size_t)min(nkb, (ch + 1) * kb_per_chunk) * kCtKS;
+    for (int mu = warp; mu < nbf; mu += blockDim.x >> 5) {
+        uint32_t m = 0u;
+        double mw = 0.0;
+        for (size_t p = p0 + lane; p < p1; p += 32) {
+            const float f = phi[(size_t)mu * npad + p];
+            m = max(m, __float_as_uint(f) & 0x7fffffffu);
+            mw = fmax(mw, fabs(W[p] * (double)f));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+            mw = fmax(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+        }
+        if (lane == 0) {
+            rowexp[(size_t)ch * nbf + mu] = exp_bound(m);
+            int e = 0;
+            if (mw > 0.0) frexp(mw, &e);           // mw < 2^e
+            swexp[(size_t)ch * nbf + mu] = e < kCtExpMin ? kCtExpMin : (e > kCtExpMax ? kCtExpMax : e);
+        }
+    }
+}
+
+// 1 / w in FP32 (0 where the weight vanishes), for the per-build bound of |c / w|
+__global__ void k_ct_winv(size_t npad, const double *__restrict__ W, float *__restrict__ winv)
+{
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < npad) winv[p] = W[p] > 1e-30 ? (float)(1.0 / W[p]) : 0.f;
+}
+
+// A slices in HBM, [nkb][slice][AR x 32 core layout]: thread per (kb, row, 8-point group)
+__global__ void k_ct_slice_A(int nbf, int AR, size_t npad, int nkb, int kb_per_chunk, const double *__restrict__ phi,
+                             const int *__restrict__ rowexp, __nv_bfloat16 *__restrict__ A)
+{
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t total = (size_t)nkb * AR * 4;
+    if (id >= total) return;
+    const int g = (int)(id & 3);
+    const int row = (int)((id >> 2) % AR);
+    const int kb = (int)(id / ((size_t)AR * 4));
+    const size_t blk = (size_t)AR * kCtKS;                  // elements of one slice block
+    const uint32_t o = core_off(row, 8 * g, kCtKcores) / 2;
+    const int e = row < nbf ? rowexp[(size_t)(kb / kb_per_chunk) * nbf + row] : 0;
+    for (int k = 0; k < 8; ++k) {
+        const size_t p = (size_t)kb * kCtKS + 8 * g + k;
+        // the FP32 amplitudes are the ones the CUDA-core path and the B operand use
+        const double x = row < nbf ? ldexp((double)(float)phi[(size_t)row * npad + p], 7 - e) : 0.0;
+        const double a1 = rint(x);
+        const double r1 = x - a1;
+        const __nv_bfloat16 h2 = __float2bfloat16_rn((float)r1);
+        const double r2 = r1 - (double)__bfloat162float(h2);
+        const size_t base = (size_t)kb * kCtSlices * blk + o + k;
+        A[base] = __float2bfloat16_rn((float)a1);
+        A[base + blk] = h2;
+        A[base + 2 * blk] = __float2bfloat16_rn((float)r2);
+    }
+}
+
+static size_t ct_smem(int nst, int NP, int nbf, bool spart)
+{
+    return (size_t)nst * ct_stage_bytes(NP) + (spart ? 2 * (size_t)nbf * nbf * sizeof(float2) : 0) + sizeof(CtShared);
+}
+
+// Sum the double-float CTA partials of every element on or above the diagonal
+// in CTA order, in FP64, and write XC, J symmetrically (column-major).  Block:
+// 32 elements x 8 CTA groups; group g sums CTAs g, g + 8, ...; the 8 group sums
+// are added in a fixed order.
+__global__ void __launch_bounds__(256) k_contract_tc_reduce(int nbf, int nparts, int want_xc, int want_j,
+                                                            const float2 *__restrict__ part,
+                                                            double *__restrict__ XC, double *__restrict__ J)
+{
+    __shared__ double shx[8][33], shj[8][33];
+    const size_t nn = (size_t)nbf * nbf;
+    const int lx = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const size_t e = (size_t)blockIdx.x * 32 + lx;          // partial element (nu * nbf + mu) = (mu, nu)
+    double sx = 0.0, sj = 0.0;
+    const int nu = (int)(e / nbf), mu = (int)(e % nbf);
+    const bool act = e < nn && mu <= nu;
+    if (act)
+        for (int c = g; c < nparts; c += 8) {
+            const float2 *p = part + (size_t)c * 2 * nn;
+            const float2 a = p[e], b = p[nn + e];
+            sx += (double)a.x + (double)a.y;
+            sj += (double)b.x + (double)b.y;
+        }
+    shx[g][lx] = sx;
+    shj[g][lx] = sj;
+    __syncthreads();
+    if (g != 0 || !act) return;
+    for (int k = 1; k < 8; ++k) {
+        sx += shx[k][lx];
+        sj += shj[k][lx];
+    }
+    if (want_xc) {
+        XC[(size_t)nu * nbf + mu] = sx;
+        XC[(size_t)mu * nbf + nu] = sx;
+    }
+    if (want_j) {
+        J[(size_t)nu * nbf + mu] = sj;
+        J[(size_t)mu * nbf + nu] = sj;
+    }
+}
 
 // chunking of the point dimension for nsm CTAs: chunks per CTA is the smallest
 // count that keeps every chunk at most kCtMaxKbPerChunk stages long
@@ -300,7 +529,7 @@ static void ct_plan(size_t npad, int nsm, int &nkb, int &kbpc, int &nchunk)
 {
     nkb = (int)(npad / kCtKS);
     const int per_cta = (nkb + nsm * kCtMaxKbPerChunk - 1) / (nsm * kCtMaxKbPerChunk);
-    int target = nsm * (per_cta > 0 ? per_cta : 1);
+    const int target = nsm * (per_cta > 0 ? per_cta : 1);
     kbpc = (nkb + target - 1) / target;
     if (kbpc < 1) kbpc = 1;
     nchunk = (nkb + kbpc - 1) / kbpc;
@@ -311,44 +540,79 @@ size_t contract_tc_part_elems(int nbf, size_t npad, int nsm)
     if (nbf > kCtMaxNbf) return 0;
     int nkb, kbpc, nchunk;
     ct_plan(npad, nsm, nkb, kbpc, nchunk);
-    return (size_t)nchunk * 2 * nbf * nbf;
+    const int grid = nchunk < nsm ? nchunk : nsm;
+    return (size_t)grid * 2 * nbf * nbf;          // one partial per CTA
 }
 
 int contract_tc_setup(dftg_ctx *c)
 {
     if (c->nbf > kCtMaxNbf) return DFTG_OK;
-    int nsm = 0;
+    int nsm = 0, optin = 0;
     DFTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
-    int optin = 0;
     DFTG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
     const int NP = (2 * c->nbf + 15) / 16 * 16;
+    const int AR = (c->nbf + 7) / 8 * 8;
+    // keep the CTA partial in shared memory if at least three stages still fit
+    bool spart = true;
     int nst = kCtMaxStages;
-    while (nst > 2 && ct_smem(nst, NP) > (size_t)optin) --nst;
-    if (ct_smem(nst, NP) > (size_t)optin) return DFTG_OK;
+    while (nst > 3 && ct_smem(nst, NP, c->nbf, spart) > (size_t)optin) --nst;
+    if (ct_smem(nst, NP, c->nbf, spart) > (size_t)optin) {
+        spart = false;
+        nst = kCtMaxStages;
+        while (nst > 2 && ct_smem(nst, NP, c->nbf, spart) > (size_t)optin) --nst;
+    }
+    if (ct_smem(nst, NP, c->nbf, spart) > (size_t)optin) return DFTG_OK;
     int nkb, kbpc, nchunk;
     ct_plan(c->npad, nsm, nkb, kbpc, nchunk);
-    if ((size_t)nchunk * 2 * c->nbf * c->nbf > c->part_elems) return DFTG_OK;
-    DFTG_CUDA(cudaFuncSetAttribute(k_contract_tc<kCtSlices>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)ct_smem(nst, NP)));
+    const int grid = nchunk < nsm ? nchunk : nsm;
+    if ((size_t)grid * 2 * c->nbf * c->nbf > c->part_elems) return DFTG_OK;
+    DFTG_CUDA(cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)ct_smem(nst, NP, c->nbf, spart)));
     if (!c->d_flag) {
         DFTG_CUDA(cudaMalloc(&c->d_flag, sizeof(int)));
         DFTG_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
     }
+    DFTG_CUDA(cudaMalloc(&c->d_ct_rowexp, sizeof(int) * 2 * (size_t)nchunk * c->nbf));
+    DFTG_CUDA(cudaMalloc(&c->d_ct_winv, sizeof(float) * c->npad));
+    DFTG_CUDA(cudaMalloc(&c->d_ct_A, sizeof(__nv_bfloat16) * (size_t)nkb * kCtSlices * AR * kCtKS));
+    k_ct_rowexp<<<nchunk, 256, 0, c->stream>>>(c->nbf, c->npad, nkb, kbpc, c->d_phi32, c->d_w, c->d_ct_rowexp,
+                                               c->d_ct_rowexp + (size_t)nchunk * c->nbf);
+    DFTG_LAUNCH_CHECK();
+    k_ct_winv<<<(unsigned)((c->npad + 255) / 256), 256, 0, c->stream>>>(c->npad, c->d_w, c->d_ct_winv);
+    DFTG_LAUNCH_CHECK();
+    const size_t threads = (size_t)nkb * AR * 4;
+    k_ct_slice_A<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+        c->nbf, AR, c->npad, nkb, kbpc, c->d_phi, c->d_ct_rowexp, reinterpret_cast<__nv_bfloat16 *>(c->d_ct_A));
+    DFTG_LAUNCH_CHECK();
     c->ct_NP = NP;
+    c->ct_AR = AR;
     c->ct_nst = nst;
+    c->ct_spart = spart ? 1 : 0;
     c->ct_nkb = nkb;
     c->ct_kbpc = kbpc;
     c->ct_nchunk = nchunk;
-    c->ct_grid = nchunk < nsm ? nchunk : nsm;
+    c->ct_grid = grid;
     c->ct_ready = true;
     return DFTG_OK;
 }
 
 int launch_contract_tc(dftg_ctx *c)
 {
-    k_contract_tc<kCtSlices><<<c->ct_grid, kCtThreads, ct_smem(c->ct_nst, c->ct_NP), c->stream>>>(
-        c->nbf, c->ct_NP, c->ct_nst, c->ct_nkb, c->ct_kbpc, c->ct_nchunk, c->npad, c->d_phi32, c->d_cxc32, c->d_cj32,
-        c->d_part, c->d_flag);
+    k_contract_tc<<<c->ct_grid, kCtThreads, ct_smem(c->ct_nst, c->ct_NP, c->nbf, c->ct_spart != 0), c->stream>>>(
+        c->nbf, c->ct_AR, c->ct_NP, c->ct_nst, c->ct_spart, c->ct_nkb, c->ct_kbpc, c->ct_nchunk,
+        reinterpret_cast<const unsigned char *>(c->d_ct_A), c->d_ct_rowexp,
+        c->d_ct_rowexp + (size_t)c->ct_nchunk * c->nbf, c->d_ct_winv, c->d_cxc32, c->d_cj32,
+        reinterpret_cast<float2 *>(c->d_part), c->d_flag);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+int launch_contract_tc_reduce(dftg_ctx *c, bool want_xc, bool want_j)
+{
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    k_contract_tc_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(
+        c->nbf, c->ct_grid, want_xc ? 1 : 0, want_j ? 1 : 0, reinterpret_cast<const float2 *>(c->d_part), c->d_XC,
+        c->d_J);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }

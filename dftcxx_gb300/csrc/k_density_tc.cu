@@ -24,7 +24,8 @@
 //     128 x KP block per slice and tile, copied with cp.async.bulk;
 //   B slices: [slice][NP/8][KP/8][8][8] BF16 (rows nu, K = mu).
 // CTA: warp 0 producer (bulk copies), warp 1 TMEM owner + MMA issuer,
-// warps 2-5 epilogue (TMEM lanes 32 (w % 4) ...).  Persistent over tiles, two
+// warps 2-9 epilogue: TMEM lanes 32 (w % 4) ..., the two warps of a lane quarter
+// take alternate 16-column blocks and meet in shared memory per tile.  Persistent over tiles, two
 // A stages and two TMEM accumulator pairs, so the MMAs of one tile overlap the
 // epilogue of the previous one.  Every mbarrier wait is bounded: on expiry the
 // CTA records an error code, drains its copies, frees TMEM and exits.
@@ -38,8 +39,24 @@ namespace dftg {
 constexpr int kTcSlices = 4;
 constexpr int kTcTile = 128;
 constexpr int kTcMaxK = 80;                   // nbf <= 80 for this kernel
-constexpr int kTcThreads = 192;
+constexpr int kTcThreads = 320;
 constexpr uint32_t kTcTmemCols = 512;
+// named barrier 1 over the 8 epilogue warps
+__device__ __forceinline__ void epi8_bar_sync()
+{
+    asm volatile("bar.sync 1, 256;" ::: "memory");
+}
+
+__device__ __forceinline__ void unpack8_bf16(uint4 u, float (&v)[8])
+{
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        v[2 * j] = __uint_as_float(w[j] << 16);
+        v[2 * j + 1] = __uint_as_float(w[j] & 0xffff0000u);
+    }
+}
+
 struct TcShared {
     uint64_t full[2], empty[2], tmem_full[2], tmem_empty[2];
     uint32_t tmem_base;
@@ -59,6 +76,7 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
     TcShared *sh = reinterpret_cast<TcShared *>(sB + kTcSlices * b_slice_bytes);
     __shared__ int s_texp[kTcMaxK];
     __shared__ int s_fail;
+    __shared__ float2 s_half[kTcTile];            // (S, E) of the second column half, per row
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -149,61 +167,86 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
     } else {
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3;                 // TMEM lane quarter of this warp
+        const int half = (warp - 2) >> 2;       // column blocks half, half + 2, ...
         const int r = q * 32 + lane;            // row of the tile = TMEM lane
         const int kc = KP / 8;
         for (int it = 0; it < my_tiles; ++it) {
             const int s = it & 1, n = it >> 1;
             bool ok = mbar_wait(&sh->tmem_full[s], (uint32_t)(n & 1));
             if (!ok) { atomicExch(err, 4); s_fail = 1; }
-            epi_bar_sync();
+            epi8_bar_sync();
             if (s_fail) break;
             tc_fence_after();
             const int tile = (int)blockIdx.x + it * (int)gridDim.x;
             const size_t p = (size_t)tile * kTcTile + r;
-            const int ep = row_exp[p];
             const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
             const uint32_t ta0 = tmem + (uint32_t)(s * 256) + ((uint32_t)(q * 32) << 16);
-            float S = 0.f, E = 0.f;
-            for (int c0 = 0; c0 < NP; c0 += 16) {
+            // two independent compensated accumulators (even / odd columns)
+            float S[2] = {0.f, 0.f}, E[2] = {0.f, 0.f};
+            for (int c0 = 16 * half; c0 < NP; c0 += 32) {
                 float dh[16], dl[16];
                 tmem_ld16(ta0 + (uint32_t)c0, dh);
                 tmem_ld16(ta0 + 128u + (uint32_t)c0, dl);
                 tmem_wait_ld();
 #pragma unroll
-                for (int k = 0; k < 16; ++k) {
-                    const int nu = c0 + k;
-                    if (nu >= nbf) continue;
-                    // T~_nu 2^16 = D_hi + D_lo: exact head by TwoSum
-                    const float u = dh[k] + dl[k];
-                    const float bp = u - dh[k];
-                    float te = (dh[k] - (u - bp)) + (dl[k] - bp);
-                    const float sc = __int_as_float((127 - 16 + s_texp[nu]) << 23);
-                    const float t = u * sc;
-                    te *= sc;
-                    // phi~ 2^8 from the pre-scaled slices of this row (exact FP32 pair)
-                    const uint32_t off = core_off(r, nu, kc);
-                    const float m1 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + off));
-                    const float m2 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + a_slice_bytes + off));
-                    const float m3 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + 2 * a_slice_bytes + off));
-                    const float m4 = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(a0 + 3 * a_slice_bytes + off));
-                    const float fh = (m1 + m2) * 0x1p-8f;
-                    const float fl = (m3 + m4) * 0x1p-8f;
-                    // S + E += (t + te)(fh + fl)
-                    const float pr = t * fh;
-                    const float pe = fmaf(t, fh, -pr);
-                    const float w = S + pr;
-                    const float bq = w - S;
-                    E += (S - (w - bq)) + (pr - bq) + pe + fmaf(t, fl, te * fh);
-                    S = w;
+                for (int g8 = 0; g8 < 2; ++g8) {
+                    const int nb = c0 + 8 * g8;
+                    if (nb >= nbf) break;
+                    // phi~ 2^8 of columns nb..nb+7 from the four pre-scaled slices (16 B each)
+                    const uint32_t off = core_off(r, nb, kc);
+                    float m1[8], m2[8], m3[8], m4[8];
+                    unpack8_bf16(*reinterpret_cast<const uint4 *>(a0 + off), m1);
+                    unpack8_bf16(*reinterpret_cast<const uint4 *>(a0 + a_slice_bytes + off), m2);
+                    unpack8_bf16(*reinterpret_cast<const uint4 *>(a0 + 2 * a_slice_bytes + off), m3);
+                    unpack8_bf16(*reinterpret_cast<const uint4 *>(a0 + 3 * a_slice_bytes + off), m4);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const int nu = nb + k;
+                        if (nu >= nbf) continue;
+                        const int j = 8 * g8 + k;
+                        // T~_nu 2^16 = D_hi + D_lo: exact head by TwoSum
+                        const float u = dh[j] + dl[j];
+                        const float bp = u - dh[j];
+                        float te = (dh[j] - (u - bp)) + (dl[j] - bp);
+                        const float sc = __int_as_float((127 - 16 + s_texp[nu]) << 23);
+                        const float t = u * sc;
+                        te *= sc;
+                        const float fh = (m1[k] + m2[k]) * 0x1p-8f;
+                        const float fl = (m3[k] + m4[k]) * 0x1p-8f;
+                        // S + E += (t + te)(fh + fl)
+                        const int a = k & 1;
+                        const float pr = t * fh;
+                        const float pe = fmaf(t, fh, -pr);
+                        const float w = S[a] + pr;
+                        const float bq = w - S[a];
+                        E[a] += (S[a] - (w - bq)) + (pr - bq) + pe + fmaf(t, fl, te * fh);
+                        S[a] = w;
+                    }
                 }
             }
+            // fold the two accumulators (TwoSum)
+            float St, Et;
+            {
+                const float w = S[0] + S[1];
+                const float bq = w - S[0];
+                Et = E[0] + E[1] + (S[0] - (w - bq)) + (S[1] - bq);
+                St = w;
+            }
             tc_fence_before();
-            epi_bar_sync();                      // all TMEM reads and A-stage reads of this tile are done
+            if (half == 1) s_half[r] = make_float2(St, Et);
+            epi8_bar_sync();                     // TMEM and A-stage reads of this tile done, halves posted
             if (threadIdx.x == 64) {
                 mbar_arrive(&sh->tmem_empty[s]);
                 mbar_arrive(&sh->empty[s]);
             }
-            rho[p] = 2.0 * ((double)S + (double)E) * ldexp(1.0, 2 * ep);
+            if (half == 0) {
+                const float2 o = s_half[r];
+                const float w = St + o.x;
+                const float bq = w - St;
+                const float e = Et + o.y + (St - (w - bq)) + (o.x - bq);
+                const int ep = row_exp[p];
+                rho[p] = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
+            }
         }
     }
     tc_fence_before();

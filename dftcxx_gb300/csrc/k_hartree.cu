@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 #include "dftg_internal.cuh"
@@ -579,68 +580,121 @@ __global__ void __launch_bounds__(128) k_vcross64(size_t npts, size_t npad, int 
     cj32[p] = (float)c;
 }
 
+constexpr int kCrossPerThread = 2;               // pairs per thread of k_vcross_bins
+constexpr int kCrossTask = 128 * kCrossPerThread;  // pairs per block
+// low halves of the spline coefficients are evaluated for l <= kCrossLoLmax:
+// beyond l = 2 they change E_tot of benzene / 6-31G by < 1e-8 Ha
+constexpr int kCrossLoLmax = 2;
+
 // K5e (mixed): FP32 recursion with exact integer coefficients; the spline
 // coefficients (which carry the Y_lm normalisation) enter as split FP32 hi/lo
 // pairs so no rounding is common to all points.  No FP64 work in the pair
 // loop: the per-atom contributions accumulate in an FP32 TwoSum pair and meet
 // the FP64 own-cell part once per point.
-// One thread per (point, other atom) pair.  The pairs are ordered by (atom,
-// spline interval) once per grid, so the lanes of a warp read the same spline
-// coefficients.  Writes the pair's contribution as an FP32 (hi, lo) pair.
-__global__ void __launch_bounds__(128) k_vcross_pairs(size_t npairs, int nrad, int lmax,
-                                                      const float4 *__restrict__ pgeo,
-                                                      const float2 *__restrict__ ptk,
-                                                      const float *__restrict__ splm, float2 *__restrict__ out)
+// One block per task: up to 128 P consecutive (point, other atom) pairs of one
+// bin (atom k, spline interval iv).  The pairs are ordered by bin once per
+// grid, so the bin's spline coefficients are staged once in shared memory and
+// each thread evaluates P pairs against them (every coefficient read serves P
+// pairs).  The high halves of the coefficients are used for every l, the low
+// halves for l <= kCrossLoLmax.  Writes each pair's contribution as an FP32 (hi, lo)
+// pair.
+template <int P, int LMAX>
+__global__ void __launch_bounds__(128) k_vcross_bins(int nrad, int lmax_rt,
+                                                     const int4 *__restrict__ tasks,
+                                                     const float4 *__restrict__ pgeo,
+                                                     const float2 *__restrict__ ptk,
+                                                     const float *__restrict__ splm, float2 *__restrict__ out)
 {
-    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= npairs) return;
-    const float4 g = pgeo[e];            // unit vector from atom k to the point, 1/r
-    const float2 tk = ptk[e];            // spline offset t, (k << 16 | interval)
+    extern __shared__ float4 s_cf[];      // [nlm][2]: (c0..c3) high, (c0..c3) low
+    const int4 task = tasks[blockIdx.x];  // start, count, atom k, interval iv
+    const int lmax = LMAX >= 0 ? LMAX : lmax_rt;   // compile-time for the common cut-offs
     const int nlm = (lmax + 1) * (lmax + 1);
-    const int N = nrad;
-    const uint32_t kv = __float_as_uint(tk.y);
-    const int k = (int)(kv >> 16), iv = (int)(kv & 0xffffu);
-    const float t = tk.x, inv_r = g.w;
-    const float ux = g.x, uy = g.y, uz = g.z;
-    const float4 *cf = reinterpret_cast<const float4 *>(splm + ((size_t)k * nlm * N + iv) * 8);
-    const size_t lstride = (size_t)N * 2;   // float4 units per lm
-    float ah = 0.f, al = 0.f, cm = 1.f, sm = 0.f;
+    for (int i = threadIdx.x; i < 2 * nlm; i += blockDim.x) {
+        const int lm = i >> 1;
+        s_cf[i] = reinterpret_cast<const float4 *>(splm + (((size_t)task.z * nlm + lm) * nrad + task.w) * 8)[i & 1];
+    }
+    float ux[P], uy[P], uz[P], ir[P], t[P];
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+        const int o = threadIdx.x + j * 128;
+        if (o < task.y) {
+            const float4 g = pgeo[(size_t)task.x + o];
+            ux[j] = g.x; uy[j] = g.y; uz[j] = g.z; ir[j] = g.w;
+            t[j] = ptk[(size_t)task.x + o].x;
+        } else {
+            ux[j] = 0.f; uy[j] = 0.f; uz[j] = 1.f; ir[j] = 0.f; t[j] = 0.f;
+        }
+    }
+    __syncthreads();
+    float ah[P], al[P], cm[P], sm[P];
+#pragma unroll
+    for (int j = 0; j < P; ++j) { ah[j] = 0.f; al[j] = 0.f; cm[j] = 1.f; sm[j] = 0.f; }
+#pragma unroll
     for (int m = 0; m <= lmax; ++m) {
-        float r2 = 0.f, r1 = 1.f;
+        float r1[P], r2[P];
+#pragma unroll
+        for (int j = 0; j < P; ++j) { r1[j] = 1.f; r2[j] = 0.f; }
+#pragma unroll
         for (int l = m; l <= lmax; ++l) {
-            float q;
-            if (l == m) q = 1.f;
-            else {
-                q = (float)(2 * l - 1) * uz * r1 - (float)((l + m - 1) * (l - m - 1)) * r2;
-                r2 = r1;
-                r1 = q;
-            }
-            const int lp = l * l + l + m;
-            const float4 ch = cf[(size_t)lp * lstride];
-            const float4 cl = cf[(size_t)lp * lstride + 1];
-            const float sh = fmaf(t, fmaf(t, fmaf(t, ch.w, ch.z), ch.y), ch.x);
-            const float sl = fmaf(t, fmaf(t, fmaf(t, cl.w, cl.z), cl.y), cl.x);
-            if (m == 0) {
-                ah = fmaf(q, sh, ah);
-                al = fmaf(q, sl, al);
+            float q[P];
+            if (l == m) {
+#pragma unroll
+                for (int j = 0; j < P; ++j) q[j] = 1.f;
             } else {
-                const int ln = l * l + l - m;
-                const float4 dh = cf[(size_t)ln * lstride];
-                const float4 dl = cf[(size_t)ln * lstride + 1];
-                const float nh = fmaf(t, fmaf(t, fmaf(t, dh.w, dh.z), dh.y), dh.x);
-                const float nl = fmaf(t, fmaf(t, fmaf(t, dl.w, dl.z), dl.y), dl.x);
-                const float qc = q * cm, qs = q * sm;
-                ah = fmaf(qc, sh, fmaf(qs, nh, ah));
-                al = fmaf(qc, sl, fmaf(qs, nl, al));
+                const float fa = (float)(2 * l - 1), fb = (float)((l + m - 1) * (l - m - 1));
+#pragma unroll
+                for (int j = 0; j < P; ++j) {
+                    q[j] = fa * uz[j] * r1[j] - fb * r2[j];
+                    r2[j] = r1[j];
+                    r1[j] = q[j];
+                }
+            }
+            const bool lo = l <= kCrossLoLmax;
+            const float4 ch = s_cf[2 * (l * l + l + m)];
+            const float4 cl = lo ? s_cf[2 * (l * l + l + m) + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (m == 0) {
+#pragma unroll
+                for (int j = 0; j < P; ++j) {
+                    const float sh = fmaf(t[j], fmaf(t[j], fmaf(t[j], ch.w, ch.z), ch.y), ch.x);
+                    ah[j] = fmaf(q[j], sh, ah[j]);
+                    if (lo) {
+                        const float sl = fmaf(t[j], fmaf(t[j], fmaf(t[j], cl.w, cl.z), cl.y), cl.x);
+                        al[j] = fmaf(q[j], sl, al[j]);
+                    }
+                }
+            } else {
+                const float4 dh = s_cf[2 * (l * l + l - m)];
+                const float4 dl = lo ? s_cf[2 * (l * l + l - m) + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int j = 0; j < P; ++j) {
+                    const float sh = fmaf(t[j], fmaf(t[j], fmaf(t[j], ch.w, ch.z), ch.y), ch.x);
+                    const float nh = fmaf(t[j], fmaf(t[j], fmaf(t[j], dh.w, dh.z), dh.y), dh.x);
+                    const float qc = q[j] * cm[j], qs = q[j] * sm[j];
+                    ah[j] = fmaf(qc, sh, fmaf(qs, nh, ah[j]));
+                    if (lo) {
+                        const float sl = fmaf(t[j], fmaf(t[j], fmaf(t[j], cl.w, cl.z), cl.y), cl.x);
+                        const float nl = fmaf(t[j], fmaf(t[j], fmaf(t[j], dl.w, dl.z), dl.y), dl.x);
+                        al[j] = fmaf(qc, sl, fmaf(qs, nl, al[j]));
+                    }
+                }
             }
         }
-        const float cn = cm * ux - sm * uy, sn2 = cm * uy + sm * ux;
-        cm = cn;
-        sm = sn2;
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+            const float cn = cm[j] * ux[j] - sm[j] * uy[j], sn = cm[j] * uy[j] + sm[j] * ux[j];
+            cm[j] = cn;
+            sm[j] = sn;
+        }
     }
-    const float vh = inv_r * ah;
-    const float vl = fmaf(inv_r, ah, -vh) + inv_r * al;
-    out[e] = make_float2(vh, vl);
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+        const int o = threadIdx.x + j * 128;
+        if (o < task.y) {
+            const float vh = ir[j] * ah[j];
+            const float vl = fmaf(ir[j], ah[j], -vh) + ir[j] * al[j];
+            out[(size_t)task.x + o] = make_float2(vh, vl);
+        }
+    }
 }
 
 // total potential per point: own cell (FP64) plus the pair contributions in
@@ -709,7 +763,15 @@ int cross_pairs_setup(dftg_ctx *c)
             ++e;
         }
     }
-    for (int i = 0; i < nkeys; ++i) count[i + 1] += count[i];
+    // tasks: runs of at most kCrossTask pairs inside one bin
+    std::vector<int4> tasks;
+    for (int kk = 0; kk < nkeys; ++kk) {
+        const size_t cnt = count[(size_t)kk + 1];
+        const size_t start = count[kk];          // still the prefix sum of the bins before kk
+        for (size_t o = 0; o < cnt; o += kCrossTask)
+            tasks.push_back(make_int4((int)(start + o), (int)std::min<size_t>(kCrossTask, cnt - o), kk / N, kk % N));
+        count[(size_t)kk + 1] += count[kk];
+    }
     // the geometry of a pair is fixed for the grid: direction, 1/r and the
     // spline offset are formed in FP64 and rounded once to FP32
     std::vector<float4> geo(npairs);
@@ -735,6 +797,9 @@ int cross_pairs_setup(dftg_ctx *c)
         }
     }
     c->npairs = npairs;
+    c->ncross_tasks = (int)tasks.size();
+    DFTG_CUDA(cudaMalloc(&c->d_cross_tasks, sizeof(int4) * tasks.size()));
+    DFTG_CUDA(cudaMemcpy(c->d_cross_tasks, tasks.data(), sizeof(int4) * tasks.size(), cudaMemcpyHostToDevice));
     DFTG_CUDA(cudaMalloc(&c->d_pairs, (sizeof(float4) + sizeof(float2)) * npairs));
     DFTG_CUDA(cudaMalloc(&c->d_pairpos, sizeof(int) * pos.size()));
     DFTG_CUDA(cudaMalloc(&c->d_pairv, sizeof(float2) * npairs));
@@ -776,6 +841,29 @@ __global__ void __launch_bounds__(256) k_ej_final(int n, const double *__restric
     if (threadIdx.x == 0) scal[kScalEJ] = scaled ? sh[0] / scal[kScalScale] : sh[0];
 }
 
+template <int LMAX>
+static void vcross_bins_launch(dftg_ctx *c)
+{
+    k_vcross_bins<kCrossPerThread, LMAX><<<(unsigned)c->ncross_tasks, 128, sizeof(float4) * 2 * c->nlm, c->stream>>>(
+        c->nrad, c->lmax, reinterpret_cast<const int4 *>(c->d_cross_tasks), reinterpret_cast<const float4 *>(c->d_pairs),
+        reinterpret_cast<const float2 *>(static_cast<const char *>(c->d_pairs) + sizeof(float4) * c->npairs),
+        c->d_splm, reinterpret_cast<float2 *>(c->d_pairv));
+}
+
+static int launch_vcross_bins(dftg_ctx *c)
+{
+    switch (c->lmax) {   // fully unrolled variants for the grid presets' cut-offs
+    case 5: vcross_bins_launch<5>(c); break;
+    case 6: vcross_bins_launch<6>(c); break;
+    case 8: vcross_bins_launch<8>(c); break;
+    case 10: vcross_bins_launch<10>(c); break;
+    case 11: vcross_bins_launch<11>(c); break;
+    default: vcross_bins_launch<-1>(c); break;
+    }
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
 int launch_hartree(dftg_ctx *c)
 {
     const int N = c->nrad, S = N + 2, nlm = c->nlm;
@@ -809,11 +897,7 @@ int launch_hartree(dftg_ctx *c)
     const unsigned nb = (unsigned)(c->npad / 128);
     if (c->prec_mask & kPrecCross) {
         if (c->npairs > 0) {
-            k_vcross_pairs<<<(unsigned)((c->npairs + 127) / 128), 128, 0, c->stream>>>(
-                c->npairs, N, c->lmax, reinterpret_cast<const float4 *>(c->d_pairs),
-                reinterpret_cast<const float2 *>(static_cast<const char *>(c->d_pairs) + sizeof(float4) * c->npairs),
-                c->d_splm, reinterpret_cast<float2 *>(c->d_pairv));
-            DFTG_LAUNCH_CHECK();
+            DFTG_TRY_L(launch_vcross_bins(c));
         }
         k_vcross_gather<<<(unsigned)((c->npad + 127) / 128), 128, 0, c->stream>>>(
             c->npts, c->npad, c->natoms, N, c->nang, c->d_pairpos, reinterpret_cast<const float2 *>(c->d_pairv),

@@ -7,7 +7,7 @@
 
 namespace dftg {
 
-constexpr unsigned long long kWaitLimit = 1ull << 27;
+constexpr unsigned long long kWaitNs = 2000000000ull;   // 2 s
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
@@ -31,17 +31,31 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                  : "memory");
 }
 
-// bounded wait for the phase of the given parity; false on expiry
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// bounded wait for the phase of the given parity: gives up (false) after
+// kWaitNs nanoseconds of wall-clock time, or after 2^31 polls whatever the timer
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
 {
     const uint32_t a = smem_u32(bar);
-    for (unsigned long long it = 0; it < kWaitLimit; ++it) {
+    unsigned long long t0 = 0;
+    for (unsigned it = 0; it < (1u << 31); ++it) {
         uint32_t done;
         asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
                      : "=r"(done)
                      : "r"(a), "r"(parity)
                      : "memory");
         if (done) return true;
+        if ((it & 255u) == 0u) {
+            const unsigned long long t = global_ns();
+            if (it == 0) t0 = t;
+            else if (t - t0 > kWaitNs) return false;
+        }
     }
     return false;
 }

@@ -158,3 +158,23 @@ def test_mixed_density_tensor_core_accuracy(gpu_lib, name, basis, nrad, leb):
     a, b = g64.fock_build(P), gmx.fock_build(P)
     assert abs(a["Exc"] - b["Exc"]) < 2e-7
     assert abs(a["EJ"] - b["EJ"]) < 2e-9 * abs(a["EJ"])
+
+
+@pytest.mark.parametrize("name,basis,nrad,leb", [("H2O", "sto3g", 32, 7), ("C6H6", "p631", 20, 8)])
+def test_mixed_contraction_tensor_core_accuracy(gpu_lib, name, basis, nrad, leb):
+    """XC and J from the tensor-core contraction alone (all other steps FP64):
+    integer leading slices make the leading sums exact, so the error is the
+    FP32 rounding of the amplitudes and point coefficients."""
+    from dftcxx_gb300.grid import MolecularGrid
+    Z, xyz = small_molecule(name)
+    mol = Molecule(Z, xyz, basis)
+    g64 = MolecularGrid(mol, nrad, leb, 6, precision="fp64")
+    gtc = MolecularGrid(mol, nrad, leb, 6, precision="fp64")
+    gtc.set_precision_mask(MolecularGrid.MIX_BITS["contract"])
+    P = _density(mol, 11)
+    a, b = g64.fock_build(P), gtc.fock_build(P)
+    dJ, dXC = np.abs(a["J"] - b["J"]).max(), np.abs(a["XC"] - b["XC"]).max()
+    e_j = abs(2.0 * np.sum(P * (a["J"] - b["J"])))
+    assert dJ < 1e-7 * np.abs(a["J"]).max() and dXC < 1e-7 * np.abs(a["XC"]).max(), (dJ, dXC, e_j)
+    assert e_j < 2e-8 * abs(a["EJ"]), (dJ, dXC, e_j)
+    assert np.abs(b["J"] - b["J"].T).max() == 0.0 and np.abs(b["XC"] - b["XC"].T).max() == 0.0
