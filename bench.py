@@ -42,7 +42,7 @@ WORKLOAD = {"workload": "benzene/6-31G grid Fock build", "molecule": "C6H6 D6h",
 
 # kernels launched per phase of one mixed-precision build (dftg_fock_build_device)
 KERNELS_PER_PHASE = {"density": 2, "charge": 2, "lda": 2, "rholm": 1, "poisson": 1, "vown": 1,
-                     "splines": 1, "vcross": 2, "hartree_energy": 2, "contract": 1, "contract_reduce": 1}
+                     "splines": 1, "vcross": 2, "hartree_energy": 2, "contract": 2, "contract_reduce": 1}
 
 
 def _env_int(name, default):

@@ -141,7 +141,8 @@ struct dftg_ctx {
     // device: tensor-core XC / J contraction (split-K over point chunks)
     bool ct_ready = false;
     int ct_NP = 0, ct_AR = 0, ct_nst = 0, ct_spart = 0, ct_nkb = 0, ct_kbpc = 0, ct_nchunk = 0, ct_grid = 0;
-    int *d_ct_rowexp = nullptr;   // [2][nchunk][nbf] exponent bounds of |phi| and |w phi| per point chunk
+    int *d_ct_rowexp = nullptr;   // [2][nchunk][nbf] exponent bounds of |phi| and |w phi| per point
+                                  // chunk, then [nchunk] int2 bounds of |c_xc / w|, |c_j / w| (per build)
     float *d_ct_winv = nullptr;   // [npad] 1 / w (0 where w vanishes)
     void *d_ct_A = nullptr;       // [nkb][3][AR x 32] BF16 slices of phi, shared-memory operand layout
 

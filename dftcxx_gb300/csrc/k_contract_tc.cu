@@ -112,51 +112,75 @@ __device__ __forceinline__ void unpack8(uint4 u, float (&v)[8])
     }
 }
 
-// warp-wide exponent bounds of max |c_xc / w| and max |c_j / w| over points [p0, p1)
-__device__ __forceinline__ void chunk_v_exps(const float *__restrict__ cxc, const float *__restrict__ cj,
-                                             const float *__restrict__ winv, size_t p0, size_t p1, int lane,
-                                             int &ex, int &ej)
+// per chunk: exponent bounds of max |c_xc / w| and max |c_j / w| (block per chunk)
+__global__ void __launch_bounds__(256) k_ct_cexp(int nkb, int kb_per_chunk, const float *__restrict__ cxc,
+                                                 const float *__restrict__ cj, const float *__restrict__ winv,
+                                                 int2 *__restrict__ cexp)
 {
+    __shared__ float sx[8], sj[8];
+    const int ch = blockIdx.x;
+    const size_t p0 = (size_t)ch * kb_per_chunk * kCtKS;
+    const size_t p1 = (size_t)min(nkb, (ch + 1) * kb_per_chunk) * kCtKS;
     float mx = 0.f, mj = 0.f;
-    for (size_t p = p0 + 4 * lane; p < p1; p += 128) {
-        const float4 a = *reinterpret_cast<const float4 *>(cxc + p);
-        const float4 b = *reinterpret_cast<const float4 *>(cj + p);
-        const float4 u = *reinterpret_cast<const float4 *>(winv + p);
-        mx = fmaxf(mx, fmaxf(fmaxf(fabsf(a.x) * u.x, fabsf(a.y) * u.y), fmaxf(fabsf(a.z) * u.z, fabsf(a.w) * u.w)));
-        mj = fmaxf(mj, fmaxf(fmaxf(fabsf(b.x) * u.x, fabsf(b.y) * u.y), fmaxf(fabsf(b.z) * u.z, fabsf(b.w) * u.w)));
+    for (size_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+        const float u = winv[p];
+        mx = fmaxf(mx, fabsf(cxc[p]) * u);
+        mj = fmaxf(mj, fabsf(cj[p]) * u);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         mj = fmaxf(mj, __shfl_xor_sync(0xffffffffu, mj, o));
     }
-    ex = exp_bound(__float_as_uint(mx));
-    ej = exp_bound(__float_as_uint(mj));
+    if ((threadIdx.x & 31) == 0) {
+        sx[threadIdx.x >> 5] = mx;
+        sj[threadIdx.x >> 5] = mj;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            mx = fmaxf(mx, sx[w]);
+            mj = fmaxf(mj, sj[w]);
+        }
+        cexp[ch] = make_int2(exp_bound(__float_as_uint(mx)), exp_bound(__float_as_uint(mj)));
+    }
 }
 
-__host__ __device__ constexpr uint32_t ct_a_slice_bytes() { return (uint32_t)kCtM * kCtKS * 2; }
-__host__ __device__ constexpr uint32_t ct_b_slice_bytes(int NP) { return (uint32_t)NP * kCtKS * 2; }
-__host__ __device__ constexpr uint32_t ct_stage_bytes(int NP)
+// Stage layout in shared memory: the three A slices packed at a stride of AR
+// rows (AR = nbf rounded up to 8) -- the MMA reads 128 rows from each slice
+// start, and rows >= AR (the next slice, or the tail) only feed accumulator
+// rows >= nbf, which are never read -- then the three B slices of NP rows,
+// then c_xc[32] and c_j[32].
+__host__ __device__ constexpr uint32_t ct_a_slice_bytes(int AR) { return (uint32_t)AR * kCtKS * 2; }
+__host__ __device__ constexpr uint32_t ct_a_region_bytes(int AR)
 {
-    return (uint32_t)kCtSlices * (ct_a_slice_bytes() + ct_b_slice_bytes(NP)) + 2 * kCtKS * 4;
+    return (uint32_t)(kCtSlices - 1) * ct_a_slice_bytes(AR) + (uint32_t)kCtM * kCtKS * 2;
+}
+__host__ __device__ constexpr uint32_t ct_b_slice_bytes(int NP) { return (uint32_t)NP * kCtKS * 2; }
+__host__ __device__ constexpr uint32_t ct_stage_bytes(int NP, int AR)
+{
+    return ct_a_region_bytes(AR) + (uint32_t)kCtSlices * ct_b_slice_bytes(NP) + 2 * kCtKS * 4;
 }
 
 __global__ void __launch_bounds__(kCtThreads, 1)
 k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_chunk, int nchunk,
               const unsigned char *__restrict__ aslices, const int *__restrict__ rowexp,
-              const int *__restrict__ swexp, const float *__restrict__ winv, const float *__restrict__ cxc,
+              const int *__restrict__ swexp, const int2 *__restrict__ cexp, const float *__restrict__ cxc,
               const float *__restrict__ cj, float2 *__restrict__ part, int *__restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const uint32_t a_slice = ct_a_slice_bytes(), b_slice = ct_b_slice_bytes(NP);
-    const uint32_t stage = ct_stage_bytes(NP);
-    const uint32_t c_off = kCtSlices * (a_slice + b_slice);     // c_xc[32], c_j[32] of the stage
-    const uint32_t a_hbm = (uint32_t)AR * kCtKS * 2;           // bytes of one A slice block in HBM
-    // CTA partial [2][nbf][nbf] double-float in shared memory when spart (else in HBM / L2)
+    const uint32_t a_slice = ct_a_slice_bytes(AR), b_slice = ct_b_slice_bytes(NP);
+    const uint32_t a_region = ct_a_region_bytes(AR);
+    const uint32_t stage = ct_stage_bytes(NP, AR);
+    const uint32_t c_off = a_region + kCtSlices * b_slice;     // c_xc[32], c_j[32] of the stage
+    const size_t ntri = (size_t)nbf * (nbf + 1) / 2;            // packed upper triangle per matrix
+    // CTA partial: XC and J upper triangles, packed (element (mu, nu), mu <= nu, at
+    // nu (nu + 1) / 2 + mu), double-float, in shared memory when spart (else in HBM / L2)
     float2 *s_part = reinterpret_cast<float2 *>(smem + (size_t)nst * stage);
     CtShared *sh = reinterpret_cast<CtShared *>(smem + (size_t)nst * stage +
-                                                (spart ? 2 * (size_t)nbf * nbf * sizeof(float2) : 0));
+                                                (spart ? 2 * ntri * sizeof(float2) : 0));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ float s_colf[2 * kCtMaxNbf];     // column scales of the current chunk (epilogue)
 
     // zero the operand stages once: rows >= AR of A and >= 2 nbf of B are never written
     {
@@ -168,7 +192,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
     if (threadIdx.x == 0) {
         for (int s = 0; s < nst; ++s) {
             mbar_init(&sh->a_full[s], 1);
-            mbar_init(&sh->full[s], 1);
+            mbar_init(&sh->full[s], 4);          // the four producer warps
             mbar_init(&sh->empty[s], 1);
         }
         mbar_init(&sh->tmem_full, 1);
@@ -190,20 +214,27 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
 
     if (warp < 4) {
         // ------------------------------------------------------------ producers
-        const int g = lane & 3, mrow = lane >> 2;      // 8-point group, row within a group of 8 rows
+        // all four warps fill every stage: warp w takes row groups w, w + 4, ...;
+        // lane = (row within the group of 8) x (8-point group g)
+        const int g = lane & 3, mrow = lane >> 2;
         int it = 0;
         bool ok = true;
         for (int ch = blockIdx.x; ch < nchunk && ok; ch += gridDim.x) {
             const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
-            int ex, ej;
-            chunk_v_exps(cxc, cj, winv, (size_t)kb0 * kCtKS, (size_t)kb1 * kCtKS, lane, ex, ej);
-            const float sx = pow2f(-ex), sj = pow2f(-ej);
-            const int *ea = rowexp + (size_t)ch * nbf, *es = swexp + (size_t)ch * nbf;
+            const int2 ce = cexp[ch];
+            const float sx = pow2f(-ce.x), sj = pow2f(-ce.y);
+            // B row scales of this lane's rows for the chunk, in registers
+            float rfr[kCtMaxNbf / 32];
+            {
+                const int *ea = rowexp + (size_t)ch * nbf, *es = swexp + (size_t)ch * nbf;
+#pragma unroll
+                for (int j = 0; j < kCtMaxNbf / 32; ++j) {
+                    const int mu = 32 * j + 8 * warp + mrow;
+                    rfr[j] = mu < nbf ? pow2f(max(-126, min(127, ea[mu] - es[mu]))) : 0.f;
+                }
+            }
             for (int kb = kb0; kb < kb1; ++kb, ++it) {
-                // each ring slot has exactly one producer warp (slot % 4), which
-                // therefore waits on the slot's phases strictly in order
                 const int s = it % nst, n = it / nst;
-                if ((s & 3) != warp) continue;
                 int w_ok = 1;
                 if (lane == 0) w_ok = mbar_wait(&sh->a_full[s], (uint32_t)(n & 1)) ? 1 : 0;
                 w_ok = __shfl_sync(0xffffffffu, w_ok, 0);
@@ -213,7 +244,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                     break;
                 }
                 unsigned char *sA = smem + (size_t)s * stage;
-                unsigned char *sB = sA + kCtSlices * a_slice;
+                unsigned char *sB = sA + a_region;
                 const float *sc = reinterpret_cast<const float *>(sA + c_off);
                 float cx[8], cy[8];
 #pragma unroll
@@ -221,10 +252,13 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                     cx[k] = sc[8 * g + k] * sx;
                     cy[k] = sc[kCtKS + 8 * g + k] * sj;
                 }
-                for (int mu = mrow; mu < nbf; mu += 8) {
+#pragma unroll
+                for (int j = 0; j < kCtMaxNbf / 32; ++j) {
+                    const int mu = 32 * j + 8 * warp + mrow;
+                    if (mu >= nbf) break;
                     const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
                     // B row scale: phi 2^(7 - e_mu) -> phi 2^(7 - s_mu)
-                    const float rf = pow2f(max(-126, min(127, ea[mu] - es[mu])));
+                    const float rf = rfr[j];
                     float v[8], t[8];
                     unpack8(*reinterpret_cast<const uint4 *>(sA + oa), v);
                     unpack8(*reinterpret_cast<const uint4 *>(sA + a_slice + oa), t);
@@ -277,7 +311,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                     }
                     tc_fence_after();
                     const unsigned char *sA = smem + (size_t)s * stage;
-                    const unsigned char *sB = sA + kCtSlices * a_slice;
+                    const unsigned char *sB = sA + a_region;
 #pragma unroll
                     for (int kk = 0; kk < kCtKS / 16; ++kk) {
                         const uint32_t ko = (uint32_t)kk * 2 * lbo;
@@ -311,16 +345,21 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
         const int q = warp & 3;                  // TMEM lane quarter of this warp
         const int h = (warp - 5) >> 2;           // column blocks h, h + 2, ...
         const int r = q * 32 + lane;             // accumulator row = basis function mu
-        const size_t nn = (size_t)nbf * nbf;
-        float2 *gpart = part + (size_t)blockIdx.x * 2 * nn;   // this CTA's partial in HBM
+        float2 *gpart = part + (size_t)blockIdx.x * 2 * ntri;   // this CTA's partial in HBM
         float2 *px = spart ? s_part : gpart;
         int cc = 0;
         for (int ch = blockIdx.x; ch < nchunk; ch += gridDim.x, ++cc) {
             const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
-            int ex, ej;
-            chunk_v_exps(cxc, cj, winv, (size_t)kb0 * kCtKS, (size_t)kb1 * kCtKS, lane, ex, ej);
-            const int *ea = rowexp + (size_t)ch * nbf, *es = swexp + (size_t)ch * nbf;
-            const int er = r < nbf ? ea[r] : 0;
+            // column scales 2^(s_nu + v - 14) of the chunk in shared memory, row scale 2^e_mu in a register
+            {
+                const int2 ce = cexp[ch];
+                const int *es = swexp + (size_t)ch * nbf;
+                for (int n = threadIdx.x - 160; n < 2 * nbf; n += 256) {
+                    const int e = (n < nbf ? es[n] + ce.x : es[n - nbf] + ce.y) - 14;
+                    s_colf[n] = pow2f(max(-126, min(127, e)));
+                }
+            }
+            const float fr = r < nbf ? pow2f(max(-126, min(127, rowexp[(size_t)ch * nbf + r]))) : 0.f;
             const bool ok = mbar_wait(&sh->tmem_full, (uint32_t)(cc & 1));
             if (!ok) { atomicExch(err, 14); sh->fail = 1; }
             ct_epi_bar();
@@ -338,9 +377,10 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
 #pragma unroll
                     for (int k = 0; k < 16; ++k) {
                         const int n = c0 + k;
+                        const int nu = n < nbf ? n : n - nbf;
                         old[k] = make_float2(0.f, 0.f);
-                        if (cc > 0 && n < 2 * nbf)
-                            old[k] = px[(n < nbf ? 0 : nn) + (size_t)(n < nbf ? n : n - nbf) * nbf + r];
+                        if (cc > 0 && n < 2 * nbf && r <= nu)
+                            old[k] = px[(n < nbf ? 0 : ntri) + (size_t)nu * (nu + 1) / 2 + r];
                     }
 #pragma unroll
                     for (int k = 0; k < 16; ++k) {
@@ -348,11 +388,10 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                         if (n >= 2 * nbf) continue;
                         const bool xc = n < nbf;
                         const int nu = xc ? n : n - nbf;
-                        // exact power-of-two scaling (two factors cover the clamped exponent range)
-                        const int sc = er + es[nu] + (xc ? ex : ej) - 14;
-                        const int sc1 = max(-126, min(127, sc));
-                        const float f = pow2f(sc1) * pow2f(max(-126, min(127, sc - sc1)));
-                        const float vh = dh[k] * f, vl = dl[k] * f;
+                        if (r > nu) continue;                  // upper triangle only
+                        // exact power-of-two scaling (row and column factors)
+                        const float f = s_colf[n];
+                        const float vh = (dh[k] * fr) * f, vl = (dl[k] * fr) * f;
                         // (s, e) += vh + vl, then renormalise so |e| <= ulp(s) / 2
                         float s2 = old[k].x, e2 = old[k].y;
                         const float t = s2 + vh;
@@ -360,7 +399,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                         e2 += (s2 - (t - bp)) + (vh - bp) + vl;
                         s2 = t + e2;
                         e2 = e2 - (s2 - t);
-                        px[(xc ? 0 : nn) + (size_t)nu * nbf + r] = make_float2(s2, e2);
+                        px[(xc ? 0 : ntri) + (size_t)nu * (nu + 1) / 2 + r] = make_float2(s2, e2);
                     }
                 }
             }
@@ -369,12 +408,12 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
             if (threadIdx.x == 160) mbar_arrive(&sh->tmem_empty);
         }
         if (spart && !sh->fail) {
-            for (size_t i = threadIdx.x - 160; i < 2 * nn; i += 256) gpart[i] = s_part[i];
+            for (size_t i = threadIdx.x - 160; i < 2 * ntri; i += 256) gpart[i] = s_part[i];
         }
     } else {
         // ------------------------------------------------------------ loader
         if (lane == 0) {
-            const uint32_t tx = kCtSlices * a_hbm + 2 * kCtKS * 4;
+            const uint32_t tx = kCtSlices * a_slice + 2 * kCtKS * 4;
             int it = 0, issued = 0;
             for (int ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
                 const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
@@ -389,8 +428,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                     }
                     unsigned char *sA = smem + (size_t)s * stage;
                     mbar_arrive_expect_tx(&sh->a_full[s], tx);
-                    for (int i = 0; i < kCtSlices; ++i)
-                        bulk_g2s(sA + i * a_slice, aslices + ((size_t)kb * kCtSlices + i) * a_hbm, a_hbm, &sh->a_full[s]);
+                    bulk_g2s(sA, aslices + (size_t)kb * kCtSlices * a_slice, kCtSlices * a_slice, &sh->a_full[s]);
                     bulk_g2s(sA + c_off, cxc + (size_t)kb * kCtKS, kCtKS * 4, &sh->a_full[s]);
                     bulk_g2s(sA + c_off + kCtKS * 4, cj + (size_t)kb * kCtKS, kCtKS * 4, &sh->a_full[s]);
                     issued = it + 1;
@@ -478,9 +516,10 @@ __global__ void k_ct_slice_A(int nbf, int AR, size_t npad, int nkb, int kb_per_c
     }
 }
 
-static size_t ct_smem(int nst, int NP, int nbf, bool spart)
+static size_t ct_smem(int nst, int NP, int AR, int nbf, bool spart)
 {
-    return (size_t)nst * ct_stage_bytes(NP) + (spart ? 2 * (size_t)nbf * nbf * sizeof(float2) : 0) + sizeof(CtShared);
+    return (size_t)nst * ct_stage_bytes(NP, AR) + (spart ? (size_t)nbf * (nbf + 1) * sizeof(float2) : 0) +
+           sizeof(CtShared);
 }
 
 // Sum the double-float CTA partials of every element on or above the diagonal
@@ -492,16 +531,17 @@ __global__ void __launch_bounds__(256) k_contract_tc_reduce(int nbf, int nparts,
                                                             double *__restrict__ XC, double *__restrict__ J)
 {
     __shared__ double shx[8][33], shj[8][33];
-    const size_t nn = (size_t)nbf * nbf;
+    const size_t nn = (size_t)nbf * nbf, ntri = (size_t)nbf * (nbf + 1) / 2;
     const int lx = threadIdx.x & 31, g = threadIdx.x >> 5;
-    const size_t e = (size_t)blockIdx.x * 32 + lx;          // partial element (nu * nbf + mu) = (mu, nu)
+    const size_t e = (size_t)blockIdx.x * 32 + lx;          // element (mu, nu) = e % nbf, e / nbf
     double sx = 0.0, sj = 0.0;
     const int nu = (int)(e / nbf), mu = (int)(e % nbf);
     const bool act = e < nn && mu <= nu;
+    const size_t t = (size_t)nu * (nu + 1) / 2 + mu;        // packed upper-triangle index
     if (act)
         for (int c = g; c < nparts; c += 8) {
-            const float2 *p = part + (size_t)c * 2 * nn;
-            const float2 a = p[e], b = p[nn + e];
+            const float2 *p = part + (size_t)c * 2 * ntri;
+            const float2 a = p[t], b = p[ntri + t];
             sx += (double)a.x + (double)a.y;
             sj += (double)b.x + (double)b.y;
         }
@@ -541,7 +581,7 @@ size_t contract_tc_part_elems(int nbf, size_t npad, int nsm)
     int nkb, kbpc, nchunk;
     ct_plan(npad, nsm, nkb, kbpc, nchunk);
     const int grid = nchunk < nsm ? nchunk : nsm;
-    return (size_t)grid * 2 * nbf * nbf;          // one partial per CTA
+    return (size_t)grid * nbf * (nbf + 1);        // one packed partial (XC and J triangles) per CTA
 }
 
 int contract_tc_setup(dftg_ctx *c)
@@ -552,27 +592,30 @@ int contract_tc_setup(dftg_ctx *c)
     DFTG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
     const int NP = (2 * c->nbf + 15) / 16 * 16;
     const int AR = (c->nbf + 7) / 8 * 8;
+    cudaFuncAttributes fa{};
+    DFTG_CUDA(cudaFuncGetAttributes(&fa, k_contract_tc));
+    optin -= (int)fa.sharedSizeBytes;                 // static shared memory of the kernel
     // keep the CTA partial in shared memory if at least three stages still fit
     bool spart = true;
     int nst = kCtMaxStages;
-    while (nst > 3 && ct_smem(nst, NP, c->nbf, spart) > (size_t)optin) --nst;
-    if (ct_smem(nst, NP, c->nbf, spart) > (size_t)optin) {
+    while (nst > 3 && ct_smem(nst, NP, AR, c->nbf, spart) > (size_t)optin) --nst;
+    if (ct_smem(nst, NP, AR, c->nbf, spart) > (size_t)optin) {
         spart = false;
         nst = kCtMaxStages;
-        while (nst > 2 && ct_smem(nst, NP, c->nbf, spart) > (size_t)optin) --nst;
+        while (nst > 2 && ct_smem(nst, NP, AR, c->nbf, spart) > (size_t)optin) --nst;
     }
-    if (ct_smem(nst, NP, c->nbf, spart) > (size_t)optin) return DFTG_OK;
+    if (ct_smem(nst, NP, AR, c->nbf, spart) > (size_t)optin) return DFTG_OK;
     int nkb, kbpc, nchunk;
     ct_plan(c->npad, nsm, nkb, kbpc, nchunk);
     const int grid = nchunk < nsm ? nchunk : nsm;
-    if ((size_t)grid * 2 * c->nbf * c->nbf > c->part_elems) return DFTG_OK;
+    if ((size_t)grid * c->nbf * (c->nbf + 1) > c->part_elems) return DFTG_OK;
     DFTG_CUDA(cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)ct_smem(nst, NP, c->nbf, spart)));
+                                   (int)ct_smem(nst, NP, AR, c->nbf, spart)));
     if (!c->d_flag) {
         DFTG_CUDA(cudaMalloc(&c->d_flag, sizeof(int)));
         DFTG_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
     }
-    DFTG_CUDA(cudaMalloc(&c->d_ct_rowexp, sizeof(int) * 2 * (size_t)nchunk * c->nbf));
+    DFTG_CUDA(cudaMalloc(&c->d_ct_rowexp, sizeof(int) * 2 * (size_t)nchunk * c->nbf + sizeof(int2) * (size_t)nchunk));
     DFTG_CUDA(cudaMalloc(&c->d_ct_winv, sizeof(float) * c->npad));
     DFTG_CUDA(cudaMalloc(&c->d_ct_A, sizeof(__nv_bfloat16) * (size_t)nkb * kCtSlices * AR * kCtKS));
     k_ct_rowexp<<<nchunk, 256, 0, c->stream>>>(c->nbf, c->npad, nkb, kbpc, c->d_phi32, c->d_w, c->d_ct_rowexp,
@@ -598,10 +641,13 @@ int contract_tc_setup(dftg_ctx *c)
 
 int launch_contract_tc(dftg_ctx *c)
 {
-    k_contract_tc<<<c->ct_grid, kCtThreads, ct_smem(c->ct_nst, c->ct_NP, c->nbf, c->ct_spart != 0), c->stream>>>(
+    int2 *cexp = reinterpret_cast<int2 *>(c->d_ct_rowexp + 2 * (size_t)c->ct_nchunk * c->nbf);
+    k_ct_cexp<<<c->ct_nchunk, 256, 0, c->stream>>>(c->ct_nkb, c->ct_kbpc, c->d_cxc32, c->d_cj32, c->d_ct_winv, cexp);
+    DFTG_LAUNCH_CHECK();
+    k_contract_tc<<<c->ct_grid, kCtThreads, ct_smem(c->ct_nst, c->ct_NP, c->ct_AR, c->nbf, c->ct_spart != 0), c->stream>>>(
         c->nbf, c->ct_AR, c->ct_NP, c->ct_nst, c->ct_spart, c->ct_nkb, c->ct_kbpc, c->ct_nchunk,
         reinterpret_cast<const unsigned char *>(c->d_ct_A), c->d_ct_rowexp,
-        c->d_ct_rowexp + (size_t)c->ct_nchunk * c->nbf, c->d_ct_winv, c->d_cxc32, c->d_cj32,
+        c->d_ct_rowexp + (size_t)c->ct_nchunk * c->nbf, cexp, c->d_cxc32, c->d_cj32,
         reinterpret_cast<float2 *>(c->d_part), c->d_flag);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;

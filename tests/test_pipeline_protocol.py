@@ -1,35 +1,46 @@
 """Model of the mbarrier protocol of the tensor-core contraction kernel
 (dftcxx_gb300/csrc/k_contract_tc.cu), checked on the CPU under random
-schedules: ring slots with a loader (A slices), producer warps (B slices),
-one MMA issuer and the epilogue.  A wait passes when the phase of the given
-parity has completed, as mbarrier.try_wait.parity does (a fresh barrier
-counts its preceding phase as complete).  The kernel's rule -- each ring slot
-is produced by exactly one warp (slot % 4) -- must keep every stage's data
-consistent for every ring depth; the rule "stage % 4" fails for rings shorter
-than the number of producer warps."""
+schedules: ring slots with a loader (A slices), four producer warps (B
+slices), one MMA issuer and the epilogue.  A wait passes when the phase of the
+given parity has completed, as mbarrier.try_wait.parity does (a fresh barrier
+counts its preceding phase as complete).  In the kernel every producer warp
+fills its rows of every stage and the stage-full barrier expects four
+arrivals; each waiter then sees each slot's phases strictly in order, which
+keeps every stage's data consistent for every ring depth.  Splitting stages
+between warps round-robin instead ("stage % 4") breaks rings shorter than the
+number of warps: a warp then waits on a parity whose preceding phase counts as
+complete and reads a stage that has not landed."""
 import random
 
 import pytest
 
 
 class _Bar:
-    def __init__(self):
+    def __init__(self, count=1):
         self.ph = 0
+        self.count = count
+        self.pending = count
 
     def arrive(self):
-        self.ph += 1
+        self.pending -= 1
+        if self.pending == 0:
+            self.ph += 1
+            self.pending = self.count
 
     def ok(self, parity):
         return (self.ph & 1) != parity
 
 
-def _run(nst, chunks, owner, seed):
+def _run(nst, chunks, owner, seed, per_stage=1):
+    """owner(it, s) -> the producing warp of stage it, or None when all
+    per_stage warps produce every stage (full barrier count per_stage)."""
     rng = random.Random(seed)
     a_full = [_Bar() for _ in range(nst)]
-    full = [_Bar() for _ in range(nst)]
+    full = [_Bar(per_stage) for _ in range(nst)]
     empty = [_Bar() for _ in range(nst)]
     tmem_full, tmem_empty = _Bar(), _Bar()
-    a_in, b_in = [None] * nst, [None] * nst
+    a_in = [None] * nst
+    b_in = [[None] * 4 for _ in range(nst)]
     ns = sum(chunks)
 
     def loader():
@@ -44,13 +55,16 @@ def _run(nst, chunks, owner, seed):
     def producer(w):
         for it in range(ns):
             s, n = it % nst, it // nst
-            if owner(it, s) != w:
+            if owner is not None and owner(it, s) != w:
                 continue
             while not a_full[s].ok(n & 1):
                 yield
             if a_in[s] != it:
                 raise AssertionError("producer %d read stage %s for %d" % (w, a_in[s], it))
-            b_in[s] = it
+            for part in range(4):
+                if owner is None and part != w:
+                    continue
+                b_in[s][part] = it
             yield
             full[s].arrive()
 
@@ -63,7 +77,7 @@ def _run(nst, chunks, owner, seed):
                 s, n = it % nst, it // nst
                 while not full[s].ok(n & 1):
                     yield
-                if a_in[s] != it or b_in[s] != it:
+                if a_in[s] != it or any(b != it for b in b_in[s]):
                     raise AssertionError("MMA saw (%s, %s) for %d" % (a_in[s], b_in[s], it))
                 yield
                 empty[s].arrive()
@@ -92,9 +106,15 @@ def _run(nst, chunks, owner, seed):
 
 @pytest.mark.parametrize("nst", [2, 3, 4, 5, 6, 8])
 @pytest.mark.parametrize("chunks", [[8] * 7, [8] * 6 + [3], [1, 1, 2], [5]])
-def test_slot_owned_producers_keep_stages_consistent(nst, chunks):
+def test_all_warps_per_stage_keep_stages_consistent(nst, chunks):
     for seed in range(20):
-        _run(nst, chunks, lambda it, s: s & 3, seed)
+        _run(nst, chunks, None, seed, per_stage=4)
+
+
+@pytest.mark.parametrize("nst", [2, 3, 4, 8])
+def test_slot_owned_producers_keep_stages_consistent(nst):
+    for seed in range(20):
+        _run(nst, [8] * 7, lambda it, s: s & 3, seed)
 
 
 def test_stage_round_robin_breaks_short_rings():
