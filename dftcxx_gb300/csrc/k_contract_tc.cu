@@ -181,6 +181,8 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                                                 (spart ? 2 * ntri * sizeof(float2) : 0));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __shared__ float s_colf[2 * kCtMaxNbf];     // column scales of the current chunk (epilogue)
+    __shared__ int s_coloff[2 * kCtMaxNbf];     // packed-triangle offset of column n, row 0
+    __shared__ int s_colnu[2 * kCtMaxNbf];      // basis function of column n
 
     // zero the operand stages once: rows >= AR of A and >= 2 nbf of B are never written
     {
@@ -355,8 +357,13 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                 const int2 ce = cexp[ch];
                 const int *es = swexp + (size_t)ch * nbf;
                 for (int n = threadIdx.x - 160; n < 2 * nbf; n += 256) {
-                    const int e = (n < nbf ? es[n] + ce.x : es[n - nbf] + ce.y) - 14;
+                    const int nu = n < nbf ? n : n - nbf;
+                    const int e = es[nu] + (n < nbf ? ce.x : ce.y) - 14;
                     s_colf[n] = pow2f(max(-126, min(127, e)));
+                    if (cc == 0) {
+                        s_colnu[n] = nu;
+                        s_coloff[n] = (n < nbf ? 0 : (int)ntri) + nu * (nu + 1) / 2;
+                    }
                 }
             }
             const float fr = r < nbf ? pow2f(max(-126, min(127, rowexp[(size_t)ch * nbf + r]))) : 0.f;
@@ -372,35 +379,35 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                 tmem_ld16(ta + 256u + (uint32_t)c0, dl);
                 tmem_wait_ld();
                 if (r < nbf) {
-                    // all loads of the block before its stores, so they are in flight together
+                    // (s, e) += (D_hi + D_lo) 2^(e_mu + s_nu + v - 14) for the upper-triangle
+                    // elements of the block: column tables and old values first, then the
+                    // arithmetic, then the stores, so no access waits on another
+                    const int kend = min(16, 2 * nbf - c0);
+                    int off[16];
+                    float fk[16];
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        const bool v = k < kend && r <= s_colnu[c0 + k];
+                        off[k] = v ? s_coloff[c0 + k] + r : -1;
+                        fk[k] = v ? s_colf[c0 + k] * fr : 0.f;   // exact power of two
+                    }
                     float2 old[16];
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) {
-                        const int n = c0 + k;
-                        const int nu = n < nbf ? n : n - nbf;
-                        old[k] = make_float2(0.f, 0.f);
-                        if (cc > 0 && n < 2 * nbf && r <= nu)
-                            old[k] = px[(n < nbf ? 0 : ntri) + (size_t)nu * (nu + 1) / 2 + r];
-                    }
+                    for (int k = 0; k < 16; ++k)
+                        old[k] = (cc > 0 && off[k] >= 0) ? px[off[k]] : make_float2(0.f, 0.f);
 #pragma unroll
                     for (int k = 0; k < 16; ++k) {
-                        const int n = c0 + k;
-                        if (n >= 2 * nbf) continue;
-                        const bool xc = n < nbf;
-                        const int nu = xc ? n : n - nbf;
-                        if (r > nu) continue;                  // upper triangle only
-                        // exact power-of-two scaling (row and column factors)
-                        const float f = s_colf[n];
-                        const float vh = (dh[k] * fr) * f, vl = (dl[k] * fr) * f;
-                        // (s, e) += vh + vl, then renormalise so |e| <= ulp(s) / 2
+                        const float vh = dh[k] * fk[k], vl = dl[k] * fk[k];
                         float s2 = old[k].x, e2 = old[k].y;
                         const float t = s2 + vh;
                         const float bp = t - s2;
                         e2 += (s2 - (t - bp)) + (vh - bp) + vl;
-                        s2 = t + e2;
-                        e2 = e2 - (s2 - t);
-                        px[(xc ? 0 : ntri) + (size_t)nu * (nu + 1) / 2 + r] = make_float2(s2, e2);
+                        s2 = t + e2;                                 // renormalise: |e| <= ulp(s) / 2
+                        old[k] = make_float2(s2, e2 - (s2 - t));
                     }
+#pragma unroll
+                    for (int k = 0; k < 16; ++k)
+                        if (off[k] >= 0) px[off[k]] = old[k];
                 }
             }
             tc_fence_before();
@@ -418,6 +425,13 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
             for (int ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
                 const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
                 bool ok = true;
+                // L2 prefetch: this chunk's A block (first chunk only) and the next chunk's
+                for (int pc = (ch == (int)blockIdx.x ? ch : ch + (int)gridDim.x); pc <= ch + (int)gridDim.x; pc += (int)gridDim.x) {
+                    if (pc >= nchunk) break;
+                    const int p0 = pc * kb_per_chunk, p1 = min(nkb, p0 + kb_per_chunk);
+                    for (int kb = p0; kb < p1; ++kb)
+                        prefetch_l2(aslices + (size_t)kb * kCtSlices * a_slice, kCtSlices * a_slice);
+                }
                 for (int kb = kb0; kb < kb1; ++kb, ++it) {
                     const int s = it % nst, n = it / nst;
                     if (!mbar_wait(&sh->empty[s], (uint32_t)((n & 1) ^ 1)) || sh->fail) {

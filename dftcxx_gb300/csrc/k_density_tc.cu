@@ -114,8 +114,16 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
         // ------------------------------------------------------------ producer
         int issued = 0;
         if (lane == 0) {
+            // L2 prefetch two tiles ahead of the bulk copies
+            for (int it = 0; it < 2 && it < my_tiles; ++it)
+                for (int i = 0; i < kTcSlices; ++i)
+                    prefetch_l2(Aslices + ((size_t)i * ntiles + blockIdx.x + it * gridDim.x) * a_slice_bytes, a_slice_bytes);
             for (int it = 0; it < my_tiles; ++it) {
                 const int s = it & 1, n = it >> 1;
+                if (it + 2 < my_tiles)
+                    for (int i = 0; i < kTcSlices; ++i)
+                        prefetch_l2(Aslices + ((size_t)i * ntiles + blockIdx.x + (it + 2) * gridDim.x) * a_slice_bytes,
+                                    a_slice_bytes);
                 if (!mbar_wait(&sh->empty[s], (uint32_t)((n & 1) ^ 1))) { atomicExch(err, 1); s_fail = 1; break; }
                 if (s_fail) break;
                 const int tile = (int)blockIdx.x + it * (int)gridDim.x;

@@ -1,8 +1,8 @@
 // k_integrals.cu -- K7: one-electron matrices S, T, V in FP64 on the device.
 //
-// One thread per basis-function pair (i <= j).  Primitive integrals follow the
-// reference's Obara-Saika / THO formulas: overlap through binomial prefactors
-// (integrals.cpp:252-290), kinetic from shifted overlaps (integrals.cpp:101-121)
+// Primitive integrals follow the reference's Obara-Saika / THO formulas:
+// overlap through binomial prefactors (integrals.cpp:252-290), kinetic from
+// shifted overlaps (integrals.cpp:101-121)
 // and nuclear attraction through the A-array and the Boys function
 // (integrals.cpp:336-387), with the truncated pi of integrals.cpp:342.
 // Boys function F_m(x): the reference clamps x = max(|x|, 1e-8) and evaluates
@@ -144,12 +144,15 @@ __device__ double nuc_prim_d(const double *A, int l1, int m1, int n1, double a1,
     return -2.0 * kPiTrunc / g * exp(-a1 * a2 * rab2 / g) * sum;
 }
 
-__global__ void k_one_electron(int nbf, int natoms, const double *__restrict__ atoms, const int *__restrict__ bf_lmn,
-                               const int *__restrict__ bf_off, const int *__restrict__ bf_atom,
-                               const double *__restrict__ pa, const double *__restrict__ pcn, double *S, double *T,
-                               double *V)
+// One warp per basis-function pair (i <= j); the lanes share the (primitive
+// pair, nucleus) terms -- nucleus slot 0 carries the overlap and kinetic terms --
+// and the warp sums them in a fixed shuffle order.
+__global__ void __launch_bounds__(128) k_one_electron(int nbf, int natoms, const double *__restrict__ atoms,
+                                                      const int *__restrict__ bf_lmn, const int *__restrict__ bf_off,
+                                                      const int *__restrict__ bf_atom, const double *__restrict__ pa,
+                                                      const double *__restrict__ pcn, double *S, double *T, double *V)
 {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int id = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     const int npair = nbf * (nbf + 1) / 2;
     if (id >= npair) return;
     // id -> (i, j), i <= j, row-major over the upper triangle
@@ -159,21 +162,28 @@ __global__ void k_one_electron(int nbf, int natoms, const double *__restrict__ a
     const int *qi = bf_lmn + 3 * i, *qj = bf_lmn + 3 * j;
     const double A[3] = {atoms[4 * bf_atom[i]], atoms[4 * bf_atom[i] + 1], atoms[4 * bf_atom[i] + 2]};
     const double B[3] = {atoms[4 * bf_atom[j]], atoms[4 * bf_atom[j] + 1], atoms[4 * bf_atom[j] + 2]};
+    const int ki = bf_off[i], ni = bf_off[i + 1] - ki, kj = bf_off[j], nj = bf_off[j + 1] - kj;
+    const int nterm = ni * nj * (natoms + 1);
     double s = 0.0, t = 0.0, v = 0.0;
-    for (int k = bf_off[i]; k < bf_off[i + 1]; ++k)
-        for (int l = bf_off[j]; l < bf_off[j + 1]; ++l) {
-            const double pre = pcn[k] * pcn[l];
+    for (int e = lane; e < nterm; e += 32) {
+        const int c = e / (ni * nj) - 1, pr = e % (ni * nj);
+        const int k = ki + pr / nj, l = kj + pr % nj;
+        const double pre = pcn[k] * pcn[l];
+        if (c < 0) {
             s += pre * ovl_prim_d(pa[k], qi[0], qi[1], qi[2], A, pa[l], qj[0], qj[1], qj[2], B);
             t += pre * kin_prim_d(pa[k], qi[0], qi[1], qi[2], A, pa[l], qj[0], qj[1], qj[2], B);
+        } else {
+            const double C[3] = {atoms[4 * c], atoms[4 * c + 1], atoms[4 * c + 2]};
+            v += atoms[4 * c + 3] * pre * nuc_prim_d(A, qi[0], qi[1], qi[2], pa[k], B, qj[0], qj[1], qj[2], pa[l], C);
         }
-    for (int c = 0; c < natoms; ++c) {
-        const double C[3] = {atoms[4 * c], atoms[4 * c + 1], atoms[4 * c + 2]};
-        double vs = 0.0;
-        for (int k = bf_off[i]; k < bf_off[i + 1]; ++k)
-            for (int l = bf_off[j]; l < bf_off[j + 1]; ++l)
-                vs += pcn[k] * pcn[l] * nuc_prim_d(A, qi[0], qi[1], qi[2], pa[k], B, qj[0], qj[1], qj[2], pa[l], C);
-        v += vs * atoms[4 * c + 3];
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        t += __shfl_xor_sync(0xffffffffu, t, o);
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    if (lane != 0) return;
     const size_t ij = (size_t)i + (size_t)j * nbf, ji = (size_t)j + (size_t)i * nbf;
     S[ij] = s; S[ji] = s;
     T[ij] = t; T[ji] = t;
@@ -183,8 +193,8 @@ __global__ void k_one_electron(int nbf, int natoms, const double *__restrict__ a
 int launch_one_electron(dftg_ctx *c, double *dS, double *dT, double *dV)
 {
     const int npair = c->nbf * (c->nbf + 1) / 2;
-    k_one_electron<<<(npair + 63) / 64, 64, 0, c->stream>>>(c->nbf, c->natoms, c->d_atoms, c->d_bf_lmn, c->d_bf_off,
-                                                            c->d_bf_atom, c->d_pa, c->d_pcn, dS, dT, dV);
+    k_one_electron<<<(npair + 3) / 4, 128, 0, c->stream>>>(c->nbf, c->natoms, c->d_atoms, c->d_bf_lmn, c->d_bf_off,
+                                                           c->d_bf_atom, c->d_pa, c->d_pcn, dS, dT, dV);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }
