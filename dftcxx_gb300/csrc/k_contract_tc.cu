@@ -295,6 +295,8 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(kCtM, NP);
             const uint32_t lbo = 128, sbo = kCtKcores * 128;
+            // descriptors built once; every operand is a fixed byte offset from these
+            const uint64_t desc0 = smem_desc(smem, lbo, sbo);
             const uint32_t d_hi = tmem, d_lo = tmem + 256;
             int it = 0, cc = 0;
             bool ok = true;
@@ -312,8 +314,8 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                         break;
                     }
                     tc_fence_after();
-                    const unsigned char *sA = smem + (size_t)s * stage;
-                    const unsigned char *sB = sA + a_region;
+                    const uint64_t a_st = desc_add(desc0, (uint32_t)s * stage);
+                    const uint64_t b_st = desc_add(a_st, a_region);
 #pragma unroll
                     for (int kk = 0; kk < kCtKS / 16; ++kk) {
                         const uint32_t ko = (uint32_t)kk * 2 * lbo;
@@ -321,8 +323,8 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                         for (int i = 0; i < kCtSlices; ++i)
 #pragma unroll
                             for (int j = 0; i + j < kCtSlices; ++j) {
-                                const uint64_t ad = smem_desc(sA + i * a_slice + ko, lbo, sbo);
-                                const uint64_t bd = smem_desc(sB + j * b_slice + ko, lbo, sbo);
+                                const uint64_t ad = desc_add(a_st, i * a_slice + ko);
+                                const uint64_t bd = desc_add(b_st, j * b_slice + ko);
                                 if (i == 0 && j == 0) {
                                     mma_bf16(d_hi, ad, bd, idesc, acc_hi);
                                     acc_hi = 1;

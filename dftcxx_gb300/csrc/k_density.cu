@@ -108,50 +108,51 @@ __global__ void __launch_bounds__(128) k_density_split(int nbf, size_t npad, con
 }
 
 // stage 1: partial sums of w*rho over chunks that never straddle two atoms
-__global__ void k_atom_partials(size_t per_atom, int chunks_per_atom, const double *__restrict__ w,
-                                const double *__restrict__ rho, double *__restrict__ part)
+__global__ void __launch_bounds__(kRedBlock) k_atom_sums(size_t per_atom, int chunks_per_atom, int natoms,
+                                                          const double *__restrict__ w, const double *__restrict__ rho,
+                                                          double *__restrict__ part, const double *__restrict__ atoms,
+                                                          double *scal, int mode, int *counter)
 {
-    __shared__ double sh[kRedBlock];
+    __shared__ double sh[32];
+    __shared__ double sq[kMaxAtoms];
+    __shared__ int s_last;
     const int b = blockIdx.x;
     const int a = b / chunks_per_atom, ch = b % chunks_per_atom;
     const size_t base = (size_t)a * per_atom;
     const size_t lo = (size_t)ch * kRedChunk, hi = min(per_atom, lo + kRedChunk);
     double s = 0.0;
     for (size_t i = lo + threadIdx.x; i < hi; i += kRedBlock) s += w[base + i] * rho[base + i];
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = kRedBlock / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) part[b] = sh[0];
-}
-
-// stage 2 (one warp): per-atom sums, total, correction factor
-__global__ void k_atom_final(int natoms, int chunks_per_atom, const double *__restrict__ part,
-                             const double *__restrict__ atoms, double *scal, int mode)
-{
-    if (threadIdx.x != 0) return;
-    double total = 0.0, charge = 0.0;
-    for (int a = 0; a < natoms; ++a) {
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) part[b] = s;
+    if (!last_block(counter, &s_last)) return;
+    // last block: per-atom sums in chunk order, total, correction factor
+    for (int t = threadIdx.x; t < natoms; t += kRedBlock) {
         double q = 0.0;
-        for (int ch = 0; ch < chunks_per_atom; ++ch) q += part[a * chunks_per_atom + ch];
-        scal[kScalAtomQ + a] = q;
-        total += q;
-        charge += atoms[4 * a + 3];
+        for (int c = 0; c < chunks_per_atom; ++c) q += __ldcg(part + (size_t)t * chunks_per_atom + c);
+        sq[t] = q;
     }
-    if (mode == 0) {           // before correction; charges scaled to the corrected density
-        scal[kScalSum] = total;
-        const double cf = charge / total;
-        scal[kScalScale] = cf;
-        double n = 0.0;
-        for (int a = 0; a < natoms; ++a) {
-            scal[kScalAtomQ + a] *= cf;
-            n += scal[kScalAtomQ + a];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double total = 0.0, charge = 0.0;
+        for (int t = 0; t < natoms; ++t) {
+            total += sq[t];
+            charge += atoms[4 * t + 3];
         }
-        scal[kScalNelec] = n;
-    } else {                   // after correction
-        scal[kScalNelec] = total;
+        if (mode == 0) {           // before correction; charges scaled to the corrected density
+            scal[kScalSum] = total;
+            const double cf = charge / total;
+            scal[kScalScale] = cf;
+            double n = 0.0;
+            for (int t = 0; t < natoms; ++t) {
+                const double q = sq[t] * cf;
+                scal[kScalAtomQ + t] = q;
+                n += q;
+            }
+            scal[kScalNelec] = n;
+        } else {                   // after correction
+            for (int t = 0; t < natoms; ++t) scal[kScalAtomQ + t] = sq[t];
+            scal[kScalNelec] = total;
+        }
     }
 }
 
@@ -276,11 +277,12 @@ __device__ void lda_point_mixed(double rho, double &e, float &v)
 
 template <bool MIXED>
 __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restrict__ rho,
-                                                   const double *__restrict__ w, const double *__restrict__ scal,
+                                                   const double *__restrict__ w, double *__restrict__ scal,
                                                    int apply_scale, double *__restrict__ cxc,
-                                                   float *__restrict__ cxc32, double *__restrict__ part)
+                                                   float *__restrict__ cxc32, double *__restrict__ part, int *counter)
 {
-    __shared__ double sh[kRedBlock];
+    __shared__ double sh[32];
+    __shared__ int s_last;
     const size_t p = (size_t)blockIdx.x * kRedBlock + threadIdx.x;
     double ew = 0.0;
     if (p < npad) {
@@ -304,27 +306,14 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
         cxc[p] = c;
         cxc32[p] = (float)c;
     }
-    sh[threadIdx.x] = ew;
-    __syncthreads();
-    for (int o = kRedBlock / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
-}
-
-__global__ void k_sum_to_scalar(int n, const double *__restrict__ part, double *scal, int slot)
-{
-    __shared__ double sh[kRedBlock];
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += kRedBlock) s += part[i];
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = kRedBlock / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) scal[slot] = sh[0];
+    ew = block_sum(ew, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = ew;
+    if (!last_block(counter, &s_last)) return;
+    // last block: E_xc = sum of the block partials (fixed assignment and order)
+    double t = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += kRedBlock) t += __ldcg(part + i);
+    t = block_sum(t, sh);
+    if (threadIdx.x == 0) scal[kScalExc] = t;
 }
 
 // ---------------------------------------------------------------- launchers
@@ -357,16 +346,15 @@ int launch_atom_sums(dftg_ctx *c, int mode)
     const size_t per_atom = (size_t)c->nrad * c->nang;
     const int cpa = (int)((per_atom + kRedChunk - 1) / kRedChunk);
     const int nb = cpa * c->natoms;
-    k_atom_partials<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, c->d_w, c->d_rho, c->d_red);
-    DFTG_LAUNCH_CHECK();
-    k_atom_final<<<1, 32, 0, c->stream>>>(c->natoms, cpa, c->d_red, c->d_atoms, c->d_scal, mode == kSumsOnly ? 1 : 0);
+    int *cnt = c->d_counters + kCntAtoms;
+    k_atom_sums<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, c->natoms, c->d_w, c->d_rho, c->d_red, c->d_atoms,
+                                                 c->d_scal, mode == kSumsOnly ? 1 : 0, cnt);
     DFTG_LAUNCH_CHECK();
     if (mode == kSumsCorrect) {
         k_scale<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, c->d_scal, c->d_rho);
         DFTG_LAUNCH_CHECK();
-        k_atom_partials<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, c->d_w, c->d_rho, c->d_red);
-        DFTG_LAUNCH_CHECK();
-        k_atom_final<<<1, 32, 0, c->stream>>>(c->natoms, cpa, c->d_red, c->d_atoms, c->d_scal, 1);
+        k_atom_sums<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, c->natoms, c->d_w, c->d_rho, c->d_red, c->d_atoms,
+                                                     c->d_scal, 1, cnt);
         DFTG_LAUNCH_CHECK();
     }
     DFTG_MARK(c, "charge");
@@ -379,12 +367,10 @@ int launch_xc_points(dftg_ctx *c, bool apply_scale)
     const int sc = apply_scale ? 1 : 0;
     if (c->prec_mask & kPrecLda)
         k_lda<true><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_scal, sc, c->d_cxc, c->d_cxc32,
-                                                     c->d_red);
+                                                     c->d_red, c->d_counters + kCntLda);
     else
         k_lda<false><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_scal, sc, c->d_cxc,
-                                                      c->d_cxc32, c->d_red);
-    DFTG_LAUNCH_CHECK();
-    k_sum_to_scalar<<<1, kRedBlock, 0, c->stream>>>((int)nb, c->d_red, c->d_scal, kScalExc);
+                                                      c->d_cxc32, c->d_red, c->d_counters + kCntLda);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "lda");
     return DFTG_OK;

@@ -143,29 +143,31 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(kTcTile, NP);
             const uint32_t lbo = 128, sbo = (uint32_t)(KP / 8) * 128;
+            // descriptors built once; every operand is a fixed byte offset from these
+            const uint64_t a_desc0 = smem_desc(sA, lbo, sbo), b_desc0 = smem_desc(sB, lbo, sbo);
+            const int ksteps = KP / 16;
             for (int it = 0; it < my_tiles; ++it) {
                 const int s = it & 1, n = it >> 1;   // A stage and TMEM buffer share the index
                 if (!mbar_wait(&sh->full[s], (uint32_t)(n & 1))) { atomicExch(err, 2); s_fail = 1; break; }
                 if (!mbar_wait(&sh->tmem_empty[s], (uint32_t)((n & 1) ^ 1))) { atomicExch(err, 3); s_fail = 1; break; }
                 if (s_fail) break;
                 tc_fence_after();
-                const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
+                const uint64_t a_st = desc_add(a_desc0, (uint32_t)s * a_stage_bytes);
                 const uint32_t d_hi = tmem + (uint32_t)(s * 256), d_lo = d_hi + 128;
-                int first_lo = 1;
+                // leading product A_1 B_1 into D_hi, then the nine correction pairs into D_lo
+                for (int kk = 0; kk < ksteps; ++kk)
+                    mma_bf16(d_hi, desc_add(a_st, kk * 2 * lbo), desc_add(b_desc0, kk * 2 * lbo), idesc, kk > 0 ? 1u : 0u);
+                uint32_t acc = 0u;
+#pragma unroll
                 for (int i = 1; i <= 4; ++i)
+#pragma unroll
                     for (int j = 1; i + j <= 5; ++j) {
-                        const unsigned char *ai = a0 + (size_t)(i - 1) * a_slice_bytes;
-                        const unsigned char *bj = sB + (size_t)(j - 1) * b_slice_bytes;
-                        const bool hi = (i == 1 && j == 1);
-                        for (int kk = 0; kk < KP / 16; ++kk) {
-                            const uint64_t ad = smem_desc(ai + (size_t)kk * 2 * lbo, lbo, sbo);
-                            const uint64_t bd = smem_desc(bj + (size_t)kk * 2 * lbo, lbo, sbo);
-                            if (hi) {
-                                mma_bf16(d_hi, ad, bd, idesc, kk > 0 ? 1u : 0u);
-                            } else {
-                                mma_bf16(d_lo, ad, bd, idesc, first_lo ? 0u : 1u);
-                                first_lo = 0;
-                            }
+                        if (i == 1 && j == 1) continue;
+                        const uint64_t ai = desc_add(a_st, (uint32_t)(i - 1) * a_slice_bytes);
+                        const uint64_t bj = desc_add(b_desc0, (uint32_t)(j - 1) * b_slice_bytes);
+                        for (int kk = 0; kk < ksteps; ++kk) {
+                            mma_bf16(d_lo, desc_add(ai, kk * 2 * lbo), desc_add(bj, kk * 2 * lbo), idesc, acc);
+                            acc = 1u;
                         }
                     }
                 mma_commit(&sh->tmem_full[s]);

@@ -93,6 +93,10 @@ __device__ __forceinline__ uint64_t smem_desc(const void *base, uint32_t lbo, ui
     return a | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
 }
 
+// descriptor of the same layout at base + bytes (bytes a multiple of 16; the
+// start-address field counts 16-byte units and the result stays below 256 KB)
+__device__ __forceinline__ uint64_t desc_add(uint64_t d, uint32_t bytes) { return d + (uint64_t)(bytes >> 4); }
+
 // instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
 {
