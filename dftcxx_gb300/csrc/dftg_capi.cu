@@ -77,7 +77,7 @@ static void free_ctx(dftg_ctx *c)
                     c->d_rec32, c->d_rholm, c->d_U, c->d_U32, c->d_Y32, c->d_Ywt32, c->d_fold, c->d_Gt,
                     c->d_Gb, c->d_Kt, c->d_sx, c->d_splf, c->d_spl, c->d_splm, c->d_tiles,
                     c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_flag,
-                    c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv};
+                    c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -173,6 +173,8 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     c->red_elems = reduction_elems(c->npad, c->natoms, c->nrad, c->nang) + 64;
     DFTG_TRY(dalloc(&c->d_red, c->red_elems));
     DFTG_TRY(dalloc(&c->d_scal, scal_elems(c->natoms)));
+    DFTG_CUDA(cudaMalloc(&c->d_counters, sizeof(int) * kNumCounters));
+    DFTG_CUDA(cudaMemset(c->d_counters, 0, sizeof(int) * kNumCounters));
     DFTG_CUDA(cudaMallocHost(&c->h_scal, sizeof(double) * scal_elems(c->natoms)));
     DFTG_TRY(dalloc(&c->d_Y, nlm * c->nang));
     DFTG_TRY(dalloc(&c->d_Yw, nlm * c->nang));

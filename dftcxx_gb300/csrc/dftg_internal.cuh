@@ -45,6 +45,76 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &e, float x)
     s = t;
 }
 
+// Double-float arithmetic (value = h + l, |l| <= ulp(h) / 2): about 48-bit
+// precision from FP32 operations, for per-build loops that would otherwise run
+// in FP64 (slow on this GPU).  TwoSum / TwoProd with fmaf (Dekker, Knuth).
+struct dfl {
+    float h, l;
+};
+__device__ __forceinline__ dfl df_norm(float s, float e)
+{
+    const float h = s + e;
+    return {h, e - (h - s)};
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b)
+{
+    const float s = a.h + b.h;
+    const float bp = s - a.h;
+    const float e = (a.h - (s - bp)) + (b.h - bp) + a.l + b.l;
+    return df_norm(s, e);
+}
+__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b)
+{
+    const float p = a.h * b.h;
+    const float e = fmaf(a.h, b.h, -p) + (a.h * b.l + a.l * b.h);
+    return df_norm(p, e);
+}
+__device__ __forceinline__ dfl df_fma(dfl acc, dfl a, dfl b) { return df_add(acc, df_mul(a, b)); }
+__host__ __device__ __forceinline__ dfl df_from(double x)
+{
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+__device__ __forceinline__ double df_to(dfl a) { return (double)a.h + (double)a.l; }
+
+// Deterministic sum of v over the block (blockDim.x a multiple of 32, at most
+// 1024): butterfly shuffles inside each warp, then warp totals in warp order.
+// The result is valid in thread 0.  sh: 32 doubles of shared memory.
+__device__ __forceinline__ double block_sum(double v, double *sh)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+    __syncthreads();
+    return s;
+}
+
+// True in exactly one block: the last to get here.  Every block's global writes
+// made before the call are visible to that block (read them with __ldcg).  The
+// counter is reset for the next launch.
+__device__ __forceinline__ bool last_block(int *counter, int *s_flag)
+{
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int t = atomicAdd(counter, 1);
+        *s_flag = (t == (int)gridDim.x - 1) ? 1 : 0;
+        if (*s_flag) *counter = 0;
+    }
+    __syncthreads();
+    if (*s_flag) __threadfence();
+    return *s_flag != 0;
+}
+
+// counters of the last-block reductions
+enum { kCntAtoms = 0, kCntLda = 1, kCntEJ = 2, kNumCounters = 4 };
+
 }  // namespace dftg
 
 struct dftg_ctx {
@@ -82,6 +152,7 @@ struct dftg_ctx {
     double *d_x = nullptr, *d_y = nullptr, *d_z = nullptr;
     double *d_w = nullptr, *d_wb = nullptr;
     double *d_rho = nullptr, *d_V = nullptr, *d_Vown = nullptr;
+    double *d_invr = nullptr;     // [npts] 1 / distance to the owning atom
     double *d_cxc = nullptr, *d_cj = nullptr;
     float *d_cxc32 = nullptr, *d_cj32 = nullptr;
     double *d_phi = nullptr;
@@ -99,6 +170,7 @@ struct dftg_ctx {
     double *d_red = nullptr;      // reduction partials
     size_t red_elems = 0;
     double *d_scal = nullptr;     // scalars, see kScal* below
+    int *d_counters = nullptr;    // [kNumCounters] last-block counters (zero between launches)
     double *h_scal = nullptr;     // pinned host mirror of d_scal
 
     // device: Hartree
@@ -117,6 +189,7 @@ struct dftg_ctx {
     double *d_Gt = nullptr;       // [lmax+1][nrad (k)][nrad (i)] radial Poisson solution map
     double *d_Gb = nullptr;       // [nrad] boundary column of the l = 0 map (times q_a)
     double *d_Kt = nullptr;       // [nrad (j)][nrad (i)] spline derivative map
+    float *d_maps32 = nullptr;    // double-float (hi block, lo block) copies of Gt, Gb, Kt, 1/h, fold
     size_t npairs = 0;            // (point, other atom) pairs of the cross-atom potential
     void *d_pairs = nullptr;      // [npairs] float4 (unit vector, 1/r) then [npairs] float2 (t, k << 16 | interval),
                                   // ordered by (atom, spline interval)

@@ -254,35 +254,49 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                     cx[k] = sc[8 * g + k] * sx;
                     cy[k] = sc[kCtKS + 8 * g + k] * sj;
                 }
+                // all slice loads of this lane's rows first, then the arithmetic
+                // (predicated, no early exit, so the rows interleave)
+                uint4 q0[kCtMaxNbf / 32], q1[kCtMaxNbf / 32], q2[kCtMaxNbf / 32];
 #pragma unroll
                 for (int j = 0; j < kCtMaxNbf / 32; ++j) {
                     const int mu = 32 * j + 8 * warp + mrow;
-                    if (mu >= nbf) break;
-                    const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
-                    // B row scale: phi 2^(7 - e_mu) -> phi 2^(7 - s_mu)
-                    const float rf = rfr[j];
-                    float v[8], t[8];
-                    unpack8(*reinterpret_cast<const uint4 *>(sA + oa), v);
-                    unpack8(*reinterpret_cast<const uint4 *>(sA + a_slice + oa), t);
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) v[k] += t[k];
-                    unpack8(*reinterpret_cast<const uint4 *>(sA + 2 * a_slice + oa), t);
-                    float bx[8], by[8];
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) {
-                        v[k] += t[k];                          // phi 2^(7 - e_mu), |v| < 128
-                        const float u = v[k] * rf;
-                        bx[k] = cx[k] * u;                     // c phi 2^(7 - s_mu - v), |bx| < 128
-                        by[k] = cy[k] * u;
+                    if (mu < nbf) {
+                        const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
+                        q0[j] = *reinterpret_cast<const uint4 *>(sA + oa);
+                        q1[j] = *reinterpret_cast<const uint4 *>(sA + a_slice + oa);
+                        q2[j] = *reinterpret_cast<const uint4 *>(sA + 2 * a_slice + oa);
                     }
-                    uint4 sbx[kCtSlices], sby[kCtSlices];
-                    slice8_fixed(bx, sbx);
-                    slice8_fixed(by, sby);
-                    const uint32_t oj = core_off(nbf + mu, 8 * g, kCtKcores);
+                }
 #pragma unroll
-                    for (int i = 0; i < kCtSlices; ++i) {
-                        *reinterpret_cast<uint4 *>(sB + i * b_slice + oa) = sbx[i];
-                        *reinterpret_cast<uint4 *>(sB + i * b_slice + oj) = sby[i];
+                for (int j = 0; j < kCtMaxNbf / 32; ++j) {
+                    const int mu = 32 * j + 8 * warp + mrow;
+                    if (mu < nbf) {
+                        const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
+                        // B row scale: phi 2^(7 - e_mu) -> phi 2^(7 - s_mu)
+                        const float rf = rfr[j];
+                        float v[8], t[8];
+                        unpack8(q0[j], v);
+                        unpack8(q1[j], t);
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) v[k] += t[k];
+                        unpack8(q2[j], t);
+                        float bx[8], by[8];
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            v[k] += t[k];                          // phi 2^(7 - e_mu), |v| < 128
+                            const float u = v[k] * rf;
+                            bx[k] = cx[k] * u;                     // c phi 2^(7 - s_mu - v), |bx| < 128
+                            by[k] = cy[k] * u;
+                        }
+                        uint4 sbx[kCtSlices], sby[kCtSlices];
+                        slice8_fixed(bx, sbx);
+                        slice8_fixed(by, sby);
+                        const uint32_t oj = core_off(nbf + mu, 8 * g, kCtKcores);
+#pragma unroll
+                        for (int i = 0; i < kCtSlices; ++i) {
+                            *reinterpret_cast<uint4 *>(sB + i * b_slice + oa) = sbx[i];
+                            *reinterpret_cast<uint4 *>(sB + i * b_slice + oj) = sby[i];
+                        }
                     }
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

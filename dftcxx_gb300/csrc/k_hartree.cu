@@ -212,9 +212,26 @@ static void split_f32(double v, float &hi, float &lo)
     lo = (float)(v - (double)hi);
 }
 
+// 1 / |p - atom| of every grid point, computed as in the FP64 own-cell kernel
+__global__ void k_inv_radius(size_t npts, int nrad, int nang, const double *__restrict__ rn,
+                             const double *__restrict__ leb, double *__restrict__ invr)
+{
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npts) return;
+    const int per_atom = nrad * nang;
+    const int rem = (int)(p % per_atom), i = rem / nang, j = rem % nang;
+    const double ri = rn[i];
+    const double px = leb[4 * j] * ri, py = leb[4 * j + 1] * ri, pz = leb[4 * j + 2] * ri;
+    invr[p] = 1.0 / sqrt(px * px + py * py + pz * pz);
+}
+
 int hartree_setup(dftg_ctx *c)
 {
     const int nang = c->nang, nlm = c->nlm, N = c->nrad, S = N + 2;
+    DFTG_CUDA(cudaMalloc(&c->d_invr, sizeof(double) * c->npts));
+    k_inv_radius<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, N, nang, c->d_rn, c->d_leb,
+                                                                           c->d_invr);
+    DFTG_LAUNCH_CHECK();
     std::vector<double> Y((size_t)nlm * nang), Yw((size_t)nlm * nang), pre(nlm), fold(nlm);
     std::vector<float> Y32(2 * (size_t)nlm * nang), Ywt32(2 * (size_t)nlm * nang);
     std::vector<double> leb((size_t)nang * 4);
@@ -319,6 +336,23 @@ int hartree_setup(dftg_ctx *c)
     DFTG_CUDA(cudaMemcpy(c->d_rec32, rec32.data(), sizeof(float) * rec32.size(), cudaMemcpyHostToDevice));
     DFTG_CUDA(cudaMemcpy(c->d_sx, sx.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
     DFTG_CUDA(cudaMemcpy(c->d_splf, f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice));
+    // double-float copies of the fixed maps for the mixed Poisson / spline kernels:
+    // [hi block][lo block] of Gt, Gb, Kt, 1/h, fold
+    {
+        std::vector<float> m32;
+        auto push = [&](const std::vector<double> &v, size_t n) {
+            const size_t o = m32.size();
+            m32.resize(o + 2 * n);
+            for (size_t i = 0; i < n; ++i) split_f32(v[i], m32[o + i], m32[o + n + i]);
+        };
+        push(Gt, Gt.size());
+        push(Gb, Gb.size());
+        push(Kt, Kt.size());
+        push(f, (size_t)N);                  // inv_h
+        push(fold, fold.size());
+        DFTG_CUDA(cudaMalloc(&c->d_maps32, sizeof(float) * m32.size()));
+        DFTG_CUDA(cudaMemcpy(c->d_maps32, m32.data(), sizeof(float) * m32.size(), cudaMemcpyHostToDevice));
+    }
     return DFTG_OK;
 }
 
@@ -343,28 +377,47 @@ __global__ void k_rholm(int nrad, int nang, int nlm, const double *__restrict__ 
 
 // K5a (mixed): split-FP32 products (hi*hi + hi*lo + lo*hi), FP32 partial sums of
 // 16 terms added in FP64
-__global__ void k_rholm_split(int nrad, int nang, int nlm, const double *__restrict__ rho,
-                              const double *__restrict__ wb, const float *__restrict__ Ywt, double *__restrict__ rholm)
+// Mixed form: w_becke rho split into FP32 hi + lo, Y_lm w_leb split likewise,
+// TwoSum accumulation.  One block per (atom, kRholmShells radial shells), one
+// thread per lm: each Y_lm load serves kRholmShells independent accumulators.
+constexpr int kRholmShells = 4;
+__global__ void __launch_bounds__(96) k_rholm_split(int nrad, int nang, int nlm, const double *__restrict__ rho,
+                                                    const double *__restrict__ wb, const float *__restrict__ Ywt,
+                                                    double *__restrict__ rholm)
 {
-    extern __shared__ float s_sp[];    // [2][nang]
-    const int a = blockIdx.x / nrad, i = blockIdx.x % nrad;
-    const size_t base = ((size_t)a * nrad + i) * nang;
-    for (int j = threadIdx.x; j < nang; j += blockDim.x) {
-        const double v = rho[base + j] * wb[base + j];
+    extern __shared__ float s_sp[];    // [kRholmShells][2][nang]
+    constexpr int RS = kRholmShells;
+    const int ngrp = (nrad + RS - 1) / RS;
+    const int a = blockIdx.x / ngrp, i0 = (blockIdx.x % ngrp) * RS;
+    for (int idx = threadIdx.x; idx < RS * nang; idx += blockDim.x) {
+        const int r = idx / nang, j = idx % nang, i = i0 + r;
+        double v = 0.0;
+        if (i < nrad) {
+            const size_t q = ((size_t)a * nrad + i) * nang + j;
+            v = rho[q] * wb[q];
+        }
         const float hi = (float)v;
-        s_sp[j] = hi;
-        s_sp[nang + j] = (float)(v - (double)hi);
+        s_sp[(2 * r) * nang + j] = hi;
+        s_sp[(2 * r + 1) * nang + j] = (float)(v - (double)hi);
     }
     __syncthreads();
     const size_t half = (size_t)nlm * nang;
     for (int lm = threadIdx.x; lm < nlm; lm += blockDim.x) {
-        float s = 0.f, e = 0.f;
+        float sa[RS], ea[RS];
+#pragma unroll
+        for (int r = 0; r < RS; ++r) { sa[r] = 0.f; ea[r] = 0.f; }
+#pragma unroll 2
         for (int j = 0; j < nang; ++j) {
             const float yh = Ywt[(size_t)j * nlm + lm], yl = Ywt[half + (size_t)j * nlm + lm];
-            const float sh = s_sp[j], sl = s_sp[nang + j];
-            two_sum_acc(s, e, fmaf(sh, yh, fmaf(sh, yl, sl * yh)));
+#pragma unroll
+            for (int r = 0; r < RS; ++r) {
+                const float sh = s_sp[(2 * r) * nang + j], sl = s_sp[(2 * r + 1) * nang + j];
+                two_sum_acc(sa[r], ea[r], fmaf(sh, yh, fmaf(sh, yl, sl * yh)));
+            }
         }
-        rholm[((size_t)a * nlm + lm) * nrad + i] = ((double)s + (double)e) * 4.0 * kPi;
+#pragma unroll
+        for (int r = 0; r < RS; ++r)
+            if (i0 + r < nrad) rholm[((size_t)a * nlm + lm) * nrad + i0 + r] = ((double)sa[r] + (double)ea[r]) * 4.0 * kPi;
     }
 }
 
@@ -404,6 +457,44 @@ __global__ void k_poisson(int natoms, int nrad, int lmax, const double *__restri
     }
 }
 
+// K5b (mixed): the same map in double-float arithmetic.  maps: the double-float
+// copies laid out as in hartree_setup.
+__global__ void k_poisson_split(int natoms, int nrad, int lmax, const float *__restrict__ maps,
+                                const double *__restrict__ rholm, const double *__restrict__ scal,
+                                double *__restrict__ U, float *__restrict__ U32)
+{
+    extern __shared__ float s_r2[];     // [2][nrad] rho_lm hi, lo
+    const int nlm = (lmax + 1) * (lmax + 1);
+    const int id = blockIdx.x, a = id / nlm, lm = id % nlm, N = nrad;
+    int l = 0;
+    while ((l + 1) * (l + 1) <= lm) ++l;
+    const size_t ng = (size_t)(lmax + 1) * N * N;
+    const float *Gh = maps + (size_t)l * N * N, *Gl = Gh + ng;
+    const float *Gbh = maps + 2 * ng, *Gbl = Gbh + N;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+        const dfl r = df_from(rholm[(size_t)id * N + k]);
+        s_r2[k] = r.h;
+        s_r2[N + k] = r.l;
+    }
+    __syncthreads();
+    const dfl q = lm == 0 ? df_from(scal[kScalAtomQ + a]) : dfl{0.f, 0.f};
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        dfl acc0{0.f, 0.f}, acc1{0.f, 0.f};
+        int k = 0;
+        for (; k + 1 < N; k += 2) {
+            acc0 = df_fma(acc0, dfl{Gh[(size_t)k * N + i], Gl[(size_t)k * N + i]}, dfl{s_r2[k], s_r2[N + k]});
+            acc1 = df_fma(acc1, dfl{Gh[(size_t)(k + 1) * N + i], Gl[(size_t)(k + 1) * N + i]},
+                          dfl{s_r2[k + 1], s_r2[N + k + 1]});
+        }
+        if (k < N) acc0 = df_fma(acc0, dfl{Gh[(size_t)k * N + i], Gl[(size_t)k * N + i]}, dfl{s_r2[k], s_r2[N + k]});
+        dfl v = df_add(acc0, acc1);
+        if (lm == 0) v = df_fma(v, dfl{Gbh[i], Gbl[i]}, q);
+        U[(size_t)id * N + i] = df_to(v);
+        U32[(size_t)id * N + i] = v.h;
+        U32[(size_t)natoms * nlm * N + (size_t)id * N + i] = v.l;
+    }
+}
+
 // K5c (FP64): own-cell potential for every point
 __global__ void k_vown(size_t npts, int nrad, int nang, int nlm, const double *__restrict__ rn,
                        const double *__restrict__ leb, const double *__restrict__ Y, const double *__restrict__ U,
@@ -423,17 +514,14 @@ __global__ void k_vown(size_t npts, int nrad, int nang, int nlm, const double *_
 }
 
 // K5c (mixed): split-FP32 products, 16-term FP32 partials added in FP64
-__global__ void k_vown_split(size_t npts, int natoms, int nrad, int nang, int nlm, const double *__restrict__ rn,
-                             const double *__restrict__ leb, const float *__restrict__ Y32,
-                             const float *__restrict__ U32, double *__restrict__ Vown)
+__global__ void k_vown_split(size_t npts, int natoms, int nrad, int nang, int nlm, const double *__restrict__ invr,
+                             const float *__restrict__ Y32, const float *__restrict__ U32, double *__restrict__ Vown)
 {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npts) return;
     const int per_atom = nrad * nang;
     const int a = (int)(p / per_atom), rem = (int)(p % per_atom), i = rem / nang, j = rem % nang;
-    const double ri = rn[i];
-    const double px = leb[4 * j] * ri, py = leb[4 * j + 1] * ri, pz = leb[4 * j + 2] * ri;
-    const double inv_r = 1.0 / sqrt(px * px + py * py + pz * pz);
+    const double inv_r = invr[p];          // 1 / |r_i leb_j|, fixed for the grid
     const size_t uhalf = (size_t)natoms * nlm * nrad, yhalf = (size_t)nlm * nang;
     const float *uh = U32 + (size_t)a * nlm * nrad + i, *ul = uh + uhalf;
     float s = 0.f, e = 0.f;
@@ -494,6 +582,65 @@ __global__ void k_splines(int natoms, int nrad, int nlm, const double *__restric
             const float hi = (float)v;
             o32[8 * i + k] = hi;
             o32[8 * i + 4 + k] = (float)(v - (double)hi);
+        }
+    }
+}
+
+// K5d (mixed): the same spline fit in double-float arithmetic from the split U;
+// the FP64 table is written only when want64 (an FP64 cross-atom step follows).
+__global__ void k_splines_split(int natoms, int nrad, int nlm, int lmax, const float *__restrict__ maps,
+                                const float *__restrict__ U32, int want64, double *__restrict__ spl,
+                                float *__restrict__ splm)
+{
+    extern __shared__ float s_y2[];    // y hi [n], y lo [n], D hi [n], D lo [n]
+    const int id = blockIdx.x, n = nrad;
+    const size_t ng = (size_t)(lmax + 1) * n * n;
+    const float *Kh = maps + 2 * ng + 2 * (size_t)n, *Kl = Kh + (size_t)n * n;
+    const float *ih = Kl + (size_t)n * n, *il = ih + n;
+    const float *fh = il + n, *fl = fh + nlm;
+    const size_t uhalf = (size_t)natoms * nlm * n;
+    float *yh = s_y2, *yl = s_y2 + n, *Dh = s_y2 + 2 * n, *Dl = s_y2 + 3 * n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {   // increasing r: reverse the radial order
+        yh[i] = U32[(size_t)id * n + n - 1 - i];
+        yl[i] = U32[uhalf + (size_t)id * n + n - 1 - i];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        dfl a0{0.f, 0.f}, a1{0.f, 0.f};
+        int j = 0;
+        for (; j + 1 < n; j += 2) {
+            a0 = df_fma(a0, dfl{Kh[(size_t)j * n + i], Kl[(size_t)j * n + i]}, dfl{yh[j], yl[j]});
+            a1 = df_fma(a1, dfl{Kh[(size_t)(j + 1) * n + i], Kl[(size_t)(j + 1) * n + i]}, dfl{yh[j + 1], yl[j + 1]});
+        }
+        if (j < n) a0 = df_fma(a0, dfl{Kh[(size_t)j * n + i], Kl[(size_t)j * n + i]}, dfl{yh[j], yl[j]});
+        const dfl d = df_add(a0, a1);
+        Dh[i] = d.h;
+        Dl[i] = d.l;
+    }
+    __syncthreads();
+    const int lm = id % nlm;
+    const dfl F{fh[lm], fl[lm]};
+    float *o32 = splm + (size_t)id * n * 8;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        dfl cc[4];
+        if (i < n - 1) {
+            const dfl dx{ih[i], il[i]}, y0{yh[i], yl[i]}, y1{yh[i + 1], yl[i + 1]};
+            const dfl D0{Dh[i], Dl[i]}, D1{Dh[i + 1], Dl[i + 1]};
+            const dfl dy = df_mul(df_sub(y1, y0), dx);
+            const dfl three{3.f, 0.f}, two{2.f, 0.f};
+            cc[0] = y0;
+            cc[1] = D0;
+            cc[2] = df_mul(dx, df_sub(df_sub(df_mul(three, dy), df_mul(two, D0)), D1));
+            cc[3] = df_mul(df_mul(dx, dx), df_add(df_add(df_mul(dfl{-2.f, 0.f}, dy), D0), D1));
+        } else {                     // clamp value of the last knot
+            cc[0] = dfl{yh[n - 1], yl[n - 1]};
+            cc[1] = cc[2] = cc[3] = dfl{0.f, 0.f};
+        }
+        for (int k = 0; k < 4; ++k) {
+            const dfl v = df_mul(F, cc[k]);
+            o32[8 * i + k] = v.h;
+            o32[8 * i + 4 + k] = v.l;
+            if (want64) spl[((size_t)id * n + i) * 4 + k] = df_to(cc[k]);
         }
     }
 }
@@ -811,34 +958,23 @@ int cross_pairs_setup(dftg_ctx *c)
 }
 
 // E_J = 2 tr(P J) = sum_p (w V / 2) rho_raw (the J assembly contracted with P,
-// evaluated directly on the grid in FP64): deterministic block partials...
-__global__ void __launch_bounds__(256) k_ej_partials(size_t npad, const double *__restrict__ cj,
-                                                     const double *__restrict__ rho, double *__restrict__ part)
+// evaluated directly on the grid in FP64): deterministic block partials, summed
+// by the last block
+__global__ void __launch_bounds__(256) k_ej(size_t npad, const double *__restrict__ cj, const double *__restrict__ rho,
+                                            double *__restrict__ part, int scaled, double *scal, int *counter)
 {
-    __shared__ double sh[256];
+    __shared__ double sh[32];
+    __shared__ int s_last;
     const size_t p = (size_t)blockIdx.x * 256 + threadIdx.x;
-    sh[threadIdx.x] = p < npad ? cj[p] * rho[p] : 0.0;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
-}
-
-// ...summed in order; rho on the device carries the correction factor when scaled
-__global__ void __launch_bounds__(256) k_ej_final(int n, const double *__restrict__ part, int scaled, double *scal)
-{
-    __shared__ double sh[256];
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += 256) s += part[i];
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) scal[kScalEJ] = scaled ? sh[0] / scal[kScalScale] : sh[0];
+    double v = block_sum(p < npad ? cj[p] * rho[p] : 0.0, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = v;
+    if (!last_block(counter, &s_last)) return;
+    // last block: sum of the block partials in a fixed order; rho on the device
+    // carries the correction factor when scaled
+    double t = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += 256) t += __ldcg(part + i);
+    t = block_sum(t, sh);
+    if (threadIdx.x == 0) scal[kScalEJ] = scaled ? t / scal[kScalScale] : t;
 }
 
 template <int LMAX>
@@ -869,8 +1005,9 @@ int launch_hartree(dftg_ctx *c)
     const int N = c->nrad, S = N + 2, nlm = c->nlm;
     const bool mp = (c->prec_mask & kPrecMultipole) != 0;
     if (mp)
-        k_rholm_split<<<c->natoms * N, 96, sizeof(float) * 2 * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho,
-                                                                                     c->d_wb, c->d_Ywt32, c->d_rholm);
+        k_rholm_split<<<c->natoms * ((N + kRholmShells - 1) / kRholmShells), 96,
+                        sizeof(float) * 2 * kRholmShells * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho, c->d_wb,
+                                                                                 c->d_Ywt32, c->d_rholm);
     else
         k_rholm<<<c->natoms * N, 96, sizeof(double) * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho, c->d_wb,
                                                                             c->d_Yw, c->d_rholm);
@@ -878,20 +1015,29 @@ int launch_hartree(dftg_ctx *c)
     DFTG_MARK(c, "rholm");
     const int nrhs = c->natoms * nlm;
     (void)S;
-    k_poisson<<<nrhs, 128, sizeof(double) * N, c->stream>>>(c->natoms, N, c->lmax, c->d_Gt, c->d_Gb, c->d_rholm,
-                                                            c->d_scal, c->d_U, c->d_U32);
+    if (mp)
+        k_poisson_split<<<nrhs, 128, sizeof(float) * 2 * N, c->stream>>>(c->natoms, N, c->lmax, c->d_maps32,
+                                                                         c->d_rholm, c->d_scal, c->d_U, c->d_U32);
+    else
+        k_poisson<<<nrhs, 128, sizeof(double) * N, c->stream>>>(c->natoms, N, c->lmax, c->d_Gt, c->d_Gb, c->d_rholm,
+                                                                c->d_scal, c->d_U, c->d_U32);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "poisson");
     const unsigned npb = (unsigned)((c->npts + 127) / 128);
     if (mp)
-        k_vown_split<<<npb, 128, 0, c->stream>>>(c->npts, c->natoms, N, c->nang, nlm, c->d_rn, c->d_leb, c->d_Y32,
-                                                 c->d_U32, c->d_Vown);
+        k_vown_split<<<npb, 128, 0, c->stream>>>(c->npts, c->natoms, N, c->nang, nlm, c->d_invr, c->d_Y32, c->d_U32,
+                                                 c->d_Vown);
     else
         k_vown<<<npb, 128, 0, c->stream>>>(c->npts, N, c->nang, nlm, c->d_rn, c->d_leb, c->d_Y, c->d_U, c->d_Vown);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "vown");
-    k_splines<<<nrhs, 128, sizeof(double) * 2 * N, c->stream>>>(c->natoms, N, nlm, c->d_splf, c->d_Kt, c->d_U,
-                                                                c->d_fold, c->d_spl, c->d_splm);
+    if (mp)
+        k_splines_split<<<nrhs, 128, sizeof(float) * 4 * N, c->stream>>>(
+            c->natoms, N, nlm, c->lmax, c->d_maps32, c->d_U32, (c->prec_mask & kPrecCross) ? 0 : 1, c->d_spl,
+            c->d_splm);
+    else
+        k_splines<<<nrhs, 128, sizeof(double) * 2 * N, c->stream>>>(c->natoms, N, nlm, c->d_splf, c->d_Kt, c->d_U,
+                                                                    c->d_fold, c->d_spl, c->d_splm);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "splines");
     const unsigned nb = (unsigned)(c->npad / 128);
@@ -909,9 +1055,8 @@ int launch_hartree(dftg_ctx *c)
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "vcross");
     const unsigned ne = (unsigned)((c->npad + 255) / 256);
-    k_ej_partials<<<ne, 256, 0, c->stream>>>(c->npad, c->d_cj, c->d_rho, c->d_red);
-    DFTG_LAUNCH_CHECK();
-    k_ej_final<<<1, 256, 0, c->stream>>>((int)ne, c->d_red, c->rho_scaled ? 1 : 0, c->d_scal);
+    k_ej<<<ne, 256, 0, c->stream>>>(c->npad, c->d_cj, c->d_rho, c->d_red, c->rho_scaled ? 1 : 0, c->d_scal,
+                                    c->d_counters + kCntEJ);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "hartree_energy");
     return DFTG_OK;
