@@ -77,7 +77,7 @@ static void free_ctx(dftg_ctx *c)
                     c->d_rec32, c->d_rholm, c->d_U, c->d_U32, c->d_Y32, c->d_Ywt32, c->d_fold, c->d_Gt,
                     c->d_Gb, c->d_Kt, c->d_sx, c->d_splf, c->d_spl, c->d_splm, c->d_tiles,
                     c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_flag,
-                    c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32};
+                    c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32, c->d_U32T, c->d_red2};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -182,9 +182,11 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(dalloc(&c->d_pre32, nlm));
     DFTG_TRY(dalloc(&c->d_rec, 2 * nlm));
     DFTG_TRY(dalloc(&c->d_rec32, 2 * nlm));
-    DFTG_TRY(dalloc(&c->d_rholm, (size_t)c->natoms * nlm * N));
+    DFTG_TRY(dalloc(&c->d_rholm, 2 * (size_t)c->natoms * nlm * N));    // two K-slice planes in the mixed path
     DFTG_TRY(dalloc(&c->d_U, (size_t)c->natoms * nlm * N));
     DFTG_TRY(dalloc(&c->d_U32, 2 * (size_t)c->natoms * nlm * N));
+    DFTG_TRY(dalloc(&c->d_U32T, 2 * (size_t)c->natoms * nlm * N));
+    DFTG_TRY(dalloc(&c->d_red2, c->npad));
     DFTG_TRY(dalloc(&c->d_Y32, 2 * nlm * c->nang));
     DFTG_TRY(dalloc(&c->d_Ywt32, 2 * nlm * c->nang));
     DFTG_TRY(dalloc(&c->d_fold, nlm));

@@ -183,6 +183,8 @@ struct dftg_ctx {
     double *d_rholm = nullptr;    // [natoms][nlm][nrad]
     double *d_U = nullptr;        // [natoms][nlm][nrad]
     float *d_U32 = nullptr;       // [2][natoms][nlm][nrad] U split into FP32 hi, lo
+    float *d_U32T = nullptr;      // [2][natoms][nrad][nlm] the same, transposed
+    double *d_red2 = nullptr;     // [npts] work plane (rho w_becke split for the rho_lm GEMM)
     float *d_Y32 = nullptr;       // [2][nlm][nang] Y_lm split into FP32 hi, lo
     float *d_Ywt32 = nullptr;     // [2][nang][nlm] w_leb Y_lm split, transposed
     double *d_fold = nullptr;     // [nlm] Y_lm normalisation of the integer recursion

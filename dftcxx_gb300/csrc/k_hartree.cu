@@ -377,48 +377,104 @@ __global__ void k_rholm(int nrad, int nang, int nlm, const double *__restrict__ 
 
 // K5a (mixed): split-FP32 products (hi*hi + hi*lo + lo*hi), FP32 partial sums of
 // 16 terms added in FP64
-// Mixed form: w_becke rho split into FP32 hi + lo, Y_lm w_leb split likewise,
-// TwoSum accumulation.  One block per (atom, kRholmShells radial shells), one
-// thread per lm: each Y_lm load serves kRholmShells independent accumulators.
-constexpr int kRholmShells = 4;
-__global__ void __launch_bounds__(96) k_rholm_split(int nrad, int nang, int nlm, const double *__restrict__ rho,
-                                                    const double *__restrict__ wb, const float *__restrict__ Ywt,
-                                                    double *__restrict__ rholm)
+// ------------------------------------------------------------------
+// Double-float GEMM for the mixed multipole steps: C = A B with A (M x K) and
+// B (K x N) given as FP32 hi + lo planes (row-major, leading dimensions lda /
+// ldb), every product formed exactly (TwoProd) and accumulated with TwoSum, so
+// C carries ~2^-44 relative error.  Tile 16 x 32 per block of 128 threads, 2 x 2
+// outputs per thread; K split over gridDim.z slices whose partial results the
+// epilogue functor receives with their slice index.
+constexpr int kDgBM = 16, kDgBN = 32, kDgBK = 16;
+
+__device__ __forceinline__ void df_mac(float &s, float &e, float ah, float al, float bh, float bl)
 {
-    extern __shared__ float s_sp[];    // [kRholmShells][2][nang]
-    constexpr int RS = kRholmShells;
-    const int ngrp = (nrad + RS - 1) / RS;
-    const int a = blockIdx.x / ngrp, i0 = (blockIdx.x % ngrp) * RS;
-    for (int idx = threadIdx.x; idx < RS * nang; idx += blockDim.x) {
-        const int r = idx / nang, j = idx % nang, i = i0 + r;
-        double v = 0.0;
-        if (i < nrad) {
-            const size_t q = ((size_t)a * nrad + i) * nang + j;
-            v = rho[q] * wb[q];
+    const float p = ah * bh;
+    const float pe = fmaf(ah, bh, -p);
+    const float t = s + p;
+    const float bp = t - s;
+    e += ((s - (t - bp)) + (p - bp)) + fmaf(ah, bl, fmaf(al, bh, pe));
+    s = t;
+}
+
+template <class Epi>
+__global__ void __launch_bounds__(128) k_dfgemm(int M, int N, int K, const float *__restrict__ Ah,
+                                                const float *__restrict__ Al, int lda, const float *__restrict__ Bh,
+                                                const float *__restrict__ Bl, int ldb, Epi epi)
+{
+    __shared__ float sa[2][kDgBK][kDgBM + 1], sb[2][kDgBK][kDgBN + 1];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;        // ty 0..7
+    const int m0 = blockIdx.y * kDgBM, n0 = blockIdx.x * kDgBN;
+    const int kchunk = (K + gridDim.z - 1) / gridDim.z;
+    const int kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
+    float s[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, e[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    for (int k0 = kbeg; k0 < kend; k0 += kDgBK) {
+        for (int i = threadIdx.x; i < kDgBM * kDgBK; i += 128) {          // A tile, transposed
+            const int r = i / kDgBK, kk = i % kDgBK, m = m0 + r, k = k0 + kk;
+            const bool ok = m < M && k < kend;
+            sa[0][kk][r] = ok ? Ah[(size_t)m * lda + k] : 0.f;
+            sa[1][kk][r] = ok ? Al[(size_t)m * lda + k] : 0.f;
         }
-        const float hi = (float)v;
-        s_sp[(2 * r) * nang + j] = hi;
-        s_sp[(2 * r + 1) * nang + j] = (float)(v - (double)hi);
-    }
-    __syncthreads();
-    const size_t half = (size_t)nlm * nang;
-    for (int lm = threadIdx.x; lm < nlm; lm += blockDim.x) {
-        float sa[RS], ea[RS];
-#pragma unroll
-        for (int r = 0; r < RS; ++r) { sa[r] = 0.f; ea[r] = 0.f; }
-#pragma unroll 2
-        for (int j = 0; j < nang; ++j) {
-            const float yh = Ywt[(size_t)j * nlm + lm], yl = Ywt[half + (size_t)j * nlm + lm];
-#pragma unroll
-            for (int r = 0; r < RS; ++r) {
-                const float sh = s_sp[(2 * r) * nang + j], sl = s_sp[(2 * r + 1) * nang + j];
-                two_sum_acc(sa[r], ea[r], fmaf(sh, yh, fmaf(sh, yl, sl * yh)));
-            }
+        for (int i = threadIdx.x; i < kDgBK * kDgBN; i += 128) {          // B tile
+            const int kk = i / kDgBN, c = i % kDgBN, n = n0 + c, k = k0 + kk;
+            const bool ok = n < N && k < kend;
+            sb[0][kk][c] = ok ? Bh[(size_t)k * ldb + n] : 0.f;
+            sb[1][kk][c] = ok ? Bl[(size_t)k * ldb + n] : 0.f;
         }
-#pragma unroll
-        for (int r = 0; r < RS; ++r)
-            if (i0 + r < nrad) rholm[((size_t)a * nlm + lm) * nrad + i0 + r] = ((double)sa[r] + (double)ea[r]) * 4.0 * kPi;
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < kDgBK; ++kk) {
+            const float a0h = sa[0][kk][ty], a0l = sa[1][kk][ty], a1h = sa[0][kk][ty + 8], a1l = sa[1][kk][ty + 8];
+            const float b0h = sb[0][kk][tx], b0l = sb[1][kk][tx], b1h = sb[0][kk][tx + 16], b1l = sb[1][kk][tx + 16];
+            df_mac(s[0][0], e[0][0], a0h, a0l, b0h, b0l);
+            df_mac(s[0][1], e[0][1], a0h, a0l, b1h, b1l);
+            df_mac(s[1][0], e[1][0], a1h, a1l, b0h, b0l);
+            df_mac(s[1][1], e[1][1], a1h, a1l, b1h, b1l);
+        }
+        __syncthreads();
     }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int m = m0 + ty + 8 * i, n = n0 + tx + 16 * j;
+            if (m < M && n < N) epi(m, n, (int)blockIdx.z, df_norm(s[i][j], e[i][j]));
+        }
+}
+
+// rho_lm[a][lm][i] = 4 pi sum_j (rho w_becke)[a, i, j] (w_leb Y_lm)[j]: rows m = a N + i.
+// K is split in two; the slices go to two planes, summed by the Poisson kernel.
+struct EpiRholm {
+    int nrad, nlm;
+    size_t plane;
+    double *out;
+    __device__ void operator()(int m, int n, int z, dfl v) const
+    {
+        const int a = m / nrad, i = m % nrad;
+        out[z * plane + ((size_t)a * nlm + n) * nrad + i] = df_to(v) * (4.0 * kPi);
+    }
+};
+
+// V_own[p] = (1 / r_p) sum_lm U[a][lm][i] Y_lm[j], p = (a N + i) nang + j
+struct EpiVown {
+    int nang;
+    const double *invr;
+    double *Vown;
+    __device__ void operator()(int m, int n, int, dfl v) const
+    {
+        const size_t p = (size_t)m * nang + n;
+        Vown[p] = df_to(v) * invr[p];
+    }
+};
+
+// rho w_becke split into FP32 hi / lo planes [2][npts]
+__global__ void k_split_rhow(size_t npts, const double *__restrict__ rho, const double *__restrict__ wb,
+                             float *__restrict__ out)
+{
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npts) return;
+    const dfl v = df_from(rho[p] * wb[p]);
+    out[p] = v.h;
+    out[npts + p] = v.l;
 }
 
 // K5b: U_lm = G_l rho_lm (+ the l = 0 boundary column times q_a): one block per
@@ -460,8 +516,8 @@ __global__ void k_poisson(int natoms, int nrad, int lmax, const double *__restri
 // K5b (mixed): the same map in double-float arithmetic.  maps: the double-float
 // copies laid out as in hartree_setup.
 __global__ void k_poisson_split(int natoms, int nrad, int lmax, const float *__restrict__ maps,
-                                const double *__restrict__ rholm, const double *__restrict__ scal,
-                                double *__restrict__ U, float *__restrict__ U32)
+                                const double *__restrict__ rholm, size_t rplane, const double *__restrict__ scal,
+                                double *__restrict__ U, float *__restrict__ U32, float *__restrict__ U32T)
 {
     extern __shared__ float s_r2[];     // [2][nrad] rho_lm hi, lo
     const int nlm = (lmax + 1) * (lmax + 1);
@@ -471,8 +527,8 @@ __global__ void k_poisson_split(int natoms, int nrad, int lmax, const float *__r
     const size_t ng = (size_t)(lmax + 1) * N * N;
     const float *Gh = maps + (size_t)l * N * N, *Gl = Gh + ng;
     const float *Gbh = maps + 2 * ng, *Gbl = Gbh + N;
-    for (int k = threadIdx.x; k < N; k += blockDim.x) {
-        const dfl r = df_from(rholm[(size_t)id * N + k]);
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {     // the two K slices of the projection
+        const dfl r = df_add(df_from(rholm[(size_t)id * N + k]), df_from(rholm[rplane + (size_t)id * N + k]));
         s_r2[k] = r.h;
         s_r2[N + k] = r.l;
     }
@@ -492,6 +548,9 @@ __global__ void k_poisson_split(int natoms, int nrad, int lmax, const float *__r
         U[(size_t)id * N + i] = df_to(v);
         U32[(size_t)id * N + i] = v.h;
         U32[(size_t)natoms * nlm * N + (size_t)id * N + i] = v.l;
+        // transposed copy [2][(a, i)][lm] for the own-cell GEMM
+        U32T[((size_t)a * N + i) * nlm + lm] = v.h;
+        U32T[(size_t)natoms * nlm * N + ((size_t)a * N + i) * nlm + lm] = v.l;
     }
 }
 
@@ -513,25 +572,6 @@ __global__ void k_vown(size_t npts, int nrad, int nang, int nlm, const double *_
     Vown[p] = v;
 }
 
-// K5c (mixed): split-FP32 products, 16-term FP32 partials added in FP64
-__global__ void k_vown_split(size_t npts, int natoms, int nrad, int nang, int nlm, const double *__restrict__ invr,
-                             const float *__restrict__ Y32, const float *__restrict__ U32, double *__restrict__ Vown)
-{
-    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npts) return;
-    const int per_atom = nrad * nang;
-    const int a = (int)(p / per_atom), rem = (int)(p % per_atom), i = rem / nang, j = rem % nang;
-    const double inv_r = invr[p];          // 1 / |r_i leb_j|, fixed for the grid
-    const size_t uhalf = (size_t)natoms * nlm * nrad, yhalf = (size_t)nlm * nang;
-    const float *uh = U32 + (size_t)a * nlm * nrad + i, *ul = uh + uhalf;
-    float s = 0.f, e = 0.f;
-    for (int lm = 0; lm < nlm; ++lm) {
-        const float yh = Y32[(size_t)lm * nang + j], yl = Y32[yhalf + (size_t)lm * nang + j];
-        const float h = uh[(size_t)lm * nrad], lo = ul[(size_t)lm * nrad];
-        two_sum_acc(s, e, fmaf(h, yh, fmaf(h, yl, lo * yh)));
-    }
-    Vown[p] = inv_r * ((double)s + (double)e);
-}
 
 // K5d: spline coefficients of U_lm over increasing r (cspline.cpp:66-142):
 // derivatives D = K y with the precomputed x-only map K, then the per-interval
@@ -1004,11 +1044,18 @@ int launch_hartree(dftg_ctx *c)
 {
     const int N = c->nrad, S = N + 2, nlm = c->nlm;
     const bool mp = (c->prec_mask & kPrecMultipole) != 0;
-    if (mp)
-        k_rholm_split<<<c->natoms * ((N + kRholmShells - 1) / kRholmShells), 96,
-                        sizeof(float) * 2 * kRholmShells * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho, c->d_wb,
-                                                                                 c->d_Ywt32, c->d_rholm);
-    else
+    const size_t rplane = (size_t)c->natoms * nlm * N;
+    if (mp) {
+        // rho_lm as a double-float GEMM [(a, i) x j] x [j x lm], K split in two planes
+        float *S32 = reinterpret_cast<float *>(c->d_red2);
+        k_split_rhow<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, c->d_rho, c->d_wb, S32);
+        DFTG_LAUNCH_CHECK();
+        const int M = c->natoms * N;
+        dim3 grid((unsigned)((nlm + kDgBN - 1) / kDgBN), (unsigned)((M + kDgBM - 1) / kDgBM), 2);
+        k_dfgemm<EpiRholm><<<grid, 128, 0, c->stream>>>(M, nlm, c->nang, S32, S32 + c->npts, c->nang, c->d_Ywt32,
+                                                        c->d_Ywt32 + (size_t)nlm * c->nang, nlm,
+                                                        EpiRholm{N, nlm, rplane, c->d_rholm});
+    } else
         k_rholm<<<c->natoms * N, 96, sizeof(double) * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho, c->d_wb,
                                                                             c->d_Yw, c->d_rholm);
     DFTG_LAUNCH_CHECK();
@@ -1017,17 +1064,22 @@ int launch_hartree(dftg_ctx *c)
     (void)S;
     if (mp)
         k_poisson_split<<<nrhs, 128, sizeof(float) * 2 * N, c->stream>>>(c->natoms, N, c->lmax, c->d_maps32,
-                                                                         c->d_rholm, c->d_scal, c->d_U, c->d_U32);
+                                                                         c->d_rholm, rplane, c->d_scal, c->d_U,
+                                                                         c->d_U32, c->d_U32T);
     else
         k_poisson<<<nrhs, 128, sizeof(double) * N, c->stream>>>(c->natoms, N, c->lmax, c->d_Gt, c->d_Gb, c->d_rholm,
                                                                 c->d_scal, c->d_U, c->d_U32);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "poisson");
     const unsigned npb = (unsigned)((c->npts + 127) / 128);
-    if (mp)
-        k_vown_split<<<npb, 128, 0, c->stream>>>(c->npts, c->natoms, N, c->nang, nlm, c->d_invr, c->d_Y32, c->d_U32,
-                                                 c->d_Vown);
-    else
+    if (mp) {
+        // own-cell potential as a double-float GEMM [(a, i) x lm] x [lm x j]
+        const int M = c->natoms * N;
+        dim3 grid((unsigned)((c->nang + kDgBN - 1) / kDgBN), (unsigned)((M + kDgBM - 1) / kDgBM), 1);
+        k_dfgemm<EpiVown><<<grid, 128, 0, c->stream>>>(M, c->nang, nlm, c->d_U32T, c->d_U32T + rplane, nlm, c->d_Y32,
+                                                       c->d_Y32 + (size_t)nlm * c->nang, c->nang,
+                                                       EpiVown{c->nang, c->d_invr, c->d_Vown});
+    } else
         k_vown<<<npb, 128, 0, c->stream>>>(c->npts, N, c->nang, nlm, c->d_rn, c->d_leb, c->d_Y, c->d_U, c->d_Vown);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "vown");
