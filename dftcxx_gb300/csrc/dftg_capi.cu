@@ -81,6 +81,7 @@ static void free_ctx(dftg_ctx *c)
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
+    if (c->pipe_exec) cudaGraphExecDestroy(c->pipe_exec);
     for (cudaEvent_t ev : c->prof_ev)
         if (ev) cudaEventDestroy(ev);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -182,7 +183,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(dalloc(&c->d_pre32, nlm));
     DFTG_TRY(dalloc(&c->d_rec, 2 * nlm));
     DFTG_TRY(dalloc(&c->d_rec32, 2 * nlm));
-    DFTG_TRY(dalloc(&c->d_rholm, 2 * (size_t)c->natoms * nlm * N));    // two K-slice planes in the mixed path
+    DFTG_TRY(dalloc(&c->d_rholm, kRholmSlices * (size_t)c->natoms * nlm * N));   // K-slice planes (mixed path)
     DFTG_TRY(dalloc(&c->d_U, (size_t)c->natoms * nlm * N));
     DFTG_TRY(dalloc(&c->d_U32, 2 * (size_t)c->natoms * nlm * N));
     DFTG_TRY(dalloc(&c->d_U32T, 2 * (size_t)c->natoms * nlm * N));
@@ -274,6 +275,44 @@ static int fock_pipeline(dftg_ctx *c)
     c->rho_scaled = true;
     DFTG_TRY(launch_hartree(c));
     DFTG_TRY(launch_contract(c, true, true));
+    return DFTG_OK;
+}
+
+// One build on the device buffers (d_P in; d_J, d_XC, d_scal out).  The kernel
+// sequence of a (precision mask, stream) pair is captured once into a CUDA
+// graph and replayed; the first build of each pair runs eagerly.
+static int fock_pipeline_graph(dftg_ctx *c)
+{
+    if (c->pipe_exec && (c->pipe_mask != c->prec_mask || c->pipe_stream != c->stream)) {
+        cudaGraphExecDestroy(c->pipe_exec);
+        c->pipe_exec = nullptr;
+        c->pipe_warm = false;
+    }
+    if (!c->pipe_exec) {
+        if (!c->pipe_warm || c->pipe_mask != c->prec_mask || c->pipe_stream != c->stream) {
+            c->pipe_warm = true;
+            c->pipe_mask = c->prec_mask;
+            c->pipe_stream = c->stream;
+            return fock_pipeline(c);
+        }
+        cudaGraph_t g = nullptr;
+        DFTG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = fock_pipeline(c);
+        const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (rc != DFTG_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+        const cudaError_t ei = cudaGraphInstantiate(&c->pipe_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            c->pipe_exec = nullptr;
+            return cuda_fail(ei, "cudaGraphInstantiate", __FILE__, __LINE__);
+        }
+    }
+    DFTG_CUDA(cudaGraphLaunch(c->pipe_exec, c->stream));
+    c->rho_scaled = true;
     return DFTG_OK;
 }
 
@@ -460,7 +499,7 @@ int dftg_fock_build_device(dftg_ctx *c, const double *P_dev, double *J_dev, doub
     DFTG_CUDA(cudaSetDevice(c->device));
     const size_t nn = (size_t)c->nbf * c->nbf;
     if (P_dev != c->d_P) DFTG_CUDA(cudaMemcpyAsync(c->d_P, P_dev, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
-    DFTG_TRY(fock_pipeline(c));
+    DFTG_TRY(fock_pipeline_graph(c));
     if (J_dev) DFTG_CUDA(cudaMemcpyAsync(J_dev, c->d_J, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
     if (XC_dev) DFTG_CUDA(cudaMemcpyAsync(XC_dev, c->d_XC, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
     if (scalars_dev) {
@@ -512,7 +551,7 @@ int dftg_fock_build(dftg_ctx *c, const double *P, double *J, double *XC, double 
     DFTG_CUDA(cudaSetDevice(c->device));
     const size_t nn = (size_t)c->nbf * c->nbf;
     DFTG_CUDA(cudaMemcpyAsync(c->d_P, P, sizeof(double) * nn, cudaMemcpyHostToDevice, c->stream));
-    DFTG_TRY(fock_pipeline(c));
+    DFTG_TRY(fock_pipeline_graph(c));
     if (J) DFTG_CUDA(cudaMemcpyAsync(J, c->d_J, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream));
     if (XC) DFTG_CUDA(cudaMemcpyAsync(XC, c->d_XC, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream));
     DFTG_TRY(sync_scalars(c));

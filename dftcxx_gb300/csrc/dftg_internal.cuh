@@ -23,6 +23,7 @@ constexpr double kPiTrunc = 3.14159265359;          // cgf.cpp:103, integrals.cp
 constexpr int kLmaxCap = 16;
 constexpr int kMaxAtoms = 256;
 constexpr int kPtsAlign = 128;
+constexpr int kRholmSlices = 6;      // K slices of the mixed rho_lm GEMM (planes of d_rholm)
 
 void set_error(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
@@ -228,6 +229,12 @@ struct dftg_ctx {
     bool have_density = false;
     bool have_hartree = false;
     bool rho_scaled = false;      // rho on the device carries the correction factor
+
+    // CUDA graph of the per-build kernel sequence (keyed by precision mask and stream)
+    cudaGraphExec_t pipe_exec = nullptr;
+    unsigned pipe_mask = 0;
+    cudaStream_t pipe_stream = nullptr;
+    bool pipe_warm = false;
 
     // per-phase CUDA-event timing (dftg_fock_build_profile)
     static constexpr int kMaxMarks = 24;

@@ -258,7 +258,10 @@ __device__ void lda_point_mixed(double rho, double &e, float &v)
     double ec = 0.0;
     float vc = 0.f;
     if (!(rho < 1e-10)) {
-        const float x = sqrtf(cbrtf((float)(K34PI / rho)));
+        // x^6 = (3 / 4 pi) / rho in FP32 (no FP64 division): K split hi + lo
+        constexpr float K34PIh = (float)K34PI, K34PIl = (float)(K34PI - (double)(float)K34PI);
+        const float rinv = 1.f / (float)rho;
+        const float x = sqrtf(cbrtf(fmaf(K34PIh, rinv, K34PIl * rinv)));
         const float X = fmaf(x, x + Bf, Cf);
         const float L1 = logf(x * x / X);
         const float L2 = logf((x - X0f) * (x - X0f) / X);

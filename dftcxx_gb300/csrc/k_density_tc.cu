@@ -154,22 +154,20 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
                 tc_fence_after();
                 const uint64_t a_st = desc_add(a_desc0, (uint32_t)s * a_stage_bytes);
                 const uint32_t d_hi = tmem + (uint32_t)(s * 256), d_lo = d_hi + 128;
-                // leading product A_1 B_1 into D_hi, then the nine correction pairs into D_lo
-                for (int kk = 0; kk < ksteps; ++kk)
-                    mma_bf16(d_hi, desc_add(a_st, kk * 2 * lbo), desc_add(b_desc0, kk * 2 * lbo), idesc, kk > 0 ? 1u : 0u);
-                uint32_t acc = 0u;
+                // K step outermost (the tensor core reuses the K block's operands): the
+                // leading product A_1 B_1 into D_hi, the nine correction pairs into D_lo
+                for (int kk = 0; kk < ksteps; ++kk) {
+                    const uint64_t ak = desc_add(a_st, kk * 2 * lbo), bk = desc_add(b_desc0, kk * 2 * lbo);
 #pragma unroll
-                for (int i = 1; i <= 4; ++i)
+                    for (int i = 1; i <= 4; ++i)
 #pragma unroll
-                    for (int j = 1; i + j <= 5; ++j) {
-                        if (i == 1 && j == 1) continue;
-                        const uint64_t ai = desc_add(a_st, (uint32_t)(i - 1) * a_slice_bytes);
-                        const uint64_t bj = desc_add(b_desc0, (uint32_t)(j - 1) * b_slice_bytes);
-                        for (int kk = 0; kk < ksteps; ++kk) {
-                            mma_bf16(d_lo, desc_add(ai, kk * 2 * lbo), desc_add(bj, kk * 2 * lbo), idesc, acc);
-                            acc = 1u;
+                        for (int j = 1; i + j <= 5; ++j) {
+                            const uint64_t ad = desc_add(ak, (uint32_t)(i - 1) * a_slice_bytes);
+                            const uint64_t bd = desc_add(bk, (uint32_t)(j - 1) * b_slice_bytes);
+                            if (i == 1 && j == 1) mma_bf16(d_hi, ad, bd, idesc, kk > 0 ? 1u : 0u);
+                            else mma_bf16(d_lo, ad, bd, idesc, (kk == 0 && i == 1 && j == 2) ? 0u : 1u);
                         }
-                    }
+                }
                 mma_commit(&sh->tmem_full[s]);
             }
         }
