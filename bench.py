@@ -41,8 +41,9 @@ WORKLOAD = {"workload": "benzene/6-31G grid Fock build", "molecule": "C6H6 D6h",
             "radial_points": 75, "lebedev_points": 302, "lmax": 8, "grid_points": 271800}
 
 # kernels launched per phase of one mixed-precision build (dftg_fock_build_device)
-KERNELS_PER_PHASE = {"density": 2, "charge": 2, "lda": 2, "rholm": 1, "poisson": 1, "vown": 1,
-                     "splines": 1, "vcross": 2, "hartree_energy": 2, "contract": 2, "contract_reduce": 1}
+KERNELS_PER_PHASE = {"density": 2, "charge": 1, "lda": 1, "rholm": 2, "poisson": 1, "vown": 1,
+                     "splines": 1, "vcross": 2, "hartree_energy": 1, "contract_bounds": 1, "contract": 1,
+                     "contract_reduce": 1}
 
 
 def _env_int(name, default):
@@ -343,20 +344,33 @@ def run_ours(args, rank, world):
     if world > 1:
         ms_mx, ms_e2e, ms_64 = max_over_ranks([ms_mx, ms_e2e, ms_64], f"cuda:{dev}")
 
-    # roofline of the dominant mixed-precision kernel
+    # roofline of the dominant mixed-precision kernel: algorithmic bytes per
+    # launch (the operands each kernel must stream) over the per-phase CUDA-event
+    # time of that kernel; DRAM traffic per launch from the committed ncu summary
     hbm, _, peak_src = _peaks()
     npts, nbf = grid.grid_size, mol.nbf
     npad = (npts + 127) // 128 * 128
+    kp, ar = (nbf + 15) // 16 * 16, (nbf + 7) // 8 * 8
+    npairs = npts * (mol.natoms - 1)
     alg_bytes = {
-        "density": npad * nbf * 4 + 8 * npad + 4 * nbf * nbf,          # phi32 read, rho written, P read
-        "contract": npad * nbf * 4 + 2 * 4 * npad,                      # phi32 + two coefficient planes
-        "vcross": npad * (3 * 8 + 8 + 8 + 16),                          # xyz, w, V_own in; V, cj out
-        "lda": npad * (8 + 8) + npad * (8 + 4),
+        # four BF16 slices of phi per point (tile layout), rho written
+        "density": 4 * npad * kp * 2 + 8 * npad,
+        # three BF16 slices of phi per point (chunk layout), c_xc and c_j (FP32), CTA partials
+        "contract": 3 * npad * ar * 2 + 2 * 4 * npad,
+        # per pair: direction and 1/r (16 B), offset and bin (8 B) in, contribution (8 B) out
+        "vcross": 32 * npairs,
+        "lda": npad * (8 + 8 + 8) + npad * (8 + 4),
     }
     dom = max(prof_mx, key=lambda k: prof_mx[k])
     dom_ms = prof_mx[dom]
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
+            traffic = json.load(f).get(dom)
+    except Exception:
+        traffic = None
     roof = {"kernel": dom, "bound": "hbm", "unit": "GB/s", "peak": hbm, "peak_source": peak_src,
-            "traffic": None}
+            "traffic": traffic}
     if dom in alg_bytes:
         ach = alg_bytes[dom] / (dom_ms * 1e-3) / 1e9
         roof.update(achieved=ach, frac=ach / hbm, bytes_per_launch=alg_bytes[dom])

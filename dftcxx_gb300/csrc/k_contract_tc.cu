@@ -674,6 +674,7 @@ int launch_contract_tc(dftg_ctx *c)
     int2 *cexp = reinterpret_cast<int2 *>(c->d_ct_rowexp + 2 * (size_t)c->ct_nchunk * c->nbf);
     k_ct_cexp<<<c->ct_nchunk, 256, 0, c->stream>>>(c->ct_nkb, c->ct_kbpc, c->d_cxc32, c->d_cj32, c->d_ct_winv, cexp);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "contract_bounds");
     k_contract_tc<<<c->ct_grid, kCtThreads, ct_smem(c->ct_nst, c->ct_NP, c->ct_AR, c->nbf, c->ct_spart != 0), c->stream>>>(
         c->nbf, c->ct_AR, c->ct_NP, c->ct_nst, c->ct_spart, c->ct_nkb, c->ct_kbpc, c->ct_nchunk,
         reinterpret_cast<const unsigned char *>(c->d_ct_A), c->d_ct_rowexp,

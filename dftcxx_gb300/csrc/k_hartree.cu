@@ -514,36 +514,6 @@ __global__ void k_poisson(int natoms, int nrad, int lmax, const double *__restri
     }
 }
 
-// y_i = sum_k M[k][i] x_k for i < n (M: n x n, row k contiguous, double-float
-// planes Mh / Ml; x in shared memory as xh / xl), all threads of the block
-// taking part: M passes through shared memory in tiles of kMvTile rows loaded
-// cooperatively (coalesced), so no thread waits on its own chain of loads.
-constexpr int kMvTile = 16;
-__device__ __forceinline__ dfl matvec_df_tiled(int n, int i, const float *__restrict__ Mh, const float *__restrict__ Ml,
-                                               const float *xh, const float *xl, float *tile /* [2][kMvTile][n] */)
-{
-    dfl a0{0.f, 0.f}, a1{0.f, 0.f};
-    for (int k0 = 0; k0 < n; k0 += kMvTile) {
-        const int kt = min(kMvTile, n - k0);
-        for (int e = threadIdx.x; e < kt * n; e += blockDim.x) {
-            tile[e] = Mh[(size_t)k0 * n + e];
-            tile[kMvTile * n + e] = Ml[(size_t)k0 * n + e];
-        }
-        __syncthreads();
-        if (i < n) {
-            int k = 0;
-            for (; k + 1 < kt; k += 2) {
-                a0 = df_fma(a0, dfl{tile[k * n + i], tile[kMvTile * n + k * n + i]}, dfl{xh[k0 + k], xl[k0 + k]});
-                a1 = df_fma(a1, dfl{tile[(k + 1) * n + i], tile[kMvTile * n + (k + 1) * n + i]},
-                            dfl{xh[k0 + k + 1], xl[k0 + k + 1]});
-            }
-            if (k < kt) a0 = df_fma(a0, dfl{tile[k * n + i], tile[kMvTile * n + k * n + i]}, dfl{xh[k0 + k], xl[k0 + k]});
-        }
-        __syncthreads();
-    }
-    return df_add(a0, a1);
-}
-
 // K5b (mixed): the same map in double-float arithmetic.  maps: the double-float
 // copies laid out as in hartree_setup.
 __global__ void k_poisson_split(int natoms, int nrad, int lmax, const float *__restrict__ maps,
@@ -566,9 +536,16 @@ __global__ void k_poisson_split(int natoms, int nrad, int lmax, const float *__r
     }
     __syncthreads();
     const dfl q = lm == 0 ? df_from(scal[kScalAtomQ + a]) : dfl{0.f, 0.f};
-    const int i = threadIdx.x;                 // blockDim.x >= N
-    dfl v = matvec_df_tiled(N, i, Gh, Gl, s_r2, s_r2 + N, s_r2 + 2 * N);
-    if (i < N) {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        dfl acc0{0.f, 0.f}, acc1{0.f, 0.f};
+        int k = 0;
+        for (; k + 1 < N; k += 2) {
+            acc0 = df_fma(acc0, dfl{Gh[(size_t)k * N + i], Gl[(size_t)k * N + i]}, dfl{s_r2[k], s_r2[N + k]});
+            acc1 = df_fma(acc1, dfl{Gh[(size_t)(k + 1) * N + i], Gl[(size_t)(k + 1) * N + i]},
+                          dfl{s_r2[k + 1], s_r2[N + k + 1]});
+        }
+        if (k < N) acc0 = df_fma(acc0, dfl{Gh[(size_t)k * N + i], Gl[(size_t)k * N + i]}, dfl{s_r2[k], s_r2[N + k]});
+        dfl v = df_add(acc0, acc1);
         if (lm == 0) v = df_fma(v, dfl{Gbh[i], Gbl[i]}, q);
         U[(size_t)id * N + i] = df_to(v);
         U32[(size_t)id * N + i] = v.h;
@@ -670,13 +647,17 @@ __global__ void k_splines_split(int natoms, int nrad, int nlm, int lmax, const f
         yl[i] = U32[uhalf + (size_t)id * n + n - 1 - i];
     }
     __syncthreads();
-    {
-        const int i = threadIdx.x;             // blockDim.x >= n
-        const dfl d = matvec_df_tiled(n, i, Kh, Kl, yh, yl, s_y2 + 4 * n);
-        if (i < n) {
-            Dh[i] = d.h;
-            Dl[i] = d.l;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        dfl a0{0.f, 0.f}, a1{0.f, 0.f};
+        int j = 0;
+        for (; j + 1 < n; j += 2) {
+            a0 = df_fma(a0, dfl{Kh[(size_t)j * n + i], Kl[(size_t)j * n + i]}, dfl{yh[j], yl[j]});
+            a1 = df_fma(a1, dfl{Kh[(size_t)(j + 1) * n + i], Kl[(size_t)(j + 1) * n + i]}, dfl{yh[j + 1], yl[j + 1]});
         }
+        if (j < n) a0 = df_fma(a0, dfl{Kh[(size_t)j * n + i], Kl[(size_t)j * n + i]}, dfl{yh[j], yl[j]});
+        const dfl d = df_add(a0, a1);
+        Dh[i] = d.h;
+        Dl[i] = d.l;
     }
     __syncthreads();
     const int lm = id % nlm;
@@ -788,11 +769,11 @@ __global__ void __launch_bounds__(128) k_vcross64(size_t npts, size_t npad, int 
     cj32[p] = (float)c;
 }
 
-constexpr int kCrossPerThread = 2;               // pairs per thread of k_vcross_bins
+constexpr int kCrossPerThread = 4;               // pairs per thread of k_vcross_bins
 constexpr int kCrossTask = 128 * kCrossPerThread;  // pairs per block
 // low halves of the spline coefficients are evaluated for l <= kCrossLoLmax:
-// beyond l = 2 they change E_tot of benzene / 6-31G by < 1e-8 Ha
-constexpr int kCrossLoLmax = 2;
+// beyond l = 0 they change E_tot of benzene / 6-31G by < 1e-9 Ha
+constexpr int kCrossLoLmax = 0;
 
 // K5e (mixed): FP32 recursion with exact integer coefficients; the spline
 // coefficients (which carry the Y_lm normalisation) enter as split FP32 hi/lo
@@ -1064,8 +1045,8 @@ static int launch_vcross_bins(dftg_ctx *c)
 int launch_hartree(dftg_ctx *c)
 {
     const int N = c->nrad, S = N + 2, nlm = c->nlm;
-    // the mixed multipole kernels keep a radial vector and a matrix tile per block
-    // in shared memory: up to 256 radial points (the FP64 kernels take any)
+    // the mixed multipole kernels keep radial vectors per block in shared
+    // memory: up to 256 radial points (the FP64 kernels take any)
     const bool mp = (c->prec_mask & kPrecMultipole) != 0 && N <= 256;
     const size_t rplane = (size_t)c->natoms * nlm * N;
     if (mp) {
@@ -1086,7 +1067,7 @@ int launch_hartree(dftg_ctx *c)
     const int nrhs = c->natoms * nlm;
     (void)S;
     if (mp)
-        k_poisson_split<<<nrhs, ((N + 31) / 32) * 32, sizeof(float) * (2 * N + 2 * kMvTile * N), c->stream>>>(
+        k_poisson_split<<<nrhs, 128, sizeof(float) * 2 * N, c->stream>>>(
             c->natoms, N, c->lmax, c->d_maps32,
                                                                          c->d_rholm, rplane, c->d_scal, c->d_U,
                                                                          c->d_U32, c->d_U32T);
@@ -1108,7 +1089,7 @@ int launch_hartree(dftg_ctx *c)
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "vown");
     if (mp)
-        k_splines_split<<<nrhs, ((N + 31) / 32) * 32, sizeof(float) * (4 * N + 2 * kMvTile * N), c->stream>>>(
+        k_splines_split<<<nrhs, 128, sizeof(float) * 4 * N, c->stream>>>(
             c->natoms, N, nlm, c->lmax, c->d_maps32, c->d_U32, (c->prec_mask & kPrecCross) ? 0 : 1, c->d_spl,
             c->d_splm);
     else
