@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <mutex>
 #include <vector>
 #include "dftg_internal.cuh"
 #include "lebedev_data.h"
@@ -228,6 +229,22 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(density_tc_setup(c));
     DFTG_TRY(cross_pairs_setup(c));
     DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    return DFTG_OK;
+}
+
+int allow_max_dyn_smem(const void *func, int device)
+{
+    static std::mutex mu;
+    static std::vector<std::pair<const void *, int>> done;
+    std::lock_guard<std::mutex> lock(mu);
+    for (const auto &d : done)
+        if (d.first == func && d.second == device) return DFTG_OK;
+    int optin = 0;
+    DFTG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    cudaFuncAttributes fa{};
+    DFTG_CUDA(cudaFuncGetAttributes(&fa, func));
+    DFTG_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    done.emplace_back(func, device);
     return DFTG_OK;
 }
 
@@ -637,3 +654,145 @@ int dftg_nuclear_repulsion(const dftg_ctx *c, double *enuc)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ batches
+
+struct dftg_batch {
+    std::vector<dftg_ctx *> ctx;
+    std::vector<cudaEvent_t> join;      // per context: end of its branch
+    cudaEvent_t fork = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<const void *> key;      // buffers, masks and stream the graph was captured with
+    bool warm = false;
+};
+
+static void batch_free(dftg_batch *b)
+{
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->fork) cudaEventDestroy(b->fork);
+    for (cudaEvent_t e : b->join)
+        if (e) cudaEventDestroy(e);
+    delete b;
+}
+
+// one context's build on its own stream (copies in and out included)
+static int batch_branch(dftg_ctx *c, const double *P, double *J, double *XC, double *sc)
+{
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    if (P != c->d_P) DFTG_CUDA(cudaMemcpyAsync(c->d_P, P, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
+    DFTG_TRY(fock_pipeline(c));
+    if (J) DFTG_CUDA(cudaMemcpyAsync(J, c->d_J, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
+    if (XC) DFTG_CUDA(cudaMemcpyAsync(XC, c->d_XC, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
+    if (sc) {
+        DFTG_CUDA(cudaMemcpyAsync(sc, c->d_scal + kScalExc, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        DFTG_CUDA(cudaMemcpyAsync(sc + 1, c->d_scal + kScalNelec, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        DFTG_CUDA(cudaMemcpyAsync(sc + 2, c->d_scal + kScalEJ, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    c->have_density = true;
+    c->have_hartree = true;
+    return DFTG_OK;
+}
+
+extern "C" int dftg_batch_create(dftg_ctx *const *ctxs, int n, dftg_batch **out)
+{
+    if (!out) { set_error("out is NULL"); return DFTG_ERR_ARG; }
+    *out = nullptr;
+    if (!ctxs || n < 1) { set_error("empty batch"); return DFTG_ERR_ARG; }
+    for (int i = 0; i < n; ++i) {
+        if (!ctxs[i]) { set_error("context %d is NULL", i); return DFTG_ERR_ARG; }
+        for (int j = 0; j < i; ++j)
+            if (ctxs[j] == ctxs[i]) { set_error("context %d repeated", i); return DFTG_ERR_ARG; }
+        if (ctxs[i]->device != ctxs[0]->device) { set_error("contexts on different devices"); return DFTG_ERR_ARG; }
+    }
+    dftg_batch *b = new (std::nothrow) dftg_batch();
+    if (!b) { set_error("host allocation failed"); return DFTG_ERR_NOMEM; }
+    b->ctx.assign(ctxs, ctxs + n);
+    b->join.assign(n, nullptr);
+    cudaError_t e = cudaSetDevice(ctxs[0]->device);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        batch_free(b);
+        return cuda_fail(e, "batch events", __FILE__, __LINE__);
+    }
+    *out = b;
+    return DFTG_OK;
+}
+
+extern "C" int dftg_batch_destroy(dftg_batch *b)
+{
+    batch_free(b);
+    return DFTG_OK;
+}
+
+extern "C" int dftg_batch_fock_build_device(dftg_batch *b, const double *const *P_devs, double *const *J_devs,
+                                            double *const *XC_devs, double *const *scalars_devs, void *stream)
+{
+    if (!b) { set_error("null batch"); return DFTG_ERR_ARG; }
+    if (!P_devs) { set_error("P_devs NULL"); return DFTG_ERR_ARG; }
+    const int n = (int)b->ctx.size();
+    for (int i = 0; i < n; ++i)
+        if (!P_devs[i]) { set_error("P_devs[%d] NULL", i); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(b->ctx[0]->device));
+    cudaStream_t s0 = stream ? reinterpret_cast<cudaStream_t>(stream) : b->ctx[0]->stream;
+    std::vector<const void *> key;
+    key.push_back(s0);
+    for (int i = 0; i < n; ++i) {
+        key.push_back(P_devs[i]);
+        key.push_back(J_devs ? J_devs[i] : nullptr);
+        key.push_back(XC_devs ? XC_devs[i] : nullptr);
+        key.push_back(scalars_devs ? scalars_devs[i] : nullptr);
+        key.push_back(reinterpret_cast<const void *>((uintptr_t)b->ctx[i]->prec_mask));
+        key.push_back(b->ctx[i]->stream);
+    }
+    if (b->exec && key != b->key) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+        b->warm = false;
+    }
+    auto enqueue = [&]() -> int {
+        // fork: every branch waits for s0, s0 waits for every branch
+        DFTG_CUDA(cudaEventRecord(b->fork, s0));
+        for (int i = 0; i < n; ++i) {
+            dftg_ctx *c = b->ctx[i];
+            if (c->stream != s0) DFTG_CUDA(cudaStreamWaitEvent(c->stream, b->fork, 0));
+            DFTG_TRY(batch_branch(c, P_devs[i], J_devs ? J_devs[i] : nullptr, XC_devs ? XC_devs[i] : nullptr,
+                                  scalars_devs ? scalars_devs[i] : nullptr));
+            if (c->stream != s0) {
+                DFTG_CUDA(cudaEventRecord(b->join[i], c->stream));
+                DFTG_CUDA(cudaStreamWaitEvent(s0, b->join[i], 0));
+            }
+        }
+        return DFTG_OK;
+    };
+    if (!b->exec) {
+        if (!b->warm || key != b->key) {
+            b->warm = true;
+            b->key = key;
+            return enqueue();
+        }
+        cudaGraph_t g = nullptr;
+        DFTG_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue();
+        const cudaError_t e = cudaStreamEndCapture(s0, &g);
+        if (rc != DFTG_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+        const cudaError_t ei = cudaGraphInstantiate(&b->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            b->exec = nullptr;
+            return cuda_fail(ei, "cudaGraphInstantiate", __FILE__, __LINE__);
+        }
+    }
+    DFTG_CUDA(cudaGraphLaunch(b->exec, s0));
+    for (dftg_ctx *c : b->ctx) {
+        c->rho_scaled = true;
+        c->have_density = true;
+        c->have_hartree = true;
+    }
+    return DFTG_OK;
+}

@@ -267,6 +267,11 @@ enum {
 };
 inline size_t scal_elems(int natoms) { return 8 + (size_t)natoms; }
 
+// Raise a kernel's dynamic shared-memory limit to the device maximum (minus
+// its static shared memory), once per kernel and device.  The limit is a
+// property of the function, shared by every context, so it is never lowered.
+int allow_max_dyn_smem(const void *func, int device);
+
 // records a named event after the preceding launch when profiling is on
 int mark(dftg_ctx *c, const char *name);
 #define DFTG_MARK(c, name) do { if ((c)->prof_on) { int rc_m_ = ::dftg::mark((c), (name)); if (rc_m_) return rc_m_; } } while (0)

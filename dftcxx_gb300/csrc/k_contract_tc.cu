@@ -553,43 +553,44 @@ static size_t ct_smem(int nst, int NP, int AR, int nbf, bool spart)
 }
 
 // Sum the double-float CTA partials of every element on or above the diagonal
-// in CTA order, in FP64, and write XC, J symmetrically (column-major).  Block:
-// 32 elements x 8 CTA groups; group g sums CTAs g, g + 8, ...; the 8 group sums
-// are added in a fixed order.
-__global__ void __launch_bounds__(256) k_contract_tc_reduce(int nbf, int nparts, int want_xc, int want_j,
-                                                            const float2 *__restrict__ part,
-                                                            double *__restrict__ XC, double *__restrict__ J)
+// in CTA order (double-float, no FP64 until the final value) and write XC, J
+// symmetrically (column-major).  Block: 32 elements x 32 CTA groups; group g
+// sums CTAs g, g + 32, ...; the 32 group sums are added in a fixed order.
+__global__ void __launch_bounds__(1024) k_contract_tc_reduce(int nbf, int nparts, int want_xc, int want_j,
+                                                             const float2 *__restrict__ part,
+                                                             double *__restrict__ XC, double *__restrict__ J)
 {
-    __shared__ double shx[8][33], shj[8][33];
+    __shared__ float2 shx[32][33], shj[32][33];
     const size_t nn = (size_t)nbf * nbf, ntri = (size_t)nbf * (nbf + 1) / 2;
     const int lx = threadIdx.x & 31, g = threadIdx.x >> 5;
     const size_t e = (size_t)blockIdx.x * 32 + lx;          // element (mu, nu) = e % nbf, e / nbf
-    double sx = 0.0, sj = 0.0;
     const int nu = (int)(e / nbf), mu = (int)(e % nbf);
     const bool act = e < nn && mu <= nu;
     const size_t t = (size_t)nu * (nu + 1) / 2 + mu;        // packed upper-triangle index
+    dfl sx{0.f, 0.f}, sj{0.f, 0.f};
     if (act)
-        for (int c = g; c < nparts; c += 8) {
+        for (int c = g; c < nparts; c += 32) {
             const float2 *p = part + (size_t)c * 2 * ntri;
             const float2 a = p[t], b = p[ntri + t];
-            sx += (double)a.x + (double)a.y;
-            sj += (double)b.x + (double)b.y;
+            sx = df_add(sx, dfl{a.x, a.y});
+            sj = df_add(sj, dfl{b.x, b.y});
         }
-    shx[g][lx] = sx;
-    shj[g][lx] = sj;
+    shx[g][lx] = make_float2(sx.h, sx.l);
+    shj[g][lx] = make_float2(sj.h, sj.l);
     __syncthreads();
     if (g != 0 || !act) return;
-    for (int k = 1; k < 8; ++k) {
-        sx += shx[k][lx];
-        sj += shj[k][lx];
+    for (int k = 1; k < 32; ++k) {
+        sx = df_add(sx, dfl{shx[k][lx].x, shx[k][lx].y});
+        sj = df_add(sj, dfl{shj[k][lx].x, shj[k][lx].y});
     }
+    const double vx = df_to(sx), vj = df_to(sj);
     if (want_xc) {
-        XC[(size_t)nu * nbf + mu] = sx;
-        XC[(size_t)mu * nbf + nu] = sx;
+        XC[(size_t)nu * nbf + mu] = vx;
+        XC[(size_t)mu * nbf + nu] = vx;
     }
     if (want_j) {
-        J[(size_t)nu * nbf + mu] = sj;
-        J[(size_t)mu * nbf + nu] = sj;
+        J[(size_t)nu * nbf + mu] = vj;
+        J[(size_t)mu * nbf + nu] = vj;
     }
 }
 
@@ -639,8 +640,7 @@ int contract_tc_setup(dftg_ctx *c)
     ct_plan(c->npad, nsm, nkb, kbpc, nchunk);
     const int grid = nchunk < nsm ? nchunk : nsm;
     if ((size_t)grid * c->nbf * (c->nbf + 1) > c->part_elems) return DFTG_OK;
-    DFTG_CUDA(cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)ct_smem(nst, NP, AR, c->nbf, spart)));
+    DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_contract_tc), c->device));
     if (!c->d_flag) {
         DFTG_CUDA(cudaMalloc(&c->d_flag, sizeof(int)));
         DFTG_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
@@ -687,7 +687,7 @@ int launch_contract_tc(dftg_ctx *c)
 int launch_contract_tc_reduce(dftg_ctx *c, bool want_xc, bool want_j)
 {
     const size_t nn = (size_t)c->nbf * c->nbf;
-    k_contract_tc_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(
+    k_contract_tc_reduce<<<(unsigned)((nn + 31) / 32), 1024, 0, c->stream>>>(
         c->nbf, c->ct_grid, want_xc ? 1 : 0, want_j ? 1 : 0, reinterpret_cast<const float2 *>(c->d_part), c->d_XC,
         c->d_J);
     DFTG_LAUNCH_CHECK();

@@ -233,61 +233,102 @@ __device__ void lda_point(double rho_d, T &e, T &v)
     v = vx + vc;
 }
 
-// Mixed-path point kernel.  The transcendental functions run in FP32 on
-// per-point arguments (their errors differ point by point); every constant and
-// the energy density are combined in FP64, so no rounding is shared by all
-// points.  The potential (which enters the Fock matrix, not the energy) stays
-// FP32.  Constants: fac = -9/4 (2/3) (3/4pi)^(1/3); VWN paramagnetic
-// A = 0.0310907, x0 = -0.10498, b = 3.72744, c = 12.9352 (functionals.cpp:120),
-// Q = sqrt(4c - b^2), X0 = x0^2 + b x0 + c, K1 = b x0 / X0,
-// K2 = 2b/Q (1 - x0 (2 x0 + b) / X0).
-__device__ void lda_point_mixed(double rho, double &e, float &v)
+// Mixed point kernel with the energy density as a double-float (no FP64 work):
+// the transcendental parts in FP32, every constant shared by all points and
+// every product that carries the energy in double-float (TwoProd), so no
+// rounding is common to all points.
+__device__ void lda_point_df(dfl rho, dfl &e, float &v)
 {
     constexpr double FAC = -0.93052573634910019, K34PI = 0.238732414637843;
     constexpr double A = 0.0310907, K1 = -0.031167608678943783, K2 = 1.2474243062431216;
     constexpr float Af = 0.0310907f, X0f = -0.10498f, Bf = 3.72744f, Cf = 12.9352f, Qf = 6.1519908197590798f,
                     Q2f = 37.846991046399992f, K1f = -0.031167608678943783f, VXf = -1.2407009817988002f;
-    const double da = rho * 0.5;
-    double ex = 0.0;
-    float vx = 0.f;
-    if (!(da < 1e-10)) {
-        const float r3 = cbrtf((float)da);
-        ex = 2.0 * (FAC * da) * (double)r3;
-        vx = VXf * r3;
+    const dfl FACd = {(float)FAC, (float)(FAC - (double)(float)FAC)};
+    const dfl Ad = {(float)A, (float)(A - (double)(float)A)};
+    const dfl K1d = {(float)K1, (float)(K1 - (double)(float)K1)};
+    const dfl K2d = {(float)K2, (float)(K2 - (double)(float)K2)};
+    constexpr float K34PIh = (float)K34PI, K34PIl = (float)(K34PI - (double)(float)K34PI);
+    const float rf = rho.h + rho.l;
+    const dfl da = {0.5f * rho.h, 0.5f * rho.l};             // exact
+    e = dfl{0.f, 0.f};
+    v = 0.f;
+    if (!(rf * 0.5f < 1e-10f)) {
+        const float r3 = cbrtf(da.h);
+        const dfl ex = df_mul(df_mul(FACd, da), dfl{2.f * r3, 0.f});   // 2 FAC da^(4/3)
+        e = ex;
+        v = VXf * r3;
     }
-    double ec = 0.0;
-    float vc = 0.f;
-    if (!(rho < 1e-10)) {
-        // x^6 = (3 / 4 pi) / rho in FP32 (no FP64 division): K split hi + lo
-        constexpr float K34PIh = (float)K34PI, K34PIl = (float)(K34PI - (double)(float)K34PI);
-        const float rinv = 1.f / (float)rho;
+    if (!(rf < 1e-10f)) {
+        // x^6 = (3 / 4 pi) / rho in FP32 (no division in FP64): K split hi + lo
+        const float rinv = 1.f / rf;
         const float x = sqrtf(cbrtf(fmaf(K34PIh, rinv, K34PIl * rinv)));
         const float X = fmaf(x, x + Bf, Cf);
         const float L1 = logf(x * x / X);
         const float L2 = logf((x - X0f) * (x - X0f) / X);
         const float tb = 2.f * x + Bf;
         const float T = atanf(Qf / tb);
-        const double eps = A * ((double)L1 - K1 * (double)L2 + K2 * (double)T);
-        ec = eps * rho;
+        // eps = A (L1 - K1 L2 + K2 T), ec = eps rho
+        const dfl inner = df_add(df_sub(dfl{L1, 0.f}, df_mul(K1d, dfl{L2, 0.f})), df_mul(K2d, dfl{T, 0.f}));
+        const dfl eps = df_mul(Ad, inner);
+        e = df_add(e, df_mul(eps, rho));
         const float den = tb * tb + Q2f;
         const float deps = Af * (2.f / x - tb / X - 4.f * Bf / den -
                                  K1f * (2.f / (x - X0f) - tb / X - 4.f * (2.f * X0f + Bf) / den));
-        vc = (float)eps - (x / 6.f) * deps;
+        v += (eps.h + eps.l) - (x / 6.f) * deps;
     }
-    e = ex + ec;
-    v = vx + vc;
 }
 
 template <bool MIXED>
 __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restrict__ rho,
                                                    const double *__restrict__ w, double *__restrict__ scal,
                                                    int apply_scale, double *__restrict__ cxc,
-                                                   float *__restrict__ cxc32, double *__restrict__ part, int *counter)
+                                                   float *__restrict__ cxc32, double *__restrict__ part, int *counter,
+                                                   int want64)
 {
     __shared__ double sh[32];
+    __shared__ float shf[2][32];
     __shared__ int s_last;
     const size_t p = (size_t)blockIdx.x * kRedBlock + threadIdx.x;
     double ew = 0.0;
+    if (MIXED) {
+        // double-float point kernel and block sum; FP64 only for the density
+        // correction, the weight split and the block partial
+        dfl ewd{0.f, 0.f};
+        if (p < npad) {
+            double r = rho[p];
+            if (apply_scale) {
+                r *= scal[kScalScale];
+                rho[p] = r;
+            }
+            dfl e;
+            float v;
+            lda_point_df(df_from(r), e, v);
+            const dfl wd = df_from(w[p]);
+            ewd = df_mul(wd, e);
+            const float c32 = (wd.h + wd.l) * v;
+            cxc32[p] = c32;
+            if (want64) cxc[p] = w[p] * (double)v;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            ewd = df_add(ewd, dfl{__shfl_xor_sync(0xffffffffu, ewd.h, o), __shfl_xor_sync(0xffffffffu, ewd.l, o)});
+        if ((threadIdx.x & 31) == 0) {
+            shf[0][threadIdx.x >> 5] = ewd.h;
+            shf[1][threadIdx.x >> 5] = ewd.l;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            dfl t{0.f, 0.f};
+            for (int i = 0; i < kRedBlock / 32; ++i) t = df_add(t, dfl{shf[0][i], shf[1][i]});
+            part[blockIdx.x] = df_to(t);
+        }
+        if (!last_block(counter, &s_last)) return;
+        double t = 0.0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += kRedBlock) t += __ldcg(part + i);
+        t = block_sum(t, sh);
+        if (threadIdx.x == 0) scal[kScalExc] = t;
+        return;
+    }
     if (p < npad) {
         double r = rho[p];
         if (apply_scale) {        // density correction fused into the point kernel
@@ -296,13 +337,7 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
         }
         double e;
         double vd;
-        if (MIXED) {
-            float v;
-            lda_point_mixed(r, e, v);
-            vd = (double)v;
-        } else {
-            lda_point<double>(r, e, vd);
-        }
+        lda_point<double>(r, e, vd);
         const double wp = w[p];
         ew = wp * e;
         const double c = wp * vd;
@@ -326,14 +361,14 @@ int launch_density(dftg_ctx *c)
     if (!(c->prec_mask & kPrecDensity)) {
         const unsigned nb = (unsigned)(c->npad / 128);
         const size_t sm = (size_t)c->nbf * 32 * sizeof(double);
-        if (sm > 48 * 1024) DFTG_CUDA(cudaFuncSetAttribute(k_density<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_density<double>), c->device));
         k_density<double><<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi, c->d_P, c->d_rho);
     } else if (c->tc_ready) {
         DFTG_TRY_L(launch_density_tc(c));
     } else {
         const unsigned nb = (unsigned)((c->npad + 255) / 256);
         const size_t sm = (size_t)c->nbf * 16 * sizeof(float2);
-        if (sm > 48 * 1024) DFTG_CUDA(cudaFuncSetAttribute(k_density_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_density_split), c->device));
         k_density_split<<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi32, c->d_P, c->d_rho);
     }
     DFTG_LAUNCH_CHECK();
@@ -370,10 +405,11 @@ int launch_xc_points(dftg_ctx *c, bool apply_scale)
     const int sc = apply_scale ? 1 : 0;
     if (c->prec_mask & kPrecLda)
         k_lda<true><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_scal, sc, c->d_cxc, c->d_cxc32,
-                                                     c->d_red, c->d_counters + kCntLda);
+                                                     c->d_red, c->d_counters + kCntLda,
+                                                     (c->prec_mask & kPrecContract) && c->ct_ready ? 0 : 1);
     else
         k_lda<false><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_scal, sc, c->d_cxc,
-                                                      c->d_cxc32, c->d_red, c->d_counters + kCntLda);
+                                                      c->d_cxc32, c->d_red, c->d_counters + kCntLda, 1);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "lda");
     return DFTG_OK;

@@ -345,7 +345,8 @@ int density_tc_setup(dftg_ctx *c)
         c->nbf, c->tc_KP, c->npad, ntiles, c->d_phi, reinterpret_cast<__nv_bfloat16 *>(c->d_tcA), c->d_tc_rowexp);
     DFTG_LAUNCH_CHECK();
     const size_t sm = density_tc_smem(c->tc_KP, c->tc_NP);
-    DFTG_CUDA(cudaFuncSetAttribute(k_density_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    (void)sm;
+    DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_density_tc), c->device));
     int nsm = 0;
     DFTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     c->tc_grid = nsm < ntiles ? nsm : ntiles;

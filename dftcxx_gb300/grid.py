@@ -226,3 +226,40 @@ class DFT:
             if it >= max_iter:
                 break
         return self.et
+
+
+class Batch:
+    """Many MolecularGrid contexts built in one launch (dftg_batch_*): the
+    per-build kernel sequences are captured into one CUDA graph with a stream
+    branch per context and replayed.  Buffers are device tensors (torch), one
+    set per context; build() returns nothing and does not synchronise."""
+
+    def __init__(self, grids):
+        self.grids = list(grids)
+        n = len(self.grids)
+        arr = (ctypes.c_void_p * n)(*[g.handle for g in self.grids])
+        h = ctypes.c_void_p()
+        check(_lib.load().dftg_batch_create(arr, n, ctypes.byref(h)))
+        self._h = h.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().dftg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build(self, P_devs, J_devs=None, XC_devs=None, scal_devs=None, stream=None):
+        n = len(self.grids)
+
+        def ptrs(ts):
+            if ts is None:
+                return None
+            return (ctypes.c_void_p * n)(*[t.data_ptr() if t is not None else None for t in ts])
+
+        check(_lib.load().dftg_batch_fock_build_device(self._h, ptrs(P_devs), ptrs(J_devs), ptrs(XC_devs),
+                                                       ptrs(scal_devs), stream))

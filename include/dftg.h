@@ -161,6 +161,23 @@ int dftg_get_potential(const dftg_ctx *ctx, double *out, size_t cap);   /* Hartr
 int dftg_one_electron(dftg_ctx *ctx, double *S, double *T, double *V);
 int dftg_nuclear_repulsion(const dftg_ctx *ctx, double *enuc);
 
+/* Batched builds (no counterpart in the reference): many contexts -- molecules
+ * or geometries of any size -- built in one launch.  The per-build kernel
+ * sequences of all contexts are captured once into one CUDA graph, each
+ * context on its own stream branch, and the graph is replayed; the first call
+ * with a new set of buffers runs the builds one after another and the next one
+ * captures.  The contexts must be distinct and stay alive while the batch
+ * exists; each context keeps its own precision setting. */
+typedef struct dftg_batch dftg_batch;
+int dftg_batch_create(dftg_ctx *const *ctxs, int n, dftg_batch **out);
+int dftg_batch_destroy(dftg_batch *b);
+/* dftg_fock_build_device for every context i with P_devs[i], J_devs[i],
+ * XC_devs[i], scalars_devs[i] (arrays of n device pointers; J, XC and scalars
+ * entries may be NULL).  stream: a cudaStream_t the batch is ordered on (NULL:
+ * the first context's stream); the call returns without synchronising. */
+int dftg_batch_fock_build_device(dftg_batch *b, const double *const *P_devs, double *const *J_devs,
+                                 double *const *XC_devs, double *const *scalars_devs, void *stream);
+
 /* XC and J contraction that allocates nothing.  No counterpart in the
  * reference: it exists for callers that may not call cudaMalloc / cudaFree
  * while serving (their framework owns all device memory, or they run under a
