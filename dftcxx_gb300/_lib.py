@@ -77,6 +77,8 @@ SIGNATURES = {
                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     "dftg_nuclear_repulsion": [ctypes.c_void_p, _dp],
     "dftg_get_energies": [ctypes.c_void_p, _dp, _dp, _dp],
+    "dftg_backward": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _dp, _dp],
+    "dftg_backward_device": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p],
     "dftg_batch_create": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)],
     "dftg_batch_destroy": [ctypes.c_void_p],
     "dftg_batch_fock_build_device": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),

@@ -78,7 +78,9 @@ static void free_ctx(dftg_ctx *c)
                     c->d_rec32, c->d_rholm, c->d_U, c->d_U32, c->d_Y32, c->d_Ywt32, c->d_fold, c->d_Gt,
                     c->d_Gb, c->d_Kt, c->d_sx, c->d_splf, c->d_spl, c->d_splm, c->d_tiles,
                     c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_flag,
-                    c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32, c->d_U32T, c->d_red2};
+                    c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32, c->d_U32T, c->d_red2,
+                    c->d_bw_pt, c->d_bw_lm, c->d_bw_fpart, c->d_bw_out, c->d_bw_counter, c->d_bw_pairp,
+                    c->d_bw_binfirst, c->d_bw_cpart};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -455,6 +457,7 @@ int dftg_set_density(dftg_ctx *c, const double *P)
     c->have_density = true;
     c->have_hartree = false;
     c->rho_scaled = false;
+    c->have_build = false;
     return DFTG_OK;
 }
 
@@ -526,6 +529,7 @@ int dftg_fock_build_device(dftg_ctx *c, const double *P_dev, double *J_dev, doub
     }
     c->have_density = true;
     c->have_hartree = true;
+    c->have_build = true;
     return DFTG_OK;
 }
 
@@ -557,6 +561,7 @@ int dftg_fock_build_profile(dftg_ctx *c, const double *P_dev, double *phase_ms, 
     *nphase = n;
     c->have_density = true;
     c->have_hartree = true;
+    c->have_build = true;
     return DFTG_OK;
 }
 
@@ -576,6 +581,7 @@ int dftg_fock_build(dftg_ctx *c, const double *P, double *J, double *XC, double 
     if (nelec) *nelec = c->h_scal[kScalNelec];
     c->have_density = true;
     c->have_hartree = true;
+    c->have_build = true;
     return DFTG_OK;
 }
 
@@ -638,6 +644,33 @@ int dftg_get_energies(dftg_ctx *c, double *exc, double *ej, double *nelec)
     return DFTG_OK;
 }
 
+int dftg_backward_device(dftg_ctx *c, double seed_exc, double seed_ej, double *dEdP_dev, double *dEdR_dev)
+{
+    CHECK_CTX(c);
+    if (!c->have_build) { set_error("backward before a complete Fock build"); return DFTG_ERR_STATE; }
+    if (!std::isfinite(seed_exc) || !std::isfinite(seed_ej)) { set_error("non-finite seed"); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    return launch_backward(c, seed_exc, seed_ej, dEdP_dev, dEdR_dev);
+}
+
+int dftg_backward(dftg_ctx *c, double seed_exc, double seed_ej, double *dEdP, double *dEdR)
+{
+    CHECK_CTX(c);
+    if (!c->have_build) { set_error("backward before a complete Fock build"); return DFTG_ERR_STATE; }
+    if (!std::isfinite(seed_exc) || !std::isfinite(seed_ej)) { set_error("non-finite seed"); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    if (!c->d_bw_out) {
+        DFTG_CUDA(cudaMalloc(&c->d_bw_out, sizeof(double) * ((size_t)c->nbf * c->nbf + (size_t)c->natoms * 3)));
+    }
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    double *dP = dEdP ? c->d_bw_out : nullptr, *dR = dEdR ? c->d_bw_out + nn : nullptr;
+    DFTG_TRY(launch_backward(c, seed_exc, seed_ej, dP, dR));
+    if (dEdP) DFTG_CUDA(cudaMemcpyAsync(dEdP, dP, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream));
+    if (dEdR) DFTG_CUDA(cudaMemcpyAsync(dEdR, dR, sizeof(double) * 3 * c->natoms, cudaMemcpyDeviceToHost, c->stream));
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    return DFTG_OK;
+}
+
 int dftg_nuclear_repulsion(const dftg_ctx *c, double *enuc)
 {
     CHECK_CTX(c);
@@ -691,6 +724,7 @@ static int batch_branch(dftg_ctx *c, const double *P, double *J, double *XC, dou
     }
     c->have_density = true;
     c->have_hartree = true;
+    c->have_build = true;
     return DFTG_OK;
 }
 
@@ -793,6 +827,7 @@ extern "C" int dftg_batch_fock_build_device(dftg_batch *b, const double *const *
         c->rho_scaled = true;
         c->have_density = true;
         c->have_hartree = true;
+        c->have_build = true;
     }
     return DFTG_OK;
 }

@@ -225,6 +225,19 @@ struct dftg_ctx {
     // device: one-electron integrals output (allocated on first use)
     double *d_ints_work = nullptr;
 
+    // backward pass (allocated on first use)
+    bool bw_ready = false;
+    int bw_nb_phi = 0, bw_nb_becke = 0, bw_nb_cross = 0;   // partial rows of the three force kernels
+    double *d_bw_pt = nullptr;    // [7][npad] u, mbar, g, e, h, 2h, dE/dwb
+    double *d_bw_lm = nullptr;    // Ubar, rbar [natoms][nlm][nrad], qbar [natoms], scalars [8], block sums
+    double *d_bw_fpart = nullptr; // [rows][natoms][3] per-block force partials
+    double *d_bw_out = nullptr;   // dE/dP [nbf][nbf], dE/dR [natoms][3]
+    int *d_bw_counter = nullptr;  // last-block counter of the gamma reduction
+    int *d_bw_pairp = nullptr;    // [npairs] grid point of each sorted pair
+    int *d_bw_binfirst = nullptr; // [natoms * nrad + 1] first task of each (atom, interval) bin
+    double *d_bw_cpart = nullptr; // [ncross_tasks][nlm][4] transposed cross-atom partials
+    bool have_build = false;      // a complete build left rho, V and the scalars on the device
+
     // call-order state
     bool have_density = false;
     bool have_hartree = false;
@@ -292,6 +305,9 @@ int hartree_setup(dftg_ctx *c);
 int cross_pairs_setup(dftg_ctx *c);
 size_t hartree_splf_elems(int nrad);
 int launch_hartree(dftg_ctx *c);
+int launch_multipoles_fp64(dftg_ctx *c);
+// k_adjoint.cu
+int launch_backward(dftg_ctx *c, double sxc, double sj, double *dEdP_dev, double *dEdR_dev);
 // k_integrals.cu
 int launch_one_electron(dftg_ctx *c, double *dS, double *dT, double *dV);
 // k_contract.cu
@@ -299,6 +315,7 @@ int contract_setup(dftg_ctx *c);
 size_t contract_part_elems(int nbf, size_t npad);
 size_t reduction_elems(size_t npad, int natoms, int nrad, int nang);
 int launch_contract(dftg_ctx *c, bool want_xc, bool want_j);
+int launch_contract_coef(dftg_ctx *c, const double *coef, double *out);
 // k_contract_tc.cu
 size_t contract_tc_part_elems(int nbf, size_t npad, int nsm);
 int contract_tc_setup(dftg_ctx *c);

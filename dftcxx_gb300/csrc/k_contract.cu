@@ -192,4 +192,23 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
     return DFTG_OK;
 }
 
+// out = phi^T diag(coef) phi in FP64 (the same kernels as the FP64 XC step),
+// for contractions with other point weights (the backward pass)
+int launch_contract_coef(dftg_ctx *c, const double *coef, double *out)
+{
+    const int R = tile_R(c->nbf), tile = 16 * R;
+    const int2 *d_tiles = reinterpret_cast<const int2 *>(c->d_tiles);
+    size_t per = (c->npad + c->nchunk - 1) / c->nchunk;
+    per = (per + kKB - 1) / kKB * kKB;
+    dim3 grid((unsigned)c->ntiles, (unsigned)c->nchunk);
+    if (R == 5) k_contract<double, 5><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, coef, coef, 1, 0, d_tiles, c->d_part);
+    else k_contract<double, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, coef, coef, 1, 0, d_tiles, c->d_part);
+    DFTG_LAUNCH_CHECK();
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, tile, c->nchunk, 1, 0, c->d_part,
+                                                                        out, nullptr);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
 }  // namespace dftg

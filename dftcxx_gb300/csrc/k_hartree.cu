@@ -1042,6 +1042,23 @@ static int launch_vcross_bins(dftg_ctx *c)
     return DFTG_OK;
 }
 
+// FP64 rho_lm, U_lm and spline coefficients of the density on the device
+// (the multipole steps of the FP64 build), for the backward pass
+int launch_multipoles_fp64(dftg_ctx *c)
+{
+    const int N = c->nrad, nlm = c->nlm, na = c->natoms;
+    k_rholm<<<na * N, 96, sizeof(double) * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho, c->d_wb, c->d_Yw,
+                                                                 c->d_rholm);
+    DFTG_LAUNCH_CHECK();
+    k_poisson<<<na * nlm, 128, sizeof(double) * N, c->stream>>>(na, N, c->lmax, c->d_Gt, c->d_Gb, c->d_rholm,
+                                                               c->d_scal, c->d_U, c->d_U32);
+    DFTG_LAUNCH_CHECK();
+    k_splines<<<na * nlm, 128, sizeof(double) * 2 * N, c->stream>>>(na, N, nlm, c->d_splf, c->d_Kt, c->d_U,
+                                                                   c->d_fold, c->d_spl, c->d_splm);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
 int launch_hartree(dftg_ctx *c)
 {
     const int N = c->nrad, S = N + 2, nlm = c->nlm;

@@ -119,6 +119,16 @@ class MolecularGrid:
         return {"J": np.ascontiguousarray(J), "XC": np.ascontiguousarray(XC), "Exc": e.value, "nelec": n.value,
                 "EJ": self.energies()["EJ"]}
 
+    def backward(self, seed_exc=1.0, seed_ej=1.0):
+        """Backward pass of the last fock_build (autograd-style vector-Jacobian
+        product): for E = seed_exc E_xc + seed_ej E_J returns (dE/dP [nbf x nbf],
+        dE/dR [natoms x 3] at fixed P).  The grid part of the nuclear forces
+        is -dE/dR."""
+        dP = np.zeros((self.nbf, self.nbf), order="F")
+        dR = np.zeros((self.mol.natoms, 3))
+        check(_lib.load().dftg_backward(self._h, float(seed_exc), float(seed_ej), _ptr(dP), _ptr(dR)))
+        return np.ascontiguousarray(dP), dR
+
     def energies(self):
         """E_xc, E_J = 2 tr(P J) summed on the grid in FP64, integrated density
         of the last build."""

@@ -161,6 +161,24 @@ int dftg_get_potential(const dftg_ctx *ctx, double *out, size_t cap);   /* Hartr
 int dftg_one_electron(dftg_ctx *ctx, double *S, double *T, double *V);
 int dftg_nuclear_repulsion(const dftg_ctx *ctx, double *enuc);
 
+/* Backward pass of the grid energy (no counterpart in the reference; the
+ * forward is the last complete Fock build on the context: dftg_fock_build,
+ * dftg_fock_build_device or a batch).  With E = seed_exc * E_xc + seed_ej * E_J,
+ * E_J = 2 tr(P J), computed by that build, writes
+ *   dEdP [nbf x nbf]  dE/dP_{mu nu}, every element of P taken as independent
+ *                     (symmetric; E changes by sum dEdP .* dP for a change dP),
+ *   dEdR [natoms][3]  dE/dR at fixed P: basis functions and grid points move
+ *                     with their atoms (amplitude gradients, Becke-weight
+ *                     derivatives, cross-atom potential geometry).  The grid
+ *                     part of the nuclear forces is -dEdR.
+ * Either output may be NULL.  The forward state (density, potential, weights)
+ * is read, not changed, except that the FP64 multipole work arrays are
+ * recomputed.  Errors: DFTG_ERR_STATE without a preceding complete build;
+ * DFTG_ERR_ARG for lmax > 13 or an amplitude block too large for shared memory. */
+int dftg_backward(dftg_ctx *ctx, double seed_exc, double seed_ej, double *dEdP, double *dEdR);
+/* The same on device buffers, ordered on the context's stream, no synchronisation. */
+int dftg_backward_device(dftg_ctx *ctx, double seed_exc, double seed_ej, double *dEdP_dev, double *dEdR_dev);
+
 /* Batched builds (no counterpart in the reference): many contexts -- molecules
  * or geometries of any size -- built in one launch.  The per-build kernel
  * sequences of all contexts are captured once into one CUDA graph, each
