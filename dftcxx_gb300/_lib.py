@@ -78,6 +78,8 @@ SIGNATURES = {
     "dftg_nuclear_repulsion": [ctypes.c_void_p, _dp],
     "dftg_get_energies": [ctypes.c_void_p, _dp, _dp, _dp],
     "dftg_backward": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _dp, _dp],
+    "dftg_backward_profile": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _dp, ctypes.POINTER(ctypes.c_char_p),
+                              ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
     "dftg_backward_device": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p],
     "dftg_batch_create": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)],
     "dftg_batch_destroy": [ctypes.c_void_p],

@@ -80,7 +80,7 @@ static void free_ctx(dftg_ctx *c)
                     c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_flag,
                     c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32, c->d_U32T, c->d_red2,
                     c->d_bw_pt, c->d_bw_lm, c->d_bw_fpart, c->d_bw_out, c->d_bw_counter, c->d_bw_pairp,
-                    c->d_bw_binfirst, c->d_bw_cpart};
+                    c->d_bw_binfirst, c->d_bw_cpart, c->d_bw_geo, c->d_bw_geo64};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -530,6 +530,7 @@ int dftg_fock_build_device(dftg_ctx *c, const double *P_dev, double *J_dev, doub
     c->have_density = true;
     c->have_hartree = true;
     c->have_build = true;
+    c->fwd_mask = c->prec_mask;
     return DFTG_OK;
 }
 
@@ -562,6 +563,7 @@ int dftg_fock_build_profile(dftg_ctx *c, const double *P_dev, double *phase_ms, 
     c->have_density = true;
     c->have_hartree = true;
     c->have_build = true;
+    c->fwd_mask = c->prec_mask;
     return DFTG_OK;
 }
 
@@ -582,6 +584,7 @@ int dftg_fock_build(dftg_ctx *c, const double *P, double *J, double *XC, double 
     c->have_density = true;
     c->have_hartree = true;
     c->have_build = true;
+    c->fwd_mask = c->prec_mask;
     return DFTG_OK;
 }
 
@@ -671,6 +674,34 @@ int dftg_backward(dftg_ctx *c, double seed_exc, double seed_ej, double *dEdP, do
     return DFTG_OK;
 }
 
+int dftg_backward_profile(dftg_ctx *c, double seed_exc, double seed_ej, double *phase_ms, const char **names,
+                          int cap, int *nphase)
+{
+    CHECK_CTX(c);
+    if (!phase_ms || !nphase) { set_error("NULL argument"); return DFTG_ERR_ARG; }
+    if (!c->have_build) { set_error("backward before a complete Fock build"); return DFTG_ERR_STATE; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    if (!c->d_bw_out)
+        DFTG_CUDA(cudaMalloc(&c->d_bw_out, sizeof(double) * ((size_t)c->nbf * c->nbf + (size_t)c->natoms * 3)));
+    c->prof_n = 0;
+    c->prof_on = true;
+    int rc = mark(c, "start");
+    if (rc == DFTG_OK)
+        rc = launch_backward(c, seed_exc, seed_ej, c->d_bw_out, c->d_bw_out + (size_t)c->nbf * c->nbf);
+    c->prof_on = false;
+    if (rc != DFTG_OK) return rc;
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    const int n = c->prof_n - 1 < cap ? c->prof_n - 1 : cap;
+    for (int i = 0; i < n; ++i) {
+        float ms = 0.f;
+        DFTG_CUDA(cudaEventElapsedTime(&ms, c->prof_ev[i], c->prof_ev[i + 1]));
+        phase_ms[i] = ms;
+        if (names) names[i] = c->prof_name[i + 1];
+    }
+    *nphase = n;
+    return DFTG_OK;
+}
+
 int dftg_nuclear_repulsion(const dftg_ctx *c, double *enuc)
 {
     CHECK_CTX(c);
@@ -725,6 +756,7 @@ static int batch_branch(dftg_ctx *c, const double *P, double *J, double *XC, dou
     c->have_density = true;
     c->have_hartree = true;
     c->have_build = true;
+    c->fwd_mask = c->prec_mask;
     return DFTG_OK;
 }
 
@@ -828,6 +860,7 @@ extern "C" int dftg_batch_fock_build_device(dftg_batch *b, const double *const *
         c->have_density = true;
         c->have_hartree = true;
         c->have_build = true;
+    c->fwd_mask = c->prec_mask;
     }
     return DFTG_OK;
 }

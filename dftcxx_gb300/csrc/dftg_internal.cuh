@@ -227,7 +227,10 @@ struct dftg_ctx {
 
     // backward pass (allocated on first use)
     bool bw_ready = false;
-    int bw_nb_phi = 0, bw_nb_becke = 0, bw_nb_cross = 0;   // partial rows of the three force kernels
+    int bw_nb_phi = 0, bw_nb_becke = 0, bw_nb_cross = 0, bw_nb_cross32 = 0;   // partial rows of the force kernels
+    float *d_bw_geo = nullptr;    // FP32 1 / R_Bk [natoms^2] (padded to 4), then [natoms^2][4] (R_B - R_k) / R_Bk
+    double *d_bw_geo64 = nullptr; // the same in FP64
+    int bw_geo_off = 0;           // element offset of the unit-vector table
     double *d_bw_pt = nullptr;    // [7][npad] u, mbar, g, e, h, 2h, dE/dwb
     double *d_bw_lm = nullptr;    // Ubar, rbar [natoms][nlm][nrad], qbar [natoms], scalars [8], block sums
     double *d_bw_fpart = nullptr; // [rows][natoms][3] per-block force partials
@@ -237,6 +240,7 @@ struct dftg_ctx {
     int *d_bw_binfirst = nullptr; // [natoms * nrad + 1] first task of each (atom, interval) bin
     double *d_bw_cpart = nullptr; // [ncross_tasks][nlm][4] transposed cross-atom partials
     bool have_build = false;      // a complete build left rho, V and the scalars on the device
+    unsigned fwd_mask = 0;        // precision mask of that build (the backward follows it)
 
     // call-order state
     bool have_density = false;
@@ -305,7 +309,6 @@ int hartree_setup(dftg_ctx *c);
 int cross_pairs_setup(dftg_ctx *c);
 size_t hartree_splf_elems(int nrad);
 int launch_hartree(dftg_ctx *c);
-int launch_multipoles_fp64(dftg_ctx *c);
 // k_adjoint.cu
 int launch_backward(dftg_ctx *c, double sxc, double sj, double *dEdP_dev, double *dEdR_dev);
 // k_integrals.cu
@@ -316,10 +319,13 @@ size_t contract_part_elems(int nbf, size_t npad);
 size_t reduction_elems(size_t npad, int natoms, int nrad, int nang);
 int launch_contract(dftg_ctx *c, bool want_xc, bool want_j);
 int launch_contract_coef(dftg_ctx *c, const double *coef, double *out);
+int launch_contract_coef32(dftg_ctx *c, const float *coef, double *out);
 // k_contract_tc.cu
 size_t contract_tc_part_elems(int nbf, size_t npad, int nsm);
 int contract_tc_setup(dftg_ctx *c);
 int launch_contract_tc(dftg_ctx *c);
 int launch_contract_tc_reduce(dftg_ctx *c, bool want_xc, bool want_j);
+int launch_contract_tc_on(dftg_ctx *c, const float *cxc32, const float *cj32);
+int launch_contract_tc_reduce_to(dftg_ctx *c, bool want_xc, bool want_j, double *XC, double *J);
 
 }  // namespace dftg

@@ -25,6 +25,8 @@
 //              + rho_p mbar_p / 2.
 // Every kernel here runs in FP64; per-atom force partials are reduced in a
 // fixed order (no floating-point atomics across blocks).
+#include <algorithm>
+#include <cmath>
 #include <vector>
 #include "dftg_internal.cuh"
 #include "lda_point.cuh"
@@ -253,7 +255,9 @@ __global__ void k_bw_poisson_T(int nrad, int lmax, const double *__restrict__ Gt
 }
 
 // Per point: mbar (transposed projection), g = s_xc w v + (A^T u) / 2, the
-// energy density e; block sums of g rho, the last block forms gamma.
+// energy density e (with the point functions of the build's precision); block
+// sums of g rho, the last block forms gamma.
+template <bool MIXED>
 __global__ void __launch_bounds__(kBwRed) k_bw_points(size_t npts, size_t npad, int nrad, int nang, int nlm,
                                                       const double *__restrict__ rho, const double *__restrict__ w,
                                                       const double *__restrict__ wb, const double *__restrict__ Yw,
@@ -277,7 +281,15 @@ __global__ void __launch_bounds__(kBwRed) k_bw_points(size_t npts, size_t npad, 
             mb *= 4.0 * kPi;
             const double at = wb[p] * mb + w[p] * qbar[a];
             double v;
-            lda_point<double>(rho[p], ep, v);
+            if (MIXED) {   // the mixed point kernel of the build: FP32 potential, double-float energy
+                dfl ed;
+                float vf;
+                lda_point_df(df_from(rho[p]), ed, vf);
+                ep = df_to(ed);
+                v = (double)vf;
+            } else {
+                lda_point<double>(rho[p], ep, v);
+            }
             gp = sxc * w[p] * v + 0.5 * at;
             gr = gp * rho[p];
         }
@@ -302,11 +314,11 @@ __global__ void k_bw_coef(size_t npts, size_t npad, int nrad, int nang, const do
                           const double *__restrict__ g, const double *__restrict__ e, const double *__restrict__ mbar,
                           const double *__restrict__ qbar, const double *__restrict__ scal,
                           const double *__restrict__ bw_scal, double sxc, double sj, double *__restrict__ h,
-                          double *__restrict__ h2, double *__restrict__ ewb)
+                          double *__restrict__ h2, float *__restrict__ h2f, double *__restrict__ ewb)
 {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npad) return;
-    if (p >= npts) { h[p] = 0.0; h2[p] = 0.0; ewb[p] = 0.0; return; }
+    if (p >= npts) { h[p] = 0.0; h2[p] = 0.0; h2f[p] = 0.f; ewb[p] = 0.0; return; }
     const int per_atom = nrad * nang;
     const int a = (int)(p / per_atom), rem = (int)(p % per_atom), i = rem / nang, j = rem % nang;
     const double c = scal[kScalScale], gamma = bw_scal[0];
@@ -314,6 +326,7 @@ __global__ void k_bw_coef(size_t npts, size_t npad, int nrad, int nang, const do
     const double hp = sj * 0.5 * wp * Vp + c * g[p] - gamma * wp;
     h[p] = hp;
     h2[p] = 2.0 * hp;
+    h2f[p] = (float)(2.0 * hp);
     // w0: the grid weight before the Becke factor, as the grid kernel forms it
     const double ri = rn[i];
     const double p2x = leb[4 * j] * ri, p2y = leb[4 * j + 1] * ri, p2z = leb[4 * j + 2] * ri;
@@ -673,14 +686,468 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_force_cross(size_t npts, int na
             ((s_a[e] + s_a[natoms * 3 + e]) + s_a[2 * natoms * 3 + e]) + s_a[3 * natoms * 3 + e];
 }
 
-// dEdR[a][c] = sum over the partial rows of the three force kernels, in row order
-__global__ void k_bw_force_sum(int natoms, int nrows, const double *__restrict__ part, double *__restrict__ dEdR)
+// dEdR[a][c] = sum over the partial rows of the three force kernels: one block
+// per element, fixed row assignment and order
+__global__ void __launch_bounds__(256) k_bw_force_sum(int natoms, int nrows, const double *__restrict__ part,
+                                                      double *__restrict__ dEdR)
 {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= natoms * 3) return;
+    __shared__ double sh[32];
+    const int e = blockIdx.x;
     double s = 0.0;
-    for (int r = 0; r < nrows; ++r) s += part[(size_t)r * natoms * 3 + e];
-    dEdR[e] = s;
+    for (int r = threadIdx.x; r < nrows; r += 256) s += part[(size_t)r * natoms * 3 + e];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) dEdR[e] = s;
+}
+
+// ---------------------------------------------------------------- mixed form
+// FP32 arithmetic per point or pair, FP64 sums per block and across blocks.
+
+// Becke cell function factors in factored form: with g_n = 1 - f_n and
+// h_n = 1 + f_n, 1 - f(x) = (1 - x)^2 (2 + x) / 2 and 1 + f(x) = (1 + x)^2 (2 - x) / 2,
+// so s(mu) = g_3 / 2 and s(-mu) = h_3 / 2 keep full relative precision down to
+// underflow; ds/dmu = -(3/2)^3 (1 - mu^2) g_1 h_1 g_2 h_2 / 2 (the same for s(-mu)).
+template <typename T>
+__device__ __forceinline__ void becke_sT(T mu, T &s_p, T &s_m, T &ds)
+{
+    const T g0 = T(1) - mu, h0 = T(1) + mu;
+    const T g1 = T(0.5) * g0 * g0 * (T(3) - g0), h1 = T(0.5) * h0 * h0 * (T(3) - h0);
+    const T g2 = T(0.5) * g1 * g1 * (T(3) - g1), h2 = T(0.5) * h1 * h1 * (T(3) - h1);
+    const T g3 = T(0.5) * g2 * g2 * (T(3) - g2), h3 = T(0.5) * h2 * h2 * (T(3) - h2);
+    s_p = T(0.5) * g3;
+    s_m = T(0.5) * h3;
+    ds = T(-0.5 * 3.375) * (g0 * h0) * (g1 * h1) * (g2 * h2);
+}
+
+// Becke-weight term, a group of G lanes per point (32 / G points per warp),
+// lane B of a group = cell B (natoms <= G).  Lane B forms P_B = prod_k s(mu_Bk)
+// and, for every k != B (k = B + t mod n at step t, so the lanes' targets
+// differ), coef = E alpha_B sigma_Bk / R_Bk: its own atom takes
+// coef (-e_B - mu e_Bk) and atom k, through a shuffle, takes coef (e_k + mu e_Bk)
+// (derivatives with the point held fixed).  Per point the lanes' vectors go to
+// FP64 and the point's own atom takes minus their sum over the other atoms (the
+// point moves with it), so each point adds exactly zero net force.
+// T = float (mixed) or double.
+template <typename T, int G>
+__global__ void __launch_bounds__(kBwBlock) k_bw_becke_w(size_t npts, int per_atom, int natoms,
+                                                         const double *__restrict__ atoms, const T *__restrict__ invR,
+                                                         const T *__restrict__ ebk, const double *__restrict__ X,
+                                                         const double *__restrict__ Yc, const double *__restrict__ Zc,
+                                                         const double *__restrict__ ewb, double *__restrict__ part)
+{
+    constexpr int NG = 32 / G;
+    __shared__ double s_acc[4][32][3];
+    __shared__ T s_dist[4][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = lane / G, B0 = lane % G;
+    const int n = natoms;
+    const bool act = B0 < n;
+    const int B = act ? B0 : 0;
+    T *sd = s_dist[warp] + grp * G;
+    const double ax = atoms[4 * B], ay = atoms[4 * B + 1], az = atoms[4 * B + 2];
+    double accx = 0.0, accy = 0.0, accz = 0.0;
+    const size_t stride = (size_t)gridDim.x * 4 * NG;
+    for (size_t base = ((size_t)blockIdx.x * 4 + warp) * NG; base < npts; base += stride) {
+        const size_t p = base + grp;
+        const double Ed = p < npts ? ewb[p] : 0.0;
+        const bool live = Ed != 0.0;
+        const T E = (T)Ed;
+        const int a = live ? (int)(p / per_atom) : 0;
+        const T vx = live ? (T)(X[p] - ax) : T(1), vy = live ? (T)(Yc[p] - ay) : T(0),
+                vz = live ? (T)(Zc[p] - az) : T(0);
+        const T dB = act ? sqrt(vx * vx + vy * vy + vz * vz) : T(1);
+        __syncwarp();
+        sd[B0] = dB;
+        __syncwarp();
+        T PB = T(1);
+        for (int k = 0; k < n; ++k)
+            if (k != B) {
+                T sp, sm, ds;
+                becke_sT<T>((dB - sd[k]) * invR[B * n + k], sp, sm, ds);
+                PB *= sp;
+            }
+        if (!act) PB = T(0);
+        T Z = PB;
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) Z += __shfl_xor_sync(0xffffffffu, Z, o, G);
+        const T iZ = T(1) / Z;
+        const T wb = __shfl_sync(0xffffffffu, PB, a, G) * iZ;
+        const T alB = ((B == a ? T(1) : T(0)) - wb) * iZ;
+        const T iB = T(1) / dB;
+        const T eBx = vx * iB, eBy = vy * iB, eBz = vz * iB;
+        T Dx = T(0), Dy = T(0), Dz = T(0);
+        for (int t = 1; t < n; ++t) {
+            const int k = act ? (B + t) % n : 0;
+            const int src = act ? (B - t + n) % n : 0;
+            const T ekx = __shfl_sync(0xffffffffu, eBx, k, G), eky = __shfl_sync(0xffffffffu, eBy, k, G),
+                    ekz = __shfl_sync(0xffffffffu, eBz, k, G);
+            T hx = T(0), hy = T(0), hz = T(0);
+            if (act && live) {
+                const T iR = invR[B * n + k];
+                const T mu = (dB - sd[k]) * iR;
+                T sp, sm, ds;
+                becke_sT<T>(mu, sp, sm, ds);
+                T sig;
+                if (sp > (sizeof(T) == 4 ? T(1e-30) : T(1e-290))) sig = ds * (PB / sp);
+                else {   // the factor underflows: product of the others
+                    sig = ds;
+                    for (int k2 = 0; k2 < n; ++k2)
+                        if (k2 != B && k2 != k) {
+                            T s2, m2, d2;
+                            becke_sT<T>((dB - sd[k2]) * invR[B * n + k2], s2, m2, d2);
+                            sig *= s2;
+                        }
+                }
+                const T coef = E * alB * sig * iR;
+                const T *u = ebk + 4 * ((size_t)B * n + k);
+                Dx -= coef * (eBx + mu * u[0]);
+                Dy -= coef * (eBy + mu * u[1]);
+                Dz -= coef * (eBz + mu * u[2]);
+                hx = coef * (ekx + mu * u[0]);
+                hy = coef * (eky + mu * u[1]);
+                hz = coef * (ekz + mu * u[2]);
+            }
+            Dx += __shfl_sync(0xffffffffu, hx, src, G);
+            Dy += __shfl_sync(0xffffffffu, hy, src, G);
+            Dz += __shfl_sync(0xffffffffu, hz, src, G);
+        }
+        // FP64 per point: other atoms take D, the owning atom minus their sum
+        const bool other = act && live && B != a;
+        double ox = other ? (double)Dx : 0.0, oy = other ? (double)Dy : 0.0, oz = other ? (double)Dz : 0.0;
+        double sx = ox, sy = oy, sz = oz;
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
+            sx += __shfl_xor_sync(0xffffffffu, sx, o, G);
+            sy += __shfl_xor_sync(0xffffffffu, sy, o, G);
+            sz += __shfl_xor_sync(0xffffffffu, sz, o, G);
+        }
+        if (other) { accx += ox; accy += oy; accz += oz; }
+        else if (act && live) { accx -= sx; accy -= sy; accz -= sz; }
+    }
+    s_acc[warp][lane][0] = accx;
+    s_acc[warp][lane][1] = accy;
+    s_acc[warp][lane][2] = accz;
+    __syncthreads();
+    for (int e = threadIdx.x; e < natoms * 3; e += kBwBlock) {
+        const int at = e / 3, d = e % 3;
+        double s = 0.0;
+        for (int w = 0; w < 4; ++w)
+            for (int g = 0; g < NG; ++g) s += s_acc[w][g * G + at][d];
+        part[(size_t)blockIdx.x * natoms * 3 + e] = s;
+    }
+}
+
+template <typename T>
+static void launch_becke_w(dftg_ctx *c, int G, const T *iR, const T *eb, const double *ewb, double *fp)
+{
+    const int na = c->natoms, per_atom = c->nrad * c->nang;
+    if (G == 8)
+        k_bw_becke_w<T, 8><<<c->bw_nb_becke, kBwBlock, 0, c->stream>>>(c->npts, per_atom, na, c->d_atoms, iR, eb,
+                                                                       c->d_x, c->d_y, c->d_z, ewb, fp);
+    else if (G == 16)
+        k_bw_becke_w<T, 16><<<c->bw_nb_becke, kBwBlock, 0, c->stream>>>(c->npts, per_atom, na, c->d_atoms, iR, eb,
+                                                                        c->d_x, c->d_y, c->d_z, ewb, fp);
+    else
+        k_bw_becke_w<T, 32><<<c->bw_nb_becke, kBwBlock, 0, c->stream>>>(c->npts, per_atom, na, c->d_atoms, iR, eb,
+                                                                        c->d_x, c->d_y, c->d_z, ewb, fp);
+}
+
+// Transposed cross-atom evaluation from the FP32 pair geometry and the integer
+// Y_lm recursion of the mixed forward: part[task][lm][n] = fold_lm sum_pairs
+// u_p / r R_lm(dir) t^n, FP32 sums over 128 pairs, FP64 across them.
+__global__ void __launch_bounds__(kBwBlock) k_bw_cross_T32(int nlm, int lmax, const int4 *__restrict__ tasks,
+                                                           const float4 *__restrict__ pgeo,
+                                                           const float2 *__restrict__ ptk,
+                                                           const int *__restrict__ pairp, const double *__restrict__ u,
+                                                           const double *__restrict__ fold, double *__restrict__ part)
+{
+    constexpr int LDB = kBwBlock + 1;
+    extern __shared__ float s_bf[];              // [nlm][LDB] then [4][128]
+    float *s_t = s_bf + (size_t)nlm * LDB;
+    const int4 tk = tasks[blockIdx.x];
+    double acc[2][4] = {{0.0, 0.0, 0.0, 0.0}, {0.0, 0.0, 0.0, 0.0}};
+    for (int q0 = 0; q0 < tk.y; q0 += kBwBlock) {
+        const int q = q0 + threadIdx.x;
+        float *b = s_bf + threadIdx.x;
+        if (q < tk.y) {
+            const float4 g = pgeo[(size_t)tk.x + q];
+            const float t = ptk[(size_t)tk.x + q].x;
+            const float s0 = (float)u[pairp[tk.x + q]] * g.w;
+            s_t[threadIdx.x] = s0;
+            s_t[kBwBlock + threadIdx.x] = s0 * t;
+            s_t[2 * kBwBlock + threadIdx.x] = s0 * t * t;
+            s_t[3 * kBwBlock + threadIdx.x] = s0 * t * t * t;
+            float cm = 1.f, sm = 0.f;
+            for (int m = 0; m <= lmax; ++m) {
+                float r1 = 1.f, r2 = 0.f;
+                for (int l = m; l <= lmax; ++l) {
+                    float qv = 1.f;
+                    if (l != m) {
+                        qv = (float)(2 * l - 1) * g.z * r1 - (float)((l + m - 1) * (l - m - 1)) * r2;
+                        r2 = r1;
+                        r1 = qv;
+                    }
+                    if (m == 0) b[(size_t)(l * l + l) * LDB] = qv;
+                    else {
+                        b[(size_t)(l * l + l + m) * LDB] = qv * cm;
+                        b[(size_t)(l * l + l - m) * LDB] = qv * sm;
+                    }
+                }
+                const float cn = cm * g.x - sm * g.y, sn = cm * g.y + sm * g.x;
+                cm = cn;
+                sm = sn;
+            }
+        } else {
+            for (int n = 0; n < 4; ++n) s_t[n * kBwBlock + threadIdx.x] = 0.f;
+            for (int lm = 0; lm < nlm; ++lm) b[(size_t)lm * LDB] = 0.f;
+        }
+        __syncthreads();
+        for (int s = 0; s < 2; ++s) {
+            const int lm = threadIdx.x + s * kBwBlock;
+            if (lm >= nlm) break;
+            const float *bl = s_bf + (size_t)lm * LDB;
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll 4
+            for (int j = 0; j < kBwBlock; ++j) {
+                const float bv = bl[j];
+                a0 = fmaf(bv, s_t[j], a0);
+                a1 = fmaf(bv, s_t[kBwBlock + j], a1);
+                a2 = fmaf(bv, s_t[2 * kBwBlock + j], a2);
+                a3 = fmaf(bv, s_t[3 * kBwBlock + j], a3);
+            }
+            acc[s][0] += a0;
+            acc[s][1] += a1;
+            acc[s][2] += a2;
+            acc[s][3] += a3;
+        }
+        __syncthreads();
+    }
+    for (int s = 0; s < 2; ++s) {
+        const int lm = threadIdx.x + s * kBwBlock;
+        if (lm >= nlm) break;
+        double *o = part + ((size_t)blockIdx.x * nlm + lm) * 4;
+        const double f = fold[lm];
+        for (int n = 0; n < 4; ++n) o[n] = f * acc[s][n];
+    }
+}
+
+// Cross-atom geometry term in FP32 over the pair bins (grid-stride over tasks):
+// per pair (u_p / 2) grad f_k with the folded spline coefficients (high halves,
+// plus the low halves for l = 0) and the integer Y_lm recursion; the bin's atom
+// k takes minus the task's sum, the pairs' own atoms (runs of equal atom, the
+// pairs of a bin are in point order) take the pair vectors.
+__global__ void __launch_bounds__(kBwBlock) k_bw_force_cross32(int ntasks, int nlm, int lmax, int nrad, int natoms,
+                                                               int per_atom, const int4 *__restrict__ tasks,
+                                                               const float4 *__restrict__ pgeo,
+                                                               const float2 *__restrict__ ptk,
+                                                               const int *__restrict__ pairp,
+                                                               const double *__restrict__ u,
+                                                               const float *__restrict__ splm, double *__restrict__ part)
+{
+    extern __shared__ double s_x[];               // [4][natoms][3] doubles, then [nlm][2] float4 coefficients
+    double *s_acc = s_x;
+    float4 *s_cf = reinterpret_cast<float4 *>(s_x + 4 * (size_t)natoms * 3);
+    __shared__ double s_k[4][3];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *acc = s_acc + (size_t)warp * natoms * 3;
+    for (int e = threadIdx.x; e < 4 * natoms * 3; e += kBwBlock) s_acc[e] = 0.0;
+    for (int task = blockIdx.x; task < ntasks; task += gridDim.x) {
+        const int4 tk = tasks[task];
+        __syncthreads();
+        for (int i = threadIdx.x; i < 2 * nlm; i += kBwBlock) {
+            const int lm = i >> 1;
+            s_cf[i] = reinterpret_cast<const float4 *>(splm + (((size_t)tk.z * nlm + lm) * nrad + tk.w) * 8)[i & 1];
+        }
+        __syncthreads();
+        double kx = 0.0, ky = 0.0, kz = 0.0;
+        for (int q0 = 0; q0 < tk.y; q0 += kBwBlock) {
+            const int q = q0 + threadIdx.x;
+            double v[3] = {0.0, 0.0, 0.0};
+            int key = 0;
+            if (q < tk.y) {
+                const float4 g = pgeo[(size_t)tk.x + q];
+                const float t = ptk[(size_t)tk.x + q].x;
+                const int p = pairp[tk.x + q];
+                key = p / per_atom;
+                const bool clamp = (tk.w == 0 && t == 0.f);   // below the first knot: constant
+                const float ir = g.w, ir2 = ir * ir;
+                float A1h = 0.f, A1l = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+                float cm = 1.f, sm = 0.f, cm1 = 0.f, sm1 = 0.f;
+                for (int m = 0; m <= lmax; ++m) {
+                    float r1 = 1.f, r2 = 0.f, d1 = 0.f, d2 = 0.f;
+                    for (int l = m; l <= lmax; ++l) {
+                        float qv = 1.f, dq = 0.f;
+                        if (l != m) {
+                            const float fa = (float)(2 * l - 1), fb = (float)((l + m - 1) * (l - m - 1));
+                            qv = fa * g.z * r1 - fb * r2;
+                            dq = fa * (r1 + g.z * d1) - fb * d2;
+                            r2 = r1;
+                            r1 = qv;
+                            d2 = d1;
+                            d1 = dq;
+                        }
+                        const float4 ch = s_cf[2 * (l * l + l + m)];
+                        const float S = fmaf(t, fmaf(t, fmaf(t, ch.w, ch.z), ch.y), ch.x);
+                        const float Sp = clamp ? 0.f : fmaf(t, fmaf(3.f * t, ch.w, 2.f * ch.z), ch.y);
+                        if (m == 0) {
+                            A1h = fmaf(qv, Sp * ir - S * ir2, A1h);
+                            gz = fmaf(S, dq, gz);
+                            if (l == 0) {
+                                const float4 cl = s_cf[1];
+                                const float Sl = fmaf(t, fmaf(t, fmaf(t, cl.w, cl.z), cl.y), cl.x);
+                                const float Spl = clamp ? 0.f : fmaf(t, fmaf(3.f * t, cl.w, 2.f * cl.z), cl.y);
+                                A1l = fmaf(qv, Spl * ir - Sl * ir2, A1l);
+                            }
+                        } else {
+                            const float4 dh = s_cf[2 * (l * l + l - m)];
+                            const float Sn = fmaf(t, fmaf(t, fmaf(t, dh.w, dh.z), dh.y), dh.x);
+                            const float Spn = clamp ? 0.f : fmaf(t, fmaf(3.f * t, dh.w, 2.f * dh.z), dh.y);
+                            const float fm = (float)m;
+                            A1h = fmaf(qv * cm, Sp * ir - S * ir2, A1h);
+                            A1h = fmaf(qv * sm, Spn * ir - Sn * ir2, A1h);
+                            gx = fmaf(qv * fm, S * cm1 + Sn * sm1, gx);
+                            gy = fmaf(qv * fm, Sn * cm1 - S * sm1, gy);
+                            gz = fmaf(dq, S * cm + Sn * sm, gz);
+                        }
+                    }
+                    cm1 = cm;
+                    sm1 = sm;
+                    const float cn = cm * g.x - sm * g.y, sn = cm * g.y + sm * g.x;
+                    cm = cn;
+                    sm = sn;
+                }
+                const float A1 = A1h + A1l;
+                const float ug = g.x * gx + g.y * gy + g.z * gz;
+                const float c = 0.5f * (float)u[p];
+                v[0] = (double)(c * (A1 * g.x + ir2 * (gx - ug * g.x)));
+                v[1] = (double)(c * (A1 * g.y + ir2 * (gy - ug * g.y)));
+                v[2] = (double)(c * (A1 * g.z + ir2 * (gz - ug * g.z)));
+            }
+            kx += v[0];
+            ky += v[1];
+            kz += v[2];
+            warp_add_by_key(key, v, acc);
+        }
+        kx = warp_sum_d(kx);
+        ky = warp_sum_d(ky);
+        kz = warp_sum_d(kz);
+        if (lane == 0) {
+            s_k[warp][0] = kx;
+            s_k[warp][1] = ky;
+            s_k[warp][2] = kz;
+        }
+        __syncthreads();
+        if (threadIdx.x < 3)
+            s_acc[3 * tk.z + threadIdx.x] -= ((s_k[0][threadIdx.x] + s_k[1][threadIdx.x]) + s_k[2][threadIdx.x]) +
+                                             s_k[3][threadIdx.x];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < natoms * 3; e += kBwBlock)
+        part[(size_t)blockIdx.x * natoms * 3 + e] =
+            ((s_acc[e] + s_acc[natoms * 3 + e]) + s_acc[2 * natoms * 3 + e]) + s_acc[3 * natoms * 3 + e];
+}
+
+// Amplitude term in FP32 (one thread per point, FP32 phi and P in shared
+// memory, (P phi)_mu formed four functions at a time from a broadcast row of
+// P); per-atom vectors leave each point in FP64.
+__global__ void __launch_bounds__(kBwBlock) k_bw_force_phi32(int nbf, int natoms, size_t npts, size_t npad,
+                                                             int per_atom, const float *__restrict__ phi32,
+                                                             const double *__restrict__ P, const double *__restrict__ h,
+                                                             const double *__restrict__ X,
+                                                             const double *__restrict__ Yc,
+                                                             const double *__restrict__ Zc,
+                                                             const double *__restrict__ atoms,
+                                                             const int *__restrict__ bf_lmn,
+                                                             const int *__restrict__ bf_off,
+                                                             const int *__restrict__ bf_atom,
+                                                             const double *__restrict__ pa,
+                                                             const double *__restrict__ pcn, double *__restrict__ part)
+{
+    extern __shared__ double s_dd[];   // [4][natoms][3] doubles, [nbf][128] phi, [nbf][nbf4] P floats
+    const int nbf4 = (nbf + 3) & ~3;
+    double *s_acc = s_dd;
+    float *s_phi = reinterpret_cast<float *>(s_dd + 4 * (size_t)natoms * 3);
+    float *s_P = s_phi + (size_t)nbf * kBwBlock;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t p = (size_t)blockIdx.x * kBwBlock + threadIdx.x;
+    for (int nu = 0; nu < nbf; ++nu) s_phi[(size_t)nu * kBwBlock + threadIdx.x] = phi32[(size_t)nu * npad + p];
+    // s_P[nu][mu] = P(mu, nu) (P is symmetric; column-major element (mu, nu) at mu + nu nbf)
+    for (int e = threadIdx.x; e < nbf * nbf4; e += kBwBlock) {
+        const int nu = e / nbf4, mu = e % nbf4;
+        s_P[e] = mu < nbf ? (float)P[(size_t)nu * nbf + mu] : 0.f;
+    }
+    for (int e = threadIdx.x; e < 4 * natoms * 3; e += kBwBlock) s_acc[e] = 0.0;
+    __syncthreads();
+    const bool valid = p < npts;
+    const int ap = valid ? (int)(p / per_atom) : 0;
+    const float G = valid ? (float)(4.0 * h[p]) : 0.f;
+    const double px = X[p], py = Yc[p], pz = Zc[p];
+    double *acc = s_acc + (size_t)warp * natoms * 3;
+    double self[3] = {0.0, 0.0, 0.0};
+    float vb[3] = {0.f, 0.f, 0.f};
+    int cur = bf_atom[0];
+    float cx = 0.f, cy = 0.f, cz = 0.f;   // p - R_cur
+    auto set_centre = [&](int b) {
+        cx = (float)(px - atoms[4 * b]);
+        cy = (float)(py - atoms[4 * b + 1]);
+        cz = (float)(pz - atoms[4 * b + 2]);
+    };
+    auto flush = [&](int b) {
+        const bool use = valid && b != ap;
+        double c[3];
+        for (int d = 0; d < 3; ++d) {
+            c[d] = use ? (double)(G * vb[d]) : 0.0;
+            self[d] += c[d];
+        }
+        for (int d = 0; d < 3; ++d) {
+            const double s = warp_sum_d(c[d]);
+            if (lane == 0) acc[3 * b + d] -= s;
+        }
+    };
+    set_centre(cur);
+    for (int mu0 = 0; mu0 < nbf; mu0 += 4) {
+        float t[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int nu = 0; nu < nbf; ++nu) {
+            const float f = s_phi[(size_t)nu * kBwBlock + threadIdx.x];
+            const float4 pv = *reinterpret_cast<const float4 *>(s_P + (size_t)nu * nbf4 + mu0);
+            t[0] = fmaf(pv.x, f, t[0]);
+            t[1] = fmaf(pv.y, f, t[1]);
+            t[2] = fmaf(pv.z, f, t[2]);
+            t[3] = fmaf(pv.w, f, t[3]);
+        }
+        for (int j = 0; j < 4; ++j) {
+            const int mu = mu0 + j;
+            if (mu >= nbf) break;
+            const int b = bf_atom[mu];
+            if (b != cur) {
+                flush(cur);
+                cur = b;
+                set_centre(b);
+                vb[0] = vb[1] = vb[2] = 0.f;
+            }
+            const float r2 = cx * cx + cy * cy + cz * cz;
+            const int lx = bf_lmn[3 * mu], ly = bf_lmn[3 * mu + 1], lz = bf_lmn[3 * mu + 2];
+            float s0 = 0.f, s1 = 0.f;
+            for (int k = bf_off[mu]; k < bf_off[mu + 1]; ++k) {
+                const float al = (float)pa[k];
+                const float ek = (float)pcn[k] * expf(-al * r2);
+                s0 += ek;
+                s1 = fmaf(al, ek, s1);
+            }
+            float x0 = 1.f, y0 = 1.f, z0 = 1.f, xm = 0.f, ym = 0.f, zm = 0.f;
+            for (int q = 0; q < lx; ++q) { xm = (q == lx - 1) ? (float)lx * x0 : xm; x0 *= cx; }
+            for (int q = 0; q < ly; ++q) { ym = (q == ly - 1) ? (float)ly * y0 : ym; y0 *= cy; }
+            for (int q = 0; q < lz; ++q) { zm = (q == lz - 1) ? (float)lz * z0 : zm; z0 *= cz; }
+            vb[0] = fmaf(t[j], y0 * z0 * (xm * s0 - 2.f * cx * x0 * s1), vb[0]);
+            vb[1] = fmaf(t[j], x0 * z0 * (ym * s0 - 2.f * cy * y0 * s1), vb[1]);
+            vb[2] = fmaf(t[j], x0 * y0 * (zm * s0 - 2.f * cz * z0 * s1), vb[2]);
+        }
+    }
+    flush(cur);
+    warp_add_by_key(ap, self, acc);
+    __syncthreads();
+    for (int e = threadIdx.x; e < natoms * 3; e += kBwBlock)
+        part[(size_t)blockIdx.x * natoms * 3 + e] =
+            ((s_acc[e] + s_acc[natoms * 3 + e]) + s_acc[2 * natoms * 3 + e]) + s_acc[3 * natoms * 3 + e];
 }
 
 // ---------------------------------------------------------------- host side
@@ -691,11 +1158,34 @@ static int bw_alloc(dftg_ctx *c)
     const int N = c->nrad, nlm = c->nlm, na = c->natoms;
     const size_t rplane = (size_t)na * nlm * N;
     c->bw_nb_phi = (int)(c->npad / kBwBlock);
-    c->bw_nb_becke = 152 * 4;
+    c->bw_nb_becke = 152 * 8;
     c->bw_nb_cross = (int)(c->npad / kBwBlock);
-    const size_t rows = (size_t)c->bw_nb_phi + c->bw_nb_becke + c->bw_nb_cross;
+    c->bw_nb_cross32 = std::max(1, std::min(c->ncross_tasks, 152 * 8));
+    const size_t rows = (size_t)c->bw_nb_phi + c->bw_nb_becke + std::max(c->bw_nb_cross, c->bw_nb_cross32);
     const size_t nred = (c->npad + kBwRed - 1) / kBwRed;
-    DFTG_CUDA(cudaMalloc(&c->d_bw_pt, sizeof(double) * 7 * c->npad));
+    DFTG_CUDA(cudaMalloc(&c->d_bw_pt, sizeof(double) * 7 * c->npad + sizeof(float) * c->npad));
+    {   // 1 / R_Bk, then the unit vectors (R_B - R_k) / R_Bk as [na * na][4], in FP32 and FP64
+        const size_t nR = ((size_t)na * na + 3) / 4 * 4;
+        std::vector<double> g64(nR + 4 * (size_t)na * na, 0.0);
+        for (int B = 0; B < na; ++B)
+            for (int k = 0; k < na; ++k) {
+                if (B == k) continue;
+                const double dx = c->xyz[3 * B] - c->xyz[3 * k], dy = c->xyz[3 * B + 1] - c->xyz[3 * k + 1],
+                             dz = c->xyz[3 * B + 2] - c->xyz[3 * k + 2];
+                const double R = std::sqrt(dx * dx + dy * dy + dz * dz);
+                g64[(size_t)B * na + k] = 1.0 / R;
+                double *e = g64.data() + nR + 4 * ((size_t)B * na + k);
+                e[0] = dx / R;
+                e[1] = dy / R;
+                e[2] = dz / R;
+            }
+        std::vector<float> g32(g64.begin(), g64.end());
+        DFTG_CUDA(cudaMalloc(&c->d_bw_geo, sizeof(float) * g32.size()));
+        DFTG_CUDA(cudaMemcpy(c->d_bw_geo, g32.data(), sizeof(float) * g32.size(), cudaMemcpyHostToDevice));
+        DFTG_CUDA(cudaMalloc(&c->d_bw_geo64, sizeof(double) * g64.size()));
+        DFTG_CUDA(cudaMemcpy(c->d_bw_geo64, g64.data(), sizeof(double) * g64.size(), cudaMemcpyHostToDevice));
+        c->bw_geo_off = (int)nR;
+    }
     DFTG_CUDA(cudaMalloc(&c->d_bw_lm, sizeof(double) * (2 * rplane + na + 8 + nred)));
     DFTG_CUDA(cudaMalloc(&c->d_bw_fpart, sizeof(double) * rows * na * 3));
     if (!c->d_bw_out) DFTG_CUDA(cudaMalloc(&c->d_bw_out, sizeof(double) * ((size_t)c->nbf * c->nbf + (size_t)na * 3)));
@@ -736,20 +1226,35 @@ int launch_backward(dftg_ctx *c, double sxc, double sj, double *dEdP_dev, double
     const size_t np = c->npad;
     double *u = c->d_bw_pt, *mbar = u + np, *g = mbar + np, *e = g + np, *h = e + np, *h2 = h + np, *ewb = h2 + np;
     double *Ubar = c->d_bw_lm, *rbar = Ubar + rplane, *qbar = rbar + rplane, *bws = qbar + na, *red = bws + 8;
-    // FP64 multipoles and splines of the last density (the same maps as the FP64 build)
-    DFTG_TRY_L(launch_multipoles_fp64(c));
-    DFTG_MARK(c, "bw_multipoles");
+    // the steps run in the precision of the build that produced the state: its
+    // spline tables are current (FP64 ones whenever its cross-atom step was FP64)
+    const unsigned mask = c->fwd_mask;
     const unsigned nb128 = (unsigned)(np / kBwBlock);
+    const bool mx_cross = (mask & kPrecCross) != 0;
+    const bool mx_phi = (mask & kPrecDensity) != 0;
+    const bool mx_becke = (mask & kPrecLda) != 0;
+    const bool mx_contract = (mask & kPrecContract) != 0;
+    float *h2f = reinterpret_cast<float *>(c->d_bw_pt + 7 * np);
+    const int4 *tasks = reinterpret_cast<const int4 *>(c->d_cross_tasks);
+    const float4 *pgeo = reinterpret_cast<const float4 *>(c->d_pairs);
+    const float2 *ptk = reinterpret_cast<const float2 *>(static_cast<const char *>(c->d_pairs) + sizeof(float4) * c->npairs);
     k_bw_seed<<<nb128, kBwBlock, 0, c->stream>>>(c->npts, np, c->d_rho, c->d_w, c->d_scal, sj, u);
     DFTG_LAUNCH_CHECK();
     k_bw_own_T<<<na * N, 96, sizeof(double) * nang, c->stream>>>(N, nang, nlm, u, c->d_invr, c->d_Y, Ubar);
     DFTG_LAUNCH_CHECK();
     if (c->npairs > 0) {
-        const size_t sm = sizeof(double) * ((size_t)nlm * (kBwBlock + 1) + 4 * kBwBlock);
-        if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_bw_cross_T), c->device));
-        k_bw_cross_T<<<c->ncross_tasks, kBwBlock, sm, c->stream>>>(
-            nlm, c->lmax, N, reinterpret_cast<const int4 *>(c->d_cross_tasks), c->d_bw_pairp, c->d_atoms, c->d_x,
-            c->d_y, c->d_z, u, c->d_sx, c->d_pre, c->d_rec, c->d_bw_cpart);
+        if (mx_cross) {
+            const size_t sm = sizeof(float) * ((size_t)nlm * (kBwBlock + 1) + 4 * kBwBlock);
+            if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_bw_cross_T32), c->device));
+            k_bw_cross_T32<<<c->ncross_tasks, kBwBlock, sm, c->stream>>>(nlm, c->lmax, tasks, pgeo, ptk, c->d_bw_pairp,
+                                                                          u, c->d_fold, c->d_bw_cpart);
+        } else {
+            const size_t sm = sizeof(double) * ((size_t)nlm * (kBwBlock + 1) + 4 * kBwBlock);
+            if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_bw_cross_T), c->device));
+            k_bw_cross_T<<<c->ncross_tasks, kBwBlock, sm, c->stream>>>(nlm, c->lmax, N, tasks, c->d_bw_pairp,
+                                                                        c->d_atoms, c->d_x, c->d_y, c->d_z, u, c->d_sx,
+                                                                        c->d_pre, c->d_rec, c->d_bw_cpart);
+        }
         DFTG_LAUNCH_CHECK();
         k_bw_spline_T<<<na * nlm, 128, sizeof(double) * 6 * N, c->stream>>>(N, nlm, c->d_bw_binfirst, c->d_bw_cpart,
                                                                             c->d_splf, c->d_Kt, Ubar);
@@ -759,48 +1264,100 @@ int launch_backward(dftg_ctx *c, double sxc, double sj, double *dEdP_dev, double
     k_bw_poisson_T<<<na * nlm, 128, sizeof(double) * N, c->stream>>>(N, c->lmax, c->d_Gt, c->d_Gb, Ubar, rbar, qbar);
     DFTG_LAUNCH_CHECK();
     const unsigned nbr = (unsigned)((np + kBwRed - 1) / kBwRed);
-    k_bw_points<<<nbr, kBwRed, 0, c->stream>>>(c->npts, np, N, nang, nlm, c->d_rho, c->d_w, c->d_wb, c->d_Yw, rbar,
-                                               qbar, c->d_scal, sxc, mbar, g, e, red, bws, c->d_bw_counter);
+    if (mask & kPrecLda)
+        k_bw_points<true><<<nbr, kBwRed, 0, c->stream>>>(c->npts, np, N, nang, nlm, c->d_rho, c->d_w, c->d_wb, c->d_Yw,
+                                                         rbar, qbar, c->d_scal, sxc, mbar, g, e, red, bws,
+                                                         c->d_bw_counter);
+    else
+        k_bw_points<false><<<nbr, kBwRed, 0, c->stream>>>(c->npts, np, N, nang, nlm, c->d_rho, c->d_w, c->d_wb, c->d_Yw,
+                                                          rbar, qbar, c->d_scal, sxc, mbar, g, e, red, bws,
+                                                          c->d_bw_counter);
     DFTG_LAUNCH_CHECK();
     k_bw_coef<<<nb128, kBwBlock, 0, c->stream>>>(c->npts, np, N, nang, c->d_rn, c->d_wrad, c->d_leb, c->d_rho, c->d_w,
-                                                 c->d_V, g, e, mbar, qbar, c->d_scal, bws, sxc, sj, h, h2, ewb);
+                                                 c->d_V, g, e, mbar, qbar, c->d_scal, bws, sxc, sj, h, h2, h2f, ewb);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "bw_points");
     if (dEdP_dev) {
-        DFTG_TRY_L(launch_contract_coef(c, h2, dEdP_dev));
+        if (mx_contract && c->ct_ready) {
+            DFTG_TRY_L(launch_contract_tc_on(c, h2f, h2f));
+            DFTG_TRY_L(launch_contract_tc_reduce_to(c, true, false, dEdP_dev, nullptr));
+        } else if (mx_contract) {
+            DFTG_TRY_L(launch_contract_coef32(c, h2f, dEdP_dev));
+        } else {
+            DFTG_TRY_L(launch_contract_coef(c, h2, dEdP_dev));
+        }
         DFTG_MARK(c, "bw_dEdP");
     }
     if (dEdR_dev) {
         double *fp = c->d_bw_fpart;
-        const size_t smp = sizeof(double) * ((size_t)c->nbf * kBwBlock + 4 * (size_t)na * 3);
-        if (smp > 227 * 1024) {
-            set_error("backward: nbf %d too large for the amplitude-gradient kernel", c->nbf);
-            return DFTG_ERR_ARG;
+        int rows = 0;
+        if (mx_phi) {
+            const size_t smp = sizeof(double) * 4 * (size_t)na * 3 +
+                               sizeof(float) * ((size_t)c->nbf * kBwBlock + (size_t)c->nbf * ((c->nbf + 3) & ~3));
+            if (smp > 227 * 1024) {
+                set_error("backward: nbf %d too large for the amplitude-gradient kernel", c->nbf);
+                return DFTG_ERR_ARG;
+            }
+            if (smp > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_bw_force_phi32), c->device));
+            k_bw_force_phi32<<<c->bw_nb_phi, kBwBlock, smp, c->stream>>>(c->nbf, na, c->npts, np, per_atom, c->d_phi32,
+                                                                         c->d_P, h, c->d_x, c->d_y, c->d_z, c->d_atoms,
+                                                                         c->d_bf_lmn, c->d_bf_off, c->d_bf_atom,
+                                                                         c->d_pa, c->d_pcn, fp);
+        } else {
+            const size_t smp = sizeof(double) * ((size_t)c->nbf * kBwBlock + 4 * (size_t)na * 3);
+            if (smp > 227 * 1024) {
+                set_error("backward: nbf %d too large for the amplitude-gradient kernel", c->nbf);
+                return DFTG_ERR_ARG;
+            }
+            if (smp > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_bw_force_phi), c->device));
+            k_bw_force_phi<<<c->bw_nb_phi, kBwBlock, smp, c->stream>>>(c->nbf, na, c->npts, np, per_atom, c->d_phi,
+                                                                       c->d_P, h, c->d_x, c->d_y, c->d_z, c->d_atoms,
+                                                                       c->d_bf_lmn, c->d_bf_off, c->d_bf_atom, c->d_pa,
+                                                                       c->d_pcn, fp);
         }
-        if (smp > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_bw_force_phi), c->device));
-        k_bw_force_phi<<<c->bw_nb_phi, kBwBlock, smp, c->stream>>>(c->nbf, na, c->npts, np, per_atom, c->d_phi,
-                                                                   c->d_P, h, c->d_x, c->d_y, c->d_z, c->d_atoms,
-                                                                   c->d_bf_lmn, c->d_bf_off, c->d_bf_atom, c->d_pa,
-                                                                   c->d_pcn, fp);
         DFTG_LAUNCH_CHECK();
         DFTG_MARK(c, "bw_force_phi");
         fp += (size_t)c->bw_nb_phi * na * 3;
-        const size_t smb = sizeof(double) * 4 * (size_t)na * 5;
-        if (smb > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_bw_force_becke), c->device));
-        k_bw_force_becke<<<c->bw_nb_becke, kBwBlock, smb, c->stream>>>(c->npts, per_atom, na, c->d_atoms, c->d_rab,
-                                                                       c->d_x, c->d_y, c->d_z, ewb, fp);
+        rows += c->bw_nb_phi;
+        if (na <= 32) {
+            const int G = na <= 8 ? 8 : (na <= 16 ? 16 : 32);
+            if (mx_becke) {
+                const float *iR = reinterpret_cast<const float *>(c->d_bw_geo);
+                launch_becke_w<float>(c, G, iR, iR + c->bw_geo_off, ewb, fp);
+            } else {
+                const double *iR = c->d_bw_geo64;
+                launch_becke_w<double>(c, G, iR, iR + c->bw_geo_off, ewb, fp);
+            }
+        } else {
+            const size_t smb = sizeof(double) * 4 * (size_t)na * 5;
+            if (smb > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_bw_force_becke), c->device));
+            k_bw_force_becke<<<c->bw_nb_becke, kBwBlock, smb, c->stream>>>(c->npts, per_atom, na, c->d_atoms, c->d_rab,
+                                                                           c->d_x, c->d_y, c->d_z, ewb, fp);
+        }
         DFTG_LAUNCH_CHECK();
         DFTG_MARK(c, "bw_force_becke");
         fp += (size_t)c->bw_nb_becke * na * 3;
-        const size_t smc = sizeof(double) * 4 * (size_t)na * 3;
-        if (smc > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_bw_force_cross), c->device));
-        k_bw_force_cross<<<c->bw_nb_cross, kBwBlock, smc, c->stream>>>(c->npts, na, N, per_atom, c->lmax, c->d_atoms,
-                                                                       c->d_x, c->d_y, c->d_z, u, c->d_sx, c->d_spl,
-                                                                       c->d_pre, c->d_rec, fp);
-        DFTG_LAUNCH_CHECK();
+        rows += c->bw_nb_becke;
+        if (mx_cross) {
+            if (c->npairs > 0) {
+                const size_t smc = sizeof(double) * 4 * (size_t)na * 3 + sizeof(float4) * 2 * (size_t)nlm;
+                if (smc > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_bw_force_cross32), c->device));
+                k_bw_force_cross32<<<c->bw_nb_cross32, kBwBlock, smc, c->stream>>>(
+                    c->ncross_tasks, nlm, c->lmax, N, na, per_atom, tasks, pgeo, ptk, c->d_bw_pairp, u, c->d_splm, fp);
+                DFTG_LAUNCH_CHECK();
+                rows += c->bw_nb_cross32;
+            }
+        } else {
+            const size_t smc = sizeof(double) * 4 * (size_t)na * 3;
+            if (smc > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_bw_force_cross), c->device));
+            k_bw_force_cross<<<c->bw_nb_cross, kBwBlock, smc, c->stream>>>(c->npts, na, N, per_atom, c->lmax, c->d_atoms,
+                                                                           c->d_x, c->d_y, c->d_z, u, c->d_sx, c->d_spl,
+                                                                           c->d_pre, c->d_rec, fp);
+            DFTG_LAUNCH_CHECK();
+            rows += c->bw_nb_cross;
+        }
         DFTG_MARK(c, "bw_force_cross");
-        const int rows = c->bw_nb_phi + c->bw_nb_becke + c->bw_nb_cross;
-        k_bw_force_sum<<<(unsigned)((na * 3 + 127) / 128), 128, 0, c->stream>>>(na, rows, c->d_bw_fpart, dEdR_dev);
+        k_bw_force_sum<<<(unsigned)(na * 3), 256, 0, c->stream>>>(na, rows, c->d_bw_fpart, dEdR_dev);
         DFTG_LAUNCH_CHECK();
     }
     return DFTG_OK;

@@ -7,8 +7,9 @@
 // CTA (tile, chunk) accumulates its chunk in registers (R x R outputs of each
 // matrix per thread) and stores an FP64 partial; a second kernel sums the
 // partials of each element in chunk order (deterministic FP64 reduction).
-// T = double for the FP64 path, float for the mixed path (FP32 products and
-// in-chunk accumulation, FP64 across chunks).
+// T = double for the FP64 path, float for the mixed path (FP32 products, FP32
+// sums per 32-point stage carried across stages as TwoSum pairs, FP64 across
+// chunks).
 #include <vector>
 #include "dftg_internal.cuh"
 
@@ -33,13 +34,25 @@ __global__ void __launch_bounds__(256) k_contract(int nbf, int pts_per_chunk, si
     const size_t pb = (size_t)chunk * pts_per_chunk;
     const size_t pe = min(npad, pb + (size_t)pts_per_chunk);
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    constexpr bool kF32 = sizeof(T) == 4;
     T ax[R][R], aj[R][R];
+    // FP32: per-stage sums carried across stages as compensated (TwoSum) pairs
+    float hx[R][R], lx[R][R], hj[R][R], lj[R][R];
 #pragma unroll
     for (int i = 0; i < R; ++i)
 #pragma unroll
-        for (int j = 0; j < R; ++j) { ax[i][j] = 0; aj[i][j] = 0; }
+        for (int j = 0; j < R; ++j) {
+            ax[i][j] = 0; aj[i][j] = 0;
+            hx[i][j] = 0.f; lx[i][j] = 0.f; hj[i][j] = 0.f; lj[i][j] = 0.f;
+        }
 
     for (size_t kb = pb; kb < pe; kb += kKB) {
+        if constexpr (kF32) {
+#pragma unroll
+            for (int i = 0; i < R; ++i)
+#pragma unroll
+                for (int j = 0; j < R; ++j) { ax[i][j] = 0; aj[i][j] = 0; }
+        }
         __syncthreads();
         for (int e = tid; e < TILE * kKB; e += 256) {
             const int row = e / kKB, k = e % kKB;
@@ -70,6 +83,15 @@ __global__ void __launch_bounds__(256) k_contract(int nbf, int pts_per_chunk, si
                 }
             }
         }
+        if constexpr (kF32) {
+#pragma unroll
+            for (int i = 0; i < R; ++i)
+#pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    two_sum_acc(hx[i][j], lx[i][j], (float)ax[i][j]);
+                    two_sum_acc(hj[i][j], lj[i][j], (float)aj[i][j]);
+                }
+        }
     }
     const size_t nn = (size_t)nbf * nbf;
     double *px = part + (size_t)chunk * 2 * nn, *pj = px + nn;
@@ -79,8 +101,13 @@ __global__ void __launch_bounds__(256) k_contract(int nbf, int pts_per_chunk, si
         for (int j = 0; j < R; ++j) {
             const int mu = m0 + ty + 16 * i, nu = n0 + tx + 16 * j;
             if (mu < nbf && nu < nbf) {
-                px[(size_t)mu * nbf + nu] = (double)ax[i][j];
-                pj[(size_t)mu * nbf + nu] = (double)aj[i][j];
+                if constexpr (kF32) {
+                    px[(size_t)mu * nbf + nu] = (double)hx[i][j] + (double)lx[i][j];
+                    pj[(size_t)mu * nbf + nu] = (double)hj[i][j] + (double)lj[i][j];
+                } else {
+                    px[(size_t)mu * nbf + nu] = (double)ax[i][j];
+                    pj[(size_t)mu * nbf + nu] = (double)aj[i][j];
+                }
             }
         }
 }
@@ -203,6 +230,24 @@ int launch_contract_coef(dftg_ctx *c, const double *coef, double *out)
     dim3 grid((unsigned)c->ntiles, (unsigned)c->nchunk);
     if (R == 5) k_contract<double, 5><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, coef, coef, 1, 0, d_tiles, c->d_part);
     else k_contract<double, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, coef, coef, 1, 0, d_tiles, c->d_part);
+    DFTG_LAUNCH_CHECK();
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, tile, c->nchunk, 1, 0, c->d_part,
+                                                                        out, nullptr);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+// the same in FP32 (products and in-chunk sums; FP64 across chunks) from the FP32 amplitudes
+int launch_contract_coef32(dftg_ctx *c, const float *coef, double *out)
+{
+    const int R = tile_R(c->nbf), tile = 16 * R;
+    const int2 *d_tiles = reinterpret_cast<const int2 *>(c->d_tiles);
+    size_t per = (c->npad + c->nchunk - 1) / c->nchunk;
+    per = (per + kKB - 1) / kKB * kKB;
+    dim3 grid((unsigned)c->ntiles, (unsigned)c->nchunk);
+    if (R == 5) k_contract<float, 5><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, coef, coef, 1, 0, d_tiles, c->d_part);
+    else k_contract<float, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, coef, coef, 1, 0, d_tiles, c->d_part);
     DFTG_LAUNCH_CHECK();
     const size_t nn = (size_t)c->nbf * c->nbf;
     k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, tile, c->nchunk, 1, 0, c->d_part,

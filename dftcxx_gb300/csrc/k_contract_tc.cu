@@ -669,29 +669,37 @@ int contract_tc_setup(dftg_ctx *c)
     return DFTG_OK;
 }
 
-int launch_contract_tc(dftg_ctx *c)
+// XC = phi^T diag(cxc) phi and J = phi^T diag(cj) phi partials on the tensor
+// cores for any pair of FP32 point-coefficient arrays
+int launch_contract_tc_on(dftg_ctx *c, const float *cxc32, const float *cj32)
 {
     int2 *cexp = reinterpret_cast<int2 *>(c->d_ct_rowexp + 2 * (size_t)c->ct_nchunk * c->nbf);
-    k_ct_cexp<<<c->ct_nchunk, 256, 0, c->stream>>>(c->ct_nkb, c->ct_kbpc, c->d_cxc32, c->d_cj32, c->d_ct_winv, cexp);
+    k_ct_cexp<<<c->ct_nchunk, 256, 0, c->stream>>>(c->ct_nkb, c->ct_kbpc, cxc32, cj32, c->d_ct_winv, cexp);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "contract_bounds");
     k_contract_tc<<<c->ct_grid, kCtThreads, ct_smem(c->ct_nst, c->ct_NP, c->ct_AR, c->nbf, c->ct_spart != 0), c->stream>>>(
         c->nbf, c->ct_AR, c->ct_NP, c->ct_nst, c->ct_spart, c->ct_nkb, c->ct_kbpc, c->ct_nchunk,
         reinterpret_cast<const unsigned char *>(c->d_ct_A), c->d_ct_rowexp,
-        c->d_ct_rowexp + (size_t)c->ct_nchunk * c->nbf, cexp, c->d_cxc32, c->d_cj32,
+        c->d_ct_rowexp + (size_t)c->ct_nchunk * c->nbf, cexp, cxc32, cj32,
         reinterpret_cast<float2 *>(c->d_part), c->d_flag);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+int launch_contract_tc(dftg_ctx *c) { return launch_contract_tc_on(c, c->d_cxc32, c->d_cj32); }
+
+int launch_contract_tc_reduce_to(dftg_ctx *c, bool want_xc, bool want_j, double *XC, double *J)
+{
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    k_contract_tc_reduce<<<(unsigned)((nn + 31) / 32), 1024, 0, c->stream>>>(
+        c->nbf, c->ct_grid, want_xc ? 1 : 0, want_j ? 1 : 0, reinterpret_cast<const float2 *>(c->d_part), XC, J);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }
 
 int launch_contract_tc_reduce(dftg_ctx *c, bool want_xc, bool want_j)
 {
-    const size_t nn = (size_t)c->nbf * c->nbf;
-    k_contract_tc_reduce<<<(unsigned)((nn + 31) / 32), 1024, 0, c->stream>>>(
-        c->nbf, c->ct_grid, want_xc ? 1 : 0, want_j ? 1 : 0, reinterpret_cast<const float2 *>(c->d_part), c->d_XC,
-        c->d_J);
-    DFTG_LAUNCH_CHECK();
-    return DFTG_OK;
+    return launch_contract_tc_reduce_to(c, want_xc, want_j, c->d_XC, c->d_J);
 }
 
 }  // namespace dftg

@@ -165,51 +165,6 @@ __global__ void k_scale(size_t npts, const double *__restrict__ scal, double *rh
 
 // ---------------------------------------------------------------- LDA
 
-// Mixed point kernel with the energy density as a double-float (no FP64 work):
-// the transcendental parts in FP32, every constant shared by all points and
-// every product that carries the energy in double-float (TwoProd), so no
-// rounding is common to all points.
-__device__ void lda_point_df(dfl rho, dfl &e, float &v)
-{
-    constexpr double FAC = -0.93052573634910019, K34PI = 0.238732414637843;
-    constexpr double A = 0.0310907, K1 = -0.031167608678943783, K2 = 1.2474243062431216;
-    constexpr float Af = 0.0310907f, X0f = -0.10498f, Bf = 3.72744f, Cf = 12.9352f, Qf = 6.1519908197590798f,
-                    Q2f = 37.846991046399992f, K1f = -0.031167608678943783f, VXf = -1.2407009817988002f;
-    const dfl FACd = {(float)FAC, (float)(FAC - (double)(float)FAC)};
-    const dfl Ad = {(float)A, (float)(A - (double)(float)A)};
-    const dfl K1d = {(float)K1, (float)(K1 - (double)(float)K1)};
-    const dfl K2d = {(float)K2, (float)(K2 - (double)(float)K2)};
-    constexpr float K34PIh = (float)K34PI, K34PIl = (float)(K34PI - (double)(float)K34PI);
-    const float rf = rho.h + rho.l;
-    const dfl da = {0.5f * rho.h, 0.5f * rho.l};             // exact
-    e = dfl{0.f, 0.f};
-    v = 0.f;
-    if (!(rf * 0.5f < 1e-10f)) {
-        const float r3 = cbrtf(da.h);
-        const dfl ex = df_mul(df_mul(FACd, da), dfl{2.f * r3, 0.f});   // 2 FAC da^(4/3)
-        e = ex;
-        v = VXf * r3;
-    }
-    if (!(rf < 1e-10f)) {
-        // x^6 = (3 / 4 pi) / rho in FP32 (no division in FP64): K split hi + lo
-        const float rinv = 1.f / rf;
-        const float x = sqrtf(cbrtf(fmaf(K34PIh, rinv, K34PIl * rinv)));
-        const float X = fmaf(x, x + Bf, Cf);
-        const float L1 = logf(x * x / X);
-        const float L2 = logf((x - X0f) * (x - X0f) / X);
-        const float tb = 2.f * x + Bf;
-        const float T = atanf(Qf / tb);
-        // eps = A (L1 - K1 L2 + K2 T), ec = eps rho
-        const dfl inner = df_add(df_sub(dfl{L1, 0.f}, df_mul(K1d, dfl{L2, 0.f})), df_mul(K2d, dfl{T, 0.f}));
-        const dfl eps = df_mul(Ad, inner);
-        e = df_add(e, df_mul(eps, rho));
-        const float den = tb * tb + Q2f;
-        const float deps = Af * (2.f / x - tb / X - 4.f * Bf / den -
-                                 K1f * (2.f / (x - X0f) - tb / X - 4.f * (2.f * X0f + Bf) / den));
-        v += (eps.h + eps.l) - (x / 6.f) * deps;
-    }
-}
-
 template <bool MIXED>
 __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restrict__ rho,
                                                    const double *__restrict__ w, double *__restrict__ scal,

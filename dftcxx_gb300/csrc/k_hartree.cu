@@ -918,10 +918,13 @@ int cross_pairs_setup(dftg_ctx *c)
     const size_t n = c->npts;
     const int na = c->natoms, N = c->nrad, per_atom = c->nrad * c->nang;
     if (na < 2) { c->npairs = 0; return DFTG_OK; }
+    // the grid kernel ran on the context's (non-blocking) stream: copy on that
+    // stream and wait for it
     std::vector<double> X(n), Y(n), Z(n);
-    DFTG_CUDA(cudaMemcpy(X.data(), c->d_x, sizeof(double) * n, cudaMemcpyDeviceToHost));
-    DFTG_CUDA(cudaMemcpy(Y.data(), c->d_y, sizeof(double) * n, cudaMemcpyDeviceToHost));
-    DFTG_CUDA(cudaMemcpy(Z.data(), c->d_z, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    DFTG_CUDA(cudaMemcpyAsync(X.data(), c->d_x, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    DFTG_CUDA(cudaMemcpyAsync(Y.data(), c->d_y, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    DFTG_CUDA(cudaMemcpyAsync(Z.data(), c->d_z, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
     std::vector<double> sx(N);
     for (int i = 0; i < N; ++i) sx[i] = c->r_n[N - 1 - i];
     // interval and offset of the spline evaluation at distance r, the same
@@ -1038,23 +1041,6 @@ static int launch_vcross_bins(dftg_ctx *c)
     case 11: vcross_bins_launch<11>(c); break;
     default: vcross_bins_launch<-1>(c); break;
     }
-    DFTG_LAUNCH_CHECK();
-    return DFTG_OK;
-}
-
-// FP64 rho_lm, U_lm and spline coefficients of the density on the device
-// (the multipole steps of the FP64 build), for the backward pass
-int launch_multipoles_fp64(dftg_ctx *c)
-{
-    const int N = c->nrad, nlm = c->nlm, na = c->natoms;
-    k_rholm<<<na * N, 96, sizeof(double) * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho, c->d_wb, c->d_Yw,
-                                                                 c->d_rholm);
-    DFTG_LAUNCH_CHECK();
-    k_poisson<<<na * nlm, 128, sizeof(double) * N, c->stream>>>(na, N, c->lmax, c->d_Gt, c->d_Gb, c->d_rholm,
-                                                               c->d_scal, c->d_U, c->d_U32);
-    DFTG_LAUNCH_CHECK();
-    k_splines<<<na * nlm, 128, sizeof(double) * 2 * N, c->stream>>>(na, N, nlm, c->d_splf, c->d_Kt, c->d_U,
-                                                                   c->d_fold, c->d_spl, c->d_splm);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }

@@ -129,6 +129,15 @@ class MolecularGrid:
         check(_lib.load().dftg_backward(self._h, float(seed_exc), float(seed_ej), _ptr(dP), _ptr(dR)))
         return np.ascontiguousarray(dP), dR
 
+    def backward_profile(self, seed_exc=1.0, seed_ej=1.0):
+        """Per-phase device times (ms) of one backward pass: {name: ms}."""
+        ms = (ctypes.c_double * 32)()
+        names = (ctypes.c_char_p * 32)()
+        n = ctypes.c_int()
+        check(_lib.load().dftg_backward_profile(self._h, float(seed_exc), float(seed_ej), ms, names, 32,
+                                                ctypes.byref(n)))
+        return {names[i].decode(): ms[i] for i in range(n.value)}
+
     def energies(self):
         """E_xc, E_J = 2 tr(P J) summed on the grid in FP64, integrated density
         of the last build."""

@@ -178,6 +178,11 @@ int dftg_nuclear_repulsion(const dftg_ctx *ctx, double *enuc);
 int dftg_backward(dftg_ctx *ctx, double seed_exc, double seed_ej, double *dEdP, double *dEdR);
 /* The same on device buffers, ordered on the context's stream, no synchronisation. */
 int dftg_backward_device(dftg_ctx *ctx, double seed_exc, double seed_ej, double *dEdP_dev, double *dEdR_dev);
+/* Diagnostic variant of dftg_backward (both outputs, kept on the device):
+ * per-phase durations in milliseconds with their names, as
+ * dftg_fock_build_profile. */
+int dftg_backward_profile(dftg_ctx *ctx, double seed_exc, double seed_ej, double *phase_ms, const char **names,
+                          int cap, int *nphase);
 
 /* Batched builds (no counterpart in the reference): many contexts -- molecules
  * or geometries of any size -- built in one launch.  The per-build kernel

@@ -131,3 +131,28 @@ def test_backward_ethane_mixed_within_force_bar(gpu_lib):
     em = max(abs(dRm[a, d] - fd[(a, d)]) for (a, d) in coords)
     assert e64 <= 2e-7, e64
     assert em <= 1e-5, em
+
+
+def test_backward_decane_mixed_and_fp64(gpu_lib):
+    """Decane / 6-31G / 50 x 194 (32 atoms, 134 functions) at the core-Hamiltonian
+    guess density: FP64 backward against central differences on two
+    coordinates (2e-7 Ha/bohr), the mixed forward + backward against the FP64
+    backward (1e-5 Ha/bohr, every coordinate) and the translation sum rule
+    (FP64 1e-8, mixed 1e-6)."""
+    from dftcxx_gb300.grid import DFT
+    Z, xyz = alkane(10)
+    mol = Molecule(Z, xyz, "p631")
+    nrad, leb, lmax = 50, 10, 8
+    P = DFT(mol, nrad, leb, lmax, precision="fp64").P.copy()
+    g, dP64, dR64 = _backward(mol, P, nrad, leb, lmax, "fp64")
+    assert np.abs(dR64.sum(axis=0)).max() <= 1e-8
+    coords = [(8, 0), (3, 1)]
+    fd = _fd_forces(mol, P, nrad, leb, lmax, coords)
+    err = max(abs(dR64[a, d] - fd[(a, d)]) for (a, d) in coords)
+    assert err <= 2e-7, (err, [(dR64[a, d], fd[(a, d)]) for (a, d) in coords])
+    g.set_precision("mixed")
+    g.fock_build(P)
+    dPm, dRm = g.backward()
+    assert np.abs(dRm - dR64).max() <= 1e-5, np.abs(dRm - dR64).max()
+    assert np.abs(dRm.sum(axis=0)).max() <= 1e-6
+    assert np.abs(dPm - dP64).max() <= 1e-6 * np.abs(dP64).max()

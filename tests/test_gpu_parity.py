@@ -215,3 +215,24 @@ def test_batched_builds_match_single_builds(gpu_lib):
             assert np.array_equal(J1, J0) and np.array_equal(X1, X0)
             assert s[0] == e0 and s[2] == ej0
     b.close()
+
+
+def test_mixed_forward_decane_matches_fp64(gpu_lib):
+    """32 atoms, 134 functions, 50 x 194: the mixed build (pair bins of the
+    cross-atom potential, FP32 CUDA-core contraction beyond 128 functions)
+    against the FP64 build at the core-Hamiltonian guess density:
+    |dE_xc + dE_J| <= 1e-5 Ha, every potential value finite and within 1e-4."""
+    from dftcxx_gb300.grid import DFT, MolecularGrid
+    from dftcxx_gb300.molecule import alkane
+    Z, xyz = alkane(10)
+    mol = Molecule(Z, xyz, "p631")
+    P = DFT(mol, 50, 10, 8, precision="fp64").P.copy()
+    g = MolecularGrid(mol, 50, 10, 8, precision="fp64")
+    r64 = g.fock_build(P)
+    V64 = g.get_potential()
+    g.set_precision("mixed")
+    rm = g.fock_build(P)
+    Vm = g.get_potential()
+    assert np.all(np.isfinite(Vm))
+    assert np.abs(Vm - V64).max() <= 1e-4
+    assert abs((rm["Exc"] + rm["EJ"]) - (r64["Exc"] + r64["EJ"])) <= 1e-5
