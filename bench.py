@@ -16,6 +16,10 @@ correction, Slater+VWN point kernel, Becke-Poisson Hartree potential, J and XC.
             max|dJ|, max|dXC| at the converged P
   roofline  dominant kernel of the mixed build, algorithmic bytes / measured
             duration, against the measured HBM copy bandwidth
+  adjoint   alkanes CnH2n+2 / 6-31G / 50 x 194: mixed forward and backward
+            (dE/dP, forces) times and force errors (outside the headline)
+  batched   64 jittered small molecules in one CUDA graph vs per-molecule
+            builds, with the batch autotuner (outside the headline)
 
 --impl reference times the reference algorithm on the host cores (the C port
 under oracle/, OpenMP on all cores) for the same workload.
@@ -386,6 +390,13 @@ def run_ours(args, rank, world):
         r = run_reference(ref_args, 0)
         cpu = r["cpu_baseline"]
 
+    adjoint = batched = None
+    if rank == 0 and world == 1:
+        if not args.no_adjoint:
+            adjoint = run_adjoint(dev)
+        if not args.no_batched:
+            batched = run_batched(dev)
+
     return {"metric": METRIC, "value": ms_mx, "unit": "ms",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mx,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32-split/f64",
@@ -398,7 +409,197 @@ def run_ours(args, rank, world):
                     "d2h_bytes_per_step": 2 * 8 * nn + 2 * 8},
             "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
-            "scf_seconds_outside_timing": scf_s}
+            "scf_seconds_outside_timing": scf_s,
+            "adjoint": adjoint, "batched": batched}
+
+
+def _guess_density(grid, mol):
+    """Half density matrix of the lowest core-Hamiltonian orbitals (the SCF
+    driver's first density, dft.cpp:216-226, 300-366)."""
+    S, T, V = grid.one_electron()
+    lam, U = np.linalg.eigh(S)
+    X = U / np.sqrt(lam)
+    _, Cp = np.linalg.eigh(X.T @ (T + V) @ X)
+    C = (X @ Cp)[:, :mol.nelec // 2]
+    return C @ C.T
+
+
+def _event_ms(fn, reps, stream):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_adjoint(dev, ns=(2, 4, 6, 8, 10), reps=5, h=1e-4):
+    """Adjoint workload: staggered CnH2n+2 / 6-31G / 50 x 194 at the
+    core-Hamiltonian density.  Per molecule: device time of the mixed forward
+    build and of the backward (dE/dP and dE/dR), the FP64 backward, and the
+    largest force difference between the mixed and the FP64 backward; for the
+    smallest and the largest chain, central differences (h = 1e-4 bohr) of the
+    FP64 forward on the largest force component."""
+    import torch
+    from dftcxx_gb300 import _lib
+    from dftcxx_gb300.grid import MolecularGrid
+    from dftcxx_gb300.molecule import Molecule, alkane
+    L = _lib.load()
+    stream = torch.cuda.Stream(device=dev)
+    rows = []
+    for n in ns:
+        Z, xyz = alkane(n)
+        mol = Molecule(Z, xyz, "p631")
+        g = MolecularGrid(mol, 50, 10, 8, precision="fp64", device=dev)
+        P = _guess_density(g, mol)
+        g.fock_build(P)
+        _, dR64 = g.backward()
+        g.set_stream(stream.cuda_stream)
+        nn = mol.nbf * mol.nbf
+        dP = torch.from_numpy(np.asfortranarray(P).ravel(order="F").copy()).to(f"cuda:{dev}")
+        bufs = torch.zeros(3 * nn + 3 + 3 * mol.natoms, dtype=torch.float64, device=f"cuda:{dev}")
+        J, XC, sc = bufs[:nn], bufs[nn:2 * nn], bufs[2 * nn:2 * nn + 3]
+        gP, gR = bufs[2 * nn + 3:3 * nn + 3], bufs[3 * nn + 3:]
+        vp = lambda t: ctypes.c_void_p(t.data_ptr())
+
+        def fwd():
+            _lib.check(L.dftg_fock_build_device(g.handle, vp(dP), vp(J), vp(XC), vp(sc)))
+
+        def bwd():
+            _lib.check(L.dftg_backward_device(g.handle, 1.0, 1.0, vp(gP), vp(gR)))
+
+        with torch.cuda.stream(stream):
+            fwd(); bwd()
+            bw64 = _event_ms(bwd, 2, stream)
+            fw64 = _event_ms(fwd, 2, stream)
+            g.set_precision("mixed")
+            for _ in range(3):
+                fwd(); bwd()
+            fw = _event_ms(fwd, reps, stream)
+            bw = _event_ms(bwd, reps, stream)
+            fwd(); bwd()
+            torch.cuda.synchronize(dev)
+        dRm = gR.cpu().numpy().reshape(-1, 3)
+        row = {"n": n, "natoms": mol.natoms, "nbf": mol.nbf, "grid_points": g.grid_size,
+               "mixed_forward_ms": fw, "mixed_backward_ms": bw, "fp64_forward_ms": fw64, "fp64_backward_ms": bw64,
+               "max_force_diff_mixed_vs_fp64_Ha_bohr": float(np.abs(dRm - dR64).max()),
+               "max_force_Ha_bohr": float(np.abs(dR64).max())}
+        if n in (ns[0], ns[-1]):
+            a, d = np.unravel_index(np.abs(dR64).argmax(), dR64.shape)
+            es = []
+            for sgn in (1, -1):
+                dx = np.zeros((mol.natoms, 3))
+                dx[a, d] = sgn * h
+                gd = MolecularGrid(mol.displaced(dx), 50, 10, 8, precision="fp64", device=dev)
+                r = gd.fock_build(P)
+                es.append(r["Exc"] + r["EJ"])
+                gd.close()
+            fd = (es[0] - es[1]) / (2 * h)
+            row["fd_check"] = {"atom": int(a), "axis": int(d), "fd_fp64_forward": fd,
+                               "err_fp64_backward": float(dR64[a, d] - fd), "err_mixed_backward": float(dRm[a, d] - fd)}
+        rows.append(row)
+        g.close()
+    return {"workload": "staggered CnH2n+2 / 6-31G / 50 x 194 / lmax 8, core-Hamiltonian density",
+            "gradient": "dE/dR of E_xc + E_J at fixed P (grid part of the nuclear forces) and dE/dP",
+            "molecules": rows}
+
+
+def run_batched(dev, nmol=64, reps=10, seed=20261204):
+    """Batched workload: nmol geometries drawn in turn from H2, LiH, H2O, NH3,
+    CH4, N2, CO, C2H6, C6H6, every nucleus displaced by N(0, 0.05 bohr),
+    STO-3G and 6-31G alternating by round, 50 x 194 grid, each at its own
+    core-Hamiltonian density.  Throughput in grid builds (SCF iterations) per
+    second: the per-molecule FP64 build, the per-molecule mixed build, and the
+    whole batch in one graph, before and after the batch autotuner."""
+    import torch
+    from dftcxx_gb300 import _lib
+    from dftcxx_gb300.grid import MolecularGrid, Batch
+    from dftcxx_gb300.molecule import Molecule, small_molecule
+    L = _lib.load()
+    names = ["H2", "LiH", "H2O", "NH3", "CH4", "N2", "CO", "C2H6", "C6H6"]
+    rng = np.random.default_rng(seed)
+    grids, dPs, outs = [], [], []
+    natoms = nbfs = npts = 0
+    t0 = time.perf_counter()
+    for i in range(nmol):
+        name = names[i % len(names)]
+        basis = "sto3g" if (i // len(names)) % 2 == 0 else "p631"
+        Z, xyz = small_molecule(name)
+        xyz = np.asarray(xyz, dtype=float) + rng.normal(0.0, 0.05, size=(len(Z), 3))
+        mol = Molecule(Z, xyz, basis)
+        g = MolecularGrid(mol, 50, 10, 8, precision="fp64", device=dev)
+        P = _guess_density(g, mol)
+        nn = mol.nbf * mol.nbf
+        grids.append(g)
+        dPs.append(torch.from_numpy(np.asfortranarray(P).ravel(order="F").copy()).to(f"cuda:{dev}"))
+        outs.append(torch.zeros(2 * nn + 3, dtype=torch.float64, device=f"cuda:{dev}"))
+        natoms += mol.natoms
+        nbfs += mol.nbf
+        npts += g.grid_size
+    setup_s = time.perf_counter() - t0
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    stream = torch.cuda.current_stream(dev)
+
+    def sequential():
+        for g, P, o in zip(grids, dPs, outs):
+            nn = g.nbf * g.nbf
+            _lib.check(L.dftg_fock_build_device(g.handle, vp(P), vp(o[:nn]), vp(o[nn:2 * nn]), vp(o[2 * nn:])))
+
+    for g in grids:
+        g.set_stream(stream.cuda_stream)
+    sequential(); sequential()
+    seq64 = _event_ms(sequential, 3, stream)
+    for g in grids:
+        g.set_precision("mixed")
+    sequential(); sequential()
+    seqmx = _event_ms(sequential, reps, stream)
+    for g in grids:   # every context back on its own stream: the graph's branches run concurrently
+        g.set_stream(0)
+    b = Batch(grids)
+    Js = [o[:g.nbf * g.nbf] for g, o in zip(grids, outs)]
+    XCs = [o[g.nbf * g.nbf:2 * g.nbf * g.nbf] for g, o in zip(grids, outs)]
+    Ss = [o[2 * g.nbf * g.nbf:] for g, o in zip(grids, outs)]
+    run = lambda: b.build(dPs, Js, XCs, Ss, stream=stream.cuda_stream)
+    run(); run()
+    bat = _event_ms(run, reps, stream)
+    t_tune = time.perf_counter()
+    b.autotune(reps=5)
+    tune_s = time.perf_counter() - t_tune
+    # the tuned batch does the work: after its graph is captured, outputs
+    # zeroed, one replay, then per-molecule builds of the same launch shapes
+    # must reproduce them bit for bit
+    run(); run()
+    for o in outs:
+        o.zero_()
+    run()
+    torch.cuda.synchronize(dev)
+    got = [o.clone() for o in outs]
+    nonzero = all(bool(o.abs().max() > 0) for o in got)
+    for g in grids:
+        g.set_stream(stream.cuda_stream)
+    sequential()
+    torch.cuda.synchronize(dev)
+    diff = max(float((a - b_).abs().max() / max(b_.abs().max(), 1e-300)) for a, b_ in zip(got, outs))
+    for g in grids:
+        g.set_stream(0)
+    run(); run()   # the contexts' streams are part of the graph key: recapture
+    bat_t = _event_ms(run, reps, stream)
+    shapes = sorted({g.launch_shape for g in grids})
+    b.close()
+    for g in grids:
+        g.close()
+    return {"workload": "%d geometries (H2 .. C6H6, N(0, 0.05 bohr) jitter), STO-3G / 6-31G, 50 x 194, lmax 8" % nmol,
+            "atoms": natoms, "basis_functions": nbfs, "grid_points": npts,
+            "fp64_per_molecule_builds_per_s": nmol / (seq64 * 1e-3),
+            "mixed_per_molecule_builds_per_s": nmol / (seqmx * 1e-3),
+            "mixed_batched_graph_builds_per_s": nmol / (bat * 1e-3),
+            "mixed_batched_autotuned_builds_per_s": nmol / (bat_t * 1e-3),
+            "ms_per_batch": {"fp64_sequential": seq64, "mixed_sequential": seqmx, "mixed_graph": bat,
+                             "mixed_graph_autotuned": bat_t},
+            "max_rel_diff_batch_vs_single": diff, "batch_outputs_nonzero": nonzero,
+            "autotuned_shapes": [list(s) for s in shapes], "autotune_s": tune_s, "setup_s": setup_s}
 
 
 def main():
@@ -408,6 +609,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (forces) workload")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-geometries workload")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world = _env_int("WORLD_SIZE", 1)

@@ -81,6 +81,10 @@ SIGNATURES = {
     "dftg_backward_profile": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _dp, ctypes.POINTER(ctypes.c_char_p),
                               ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
     "dftg_backward_device": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p],
+    "dftg_get_launch_shape": [ctypes.c_void_p, _ip, ctypes.c_int],
+    "dftg_set_launch_shape": [ctypes.c_void_p, _ip, ctypes.c_int],
+    "dftg_autotune": [ctypes.c_void_p, ctypes.c_int, _dp],
+    "dftg_batch_autotune": [ctypes.c_void_p, ctypes.c_int, _dp],
     "dftg_batch_create": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)],
     "dftg_batch_destroy": [ctypes.c_void_p],
     "dftg_batch_fock_build_device": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),

@@ -7,6 +7,7 @@
 //   xc points        LDA point kernel, cxc = w v_xc, E_xc (dft.cpp:394-424)
 //   hartree          K5a-e, cj = w V / 2                  (moleculargrid.cpp:336-380)
 //   contraction      K4 XC and J in one pass over phi     (dft.cpp:426-432, atomicgrid.cpp:471-488)
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -300,18 +301,26 @@ static int fock_pipeline(dftg_ctx *c)
 // One build on the device buffers (d_P in; d_J, d_XC, d_scal out).  The kernel
 // sequence of a (precision mask, stream) pair is captured once into a CUDA
 // graph and replayed; the first build of each pair runs eagerly.
+static bool pipe_shape_changed(const dftg_ctx *c)
+{
+    return c->pipe_shape[0] != c->tc_grid || c->pipe_shape[1] != c->ct_grid || c->pipe_shape[2] != c->ct_nst;
+}
+
 static int fock_pipeline_graph(dftg_ctx *c)
 {
-    if (c->pipe_exec && (c->pipe_mask != c->prec_mask || c->pipe_stream != c->stream)) {
+    if (c->pipe_exec && (c->pipe_mask != c->prec_mask || c->pipe_stream != c->stream || pipe_shape_changed(c))) {
         cudaGraphExecDestroy(c->pipe_exec);
         c->pipe_exec = nullptr;
         c->pipe_warm = false;
     }
     if (!c->pipe_exec) {
-        if (!c->pipe_warm || c->pipe_mask != c->prec_mask || c->pipe_stream != c->stream) {
+        if (!c->pipe_warm || c->pipe_mask != c->prec_mask || c->pipe_stream != c->stream || pipe_shape_changed(c)) {
             c->pipe_warm = true;
             c->pipe_mask = c->prec_mask;
             c->pipe_stream = c->stream;
+            c->pipe_shape[0] = c->tc_grid;
+            c->pipe_shape[1] = c->ct_grid;
+            c->pipe_shape[2] = c->ct_nst;
             return fock_pipeline(c);
         }
         cudaGraph_t g = nullptr;
@@ -702,6 +711,107 @@ int dftg_backward_profile(dftg_ctx *c, double seed_exc, double seed_ej, double *
     return DFTG_OK;
 }
 
+int dftg_get_launch_shape(const dftg_ctx *c, int *shape, int cap)
+{
+    CHECK_CTX(c);
+    if (!shape || cap < 3) { set_error("shape needs 3 entries"); return DFTG_ERR_ARG; }
+    shape[0] = c->tc_ready ? c->tc_grid : 0;
+    shape[1] = c->ct_ready ? c->ct_grid : 0;
+    shape[2] = c->ct_ready ? c->ct_nst : 0;
+    return DFTG_OK;
+}
+
+int dftg_set_launch_shape(dftg_ctx *c, const int *shape, int n)
+{
+    CHECK_CTX(c);
+    if (!shape || n < 3) { set_error("shape needs 3 entries"); return DFTG_ERR_ARG; }
+    if (c->tc_ready) {
+        if (shape[0] < 1 || shape[0] > c->tc_grid_max) { set_error("density CTAs %d outside 1..%d", shape[0], c->tc_grid_max); return DFTG_ERR_ARG; }
+        c->tc_grid = shape[0];
+    }
+    if (c->ct_ready) {
+        if (shape[1] < 1 || shape[1] > c->ct_grid_max) { set_error("contraction CTAs %d outside 1..%d", shape[1], c->ct_grid_max); return DFTG_ERR_ARG; }
+        if (shape[2] < c->ct_nst_min || shape[2] > c->ct_nst_max) {
+            set_error("contraction stages %d outside %d..%d", shape[2], c->ct_nst_min, c->ct_nst_max);
+            return DFTG_ERR_ARG;
+        }
+        c->ct_grid = shape[1];
+        c->ct_nst = shape[2];
+    }
+    return DFTG_OK;
+}
+
+// mean device time of reps graph-replayed builds on the context's own P
+static int time_builds(dftg_ctx *c, int reps, double *ms)
+{
+    DFTG_TRY(fock_pipeline_graph(c));   // eager (new shape) or replay
+    DFTG_TRY(fock_pipeline_graph(c));   // capture
+    cudaEvent_t e0, e1;
+    DFTG_CUDA(cudaEventCreate(&e0));
+    DFTG_CUDA(cudaEventCreate(&e1));
+    int rc = DFTG_OK;
+    if (cudaEventRecord(e0, c->stream) != cudaSuccess) rc = DFTG_ERR_CUDA;
+    for (int r = 0; r < reps && rc == DFTG_OK; ++r) rc = fock_pipeline_graph(c);
+    if (rc == DFTG_OK && cudaEventRecord(e1, c->stream) != cudaSuccess) rc = DFTG_ERR_CUDA;
+    float t = 0.f;
+    if (rc == DFTG_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = DFTG_ERR_CUDA;
+    if (rc == DFTG_OK && cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) rc = DFTG_ERR_CUDA;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != DFTG_OK) { set_error("autotune timing failed"); return rc; }
+    DFTG_TRY(sync_scalars(c));          // a bounded device wait that expired fails the candidate
+    *ms = (double)t / reps;
+    return DFTG_OK;
+}
+
+static void shape_candidates(int mx, std::vector<int> &out)
+{
+    out.clear();
+    const int f[5][2] = {{1, 1}, {3, 4}, {1, 2}, {1, 4}, {1, 8}};
+    for (const auto &q : f) {
+        const int v = mx * q[0] / q[1];
+        if (v >= 1 && std::find(out.begin(), out.end(), v) == out.end()) out.push_back(v);
+    }
+}
+
+int dftg_autotune(dftg_ctx *c, int reps, double *best_ms)
+{
+    CHECK_CTX(c);
+    if (reps < 1) { set_error("reps < 1"); return DFTG_ERR_ARG; }
+    if (!c->have_build) { set_error("autotune before a complete Fock build (it times builds of that P)"); return DFTG_ERR_STATE; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    double best = 0.0;
+    DFTG_TRY(time_builds(c, reps, &best));
+    const bool tune_tc = c->tc_ready && (c->prec_mask & kPrecDensity);
+    const bool tune_ct = c->ct_ready && (c->prec_mask & kPrecContract);
+    std::vector<int> cand;
+    // coordinate descent over the three shapes, each from the current best
+    for (int knob = 0; knob < 3; ++knob) {
+        int *field = knob == 0 ? &c->tc_grid : (knob == 1 ? &c->ct_grid : &c->ct_nst);
+        if ((knob == 0 && !tune_tc) || (knob > 0 && !tune_ct)) continue;
+        if (knob == 2) {
+            cand.clear();
+            for (int v = c->ct_nst_max; v >= c->ct_nst_min; --v) cand.push_back(v);
+        } else {
+            shape_candidates(knob == 0 ? c->tc_grid_max : c->ct_grid_max, cand);
+        }
+        const int keep = *field;
+        int best_v = keep;
+        for (int v : cand) {
+            if (v == keep) continue;
+            *field = v;
+            double t = 0.0;
+            DFTG_TRY(time_builds(c, reps, &t));
+            if (t < best) { best = t; best_v = v; }
+        }
+        *field = best_v;
+    }
+    DFTG_TRY(fock_pipeline_graph(c));   // leave the outputs of the chosen shape
+    DFTG_TRY(sync_scalars(c));
+    if (best_ms) *best_ms = best;
+    return DFTG_OK;
+}
+
 int dftg_nuclear_repulsion(const dftg_ctx *c, double *enuc)
 {
     CHECK_CTX(c);
@@ -811,6 +921,9 @@ extern "C" int dftg_batch_fock_build_device(dftg_batch *b, const double *const *
         key.push_back(scalars_devs ? scalars_devs[i] : nullptr);
         key.push_back(reinterpret_cast<const void *>((uintptr_t)b->ctx[i]->prec_mask));
         key.push_back(b->ctx[i]->stream);
+        key.push_back(reinterpret_cast<const void *>((uintptr_t)b->ctx[i]->tc_grid));
+        key.push_back(reinterpret_cast<const void *>((uintptr_t)b->ctx[i]->ct_grid));
+        key.push_back(reinterpret_cast<const void *>((uintptr_t)b->ctx[i]->ct_nst));
     }
     if (b->exec && key != b->key) {
         cudaGraphExecDestroy(b->exec);
@@ -862,5 +975,64 @@ extern "C" int dftg_batch_fock_build_device(dftg_batch *b, const double *const *
         c->have_build = true;
     c->fwd_mask = c->prec_mask;
     }
+    return DFTG_OK;
+}
+
+// Autotuner of a batch: the contexts' CTA counts scaled together by 1, 1/2,
+// 1/4 and 1/8 (branches of the graph run concurrently, so smaller grids per
+// build can raise the throughput); the graph of every candidate is timed on the
+// contexts' own density matrices and the fastest scale is kept.
+extern "C" int dftg_batch_autotune(dftg_batch *b, int reps, double *best_ms)
+{
+    if (!b) { set_error("null batch"); return DFTG_ERR_ARG; }
+    if (reps < 1) { set_error("reps < 1"); return DFTG_ERR_ARG; }
+    const int n = (int)b->ctx.size();
+    for (dftg_ctx *c : b->ctx)
+        if (!c->have_build) { set_error("batch autotune before a complete build of every context"); return DFTG_ERR_STATE; }
+    DFTG_CUDA(cudaSetDevice(b->ctx[0]->device));
+    std::vector<const double *> P(n);
+    std::vector<int> tc0(n), ct0(n);
+    for (int i = 0; i < n; ++i) {
+        P[i] = b->ctx[i]->d_P;
+        tc0[i] = b->ctx[i]->tc_grid;
+        ct0[i] = b->ctx[i]->ct_grid;
+    }
+    cudaStream_t s0 = b->ctx[0]->stream;
+    auto run = [&](int div, double *ms) -> int {
+        for (int i = 0; i < n; ++i) {
+            dftg_ctx *c = b->ctx[i];
+            if (c->tc_ready) c->tc_grid = std::max(1, tc0[i] / div);
+            if (c->ct_ready) c->ct_grid = std::max(1, ct0[i] / div);
+        }
+        for (int w = 0; w < 2; ++w)   // eager, then capture
+            DFTG_TRY(dftg_batch_fock_build_device(b, P.data(), nullptr, nullptr, nullptr, nullptr));
+        cudaEvent_t e0, e1;
+        DFTG_CUDA(cudaEventCreate(&e0));
+        DFTG_CUDA(cudaEventCreate(&e1));
+        int rc = cudaEventRecord(e0, s0) == cudaSuccess ? DFTG_OK : DFTG_ERR_CUDA;
+        for (int r = 0; r < reps && rc == DFTG_OK; ++r)
+            rc = dftg_batch_fock_build_device(b, P.data(), nullptr, nullptr, nullptr, nullptr);
+        float t = 0.f;
+        if (rc == DFTG_OK && cudaEventRecord(e1, s0) != cudaSuccess) rc = DFTG_ERR_CUDA;
+        if (rc == DFTG_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = DFTG_ERR_CUDA;
+        if (rc == DFTG_OK && cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) rc = DFTG_ERR_CUDA;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (rc != DFTG_OK) { set_error("batch autotune timing failed"); return rc; }
+        for (dftg_ctx *c : b->ctx) DFTG_TRY(sync_scalars(c));
+        *ms = (double)t / reps;
+        return DFTG_OK;
+    };
+    double best = 0.0;
+    int best_div = 1;
+    DFTG_TRY(run(1, &best));
+    for (int div : {2, 4, 8}) {
+        double t = 0.0;
+        DFTG_TRY(run(div, &t));
+        if (t < best) { best = t; best_div = div; }
+    }
+    double t = 0.0;
+    DFTG_TRY(run(best_div, &t));   // leave the chosen shapes and their outputs
+    if (best_ms) *best_ms = best;
     return DFTG_OK;
 }

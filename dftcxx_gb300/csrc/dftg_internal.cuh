@@ -247,8 +247,13 @@ struct dftg_ctx {
     bool have_hartree = false;
     bool rho_scaled = false;      // rho on the device carries the correction factor
 
-    // CUDA graph of the per-build kernel sequence (keyed by precision mask and stream)
+    // launch shapes of the tensor-core kernels (CTAs, contraction stages): set
+    // up at the largest that fits, lowered by the autotuner
+    int tc_grid_max = 0, ct_grid_max = 0, ct_nst_max = 0, ct_nst_min = 0;
+
+    // CUDA graph of the per-build kernel sequence (keyed by precision mask, stream and launch shapes)
     cudaGraphExec_t pipe_exec = nullptr;
+    int pipe_shape[3] = {0, 0, 0};
     unsigned pipe_mask = 0;
     cudaStream_t pipe_stream = nullptr;
     bool pipe_warm = false;

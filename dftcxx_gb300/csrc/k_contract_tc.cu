@@ -665,6 +665,13 @@ int contract_tc_setup(dftg_ctx *c)
     c->ct_kbpc = kbpc;
     c->ct_nchunk = nchunk;
     c->ct_grid = grid;
+    c->ct_grid_max = grid;
+    c->ct_nst_max = nst;
+    // fewest stages the autotuner may choose: a CTA still needs more than half
+    // of the shared memory, so one contraction CTA runs per SM as at setup
+    int nmin = nst;
+    while (nmin > 2 && ct_smem(nmin - 1, NP, AR, c->nbf, spart) * 2 > (size_t)optin) --nmin;
+    c->ct_nst_min = nmin;
     c->ct_ready = true;
     return DFTG_OK;
 }

@@ -350,6 +350,7 @@ int density_tc_setup(dftg_ctx *c)
     int nsm = 0;
     DFTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     c->tc_grid = nsm < ntiles ? nsm : ntiles;
+    c->tc_grid_max = c->tc_grid;
     c->tc_ready = true;
     return DFTG_OK;
 }

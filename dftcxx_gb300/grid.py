@@ -129,6 +129,25 @@ class MolecularGrid:
         check(_lib.load().dftg_backward(self._h, float(seed_exc), float(seed_ej), _ptr(dP), _ptr(dR)))
         return np.ascontiguousarray(dP), dR
 
+    def autotune(self, reps=10):
+        """Time candidate launch shapes of the tensor-core kernels on the last
+        built P and keep the fastest; returns the best ms per build."""
+        ms = ctypes.c_double()
+        check(_lib.load().dftg_autotune(self._h, int(reps), ctypes.byref(ms)))
+        return ms.value
+
+    @property
+    def launch_shape(self):
+        """(density CTAs, contraction CTAs, contraction stages); 0 = no such kernel."""
+        v = (ctypes.c_int * 3)()
+        check(_lib.load().dftg_get_launch_shape(self._h, v, 3))
+        return tuple(v)
+
+    @launch_shape.setter
+    def launch_shape(self, shape):
+        v = (ctypes.c_int * 3)(*[int(x) for x in shape])
+        check(_lib.load().dftg_set_launch_shape(self._h, v, 3))
+
     def backward_profile(self, seed_exc=1.0, seed_ej=1.0):
         """Per-phase device times (ms) of one backward pass: {name: ms}."""
         ms = (ctypes.c_double * 32)()
@@ -271,6 +290,13 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+    def autotune(self, reps=5):
+        """Scale all contexts' CTA counts together (1, 1/2, 1/4, 1/8), keep the
+        fastest for concurrent replay; returns ms per batch replay."""
+        ms = ctypes.c_double()
+        check(_lib.load().dftg_batch_autotune(self._h, int(reps), ctypes.byref(ms)))
+        return ms.value
 
     def build(self, P_devs, J_devs=None, XC_devs=None, scal_devs=None, stream=None):
         n = len(self.grids)

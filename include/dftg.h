@@ -200,6 +200,22 @@ int dftg_batch_destroy(dftg_batch *b);
  * the first context's stream); the call returns without synchronising. */
 int dftg_batch_fock_build_device(dftg_batch *b, const double *const *P_devs, double *const *J_devs,
                                  double *const *XC_devs, double *const *scalars_devs, void *stream);
+/* Batch autotuner: scales every context's CTA counts by 1, 1/2, 1/4 and 1/8
+ * together (the graph's branches run concurrently), times reps replays of the
+ * batch graph on the contexts' own last P and keeps the fastest scale; needs a
+ * complete build of every context.  best_ms (per batch replay) may be NULL. */
+int dftg_batch_autotune(dftg_batch *b, int reps, double *best_ms);
+
+/* Launch-shape autotuner (no counterpart in the reference).  Shape =
+ * {CTAs of the tensor-core density kernel, CTAs of the tensor-core XC / J
+ * contraction, pipeline stages of the contraction}; 0 where the context has no
+ * such kernel.  dftg_autotune times reps graph-replayed builds of the last
+ * built P for candidate shapes (coordinate descent, each knob from the current
+ * best) and keeps the fastest; it needs a preceding complete build and leaves
+ * the outputs of a build with the chosen shape.  best_ms may be NULL. */
+int dftg_get_launch_shape(const dftg_ctx *ctx, int *shape, int cap);
+int dftg_set_launch_shape(dftg_ctx *ctx, const int *shape, int n);
+int dftg_autotune(dftg_ctx *ctx, int reps, double *best_ms);
 
 /* XC and J contraction that allocates nothing.  No counterpart in the
  * reference: it exists for callers that may not call cudaMalloc / cudaFree

@@ -214,6 +214,20 @@ def test_batched_builds_match_single_builds(gpu_lib):
             s = sc.cpu().numpy()
             assert np.array_equal(J1, J0) and np.array_equal(X1, X0)
             assert s[0] == e0 and s[2] == ej0
+    # after the batch autotuner the batch still equals single builds of the
+    # same launch shapes, and the contexts agree with their untuned results
+    b.autotune(reps=2)
+    for _ in range(3):
+        b.build(Pd, Jd, Xd, Sd)
+    torch.cuda.synchronize()
+    for (J0, X0, e0, ej0), g, P, j, x in zip(ref, grids, Ps, Jd, Xd):
+        n = P.shape[0]
+        J1 = j.cpu().numpy().reshape(n, n, order="F")
+        X1 = x.cpu().numpy().reshape(n, n, order="F")
+        r = g.fock_build(P)
+        assert np.array_equal(J1, r["J"]) and np.array_equal(X1, r["XC"])
+        assert np.abs(J1 - J0).max() <= 1e-7 * np.abs(J0).max()
+        assert np.abs(X1 - X0).max() <= 1e-7 * np.abs(X0).max()
     b.close()
 
 
@@ -236,3 +250,33 @@ def test_mixed_forward_decane_matches_fp64(gpu_lib):
     assert np.all(np.isfinite(Vm))
     assert np.abs(Vm - V64).max() <= 1e-4
     assert abs((rm["Exc"] + rm["EJ"]) - (r64["Exc"] + r64["EJ"])) <= 1e-5
+
+
+def test_autotune_keeps_results(gpu_lib):
+    """The autotuner changes launch shapes only: builds before and after agree
+    (split-K order changes the rounding: 1e-7 of max|J|, max|XC|), the chosen
+    shape lies inside the allowed range and out-of-range shapes are refused."""
+    from dftcxx_gb300 import _lib
+    from dftcxx_gb300.grid import MolecularGrid
+    from dftcxx_gb300.molecule import benzene
+    Z, xyz = benzene()
+    mol = Molecule(Z, xyz, "p631")
+    g = MolecularGrid(mol, 40, 10, 8, precision="mixed")
+    P = _density(mol, 2)
+    r0 = g.fock_build(P)
+    shape0 = g.launch_shape
+    assert shape0[0] > 0 and shape0[1] > 0 and shape0[2] >= 2
+    ms = g.autotune(reps=2)
+    assert ms > 0.0
+    shape1 = g.launch_shape
+    assert 1 <= shape1[0] <= shape0[0] and 1 <= shape1[1] <= shape0[1] and 2 <= shape1[2] <= shape0[2]
+    r1 = g.fock_build(P)
+    assert np.abs(r1["J"] - r0["J"]).max() <= 1e-7 * np.abs(r0["J"]).max()
+    assert np.abs(r1["XC"] - r0["XC"]).max() <= 1e-7 * np.abs(r0["XC"]).max()
+    assert abs(r1["Exc"] - r0["Exc"]) <= 1e-9 * abs(r0["Exc"])
+    # an explicit shape, then the refusal of one beyond the setup maximum
+    g.launch_shape = (max(1, shape0[0] // 2), max(1, shape0[1] // 2), shape1[2])
+    r2 = g.fock_build(P)
+    assert np.abs(r2["J"] - r0["J"]).max() <= 1e-7 * np.abs(r0["J"]).max()
+    with pytest.raises(_lib.DftgError):
+        g.launch_shape = (shape0[0] + 1, shape0[1], shape0[2])
