@@ -20,6 +20,8 @@ correction, Slater+VWN point kernel, Becke-Poisson Hartree potential, J and XC.
             (dE/dP, forces) times and force errors (outside the headline)
   batched   64 jittered small molecules in one CUDA graph vs per-molecule
             builds, with the batch autotuner (outside the headline)
+  synthetic 2M points x 512 primitives: rho, LDA and XC in FP64 and mixed
+            (outside the headline)
 
 --impl reference times the reference algorithm on the host cores (the C port
 under oracle/, OpenMP on all cores) for the same workload.
@@ -390,12 +392,14 @@ def run_ours(args, rank, world):
         r = run_reference(ref_args, 0)
         cpu = r["cpu_baseline"]
 
-    adjoint = batched = None
+    adjoint = batched = synthetic = None
     if rank == 0 and world == 1:
         if not args.no_adjoint:
             adjoint = run_adjoint(dev)
         if not args.no_batched:
             batched = run_batched(dev)
+        if not args.no_synthetic:
+            synthetic = run_synthetic(dev)
 
     return {"metric": METRIC, "value": ms_mx, "unit": "ms",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mx,
@@ -410,7 +414,7 @@ def run_ours(args, rank, world):
             "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
             "scf_seconds_outside_timing": scf_s,
-            "adjoint": adjoint, "batched": batched}
+            "adjoint": adjoint, "batched": batched, "synthetic": synthetic}
 
 
 def _guess_density(grid, mol):
@@ -602,6 +606,61 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
             "autotuned_shapes": [list(s) for s in shapes], "autotune_s": tune_s, "setup_s": setup_s}
 
 
+def run_synthetic(dev, npts=2_000_000, nbf=512, nocc=128, reps=3):
+    """Synthetic contraction workload (seeded): 2M points uniform in a 20-bohr
+    cube, weights log-uniform in [1e-4, 1], 512 single-primitive Cartesian
+    s/p/d functions (exponents log-uniform in [0.1, 50], centres uniform in the
+    cube), P = C C^T with C 512 x 128 ~ N(0, 0.1).  One step: rho = 2 phi^T P phi,
+    LDA point kernel, XC = phi^T diag(w v_xc) phi (dftg_xc_build_device), FP64
+    and mixed; the mixed error against FP64 and the mixed step's rate over its
+    algorithmic bytes (the FP32 amplitudes read by the density and by the
+    contraction)."""
+    import torch
+    from dftcxx_gb300 import _lib
+    from dftcxx_gb300.grid import PointGrid
+    from dftcxx_gb300.molecule import synthetic_contraction
+    L = _lib.load()
+    t0 = time.perf_counter()
+    pts, w, lmn, alpha, centres, P = synthetic_contraction(npts=npts, nbf=nbf, nocc=nocc)
+    g = PointGrid(pts, w, centres, np.arange(nbf), lmn, np.ones(nbf, np.int32), alpha, np.ones(nbf),
+                  precision="fp64", device=dev)
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream(device=dev)
+    g.set_stream(stream.cuda_stream)
+    nn = nbf * nbf
+    dP = torch.from_numpy(np.asfortranarray(P).ravel(order="F").copy()).to(f"cuda:{dev}")
+    XC = torch.zeros(nn, dtype=torch.float64, device=f"cuda:{dev}")
+    sc = torch.zeros(2, dtype=torch.float64, device=f"cuda:{dev}")
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def step():
+        _lib.check(L.dftg_xc_build_device(g.handle, vp(dP), vp(XC), vp(sc)))
+
+    with torch.cuda.stream(stream):
+        step()
+        ms64 = _event_ms(step, 1, stream)
+        torch.cuda.synchronize(dev)
+        xc64, s64 = XC.cpu().numpy().copy(), sc.cpu().numpy().copy()
+        rho64 = g.get_densities()
+        g.set_precision("mixed")
+        step(); step()
+        msmx = _event_ms(step, reps, stream)
+        torch.cuda.synchronize(dev)
+        xcm, sm = XC.cpu().numpy().copy(), sc.cpu().numpy().copy()
+        rhom = g.get_densities()
+    npad = (npts + 127) // 128 * 128
+    alg = 2 * 4 * npad * nbf + 8 * npad * 3
+    out = {"workload": "synthetic: %d points, %d s/p/d primitives, P = C C^T (C %d x %d)" % (npts, nbf, nbf, nocc),
+           "fp64_ms_per_step": ms64, "mixed_ms_per_step": msmx, "speedup": ms64 / msmx,
+           "E_xc_fp64": float(s64[0]), "dE_xc_rel": abs(float(sm[0] - s64[0])) / abs(float(s64[0])),
+           "max_dXC_rel": float(np.abs(xcm - xc64).max() / np.abs(xc64).max()),
+           "max_drho_rel": float(np.abs(rhom - rho64).max() / np.abs(rho64).max()),
+           "mixed_path": "FP32 CUDA-core density and compensated FP32 contraction (nbf > 128: no tensor-core form yet)",
+           "mixed_alg_bytes": alg, "mixed_GBps_over_alg_bytes": alg / (msmx * 1e-3) / 1e9, "setup_s": setup_s}
+    g.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -611,6 +670,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (forces) workload")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-geometries workload")
+    ap.add_argument("--no-synthetic", action="store_true", help="skip the synthetic contraction workload")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world = _env_int("WORLD_SIZE", 1)

@@ -41,6 +41,10 @@ class GridParams(ctypes.Structure):
                 ("device", ctypes.c_int)]
 
 
+class Points(ctypes.Structure):
+    _fields_ = [("npts", ctypes.c_size_t), ("xyz", _dp), ("w", _dp)]
+
+
 class DftgError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("dftg error %d: %s" % (code, msg))
@@ -81,6 +85,10 @@ SIGNATURES = {
     "dftg_backward_profile": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _dp, ctypes.POINTER(ctypes.c_char_p),
                               ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
     "dftg_backward_device": [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p],
+    "dftg_create_points": [ctypes.POINTER(Points), ctypes.POINTER(Molecule), ctypes.POINTER(Basis), ctypes.c_int,
+                           ctypes.POINTER(ctypes.c_void_p)],
+    "dftg_xc_build": [ctypes.c_void_p, _dp, _dp, _dp, _dp],
+    "dftg_xc_build_device": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     "dftg_get_launch_shape": [ctypes.c_void_p, _ip, ctypes.c_int],
     "dftg_set_launch_shape": [ctypes.c_void_p, _ip, ctypes.c_int],
     "dftg_autotune": [ctypes.c_void_p, ctypes.c_int, _dp],

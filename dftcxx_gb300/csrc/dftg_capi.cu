@@ -81,7 +81,7 @@ static void free_ctx(dftg_ctx *c)
                     c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_flag,
                     c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32, c->d_U32T, c->d_red2,
                     c->d_bw_pt, c->d_bw_lm, c->d_bw_fpart, c->d_bw_out, c->d_bw_counter, c->d_bw_pairp,
-                    c->d_bw_binfirst, c->d_bw_cpart, c->d_bw_geo, c->d_bw_geo64};
+                    c->d_bw_binfirst, c->d_bw_cpart, c->d_bw_geo, c->d_bw_geo64, c->d_bw_prim32};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -406,6 +406,210 @@ int dftg_create(const dftg_molecule *mol, const dftg_basis *basis, const dftg_gr
     return DFTG_OK;
 }
 
+// Context over explicit points (no atoms, cells or Hartree step): the
+// amplitudes, the density, the LDA point kernel and the XC contraction of a
+// synthetic contraction workload.  centres give the function centres (their
+// Z are ignored).
+static int build_points_ctx(dftg_ctx *c, const dftg_points *pts, const dftg_molecule *ctr, const dftg_basis *basis,
+                            int device)
+{
+    c->device = device;
+    c->points_only = true;
+    DFTG_CUDA(cudaSetDevice(c->device));
+    DFTG_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+    c->stream = c->own_stream;
+    c->natoms = ctr->natoms;
+    c->Z.assign(ctr->natoms, 0);
+    c->xyz.assign(ctr->xyz, ctr->xyz + 3 * ctr->natoms);
+    c->nbf = basis->nbf;
+    c->bf_atom.assign(basis->bf_atom, basis->bf_atom + c->nbf);
+    c->bf_lmn.assign(basis->bf_lmn, basis->bf_lmn + 3 * c->nbf);
+    c->bf_off.assign(c->nbf + 1, 0);
+    for (int i = 0; i < c->nbf; ++i) c->bf_off[i + 1] = c->bf_off[i] + basis->bf_nprim[i];
+    c->nprim = c->bf_off[c->nbf];
+    c->alpha.assign(basis->prim_alpha, basis->prim_alpha + c->nprim);
+    c->coef.assign(basis->prim_coef, basis->prim_coef + c->nprim);
+    c->norm.resize(c->nprim);
+    std::vector<double> pcn(c->nprim);
+    for (int i = 0; i < c->nbf; ++i)
+        for (int k = c->bf_off[i]; k < c->bf_off[i + 1]; ++k) {
+            c->norm[k] = gto_norm(c->alpha[k], c->bf_lmn[3 * i], c->bf_lmn[3 * i + 1], c->bf_lmn[3 * i + 2]);
+            pcn[k] = c->coef[k] * c->norm[k];
+        }
+    c->nrad = 1;
+    c->leb = 0;
+    c->nang = 1;
+    c->lmax = 0;
+    c->nlm = 1;
+    c->npts = pts->npts;
+    c->npad = (c->npts + kPtsAlign - 1) / kPtsAlign * kPtsAlign;
+    const size_t np = c->npad, nn = (size_t)c->nbf * c->nbf;
+    DFTG_TRY(dalloc(&c->d_atoms, 4 * (size_t)c->natoms));
+    DFTG_TRY(dalloc(&c->d_bf_lmn, 3 * (size_t)c->nbf));
+    DFTG_TRY(dalloc(&c->d_bf_off, (size_t)c->nbf + 1));
+    DFTG_TRY(dalloc(&c->d_bf_atom, (size_t)c->nbf));
+    DFTG_TRY(dalloc(&c->d_pa, (size_t)c->nprim));
+    DFTG_TRY(dalloc(&c->d_pcn, (size_t)c->nprim));
+    DFTG_TRY(dalloc(&c->d_x, np));
+    DFTG_TRY(dalloc(&c->d_y, np));
+    DFTG_TRY(dalloc(&c->d_z, np));
+    DFTG_TRY(dalloc(&c->d_w, np));
+    DFTG_TRY(dalloc(&c->d_wb, np));
+    DFTG_TRY(dalloc(&c->d_rho, np));
+    DFTG_TRY(dalloc(&c->d_V, np));
+    DFTG_TRY(dalloc(&c->d_cxc, np));
+    DFTG_TRY(dalloc(&c->d_cj, np));
+    DFTG_TRY(dalloc(&c->d_cxc32, np));
+    DFTG_TRY(dalloc(&c->d_cj32, np));
+    DFTG_TRY(dalloc(&c->d_phi, np * c->nbf));
+    DFTG_TRY(dalloc(&c->d_phi32, np * c->nbf));
+    DFTG_TRY(dalloc(&c->d_P, nn));
+    DFTG_TRY(dalloc(&c->d_P32, nn));
+    DFTG_TRY(dalloc(&c->d_J, nn));
+    DFTG_TRY(dalloc(&c->d_XC, nn));
+    int nsm = 0;
+    DFTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+    size_t part = contract_part_elems(c->nbf, c->npad);
+    const size_t part_tc = contract_tc_part_elems(c->nbf, c->npad, nsm);
+    c->part_elems = part > part_tc ? part : part_tc;
+    DFTG_TRY(dalloc(&c->d_part, c->part_elems));
+    c->red_elems = reduction_elems(c->npad, 1, 1, (int)std::min<size_t>(c->npts, 0x7fffffff)) + 64;
+    DFTG_TRY(dalloc(&c->d_red, c->red_elems));
+    DFTG_TRY(dalloc(&c->d_scal, scal_elems(c->natoms)));
+    DFTG_CUDA(cudaMalloc(&c->d_counters, sizeof(int) * kNumCounters));
+    DFTG_CUDA(cudaMemset(c->d_counters, 0, sizeof(int) * kNumCounters));
+    DFTG_CUDA(cudaMallocHost(&c->h_scal, sizeof(double) * scal_elems(c->natoms)));
+    DFTG_CUDA(cudaMemset(c->d_scal, 0, sizeof(double) * scal_elems(c->natoms)));
+    std::vector<double> atoms(4 * (size_t)c->natoms, 0.0);
+    for (int a = 0; a < c->natoms; ++a)
+        for (int d = 0; d < 3; ++d) atoms[4 * a + d] = c->xyz[3 * a + d];
+    // points as structure of arrays, padding at zero weight; w_becke = 1
+    std::vector<double> X(np, 0.0), Y(np, 0.0), Zc(np, 0.0), W(np, 0.0), WB(np, 0.0);
+    for (size_t p = 0; p < c->npts; ++p) {
+        X[p] = pts->xyz[3 * p];
+        Y[p] = pts->xyz[3 * p + 1];
+        Zc[p] = pts->xyz[3 * p + 2];
+        W[p] = pts->w[p];
+        WB[p] = 1.0;
+    }
+    DFTG_CUDA(cudaMemcpy(c->d_atoms, atoms.data(), sizeof(double) * atoms.size(), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_x, X.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_y, Y.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_z, Zc.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_w, W.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_wb, WB.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemset(c->d_cj, 0, sizeof(double) * np));
+    DFTG_CUDA(cudaMemset(c->d_cj32, 0, sizeof(float) * np));
+    DFTG_CUDA(cudaMemcpy(c->d_bf_lmn, c->bf_lmn.data(), sizeof(int) * 3 * c->nbf, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_bf_off, c->bf_off.data(), sizeof(int) * (c->nbf + 1), cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_bf_atom, c->bf_atom.data(), sizeof(int) * c->nbf, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_pa, c->alpha.data(), sizeof(double) * c->nprim, cudaMemcpyHostToDevice));
+    DFTG_CUDA(cudaMemcpy(c->d_pcn, pcn.data(), sizeof(double) * c->nprim, cudaMemcpyHostToDevice));
+    DFTG_TRY(launch_amplitudes(c));
+    DFTG_TRY(contract_setup(c));
+    DFTG_TRY(contract_tc_setup(c));
+    DFTG_TRY(density_tc_setup(c));
+    DFTG_CUDA(cudaStreamSynchronize(c->stream));
+    return DFTG_OK;
+}
+
+int dftg_create_points(const dftg_points *pts, const dftg_molecule *centres, const dftg_basis *basis, int device,
+                       dftg_ctx **out)
+{
+    if (!out) { set_error("out is NULL"); return DFTG_ERR_ARG; }
+    *out = nullptr;
+    if (!pts || !centres || !basis || !pts->xyz || !pts->w || !centres->xyz || !basis->bf_atom || !basis->bf_lmn ||
+        !basis->bf_nprim || !basis->prim_alpha || !basis->prim_coef) {
+        set_error("NULL argument");
+        return DFTG_ERR_ARG;
+    }
+    if (pts->npts < 1) { set_error("npts 0"); return DFTG_ERR_ARG; }
+    if (centres->natoms < 1) { set_error("no centres"); return DFTG_ERR_ARG; }
+    if (basis->nbf < 1) { set_error("nbf %d < 1", basis->nbf); return DFTG_ERR_ARG; }
+    for (size_t p = 0; p < pts->npts; ++p) {
+        if (!std::isfinite(pts->xyz[3 * p]) || !std::isfinite(pts->xyz[3 * p + 1]) || !std::isfinite(pts->xyz[3 * p + 2]) ||
+            !std::isfinite(pts->w[p])) {
+            set_error("point %zu not finite", p);
+            return DFTG_ERR_NONFINITE;
+        }
+    }
+    for (int a = 0; a < 3 * centres->natoms; ++a)
+        if (!std::isfinite(centres->xyz[a])) { set_error("centre coordinate not finite"); return DFTG_ERR_NONFINITE; }
+    long long np = 0;
+    for (int i = 0; i < basis->nbf; ++i) {
+        if (basis->bf_atom[i] < 0 || basis->bf_atom[i] >= centres->natoms) { set_error("bf_atom[%d] out of range", i); return DFTG_ERR_ARG; }
+        if (basis->bf_nprim[i] < 1) { set_error("bf_nprim[%d] < 1", i); return DFTG_ERR_ARG; }
+        int L = 0;
+        for (int d = 0; d < 3; ++d) {
+            if (basis->bf_lmn[3 * i + d] < 0) { set_error("bf_lmn[%d] negative", i); return DFTG_ERR_ARG; }
+            L += basis->bf_lmn[3 * i + d];
+        }
+        if (L > 4) { set_error("bf %d: angular momentum %d > 4", i, L); return DFTG_ERR_ARG; }
+        np += basis->bf_nprim[i];
+    }
+    for (long long k = 0; k < np; ++k)
+        if (!(basis->prim_alpha[k] > 0.0) || !std::isfinite(basis->prim_coef[k])) {
+            set_error("primitive %lld: bad exponent or coefficient", k);
+            return DFTG_ERR_ARG;
+        }
+    dftg_ctx *c = new (std::nothrow) dftg_ctx();
+    if (!c) { set_error("host allocation failed"); return DFTG_ERR_NOMEM; }
+    int rc = build_points_ctx(c, pts, centres, basis, device);
+    if (rc != DFTG_OK) { free_ctx(c); return rc; }
+    *out = c;
+    return DFTG_OK;
+}
+
+// rho (no density correction), LDA point kernel, XC contraction; the scalars
+// E_xc and the integrated density stay on the device
+static int xc_pipeline(dftg_ctx *c)
+{
+    DFTG_TRY(launch_density(c));
+    DFTG_TRY(launch_atom_sums(c, kSumsOnly));
+    c->rho_scaled = false;
+    DFTG_TRY(launch_xc_points(c, false));
+    DFTG_TRY(launch_contract(c, true, false));
+    return DFTG_OK;
+}
+
+int dftg_xc_build_device(dftg_ctx *c, const double *P_dev, double *XC_dev, double *scalars_dev)
+{
+    CHECK_CTX(c);
+    if (!P_dev) { set_error("P_dev NULL"); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    if (P_dev != c->d_P) DFTG_CUDA(cudaMemcpyAsync(c->d_P, P_dev, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
+    DFTG_TRY(xc_pipeline(c));
+    if (XC_dev) DFTG_CUDA(cudaMemcpyAsync(XC_dev, c->d_XC, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream));
+    if (scalars_dev) {
+        DFTG_CUDA(cudaMemcpyAsync(scalars_dev, c->d_scal + kScalExc, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        DFTG_CUDA(cudaMemcpyAsync(scalars_dev + 1, c->d_scal + kScalNelec, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    c->have_density = true;
+    c->have_hartree = false;
+    c->have_build = false;
+    return DFTG_OK;
+}
+
+int dftg_xc_build(dftg_ctx *c, const double *P, double *XC, double *exc, double *nelec)
+{
+    CHECK_CTX(c);
+    if (!P) { set_error("P NULL"); return DFTG_ERR_ARG; }
+    DFTG_TRY(check_matrix(P, c->nbf));
+    DFTG_CUDA(cudaSetDevice(c->device));
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    DFTG_CUDA(cudaMemcpyAsync(c->d_P, P, sizeof(double) * nn, cudaMemcpyHostToDevice, c->stream));
+    DFTG_TRY(xc_pipeline(c));
+    if (XC) DFTG_CUDA(cudaMemcpyAsync(XC, c->d_XC, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream));
+    DFTG_TRY(sync_scalars(c));
+    if (exc) *exc = c->h_scal[kScalExc];
+    if (nelec) *nelec = c->h_scal[kScalNelec];
+    c->have_density = true;
+    c->have_hartree = false;
+    c->have_build = false;
+    return DFTG_OK;
+}
+
 int dftg_destroy(dftg_ctx *c)
 {
     free_ctx(c);
@@ -473,6 +677,7 @@ int dftg_set_density(dftg_ctx *c, const double *P)
 int dftg_correct_densities(dftg_ctx *c, double *scale)
 {
     CHECK_CTX(c);
+    if (c->points_only) { set_error("a point-set context has no atoms: no Hartree step or density correction"); return DFTG_ERR_STATE; }
     if (!c->have_density) { set_error("correct_densities before set_density"); return DFTG_ERR_STATE; }
     DFTG_CUDA(cudaSetDevice(c->device));
     DFTG_TRY(launch_atom_sums(c, kSumsCorrect));
@@ -497,6 +702,7 @@ int dftg_calculate_density(dftg_ctx *c, double *nelec)
 int dftg_calculate_hartree_potential(dftg_ctx *c, double *J)
 {
     CHECK_CTX(c);
+    if (c->points_only) { set_error("a point-set context has no atoms: no Hartree step or density correction"); return DFTG_ERR_STATE; }
     if (!c->have_density) { set_error("calculate_hartree_potential before set_density"); return DFTG_ERR_STATE; }
     DFTG_CUDA(cudaSetDevice(c->device));
     DFTG_TRY(launch_atom_sums(c, kSumsOnly));   // per-atom charges of the current rho
@@ -524,6 +730,7 @@ int dftg_calculate_xc(dftg_ctx *c, double *XC, double *exc)
 int dftg_fock_build_device(dftg_ctx *c, const double *P_dev, double *J_dev, double *XC_dev, double *scalars_dev)
 {
     CHECK_CTX(c);
+    if (c->points_only) { set_error("a point-set context has no atoms: no Hartree step or density correction"); return DFTG_ERR_STATE; }
     if (!P_dev) { set_error("P_dev NULL"); return DFTG_ERR_ARG; }
     DFTG_CUDA(cudaSetDevice(c->device));
     const size_t nn = (size_t)c->nbf * c->nbf;
@@ -547,6 +754,7 @@ int dftg_fock_build_profile(dftg_ctx *c, const double *P_dev, double *phase_ms, 
                             int *nphase)
 {
     CHECK_CTX(c);
+    if (c->points_only) { set_error("a point-set context has no atoms: no Hartree step"); return DFTG_ERR_STATE; }
     if (!P_dev || !phase_ms || !nphase) { set_error("NULL argument"); return DFTG_ERR_ARG; }
     DFTG_CUDA(cudaSetDevice(c->device));
     const size_t nn = (size_t)c->nbf * c->nbf;
@@ -579,6 +787,7 @@ int dftg_fock_build_profile(dftg_ctx *c, const double *P_dev, double *phase_ms, 
 int dftg_fock_build(dftg_ctx *c, const double *P, double *J, double *XC, double *exc, double *nelec)
 {
     CHECK_CTX(c);
+    if (c->points_only) { set_error("a point-set context has no atoms: no Hartree step or density correction"); return DFTG_ERR_STATE; }
     if (!P) { set_error("P NULL"); return DFTG_ERR_ARG; }
     DFTG_TRY(check_matrix(P, c->nbf));
     DFTG_CUDA(cudaSetDevice(c->device));
@@ -880,6 +1089,7 @@ extern "C" int dftg_batch_create(dftg_ctx *const *ctxs, int n, dftg_batch **out)
         for (int j = 0; j < i; ++j)
             if (ctxs[j] == ctxs[i]) { set_error("context %d repeated", i); return DFTG_ERR_ARG; }
         if (ctxs[i]->device != ctxs[0]->device) { set_error("contexts on different devices"); return DFTG_ERR_ARG; }
+        if (ctxs[i]->points_only) { set_error("context %d is a point-set context (no Fock build)", i); return DFTG_ERR_ARG; }
     }
     dftg_batch *b = new (std::nothrow) dftg_batch();
     if (!b) { set_error("host allocation failed"); return DFTG_ERR_NOMEM; }

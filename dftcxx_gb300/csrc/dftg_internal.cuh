@@ -239,8 +239,11 @@ struct dftg_ctx {
     int *d_bw_pairp = nullptr;    // [npairs] grid point of each sorted pair
     int *d_bw_binfirst = nullptr; // [natoms * nrad + 1] first task of each (atom, interval) bin
     double *d_bw_cpart = nullptr; // [ncross_tasks][nlm][4] transposed cross-atom partials
+    float *d_bw_prim32 = nullptr; // FP32 primitive exponents [nprim] then coefficients [nprim]
     bool have_build = false;      // a complete build left rho, V and the scalars on the device
     unsigned fwd_mask = 0;        // precision mask of that build (the backward follows it)
+
+    bool points_only = false;     // built from explicit points and function centres: no cells, no Hartree
 
     // call-order state
     bool have_density = false;

@@ -23,8 +23,9 @@
 // with w_p = w0_p wb_p and
 //   dE/dwb_p = w0_p (s_xc e_p + s_j rho_raw V / 2 + rho_p qbar_a / 2 - gamma rho_raw,p)
 //              + rho_p mbar_p / 2.
-// Every kernel here runs in FP64; per-atom force partials are reduced in a
-// fixed order (no floating-point atomics across blocks).
+// The FP64 kernels reduce per-atom force partials in a fixed order; the mixed
+// kernels (FP32 per point or pair, FP64 or compensated FP32 sums) are listed
+// below the FP64 ones.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -35,6 +36,15 @@ namespace dftg {
 
 constexpr int kBwBlock = 128;
 constexpr int kBwRed = 256;
+
+__global__ void k_bw_to_f32(int n, const double *__restrict__ a, const double *__restrict__ b, float *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        out[i] = (float)a[i];
+        out[n + i] = (float)b[i];
+    }
+}
 
 // pair (sorted place) -> grid point
 __global__ void k_bw_pairpoint(size_t npts, int natoms, int per_atom, const int *__restrict__ pos,
@@ -751,7 +761,7 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_becke_w(size_t npts, int per_at
         const double Ed = p < npts ? ewb[p] : 0.0;
         const bool live = Ed != 0.0;
         const T E = (T)Ed;
-        const int a = live ? (int)(p / per_atom) : 0;
+        const int a = live ? (int)p / per_atom : 0;
         const T vx = live ? (T)(X[p] - ax) : T(1), vy = live ? (T)(Yc[p] - ay) : T(0),
                 vz = live ? (T)(Zc[p] - az) : T(0);
         const T dB = act ? sqrt(vx * vx + vy * vy + vz * vz) : T(1);
@@ -775,9 +785,10 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_becke_w(size_t npts, int per_at
         const T iB = T(1) / dB;
         const T eBx = vx * iB, eBy = vy * iB, eBz = vz * iB;
         T Dx = T(0), Dy = T(0), Dz = T(0);
+        int k = B, src = B;   // k = B + t, src = B - t (mod n)
         for (int t = 1; t < n; ++t) {
-            const int k = act ? (B + t) % n : 0;
-            const int src = act ? (B - t + n) % n : 0;
+            k = k + 1 == n ? 0 : k + 1;
+            src = src == 0 ? n - 1 : src - 1;
             const T ekx = __shfl_sync(0xffffffffu, eBx, k, G), eky = __shfl_sync(0xffffffffu, eBy, k, G),
                     ekz = __shfl_sync(0xffffffffu, eBz, k, G);
             T hx = T(0), hy = T(0), hz = T(0);
@@ -1059,8 +1070,8 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_force_phi32(int nbf, int natoms
                                                              const int *__restrict__ bf_lmn,
                                                              const int *__restrict__ bf_off,
                                                              const int *__restrict__ bf_atom,
-                                                             const double *__restrict__ pa,
-                                                             const double *__restrict__ pcn, double *__restrict__ part)
+                                                             const float *__restrict__ pa,
+                                                             const float *__restrict__ pcn, double *__restrict__ part)
 {
     extern __shared__ double s_dd[];   // [4][natoms][3] doubles, [nbf][128] phi, [nbf][nbf4] P floats
     const int nbf4 = (nbf + 3) & ~3;
@@ -1128,8 +1139,8 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_force_phi32(int nbf, int natoms
             const int lx = bf_lmn[3 * mu], ly = bf_lmn[3 * mu + 1], lz = bf_lmn[3 * mu + 2];
             float s0 = 0.f, s1 = 0.f;
             for (int k = bf_off[mu]; k < bf_off[mu + 1]; ++k) {
-                const float al = (float)pa[k];
-                const float ek = (float)pcn[k] * expf(-al * r2);
+                const float al = pa[k];
+                const float ek = pcn[k] * expf(-al * r2);
                 s0 += ek;
                 s1 = fmaf(al, ek, s1);
             }
@@ -1189,6 +1200,10 @@ static int bw_alloc(dftg_ctx *c)
     DFTG_CUDA(cudaMalloc(&c->d_bw_lm, sizeof(double) * (2 * rplane + na + 8 + nred)));
     DFTG_CUDA(cudaMalloc(&c->d_bw_fpart, sizeof(double) * rows * na * 3));
     if (!c->d_bw_out) DFTG_CUDA(cudaMalloc(&c->d_bw_out, sizeof(double) * ((size_t)c->nbf * c->nbf + (size_t)na * 3)));
+    DFTG_CUDA(cudaMalloc(&c->d_bw_prim32, sizeof(float) * 2 * (size_t)std::max(1, c->nprim)));
+    k_bw_to_f32<<<(unsigned)((c->nprim + 255) / 256 + 1), 256, 0, c->stream>>>(c->nprim, c->d_pa, c->d_pcn,
+                                                                               c->d_bw_prim32);
+    DFTG_LAUNCH_CHECK();
     DFTG_CUDA(cudaMalloc(&c->d_bw_counter, sizeof(int)));
     DFTG_CUDA(cudaMemsetAsync(c->d_bw_counter, 0, sizeof(int), c->stream));
     if (c->npairs > 0) {
@@ -1302,7 +1317,7 @@ int launch_backward(dftg_ctx *c, double sxc, double sj, double *dEdP_dev, double
             k_bw_force_phi32<<<c->bw_nb_phi, kBwBlock, smp, c->stream>>>(c->nbf, na, c->npts, np, per_atom, c->d_phi32,
                                                                          c->d_P, h, c->d_x, c->d_y, c->d_z, c->d_atoms,
                                                                          c->d_bf_lmn, c->d_bf_off, c->d_bf_atom,
-                                                                         c->d_pa, c->d_pcn, fp);
+                                                                         c->d_bw_prim32, c->d_bw_prim32 + c->nprim, fp);
         } else {
             const size_t smp = sizeof(double) * ((size_t)c->nbf * kBwBlock + 4 * (size_t)na * 3);
             if (smp > 227 * 1024) {

@@ -268,11 +268,14 @@ int launch_density(dftg_ctx *c)
 // correction factor and rescaled charges only; the LDA kernel rescales rho.
 int launch_atom_sums(dftg_ctx *c, int mode)
 {
-    const size_t per_atom = (size_t)c->nrad * c->nang;
+    // a point-set context has one cell (all points) and no density correction
+    if (c->points_only) mode = kSumsOnly;
+    const int ncell = c->points_only ? 1 : c->natoms;
+    const size_t per_atom = c->points_only ? c->npts : (size_t)c->nrad * c->nang;
     const int cpa = (int)((per_atom + kRedChunk - 1) / kRedChunk);
-    const int nb = cpa * c->natoms;
+    const int nb = cpa * ncell;
     int *cnt = c->d_counters + kCntAtoms;
-    k_atom_sums<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, c->natoms, c->d_w, c->d_rho, c->d_red, c->d_atoms,
+    k_atom_sums<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, ncell, c->d_w, c->d_rho, c->d_red, c->d_atoms,
                                                  c->d_scal, mode == kSumsOnly ? 1 : 0, cnt);
     DFTG_LAUNCH_CHECK();
     if (mode == kSumsCorrect) {

@@ -205,6 +205,7 @@ extern "C" int dftg_one_electron(dftg_ctx *c, double *S, double *T, double *V)
 {
     using namespace dftg;
     if (!c) { set_error("null context"); return DFTG_ERR_ARG; }
+    if (c->points_only) { set_error("a point-set context has no nuclei"); return DFTG_ERR_STATE; }
     DFTG_CUDA(cudaSetDevice(c->device));
     const size_t nn = (size_t)c->nbf * c->nbf;
     if (!c->d_ints_work) DFTG_CUDA(cudaMalloc(&c->d_ints_work, 3 * nn * sizeof(double)));

@@ -266,6 +266,48 @@ class DFT:
         return self.et
 
 
+class PointGrid(MolecularGrid):
+    """Explicit points and weights with functions about explicit centres (no
+    atoms, cells or Hartree step): amplitudes, density, LDA point kernel and
+    the XC contraction (dftg_create_points).  The MolecularGrid getters,
+    precision and launch-shape calls apply."""
+
+    def __init__(self, xyz, w, centres, bf_centre, bf_lmn, bf_nprim, prim_alpha, prim_coef, precision="fp64",
+                 device=0):
+        L = _lib.load()
+        self.mol = None
+        self._arrays = [np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3),
+                        np.ascontiguousarray(w, dtype=np.float64),
+                        np.ascontiguousarray(centres, dtype=np.float64).reshape(-1, 3),
+                        np.ascontiguousarray(bf_centre, dtype=np.int32),
+                        np.ascontiguousarray(bf_lmn, dtype=np.int32).reshape(-1, 3),
+                        np.ascontiguousarray(bf_nprim, dtype=np.int32),
+                        np.ascontiguousarray(prim_alpha, dtype=np.float64),
+                        np.ascontiguousarray(prim_coef, dtype=np.float64)]
+        X, W, C, bc, bl, bn, pa, pc = self._arrays
+        ip = ctypes.POINTER(ctypes.c_int)
+        zeros = np.zeros(len(C), dtype=np.int32)
+        self._arrays.append(zeros)
+        pts = _lib.Points(len(W), _ptr(X), _ptr(W))
+        m = _lib.Molecule(len(C), zeros.ctypes.data_as(ip), _ptr(C))
+        b = _lib.Basis(len(bc), bc.ctypes.data_as(ip), bl.ctypes.data_as(ip), bn.ctypes.data_as(ip), _ptr(pa),
+                       _ptr(pc))
+        h = ctypes.c_void_p()
+        check(L.dftg_create_points(ctypes.byref(pts), ctypes.byref(m), ctypes.byref(b), int(device), ctypes.byref(h)))
+        self._h = h
+        self.grid_size = len(W)
+        self.nbf = len(bc)
+        self.set_precision(precision)
+
+    def xc_build(self, P):
+        """rho, LDA and XC at fixed P: {"XC", "Exc", "nelec"}."""
+        P = np.asfortranarray(P, dtype=np.float64)
+        XC = np.zeros((self.nbf, self.nbf), order="F")
+        e, n = ctypes.c_double(), ctypes.c_double()
+        check(_lib.load().dftg_xc_build(self._h, _ptr(P), _ptr(XC), ctypes.byref(e), ctypes.byref(n)))
+        return {"XC": np.ascontiguousarray(XC), "Exc": e.value, "nelec": n.value}
+
+
 class Batch:
     """Many MolecularGrid contexts built in one launch (dftg_batch_*): the
     per-build kernel sequences are captured into one CUDA graph with a stream

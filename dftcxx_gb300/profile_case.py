@@ -1,12 +1,14 @@
 """Run a few device-resident grid Fock builds of one workload, for profilers.
 
-    python -m dftcxx_gb300.profile_case [--workload benzene|h2o] [--precision mixed|fp64] [--builds N]
+    python -m dftcxx_gb300.profile_case [--workload benzene|h2o|decane] [--precision mixed|fp64] [--builds N]
+                                        [--backward N]
 
 Builds the grid (setup kernels), forms the core-Hamiltonian density from the
 device one-electron integrals, then runs N builds through
-dftg_fock_build_device on the context's stream and synchronises.  Nothing
-else runs on the GPU, so a profiler sees the setup launches followed by N
-identical builds.
+dftg_fock_build_device on the context's stream and synchronises; with
+--backward N, N backward passes (dE/dP and forces) of the last build follow.
+Nothing else runs on the GPU, so a profiler sees the setup launches followed
+by N identical builds (and the backward passes).
 """
 import argparse
 import ctypes
@@ -17,21 +19,25 @@ import numpy as np
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="benzene", choices=["benzene", "h2o"])
+    ap.add_argument("--workload", default="benzene", choices=["benzene", "h2o", "decane"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--builds", type=int, default=2)
+    ap.add_argument("--backward", type=int, default=0)
     args = ap.parse_args(argv)
 
     import torch
     from . import _lib
     from .build import build
     from .grid import MolecularGrid
-    from .molecule import Molecule, benzene, h2o
+    from .molecule import Molecule, alkane, benzene, h2o
 
     build()
     if args.workload == "benzene":
         Z, xyz = benzene()
         mol, grid = Molecule(Z, xyz, "p631"), (75, 11, 8)
+    elif args.workload == "decane":
+        Z, xyz = alkane(10)
+        mol, grid = Molecule(Z, xyz, "p631"), (50, 10, 8)
     else:
         Z, xyz = h2o()
         mol, grid = Molecule(Z, xyz, "sto3g"), (32, 7, 8)
@@ -51,6 +57,11 @@ def main(argv=None):
     for _ in range(args.builds):
         _lib.check(L.dftg_fock_build_device(g.handle, ctypes.c_void_p(dP.data_ptr()), ctypes.c_void_p(dJ.data_ptr()),
                                             ctypes.c_void_p(dXC.data_ptr()), ctypes.c_void_p(dS.data_ptr())))
+    gP = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+    gR = torch.zeros(3 * mol.natoms, dtype=torch.float64, device="cuda")
+    for _ in range(args.backward):
+        _lib.check(L.dftg_backward_device(g.handle, 1.0, 1.0, ctypes.c_void_p(gP.data_ptr()),
+                                          ctypes.c_void_p(gR.data_ptr())))
     torch.cuda.synchronize()
     e = g.energies()
     print("builds %d  npts %d  nbf %d  Exc %.10f  EJ %.10f  N %.10f" % (args.builds, g.grid_size, n, e["Exc"], e["EJ"],

@@ -145,6 +145,30 @@ int dftg_get_energies(dftg_ctx *ctx, double *exc, double *ej, double *nelec);
 int dftg_fock_build_profile(dftg_ctx *ctx, const double *P_dev, double *phase_ms,
                             const char **names, int cap, int *nphase);
 
+/* Point-set context (no counterpart in the reference): the amplitude, density,
+ * LDA and XC steps on explicit points with explicit weights, for contraction
+ * workloads without a molecular grid.  centres->xyz gives the function centres
+ * (bf_atom indexes them; centres->Z is ignored).  Such a context supports
+ * dftg_set_density (rho = 2 phi^T P phi, no density correction),
+ * dftg_calculate_density, dftg_calculate_xc, dftg_xc_build*, the getters and
+ * the launch-shape calls; calls that need nuclei or the Hartree step return
+ * DFTG_ERR_STATE. */
+typedef struct {
+    size_t npts;
+    const double *xyz;     /* [npts][3] bohr */
+    const double *w;       /* [npts] quadrature weights */
+} dftg_points;
+int dftg_create_points(const dftg_points *pts, const dftg_molecule *centres, const dftg_basis *basis, int device,
+                       dftg_ctx **ctx);
+
+/* rho, the LDA point kernel and XC = phi^T diag(w v_xc) phi in one call, on any
+ * context, without the density correction (DFT::calculate_exchange_correlation_matrix,
+ * dft.cpp:394-433, for a fixed rho).  XC may be NULL; exc and nelec (the
+ * integral of w rho) may be NULL.  The device form writes scalars_dev[0] = E_xc,
+ * [1] = the integral, and does not synchronise. */
+int dftg_xc_build(dftg_ctx *ctx, const double *P, double *XC, double *exc, double *nelec);
+int dftg_xc_build_device(dftg_ctx *ctx, const double *P_dev, double *XC_dev, double *scalars_dev);
+
 /* Getters (copies): MolecularGrid::get_weights / get_densities /
  * get_amplitudes (moleculargrid.cpp:61-127).  cap is the element capacity of
  * out.  Amplitudes are nbf x npts column-major (the reference's layout). */

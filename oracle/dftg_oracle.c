@@ -944,3 +944,76 @@ int orc_num_threads(void)
     return 1;
 #endif
 }
+
+/* ------------------------------------------------ explicit-point XC step */
+
+/*
+ * The XC step on explicit points with explicit weights (no atoms, cells or
+ * density correction), for the synthetic contraction workload:
+ *   phi_i(p)  contracted Cartesian Gaussians about centre bf_centre[i]
+ *             (cgf.cpp:49-57, 102-114, 146-154),
+ *   rho_p     = 2 phi_p^T P phi_p (gridpoint.cpp:82-84),
+ *   e_p, v_p  Slater + VWN (functionals.cpp:24-158, orc_lda_point),
+ *   XC_ij     = sum_p w_p v_p phi_i(p) phi_j(p) (dft.cpp:424-432),
+ * returning E_xc = sum_p w_p e_p.  rho_out [npts] and XC [nbf][nbf] (full
+ * square) may be NULL.  Points run in parallel (OpenMP); the XC sums take
+ * every stride-th point and scale by the stride (stride 1: exact).
+ */
+double orc_points_xc(long npts, const double *xyz, const double *w, int nbf, const double *centres,
+                     const int *bf_centre, const int *lmn, const int *nprim, const double *alpha,
+                     const double *coef, const double *P, int stride, double *rho_out, double *XC)
+{
+    int *off = malloc(sizeof(int) * (nbf + 1));
+    off[0] = 0;
+    for (int i = 0; i < nbf; ++i) off[i + 1] = off[i] + nprim[i];
+    double *pcn = malloc(sizeof(double) * off[nbf]);
+    for (int i = 0; i < nbf; ++i)
+        for (int k = off[i]; k < off[i + 1]; ++k)
+            pcn[k] = coef[k] * orc_gto_norm(alpha[k], lmn[3 * i], lmn[3 * i + 1], lmn[3 * i + 2]);
+    if (stride < 1) stride = 1;
+    const long ns = (npts + stride - 1) / stride;
+    double *wv = malloc(sizeof(double) * ns);
+    double *phis = malloc(sizeof(double) * (size_t)ns * nbf);
+    double exc = 0.0;
+    #pragma omp parallel for schedule(static) reduction(+ : exc)
+    for (long s = 0; s < ns; ++s) {
+        const long p = s * stride;
+        double *phi = phis + (size_t)s * nbf;
+        for (int i = 0; i < nbf; ++i) {
+            const double *c = centres + 3 * bf_centre[i];
+            const int *q = lmn + 3 * i;
+            double dx = xyz[3 * p] - c[0], dy = xyz[3 * p + 1] - c[1], dz = xyz[3 * p + 2] - c[2];
+            double r2 = dx * dx + dy * dy + dz * dz, v = 0.0;
+            for (int k = off[i]; k < off[i + 1]; ++k)
+                v += pcn[k] * ipow(dx, q[0]) * ipow(dy, q[1]) * ipow(dz, q[2]) * exp(-alpha[k] * r2);
+            phi[i] = v;
+        }
+        double rho = 0.0;
+        for (int i = 0; i < nbf; ++i) {
+            double t = 0.0;
+            for (int j = 0; j < nbf; ++j) t += P[(size_t)i * nbf + j] * phi[j];
+            rho += phi[i] * t;
+        }
+        rho *= 2.0;
+        if (rho_out) rho_out[p] = rho;
+        double e, v;
+        orc_lda_point(rho, &e, &v);
+        exc += w[p] * e * stride;
+        wv[s] = w[p] * v * stride;
+    }
+    if (XC) {
+        #pragma omp parallel for schedule(dynamic)
+        for (int i = 0; i < nbf; ++i)
+            for (int j = i; j < nbf; ++j) {
+                double sum = 0.0;
+                for (long s = 0; s < ns; ++s) sum += wv[s] * phis[(size_t)s * nbf + i] * phis[(size_t)s * nbf + j];
+                XC[(size_t)i * nbf + j] = sum;
+                XC[(size_t)j * nbf + i] = sum;
+            }
+    }
+    free(phis);
+    free(wv);
+    free(pcn);
+    free(off);
+    return exc;
+}

@@ -66,6 +66,9 @@ def lib():
         L.orc_gto_norm.restype = ctypes.c_double
         L.orc_gto_norm.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.orc_poisson_matrix.argtypes = [ctypes.c_int, _dp, _dp]
+        L.orc_points_xc.restype = ctypes.c_double
+        L.orc_points_xc.argtypes = [ctypes.c_long, _dp, _dp, ctypes.c_int, _dp, _ip, _ip, _ip, _dp, _dp, _dp,
+                                    ctypes.c_int, _dp, _dp]
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_set_sample_stride.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_get_timings.argtypes = [ctypes.c_void_p, _dp]
@@ -259,3 +262,24 @@ def scf(grid, max_iter=100, tol=1e-8, min_iter=3, alpha=0.5):
         if it >= max_iter:
             break
     return hist, {"S": S, "T": T, "V": Vn, "H": H, "enuc": enuc}
+
+
+def points_xc(xyz, w, centres, bf_centre, lmn, nprim, alpha, coef, P, stride=1, want_rho=True, want_xc=True):
+    """Explicit-point XC step (orc_points_xc): returns (E_xc, rho, XC)."""
+    L = lib()
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    centres = np.ascontiguousarray(centres, dtype=np.float64)
+    bc = np.ascontiguousarray(bf_centre, dtype=np.int32)
+    lmn = np.ascontiguousarray(lmn, dtype=np.int32)
+    nprim = np.ascontiguousarray(nprim, dtype=np.int32)
+    alpha = np.ascontiguousarray(alpha, dtype=np.float64)
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    n, nbf = len(w), len(bc)
+    rho = np.zeros(n) if want_rho else None
+    XC = np.zeros((nbf, nbf)) if want_xc else None
+    e = L.orc_points_xc(n, _p(xyz), _p(w), nbf, _p(centres), _p(bc, _ip), _p(lmn, _ip), _p(nprim, _ip), _p(alpha),
+                        _p(coef), _p(P), int(stride), _p(rho) if rho is not None else None,
+                        _p(XC) if XC is not None else None)
+    return e, rho, XC

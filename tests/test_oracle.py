@@ -241,3 +241,32 @@ def test_oracle_scf_golden(oracle_mod):
     assert np.abs(np.array([h["E"] for h in hist]) - gold["E"]).max() < 1e-9
     assert abs(mats["enuc"] - gold["enuc"]) < 1e-12
     assert abs(hist[-1]["nelec"] - 10.0) < 1e-9
+
+
+def test_points_xc_matches_numpy(oracle_mod):
+    """Explicit-point XC step of the oracle against a numpy restatement on a
+    small synthetic set: amplitudes from the normalised primitives, rho =
+    2 phi^T P phi, the oracle's LDA point function, XC = phi^T diag(w v) phi."""
+    from dftcxx_gb300.molecule import synthetic_contraction
+    pts, w, lmn, alpha, centres, P = synthetic_contraction(npts=400, nbf=10, nocc=3, box=6.0)
+    nbf = len(alpha)
+    L = oracle_mod.lib()
+    phi = np.zeros((len(w), nbf))
+    for i in range(nbf):
+        d = pts - centres[i]
+        norm = L.orc_gto_norm(float(alpha[i]), int(lmn[i, 0]), int(lmn[i, 1]), int(lmn[i, 2]))
+        phi[:, i] = norm * d[:, 0] ** lmn[i, 0] * d[:, 1] ** lmn[i, 1] * d[:, 2] ** lmn[i, 2] * \
+            np.exp(-alpha[i] * (d * d).sum(axis=1))
+    rho = 2.0 * np.einsum("pi,ij,pj->p", phi, P, phi)
+    e = np.zeros(len(w))
+    v = np.zeros(len(w))
+    ex, vx = ctypes.c_double(), ctypes.c_double()
+    for p in range(len(w)):
+        L.orc_lda_point(float(rho[p]), ctypes.byref(ex), ctypes.byref(vx))
+        e[p], v[p] = ex.value, vx.value
+    XC = phi.T @ (phi * (w * v)[:, None])
+    got_e, got_rho, got_xc = oracle_mod.points_xc(pts, w, centres, np.arange(nbf), lmn, np.ones(nbf, np.int32), alpha,
+                                                  np.ones(nbf), P)
+    np.testing.assert_allclose(got_rho, rho, rtol=1e-13, atol=1e-300)
+    assert abs(got_e - float(w @ e)) <= 1e-12 * abs(float(w @ e))
+    np.testing.assert_allclose(got_xc, XC, rtol=1e-12, atol=1e-14 * np.abs(XC).max())
