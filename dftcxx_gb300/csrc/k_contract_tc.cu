@@ -7,14 +7,14 @@
 //   A = phi                         rows mu < nbf of M = 128
 //   B = [c_xc o phi ; c_j o phi]    rows n < 2 nbf of N = NP (2 nbf rounded up to 16)
 //
-// Number format (per point chunk of at most 256 points).  Row mu of A is scaled
+// Number format (per point chunk of at most 512 points).  Row mu of A is scaled
 // by 2^(7 - e_mu), e_mu the exponent bound of max |phi_mu| over the chunk, and
 // split into three BF16 slices: a_1 = rint(x) (an integer, |a_1| <= 128),
 // a_2 = bf16(x - a_1), a_3 = bf16(x - a_1 - a_2).  B row nu is scaled by
 // 2^(7 - s_nu - v), s_nu the bound of max |w phi_nu| over the chunk (fixed for
 // the grid) and v the bound of max |c / w| (per build), and split likewise.  The
 // leading products a_1 b_1 are integers below 2^14, so their sum over a chunk
-// (< 2^22) is exact in the FP32 accumulator whatever the accumulator's
+// (< 2^23) is exact in the FP32 accumulator whatever the accumulator's
 // rounding; the five correction products (a_1 b_2, a_2 b_1, a_1 b_3, a_2 b_2,
 // a_3 b_1) go to a second accumulator, about 2^-8 of the first.  The epilogue
 // scales D_hi and D_lo back by exact powers of two and adds them to the CTA's
@@ -23,14 +23,15 @@
 // sums the CTA partials in FP64 in a fixed order and symmetrises.  A (phi is fixed for the grid) is sliced once at setup into HBM
 // in the shared-memory operand layout; B is formed every build from A and c.
 //
-// CTA (persistent over chunks, 448 threads):
-//   warps 0-3  producers: warp w builds the B slices of the stages in ring slots
-//              w, w + 4, ... from the A slices and c values of the stage (shared
-//              memory), then a proxy fence and an mbarrier arrive;
-//   warp 4     TMEM owner and MMA issuer (one thread);
-//   warps 5-12 epilogue: TMEM -> FP64 partial (TMEM lane quarter = warp % 4,
-//              alternate 16-column blocks for the two warps of a quarter);
-//   warp 13    loader: bulk copies of the A slices and c values of each stage.
+// CTA (persistent over chunks, 576 threads):
+//   warps 0-7  producers: every warp builds its rows (w, w + 8, ... in groups
+//              of eight) of the B slices of every stage from the A slices and
+//              c values of the stage (shared memory), then a proxy fence and an
+//              mbarrier arrive (the stage's full barrier counts eight);
+//   warp 8     TMEM owner and MMA issuer (one thread);
+//   warps 9-16 epilogue: TMEM -> double-float partial (TMEM lane quarter =
+//              warp % 4, alternate 16-column blocks for the two warps of a quarter);
+//   warp 17    loader: bulk copies of the A slices and c values of each stage.
 // Every mbarrier wait is bounded: on expiry the CTA records an error code, lets
 // its copies and MMAs complete, frees TMEM and exits.
 #include <cuda_bf16.h>
@@ -44,10 +45,13 @@ constexpr int kCtKS = 32;                  // points per stage
 constexpr int kCtKcores = kCtKS / 8;       // core matrices along K per stage
 constexpr int kCtM = 128;
 constexpr int kCtMaxNbf = 128;             // 2 nbf <= 256 columns per accumulator
-constexpr int kCtThreads = 448;
-constexpr int kCtLoaderWarp = 13;
+constexpr int kCtProducers = 8;           // producer warps 0..7
+constexpr int kCtMmaWarp = kCtProducers;   // TMEM owner and MMA issuer
+constexpr int kCtEpi0 = kCtMmaWarp + 1;    // epilogue warps kCtEpi0 .. kCtEpi0 + 7
+constexpr int kCtThreads = (kCtEpi0 + 9) * 32;
+constexpr int kCtLoaderWarp = kCtEpi0 + 8;
 constexpr int kCtMaxStages = 8;
-constexpr int kCtMaxKbPerChunk = 8;        // <= 256 points per exact integer accumulation
+constexpr int kCtMaxKbPerChunk = 16;       // <= 512 points per exact integer accumulation (sums < 2^23)
 constexpr uint32_t kCtTmemCols = 512;      // D_hi at column 0, D_lo at column 256
 constexpr int kCtSlices = 3;
 constexpr int kCtExpMin = -100;            // exponent bounds are clamped to [-100, 100]
@@ -194,7 +198,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
     if (threadIdx.x == 0) {
         for (int s = 0; s < nst; ++s) {
             mbar_init(&sh->a_full[s], 1);
-            mbar_init(&sh->full[s], 4);          // the four producer warps
+            mbar_init(&sh->full[s], kCtProducers);   // every producer warp
             mbar_init(&sh->empty[s], 1);
         }
         mbar_init(&sh->tmem_full, 1);
@@ -203,7 +207,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
         sh->fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 4) {
+    if (warp == kCtMmaWarp) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem_base)),
                      "r"(kCtTmemCols)
                      : "memory");
@@ -214,9 +218,9 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
     tc_fence_after();
     const uint32_t tmem = sh->tmem_base;
 
-    if (warp < 4) {
+    if (warp < kCtProducers) {
         // ------------------------------------------------------------ producers
-        // all four warps fill every stage: warp w takes row groups w, w + 4, ...;
+        // all producer warps fill every stage: warp w takes row groups w, w + 8, ...;
         // lane = (row within the group of 8) x (8-point group g)
         const int g = lane & 3, mrow = lane >> 2;
         int it = 0;
@@ -226,12 +230,12 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
             const int2 ce = cexp[ch];
             const float sx = pow2f(-ce.x), sj = pow2f(-ce.y);
             // B row scales of this lane's rows for the chunk, in registers
-            float rfr[kCtMaxNbf / 32];
+            float rfr[kCtMaxNbf / (8 * kCtProducers)];
             {
                 const int *ea = rowexp + (size_t)ch * nbf, *es = swexp + (size_t)ch * nbf;
 #pragma unroll
-                for (int j = 0; j < kCtMaxNbf / 32; ++j) {
-                    const int mu = 32 * j + 8 * warp + mrow;
+                for (int j = 0; j < kCtMaxNbf / (8 * kCtProducers); ++j) {
+                    const int mu = 8 * kCtProducers * j + 8 * warp + mrow;
                     rfr[j] = mu < nbf ? pow2f(max(-126, min(127, ea[mu] - es[mu]))) : 0.f;
                 }
             }
@@ -256,10 +260,11 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                 }
                 // all slice loads of this lane's rows first, then the arithmetic
                 // (predicated, no early exit, so the rows interleave)
-                uint4 q0[kCtMaxNbf / 32], q1[kCtMaxNbf / 32], q2[kCtMaxNbf / 32];
+                uint4 q0[kCtMaxNbf / (8 * kCtProducers)], q1[kCtMaxNbf / (8 * kCtProducers)],
+                    q2[kCtMaxNbf / (8 * kCtProducers)];
 #pragma unroll
-                for (int j = 0; j < kCtMaxNbf / 32; ++j) {
-                    const int mu = 32 * j + 8 * warp + mrow;
+                for (int j = 0; j < kCtMaxNbf / (8 * kCtProducers); ++j) {
+                    const int mu = 8 * kCtProducers * j + 8 * warp + mrow;
                     if (mu < nbf) {
                         const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
                         q0[j] = *reinterpret_cast<const uint4 *>(sA + oa);
@@ -268,8 +273,8 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                     }
                 }
 #pragma unroll
-                for (int j = 0; j < kCtMaxNbf / 32; ++j) {
-                    const int mu = 32 * j + 8 * warp + mrow;
+                for (int j = 0; j < kCtMaxNbf / (8 * kCtProducers); ++j) {
+                    const int mu = 8 * kCtProducers * j + 8 * warp + mrow;
                     if (mu < nbf) {
                         const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
                         // B row scale: phi 2^(7 - e_mu) -> phi 2^(7 - s_mu)
@@ -304,7 +309,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                 if (lane == 0) mbar_arrive(&sh->full[s]);
             }
         }
-    } else if (warp == 4) {
+    } else if (warp == kCtMmaWarp) {
         // ------------------------------------------------------------ MMA issuer
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(kCtM, NP);
@@ -361,7 +366,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
     } else if (warp < kCtLoaderWarp) {
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3;                  // TMEM lane quarter of this warp
-        const int h = (warp - 5) >> 2;           // column blocks h, h + 2, ...
+        const int h = (warp - kCtEpi0) >> 2;     // column blocks h, h + 2, ...
         const int r = q * 32 + lane;             // accumulator row = basis function mu
         float2 *gpart = part + (size_t)blockIdx.x * 2 * ntri;   // this CTA's partial in HBM
         float2 *px = spart ? s_part : gpart;
@@ -372,7 +377,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
             {
                 const int2 ce = cexp[ch];
                 const int *es = swexp + (size_t)ch * nbf;
-                for (int n = threadIdx.x - 160; n < 2 * nbf; n += 256) {
+                for (int n = threadIdx.x - 32 * kCtEpi0; n < 2 * nbf; n += 256) {
                     const int nu = n < nbf ? n : n - nbf;
                     const int e = es[nu] + (n < nbf ? ce.x : ce.y) - 14;
                     s_colf[n] = pow2f(max(-126, min(127, e)));
@@ -396,42 +401,46 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                 tmem_wait_ld();
                 if (r < nbf) {
                     // (s, e) += (D_hi + D_lo) 2^(e_mu + s_nu + v - 14) for the upper-triangle
-                    // elements of the block: column tables and old values first, then the
-                    // arithmetic, then the stores, so no access waits on another
+                    // elements of the block, eight columns at a time: column tables and
+                    // old values first, then the arithmetic, then the stores, so no
+                    // access waits on another
                     const int kend = min(16, 2 * nbf - c0);
-                    int off[16];
-                    float fk[16];
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) {
-                        const bool v = k < kend && r <= s_colnu[c0 + k];
-                        off[k] = v ? s_coloff[c0 + k] + r : -1;
-                        fk[k] = v ? s_colf[c0 + k] * fr : 0.f;   // exact power of two
+                    for (int hh = 0; hh < 16; hh += 8) {
+                        int off[8];
+                        float fk[8];
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            const bool v = hh + k < kend && r <= s_colnu[c0 + hh + k];
+                            off[k] = v ? s_coloff[c0 + hh + k] + r : -1;
+                            fk[k] = v ? s_colf[c0 + hh + k] * fr : 0.f;   // exact power of two
+                        }
+                        float2 old[8];
+#pragma unroll
+                        for (int k = 0; k < 8; ++k)
+                            old[k] = (cc > 0 && off[k] >= 0) ? px[off[k]] : make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            const float vh = dh[hh + k] * fk[k], vl = dl[hh + k] * fk[k];
+                            float s2 = old[k].x, e2 = old[k].y;
+                            const float t = s2 + vh;
+                            const float bp = t - s2;
+                            e2 += (s2 - (t - bp)) + (vh - bp) + vl;
+                            s2 = t + e2;                             // renormalise: |e| <= ulp(s) / 2
+                            old[k] = make_float2(s2, e2 - (s2 - t));
+                        }
+#pragma unroll
+                        for (int k = 0; k < 8; ++k)
+                            if (off[k] >= 0) px[off[k]] = old[k];
                     }
-                    float2 old[16];
-#pragma unroll
-                    for (int k = 0; k < 16; ++k)
-                        old[k] = (cc > 0 && off[k] >= 0) ? px[off[k]] : make_float2(0.f, 0.f);
-#pragma unroll
-                    for (int k = 0; k < 16; ++k) {
-                        const float vh = dh[k] * fk[k], vl = dl[k] * fk[k];
-                        float s2 = old[k].x, e2 = old[k].y;
-                        const float t = s2 + vh;
-                        const float bp = t - s2;
-                        e2 += (s2 - (t - bp)) + (vh - bp) + vl;
-                        s2 = t + e2;                                 // renormalise: |e| <= ulp(s) / 2
-                        old[k] = make_float2(s2, e2 - (s2 - t));
-                    }
-#pragma unroll
-                    for (int k = 0; k < 16; ++k)
-                        if (off[k] >= 0) px[off[k]] = old[k];
                 }
             }
             tc_fence_before();
             ct_epi_bar();                        // all TMEM reads of this chunk are done
-            if (threadIdx.x == 160) mbar_arrive(&sh->tmem_empty);
+            if (threadIdx.x == 32 * kCtEpi0) mbar_arrive(&sh->tmem_empty);
         }
         if (spart && !sh->fail) {
-            for (size_t i = threadIdx.x - 160; i < 2 * ntri; i += 256) gpart[i] = s_part[i];
+            for (size_t i = threadIdx.x - 32 * kCtEpi0; i < 2 * ntri; i += 256) gpart[i] = s_part[i];
         }
     } else {
         // ------------------------------------------------------------ loader
@@ -473,7 +482,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 4) {
+    if (warp == kCtMmaWarp) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCtTmemCols) : "memory");
     }

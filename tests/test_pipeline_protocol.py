@@ -1,11 +1,11 @@
 """Model of the mbarrier protocol of the tensor-core contraction kernel
 (dftcxx_gb300/csrc/k_contract_tc.cu), checked on the CPU under random
-schedules: ring slots with a loader (A slices), four producer warps (B
-slices), one MMA issuer and the epilogue.  A wait passes when the phase of the
+schedules: ring slots with a loader (A slices), producer warps (B slices;
+eight in the kernel), one MMA issuer and the epilogue.  A wait passes when the phase of the
 given parity has completed, as mbarrier.try_wait.parity does (a fresh barrier
 counts its preceding phase as complete).  In the kernel every producer warp
-fills its rows of every stage and the stage-full barrier expects four
-arrivals; each waiter then sees each slot's phases strictly in order, which
+fills its rows of every stage and the stage-full barrier expects one
+arrival per producer warp; each waiter then sees each slot's phases strictly in order, which
 keeps every stage's data consistent for every ring depth.  Splitting stages
 between warps round-robin instead ("stage % 4") breaks rings shorter than the
 number of warps: a warp then waits on a parity whose preceding phase counts as
@@ -31,7 +31,7 @@ class _Bar:
         return (self.ph & 1) != parity
 
 
-def _run(nst, chunks, owner, seed, per_stage=1):
+def _run(nst, chunks, owner, seed, per_stage=1, nwarps=4):
     """owner(it, s) -> the producing warp of stage it, or None when all
     per_stage warps produce every stage (full barrier count per_stage)."""
     rng = random.Random(seed)
@@ -40,7 +40,7 @@ def _run(nst, chunks, owner, seed, per_stage=1):
     empty = [_Bar() for _ in range(nst)]
     tmem_full, tmem_empty = _Bar(), _Bar()
     a_in = [None] * nst
-    b_in = [[None] * 4 for _ in range(nst)]
+    b_in = [[None] * nwarps for _ in range(nst)]
     ns = sum(chunks)
 
     def loader():
@@ -61,7 +61,7 @@ def _run(nst, chunks, owner, seed, per_stage=1):
                 yield
             if a_in[s] != it:
                 raise AssertionError("producer %d read stage %s for %d" % (w, a_in[s], it))
-            for part in range(4):
+            for part in range(nwarps):
                 if owner is None and part != w:
                     continue
                 b_in[s][part] = it
@@ -91,7 +91,7 @@ def _run(nst, chunks, owner, seed, per_stage=1):
             yield
             tmem_empty.arrive()
 
-    alive = [loader(), mma(), epilogue()] + [producer(w) for w in range(4)]
+    alive = [loader(), mma(), epilogue()] + [producer(w) for w in range(nwarps)]
     steps = 0
     while alive:
         a = rng.choice(alive)
@@ -104,11 +104,12 @@ def _run(nst, chunks, owner, seed, per_stage=1):
             raise AssertionError("no progress")
 
 
+@pytest.mark.parametrize("nwarps", [4, 8])
 @pytest.mark.parametrize("nst", [2, 3, 4, 5, 6, 8])
 @pytest.mark.parametrize("chunks", [[8] * 7, [8] * 6 + [3], [1, 1, 2], [5]])
-def test_all_warps_per_stage_keep_stages_consistent(nst, chunks):
+def test_all_warps_per_stage_keep_stages_consistent(nst, chunks, nwarps):
     for seed in range(20):
-        _run(nst, chunks, None, seed, per_stage=4)
+        _run(nst, chunks, None, seed, per_stage=nwarps, nwarps=nwarps)
 
 
 @pytest.mark.parametrize("nst", [2, 3, 4, 8])
