@@ -940,8 +940,8 @@ int dftg_set_launch_shape(dftg_ctx *c, const int *shape, int n)
     }
     if (c->ct_ready) {
         if (shape[1] < 1 || shape[1] > c->ct_grid_max) { set_error("contraction CTAs %d outside 1..%d", shape[1], c->ct_grid_max); return DFTG_ERR_ARG; }
-        if (shape[2] < c->ct_nst_min || shape[2] > c->ct_nst_max) {
-            set_error("contraction stages %d outside %d..%d", shape[2], c->ct_nst_min, c->ct_nst_max);
+        if (shape[2] < c->ct_nst_min || shape[2] > c->ct_nst_max || (shape[2] & 1)) {
+            set_error("contraction stages %d: an even count in %d..%d", shape[2], c->ct_nst_min, c->ct_nst_max);
             return DFTG_ERR_ARG;
         }
         c->ct_grid = shape[1];
@@ -1000,7 +1000,7 @@ int dftg_autotune(dftg_ctx *c, int reps, double *best_ms)
         if ((knob == 0 && !tune_tc) || (knob > 0 && !tune_ct)) continue;
         if (knob == 2) {
             cand.clear();
-            for (int v = c->ct_nst_max; v >= c->ct_nst_min; --v) cand.push_back(v);
+            for (int v = c->ct_nst_max; v >= c->ct_nst_min; v -= 2) cand.push_back(v);   // even depths
         } else {
             shape_candidates(knob == 0 ? c->tc_grid_max : c->ct_grid_max, cand);
         }

@@ -24,10 +24,12 @@
 // in the shared-memory operand layout; B is formed every build from A and c.
 //
 // CTA (persistent over chunks, 576 threads):
-//   warps 0-7  producers: every warp builds its rows (w, w + 8, ... in groups
-//              of eight) of the B slices of every stage from the A slices and
-//              c values of the stage (shared memory), then a proxy fence and an
-//              mbarrier arrive (the stage's full barrier counts eight);
+//   warps 0-7  producers in two groups of four: group g builds the B slices of
+//              the stages in ring slots of parity g (the ring depth is even, so
+//              a group sees each of its slots' phases in order), every warp of
+//              the group its rows (w, w + 4, ... in groups of eight), from the A
+//              slices and c values of the stage (shared memory), then a proxy
+//              fence and an mbarrier arrive (the full barrier counts four);
 //   warp 8     TMEM owner and MMA issuer (one thread);
 //   warps 9-16 epilogue: TMEM -> double-float partial (TMEM lane quarter =
 //              warp % 4, alternate 16-column blocks for the two warps of a quarter);
@@ -198,7 +200,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
     if (threadIdx.x == 0) {
         for (int s = 0; s < nst; ++s) {
             mbar_init(&sh->a_full[s], 1);
-            mbar_init(&sh->full[s], kCtProducers);   // every producer warp
+            mbar_init(&sh->full[s], kCtProducers / 2);   // the four warps of the slot's group
             mbar_init(&sh->empty[s], 1);
         }
         mbar_init(&sh->tmem_full, 1);
@@ -220,8 +222,11 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
 
     if (warp < kCtProducers) {
         // ------------------------------------------------------------ producers
-        // all producer warps fill every stage: warp w takes row groups w, w + 8, ...;
-        // lane = (row within the group of 8) x (8-point group g)
+        // two groups of four warps own the even and the odd ring slots (nst is
+        // even, so each group sees its slots' phases in order); in a group, warp
+        // w takes row groups w, w + 4, ...; lane = (row within the group of 8) x
+        // (8-point group g)
+        const int grp = warp >> 2, wg = warp & 3;
         const int g = lane & 3, mrow = lane >> 2;
         int it = 0;
         bool ok = true;
@@ -230,17 +235,18 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
             const int2 ce = cexp[ch];
             const float sx = pow2f(-ce.x), sj = pow2f(-ce.y);
             // B row scales of this lane's rows for the chunk, in registers
-            float rfr[kCtMaxNbf / (8 * kCtProducers)];
+            float rfr[kCtMaxNbf / 32];
             {
                 const int *ea = rowexp + (size_t)ch * nbf, *es = swexp + (size_t)ch * nbf;
 #pragma unroll
-                for (int j = 0; j < kCtMaxNbf / (8 * kCtProducers); ++j) {
-                    const int mu = 8 * kCtProducers * j + 8 * warp + mrow;
+                for (int j = 0; j < kCtMaxNbf / 32; ++j) {
+                    const int mu = 32 * j + 8 * wg + mrow;
                     rfr[j] = mu < nbf ? pow2f(max(-126, min(127, ea[mu] - es[mu]))) : 0.f;
                 }
             }
             for (int kb = kb0; kb < kb1; ++kb, ++it) {
                 const int s = it % nst, n = it / nst;
+                if ((s & 1) != grp) continue;        // the other group's slot
                 int w_ok = 1;
                 if (lane == 0) w_ok = mbar_wait(&sh->a_full[s], (uint32_t)(n & 1)) ? 1 : 0;
                 w_ok = __shfl_sync(0xffffffffu, w_ok, 0);
@@ -258,49 +264,51 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                     cx[k] = sc[8 * g + k] * sx;
                     cy[k] = sc[kCtKS + 8 * g + k] * sj;
                 }
-                // all slice loads of this lane's rows first, then the arithmetic
-                // (predicated, no early exit, so the rows interleave)
-                uint4 q0[kCtMaxNbf / (8 * kCtProducers)], q1[kCtMaxNbf / (8 * kCtProducers)],
-                    q2[kCtMaxNbf / (8 * kCtProducers)];
+                // the lane's rows two at a time: their slice loads first, then the
+                // arithmetic (predicated, no early exit, so the rows interleave)
 #pragma unroll
-                for (int j = 0; j < kCtMaxNbf / (8 * kCtProducers); ++j) {
-                    const int mu = 8 * kCtProducers * j + 8 * warp + mrow;
-                    if (mu < nbf) {
-                        const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
-                        q0[j] = *reinterpret_cast<const uint4 *>(sA + oa);
-                        q1[j] = *reinterpret_cast<const uint4 *>(sA + a_slice + oa);
-                        q2[j] = *reinterpret_cast<const uint4 *>(sA + 2 * a_slice + oa);
-                    }
-                }
+                for (int j0 = 0; j0 < kCtMaxNbf / 32; j0 += 2) {
+                    uint4 q0[2], q1[2], q2[2];
 #pragma unroll
-                for (int j = 0; j < kCtMaxNbf / (8 * kCtProducers); ++j) {
-                    const int mu = 8 * kCtProducers * j + 8 * warp + mrow;
-                    if (mu < nbf) {
-                        const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
-                        // B row scale: phi 2^(7 - e_mu) -> phi 2^(7 - s_mu)
-                        const float rf = rfr[j];
-                        float v[8], t[8];
-                        unpack8(q0[j], v);
-                        unpack8(q1[j], t);
-#pragma unroll
-                        for (int k = 0; k < 8; ++k) v[k] += t[k];
-                        unpack8(q2[j], t);
-                        float bx[8], by[8];
-#pragma unroll
-                        for (int k = 0; k < 8; ++k) {
-                            v[k] += t[k];                          // phi 2^(7 - e_mu), |v| < 128
-                            const float u = v[k] * rf;
-                            bx[k] = cx[k] * u;                     // c phi 2^(7 - s_mu - v), |bx| < 128
-                            by[k] = cy[k] * u;
+                    for (int jj = 0; jj < 2; ++jj) {
+                        const int mu = 32 * (j0 + jj) + 8 * wg + mrow;
+                        if (mu < nbf) {
+                            const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
+                            q0[jj] = *reinterpret_cast<const uint4 *>(sA + oa);
+                            q1[jj] = *reinterpret_cast<const uint4 *>(sA + a_slice + oa);
+                            q2[jj] = *reinterpret_cast<const uint4 *>(sA + 2 * a_slice + oa);
                         }
-                        uint4 sbx[kCtSlices], sby[kCtSlices];
-                        slice8_fixed(bx, sbx);
-                        slice8_fixed(by, sby);
-                        const uint32_t oj = core_off(nbf + mu, 8 * g, kCtKcores);
+                    }
 #pragma unroll
-                        for (int i = 0; i < kCtSlices; ++i) {
-                            *reinterpret_cast<uint4 *>(sB + i * b_slice + oa) = sbx[i];
-                            *reinterpret_cast<uint4 *>(sB + i * b_slice + oj) = sby[i];
+                    for (int jj = 0; jj < 2; ++jj) {
+                        const int mu = 32 * (j0 + jj) + 8 * wg + mrow;
+                        if (mu < nbf) {
+                            const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
+                            // B row scale: phi 2^(7 - e_mu) -> phi 2^(7 - s_mu)
+                            const float rf = rfr[j0 + jj];
+                            float v[8], t[8];
+                            unpack8(q0[jj], v);
+                            unpack8(q1[jj], t);
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) v[k] += t[k];
+                            unpack8(q2[jj], t);
+                            float bx[8], by[8];
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) {
+                                v[k] += t[k];                          // phi 2^(7 - e_mu), |v| < 128
+                                const float u = v[k] * rf;
+                                bx[k] = cx[k] * u;                     // c phi 2^(7 - s_mu - v), |bx| < 128
+                                by[k] = cy[k] * u;
+                            }
+                            uint4 sbx[kCtSlices], sby[kCtSlices];
+                            slice8_fixed(bx, sbx);
+                            slice8_fixed(by, sby);
+                            const uint32_t oj = core_off(nbf + mu, 8 * g, kCtKcores);
+#pragma unroll
+                            for (int i = 0; i < kCtSlices; ++i) {
+                                *reinterpret_cast<uint4 *>(sB + i * b_slice + oa) = sbx[i];
+                                *reinterpret_cast<uint4 *>(sB + i * b_slice + oj) = sby[i];
+                            }
                         }
                     }
                 }
@@ -369,7 +377,6 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
         const int h = (warp - kCtEpi0) >> 2;     // column blocks h, h + 2, ...
         const int r = q * 32 + lane;             // accumulator row = basis function mu
         float2 *gpart = part + (size_t)blockIdx.x * 2 * ntri;   // this CTA's partial in HBM
-        float2 *px = spart ? s_part : gpart;
         int cc = 0;
         for (int ch = blockIdx.x; ch < nchunk; ch += gridDim.x, ++cc) {
             const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
@@ -394,47 +401,54 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
             if (sh->fail) break;
             tc_fence_after();
             const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16);
-            for (int c0 = 16 * h; c0 < NP; c0 += 32) {
-                float dh[16], dl[16];
-                tmem_ld16(ta + (uint32_t)c0, dh);
-                tmem_ld16(ta + 256u + (uint32_t)c0, dl);
-                tmem_wait_ld();
-                if (r < nbf) {
-                    // (s, e) += (D_hi + D_lo) 2^(e_mu + s_nu + v - 14) for the upper-triangle
-                    // elements of the block, eight columns at a time: column tables and
-                    // old values first, then the arithmetic, then the stores, so no
-                    // access waits on another
-                    const int kend = min(16, 2 * nbf - c0);
+            // the partial is either shared or global memory: one inlined copy of
+            // the drain per space, so its accesses compile to the space's own
+            // loads and stores instead of generic ones
+            auto drain = [&](float2 *__restrict__ pxs) {
+                for (int c0 = 16 * h; c0 < NP; c0 += 32) {
+                    float dh[16], dl[16];
+                    tmem_ld16(ta + (uint32_t)c0, dh);
+                    tmem_ld16(ta + 256u + (uint32_t)c0, dl);
+                    tmem_wait_ld();
+                    if (r < nbf) {
+                        // (s, e) += (D_hi + D_lo) 2^(e_mu + s_nu + v - 14) for the upper-triangle
+                        // elements of the block, eight columns at a time: column tables and
+                        // old values first, then the arithmetic, then the stores, so no
+                        // access waits on another
+                        const int kend = min(16, 2 * nbf - c0);
 #pragma unroll
-                    for (int hh = 0; hh < 16; hh += 8) {
-                        int off[8];
-                        float fk[8];
+                        for (int hh = 0; hh < 16; hh += 8) {
+                            int off[8];
+                            float fk[8];
 #pragma unroll
-                        for (int k = 0; k < 8; ++k) {
-                            const bool v = hh + k < kend && r <= s_colnu[c0 + hh + k];
-                            off[k] = v ? s_coloff[c0 + hh + k] + r : -1;
-                            fk[k] = v ? s_colf[c0 + hh + k] * fr : 0.f;   // exact power of two
+                            for (int k = 0; k < 8; ++k) {
+                                const bool v = hh + k < kend && r <= s_colnu[c0 + hh + k];
+                                off[k] = v ? s_coloff[c0 + hh + k] + r : -1;
+                                fk[k] = v ? s_colf[c0 + hh + k] * fr : 0.f;   // exact power of two
+                            }
+                            float2 old[8];
+#pragma unroll
+                            for (int k = 0; k < 8; ++k)
+                                old[k] = (cc > 0 && off[k] >= 0) ? pxs[off[k]] : make_float2(0.f, 0.f);
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) {
+                                const float vh = dh[hh + k] * fk[k], vl = dl[hh + k] * fk[k];
+                                float s2 = old[k].x, e2 = old[k].y;
+                                const float t = s2 + vh;
+                                const float bp = t - s2;
+                                e2 += (s2 - (t - bp)) + (vh - bp) + vl;
+                                s2 = t + e2;                             // renormalise: |e| <= ulp(s) / 2
+                                old[k] = make_float2(s2, e2 - (s2 - t));
+                            }
+#pragma unroll
+                            for (int k = 0; k < 8; ++k)
+                                if (off[k] >= 0) pxs[off[k]] = old[k];
                         }
-                        float2 old[8];
-#pragma unroll
-                        for (int k = 0; k < 8; ++k)
-                            old[k] = (cc > 0 && off[k] >= 0) ? px[off[k]] : make_float2(0.f, 0.f);
-#pragma unroll
-                        for (int k = 0; k < 8; ++k) {
-                            const float vh = dh[hh + k] * fk[k], vl = dl[hh + k] * fk[k];
-                            float s2 = old[k].x, e2 = old[k].y;
-                            const float t = s2 + vh;
-                            const float bp = t - s2;
-                            e2 += (s2 - (t - bp)) + (vh - bp) + vl;
-                            s2 = t + e2;                             // renormalise: |e| <= ulp(s) / 2
-                            old[k] = make_float2(s2, e2 - (s2 - t));
-                        }
-#pragma unroll
-                        for (int k = 0; k < 8; ++k)
-                            if (off[k] >= 0) px[off[k]] = old[k];
                     }
                 }
-            }
+            };
+            if (spart) drain(s_part);
+            else drain(gpart);
             tc_fence_before();
             ct_epi_bar();                        // all TMEM reads of this chunk are done
             if (threadIdx.x == 32 * kCtEpi0) mbar_arrive(&sh->tmem_empty);
@@ -644,7 +658,8 @@ int contract_tc_setup(dftg_ctx *c)
         nst = kCtMaxStages;
         while (nst > 2 && ct_smem(nst, NP, AR, c->nbf, spart) > (size_t)optin) --nst;
     }
-    if (ct_smem(nst, NP, AR, c->nbf, spart) > (size_t)optin) return DFTG_OK;
+    nst &= ~1;                                        // the producer groups own even / odd slots
+    if (nst < 2 || ct_smem(nst, NP, AR, c->nbf, spart) > (size_t)optin) return DFTG_OK;
     int nkb, kbpc, nchunk;
     ct_plan(c->npad, nsm, nkb, kbpc, nchunk);
     const int grid = nchunk < nsm ? nchunk : nsm;
@@ -680,7 +695,8 @@ int contract_tc_setup(dftg_ctx *c)
     // of the shared memory, so one contraction CTA runs per SM as at setup
     int nmin = nst;
     while (nmin > 2 && ct_smem(nmin - 1, NP, AR, c->nbf, spart) * 2 > (size_t)optin) --nmin;
-    c->ct_nst_min = nmin;
+    nmin = (nmin + 1) & ~1;                           // even ring depths only
+    c->ct_nst_min = nmin < nst ? nmin : nst;
     c->ct_ready = true;
     return DFTG_OK;
 }

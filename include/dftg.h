@@ -232,8 +232,8 @@ int dftg_batch_autotune(dftg_batch *b, int reps, double *best_ms);
 
 /* Launch-shape autotuner (no counterpart in the reference).  Shape =
  * {CTAs of the tensor-core density kernel, CTAs of the tensor-core XC / J
- * contraction, pipeline stages of the contraction}; 0 where the context has no
- * such kernel.  dftg_autotune times reps graph-replayed builds of the last
+ * contraction, pipeline stages of the contraction (even)}; 0 where the context
+ * has no such kernel.  dftg_autotune times reps graph-replayed builds of the last
  * built P for candidate shapes (coordinate descent, each knob from the current
  * best) and keeps the fastest; it needs a preceding complete build and leaves
  * the outputs of a build with the chosen shape.  best_ms may be NULL. */

@@ -270,6 +270,7 @@ def test_autotune_keeps_results(gpu_lib):
     assert ms > 0.0
     shape1 = g.launch_shape
     assert 1 <= shape1[0] <= shape0[0] and 1 <= shape1[1] <= shape0[1] and 2 <= shape1[2] <= shape0[2]
+    assert shape1[2] % 2 == 0
     r1 = g.fock_build(P)
     assert np.abs(r1["J"] - r0["J"]).max() <= 1e-7 * np.abs(r0["J"]).max()
     assert np.abs(r1["XC"] - r0["XC"]).max() <= 1e-7 * np.abs(r0["XC"]).max()
