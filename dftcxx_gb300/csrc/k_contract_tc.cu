@@ -23,7 +23,7 @@
 // sums the CTA partials in FP64 in a fixed order and symmetrises.  A (phi is fixed for the grid) is sliced once at setup into HBM
 // in the shared-memory operand layout; B is formed every build from A and c.
 //
-// CTA (persistent over chunks, 576 threads):
+// CTA (persistent over chunks, 832 threads):
 //   warps 0-7  producers in two groups of four: group g builds the B slices of
 //              the stages in ring slots of parity g (the ring depth is even, so
 //              a group sees each of its slots' phases in order), every warp of
@@ -31,9 +31,10 @@
 //              slices and c values of the stage (shared memory), then a proxy
 //              fence and an mbarrier arrive (the full barrier counts four);
 //   warp 8     TMEM owner and MMA issuer (one thread);
-//   warps 9-16 epilogue: TMEM -> double-float partial (TMEM lane quarter =
-//              warp % 4, alternate 16-column blocks for the two warps of a quarter);
-//   warp 17    loader: bulk copies of the A slices and c values of each stage.
+//   warps 9-24 epilogue: TMEM -> double-float partial (TMEM lane quarter =
+//              warp % 4, the four warps of a quarter take every fourth
+//              16-column block);
+//   warp 25    loader: bulk copies of the A slices and c values of each stage.
 // Every mbarrier wait is bounded: on expiry the CTA records an error code, lets
 // its copies and MMAs complete, frees TMEM and exits.
 #include <cuda_bf16.h>
@@ -50,8 +51,9 @@ constexpr int kCtMaxNbf = 128;             // 2 nbf <= 256 columns per accumulat
 constexpr int kCtProducers = 8;           // producer warps 0..7
 constexpr int kCtMmaWarp = kCtProducers;   // TMEM owner and MMA issuer
 constexpr int kCtEpi0 = kCtMmaWarp + 1;    // epilogue warps kCtEpi0 .. kCtEpi0 + 7
-constexpr int kCtThreads = (kCtEpi0 + 9) * 32;
-constexpr int kCtLoaderWarp = kCtEpi0 + 8;
+constexpr int kCtEpiWarps = 16;           // four per TMEM lane quarter
+constexpr int kCtThreads = (kCtEpi0 + kCtEpiWarps + 1) * 32;
+constexpr int kCtLoaderWarp = kCtEpi0 + kCtEpiWarps;
 constexpr int kCtMaxStages = 8;
 constexpr int kCtMaxKbPerChunk = 16;       // <= 512 points per exact integer accumulation (sums < 2^23)
 constexpr uint32_t kCtTmemCols = 512;      // D_hi at column 0, D_lo at column 256
@@ -68,9 +70,9 @@ struct CtShared {
     int fail;
 };
 
-__device__ __forceinline__ void ct_epi_bar()   // named barrier 1 over the 8 epilogue warps
+__device__ __forceinline__ void ct_epi_bar()   // named barrier 1 over the epilogue warps
 {
-    asm volatile("bar.sync 1, 256;" ::: "memory");
+    asm volatile("bar.sync 1, %0;" ::"n"(kCtEpiWarps * 32) : "memory");
 }
 
 __device__ __forceinline__ float pow2f(int k)   // 2^k, -126 <= k <= 127
@@ -264,13 +266,13 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                     cx[k] = sc[8 * g + k] * sx;
                     cy[k] = sc[kCtKS + 8 * g + k] * sj;
                 }
-                // the lane's rows two at a time: their slice loads first, then the
-                // arithmetic (predicated, no early exit, so the rows interleave)
+                // the lane's rows one at a time: its slice loads first, then the
+                // arithmetic (predicated, no early exit)
 #pragma unroll
-                for (int j0 = 0; j0 < kCtMaxNbf / 32; j0 += 2) {
-                    uint4 q0[2], q1[2], q2[2];
+                for (int j0 = 0; j0 < kCtMaxNbf / 32; j0 += 1) {
+                    uint4 q0[1], q1[1], q2[1];
 #pragma unroll
-                    for (int jj = 0; jj < 2; ++jj) {
+                    for (int jj = 0; jj < 1; ++jj) {
                         const int mu = 32 * (j0 + jj) + 8 * wg + mrow;
                         if (mu < nbf) {
                             const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
@@ -280,7 +282,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                         }
                     }
 #pragma unroll
-                    for (int jj = 0; jj < 2; ++jj) {
+                    for (int jj = 0; jj < 1; ++jj) {
                         const int mu = 32 * (j0 + jj) + 8 * wg + mrow;
                         if (mu < nbf) {
                             const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
@@ -374,7 +376,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
     } else if (warp < kCtLoaderWarp) {
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3;                  // TMEM lane quarter of this warp
-        const int h = (warp - kCtEpi0) >> 2;     // column blocks h, h + 2, ...
+        const int h = (warp - kCtEpi0) >> 2;     // column blocks h, h + kCtEpiWarps / 4, ...
         const int r = q * 32 + lane;             // accumulator row = basis function mu
         float2 *gpart = part + (size_t)blockIdx.x * 2 * ntri;   // this CTA's partial in HBM
         int cc = 0;
@@ -384,7 +386,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
             {
                 const int2 ce = cexp[ch];
                 const int *es = swexp + (size_t)ch * nbf;
-                for (int n = threadIdx.x - 32 * kCtEpi0; n < 2 * nbf; n += 256) {
+                for (int n = threadIdx.x - 32 * kCtEpi0; n < 2 * nbf; n += 32 * kCtEpiWarps) {
                     const int nu = n < nbf ? n : n - nbf;
                     const int e = es[nu] + (n < nbf ? ce.x : ce.y) - 14;
                     s_colf[n] = pow2f(max(-126, min(127, e)));
@@ -405,24 +407,24 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
             // the drain per space, so its accesses compile to the space's own
             // loads and stores instead of generic ones
             auto drain = [&](float2 *__restrict__ pxs) {
-                for (int c0 = 16 * h; c0 < NP; c0 += 32) {
-                    float dh[16], dl[16];
-                    tmem_ld16(ta + (uint32_t)c0, dh);
-                    tmem_ld16(ta + 256u + (uint32_t)c0, dl);
-                    tmem_wait_ld();
-                    if (r < nbf) {
-                        // (s, e) += (D_hi + D_lo) 2^(e_mu + s_nu + v - 14) for the upper-triangle
-                        // elements of the block, eight columns at a time: column tables and
-                        // old values first, then the arithmetic, then the stores, so no
-                        // access waits on another
-                        const int kend = min(16, 2 * nbf - c0);
+                for (int c0 = 16 * h; c0 < NP; c0 += 16 * (kCtEpiWarps / 4)) {
 #pragma unroll
-                        for (int hh = 0; hh < 16; hh += 8) {
+                    for (int hh = 0; hh < 16; hh += 8) {
+                        // eight columns: D_hi and D_lo from TMEM, the column tables and
+                        // old values, then the arithmetic, then the stores
+                        float dh[8], dl[8];
+                        tmem_ld8(ta + (uint32_t)(c0 + hh), dh);
+                        tmem_ld8(ta + 256u + (uint32_t)(c0 + hh), dl);
+                        tmem_wait_ld();
+                        if (r < nbf) {
+                            // (s, e) += (D_hi + D_lo) 2^(e_mu + s_nu + v - 14) for the
+                            // upper-triangle elements
+                            const int kend = min(8, 2 * nbf - c0 - hh);
                             int off[8];
                             float fk[8];
 #pragma unroll
                             for (int k = 0; k < 8; ++k) {
-                                const bool v = hh + k < kend && r <= s_colnu[c0 + hh + k];
+                                const bool v = k < kend && r <= s_colnu[c0 + hh + k];
                                 off[k] = v ? s_coloff[c0 + hh + k] + r : -1;
                                 fk[k] = v ? s_colf[c0 + hh + k] * fr : 0.f;   // exact power of two
                             }
@@ -432,7 +434,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
                                 old[k] = (cc > 0 && off[k] >= 0) ? pxs[off[k]] : make_float2(0.f, 0.f);
 #pragma unroll
                             for (int k = 0; k < 8; ++k) {
-                                const float vh = dh[hh + k] * fk[k], vl = dl[hh + k] * fk[k];
+                                const float vh = dh[k] * fk[k], vl = dl[k] * fk[k];
                                 float s2 = old[k].x, e2 = old[k].y;
                                 const float t = s2 + vh;
                                 const float bp = t - s2;
@@ -454,7 +456,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
             if (threadIdx.x == 32 * kCtEpi0) mbar_arrive(&sh->tmem_empty);
         }
         if (spart && !sh->fail) {
-            for (size_t i = threadIdx.x - 32 * kCtEpi0; i < 2 * ntri; i += 256) gpart[i] = s_part[i];
+            for (size_t i = threadIdx.x - 32 * kCtEpi0; i < 2 * ntri; i += 32 * kCtEpiWarps) gpart[i] = s_part[i];
         }
     } else {
         // ------------------------------------------------------------ loader
