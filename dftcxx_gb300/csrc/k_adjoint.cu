@@ -754,7 +754,10 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_becke_w(size_t npts, int per_at
     const int B = act ? B0 : 0;
     T *sd = s_dist[warp] + grp * G;
     const double ax = atoms[4 * B], ay = atoms[4 * B + 1], az = atoms[4 * B + 2];
+    // per-lane totals: FP64 for T = double; a double-float (TwoSum) pair for
+    // T = float, so no FP64 work runs per point
     double accx = 0.0, accy = 0.0, accz = 0.0;
+    dfl fax{0.f, 0.f}, fay{0.f, 0.f}, faz{0.f, 0.f};
     const size_t stride = (size_t)gridDim.x * 4 * NG;
     for (size_t base = ((size_t)blockIdx.x * 4 + warp) * NG; base < npts; base += stride) {
         const size_t p = base + grp;
@@ -821,18 +824,44 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_becke_w(size_t npts, int per_at
             Dy += __shfl_sync(0xffffffffu, hy, src, G);
             Dz += __shfl_sync(0xffffffffu, hz, src, G);
         }
-        // FP64 per point: other atoms take D, the owning atom minus their sum
+        // per point: other atoms take D, the owning atom minus their sum (exactly,
+        // up to the final rounding: double-float sums for T = float)
         const bool other = act && live && B != a;
-        double ox = other ? (double)Dx : 0.0, oy = other ? (double)Dy : 0.0, oz = other ? (double)Dz : 0.0;
-        double sx = ox, sy = oy, sz = oz;
+        if (sizeof(T) == 8) {
+            double ox = other ? (double)Dx : 0.0, oy = other ? (double)Dy : 0.0, oz = other ? (double)Dz : 0.0;
+            double sx = ox, sy = oy, sz = oz;
 #pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) {
-            sx += __shfl_xor_sync(0xffffffffu, sx, o, G);
-            sy += __shfl_xor_sync(0xffffffffu, sy, o, G);
-            sz += __shfl_xor_sync(0xffffffffu, sz, o, G);
+            for (int o = G / 2; o > 0; o >>= 1) {
+                sx += __shfl_xor_sync(0xffffffffu, sx, o, G);
+                sy += __shfl_xor_sync(0xffffffffu, sy, o, G);
+                sz += __shfl_xor_sync(0xffffffffu, sz, o, G);
+            }
+            if (other) { accx += ox; accy += oy; accz += oz; }
+            else if (act && live) { accx -= sx; accy -= sy; accz -= sz; }
+        } else {
+            const float ox = other ? (float)Dx : 0.f, oy = other ? (float)Dy : 0.f, oz = other ? (float)Dz : 0.f;
+            dfl sx{ox, 0.f}, sy{oy, 0.f}, sz{oz, 0.f};
+#pragma unroll
+            for (int o = G / 2; o > 0; o >>= 1) {
+                sx = df_add(sx, dfl{__shfl_xor_sync(0xffffffffu, sx.h, o, G), __shfl_xor_sync(0xffffffffu, sx.l, o, G)});
+                sy = df_add(sy, dfl{__shfl_xor_sync(0xffffffffu, sy.h, o, G), __shfl_xor_sync(0xffffffffu, sy.l, o, G)});
+                sz = df_add(sz, dfl{__shfl_xor_sync(0xffffffffu, sz.h, o, G), __shfl_xor_sync(0xffffffffu, sz.l, o, G)});
+            }
+            if (other) {
+                fax = df_add(fax, dfl{ox, 0.f});
+                fay = df_add(fay, dfl{oy, 0.f});
+                faz = df_add(faz, dfl{oz, 0.f});
+            } else if (act && live) {
+                fax = df_sub(fax, sx);
+                fay = df_sub(fay, sy);
+                faz = df_sub(faz, sz);
+            }
         }
-        if (other) { accx += ox; accy += oy; accz += oz; }
-        else if (act && live) { accx -= sx; accy -= sy; accz -= sz; }
+    }
+    if (sizeof(T) == 4) {
+        accx = df_to(fax);
+        accy = df_to(fay);
+        accz = df_to(faz);
     }
     s_acc[warp][lane][0] = accx;
     s_acc[warp][lane][1] = accy;
@@ -1093,7 +1122,6 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_force_phi32(int nbf, int natoms
     const float G = valid ? (float)(4.0 * h[p]) : 0.f;
     const double px = X[p], py = Yc[p], pz = Zc[p];
     double *acc = s_acc + (size_t)warp * natoms * 3;
-    double self[3] = {0.0, 0.0, 0.0};
     float vb[3] = {0.f, 0.f, 0.f};
     int cur = bf_atom[0];
     float cx = 0.f, cy = 0.f, cz = 0.f;   // p - R_cur
@@ -1102,16 +1130,29 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_force_phi32(int nbf, int natoms
         cy = (float)(py - atoms[4 * b + 1]);
         cz = (float)(pz - atoms[4 * b + 2]);
     };
+    // the point's vector for atom b (FP32, GB300's FP64 rate is low): summed in
+    // FP32 over the warp's points of each owning atom (usually one), and that same
+    // sum, once in FP64, taken from atom b and given to the owning atom, so the
+    // term adds exactly zero net force
     auto flush = [&](int b) {
         const bool use = valid && b != ap;
-        double c[3];
-        for (int d = 0; d < 3; ++d) {
-            c[d] = use ? (double)(G * vb[d]) : 0.0;
-            self[d] += c[d];
-        }
-        for (int d = 0; d < 3; ++d) {
-            const double s = warp_sum_d(c[d]);
-            if (lane == 0) acc[3 * b + d] -= s;
+        float c[3];
+        for (int d = 0; d < 3; ++d) c[d] = use ? G * vb[d] : 0.f;
+        unsigned todo = 0xffffffffu;
+        while (todo) {
+            const int leader = __ffs(todo) - 1;
+            const int kl = __shfl_sync(0xffffffffu, ap, leader);
+            const unsigned grp = __ballot_sync(0xffffffffu, ap == kl) & todo;
+            for (int d = 0; d < 3; ++d) {
+                float s = (grp >> lane) & 1u ? c[d] : 0.f;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                if (lane == leader && kl != b) {
+                    acc[3 * b + d] -= (double)s;
+                    acc[3 * kl + d] += (double)s;
+                }
+            }
+            todo &= ~grp;
         }
     };
     set_centre(cur);
@@ -1154,7 +1195,6 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_force_phi32(int nbf, int natoms
         }
     }
     flush(cur);
-    warp_add_by_key(ap, self, acc);
     __syncthreads();
     for (int e = threadIdx.x; e < natoms * 3; e += kBwBlock)
         part[(size_t)blockIdx.x * natoms * 3 + e] =
