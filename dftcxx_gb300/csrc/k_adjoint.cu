@@ -973,8 +973,10 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_cross_T32(int nlm, int lmax, co
 // Cross-atom geometry term in FP32 over the pair bins (grid-stride over tasks):
 // per pair (u_p / 2) grad f_k with the folded spline coefficients (high halves,
 // plus the low halves for l = 0) and the integer Y_lm recursion; the bin's atom
-// k takes minus the task's sum, the pairs' own atoms (runs of equal atom, the
-// pairs of a bin are in point order) take the pair vectors.
+// k takes minus the pair vectors, the pairs' own atoms take them: per pair slot
+// the vectors are summed in FP32 over the lanes of each owning atom (runs of
+// equal atom: the pairs of a bin are in point order) and that same sum goes, in
+// FP64, to both atoms (exact translation sum rule, no FP64 work per pair).
 __global__ void __launch_bounds__(kBwBlock) k_bw_force_cross32(int ntasks, int nlm, int lmax, int nrad, int natoms,
                                                                int per_atom, const int4 *__restrict__ tasks,
                                                                const float4 *__restrict__ pgeo,
@@ -986,7 +988,6 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_force_cross32(int ntasks, int n
     extern __shared__ double s_x[];               // [4][natoms][3] doubles, then [nlm][2] float4 coefficients
     double *s_acc = s_x;
     float4 *s_cf = reinterpret_cast<float4 *>(s_x + 4 * (size_t)natoms * 3);
-    __shared__ double s_k[4][3];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double *acc = s_acc + (size_t)warp * natoms * 3;
     for (int e = threadIdx.x; e < 4 * natoms * 3; e += kBwBlock) s_acc[e] = 0.0;
@@ -998,11 +999,10 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_force_cross32(int ntasks, int n
             s_cf[i] = reinterpret_cast<const float4 *>(splm + (((size_t)tk.z * nlm + lm) * nrad + tk.w) * 8)[i & 1];
         }
         __syncthreads();
-        double kx = 0.0, ky = 0.0, kz = 0.0;
         for (int q0 = 0; q0 < tk.y; q0 += kBwBlock) {
             const int q = q0 + threadIdx.x;
-            double v[3] = {0.0, 0.0, 0.0};
-            int key = 0;
+            float v[3] = {0.f, 0.f, 0.f};
+            int key = -1;
             if (q < tk.y) {
                 const float4 g = pgeo[(size_t)tk.x + q];
                 const float t = ptk[(size_t)tk.x + q].x;
@@ -1058,27 +1058,27 @@ __global__ void __launch_bounds__(kBwBlock) k_bw_force_cross32(int ntasks, int n
                 const float A1 = A1h + A1l;
                 const float ug = g.x * gx + g.y * gy + g.z * gz;
                 const float c = 0.5f * (float)u[p];
-                v[0] = (double)(c * (A1 * g.x + ir2 * (gx - ug * g.x)));
-                v[1] = (double)(c * (A1 * g.y + ir2 * (gy - ug * g.y)));
-                v[2] = (double)(c * (A1 * g.z + ir2 * (gz - ug * g.z)));
+                v[0] = c * (A1 * g.x + ir2 * (gx - ug * g.x));
+                v[1] = c * (A1 * g.y + ir2 * (gy - ug * g.y));
+                v[2] = c * (A1 * g.z + ir2 * (gz - ug * g.z));
             }
-            kx += v[0];
-            ky += v[1];
-            kz += v[2];
-            warp_add_by_key(key, v, acc);
+            unsigned todo = 0xffffffffu;
+            while (todo) {
+                const int leader = __ffs(todo) - 1;
+                const int kl = __shfl_sync(0xffffffffu, key, leader);
+                const unsigned grp = __ballot_sync(0xffffffffu, key == kl) & todo;
+                for (int d = 0; d < 3; ++d) {
+                    float sv = (grp >> lane) & 1u ? v[d] : 0.f;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
+                    if (lane == leader && kl >= 0) {
+                        acc[3 * kl + d] += (double)sv;
+                        acc[3 * tk.z + d] -= (double)sv;
+                    }
+                }
+                todo &= ~grp;
+            }
         }
-        kx = warp_sum_d(kx);
-        ky = warp_sum_d(ky);
-        kz = warp_sum_d(kz);
-        if (lane == 0) {
-            s_k[warp][0] = kx;
-            s_k[warp][1] = ky;
-            s_k[warp][2] = kz;
-        }
-        __syncthreads();
-        if (threadIdx.x < 3)
-            s_acc[3 * tk.z + threadIdx.x] -= ((s_k[0][threadIdx.x] + s_k[1][threadIdx.x]) + s_k[2][threadIdx.x]) +
-                                             s_k[3][threadIdx.x];
     }
     __syncthreads();
     for (int e = threadIdx.x; e < natoms * 3; e += kBwBlock)
