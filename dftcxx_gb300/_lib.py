@@ -45,6 +45,17 @@ class Points(ctypes.Structure):
     _fields_ = [("npts", ctypes.c_size_t), ("xyz", _dp), ("w", _dp)]
 
 
+class ScfParams(ctypes.Structure):
+    _fields_ = [("nelec", ctypes.c_int), ("alpha", ctypes.c_double), ("tol", ctypes.c_double),
+                ("min_iter", ctypes.c_int), ("max_iter", ctypes.c_int), ("refine_steps", ctypes.c_int)]
+
+
+SCF_MAX_NBF = 160
+SCF_MAX_ITER = 1000
+SCF_P, SCF_J, SCF_XC, SCF_H, SCF_X, SCF_EPS, SCF_COCC, SCF_HISTORY, SCF_DIAG, SCF_STATE = range(10)
+SCF_HIST_W = 6
+
+
 class DftgError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("dftg error %d: %s" % (code, msg))
@@ -98,6 +109,10 @@ SIGNATURES = {
     "dftg_batch_fock_build_device": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.c_void_p],
+    "dftg_scf_init": [ctypes.c_void_p, ctypes.POINTER(ScfParams)],
+    "dftg_scf_run": [ctypes.c_void_p, _dp, _ip],
+    "dftg_scf_step": [ctypes.c_void_p, _dp, _ip],
+    "dftg_scf_get": [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
 }
 
 _lib = None

@@ -86,6 +86,7 @@ static void free_ctx(dftg_ctx *c)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->pipe_exec) cudaGraphExecDestroy(c->pipe_exec);
+    scf_free(c);
     for (cudaEvent_t ev : c->prof_ev)
         if (ev) cudaEventDestroy(ev);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -269,7 +270,7 @@ static int check_matrix(const double *P, int n)
     return DFTG_OK;
 }
 
-static int sync_scalars(dftg_ctx *c)
+int sync_scalars(dftg_ctx *c)
 {
     DFTG_CUDA(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(double) * scal_elems(c->natoms), cudaMemcpyDeviceToHost,
                               c->stream));
@@ -287,7 +288,7 @@ static int sync_scalars(dftg_ctx *c)
 }
 
 // device part of one Fock build; P already in c->d_P
-static int fock_pipeline(dftg_ctx *c)
+int fock_pipeline(dftg_ctx *c)
 {
     DFTG_TRY(launch_density(c));
     DFTG_TRY(launch_atom_sums(c, kSumsFactor));
@@ -306,7 +307,7 @@ static bool pipe_shape_changed(const dftg_ctx *c)
     return c->pipe_shape[0] != c->tc_grid || c->pipe_shape[1] != c->ct_grid || c->pipe_shape[2] != c->ct_nst;
 }
 
-static int fock_pipeline_graph(dftg_ctx *c)
+int fock_pipeline_graph(dftg_ctx *c)
 {
     if (c->pipe_exec && (c->pipe_mask != c->prec_mask || c->pipe_stream != c->stream || pipe_shape_changed(c))) {
         cudaGraphExecDestroy(c->pipe_exec);

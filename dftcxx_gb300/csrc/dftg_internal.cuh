@@ -261,6 +261,9 @@ struct dftg_ctx {
     cudaStream_t pipe_stream = nullptr;
     bool pipe_warm = false;
 
+    // device SCF driver (k_scf.cu), created by dftg_scf_init
+    struct dftg_scf_state *scf = nullptr;
+
     // per-phase CUDA-event timing (dftg_fock_build_profile)
     static constexpr int kMaxMarks = 24;
     cudaEvent_t prof_ev[kMaxMarks] = {};
@@ -321,6 +324,13 @@ int launch_hartree(dftg_ctx *c);
 int launch_backward(dftg_ctx *c, double sxc, double sj, double *dEdP_dev, double *dEdR_dev);
 // k_integrals.cu
 int launch_one_electron(dftg_ctx *c, double *dS, double *dT, double *dV);
+// dftg_capi.cu: one build on d_P (raw launches, capturable), the same through the
+// context's cached graph, and the host read of the scalars + bounded-wait flag
+int fock_pipeline(dftg_ctx *c);
+int fock_pipeline_graph(dftg_ctx *c);
+int sync_scalars(dftg_ctx *c);
+// k_scf.cu
+void scf_free(dftg_ctx *c);
 // k_contract.cu
 int contract_setup(dftg_ctx *c);
 size_t contract_part_elems(int nbf, size_t npad);

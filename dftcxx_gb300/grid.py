@@ -266,6 +266,80 @@ class DFT:
         return self.et
 
 
+class DeviceSCF:
+    """The reference's DFT constructor + DFT::scf (dft.cpp:57-61, 84-142,
+    160-227, 300-366) with every step on the GPU (dftg_scf_*): one-electron
+    matrices, X, eigen-solves, damping, grid Fock builds and the energy.  run()
+    is one CUDA graph launch for the whole loop."""
+
+    def __init__(self, mol, radial_points=15, lebedev_order=7, lmax=8, precision="fp64", device=0,
+                 alpha=0.5, tol=1e-4, min_iter=3, max_iter=100, nelec=0, refine_steps=0):
+        self.mol = mol
+        self.molgrid = MolecularGrid(mol, radial_points, lebedev_order, lmax, precision, device)
+        self.nbf = mol.nbf
+        prm = _lib.ScfParams(int(nelec), float(alpha), float(tol), int(min_iter), int(max_iter), int(refine_steps))
+        check(_lib.load().dftg_scf_init(self.molgrid.handle, ctypes.byref(prm)))
+        self.nocc = (nelec or int(np.sum(mol.Z))) // 2
+        self.et = self.state()["E"]      # E_0 of the set-up (E_xc = 0)
+
+    def state(self):
+        """{E: last energy, iterations, dE: last |E_n - E_(n-1)|, running: the loop would continue}."""
+        st = self._get(_lib.SCF_STATE, 4)
+        return {"E": st[0], "iterations": int(st[1]), "dE": st[2], "running": bool(st[3])}
+
+    def run(self):
+        """Iterate to convergence; returns the final energy (DFT::scf)."""
+        e, it = ctypes.c_double(), ctypes.c_int()
+        check(_lib.load().dftg_scf_run(self.molgrid.handle, ctypes.byref(e), ctypes.byref(it)))
+        self.et, self.iterations = e.value, it.value
+        return e.value
+
+    scf = run
+
+    def step(self):
+        """One iteration; returns (E, converged)."""
+        e, conv = ctypes.c_double(), ctypes.c_int()
+        check(_lib.load().dftg_scf_step(self.molgrid.handle, ctypes.byref(e), ctypes.byref(conv)))
+        self.et = e.value
+        return e.value, bool(conv.value)
+
+    def _get(self, what, count, shape=None):
+        out = np.zeros(max(count, 1))
+        n = ctypes.c_size_t()
+        check(_lib.load().dftg_scf_get(self.molgrid.handle, what, _ptr(out), out.size, ctypes.byref(n)))
+        out = out[:n.value]
+        return out if shape is None else out.reshape(shape, order="F")
+
+    def matrix(self, name):
+        """'P', 'J', 'XC', 'H' or 'X' (nbf x nbf)."""
+        what = {"P": _lib.SCF_P, "J": _lib.SCF_J, "XC": _lib.SCF_XC, "H": _lib.SCF_H, "X": _lib.SCF_X}[name]
+        return np.ascontiguousarray(self._get(what, self.nbf * self.nbf, (self.nbf, self.nbf)))
+
+    @property
+    def P(self):
+        return self.matrix("P")
+
+    def orbital_energies(self):
+        return self._get(_lib.SCF_EPS, self.nbf)
+
+    def occupied_coefficients(self):
+        return self._get(_lib.SCF_COCC, self.nbf * self.nocc, (self.nbf, self.nocc))
+
+    def history(self):
+        """Per iteration of the last run: rows {E, 2tr(PH), E_J, E_xc, N, |dE|}."""
+        h = self._get(_lib.SCF_HISTORY, _lib.SCF_HIST_W * _lib.SCF_MAX_ITER)
+        return h.reshape(-1, _lib.SCF_HIST_W)
+
+    def diagnostics(self):
+        """{max |S'| across the occupied / virtual split, max |I - C'^T C'|,
+        Jacobi sweeps, loop mode (1: conditional graph, 2: host-stepped)}."""
+        d = self._get(_lib.SCF_DIAG, 4)
+        return {"cross": d[0], "orth": d[1], "sweeps": int(d[2]), "mode": int(d[3])}
+
+    def close(self):
+        self.molgrid.close()
+
+
 class PointGrid(MolecularGrid):
     """Explicit points and weights with functions about explicit centres (no
     atoms, cells or Hartree step): amplitudes, density, LDA point kernel and

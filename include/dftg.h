@@ -261,6 +261,61 @@ int dftg_contract_noalloc(const double *phi, size_t ld, size_t npts, int nbf,
                           const double *cxc, const double *cj, double *XC,
                           double *J, void *stream);
 
+/* Device SCF driver: the reference's DFT constructor and DFT::scf
+ * (dft.cpp:57-61, 84-142, 160-227, 300-366, 441-447) with every step on the
+ * GPU.  Per iteration: F = H + 2J + XC, F' = X^T F X, eigen-decomposition of F'
+ * (FP32 Jacobi rotations in one CTA, then FP64 iterative refinement that
+ * separates the occupied and virtual subspaces to FP64 accuracy),
+ * P_new = C_occ C_occ^T with C = X C', P <- (1 - alpha) P_new + alpha P, the
+ * grid Fock build of this context (its precision), and
+ * E = 2 tr(P H) + E_J + E_nuc + E_xc (E_J = 2 tr(P J) in FP64 builds, the FP64
+ * grid sum in mixed builds).  X = U diag(lambda^-1/2) from the eigenpairs of S,
+ * polished in FP64 until X^T S X = I.  dftg_scf_run runs the whole loop as one
+ * CUDA graph launch (a conditional while node whose body ends with the
+ * convergence test), so the host waits once per SCF, not once per iteration. */
+typedef struct dftg_scf_params {
+    int nelec;         /* electrons (even); 0: sum of Z (neutral molecule) */
+    double alpha;      /* weight of the old P in the damping (reference: 0.5) */
+    double tol;        /* stop when |E_n - E_(n-1)| <= tol (reference: 1e-4) */
+    int min_iter;      /* at least this many iterations (reference: 3) */
+    int max_iter;      /* at most this many, <= DFTG_SCF_MAX_ITER (reference: 100) */
+    int refine_steps;  /* FP64 refinement steps per eigen-solve; 0: default 4 */
+} dftg_scf_params;
+#define DFTG_SCF_MAX_NBF 160
+#define DFTG_SCF_MAX_ITER 1000
+/* Set-up (the reference's DFT constructor + construct_matrices): S, T, V, H,
+ * E_nuc, X, the first density from H, its Hartree J and the energy E_0 with
+ * E_xc = 0.  nbf <= DFTG_SCF_MAX_NBF.  Errors: DFTG_ERR_ARG for bad parameters,
+ * DFTG_ERR_STATE for a point-set context or an S that is not positive definite. */
+int dftg_scf_init(dftg_ctx *ctx, const dftg_scf_params *params);
+/* Iterate to convergence (or max_iter).  energy: final E; iterations: count.
+ * Calling it again continues from the current P (as a second DFT::scf would). */
+int dftg_scf_run(dftg_ctx *ctx, double *energy, int *iterations);
+/* One iteration, synchronised (for host-driven loops).  energy: its E;
+ * converged: 1 when the reference's loop would stop after this iteration. */
+int dftg_scf_step(dftg_ctx *ctx, double *energy, int *converged);
+/* Results.  DFTG_SCF_P, _J, _XC, _H, _X: nbf x nbf; DFTG_SCF_EPS: the nbf
+ * orbital energies ascending; DFTG_SCF_COCC: the occupied coefficients
+ * [nocc columns of nbf]; DFTG_SCF_HISTORY: DFTG_SCF_HIST_W values per
+ * iteration {E, 2tr(PH), E_J, E_xc, N, |dE|} of the last run; DFTG_SCF_DIAG:
+ * {max |S'_ij| between occupied and virtual vectors, max |I - C'^T C'|, Jacobi
+ * sweeps, mode (1: conditional-graph loop, 2: host-stepped graphs)} of the last
+ * eigen-solve; DFTG_SCF_STATE: {E (E_0 after dftg_scf_init), iterations of the
+ * current run, last |dE|, 1 if the loop would continue}.  cap: capacity of out
+ * in doubles; n: values written (may be NULL). */
+#define DFTG_SCF_P 0
+#define DFTG_SCF_J 1
+#define DFTG_SCF_XC 2
+#define DFTG_SCF_H 3
+#define DFTG_SCF_X 4
+#define DFTG_SCF_EPS 5
+#define DFTG_SCF_COCC 6
+#define DFTG_SCF_HISTORY 7
+#define DFTG_SCF_DIAG 8
+#define DFTG_SCF_STATE 9
+#define DFTG_SCF_HIST_W 6
+int dftg_scf_get(dftg_ctx *ctx, int what, double *out, size_t cap, size_t *n);
+
 #ifdef __cplusplus
 }
 #endif
