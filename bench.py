@@ -216,6 +216,25 @@ def _scf(grid, mol, S, H, enuc, precision, tol=1e-8, max_iter=200):
         old = E
 
 
+def _device_scf(mol, dev, precision, tol=1e-8, max_iter=200):
+    """The reference SCF (dft.cpp:84-142) run by the device driver: one CUDA
+    graph launch for the whole loop; wall times around set-up and run."""
+    import torch
+    from dftcxx_gb300.grid import DeviceSCF
+    t0 = time.perf_counter()
+    ds = DeviceSCF(mol, 75, 11, 8, precision=precision, device=dev, tol=tol, max_iter=max_iter)
+    t1 = time.perf_counter()
+    E = ds.run()
+    torch.cuda.synchronize(dev)
+    t2 = time.perf_counter()
+    out = {"E_Ha": E, "iterations": ds.iterations, "setup_ms": 1e3 * (t1 - t0), "run_ms": 1e3 * (t2 - t1),
+           "ms_per_iteration": 1e3 * (t2 - t1) / max(1, ds.iterations),
+           "loop": {1: "one conditional-graph launch", 2: "one graph launch per iteration"}[ds.diagnostics()["mode"]],
+           "P": ds.P}
+    ds.close()
+    return out
+
+
 def run_ours(args, rank, world):
     import torch
     from dftcxx_gb300 import build as b
@@ -231,10 +250,18 @@ def run_ours(args, rank, world):
     H = T + V
     enuc = grid.nuclear_repulsion()
 
-    # accuracy: converged SCF in both precisions (outside the timed region)
+    # accuracy: converged SCF in both precisions on the device driver, and the
+    # host-driven loop (numpy eigen-solves) for comparison (outside the timed region)
     t0 = time.perf_counter()
-    E64, P64, it64 = _scf(grid, mol, S, H, enuc, "fp64")
-    Emx, Pmx, itmx = _scf(grid, mol, S, H, enuc, "mixed")
+    scf_dev = {p: _device_scf(mol, dev, p) for p in ("fp64", "mixed")}
+    E64, P64, it64 = scf_dev["fp64"]["E_Ha"], scf_dev["fp64"].pop("P"), scf_dev["fp64"]["iterations"]
+    Emx, Pmx, itmx = scf_dev["mixed"]["E_Ha"], scf_dev["mixed"].pop("P"), scf_dev["mixed"]["iterations"]
+    th = time.perf_counter()
+    Eh, _, ith = _scf(grid, mol, S, H, enuc, "mixed")
+    th = time.perf_counter() - th
+    scf_info = {"device": scf_dev, "host_loop_mixed": {"E_Ha": Eh, "iterations": ith,
+                                                       "ms_per_iteration": 1e3 * th / max(1, ith)},
+                "dE_device_vs_host_loop_mixed_Ha": abs(Emx - Eh)}
     scf_s = time.perf_counter() - t0
     grid.set_precision("fp64")
     r64 = grid.fock_build(P64)
@@ -414,7 +441,7 @@ def run_ours(args, rank, world):
             "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
             "scf_seconds_outside_timing": scf_s,
-            "adjoint": adjoint, "batched": batched, "synthetic": synthetic}
+            "scf": scf_info, "adjoint": adjoint, "batched": batched, "synthetic": synthetic}
 
 
 def _guess_density(grid, mol):

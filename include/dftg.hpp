@@ -10,6 +10,8 @@
 //   DFT            (dft.h, dft.cpp:84-142, 184-226, 300-447): one-electron
 //                  matrices, canonical orthogonalisation, SCF with the
 //                  reference's linear damping, energy
+//   DeviceSCF      the same SCF with every step on the GPU (dftg_scf_*): one
+//                  CUDA graph launch per SCF
 // Matrices are nbf x nbf column-major std::vector<double> (the reference uses
 // Eigen's default column-major MatrixXXd).  Errors from the C ABI are thrown
 // as std::runtime_error on this side of the boundary only.
@@ -335,6 +337,47 @@ private:
     int n_;
     std::vector<double> H_, X_, J_, XC_, P_, history_;
     double enuc_ = 0.0, exc_ = 0.0, ej_ = 0.0, energy_ = 0.0;
+};
+
+// The reference's SCF (dft.cpp:84-142) run by the device driver: set-up in the
+// constructor, scf() iterates to convergence in one CUDA graph launch.
+class DeviceSCF {
+public:
+    DeviceSCF(const Molecule &mol, unsigned radial_points, unsigned lebedev_order, unsigned lmax,
+              int precision = DFTG_PREC_FP64, int device = 0, double tol = 1e-4, int max_iter = 100)
+        : grid_(mol), n_(mol.nbf())
+    {
+        grid_.set_grid_parameters(radial_points, lebedev_order, lmax, device);
+        grid_.set_precision(precision);
+        grid_.create_grid();
+        dftg_scf_params p{0, 0.5, tol, 3, max_iter, 0};
+        check(dftg_scf_init(grid_.ctx(), &p));
+    }
+
+    double scf()
+    {
+        double e = 0.0;
+        check(dftg_scf_run(grid_.ctx(), &e, &iterations_));
+        return e;
+    }
+
+    int iterations() const { return iterations_; }
+
+    std::vector<double> get(int what) const   // DFTG_SCF_P, _J, _XC, _H, _X, _EPS, _HISTORY
+    {
+        std::vector<double> out((size_t)n_ * n_ + (size_t)DFTG_SCF_HIST_W * DFTG_SCF_MAX_ITER);
+        size_t cnt = 0;
+        check(dftg_scf_get(grid_.ctx(), what, out.data(), out.size(), &cnt));
+        out.resize(cnt);
+        return out;
+    }
+
+    MolecularGrid &molgrid() { return grid_; }
+
+private:
+    MolecularGrid grid_;
+    int n_;
+    int iterations_ = 0;
 };
 
 }  // namespace dftg_host

@@ -5,7 +5,8 @@
 //   atom l m n nprim              (nbf lines)
 //   alpha coef                    (nprim lines)
 // and prints "E <energy> ITER <n>" plus the energy of every iteration.
-// usage: host_scf <molecule file> <radial> <lebedev order> <lmax> <fp64|mixed> <tol>
+// usage: host_scf <molecule file> <radial> <lebedev order> <lmax> <fp64|mixed> <tol> [device]
+// With "device" the SCF runs in the device driver (dftg_host::DeviceSCF).
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -41,6 +42,15 @@ int main(int argc, char **argv)
     }
     const int prec = std::string(argv[5]) == "mixed" ? DFTG_PREC_MIXED : DFTG_PREC_FP64;
     try {
+        if (argc > 7 && std::string(argv[7]) == "device") {
+            dftg_host::DeviceSCF scf(mol, (unsigned)std::atoi(argv[2]), (unsigned)std::atoi(argv[3]),
+                                     (unsigned)std::atoi(argv[4]), prec, 0, std::atof(argv[6]));
+            const double e = scf.scf();
+            const std::vector<double> h = scf.get(DFTG_SCF_HISTORY);
+            for (size_t i = 0; i < h.size(); i += DFTG_SCF_HIST_W) std::printf("IT %.15f\n", h[i]);
+            std::printf("E %.15f ITER %d NPTS %zu\n", e, scf.iterations(), scf.molgrid().get_grid_size());
+            return 0;
+        }
         dftg_host::DFT dft(mol, (unsigned)std::atoi(argv[2]), (unsigned)std::atoi(argv[3]), (unsigned)std::atoi(argv[4]),
                            prec);
         const double e = dft.scf(std::atof(argv[6]));

@@ -74,11 +74,15 @@ def test_cpp_mirror_scf_matches_python(gpu_lib, tmp_path):
     mol = Molecule(Z, xyz, "sto3g")
     mf = str(tmp_path / "h2o.txt")
     _write_molecule(mf, mol)
-    r = subprocess.run([exe, mf, "32", "7", "8", "fp64", "1e-8"], capture_output=True, text=True, timeout=300)
-    assert r.returncode == 0, r.stderr
-    last = [l for l in r.stdout.splitlines() if l.startswith("E ")][-1].split()
-    e_cpp, iters = float(last[1]), int(last[3])
     d = DFT(mol, 32, 7, 8, precision="fp64")
     e_py = d.scf(tol=1e-8)
-    assert iters == len(d.history)
-    assert abs(e_cpp - e_py) < 1e-9
+    for mode in ([], ["device"]):
+        r = subprocess.run([exe, mf, "32", "7", "8", "fp64", "1e-8"] + mode, capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stderr
+        last = [l for l in r.stdout.splitlines() if l.startswith("E ")][-1].split()
+        e_cpp, iters = float(last[1]), int(last[3])
+        its = [float(l.split()[1]) for l in r.stdout.splitlines() if l.startswith("IT ")]
+        assert iters == len(d.history) == len(its), mode
+        assert abs(e_cpp - e_py) < 1e-9, mode
+        assert max(abs(a - h["E"]) for a, h in zip(its, d.history)) < 1e-9, mode
