@@ -109,6 +109,8 @@ SIGNATURES = {
     "dftg_batch_fock_build_device": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.c_void_p],
+    "dftg_eri_coulomb": [ctypes.c_void_p, _dp, _dp],
+    "dftg_eri_list": [ctypes.c_void_p, _dp, ctypes.c_size_t],
     "dftg_scf_init": [ctypes.c_void_p, ctypes.POINTER(ScfParams)],
     "dftg_scf_run": [ctypes.c_void_p, _dp, _ip],
     "dftg_scf_step": [ctypes.c_void_p, _dp, _ip],

@@ -196,6 +196,15 @@ class MolecularGrid:
         check(_lib.load().dftg_one_electron(self._h, _ptr(S), _ptr(T), _ptr(V)))
         return np.ascontiguousarray(S), np.ascontiguousarray(T), np.ascontiguousarray(V)
 
+    def eri_coulomb(self, P):
+        """J_ij = sum_kl P_kl (ij|kl) from analytic two-electron integrals on the
+        device (the reference's TWO_ELECTRON_INTEGRALS path, dft.cpp:452-477): an
+        independent check of the grid J."""
+        P = np.asfortranarray(P, dtype=np.float64)
+        J = np.zeros((self.nbf, self.nbf), order="F")
+        check(_lib.load().dftg_eri_coulomb(self._h, _ptr(P), _ptr(J)))
+        return np.ascontiguousarray(J)
+
     def nuclear_repulsion(self):
         e = ctypes.c_double()
         check(_lib.load().dftg_nuclear_repulsion(self._h, ctypes.byref(e)))

@@ -185,6 +185,19 @@ int dftg_get_potential(const dftg_ctx *ctx, double *out, size_t cap);   /* Hartr
 int dftg_one_electron(dftg_ctx *ctx, double *S, double *T, double *V);
 int dftg_nuclear_repulsion(const dftg_ctx *ctx, double *enuc);
 
+/* The reference's analytic Hartree path (Settings::TWO_ELECTRON_INTEGRALS):
+ * J_ij = sum_kl P_kl (ij|kl) (DFT::calculate_hartree_potential_te_int,
+ * dft.cpp:452-477) from two-electron integrals over the context's basis
+ * (DFT::calculate_two_electron_integrals dft.cpp:254-288, Integrator::repulsion
+ * integrals.cpp:185-466), computed on the device in FP64 (McMurchie-Davidson)
+ * without storing the integrals.  An independent check of the grid J of
+ * dftg_calculate_hartree_potential; s, p and d functions.  P, J: host nbf x nbf. */
+int dftg_eri_coulomb(dftg_ctx *ctx, const double *P, double *J);
+/* Every unique (ij|kl) at the reference's teindex position (integrals.cpp:470-486):
+ * pair ij = i(i+1)/2 + j (i >= j), index ij(ij+1)/2 + kl (ij >= kl);
+ * T(T+1)/2 values with T = nbf(nbf+1)/2.  cap: capacity of out in doubles. */
+int dftg_eri_list(dftg_ctx *ctx, double *out, size_t cap);
+
 /* Backward pass of the grid energy (no counterpart in the reference; the
  * forward is the last complete Fock build on the context: dftg_fock_build,
  * dftg_fock_build_device or a batch).  With E = seed_exc * E_xc + seed_ej * E_J,

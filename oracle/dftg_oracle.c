@@ -926,6 +926,115 @@ void orc_one_electron(const orc_t *o, double *S, double *T, double *Vn)
         }
 }
 
+/* ---- two-electron integrals: the reference's analytic Hartree path ----
+ * Restatement of the Taketa-Huzinaga-O-ohata B-array formula that
+ * Integrator::repulsion uses (integrals.cpp:388-466; THO, J. Phys. Soc. Japan
+ * 21 (1966) 2313), with the truncated pi of integrals.cpp:394. */
+static double fact_ratio2(int a, int b) { return fact(a) / fact(b) / fact(a - 2 * b); }   /* integrals.cpp:466 */
+
+static double tho_fb(int i, int l1, int l2, double p, double a, double b, int r, double g)   /* :455-461 */
+{
+    return binomial_prefactor(i, l1, l2, p - a, p - b) * fact_ratio2(i, r) * pow(4.0 * g, r - i);
+}
+
+static void tho_b_array(int l1, int l2, int l3, int l4, double p, double a, double b, double q, double c,
+                        double d, double g1, double g2, double delta, double *arr)   /* :420-452 */
+{
+    const int imax = l1 + l2 + l3 + l4 + 1;
+    for (int i = 0; i < imax; ++i) arr[i] = 0.0;
+    for (int i1 = 0; i1 < l1 + l2 + 1; ++i1)
+        for (int i2 = 0; i2 < l3 + l4 + 1; ++i2)
+            for (int r1 = 0; r1 < i1 / 2 + 1; ++r1)
+                for (int r2 = 0; r2 < i2 / 2 + 1; ++r2)
+                    for (int u = 0; u < (i1 + i2) / 2 - r1 - r2 + 1; ++u) {
+                        const int e = i1 + i2 - 2 * (r1 + r2);
+                        const int idx = e - u;
+                        arr[idx] += tho_fb(i1, l1, l2, p, a, b, r1, g1) * ((i2 & 1) ? -1.0 : 1.0) *
+                                    tho_fb(i2, l3, l4, q, c, d, r2, g2) * ((u & 1) ? -1.0 : 1.0) *
+                                    fact_ratio2(e, u) * ipow(q - p, e - 2 * u) / ipow(delta, e - u);
+                    }
+}
+
+/* primitive (ab|cd) with the norms folded in by the caller (integrals.cpp:388-418) */
+static double eri_prim(const double *A, const int *la, double aa, const double *B, const int *lb, double ab,
+                       const double *C, const int *lc, double ac, const double *D, const int *ld, double ad)
+{
+    const double g1 = aa + ab, g2 = ac + ad, delta = 0.25 * (1.0 / g1 + 1.0 / g2);
+    double P[3], Q[3], rab2 = 0.0, rcd2 = 0.0, rpq2 = 0.0;
+    for (int x = 0; x < 3; ++x) {
+        P[x] = (aa * A[x] + ab * B[x]) / g1;
+        Q[x] = (ac * C[x] + ad * D[x]) / g2;
+        rab2 += (A[x] - B[x]) * (A[x] - B[x]);
+        rcd2 += (C[x] - D[x]) * (C[x] - D[x]);
+    }
+    for (int x = 0; x < 3; ++x) rpq2 += (P[x] - Q[x]) * (P[x] - Q[x]);
+    double bx[17], by[17], bz[17];
+    tho_b_array(la[0], lb[0], lc[0], ld[0], P[0], A[0], B[0], Q[0], C[0], D[0], g1, g2, delta, bx);
+    tho_b_array(la[1], lb[1], lc[1], ld[1], P[1], A[1], B[1], Q[1], C[1], D[1], g1, g2, delta, by);
+    tho_b_array(la[2], lb[2], lc[2], ld[2], P[2], A[2], B[2], Q[2], C[2], D[2], g1, g2, delta, bz);
+    double sum = 0.0;
+    for (int i = 0; i <= la[0] + lb[0] + lc[0] + ld[0]; ++i)
+        for (int j = 0; j <= la[1] + lb[1] + lc[1] + ld[1]; ++j)
+            for (int k = 0; k <= la[2] + lb[2] + lc[2] + ld[2]; ++k)
+                sum += bx[i] * by[j] * bz[k] * orc_fgamma(i + j + k, 0.25 * rpq2 / delta);
+    return 2.0 * pow(ORC_PI_TRUNC, 2.5) / (g1 * g2 * sqrt(g1 + g2)) * exp(-aa * ab * rab2 / g1) *
+           exp(-ac * ad * rcd2 / g2) * sum;
+}
+
+/* contracted (ij|kl), integrals.cpp:185-206 */
+double orc_eri(const orc_t *o, int i, int j, int k, int l)
+{
+    const int f[4] = {i, j, k, l};
+    double s = 0.0;
+    for (int p = o->bf_off[i]; p < o->bf_off[i + 1]; ++p)
+        for (int q = o->bf_off[j]; q < o->bf_off[j + 1]; ++q)
+            for (int r = o->bf_off[k]; r < o->bf_off[k + 1]; ++r)
+                for (int t = o->bf_off[l]; t < o->bf_off[l + 1]; ++t) {
+                    const double pre = o->pc[p] * o->pn[p] * o->pc[q] * o->pn[q] * o->pc[r] * o->pn[r] * o->pc[t] * o->pn[t];
+                    s += pre * eri_prim(o->bf_xyz + 3 * f[0], o->bf_lmn + 3 * f[0], o->pa[p],
+                                        o->bf_xyz + 3 * f[1], o->bf_lmn + 3 * f[1], o->pa[q],
+                                        o->bf_xyz + 3 * f[2], o->bf_lmn + 3 * f[2], o->pa[r],
+                                        o->bf_xyz + 3 * f[3], o->bf_lmn + 3 * f[3], o->pa[t]);
+                }
+    return s;
+}
+
+/* every unique integral at the reference's teindex position (dft.cpp:254-288,
+ * integrals.cpp:470-486): pairs ij = i(i+1)/2 + j (i >= j), index ij(ij+1)/2 + kl (ij >= kl) */
+void orc_eri_list(const orc_t *o, double *out)
+{
+    const long npair = (long)o->nbf * (o->nbf + 1) / 2;
+    #pragma omp parallel for schedule(dynamic)
+    for (long ij = 0; ij < npair; ++ij) {
+        int i = 0;
+        while ((long)(i + 1) * (i + 2) / 2 <= ij) ++i;
+        const int j = (int)(ij - (long)i * (i + 1) / 2);
+        for (long kl = 0; kl <= ij; ++kl) {
+            int k = 0;
+            while ((long)(k + 1) * (k + 2) / 2 <= kl) ++k;
+            const int l = (int)(kl - (long)k * (k + 1) / 2);
+            out[ij * (ij + 1) / 2 + kl] = orc_eri(o, i, j, k, l);
+        }
+    }
+}
+
+/* DFT::calculate_hartree_potential_te_int (dft.cpp:452-477): J_ij = sum_kl P_kl (ij|kl) */
+void orc_eri_coulomb(const orc_t *o, const double *P, double *J)
+{
+    const int n = o->nbf;
+    #pragma omp parallel for schedule(dynamic)
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j <= i; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < n; ++k)
+                for (int l = 0; l <= k; ++l) {
+                    const double pkl = (k == l ? 1.0 : 2.0) * P[k + (size_t)l * n];
+                    if (pkl != 0.0) s += pkl * orc_eri(o, i, j, k, l);
+                }
+            J[i + (size_t)j * n] = J[j + (size_t)i * n] = s;
+        }
+}
+
 /* DFT::calculate_nuclear_repulsion, dft.cpp:235-246 */
 double orc_nuclear_repulsion(const orc_t *o)
 {

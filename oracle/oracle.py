@@ -57,6 +57,12 @@ def lib():
         L.orc_one_electron.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
         L.orc_nuclear_repulsion.restype = ctypes.c_double
         L.orc_nuclear_repulsion.argtypes = [ctypes.c_void_p]
+        L.orc_eri.restype = ctypes.c_double
+        L.orc_eri.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_eri_list.restype = None
+        L.orc_eri_list.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_eri_coulomb.restype = None
+        L.orc_eri_coulomb.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.orc_fgamma.restype = ctypes.c_double
         L.orc_fgamma.argtypes = [ctypes.c_int, ctypes.c_double]
         L.orc_ylm.restype = ctypes.c_double
@@ -184,6 +190,24 @@ class OracleGrid:
 
     def nuclear_repulsion(self):
         return lib().orc_nuclear_repulsion(self.h)
+
+    def eri(self, i, j, k, l):
+        """Contracted (ij|kl), Integrator::repulsion (integrals.cpp:185-466)."""
+        return lib().orc_eri(self.h, i, j, k, l)
+
+    def eri_list(self):
+        """Every unique (ij|kl) at the reference's teindex position (integrals.cpp:470-486)."""
+        npair = self.nbf * (self.nbf + 1) // 2
+        out = np.zeros(npair * (npair + 1) // 2)
+        lib().orc_eri_list(self.h, _p(out))
+        return out
+
+    def eri_coulomb(self, P):
+        """J_ij = sum_kl P_kl (ij|kl), DFT::calculate_hartree_potential_te_int (dft.cpp:452-477)."""
+        P = np.asfortranarray(P, dtype=np.float64)
+        J = np.zeros((self.nbf, self.nbf), order="F")
+        lib().orc_eri_coulomb(self.h, P.ctypes.data_as(_dp), J.ctypes.data_as(_dp))
+        return np.ascontiguousarray(J)
 
     def set_sample_stride(self, stride):
         """Timing-only mode: point loops of the cross-atom potential, J and XC
