@@ -197,23 +197,43 @@ struct GemmOp {
     double *C;
 };
 
+// 8 x 8 output tile per CTA of 64 threads; K in panels of 64 staged in shared
+// memory with coalesced loads (the operands live in L2), then a sequential FMA
+// chain per output element in increasing K.
+constexpr int kGT = 8, kGK = 64;
 __global__ void __launch_bounds__(64) k_scf_gemm(GemmOp g0, GemmOp g1)
 {
+    __shared__ double As[kGK][kGT + 1];   // As[l][r] = op(A)(i0 + r, l0 + l)
+    __shared__ double Bs[kGK][kGT + 1];   // Bs[l][c] = op(B)(l0 + l, j0 + c)
     const GemmOp g = blockIdx.z ? g1 : g0;
-    const int i = blockIdx.x * 8 + (threadIdx.x & 7);
-    const int j = blockIdx.y * 8 + (threadIdx.x >> 3);
-    if (i >= g.m || j >= g.n) return;
-    const int jb = g.bcol ? g.bcol[j] : j;
+    const int i0 = blockIdx.x * kGT, j0 = blockIdx.y * kGT;
+    if (i0 >= g.m || j0 >= g.n) return;   // uniform over the CTA
+    const int ii = threadIdx.x & 7, jj = threadIdx.x >> 3;
     double s = 0.0;
-    if (!g.ta && !g.tb) {
-        for (int l = 0; l < g.k; ++l) s = fma(g.A[i + (size_t)l * g.lda], g.B[l + (size_t)jb * g.ldb], s);
-    } else if (g.ta && !g.tb) {
-        for (int l = 0; l < g.k; ++l) s = fma(g.A[l + (size_t)i * g.lda], g.B[l + (size_t)jb * g.ldb], s);
-    } else if (!g.ta && g.tb) {
-        for (int l = 0; l < g.k; ++l) s = fma(g.A[i + (size_t)l * g.lda], g.B[jb + (size_t)l * g.ldb], s);
-    } else {
-        for (int l = 0; l < g.k; ++l) s = fma(g.A[l + (size_t)i * g.lda], g.B[jb + (size_t)l * g.ldb], s);
+    for (int l0 = 0; l0 < g.k; l0 += kGK) {
+        const int kc = min(kGK, g.k - l0);
+        for (int e = threadIdx.x; e < kGT * kGK; e += 64) {
+            int r, l;   // A element: contiguous along i when not transposed, along l when transposed
+            if (!g.ta) { r = e & 7; l = e >> 3; } else { l = e % kGK; r = e / kGK; }
+            double v = 0.0;
+            if (l < kc && i0 + r < g.m)
+                v = g.ta ? g.A[(l0 + l) + (size_t)(i0 + r) * g.lda] : g.A[(i0 + r) + (size_t)(l0 + l) * g.lda];
+            As[l][r] = v;
+            int cb, lb;  // B element: contiguous along l when not transposed, along j when transposed
+            if (!g.tb) { lb = e % kGK; cb = e / kGK; } else { cb = e & 7; lb = e >> 3; }
+            double w = 0.0;
+            if (lb < kc && j0 + cb < g.n) {
+                const int jb = g.bcol ? g.bcol[j0 + cb] : j0 + cb;
+                w = g.tb ? g.B[jb + (size_t)(l0 + lb) * g.ldb] : g.B[(l0 + lb) + (size_t)jb * g.ldb];
+            }
+            Bs[lb][cb] = w;
+        }
+        __syncthreads();
+        for (int l = 0; l < kc; ++l) s = fma(As[l][ii], Bs[l][jj], s);
+        __syncthreads();
     }
+    const int i = i0 + ii, j = j0 + jj;
+    if (i >= g.m || j >= g.n) return;
     double r = g.alpha * s;
     if (g.beta != 0.0) r += g.beta * g.C0[i + (size_t)j * g.ldc];
     g.C[i + (size_t)j * g.ldc] = r;
@@ -253,35 +273,53 @@ __device__ __forceinline__ double block_max(double v, double *sh)
     return s;
 }
 
-// One refinement step (one CTA): E from G = V^T V and S = V^T A V; the
-// ascending eigenvalue estimates (eps), the permutation that sorts them and
-// the residual diagnostics.
-__global__ void __launch_bounds__(1024) k_scf_refine(int n, int nocc, const double *__restrict__ G,
-                                                     const double *__restrict__ S, double *__restrict__ E,
-                                                     double *__restrict__ eps, int *__restrict__ perm,
-                                                     double *__restrict__ st)
+// integer key with the order of the doubles (negative values: magnitude bits flipped)
+__device__ __forceinline__ long long order_key(double x)
+{
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
+// One refinement step: E from G = V^T V and S = V^T A V over a grid of CTAs
+// (256 elements each).  Every CTA forms the eigenvalue estimates and their
+// ranks (integer keys, ties by index); CTA 0 writes the ascending estimates
+// (eps) and the permutation that sorts them.  The residual maxima go to the
+// state vector by atomicMax on the bits of non-negative doubles (zeroed before
+// the launch), so their value does not depend on the CTA order.
+__global__ void __launch_bounds__(256) k_scf_refine(int n, int nocc, const double *__restrict__ G,
+                                                    const double *__restrict__ S, double *__restrict__ E,
+                                                    double *__restrict__ eps, int *__restrict__ perm,
+                                                    double *__restrict__ st)
 {
     __shared__ double s_lam[kScfMaxN];
+    __shared__ long long s_key[kScfMaxN];
     __shared__ int s_occ[kScfMaxN];
     __shared__ double s_red[32];
     const int tid = threadIdx.x, nt = blockDim.x;
-    for (int i = tid; i < n; i += nt) s_lam[i] = S[i + (size_t)i * n] / G[i + (size_t)i * n];
+    for (int i = tid; i < n; i += nt) {
+        const double l = S[i + (size_t)i * n] / G[i + (size_t)i * n];
+        s_lam[i] = l;
+        s_key[i] = order_key(l);
+    }
     __syncthreads();
     for (int i = tid; i < n; i += nt) {
-        const double li = s_lam[i];
+        const long long ki = s_key[i];
         int rank = 0;
         for (int j = 0; j < n; ++j) {
-            const double lj = s_lam[j];
-            rank += (lj < li || (lj == li && j < i)) ? 1 : 0;
+            const long long kj = s_key[j];
+            rank += (kj < ki || (kj == ki && j < i)) ? 1 : 0;
         }
         s_occ[i] = rank < nocc;
-        perm[rank] = i;
-        eps[rank] = li;
+        if (blockIdx.x == 0) {
+            perm[rank] = i;
+            eps[rank] = s_lam[i];
+        }
     }
     __syncthreads();
     const double tau = kDegenerateRel * st[kStAnorm];
     double cmax = 0.0, rmax = 0.0;
-    for (int idx = tid; idx < n * n; idx += nt) {
+    const int idx = blockIdx.x * nt + tid;
+    if (idx < n * n) {
         const int i = idx % n, j = idx / n;
         const double r = (i == j ? 1.0 : 0.0) - G[idx];
         double e = 0.5 * r;
@@ -289,16 +327,16 @@ __global__ void __launch_bounds__(1024) k_scf_refine(int n, int nocc, const doub
             const double den = s_lam[j] - s_lam[i];
             const double num = S[idx] + s_lam[j] * r;
             if (fabs(den) > tau && fabs(num) < fabs(den)) e = num / den;
-            cmax = fmax(cmax, fabs(S[idx]));
+            cmax = fabs(S[idx]);
         }
-        rmax = fmax(rmax, fabs(r));
+        rmax = fabs(r);
         E[idx] = e;
     }
     cmax = block_max(cmax, s_red);
     rmax = block_max(rmax, s_red);
     if (tid == 0) {
-        st[kStCross] = cmax;
-        st[kStOrth] = rmax;
+        atomicMax(reinterpret_cast<unsigned long long *>(st + kStCross), (unsigned long long)__double_as_longlong(cmax));
+        atomicMax(reinterpret_cast<unsigned long long *>(st + kStOrth), (unsigned long long)__double_as_longlong(rmax));
     }
 }
 
@@ -432,7 +470,8 @@ int eigen_solve(dftg_ctx *c, dftg_scf_state *s, const double *A, bool warm, doub
         const GemmOp g2 = gop(n, n, n, A, n, false, cur, n, false, s->W, n);
         DFTG_TRY_L(gemm(c->stream, g1, &g2));
         DFTG_TRY_L(gemm(c->stream, gop(n, n, n, cur, n, true, s->W, n, false, s->S, n)));
-        k_scf_refine<<<1, 1024, 0, c->stream>>>(n, s->nocc, s->G, s->S, s->E, s->eps, s->perm, s->st);
+        DFTG_CUDA(cudaMemsetAsync(s->st + kStCross, 0, 2 * sizeof(double), c->stream));
+        k_scf_refine<<<(n * n + 255) / 256, 256, 0, c->stream>>>(n, s->nocc, s->G, s->S, s->E, s->eps, s->perm, s->st);
         DFTG_LAUNCH_CHECK();
         DFTG_TRY_L(gemm(c->stream, gop(n, n, n, cur, n, false, s->E, n, false, nxt, n, 1.0, 1.0, cur)));
         std::swap(cur, nxt);

@@ -1,14 +1,18 @@
 """Run a few device-resident grid Fock builds of one workload, for profilers.
 
-    python -m dftcxx_gb300.profile_case [--workload benzene|h2o|decane] [--precision mixed|fp64] [--builds N]
-                                        [--backward N]
+    python -m dftcxx_gb300.profile_case [--workload benzene|h2o|decane|synthetic] [--precision mixed|fp64]
+                                        [--builds N] [--backward N] [--scf N] [--points N] [--nbf N]
 
 Builds the grid (setup kernels), forms the core-Hamiltonian density from the
 device one-electron integrals, then runs N builds through
 dftg_fock_build_device on the context's stream and synchronises; with
 --backward N, N backward passes (dE/dP and forces) of the last build follow.
 Nothing else runs on the GPU, so a profiler sees the setup launches followed
-by N identical builds (and the backward passes).
+by N identical builds (and the backward passes).  --scf N: instead, the device
+SCF driver's set-up and N iterations (one conditional-graph launch; with
+--scf-step one graph launch per iteration, for profilers).
+--workload synthetic: the seeded point-set workload (--points, --nbf; default
+2,000,000 x 512) through dftg_xc_build_device.
 """
 import argparse
 import ctypes
@@ -19,10 +23,14 @@ import numpy as np
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="benzene", choices=["benzene", "h2o", "decane"])
+    ap.add_argument("--workload", default="benzene", choices=["benzene", "h2o", "decane", "synthetic"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--builds", type=int, default=2)
     ap.add_argument("--backward", type=int, default=0)
+    ap.add_argument("--scf", type=int, default=0)
+    ap.add_argument("--scf-step", action="store_true", help="run the SCF iterations as one graph launch each")
+    ap.add_argument("--points", type=int, default=2_000_000)
+    ap.add_argument("--nbf", type=int, default=512)
     args = ap.parse_args(argv)
 
     import torch
@@ -32,6 +40,8 @@ def main(argv=None):
     from .molecule import Molecule, alkane, benzene, h2o
 
     build()
+    if args.workload == "synthetic":
+        return _synthetic(args)
     if args.workload == "benzene":
         Z, xyz = benzene()
         mol, grid = Molecule(Z, xyz, "p631"), (75, 11, 8)
@@ -41,6 +51,18 @@ def main(argv=None):
     else:
         Z, xyz = h2o()
         mol, grid = Molecule(Z, xyz, "sto3g"), (32, 7, 8)
+    if args.scf:
+        from .grid import DeviceSCF
+        d = DeviceSCF(mol, *grid, precision=args.precision, tol=0.0, min_iter=args.scf, max_iter=args.scf)
+        if args.scf_step:
+            for _ in range(args.scf):
+                E, _ = d.step()
+            d.iterations = args.scf
+        else:
+            E = d.run()
+        torch.cuda.synchronize()
+        print("scf iterations %d  E %.10f  diag %s" % (d.iterations, E, d.diagnostics()))
+        return 0
     g = MolecularGrid(mol, *grid, precision=args.precision)
     S, T, V = g.one_electron()
     lam, U = np.linalg.eigh(S)
@@ -66,6 +88,27 @@ def main(argv=None):
     e = g.energies()
     print("builds %d  npts %d  nbf %d  Exc %.10f  EJ %.10f  N %.10f" % (args.builds, g.grid_size, n, e["Exc"], e["EJ"],
                                                                       e["nelec"]))
+    return 0
+
+
+def _synthetic(args):
+    import torch
+    from . import _lib
+    from .grid import PointGrid
+    from .molecule import synthetic_contraction
+    pts, w, lmn, alpha, centres, P = synthetic_contraction(npts=args.points, nbf=args.nbf, nocc=min(128, args.nbf))
+    n = args.nbf
+    g = PointGrid(pts, w, centres, np.arange(n), lmn, np.ones(n, np.int32), alpha, np.ones(n),
+                  precision=args.precision)
+    dP = torch.from_numpy(np.asfortranarray(P).ravel(order="F").copy()).cuda()
+    XC = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+    sc = torch.zeros(2, dtype=torch.float64, device="cuda")
+    L = _lib.load()
+    for _ in range(args.builds):
+        _lib.check(L.dftg_xc_build_device(g.handle, ctypes.c_void_p(dP.data_ptr()), ctypes.c_void_p(XC.data_ptr()),
+                                          ctypes.c_void_p(sc.data_ptr())))
+    torch.cuda.synchronize()
+    print("synthetic builds %d  npts %d  nbf %d  Exc %.10f" % (args.builds, args.points, n, float(sc[0])))
     return 0
 
 
