@@ -17,7 +17,7 @@ namespace dftg {
 
 constexpr int kKB = 32;   // points per shared-memory stage
 
-template <typename T, int R>
+template <typename T, int R, bool WJ>
 __global__ void __launch_bounds__(256) k_contract(int nbf, int pts_per_chunk, size_t npad, const T *__restrict__ phi,
                                                   const T *__restrict__ cxc, const T *__restrict__ cj, int want_xc,
                                                   int want_j, const int2 *__restrict__ tiles,
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(256) k_contract(int nbf, int pts_per_chunk, si
 #pragma unroll
                 for (int j = 0; j < R; ++j) {
                     ax[i][j] += u * fn[j];
-                    aj[i][j] += s * fn[j];
+                    if constexpr (WJ) aj[i][j] += s * fn[j];
                 }
             }
         }
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) k_contract(int nbf, int pts_per_chunk, si
 #pragma unroll
                 for (int j = 0; j < R; ++j) {
                     two_sum_acc(hx[i][j], lx[i][j], (float)ax[i][j]);
-                    two_sum_acc(hj[i][j], lj[i][j], (float)aj[i][j]);
+                    if constexpr (WJ) two_sum_acc(hj[i][j], lj[i][j], (float)aj[i][j]);
                 }
         }
     }
@@ -186,6 +186,15 @@ int contract_setup(dftg_ctx *c)
     return DFTG_OK;
 }
 
+// k_contract with the J accumulators only when J is wanted
+template <typename T, int R>
+static void contract_launch(dim3 grid, cudaStream_t st, int nbf, int per, size_t npad, const T *phi, const T *cxc,
+                            const T *cj, int wx, int wj, const int2 *tiles, double *part)
+{
+    if (wj) k_contract<T, R, true><<<grid, 256, 0, st>>>(nbf, per, npad, phi, cxc, cj, wx, wj, tiles, part);
+    else k_contract<T, R, false><<<grid, 256, 0, st>>>(nbf, per, npad, phi, cxc, cj, wx, wj, tiles, part);
+}
+
 int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
 {
     const int wx = want_xc ? 1 : 0, wj = want_j ? 1 : 0;
@@ -204,11 +213,11 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
     per = (per + kKB - 1) / kKB * kKB;
     dim3 grid((unsigned)c->ntiles, (unsigned)c->nchunk);
     if (!(c->prec_mask & kPrecContract)) {
-        if (R == 5) k_contract<double, 5><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
-        else k_contract<double, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
+        if (R == 5) contract_launch<double, 5>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
+        else contract_launch<double, 4>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
     } else {
-        if (R == 5) k_contract<float, 5><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, c->d_cj32, wx, wj, d_tiles, c->d_part);
-        else k_contract<float, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, c->d_cj32, wx, wj, d_tiles, c->d_part);
+        if (R == 5) contract_launch<float, 5>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, c->d_cj32, wx, wj, d_tiles, c->d_part);
+        else contract_launch<float, 4>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, c->d_cj32, wx, wj, d_tiles, c->d_part);
     }
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "contract");
@@ -228,8 +237,8 @@ int launch_contract_coef(dftg_ctx *c, const double *coef, double *out)
     size_t per = (c->npad + c->nchunk - 1) / c->nchunk;
     per = (per + kKB - 1) / kKB * kKB;
     dim3 grid((unsigned)c->ntiles, (unsigned)c->nchunk);
-    if (R == 5) k_contract<double, 5><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, coef, coef, 1, 0, d_tiles, c->d_part);
-    else k_contract<double, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi, coef, coef, 1, 0, d_tiles, c->d_part);
+    if (R == 5) contract_launch<double, 5>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi, coef, coef, 1, 0, d_tiles, c->d_part);
+    else contract_launch<double, 4>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi, coef, coef, 1, 0, d_tiles, c->d_part);
     DFTG_LAUNCH_CHECK();
     const size_t nn = (size_t)c->nbf * c->nbf;
     k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, tile, c->nchunk, 1, 0, c->d_part,
@@ -246,8 +255,8 @@ int launch_contract_coef32(dftg_ctx *c, const float *coef, double *out)
     size_t per = (c->npad + c->nchunk - 1) / c->nchunk;
     per = (per + kKB - 1) / kKB * kKB;
     dim3 grid((unsigned)c->ntiles, (unsigned)c->nchunk);
-    if (R == 5) k_contract<float, 5><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, coef, coef, 1, 0, d_tiles, c->d_part);
-    else k_contract<float, 4><<<grid, 256, 0, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, coef, coef, 1, 0, d_tiles, c->d_part);
+    if (R == 5) contract_launch<float, 5>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi32, coef, coef, 1, 0, d_tiles, c->d_part);
+    else contract_launch<float, 4>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi32, coef, coef, 1, 0, d_tiles, c->d_part);
     DFTG_LAUNCH_CHECK();
     const size_t nn = (size_t)c->nbf * c->nbf;
     k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, tile, c->nchunk, 1, 0, c->d_part,

@@ -50,62 +50,120 @@ __global__ void __launch_bounds__(128) k_density(int nbf, size_t npad, const T *
     rho[p] = 2.0 * (double)r;
 }
 
-// Mixed path of K3.  P enters as an FP32 hi/lo pair with separate accumulators
-// (the FP32 rounding of P is common to every point and would bias the energy;
-// the roundings of phi and of the accumulation differ point by point).  Each
-// thread owns two points, so every P element read from shared memory feeds
-// four FMAs.
-__global__ void __launch_bounds__(128) k_density_split(int nbf, size_t npad, const float *__restrict__ phi,
-                                                       const double *__restrict__ P, double *__restrict__ rho)
+// P -> FP32 hi + lo (once per build; the density kernel stages from it)
+__global__ void k_split_P(int nn, const double *__restrict__ P, float *__restrict__ P32)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2 *Ps = reinterpret_cast<float2 *>(smem_raw);   // [nbf][16] (hi, lo)
-    const size_t p0 = (size_t)blockIdx.x * 256 + threadIdx.x, p1 = p0 + 128;
-    const bool v1 = p1 < npad;
-    float rh0 = 0.f, rl0 = 0.f, rh1 = 0.f, rl1 = 0.f;
-    for (int n0 = 0; n0 < nbf; n0 += 16) {
-        const int nc = min(16, nbf - n0);
-        __syncthreads();
-        for (int e = threadIdx.x; e < nbf * 16; e += 128) {
-            const int mu = e >> 4, j = e & 15;
-            float2 v = make_float2(0.f, 0.f);
-            if (j < nc) {
-                const double d = P[(size_t)mu * nbf + n0 + j];
-                v.x = (float)d;
-                v.y = (float)(d - (double)v.x);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    const double d = P[i];
+    const float h = (float)d;
+    P32[i] = h;
+    P32[nn + i] = (float)(d - (double)h);
+}
+
+// Mixed path of K3 on the CUDA cores (any nbf; the tensor-core form covers
+// nbf <= 128).  P enters as an FP32 hi/lo pair with separate accumulators (the
+// FP32 rounding of P is common to every point and would bias the energy; the
+// roundings of phi and of the accumulation differ point by point).  Register
+// tiling as in an SGEMM: a CTA takes 64 points and walks the columns of P in
+// tiles of 128; a thread owns 4 points x 8 columns (hi and lo accumulators)
+// fed from shared-memory stages of 32 basis functions (phi rows, P rows): 64
+// FMAs per five 16-byte shared loads.  After a column tile each thread dots its
+// eight columns with phi_nu at its points, the 16 column groups are summed in a
+// fixed order and the tiles are summed in FP64.
+constexpr int kDtPts = 64, kDtCols = 128, kDtK = 32, kDtThreads = 256;
+struct DtSmem {
+    float phi[kDtK][kDtPts];
+    float ph[kDtK][kDtCols];
+    float pl[kDtK][kDtCols];
+    float red[2][kDtThreads / 16][kDtPts];
+};
+
+__global__ void __launch_bounds__(kDtThreads) k_density_tiled(int nbf, size_t npad, const float *__restrict__ phi,
+                                                              const float *__restrict__ P32, double *__restrict__ rho)
+{
+    __shared__ __align__(16) DtSmem sm;
+    const int tid = threadIdx.x, pg = tid & 15, cg = tid >> 4;   // points 4 pg .. +3, columns 8 cg .. +7
+    const size_t p0 = (size_t)blockIdx.x * kDtPts;
+    const size_t nn = (size_t)nbf * nbf;
+    double rsum = 0.0;
+    for (int c0 = 0; c0 < nbf; c0 += kDtCols) {
+        float ah[4][8], al[4][8];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) { ah[i][j] = 0.f; al[i][j] = 0.f; }
+        for (int k0 = 0; k0 < nbf; k0 += kDtK) {
+            __syncthreads();
+            for (int e = tid; e < kDtK * kDtPts / 4; e += kDtThreads) {
+                const int kk = e / (kDtPts / 4), q = e % (kDtPts / 4);
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (k0 + kk < nbf) v = *reinterpret_cast<const float4 *>(phi + (size_t)(k0 + kk) * npad + p0 + 4 * q);
+                *reinterpret_cast<float4 *>(&sm.phi[kk][4 * q]) = v;
             }
-            Ps[e] = v;
+            for (int e = tid; e < kDtK * kDtCols; e += kDtThreads) {
+                const int kk = e / kDtCols, cc = e % kDtCols;
+                const int mu = k0 + kk, nu = c0 + cc;
+                float h = 0.f, l = 0.f;
+                if (mu < nbf && nu < nbf) {      // P symmetric: row mu read along nu
+                    const size_t o = (size_t)nu + (size_t)mu * nbf;
+                    h = P32[o];
+                    l = P32[nn + o];
+                }
+                sm.ph[kk][cc] = h;
+                sm.pl[kk][cc] = l;
+            }
+            __syncthreads();
+#pragma unroll 4
+            for (int kk = 0; kk < kDtK; ++kk) {
+                const float4 f = *reinterpret_cast<const float4 *>(&sm.phi[kk][4 * pg]);
+                const float4 h0 = *reinterpret_cast<const float4 *>(&sm.ph[kk][8 * cg]);
+                const float4 h1 = *reinterpret_cast<const float4 *>(&sm.ph[kk][8 * cg + 4]);
+                const float4 l0 = *reinterpret_cast<const float4 *>(&sm.pl[kk][8 * cg]);
+                const float4 l1 = *reinterpret_cast<const float4 *>(&sm.pl[kk][8 * cg + 4]);
+                const float fv[4] = {f.x, f.y, f.z, f.w};
+                const float hv[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+                const float lv[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        ah[i][j] = fmaf(fv[i], hv[j], ah[i][j]);
+                        al[i][j] = fmaf(fv[i], lv[j], al[i][j]);
+                    }
+            }
+        }
+        // this tile's columns dotted with phi_nu at the thread's points
+        float sh[4] = {0.f, 0.f, 0.f, 0.f}, sl[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int nu = c0 + 8 * cg + j;
+            if (nu < nbf) {
+                const float4 g = *reinterpret_cast<const float4 *>(phi + (size_t)nu * npad + p0 + 4 * pg);
+                const float gv[4] = {g.x, g.y, g.z, g.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    sh[i] = fmaf(ah[i][j], gv[i], sh[i]);
+                    sl[i] = fmaf(al[i][j], gv[i], sl[i]);
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            sm.red[0][cg][4 * pg + i] = sh[i];
+            sm.red[1][cg][4 * pg + i] = sl[i];
         }
         __syncthreads();
-        float ah0[16], al0[16], ah1[16], al1[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) { ah0[j] = 0.f; al0[j] = 0.f; ah1[j] = 0.f; al1[j] = 0.f; }
-        for (int mu = 0; mu < nbf; ++mu) {
-            const float f0 = phi[(size_t)mu * npad + p0];
-            const float f1 = v1 ? phi[(size_t)mu * npad + p1] : 0.f;
-            const float2 *pr = Ps + mu * 16;
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const float2 q = pr[j];
-                ah0[j] = fmaf(f0, q.x, ah0[j]);
-                al0[j] = fmaf(f0, q.y, al0[j]);
-                ah1[j] = fmaf(f1, q.x, ah1[j]);
-                al1[j] = fmaf(f1, q.y, al1[j]);
+        if (tid < kDtPts) {
+            float h = 0.f, l = 0.f;
+            for (int g = 0; g < kDtThreads / 16; ++g) {
+                h += sm.red[0][g][tid];
+                l += sm.red[1][g][tid];
             }
+            rsum += (double)h + (double)l;
         }
-#pragma unroll
-        for (int j = 0; j < 16; ++j)
-            if (j < nc) {
-                const float g0 = phi[(size_t)(n0 + j) * npad + p0];
-                const float g1 = v1 ? phi[(size_t)(n0 + j) * npad + p1] : 0.f;
-                rh0 = fmaf(ah0[j], g0, rh0);
-                rl0 = fmaf(al0[j], g0, rl0);
-                rh1 = fmaf(ah1[j], g1, rh1);
-                rl1 = fmaf(al1[j], g1, rl1);
-            }
     }
-    rho[p0] = 2.0 * ((double)rh0 + (double)rl0);
-    if (v1) rho[p1] = 2.0 * ((double)rh1 + (double)rl1);
+    if (tid < kDtPts) rho[p0 + tid] = 2.0 * rsum;
 }
 
 // stage 1: partial sums of w*rho over chunks that never straddle two atoms
@@ -253,10 +311,11 @@ int launch_density(dftg_ctx *c)
     } else if (c->tc_ready) {
         DFTG_TRY_L(launch_density_tc(c));
     } else {
-        const unsigned nb = (unsigned)((c->npad + 255) / 256);
-        const size_t sm = (size_t)c->nbf * 16 * sizeof(float2);
-        if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_density_split), c->device));
-        k_density_split<<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi32, c->d_P, c->d_rho);
+        const int nn = c->nbf * c->nbf;
+        k_split_P<<<(nn + 255) / 256, 256, 0, c->stream>>>(nn, c->d_P, c->d_P32);
+        DFTG_LAUNCH_CHECK();
+        k_density_tiled<<<(unsigned)(c->npad / kDtPts), kDtThreads, 0, c->stream>>>(c->nbf, c->npad, c->d_phi32,
+                                                                                   c->d_P32, c->d_rho);
     }
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "density");
