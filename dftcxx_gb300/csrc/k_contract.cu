@@ -159,6 +159,124 @@ __global__ void __launch_bounds__(256) k_contract_reduce(int nbf, int tile, int 
     }
 }
 
+// XC-only FP32 form for nbf > 128 (point sets, the dE/dP contraction of the
+// backward pass): out = phi^T diag(coef) phi.  Output tiles of 128 (mu) x 64
+// (nu) with block128(mu) <= block128(nu), split over point chunks like
+// k_contract.  Per stage of 32 points, c o phi_mu (128 rows) and phi_nu (64 rows)
+// are staged point-contiguous (row stride 36 floats: 16-byte rows, consecutive
+// rows in distinct bank groups); thread (tx, ty) owns rows tx + 16 i (i < 8) and
+// columns ty + 16 j (j < 4) and per four points loads 8 + 4 float4 for 128 FMAs.
+// Stage sums are carried across stages as TwoSum pairs (as k_contract<float>).
+constexpr int kXtM = 128, kXtN = 64, kXtK = 32, kXtLd = 36;
+
+__host__ __device__ inline int xc32_tiles(int nbf)
+{
+    const int n128 = (nbf + kXtM - 1) / kXtM, n64 = (nbf + kXtN - 1) / kXtN;
+    int t = 0;
+    for (int mt = 0; mt < n128; ++mt) t += n64 - 2 * mt > 0 ? n64 - 2 * mt : 0;
+    return t;
+}
+
+__device__ __forceinline__ void cp_async16(float *dst, const float *src)
+{
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+
+// one stage's panels: phi rows m0.. (A, scaled by coef after landing) and n0.. (B)
+__device__ __forceinline__ void xc32_issue(float *As, float *Bs, int nbf, size_t npad, const float *phi, int m0, int n0,
+                                           size_t kb, int tid)
+{
+    for (int e = tid; e < kXtM * (kXtK / 4); e += 256) {
+        const int row = e >> 3, q = e & 7;
+        float *d = As + row * kXtLd + 4 * q;
+        if (m0 + row < nbf) cp_async16(d, phi + (size_t)(m0 + row) * npad + kb + 4 * q);
+        else *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    for (int e = tid; e < kXtN * (kXtK / 4); e += 256) {
+        const int row = e >> 3, q = e & 7;
+        float *d = Bs + row * kXtLd + 4 * q;
+        if (n0 + row < nbf) cp_async16(d, phi + (size_t)(n0 + row) * npad + kb + 4 * q);
+        else *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(256) k_contract_xc32(int nbf, int pts_per_chunk, size_t npad,
+                                                       const float *__restrict__ phi, const float *__restrict__ coef,
+                                                       double *__restrict__ part)
+{
+    extern __shared__ __align__(16) float xsm[];   // two stages of As [128][36], Bs [64][36]
+    const int n64 = (nbf + kXtN - 1) / kXtN;
+    int t = blockIdx.x, mt = 0;
+    while (t >= n64 - 2 * mt) { t -= n64 - 2 * mt; ++mt; }
+    const int m0 = mt * kXtM, n0 = (2 * mt + t) * kXtN;
+    const int chunk = blockIdx.y;
+    const size_t pb = (size_t)chunk * pts_per_chunk;
+    const size_t pe = min(npad, pb + (size_t)pts_per_chunk);
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    constexpr int kStageF = (kXtM + kXtN) * kXtLd;
+    float ax[8][4], hx[8][4], lx[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { ax[i][j] = 0.f; hx[i][j] = 0.f; lx[i][j] = 0.f; }
+    if (pb < pe) xc32_issue(xsm, xsm + kXtM * kXtLd, nbf, npad, phi, m0, n0, pb, tid);
+    int buf = 0;
+    for (size_t kb = pb; kb < pe; kb += kXtK, buf ^= 1) {
+        float *As = xsm + buf * kStageF, *Bs = As + kXtM * kXtLd;
+        if (kb + kXtK < pe) {
+            float *An = xsm + (buf ^ 1) * kStageF;
+            xc32_issue(An, An + kXtM * kXtLd, nbf, npad, phi, m0, n0, kb + kXtK, tid);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();
+        // c o phi_mu: row-wise scaling of the landed A panel
+        for (int e = tid; e < kXtM * kXtK; e += 256) {
+            const int row = e >> 5, k = e & 31;
+            As[row * kXtLd + k] *= coef[kb + k];
+        }
+        __syncthreads();
+#pragma unroll 2
+        for (int k4 = 0; k4 < kXtK / 4; ++k4) {
+            float4 a[8], b[4];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) a[i] = *reinterpret_cast<const float4 *>(As + (tx + 16 * i) * kXtLd + 4 * k4);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = *reinterpret_cast<const float4 *>(Bs + (ty + 16 * j) * kXtLd + 4 * k4);
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    ax[i][j] = fmaf(a[i].x, b[j].x, ax[i][j]);
+                    ax[i][j] = fmaf(a[i].y, b[j].y, ax[i][j]);
+                    ax[i][j] = fmaf(a[i].z, b[j].z, ax[i][j]);
+                    ax[i][j] = fmaf(a[i].w, b[j].w, ax[i][j]);
+                }
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                two_sum_acc(hx[i][j], lx[i][j], ax[i][j]);
+                ax[i][j] = 0.f;
+            }
+        __syncthreads();   // this buffer is refilled by the prefetch of the next iteration
+    }
+    double *px = part + (size_t)chunk * 2 * nbf * nbf;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int mu = m0 + tx + 16 * i, nu = n0 + ty + 16 * j;
+            if (mu < nbf && nu < nbf) px[(size_t)mu * nbf + nu] = (double)hx[i][j] + (double)lx[i][j];
+        }
+}
+
+constexpr size_t kXtSmem = 2 * (size_t)(kXtM + kXtN) * kXtLd * sizeof(float);
+
 static int tile_R(int nbf) { return nbf <= 80 ? 5 : 4; }
 
 size_t contract_part_elems(int nbf, size_t npad)
@@ -167,6 +285,7 @@ size_t contract_part_elems(int nbf, size_t npad)
     const int nt = (nbf + tile - 1) / tile;
     const int npairs = nt * (nt + 1) / 2;
     int nchunk = (2 * 152 + npairs - 1) / npairs;
+    if (nbf > 128) nchunk = max(nchunk, (4 * 152 + xc32_tiles(nbf) - 1) / xc32_tiles(nbf));
     const size_t max_chunks = npad / (4 * kKB);
     if ((size_t)nchunk > max_chunks) nchunk = (int)(max_chunks > 0 ? max_chunks : 1);
     return (size_t)nchunk * 2 * nbf * nbf;
@@ -215,6 +334,17 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
     if (!(c->prec_mask & kPrecContract)) {
         if (R == 5) contract_launch<double, 5>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
         else contract_launch<double, 4>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
+    } else if (!want_j && c->nbf > 128) {
+        const dim3 g2((unsigned)xc32_tiles(c->nbf), (unsigned)c->nchunk);
+        DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_contract_xc32), c->device));
+        k_contract_xc32<<<g2, 256, kXtSmem, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, c->d_part);
+        DFTG_LAUNCH_CHECK();
+        DFTG_MARK(c, "contract");
+        k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, kXtM, c->nchunk, wx, wj, c->d_part,
+                                                                             c->d_XC, c->d_J);
+        DFTG_LAUNCH_CHECK();
+        DFTG_MARK(c, "contract_reduce");
+        return DFTG_OK;
     } else {
         if (R == 5) contract_launch<float, 5>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, c->d_cj32, wx, wj, d_tiles, c->d_part);
         else contract_launch<float, 4>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, c->d_cj32, wx, wj, d_tiles, c->d_part);
@@ -255,11 +385,20 @@ int launch_contract_coef32(dftg_ctx *c, const float *coef, double *out)
     size_t per = (c->npad + c->nchunk - 1) / c->nchunk;
     per = (per + kKB - 1) / kKB * kKB;
     dim3 grid((unsigned)c->ntiles, (unsigned)c->nchunk);
-    if (R == 5) contract_launch<float, 5>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi32, coef, coef, 1, 0, d_tiles, c->d_part);
-    else contract_launch<float, 4>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi32, coef, coef, 1, 0, d_tiles, c->d_part);
+    int rtile = tile;
+    if (c->nbf > 128) {
+        const dim3 g2((unsigned)xc32_tiles(c->nbf), (unsigned)c->nchunk);
+        DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_contract_xc32), c->device));
+        k_contract_xc32<<<g2, 256, kXtSmem, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, coef, c->d_part);
+        rtile = kXtM;
+    } else if (R == 5) {
+        contract_launch<float, 5>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi32, coef, coef, 1, 0, d_tiles, c->d_part);
+    } else {
+        contract_launch<float, 4>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi32, coef, coef, 1, 0, d_tiles, c->d_part);
+    }
     DFTG_LAUNCH_CHECK();
     const size_t nn = (size_t)c->nbf * c->nbf;
-    k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, tile, c->nchunk, 1, 0, c->d_part,
+    k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, rtile, c->nchunk, 1, 0, c->d_part,
                                                                         out, nullptr);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
