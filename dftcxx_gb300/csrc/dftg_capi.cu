@@ -165,7 +165,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(dalloc(&c->d_phi, np * c->nbf));
     DFTG_TRY(dalloc(&c->d_phi32, np * c->nbf));
     DFTG_TRY(dalloc(&c->d_P, nn));
-    DFTG_TRY(dalloc(&c->d_P32, 2 * nn));   // FP32 hi, lo of P
+    DFTG_TRY(dalloc(&c->d_P32, 2 * (size_t)c->nbf * ((c->nbf + 3) / 4 * 4)));   // FP32 hi, lo of P, rows padded to 4
     DFTG_TRY(dalloc(&c->d_J, nn));
     DFTG_TRY(dalloc(&c->d_XC, nn));
     int nsm = 0;
@@ -465,7 +465,7 @@ static int build_points_ctx(dftg_ctx *c, const dftg_points *pts, const dftg_mole
     DFTG_TRY(dalloc(&c->d_phi, np * c->nbf));
     DFTG_TRY(dalloc(&c->d_phi32, np * c->nbf));
     DFTG_TRY(dalloc(&c->d_P, nn));
-    DFTG_TRY(dalloc(&c->d_P32, 2 * nn));   // FP32 hi, lo of P
+    DFTG_TRY(dalloc(&c->d_P32, 2 * (size_t)c->nbf * ((c->nbf + 3) / 4 * 4)));   // FP32 hi, lo of P, rows padded to 4
     DFTG_TRY(dalloc(&c->d_J, nn));
     DFTG_TRY(dalloc(&c->d_XC, nn));
     int nsm = 0;

@@ -161,7 +161,7 @@ struct dftg_ctx {
 
     // device: matrices
     double *d_P = nullptr;
-    float *d_P32 = nullptr;       // [2][nbf][nbf] FP32 hi and lo of P (mixed CUDA-core density)
+    float *d_P32 = nullptr;       // [2][nbf][ldp] FP32 hi and lo of P, ldp = nbf rounded up to 4 (mixed CUDA-core density)
     double *d_J = nullptr, *d_XC = nullptr;
     double *d_part = nullptr;     // contraction partials [nchunk][2][nbf][nbf]
     size_t part_elems = 0;

@@ -50,15 +50,21 @@ __global__ void __launch_bounds__(128) k_density(int nbf, size_t npad, const T *
     rho[p] = 2.0 * (double)r;
 }
 
-// P -> FP32 hi + lo (once per build; the density kernel stages from it)
-__global__ void k_split_P(int nn, const double *__restrict__ P, float *__restrict__ P32)
+// P -> FP32 hi + lo (once per build; the density kernel stages from it), rows
+// of ldp = nbf rounded up to 4 (16-byte rows), the padding zero
+__global__ void k_split_P(int nbf, int ldp, const double *__restrict__ P, float *__restrict__ P32)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nn) return;
-    const double d = P[i];
-    const float h = (float)d;
+    if (i >= nbf * ldp) return;
+    const int mu = i / ldp, nu = i - mu * ldp;
+    float h = 0.f, l = 0.f;
+    if (nu < nbf) {
+        const double d = P[(size_t)mu * nbf + nu];
+        h = (float)d;
+        l = (float)(d - (double)h);
+    }
     P32[i] = h;
-    P32[nn + i] = (float)(d - (double)h);
+    P32[(size_t)nbf * ldp + i] = l;
 }
 
 // Mixed path of K3 on the CUDA cores (any nbf; the tensor-core form covers
@@ -68,99 +74,134 @@ __global__ void k_split_P(int nn, const double *__restrict__ P, float *__restric
 // tiling as in an SGEMM: a CTA takes 64 points and walks the columns of P in
 // tiles of 128; a thread owns 4 points x 8 columns (hi and lo accumulators)
 // fed from shared-memory stages of 32 basis functions (phi rows, P rows): 64
-// FMAs per five 16-byte shared loads.  After a column tile each thread dots its
-// eight columns with phi_nu at its points, the 16 column groups are summed in a
-// fixed order and the tiles are summed in FP64.
+// FMAs per five 16-byte shared loads.  The stages are double-buffered with
+// cp.async copies.  After a column tile each thread dots its eight columns with
+// phi_nu at its points, the 16 column groups are summed in a fixed order and
+// the tiles are summed in FP64.
 constexpr int kDtPts = 64, kDtCols = 128, kDtK = 32, kDtThreads = 256;
-struct DtSmem {
+struct DtStage {
     float phi[kDtK][kDtPts];
     float ph[kDtK][kDtCols];
     float pl[kDtK][kDtCols];
+};
+struct DtSmem {
+    DtStage st[2];
     float red[2][kDtThreads / 16][kDtPts];
 };
 
-__global__ void __launch_bounds__(kDtThreads) k_density_tiled(int nbf, size_t npad, const float *__restrict__ phi,
+__device__ __forceinline__ void dt_cp16(float *dst, const float *src)
+{
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+
+// stage (column tile c0, basis functions k0..k0+31) into buffer s
+__device__ __forceinline__ void dt_issue(DtStage &s, int nbf, int ldp, size_t npad, const float *phi,
+                                         const float *P32, size_t p0, int c0, int k0, int tid)
+{
+    for (int e = tid; e < kDtK * kDtPts / 4; e += kDtThreads) {
+        const int kk = e / (kDtPts / 4), q = e % (kDtPts / 4);
+        float *d = &s.phi[kk][4 * q];
+        if (k0 + kk < nbf) dt_cp16(d, phi + (size_t)(k0 + kk) * npad + p0 + 4 * q);
+        else *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const size_t lo = (size_t)nbf * ldp;
+    for (int e = tid; e < kDtK * kDtCols / 4; e += kDtThreads) {
+        const int kk = e / (kDtCols / 4), q = e % (kDtCols / 4);
+        const int mu = k0 + kk, nu = c0 + 4 * q;   // P symmetric: row mu read along nu
+        float *dh = &s.ph[kk][4 * q], *dl = &s.pl[kk][4 * q];
+        if (mu < nbf && nu < ldp) {
+            const size_t o = (size_t)mu * ldp + nu;
+            dt_cp16(dh, P32 + o);
+            dt_cp16(dl, P32 + lo + o);
+        } else {
+            *reinterpret_cast<float4 *>(dh) = make_float4(0.f, 0.f, 0.f, 0.f);
+            *reinterpret_cast<float4 *>(dl) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kDtThreads) k_density_tiled(int nbf, int ldp, size_t npad,
+                                                              const float *__restrict__ phi,
                                                               const float *__restrict__ P32, double *__restrict__ rho)
 {
-    __shared__ __align__(16) DtSmem sm;
+    extern __shared__ __align__(16) unsigned char dt_raw[];
+    DtSmem &sm = *reinterpret_cast<DtSmem *>(dt_raw);
     const int tid = threadIdx.x, pg = tid & 15, cg = tid >> 4;   // points 4 pg .. +3, columns 8 cg .. +7
     const size_t p0 = (size_t)blockIdx.x * kDtPts;
-    const size_t nn = (size_t)nbf * nbf;
+    const int nk = (nbf + kDtK - 1) / kDtK, nc = (nbf + kDtCols - 1) / kDtCols, nstage = nk * nc;
     double rsum = 0.0;
-    for (int c0 = 0; c0 < nbf; c0 += kDtCols) {
-        float ah[4][8], al[4][8];
+    float ah[4][8], al[4][8];
+    dt_issue(sm.st[0], nbf, ldp, npad, phi, P32, p0, 0, 0, tid);
+    for (int s = 0; s < nstage; ++s) {
+        const int ct = s / nk, kt = s - ct * nk;
+        if (kt == 0) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int j = 0; j < 8; ++j) { ah[i][j] = 0.f; al[i][j] = 0.f; }
-        for (int k0 = 0; k0 < nbf; k0 += kDtK) {
-            __syncthreads();
-            for (int e = tid; e < kDtK * kDtPts / 4; e += kDtThreads) {
-                const int kk = e / (kDtPts / 4), q = e % (kDtPts / 4);
-                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (k0 + kk < nbf) v = *reinterpret_cast<const float4 *>(phi + (size_t)(k0 + kk) * npad + p0 + 4 * q);
-                *reinterpret_cast<float4 *>(&sm.phi[kk][4 * q]) = v;
-            }
-            for (int e = tid; e < kDtK * kDtCols; e += kDtThreads) {
-                const int kk = e / kDtCols, cc = e % kDtCols;
-                const int mu = k0 + kk, nu = c0 + cc;
-                float h = 0.f, l = 0.f;
-                if (mu < nbf && nu < nbf) {      // P symmetric: row mu read along nu
-                    const size_t o = (size_t)nu + (size_t)mu * nbf;
-                    h = P32[o];
-                    l = P32[nn + o];
-                }
-                sm.ph[kk][cc] = h;
-                sm.pl[kk][cc] = l;
-            }
-            __syncthreads();
-#pragma unroll 4
-            for (int kk = 0; kk < kDtK; ++kk) {
-                const float4 f = *reinterpret_cast<const float4 *>(&sm.phi[kk][4 * pg]);
-                const float4 h0 = *reinterpret_cast<const float4 *>(&sm.ph[kk][8 * cg]);
-                const float4 h1 = *reinterpret_cast<const float4 *>(&sm.ph[kk][8 * cg + 4]);
-                const float4 l0 = *reinterpret_cast<const float4 *>(&sm.pl[kk][8 * cg]);
-                const float4 l1 = *reinterpret_cast<const float4 *>(&sm.pl[kk][8 * cg + 4]);
-                const float fv[4] = {f.x, f.y, f.z, f.w};
-                const float hv[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
-                const float lv[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        ah[i][j] = fmaf(fv[i], hv[j], ah[i][j]);
-                        al[i][j] = fmaf(fv[i], lv[j], al[i][j]);
-                    }
-            }
+                for (int j = 0; j < 8; ++j) { ah[i][j] = 0.f; al[i][j] = 0.f; }
         }
-        // this tile's columns dotted with phi_nu at the thread's points
-        float sh[4] = {0.f, 0.f, 0.f, 0.f}, sl[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int nu = c0 + 8 * cg + j;
-            if (nu < nbf) {
-                const float4 g = *reinterpret_cast<const float4 *>(phi + (size_t)nu * npad + p0 + 4 * pg);
-                const float gv[4] = {g.x, g.y, g.z, g.w};
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    sh[i] = fmaf(ah[i][j], gv[i], sh[i]);
-                    sl[i] = fmaf(al[i][j], gv[i], sl[i]);
-                }
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            sm.red[0][cg][4 * pg + i] = sh[i];
-            sm.red[1][cg][4 * pg + i] = sl[i];
+        if (s + 1 < nstage) {
+            const int ct1 = (s + 1) / nk, kt1 = s + 1 - ct1 * nk;
+            dt_issue(sm.st[(s + 1) & 1], nbf, ldp, npad, phi, P32, p0, ct1 * kDtCols, kt1 * kDtK, tid);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
-        if (tid < kDtPts) {
-            float h = 0.f, l = 0.f;
-            for (int g = 0; g < kDtThreads / 16; ++g) {
-                h += sm.red[0][g][tid];
-                l += sm.red[1][g][tid];
+        const DtStage &st = sm.st[s & 1];
+#pragma unroll 4
+        for (int kk = 0; kk < kDtK; ++kk) {
+            const float4 f = *reinterpret_cast<const float4 *>(&st.phi[kk][4 * pg]);
+            const float4 h0 = *reinterpret_cast<const float4 *>(&st.ph[kk][8 * cg]);
+            const float4 h1 = *reinterpret_cast<const float4 *>(&st.ph[kk][8 * cg + 4]);
+            const float4 l0 = *reinterpret_cast<const float4 *>(&st.pl[kk][8 * cg]);
+            const float4 l1 = *reinterpret_cast<const float4 *>(&st.pl[kk][8 * cg + 4]);
+            const float fv[4] = {f.x, f.y, f.z, f.w};
+            const float hv[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+            const float lv[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    ah[i][j] = fmaf(fv[i], hv[j], ah[i][j]);
+                    al[i][j] = fmaf(fv[i], lv[j], al[i][j]);
+                }
+        }
+        __syncthreads();   // the buffer is refilled by the next prefetch
+        if (kt == nk - 1) {
+            // this column tile dotted with phi_nu at the thread's points
+            const int c0 = ct * kDtCols;
+            float sh[4] = {0.f, 0.f, 0.f, 0.f}, sl[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int nu = c0 + 8 * cg + j;
+                if (nu < nbf) {
+                    const float4 g = *reinterpret_cast<const float4 *>(phi + (size_t)nu * npad + p0 + 4 * pg);
+                    const float gv[4] = {g.x, g.y, g.z, g.w};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        sh[i] = fmaf(ah[i][j], gv[i], sh[i]);
+                        sl[i] = fmaf(al[i][j], gv[i], sl[i]);
+                    }
+                }
             }
-            rsum += (double)h + (double)l;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                sm.red[0][cg][4 * pg + i] = sh[i];
+                sm.red[1][cg][4 * pg + i] = sl[i];
+            }
+            __syncthreads();
+            if (tid < kDtPts) {
+                float h = 0.f, l = 0.f;
+                for (int g = 0; g < kDtThreads / 16; ++g) {
+                    h += sm.red[0][g][tid];
+                    l += sm.red[1][g][tid];
+                }
+                rsum += (double)h + (double)l;
+            }
+            __syncthreads();   // red is rewritten after the next column tile
         }
     }
     if (tid < kDtPts) rho[p0 + tid] = 2.0 * rsum;
@@ -311,11 +352,12 @@ int launch_density(dftg_ctx *c)
     } else if (c->tc_ready) {
         DFTG_TRY_L(launch_density_tc(c));
     } else {
-        const int nn = c->nbf * c->nbf;
-        k_split_P<<<(nn + 255) / 256, 256, 0, c->stream>>>(nn, c->d_P, c->d_P32);
+        const int ldp = (c->nbf + 3) / 4 * 4, n = c->nbf * ldp;
+        k_split_P<<<(n + 255) / 256, 256, 0, c->stream>>>(c->nbf, ldp, c->d_P, c->d_P32);
         DFTG_LAUNCH_CHECK();
-        k_density_tiled<<<(unsigned)(c->npad / kDtPts), kDtThreads, 0, c->stream>>>(c->nbf, c->npad, c->d_phi32,
-                                                                                   c->d_P32, c->d_rho);
+        DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_density_tiled), c->device));
+        k_density_tiled<<<(unsigned)(c->npad / kDtPts), kDtThreads, sizeof(DtSmem), c->stream>>>(
+            c->nbf, ldp, c->npad, c->d_phi32, c->d_P32, c->d_rho);
     }
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "density");
