@@ -204,7 +204,7 @@ __device__ __forceinline__ void xc32_issue(float *As, float *Bs, int nbf, size_t
 
 __global__ void __launch_bounds__(256) k_contract_xc32(int nbf, int pts_per_chunk, size_t npad,
                                                        const float *__restrict__ phi, const float *__restrict__ coef,
-                                                       double *__restrict__ part)
+                                                       int slot, double *__restrict__ part)
 {
     extern __shared__ __align__(16) float xsm[];   // two stages of As [128][36], Bs [64][36]
     const int n64 = (nbf + kXtN - 1) / kXtN;
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(256) k_contract_xc32(int nbf, int pts_per_chun
             }
         __syncthreads();   // this buffer is refilled by the prefetch of the next iteration
     }
-    double *px = part + (size_t)chunk * 2 * nbf * nbf;
+    double *px = part + ((size_t)chunk * 2 + slot) * nbf * nbf;   // slot 0: XC, 1: J
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
@@ -334,10 +334,16 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
     if (!(c->prec_mask & kPrecContract)) {
         if (R == 5) contract_launch<double, 5>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
         else contract_launch<double, 4>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
-    } else if (!want_j && c->nbf > 128) {
+    } else if (c->nbf > 128) {
+        // one tiled pass per wanted matrix (the J pass reads the amplitudes again)
         const dim3 g2((unsigned)xc32_tiles(c->nbf), (unsigned)c->nchunk);
         DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_contract_xc32), c->device));
-        k_contract_xc32<<<g2, 256, kXtSmem, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, c->d_part);
+        if (want_xc)
+            k_contract_xc32<<<g2, 256, kXtSmem, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, c->d_cxc32, 0,
+                                                            c->d_part);
+        if (want_j)
+            k_contract_xc32<<<g2, 256, kXtSmem, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, c->d_cj32, 1,
+                                                            c->d_part);
         DFTG_LAUNCH_CHECK();
         DFTG_MARK(c, "contract");
         k_contract_reduce<<<(unsigned)((nn + 31) / 32), 256, 0, c->stream>>>(c->nbf, kXtM, c->nchunk, wx, wj, c->d_part,
@@ -389,7 +395,7 @@ int launch_contract_coef32(dftg_ctx *c, const float *coef, double *out)
     if (c->nbf > 128) {
         const dim3 g2((unsigned)xc32_tiles(c->nbf), (unsigned)c->nchunk);
         DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_contract_xc32), c->device));
-        k_contract_xc32<<<g2, 256, kXtSmem, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, coef, c->d_part);
+        k_contract_xc32<<<g2, 256, kXtSmem, c->stream>>>(c->nbf, (int)per, c->npad, c->d_phi32, coef, 0, c->d_part);
         rtile = kXtM;
     } else if (R == 5) {
         contract_launch<float, 5>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi32, coef, coef, 1, 0, d_tiles, c->d_part);
