@@ -682,7 +682,7 @@ def run_synthetic(dev, npts=2_000_000, nbf=512, nocc=128, reps=3):
            "E_xc_fp64": float(s64[0]), "dE_xc_rel": abs(float(sm[0] - s64[0])) / abs(float(s64[0])),
            "max_dXC_rel": float(np.abs(xcm - xc64).max() / np.abs(xc64).max()),
            "max_drho_rel": float(np.abs(rhom - rho64).max() / np.abs(rho64).max()),
-           "mixed_path": "FP32 CUDA-core density and compensated FP32 contraction (nbf > 128: no tensor-core form yet)",
+           "mixed_path": "register-tiled FP32 CUDA-core density (P as hi + lo) and XC contraction (TwoSum across stages); nbf > 128 has no tensor-core form yet",
            "mixed_alg_bytes": alg, "mixed_GBps_over_alg_bytes": alg / (msmx * 1e-3) / 1e9, "setup_s": setup_s}
     g.close()
     return out
