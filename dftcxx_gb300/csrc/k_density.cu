@@ -16,7 +16,7 @@
 namespace dftg {
 
 constexpr int kRedBlock = 256;
-constexpr int kRedChunk = 4096;   // points per stage-1 reduction block
+constexpr int kRedChunk = 1024;   // points per stage-1 reduction block (about two blocks per SM for benzene)
 
 template <typename T>
 __global__ void __launch_bounds__(128) k_density(int nbf, size_t npad, const T *__restrict__ phi,

@@ -1010,8 +1010,9 @@ __global__ void __launch_bounds__(256) k_ej(size_t npad, const double *__restric
 {
     __shared__ double sh[32];
     __shared__ int s_last;
-    const size_t p = (size_t)blockIdx.x * 256 + threadIdx.x;
-    double v = block_sum(p < npad ? cj[p] * rho[p] : 0.0, sh);
+    double v = 0.0;   // grid-stride: a few points per thread, one block sum per block
+    for (size_t p = (size_t)blockIdx.x * 256 + threadIdx.x; p < npad; p += (size_t)gridDim.x * 256) v += cj[p] * rho[p];
+    v = block_sum(v, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = v;
     if (!last_block(counter, &s_last)) return;
     // last block: sum of the block partials in a fixed order; rho on the device
@@ -1114,7 +1115,7 @@ int launch_hartree(dftg_ctx *c)
                                               c->d_Vown, c->d_V, c->d_cj, c->d_cj32);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "vcross");
-    const unsigned ne = (unsigned)((c->npad + 255) / 256);
+    const unsigned ne = (unsigned)std::min<size_t>((c->npad + 255) / 256, 2 * 152);
     k_ej<<<ne, 256, 0, c->stream>>>(c->npad, c->d_cj, c->d_rho, c->d_red, c->rho_scaled ? 1 : 0, c->d_scal,
                                     c->d_counters + kCntEJ);
     DFTG_LAUNCH_CHECK();
