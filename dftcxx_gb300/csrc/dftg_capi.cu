@@ -8,9 +8,11 @@
 //   hartree          K5a-e, cj = w V / 2                  (moleculargrid.cpp:336-380)
 //   contraction      K4 XC and J in one pass over phi     (dft.cpp:426-432, atomicgrid.cpp:471-488)
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <mutex>
@@ -93,12 +95,35 @@ static void free_ctx(dftg_ctx *c)
     delete c;
 }
 
+// DFTG_TRACE=1: wall time of each set-up phase on stderr (the stream is
+// synchronised at every mark, so GPU work is charged to its phase)
+struct SetupTrace {
+    bool on = false;
+    std::chrono::steady_clock::time_point t0;
+    SetupTrace()
+    {
+        const char *e = std::getenv("DFTG_TRACE");
+        on = e && e[0] == '1';
+        t0 = std::chrono::steady_clock::now();
+    }
+    void mark(cudaStream_t st, const char *what)
+    {
+        if (!on) return;
+        if (st) cudaStreamSynchronize(st);
+        const auto t = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "dftg set-up %-22s %9.3f ms\n", what, std::chrono::duration<double, std::milli>(t - t0).count());
+        t0 = t;
+    }
+};
+
 static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *basis, const dftg_grid_params *g)
 {
+    SetupTrace tr;
     c->device = g->device;
     DFTG_CUDA(cudaSetDevice(c->device));
     DFTG_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
     c->stream = c->own_stream;
+    tr.mark(c->stream, "stream");
 
     // molecule and basis
     c->natoms = mol->natoms;
@@ -140,6 +165,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     }
 
     const size_t np = c->npad, nn = (size_t)c->nbf * c->nbf, nlm = c->nlm, N = c->nrad;
+    tr.mark(nullptr, "host basis and radial grid");
     DFTG_TRY(dalloc(&c->d_atoms, 4 * (size_t)c->natoms));
     DFTG_TRY(dalloc(&c->d_rab, (size_t)c->natoms * c->natoms));
     DFTG_TRY(dalloc(&c->d_rn, N));
@@ -202,6 +228,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(dalloc(&c->d_splm, (size_t)c->natoms * nlm * N * 8));
     DFTG_CUDA(cudaMemset(c->d_scal, 0, sizeof(double) * scal_elems(c->natoms)));
 
+    tr.mark(c->stream, "allocations");
     std::vector<double> atoms(4 * (size_t)c->natoms), rab((size_t)c->natoms * c->natoms);
     for (int a = 0; a < c->natoms; ++a) {
         for (int d = 0; d < 3; ++d) atoms[4 * a + d] = c->xyz[3 * a + d];
@@ -225,13 +252,21 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_CUDA(cudaMemcpy(c->d_pa, c->alpha.data(), sizeof(double) * c->nprim, cudaMemcpyHostToDevice));
     DFTG_CUDA(cudaMemcpy(c->d_pcn, pcn.data(), sizeof(double) * c->nprim, cudaMemcpyHostToDevice));
 
+    tr.mark(c->stream, "copies");
     DFTG_TRY(launch_grid(c));
+    tr.mark(c->stream, "grid and Becke weights");
     DFTG_TRY(launch_amplitudes(c));
+    tr.mark(c->stream, "amplitudes");
     DFTG_TRY(hartree_setup(c));
+    tr.mark(c->stream, "Hartree maps");
     DFTG_TRY(contract_setup(c));
+    tr.mark(c->stream, "contraction tiles");
     DFTG_TRY(contract_tc_setup(c));
+    tr.mark(c->stream, "contraction slices");
     DFTG_TRY(density_tc_setup(c));
+    tr.mark(c->stream, "density slices");
     DFTG_TRY(cross_pairs_setup(c));
+    tr.mark(c->stream, "cross-atom pairs");
     DFTG_CUDA(cudaStreamSynchronize(c->stream));
     return DFTG_OK;
 }

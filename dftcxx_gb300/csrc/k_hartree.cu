@@ -29,6 +29,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <vector>
+#include <cub/device/device_radix_sort.cuh>
 #include "dftg_internal.cuh"
 
 namespace dftg {
@@ -912,93 +913,153 @@ __global__ void k_vcross_gather(size_t npts, size_t npad, int natoms, int nrad, 
 }
 
 // Order the (point, other atom) pairs by (atom, spline interval of their
-// distance) with a counting sort; pos[p][k] is the place of pair (p, k).
+// distance), stably in the enumeration order (point, then atom): pos[p][k] is
+// the place of pair (p, k).  On the device: the pairs' keys (FP64 distance,
+// the interval rule of spline_interval(): clamp below the first and beyond the
+// last knot) and a histogram of the keys, a stable radix sort of the keys with
+// the enumeration index as payload, then the per-pair geometry at its sorted
+// place.  The runs of at most kCrossTask pairs inside one bin (the tasks of
+// k_vcross_bins) are formed on the host from the bin counts.
+__device__ __forceinline__ void pair_of_enum(size_t e, int na, int per_atom, size_t &p, int &k)
+{
+    p = e / (size_t)(na - 1);
+    const int j = (int)(e - p * (size_t)(na - 1));
+    const int a = (int)(p / per_atom);
+    k = j < a ? j : j + 1;          // every atom but the point's own
+}
+
+__device__ __forceinline__ void pair_interval(double r, const double *__restrict__ sx, int N, int &iv, double &t)
+{
+    if (r < sx[0]) { iv = 0; t = 0.0; return; }
+    if (r >= sx[N - 1]) { iv = N - 1; t = 0.0; return; }
+    int lo = 0, hi = N;                 // first i with sx[i] >= r
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (sx[mid] < r) lo = mid + 1;
+        else hi = mid;
+    }
+    const int i = max(1, min(N - 1, lo));
+    iv = i - 1;
+    t = r - sx[iv];
+}
+
+__global__ void k_pair_keys(size_t npairs, int na, int per_atom, int N, const double *__restrict__ X,
+                            const double *__restrict__ Y, const double *__restrict__ Z,
+                            const double *__restrict__ atoms, const double *__restrict__ sx, int *__restrict__ key,
+                            int *__restrict__ idx, unsigned *__restrict__ count)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= npairs) return;
+    size_t p;
+    int k;
+    pair_of_enum(e, na, per_atom, p, k);
+    const double dx = X[p] - atoms[4 * k], dy = Y[p] - atoms[4 * k + 1], dz = Z[p] - atoms[4 * k + 2];
+    int iv;
+    double t;
+    pair_interval(sqrt(dx * dx + dy * dy + dz * dz), sx, N, iv, t);
+    const int kk = k * N + iv;
+    key[e] = kk;
+    idx[e] = (int)e;
+    atomicAdd(count + kk, 1u);
+}
+
+__global__ void k_pair_place(size_t npairs, int na, int per_atom, int N, const double *__restrict__ X,
+                             const double *__restrict__ Y, const double *__restrict__ Z,
+                             const double *__restrict__ atoms, const double *__restrict__ sx,
+                             const int *__restrict__ order, float4 *__restrict__ geo, float2 *__restrict__ tk,
+                             int *__restrict__ pos)
+{
+    const size_t dst = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (dst >= npairs) return;
+    const size_t e = (size_t)order[dst];
+    size_t p;
+    int k;
+    pair_of_enum(e, na, per_atom, p, k);
+    // the geometry of a pair is fixed for the grid: direction, 1/r and the
+    // spline offset are formed in FP64 and rounded once to FP32
+    const double dx = X[p] - atoms[4 * k], dy = Y[p] - atoms[4 * k + 1], dz = Z[p] - atoms[4 * k + 2];
+    const double r = sqrt(dx * dx + dy * dy + dz * dz);
+    int iv;
+    double t;
+    pair_interval(r, sx, N, iv, t);
+    geo[dst] = make_float4((float)(dx / r), (float)(dy / r), (float)(dz / r), (float)(1.0 / r));
+    const uint32_t kv = ((uint32_t)k << 16) | (uint32_t)iv;
+    tk[dst] = make_float2((float)t, __uint_as_float(kv));
+    pos[p * na + k] = (int)dst;
+}
+
 int cross_pairs_setup(dftg_ctx *c)
 {
     const size_t n = c->npts;
     const int na = c->natoms, N = c->nrad, per_atom = c->nrad * c->nang;
     if (na < 2) { c->npairs = 0; return DFTG_OK; }
-    // the grid kernel ran on the context's (non-blocking) stream: copy on that
-    // stream and wait for it
-    std::vector<double> X(n), Y(n), Z(n);
-    DFTG_CUDA(cudaMemcpyAsync(X.data(), c->d_x, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
-    DFTG_CUDA(cudaMemcpyAsync(Y.data(), c->d_y, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
-    DFTG_CUDA(cudaMemcpyAsync(Z.data(), c->d_z, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
-    DFTG_CUDA(cudaStreamSynchronize(c->stream));
-    std::vector<double> sx(N);
-    for (int i = 0; i < N; ++i) sx[i] = c->r_n[N - 1 - i];
-    // interval and offset of the spline evaluation at distance r, the same
-    // rule as spline_interval(): clamp below the first and beyond the last knot
-    auto interval = [&](double r, int &iv, double &t) {
-        if (r < sx[0]) { iv = 0; t = 0.0; return; }
-        if (r >= sx[N - 1]) { iv = N - 1; t = 0.0; return; }
-        int i = (int)(std::lower_bound(sx.begin(), sx.end(), r) - sx.begin());
-        i = std::max(1, std::min(N - 1, i));
-        iv = i - 1;
-        t = r - sx[iv];
-    };
     const size_t npairs = n * (size_t)(na - 1);
+    if (npairs > (size_t)INT32_MAX) { set_error("too many (point, atom) pairs: %zu", npairs); return DFTG_ERR_ARG; }
     const int nkeys = na * N;
-    std::vector<int> key(npairs);
-    std::vector<size_t> count((size_t)nkeys + 1, 0);
-    size_t e = 0;
-    for (size_t p = 0; p < n; ++p) {
-        const int a = (int)(p / per_atom);
-        for (int k = 0; k < na; ++k) {
-            if (k == a) continue;
-            const double dx = X[p] - c->xyz[3 * k], dy = Y[p] - c->xyz[3 * k + 1], dz = Z[p] - c->xyz[3 * k + 2];
-            int iv;
-            double t;
-            interval(std::sqrt(dx * dx + dy * dy + dz * dz), iv, t);
-            key[e] = k * N + iv;
-            ++count[(size_t)key[e] + 1];
-            ++e;
-        }
+    int bits = 1;
+    while ((1 << bits) < nkeys) ++bits;
+    // device work arrays: keys and indices in and out, the histogram, the sorter's scratch
+    int *kin = nullptr, *iin = nullptr, *kout = nullptr, *iout = nullptr;
+    unsigned *cnt = nullptr;
+    double *sx = nullptr;
+    void *tmp = nullptr;
+    size_t tmp_bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, kin, kout, iin, iout, (int)npairs, 0, bits, c->stream);
+    const size_t ibytes = sizeof(int) * npairs;
+    char *work = nullptr;
+    const size_t wbytes = 4 * ibytes + sizeof(unsigned) * nkeys + sizeof(double) * N + tmp_bytes + 256;
+    DFTG_CUDA(cudaMalloc(&work, wbytes));
+    kin = reinterpret_cast<int *>(work);
+    iin = kin + npairs;
+    kout = iin + npairs;
+    iout = kout + npairs;
+    cnt = reinterpret_cast<unsigned *>(iout + npairs);
+    sx = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(cnt + nkeys) + 15) & ~(uintptr_t)15);
+    tmp = reinterpret_cast<void *>((reinterpret_cast<uintptr_t>(sx + N) + 127) & ~(uintptr_t)127);
+    int rc = DFTG_OK;
+    std::vector<double> sxh(N);
+    for (int i = 0; i < N; ++i) sxh[i] = c->r_n[N - 1 - i];   // increasing spline abscissae
+    std::vector<unsigned> count(nkeys);
+    cudaError_t e = cudaMemcpyAsync(sx, sxh.data(), sizeof(double) * N, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(unsigned) * nkeys, c->stream);
+    const unsigned nb = (unsigned)((npairs + 255) / 256);
+    if (e == cudaSuccess) {
+        k_pair_keys<<<nb, 256, 0, c->stream>>>(npairs, na, per_atom, N, c->d_x, c->d_y, c->d_z, c->d_atoms, sx, kin,
+                                              iin, cnt);
+        e = cudaGetLastError();
     }
-    // tasks: runs of at most kCrossTask pairs inside one bin
+    if (e == cudaSuccess)
+        e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, kin, kout, iin, iout, (int)npairs, 0, bits, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(count.data(), cnt, sizeof(unsigned) * nkeys, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && !c->d_pairs) e = cudaMalloc(&c->d_pairs, (sizeof(float4) + sizeof(float2)) * npairs);
+    if (e == cudaSuccess && !c->d_pairpos) e = cudaMalloc(&c->d_pairpos, sizeof(int) * n * (size_t)na);
+    if (e == cudaSuccess && !c->d_pairv) e = cudaMalloc(&c->d_pairv, sizeof(float2) * npairs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_pairpos, 0, sizeof(int) * n * (size_t)na, c->stream);
+    if (e == cudaSuccess) {
+        char *base = static_cast<char *>(c->d_pairs);
+        k_pair_place<<<nb, 256, 0, c->stream>>>(npairs, na, per_atom, N, c->d_x, c->d_y, c->d_z, c->d_atoms, sx, iout,
+                                               reinterpret_cast<float4 *>(base),
+                                               reinterpret_cast<float2 *>(base + sizeof(float4) * npairs),
+                                               c->d_pairpos);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cross-atom pair sort", __FILE__, __LINE__);
+    cudaFree(work);
+    if (rc != DFTG_OK) return rc;
+    // tasks: runs of at most kCrossTask pairs inside one bin, bins in key order
     std::vector<int4> tasks;
+    size_t start = 0;
     for (int kk = 0; kk < nkeys; ++kk) {
-        const size_t cnt = count[(size_t)kk + 1];
-        const size_t start = count[kk];          // still the prefix sum of the bins before kk
-        for (size_t o = 0; o < cnt; o += kCrossTask)
-            tasks.push_back(make_int4((int)(start + o), (int)std::min<size_t>(kCrossTask, cnt - o), kk / N, kk % N));
-        count[(size_t)kk + 1] += count[kk];
-    }
-    // the geometry of a pair is fixed for the grid: direction, 1/r and the
-    // spline offset are formed in FP64 and rounded once to FP32
-    std::vector<float4> geo(npairs);
-    std::vector<float2> tk(npairs);
-    std::vector<int> pos(n * (size_t)na, 0);
-    e = 0;
-    for (size_t p = 0; p < n; ++p) {
-        const int a = (int)(p / per_atom);
-        for (int k = 0; k < na; ++k) {
-            if (k == a) continue;
-            const size_t dst = count[key[e++]]++;
-            const double dx = X[p] - c->xyz[3 * k], dy = Y[p] - c->xyz[3 * k + 1], dz = Z[p] - c->xyz[3 * k + 2];
-            const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
-            int iv;
-            double t;
-            interval(r, iv, t);
-            geo[dst] = make_float4((float)(dx / r), (float)(dy / r), (float)(dz / r), (float)(1.0 / r));
-            uint32_t kv = ((uint32_t)k << 16) | (uint32_t)iv;
-            float kvf;
-            std::memcpy(&kvf, &kv, sizeof(kvf));
-            tk[dst] = make_float2((float)t, kvf);
-            pos[p * na + k] = (int)dst;
-        }
+        const size_t cn = count[kk];
+        for (size_t o = 0; o < cn; o += kCrossTask)
+            tasks.push_back(make_int4((int)(start + o), (int)std::min<size_t>(kCrossTask, cn - o), kk / N, kk % N));
+        start += cn;
     }
     c->npairs = npairs;
     c->ncross_tasks = (int)tasks.size();
     DFTG_CUDA(cudaMalloc(&c->d_cross_tasks, sizeof(int4) * tasks.size()));
     DFTG_CUDA(cudaMemcpy(c->d_cross_tasks, tasks.data(), sizeof(int4) * tasks.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMalloc(&c->d_pairs, (sizeof(float4) + sizeof(float2)) * npairs));
-    DFTG_CUDA(cudaMalloc(&c->d_pairpos, sizeof(int) * pos.size()));
-    DFTG_CUDA(cudaMalloc(&c->d_pairv, sizeof(float2) * npairs));
-    char *base = static_cast<char *>(c->d_pairs);
-    DFTG_CUDA(cudaMemcpy(base, geo.data(), sizeof(float4) * npairs, cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(base + sizeof(float4) * npairs, tk.data(), sizeof(float2) * npairs, cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_pairpos, pos.data(), sizeof(int) * pos.size(), cudaMemcpyHostToDevice));
     return DFTG_OK;
 }
 
