@@ -28,6 +28,10 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <tuple>
 #include <vector>
 #include <cub/device/device_radix_sort.cuh>
 #include "dftg_internal.cuh"
@@ -226,19 +230,26 @@ __global__ void k_inv_radius(size_t npts, int nrad, int nang, const double *__re
     invr[p] = 1.0 / sqrt(px * px + py * py + pz * pz);
 }
 
-int hartree_setup(dftg_ctx *c)
+// Host tables of the Hartree step that depend only on the grid shape (radial
+// points, Lebedev rule, lmax), not on the geometry: Y_lm and w Y_lm of the
+// Lebedev directions, the radial Poisson maps per l, the spline derivative map
+// and factorisation, the Legendre recursion coefficients and their FP32
+// splits.  Built once per shape in the process and shared by every context
+// (a new geometry of the same grid reuses them).
+struct HartreeTables {
+    std::vector<double> Y, Yw, pre, fold, Gt, Gb, Kt, rec, sx, f;
+    std::vector<float> Y32, Ywt32, pre32, rec32, m32;
+};
+
+static std::shared_ptr<const HartreeTables> build_hartree_tables(int N, int nang, int lmax, const std::vector<double> &r_n,
+                                                                 const std::vector<double> &leb)
 {
-    const int nang = c->nang, nlm = c->nlm, N = c->nrad, S = N + 2;
-    DFTG_CUDA(cudaMalloc(&c->d_invr, sizeof(double) * c->npts));
-    k_inv_radius<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, N, nang, c->d_rn, c->d_leb,
-                                                                           c->d_invr);
-    DFTG_LAUNCH_CHECK();
+    const int nlm = (lmax + 1) * (lmax + 1), S = N + 2;
+    auto T = std::make_shared<HartreeTables>();
     std::vector<double> Y((size_t)nlm * nang), Yw((size_t)nlm * nang), pre(nlm), fold(nlm);
     std::vector<float> Y32(2 * (size_t)nlm * nang), Ywt32(2 * (size_t)nlm * nang);
-    std::vector<double> leb((size_t)nang * 4);
-    DFTG_CUDA(cudaMemcpy(leb.data(), c->d_leb, sizeof(double) * nang * 4, cudaMemcpyDeviceToHost));
     const size_t half = (size_t)nlm * nang;
-    for (int l = 0; l <= c->lmax; ++l)
+    for (int l = 0; l <= lmax; ++l)
         for (int m = -l; m <= l; ++m) {
             const int lm = l * l + l + m, am = m < 0 ? -m : m;
             pre[lm] = sh_prefactor(l, m);
@@ -259,12 +270,12 @@ int hartree_setup(dftg_ctx *c)
     // the columns of the inverse obtained with the partial-pivot LU factors.
     std::vector<double> A((size_t)S * S), M((size_t)S * S), e(S);
     std::vector<int> piv(S);
-    std::vector<double> Gt((size_t)(c->lmax + 1) * N * N), Gb(N);
-    poisson_matrix(N, c->r_n.data(), A.data());
-    for (int l = 0; l <= c->lmax; ++l) {
+    std::vector<double> Gt((size_t)(lmax + 1) * N * N), Gb(N);
+    poisson_matrix(N, r_n.data(), A.data());
+    for (int l = 0; l <= lmax; ++l) {
         M = A;
         for (int i = 1; i < N + 1; ++i)
-            M[(size_t)i * S + i] -= (double)l * (double)(l + 1) / (c->r_n[i - 1] * c->r_n[i - 1]);
+            M[(size_t)i * S + i] -= (double)l * (double)(l + 1) / (r_n[i - 1] * r_n[i - 1]);
         lu_factor(S, M.data(), piv.data());
         for (int k = 0; k <= N; ++k) {      // column k of the inverse
             for (int i = 0; i < S; ++i) e[i] = (i == k) ? 1.0 : 0.0;
@@ -273,7 +284,7 @@ int hartree_setup(dftg_ctx *c)
                 if (k == 0) {
                     if (l == 0) Gb[i - 1] = std::sqrt(4.0 * kPi) * e[i];
                 } else {
-                    Gt[((size_t)l * N + (k - 1)) * N + (i - 1)] = -4.0 * kPi * c->r_n[k - 1] * e[i];
+                    Gt[((size_t)l * N + (k - 1)) * N + (i - 1)] = -4.0 * kPi * r_n[k - 1] * e[i];
                 }
             }
         }
@@ -282,7 +293,7 @@ int hartree_setup(dftg_ctx *c)
     std::vector<double> Kt((size_t)N * N);
     {
         std::vector<double> sxv(N), yv(N), D(N);
-        for (int i = 0; i < N; ++i) sxv[i] = c->r_n[N - 1 - i];
+        for (int i = 0; i < N; ++i) sxv[i] = r_n[N - 1 - i];
         for (int j = 0; j < N; ++j) {
             for (int i = 0; i < N; ++i) yv[i] = (i == j) ? 1.0 : 0.0;
             spline_derivatives(N, sxv.data(), yv.data(), D.data());
@@ -290,14 +301,14 @@ int hartree_setup(dftg_ctx *c)
         }
     }
     std::vector<double> rec((size_t)2 * nlm, 0.0);
-    for (int l = 0; l <= c->lmax; ++l)
+    for (int l = 0; l <= lmax; ++l)
         for (int m = 0; m < l; ++m) {
             rec[2 * (l * l + l + m)] = (double)(2 * l - 1) / (double)(l - m);
             rec[2 * (l * l + l + m) + 1] = (double)(l + m - 1) / (double)(l - m);
         }
     // spline factorisation: the tridiagonal matrix of cspline.cpp:83-118 depends on x only
     std::vector<double> sx(N), f(hartree_splf_elems(N), 0.0);
-    for (int i = 0; i < N; ++i) sx[i] = c->r_n[N - 1 - i];
+    for (int i = 0; i < N; ++i) sx[i] = r_n[N - 1 - i];
     double *inv_h = f.data(), *h = inv_h + N, *Aa = h + N, *Cp = Aa + N, *inv_den = Cp + N, *k4 = inv_den + N;
     for (int i = 0; i < N - 1; ++i) { h[i] = sx[i + 1] - sx[i]; inv_h[i] = 1.0 / h[i]; }
     {
@@ -320,40 +331,72 @@ int hartree_setup(dftg_ctx *c)
         k4[3] = 3 * g0 * g1 + 2 * g0 * g0;
     }
     std::vector<float> pre32(pre.begin(), pre.end()), rec32(rec.begin(), rec.end());
-    DFTG_CUDA(cudaMalloc(&c->d_Gt, sizeof(double) * Gt.size()));
-    DFTG_CUDA(cudaMalloc(&c->d_Gb, sizeof(double) * Gb.size()));
-    DFTG_CUDA(cudaMalloc(&c->d_Kt, sizeof(double) * Kt.size()));
-    DFTG_CUDA(cudaMemcpy(c->d_Gt, Gt.data(), sizeof(double) * Gt.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_Gb, Gb.data(), sizeof(double) * Gb.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_Kt, Kt.data(), sizeof(double) * Kt.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_Y, Y.data(), sizeof(double) * Y.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_Yw, Yw.data(), sizeof(double) * Yw.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_Y32, Y32.data(), sizeof(float) * Y32.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_Ywt32, Ywt32.data(), sizeof(float) * Ywt32.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_pre, pre.data(), sizeof(double) * pre.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_fold, fold.data(), sizeof(double) * fold.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_rec, rec.data(), sizeof(double) * rec.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_pre32, pre32.data(), sizeof(float) * pre32.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_rec32, rec32.data(), sizeof(float) * rec32.size(), cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_sx, sx.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
-    DFTG_CUDA(cudaMemcpy(c->d_splf, f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice));
     // double-float copies of the fixed maps for the mixed Poisson / spline kernels:
     // [hi block][lo block] of Gt, Gb, Kt, 1/h, fold
+    std::vector<float> m32;
+    auto push = [&](const std::vector<double> &v, size_t n) {
+        const size_t o = m32.size();
+        m32.resize(o + 2 * n);
+        for (size_t i = 0; i < n; ++i) split_f32(v[i], m32[o + i], m32[o + n + i]);
+    };
+    push(Gt, Gt.size());
+    push(Gb, Gb.size());
+    push(Kt, Kt.size());
+    push(f, (size_t)N);                  // inv_h
+    push(fold, fold.size());
+    T->Y = std::move(Y); T->Yw = std::move(Yw); T->pre = std::move(pre); T->fold = std::move(fold);
+    T->Gt = std::move(Gt); T->Gb = std::move(Gb); T->Kt = std::move(Kt); T->rec = std::move(rec);
+    T->sx = std::move(sx); T->f = std::move(f);
+    T->Y32 = std::move(Y32); T->Ywt32 = std::move(Ywt32); T->pre32 = std::move(pre32); T->rec32 = std::move(rec32);
+    T->m32 = std::move(m32);
+    return T;
+}
+
+int hartree_setup(dftg_ctx *c)
+{
+    const int nang = c->nang, N = c->nrad;
+    DFTG_CUDA(cudaMalloc(&c->d_invr, sizeof(double) * c->npts));
+    k_inv_radius<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, N, nang, c->d_rn, c->d_leb,
+                                                                           c->d_invr);
+    DFTG_LAUNCH_CHECK();
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int>, std::shared_ptr<const HartreeTables>> cache;
+    std::shared_ptr<const HartreeTables> T;
     {
-        std::vector<float> m32;
-        auto push = [&](const std::vector<double> &v, size_t n) {
-            const size_t o = m32.size();
-            m32.resize(o + 2 * n);
-            for (size_t i = 0; i < n; ++i) split_f32(v[i], m32[o + i], m32[o + n + i]);
-        };
-        push(Gt, Gt.size());
-        push(Gb, Gb.size());
-        push(Kt, Kt.size());
-        push(f, (size_t)N);                  // inv_h
-        push(fold, fold.size());
-        DFTG_CUDA(cudaMalloc(&c->d_maps32, sizeof(float) * m32.size()));
-        DFTG_CUDA(cudaMemcpy(c->d_maps32, m32.data(), sizeof(float) * m32.size(), cudaMemcpyHostToDevice));
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(std::make_tuple(N, c->leb, c->lmax));
+        if (it != cache.end()) T = it->second;
     }
+    if (!T) {
+        std::vector<double> leb((size_t)nang * 4);
+        DFTG_CUDA(cudaMemcpy(leb.data(), c->d_leb, sizeof(double) * nang * 4, cudaMemcpyDeviceToHost));
+        T = build_hartree_tables(N, nang, c->lmax, c->r_n, leb);
+        std::lock_guard<std::mutex> lk(mu);
+        cache.emplace(std::make_tuple(N, c->leb, c->lmax), T);
+    }
+    auto up = [&](void *dst, const void *src, size_t bytes) -> int {
+        DFTG_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+        return DFTG_OK;
+    };
+    DFTG_CUDA(cudaMalloc(&c->d_Gt, sizeof(double) * T->Gt.size()));
+    DFTG_CUDA(cudaMalloc(&c->d_Gb, sizeof(double) * T->Gb.size()));
+    DFTG_CUDA(cudaMalloc(&c->d_Kt, sizeof(double) * T->Kt.size()));
+    DFTG_CUDA(cudaMalloc(&c->d_maps32, sizeof(float) * T->m32.size()));
+    DFTG_TRY_L(up(c->d_Gt, T->Gt.data(), sizeof(double) * T->Gt.size()));
+    DFTG_TRY_L(up(c->d_Gb, T->Gb.data(), sizeof(double) * T->Gb.size()));
+    DFTG_TRY_L(up(c->d_Kt, T->Kt.data(), sizeof(double) * T->Kt.size()));
+    DFTG_TRY_L(up(c->d_Y, T->Y.data(), sizeof(double) * T->Y.size()));
+    DFTG_TRY_L(up(c->d_Yw, T->Yw.data(), sizeof(double) * T->Yw.size()));
+    DFTG_TRY_L(up(c->d_Y32, T->Y32.data(), sizeof(float) * T->Y32.size()));
+    DFTG_TRY_L(up(c->d_Ywt32, T->Ywt32.data(), sizeof(float) * T->Ywt32.size()));
+    DFTG_TRY_L(up(c->d_pre, T->pre.data(), sizeof(double) * T->pre.size()));
+    DFTG_TRY_L(up(c->d_fold, T->fold.data(), sizeof(double) * T->fold.size()));
+    DFTG_TRY_L(up(c->d_rec, T->rec.data(), sizeof(double) * T->rec.size()));
+    DFTG_TRY_L(up(c->d_pre32, T->pre32.data(), sizeof(float) * T->pre32.size()));
+    DFTG_TRY_L(up(c->d_rec32, T->rec32.data(), sizeof(float) * T->rec32.size()));
+    DFTG_TRY_L(up(c->d_sx, T->sx.data(), sizeof(double) * N));
+    DFTG_TRY_L(up(c->d_splf, T->f.data(), sizeof(double) * T->f.size()));
+    DFTG_TRY_L(up(c->d_maps32, T->m32.data(), sizeof(float) * T->m32.size()));
     return DFTG_OK;
 }
 
