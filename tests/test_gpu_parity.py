@@ -292,12 +292,13 @@ def _synthetic_grid(npts, nbf, nocc, precision, seed=20261203):
     return g, (pts, w, lmn, alpha, centres, P)
 
 
-@pytest.mark.parametrize("nbf", [48, 160])
+@pytest.mark.parametrize("nbf", [48, 133, 160, 200])
 def test_points_context_matches_oracle(gpu_lib, oracle_mod, nbf):
     """Synthetic contraction workload (explicit points and function centres, no
     atoms) at a reduced size: the FP64 form reproduces the oracle's rho, E_xc
     and XC to 1e-10 (relative); the mixed form (tensor cores up to 128
-    functions, compensated FP32 CUDA cores beyond) stays within 1e-6 of max|XC|
+    functions, register-tiled FP32 CUDA cores beyond: 133 has padded P rows,
+    200 ragged 128 x 64 tiles) stays within 1e-6 of max|XC|, 1e-6 of max rho
     and 1e-7 of |E_xc|."""
     g, (pts, w, lmn, alpha, centres, P) = _synthetic_grid(20_000, nbf, nbf // 4, "fp64")
     r = g.xc_build(P)
@@ -310,6 +311,7 @@ def test_points_context_matches_oracle(gpu_lib, oracle_mod, nbf):
     assert abs(r["nelec"] - float(w @ rho_o)) <= 1e-10 * abs(float(w @ rho_o))
     g.set_precision("mixed")
     rm = g.xc_build(P)
+    assert np.abs(g.get_densities() - rho_o).max() <= 1e-6 * np.abs(rho_o).max()
     assert abs(rm["Exc"] - e_o) <= 1e-7 * abs(e_o)
     assert np.abs(rm["XC"] - xc_o).max() <= 1e-6 * np.abs(xc_o).max()
     from dftcxx_gb300 import _lib
