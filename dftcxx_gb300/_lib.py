@@ -110,6 +110,7 @@ SIGNATURES = {
                                      ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.c_void_p],
     "dftg_eri_coulomb": [ctypes.c_void_p, _dp, _dp],
+    "dftg_selftest_wait": [ctypes.c_void_p, ctypes.c_double],
     "dftg_eri_list": [ctypes.c_void_p, _dp, ctypes.c_size_t],
     "dftg_scf_init": [ctypes.c_void_p, ctypes.POINTER(ScfParams)],
     "dftg_scf_run": [ctypes.c_void_p, _dp, _ip],

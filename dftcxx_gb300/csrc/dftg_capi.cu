@@ -207,7 +207,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(dalloc(&c->d_scal, scal_elems(c->natoms)));
     DFTG_CUDA(cudaMalloc(&c->d_counters, sizeof(int) * kNumCounters));
     DFTG_CUDA(cudaMemset(c->d_counters, 0, sizeof(int) * kNumCounters));
-    DFTG_CUDA(cudaMallocHost(&c->h_scal, sizeof(double) * scal_elems(c->natoms)));
+    DFTG_CUDA(cudaMallocHost(&c->h_scal, sizeof(double) * (scal_elems(c->natoms) + 1)));   // + the wait flag
     DFTG_TRY(dalloc(&c->d_Y, nlm * c->nang));
     DFTG_TRY(dalloc(&c->d_Yw, nlm * c->nang));
     DFTG_TRY(dalloc(&c->d_pre, nlm));
@@ -307,17 +307,17 @@ static int check_matrix(const double *P, int n)
 
 int sync_scalars(dftg_ctx *c)
 {
-    DFTG_CUDA(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(double) * scal_elems(c->natoms), cudaMemcpyDeviceToHost,
-                              c->stream));
+    const size_t ns = scal_elems(c->natoms);
+    int *h_flag = reinterpret_cast<int *>(c->h_scal + ns);   // pinned slot after the scalars
+    DFTG_CUDA(cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(double) * ns, cudaMemcpyDeviceToHost, c->stream));
+    if (c->d_flag) DFTG_CUDA(cudaMemcpyAsync(h_flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     DFTG_CUDA(cudaStreamSynchronize(c->stream));
-    if (c->d_flag) {   // a bounded wait inside a kernel gave up
-        int flag = 0;
-        DFTG_CUDA(cudaMemcpy(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
-        if (flag) {
-            DFTG_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
-            set_error("a bounded device wait expired (code %d); results of this build are invalid", flag);
-            return DFTG_ERR_TIMEOUT;
-        }
+    if (c->d_flag && *h_flag) {   // a bounded wait inside a kernel gave up
+        const int flag = *h_flag;
+        DFTG_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
+        *h_flag = 0;
+        set_error("a bounded device wait expired (code %d); results of this build are invalid", flag);
+        return DFTG_ERR_TIMEOUT;
     }
     return DFTG_OK;
 }
@@ -514,7 +514,7 @@ static int build_points_ctx(dftg_ctx *c, const dftg_points *pts, const dftg_mole
     DFTG_TRY(dalloc(&c->d_scal, scal_elems(c->natoms)));
     DFTG_CUDA(cudaMalloc(&c->d_counters, sizeof(int) * kNumCounters));
     DFTG_CUDA(cudaMemset(c->d_counters, 0, sizeof(int) * kNumCounters));
-    DFTG_CUDA(cudaMallocHost(&c->h_scal, sizeof(double) * scal_elems(c->natoms)));
+    DFTG_CUDA(cudaMallocHost(&c->h_scal, sizeof(double) * (scal_elems(c->natoms) + 1)));   // + the wait flag
     DFTG_CUDA(cudaMemset(c->d_scal, 0, sizeof(double) * scal_elems(c->natoms)));
     std::vector<double> atoms(4 * (size_t)c->natoms, 0.0);
     for (int a = 0; a < c->natoms; ++a)

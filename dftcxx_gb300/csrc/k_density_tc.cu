@@ -369,3 +369,34 @@ int launch_density_tc(dftg_ctx *c)
 }
 
 }  // namespace dftg
+
+// ------------------------------------------------------------------ self-test of the bounded-wait path
+namespace dftg {
+// one warp waits on an mbarrier that nothing arrives at; the bounded wait gives
+// up after limit_ns and the kernel records code 99 in the context's flag
+__global__ void k_selftest_wait(unsigned long long limit_ns, int *err)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    if (threadIdx.x == 0 && !mbar_wait_ns(&bar, 0u, limit_ns)) atomicExch(err, 99);
+}
+}  // namespace dftg
+
+extern "C" int dftg_selftest_wait(dftg_ctx *c, double limit_ms)
+{
+    using namespace dftg;
+    if (!c) { set_error("null context"); return DFTG_ERR_ARG; }
+    if (!(limit_ms > 0.0 && limit_ms <= 2000.0)) { set_error("limit_ms %g out of (0, 2000]", limit_ms); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    if (!c->d_flag) {
+        DFTG_CUDA(cudaMalloc(&c->d_flag, sizeof(int)));
+        DFTG_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
+    }
+    k_selftest_wait<<<1, 32, 0, c->stream>>>((unsigned long long)(limit_ms * 1e6), c->d_flag);
+    DFTG_LAUNCH_CHECK();
+    return sync_scalars(c);
+}

@@ -40,7 +40,7 @@ __device__ __forceinline__ unsigned long long global_ns()
 
 // bounded wait for the phase of the given parity: gives up (false) after
 // kWaitNs nanoseconds of wall-clock time, or after 2^31 polls whatever the timer
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait_ns(uint64_t *bar, uint32_t parity, unsigned long long limit_ns)
 {
     const uint32_t a = smem_u32(bar);
     unsigned long long t0 = 0;
@@ -54,11 +54,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
         if ((it & 255u) == 0u) {
             const unsigned long long t = global_ns();
             if (it == 0) t0 = t;
-            else if (t - t0 > kWaitNs) return false;
+            else if (t - t0 > limit_ns) return false;
         }
     }
     return false;
 }
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) { return mbar_wait_ns(bar, parity, kWaitNs); }
 
 // hint: bring [src, src + bytes) into L2 ahead of a bulk copy (bytes a multiple of 16)
 __device__ __forceinline__ void prefetch_l2(const void *src, uint32_t bytes)

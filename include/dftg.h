@@ -254,6 +254,14 @@ int dftg_get_launch_shape(const dftg_ctx *ctx, int *shape, int cap);
 int dftg_set_launch_shape(dftg_ctx *ctx, const int *shape, int n);
 int dftg_autotune(dftg_ctx *ctx, int reps, double *best_ms);
 
+/* Self-test of the bounded-wait error path (no counterpart in the reference).
+ * Every spin-wait of the tensor-core kernels is bounded; on expiry the kernel
+ * records an error code and exits, and the host call returns DFTG_ERR_TIMEOUT.
+ * This launches one warp that waits on an mbarrier that nothing arrives at,
+ * with a limit of limit_ms (0 < limit_ms <= 2000), and returns what a build
+ * would: DFTG_ERR_TIMEOUT.  The context stays usable. */
+int dftg_selftest_wait(dftg_ctx *ctx, double limit_ms);
+
 /* XC and J contraction that allocates nothing.  No counterpart in the
  * reference: it exists for callers that may not call cudaMalloc / cudaFree
  * while serving (their framework owns all device memory, or they run under a
