@@ -83,7 +83,8 @@ static void free_ctx(dftg_ctx *c)
                     c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_flag,
                     c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32, c->d_U32T, c->d_red2,
                     c->d_bw_pt, c->d_bw_lm, c->d_bw_fpart, c->d_bw_out, c->d_bw_counter, c->d_bw_pairp,
-                    c->d_bw_binfirst, c->d_bw_cpart, c->d_bw_geo, c->d_bw_geo64, c->d_bw_prim32};
+                    c->d_bw_binfirst, c->d_bw_cpart, c->d_bw_geo, c->d_bw_geo64, c->d_bw_prim32,
+                    c->d_tt_exp, c->d_tt_winv, c->d_tt_A, c->d_tt_B, c->d_tt_part};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -262,6 +263,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(contract_setup(c));
     tr.mark(c->stream, "contraction tiles");
     DFTG_TRY(contract_tc_setup(c));
+    DFTG_TRY(contract_tt_setup(c));
     tr.mark(c->stream, "contraction slices");
     DFTG_TRY(density_tc_setup(c));
     tr.mark(c->stream, "density slices");
@@ -544,6 +546,7 @@ static int build_points_ctx(dftg_ctx *c, const dftg_points *pts, const dftg_mole
     DFTG_TRY(launch_amplitudes(c));
     DFTG_TRY(contract_setup(c));
     DFTG_TRY(contract_tc_setup(c));
+    DFTG_TRY(contract_tt_setup(c));
     DFTG_TRY(density_tc_setup(c));
     DFTG_CUDA(cudaStreamSynchronize(c->stream));
     return DFTG_OK;

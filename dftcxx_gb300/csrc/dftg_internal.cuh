@@ -222,6 +222,16 @@ struct dftg_ctx {
     float *d_ct_winv = nullptr;   // [npad] 1 / w (0 where w vanishes)
     void *d_ct_A = nullptr;       // [nkb][3][AR x 32] BF16 slices of phi, shared-memory operand layout
 
+    // device: tiled tensor-core contraction for 128 < nbf <= 1024 (128 x 128 tiles of
+    // the upper block triangle, split-K over point chunks, one pass per matrix)
+    bool tt_ready = false;
+    int tt_AR = 0, tt_nkb = 0, tt_kbpc = 0, tt_nchunk = 0, tt_ntiles = 0, tt_ksplit = 0, tt_grid = 0;
+    int *d_tt_exp = nullptr;      // [2][nchunk][nbf] exponent bounds of |phi|, |w phi|, then [nchunk] int2 of |c / w|
+    float *d_tt_winv = nullptr;   // [npad] 1 / w (0 where w vanishes)
+    void *d_tt_A = nullptr;       // [nkb][3][AR x 32] BF16 slices of phi (set-up)
+    void *d_tt_B = nullptr;       // [nkb][3][AR x 32] BF16 slices of c phi (every pass)
+    void *d_tt_part = nullptr;    // [grid][128 x 128] double-float CTA partials
+
     // device: one-electron integrals output (allocated on first use)
     double *d_ints_work = nullptr;
 
@@ -345,5 +355,13 @@ int launch_contract_tc(dftg_ctx *c);
 int launch_contract_tc_reduce(dftg_ctx *c, bool want_xc, bool want_j);
 int launch_contract_tc_on(dftg_ctx *c, const float *cxc32, const float *cj32);
 int launch_contract_tc_reduce_to(dftg_ctx *c, bool want_xc, bool want_j, double *XC, double *J);
+int ct_setup_tables(dftg_ctx *c, int AR, int nkb, int kbpc, int nchunk, int *rowexp, int *swexp, float *winv,
+                    void *A);
+int ct_launch_cexp(dftg_ctx *c, int nkb, int kbpc, int nchunk, const float *cx, const float *cy, const float *winv,
+                   int2 *cexp);
+// k_contract_tt.cu
+int contract_tt_setup(dftg_ctx *c);
+int launch_contract_tt_bounds(dftg_ctx *c, const float *cx, const float *cy);
+int launch_contract_tt(dftg_ctx *c, const float *coef, int which, double *out);
 
 }  // namespace dftg

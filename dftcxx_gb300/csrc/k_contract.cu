@@ -334,6 +334,14 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
     if (!(c->prec_mask & kPrecContract)) {
         if (R == 5) contract_launch<double, 5>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
         else contract_launch<double, 4>(grid, c->stream, c->nbf, (int)per, c->npad, c->d_phi, c->d_cxc, c->d_cj, wx, wj, d_tiles, c->d_part);
+    } else if (c->nbf > 128 && c->tt_ready) {
+        // tensor-core tiles, one pass per wanted matrix
+        DFTG_TRY_L(launch_contract_tt_bounds(c, c->d_cxc32, c->d_cj32));
+        DFTG_MARK(c, "contract_bounds");
+        if (want_xc) DFTG_TRY_L(launch_contract_tt(c, c->d_cxc32, 0, c->d_XC));
+        if (want_j) DFTG_TRY_L(launch_contract_tt(c, c->d_cj32, 1, c->d_J));
+        DFTG_MARK(c, "contract");
+        return DFTG_OK;
     } else if (c->nbf > 128) {
         // one tiled pass per wanted matrix (the J pass reads the amplitudes again)
         const dim3 g2((unsigned)xc32_tiles(c->nbf), (unsigned)c->nchunk);
@@ -392,6 +400,10 @@ int launch_contract_coef32(dftg_ctx *c, const float *coef, double *out)
     per = (per + kKB - 1) / kKB * kKB;
     dim3 grid((unsigned)c->ntiles, (unsigned)c->nchunk);
     int rtile = tile;
+    if (c->nbf > 128 && c->tt_ready) {
+        DFTG_TRY_L(launch_contract_tt_bounds(c, coef, coef));
+        return launch_contract_tt(c, coef, 0, out);
+    }
     if (c->nbf > 128) {
         const dim3 g2((unsigned)xc32_tiles(c->nbf), (unsigned)c->nchunk);
         DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_contract_xc32), c->device));

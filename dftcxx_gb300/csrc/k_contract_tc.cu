@@ -226,10 +226,12 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
         // ------------------------------------------------------------ producers
         // two groups of four warps own the even and the odd ring slots (nst is
         // even, so each group sees its slots' phases in order); in a group, warp
-        // w takes row groups w, w + 4, ...; lane = (row within the group of 8) x
-        // (8-point group g)
+        // w takes row groups w, w + 4, ...; lane = (8-point group g) x (row within
+        // the group of 8).  The eight lanes of one 16-byte shared-memory phase
+        // share g and cover the eight rows of one core matrix, 128 contiguous
+        // bytes, so the slice loads and stores are free of bank conflicts.
         const int grp = warp >> 2, wg = warp & 3;
-        const int g = lane & 3, mrow = lane >> 2;
+        const int g = lane >> 3, mrow = lane & 7;
         int it = 0;
         bool ok = true;
         for (int ch = blockIdx.x; ch < nchunk && ok; ch += gridDim.x) {
@@ -721,6 +723,32 @@ int launch_contract_tc_on(dftg_ctx *c, const float *cxc32, const float *cj32)
 }
 
 int launch_contract_tc(dftg_ctx *c) { return launch_contract_tc_on(c, c->d_cxc32, c->d_cj32); }
+
+// Set-up tables shared with the tiled kernel for nbf > 128 (k_contract_tt.cu):
+// per-chunk exponent bounds of |phi| and |w phi|, 1 / w, and the BF16 slices of
+// phi in the [nkb][3][AR x 32] operand layout (rows nbf .. AR - 1 zero)
+int ct_setup_tables(dftg_ctx *c, int AR, int nkb, int kbpc, int nchunk, int *rowexp, int *swexp, float *winv,
+                    void *A)
+{
+    k_ct_rowexp<<<nchunk, 256, 0, c->stream>>>(c->nbf, c->npad, nkb, kbpc, c->d_phi32, c->d_w, rowexp, swexp);
+    DFTG_LAUNCH_CHECK();
+    k_ct_winv<<<(unsigned)((c->npad + 255) / 256), 256, 0, c->stream>>>(c->npad, c->d_w, winv);
+    DFTG_LAUNCH_CHECK();
+    const size_t threads = (size_t)nkb * AR * 4;
+    k_ct_slice_A<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+        c->nbf, AR, c->npad, nkb, kbpc, c->d_phi, rowexp, reinterpret_cast<__nv_bfloat16 *>(A));
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+// per-chunk exponent bounds of |c_x / w| and |c_y / w| (one build)
+int ct_launch_cexp(dftg_ctx *c, int nkb, int kbpc, int nchunk, const float *cx, const float *cy, const float *winv,
+                   int2 *cexp)
+{
+    k_ct_cexp<<<nchunk, 256, 0, c->stream>>>(nkb, kbpc, cx, cy, winv, cexp);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
 
 int launch_contract_tc_reduce_to(dftg_ctx *c, bool want_xc, bool want_j, double *XC, double *J)
 {
