@@ -675,14 +675,41 @@ def run_synthetic(dev, npts=2_000_000, nbf=512, nocc=128, reps=3):
         torch.cuda.synchronize(dev)
         xcm, sm = XC.cpu().numpy().copy(), sc.cpu().numpy().copy()
         rhom = g.get_densities()
+        # per-phase CUDA-event times of the mixed step
+        ms = (ctypes.c_double * 24)()
+        names = (ctypes.c_char_p * 24)()
+        n = ctypes.c_int()
+        acc = {}
+        for _ in range(reps):
+            _lib.check(L.dftg_fock_build_profile(g.handle, vp(dP), ms, names, 24, ctypes.byref(n)))
+            for i in range(n.value):
+                acc.setdefault(names[i].decode(), []).append(ms[i])
+        phases = {k: float(np.mean(v)) for k, v in acc.items()}
     npad = (npts + 127) // 128 * 128
     alg = 2 * 4 * npad * nbf + 8 * npad * 3
+    # tensor-core contraction (nbf > 128): 128 x 128 tiles of the upper block triangle,
+    # six BF16 slice products per tile and 16-point K step; operands three BF16 slices
+    # of phi and of c phi, each streamed from HBM (L2 shares them between tiles)
+    nrb = (nbf + 127) // 128
+    ntiles = nrb * (nrb + 1) // 2
+    tt_flop = 6 * 2 * npad * 128 * 128 * ntiles
+    tt_bytes = 2 * 3 * 2 * npad * nrb * 128
+    contract_tc = None
+    if "contract" in phases and phases["contract"] > 0:
+        t = phases["contract"] * 1e-3
+        _, bf16, src = _peaks()
+        contract_tc = {"kernel": "k_contract_tt", "tiles": ntiles, "ms": phases["contract"],
+                       "bf16_tflops": tt_flop / t / 1e12, "bf16_peak_tflops": bf16,
+                       "tensor_frac": (tt_flop / t / 1e12) / bf16 if bf16 else None,
+                       "operand_GBps": tt_bytes / t / 1e9, "peak_source": src,
+                       "operand_kernel_ms": phases.get("contract_operand")}
     out = {"workload": "synthetic: %d points, %d s/p/d primitives, P = C C^T (C %d x %d)" % (npts, nbf, nbf, nocc),
            "fp64_ms_per_step": ms64, "mixed_ms_per_step": msmx, "speedup": ms64 / msmx,
            "E_xc_fp64": float(s64[0]), "dE_xc_rel": abs(float(sm[0] - s64[0])) / abs(float(s64[0])),
            "max_dXC_rel": float(np.abs(xcm - xc64).max() / np.abs(xc64).max()),
            "max_drho_rel": float(np.abs(rhom - rho64).max() / np.abs(rho64).max()),
-           "mixed_path": "register-tiled FP32 CUDA-core density (P as hi + lo) and XC contraction (TwoSum across stages); nbf > 128 has no tensor-core form yet",
+           "mixed_path": "register-tiled FP32 CUDA-core density (P as hi + lo); XC contraction on the tcgen05 tensor cores (128 x 128 tiles, three BF16 slices of phi and of c phi, exact integer leading products)",
+           "phases_ms_mixed": phases, "contract_tensor_core": contract_tc,
            "mixed_alg_bytes": alg, "mixed_GBps_over_alg_bytes": alg / (msmx * 1e-3) / 1e9, "setup_s": setup_s}
     g.close()
     return out

@@ -793,7 +793,6 @@ int dftg_fock_build_profile(dftg_ctx *c, const double *P_dev, double *phase_ms, 
                             int *nphase)
 {
     CHECK_CTX(c);
-    if (c->points_only) { set_error("a point-set context has no atoms: no Hartree step"); return DFTG_ERR_STATE; }
     if (!P_dev || !phase_ms || !nphase) { set_error("NULL argument"); return DFTG_ERR_ARG; }
     DFTG_CUDA(cudaSetDevice(c->device));
     const size_t nn = (size_t)c->nbf * c->nbf;
@@ -804,7 +803,7 @@ int dftg_fock_build_profile(dftg_ctx *c, const double *P_dev, double *phase_ms, 
         cudaError_t e = cudaMemcpyAsync(c->d_P, P_dev, sizeof(double) * nn, cudaMemcpyDeviceToDevice, c->stream);
         if (e != cudaSuccess) rc = cuda_fail(e, "copy P", __FILE__, __LINE__);
     }
-    if (rc == DFTG_OK) rc = fock_pipeline(c);
+    if (rc == DFTG_OK) rc = c->points_only ? xc_pipeline(c) : fock_pipeline(c);
     c->prof_on = false;
     if (rc != DFTG_OK) return rc;
     DFTG_CUDA(cudaStreamSynchronize(c->stream));
@@ -817,9 +816,9 @@ int dftg_fock_build_profile(dftg_ctx *c, const double *P_dev, double *phase_ms, 
     }
     *nphase = n;
     c->have_density = true;
-    c->have_hartree = true;
-    c->have_build = true;
-    c->fwd_mask = c->prec_mask;
+    c->have_hartree = !c->points_only;
+    c->have_build = !c->points_only;
+    if (!c->points_only) c->fwd_mask = c->prec_mask;
     return DFTG_OK;
 }
 

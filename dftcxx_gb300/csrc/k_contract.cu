@@ -340,7 +340,6 @@ int launch_contract(dftg_ctx *c, bool want_xc, bool want_j)
         DFTG_MARK(c, "contract_bounds");
         if (want_xc) DFTG_TRY_L(launch_contract_tt(c, c->d_cxc32, 0, c->d_XC));
         if (want_j) DFTG_TRY_L(launch_contract_tt(c, c->d_cj32, 1, c->d_J));
-        DFTG_MARK(c, "contract");
         return DFTG_OK;
     } else if (c->nbf > 128) {
         // one tiled pass per wanted matrix (the J pass reads the amplitudes again)

@@ -409,15 +409,18 @@ int launch_contract_tt(dftg_ctx *c, const float *coef, int which, double *out)
         c->nbf, c->tt_AR, c->npad, c->tt_nkb, c->tt_kbpc, which, c->d_phi32, coef, swexp, tt_cexp(c),
         reinterpret_cast<uint4 *>(c->d_tt_B));
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "contract_operand");
     k_contract_tt<<<c->tt_grid, kTtThreads, tt_smem(kTtStages), c->stream>>>(
         c->nbf, c->tt_AR, kTtStages, c->tt_nkb, c->tt_kbpc, c->tt_nchunk, c->tt_ntiles, c->tt_ksplit, which,
         reinterpret_cast<const unsigned char *>(c->d_tt_B), reinterpret_cast<const unsigned char *>(c->d_tt_A), rowexp,
         swexp, tt_cexp(c), reinterpret_cast<float2 *>(c->d_tt_part), c->d_flag);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "contract");
     const size_t nn = (size_t)c->nbf * c->nbf;
     k_contract_tt_reduce<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(
         c->nbf, c->tt_AR / kTtBlk, c->tt_ntiles, c->tt_ksplit, reinterpret_cast<const float2 *>(c->d_tt_part), out);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "contract_reduce");
     return DFTG_OK;
 }
 

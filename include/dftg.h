@@ -141,7 +141,8 @@ int dftg_get_energies(dftg_ctx *ctx, double *exc, double *ej, double *nelec);
 /* Diagnostic variant of dftg_fock_build_device (no counterpart in the
  * reference, which only prints wall-clock totals, dft.cpp:98-119): runs one
  * build with CUDA events between the kernel phases and returns up to cap
- * per-phase durations in milliseconds with their names (static strings). */
+ * per-phase durations in milliseconds with their names (static strings).  On a
+ * point-set context it profiles the step of dftg_xc_build_device instead. */
 int dftg_fock_build_profile(dftg_ctx *ctx, const double *P_dev, double *phase_ms,
                             const char **names, int cap, int *nphase);
 

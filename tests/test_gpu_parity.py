@@ -292,14 +292,17 @@ def _synthetic_grid(npts, nbf, nocc, precision, seed=20261203):
     return g, (pts, w, lmn, alpha, centres, P)
 
 
-@pytest.mark.parametrize("nbf", [48, 133, 160, 200])
+@pytest.mark.parametrize("nbf", [48, 133, 160, 200, 300, 512])
 def test_points_context_matches_oracle(gpu_lib, oracle_mod, nbf):
     """Synthetic contraction workload (explicit points and function centres, no
     atoms) at a reduced size: the FP64 form reproduces the oracle's rho, E_xc
-    and XC to 1e-10 (relative); the mixed form (tensor cores up to 128
-    functions, register-tiled FP32 CUDA cores beyond: 133 has padded P rows,
-    200 ragged 128 x 64 tiles) stays within 1e-6 of max|XC|, 1e-6 of max rho
-    and 1e-7 of |E_xc|."""
+    and XC to 1e-10 (relative); the mixed form stays within 1e-6 of max|XC|,
+    1e-6 of max rho and 1e-7 of |E_xc|.  Mixed density: tensor cores up to 80
+    functions, register-tiled FP32 CUDA cores beyond (133 has padded P rows,
+    200 ragged 128 x 64 tiles).  Mixed XC contraction: one tensor-core kernel
+    up to 128 functions, 128 x 128 tensor-core tiles beyond (133: two row
+    blocks, the second nearly empty; 300: six tiles, a ragged last block; 512:
+    ten full tiles)."""
     g, (pts, w, lmn, alpha, centres, P) = _synthetic_grid(20_000, nbf, nbf // 4, "fp64")
     r = g.xc_build(P)
     rho = g.get_densities()
