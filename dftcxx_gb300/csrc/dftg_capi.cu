@@ -84,7 +84,8 @@ static void free_ctx(dftg_ctx *c)
                     c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32, c->d_U32T, c->d_red2,
                     c->d_bw_pt, c->d_bw_lm, c->d_bw_fpart, c->d_bw_out, c->d_bw_counter, c->d_bw_pairp,
                     c->d_bw_binfirst, c->d_bw_cpart, c->d_bw_geo, c->d_bw_geo64, c->d_bw_prim32,
-                    c->d_tt_exp, c->d_tt_winv, c->d_tt_A, c->d_tt_B, c->d_tt_part};
+                    c->d_tt_exp, c->d_tt_winv, c->d_tt_A, c->d_tt_B, c->d_tt_part,
+                    c->d_dt_A, c->d_dt_B, c->d_dt_exp};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -266,6 +267,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(contract_tt_setup(c));
     tr.mark(c->stream, "contraction slices");
     DFTG_TRY(density_tc_setup(c));
+    DFTG_TRY(density_tt_setup(c));
     tr.mark(c->stream, "density slices");
     DFTG_TRY(cross_pairs_setup(c));
     tr.mark(c->stream, "cross-atom pairs");
@@ -548,6 +550,7 @@ static int build_points_ctx(dftg_ctx *c, const dftg_points *pts, const dftg_mole
     DFTG_TRY(contract_tc_setup(c));
     DFTG_TRY(contract_tt_setup(c));
     DFTG_TRY(density_tc_setup(c));
+    DFTG_TRY(density_tt_setup(c));
     DFTG_CUDA(cudaStreamSynchronize(c->stream));
     return DFTG_OK;
 }

@@ -214,6 +214,13 @@ struct dftg_ctx {
     int *d_tc_colexp = nullptr;   // [NP] per-column scale exponents of P
     int *d_flag = nullptr;        // device error flag (bounded waits that expired)
 
+    // device: tensor-core density for 81 <= nbf <= 1024 (128-point tiles x 128-column blocks)
+    bool dt_ready = false;
+    int dt_nks = 0, dt_nnb = 0, dt_grid = 0;
+    void *d_dt_A = nullptr;       // [tiles][K stages][4][128 x 32] BF16 slices of phi (set-up)
+    void *d_dt_B = nullptr;       // [column blocks][K stages][4][128 x 32] BF16 slices of P (every build)
+    int *d_dt_exp = nullptr;      // [npad] point exponents, then [blocks x 128] column exponents
+
     // device: tensor-core XC / J contraction (split-K over point chunks)
     bool ct_ready = false;
     int ct_NP = 0, ct_AR = 0, ct_nst = 0, ct_spart = 0, ct_nkb = 0, ct_kbpc = 0, ct_nchunk = 0, ct_grid = 0;
@@ -323,6 +330,9 @@ enum { kSumsOnly = 0, kSumsCorrect = 1, kSumsFactor = 2 };
 // k_density_tc.cu
 int density_tc_setup(dftg_ctx *c);
 int launch_density_tc(dftg_ctx *c);
+// k_density_tt.cu
+int density_tt_setup(dftg_ctx *c);
+int launch_density_tt(dftg_ctx *c);
 int launch_atom_sums(dftg_ctx *c, int mode);
 int launch_xc_points(dftg_ctx *c, bool apply_scale);
 // k_hartree.cu

@@ -351,6 +351,8 @@ int launch_density(dftg_ctx *c)
         k_density<double><<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi, c->d_P, c->d_rho);
     } else if (c->tc_ready) {
         DFTG_TRY_L(launch_density_tc(c));
+    } else if (c->dt_ready) {
+        DFTG_TRY_L(launch_density_tt(c));
     } else {
         const int ldp = (c->nbf + 3) / 4 * 4, n = c->nbf * ldp;
         k_split_P<<<(n + 255) / 256, 256, 0, c->stream>>>(c->nbf, ldp, c->d_P, c->d_P32);
