@@ -639,9 +639,9 @@ def run_synthetic(dev, npts=2_000_000, nbf=512, nocc=128, reps=3):
     s/p/d functions (exponents log-uniform in [0.1, 50], centres uniform in the
     cube), P = C C^T with C 512 x 128 ~ N(0, 0.1).  One step: rho = 2 phi^T P phi,
     LDA point kernel, XC = phi^T diag(w v_xc) phi (dftg_xc_build_device), FP64
-    and mixed; the mixed error against FP64 and the mixed step's rate over its
-    algorithmic bytes (the FP32 amplitudes read by the density and by the
-    contraction)."""
+    and mixed; the mixed error against FP64, the per-phase times, the BF16
+    tensor rates of the density and contraction kernels, and the mixed step's
+    rate over the operand bytes it streams."""
     import torch
     from dftcxx_gb300 import _lib
     from dftcxx_gb300.grid import PointGrid
@@ -686,7 +686,11 @@ def run_synthetic(dev, npts=2_000_000, nbf=512, nocc=128, reps=3):
                 acc.setdefault(names[i].decode(), []).append(ms[i])
         phases = {k: float(np.mean(v)) for k, v in acc.items()}
     npad = (npts + 127) // 128 * 128
-    alg = 2 * 4 * npad * nbf + 8 * npad * 3
+    # operand bytes the mixed step streams: density (four BF16 slices of phi and the
+    # FP64 amplitudes of its epilogue), the c phi operand pass (FP32 phi in, three
+    # BF16 slices out), the contraction (three BF16 slices each of phi and c phi),
+    # and the point arrays (rho, w, c)
+    alg = (8 + 8 + 4 + 6 + 12) * npad * nbf + 8 * npad * 3
     # tensor-core contraction (nbf > 128): 128 x 128 tiles of the upper block triangle,
     # six BF16 slice products per tile and 16-point K step; operands three BF16 slices
     # of phi and of c phi, each streamed from HBM (L2 shares them between tiles)
@@ -694,6 +698,17 @@ def run_synthetic(dev, npts=2_000_000, nbf=512, nocc=128, reps=3):
     ntiles = nrb * (nrb + 1) // 2
     tt_flop = 6 * 2 * npad * 128 * 128 * ntiles
     tt_bytes = 2 * 3 * 2 * npad * nrb * 128
+    # tensor-core density (nbf > 80): 128-point tiles x 128-column blocks of Phi P, K = all
+    # functions in 32-function stages, ten BF16 slice products per 16-function step
+    nks = (nbf + 31) // 32
+    dt_flop = 10 * 2 * npad * 128 * nrb * 32 * nks
+    density_tc = None
+    if "density" in phases and phases["density"] > 0:
+        t = phases["density"] * 1e-3
+        _, bf16, src = _peaks()
+        density_tc = {"kernel": "k_density_tt (with the per-build P slicing)", "ms": phases["density"],
+                      "bf16_tflops": dt_flop / t / 1e12, "bf16_peak_tflops": bf16,
+                      "tensor_frac": (dt_flop / t / 1e12) / bf16 if bf16 else None, "peak_source": src}
     contract_tc = None
     if "contract" in phases and phases["contract"] > 0:
         t = phases["contract"] * 1e-3
@@ -708,8 +723,8 @@ def run_synthetic(dev, npts=2_000_000, nbf=512, nocc=128, reps=3):
            "E_xc_fp64": float(s64[0]), "dE_xc_rel": abs(float(sm[0] - s64[0])) / abs(float(s64[0])),
            "max_dXC_rel": float(np.abs(xcm - xc64).max() / np.abs(xc64).max()),
            "max_drho_rel": float(np.abs(rhom - rho64).max() / np.abs(rho64).max()),
-           "mixed_path": "register-tiled FP32 CUDA-core density (P as hi + lo); XC contraction on the tcgen05 tensor cores (128 x 128 tiles, three BF16 slices of phi and of c phi, exact integer leading products)",
-           "phases_ms_mixed": phases, "contract_tensor_core": contract_tc,
+           "mixed_path": "tcgen05 tensor cores: density Phi P over 128-point x 128-column tiles (four BF16 slices of phi and of P, ten slice products) and XC contraction over 128 x 128 tiles (three BF16 slices of phi and of c phi, six slice products); exact integer leading products, double-float epilogues",
+           "phases_ms_mixed": phases, "density_tensor_core": density_tc, "contract_tensor_core": contract_tc,
            "mixed_alg_bytes": alg, "mixed_GBps_over_alg_bytes": alg / (msmx * 1e-3) / 1e9, "setup_s": setup_s}
     g.close()
     return out
