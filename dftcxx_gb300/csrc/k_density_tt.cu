@@ -105,16 +105,24 @@ __global__ void k_dt_slice_A(int nbf, int nks, size_t npad, const double *__rest
     const size_t t = id / ((size_t)4 * kDtBlk * nks);
     const size_t p = t * kDtBlk + r;
     const int e = pexp[p];
-    __nv_bfloat16 *dst = A + ((t * nks + ks) * kDtSlices) * (kDtSlice / 2) + core_off(r, 8 * g, kDtKcores) / 2;
+    // the eight K values of one core-matrix row: one 16-byte store per slice
+    uint32_t w[kDtSlices][4];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < 8; k += 2) {
         const int mu = ks * kDtKS + 8 * g + k;
-        const double x = mu < nbf ? ldexp(phi[(size_t)mu * npad + p], 7 - e) : 0.0;
-        __nv_bfloat16 s[kDtSlices];
-        dt_split4(x, s);
+        const double x0 = mu < nbf ? ldexp(phi[(size_t)mu * npad + p], 7 - e) : 0.0;
+        const double x1 = mu + 1 < nbf ? ldexp(phi[(size_t)(mu + 1) * npad + p], 7 - e) : 0.0;
+        __nv_bfloat16 s0[kDtSlices], s1[kDtSlices];
+        dt_split4(x0, s0);
+        dt_split4(x1, s1);
 #pragma unroll
-        for (int i = 0; i < kDtSlices; ++i) dst[(size_t)i * (kDtSlice / 2) + k] = s[i];
+        for (int i = 0; i < kDtSlices; ++i)
+            w[i][k / 2] = (uint32_t)__bfloat16_as_ushort(s0[i]) | ((uint32_t)__bfloat16_as_ushort(s1[i]) << 16);
     }
+    uint4 *dst = reinterpret_cast<uint4 *>(A + ((t * nks + ks) * kDtSlices) * (kDtSlice / 2)) +
+                 core_off(r, 8 * g, kDtKcores) / 16;
+#pragma unroll
+    for (int i = 0; i < kDtSlices; ++i) dst[(size_t)i * (kDtSlice / 16)] = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
 }
 
 // every build: B slices of P and the column exponents, warp per column nu < nnb * 128
@@ -290,7 +298,8 @@ k_density_tt(int nbf, int nks, int nnb, int ntile, size_t npad, const unsigned c
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
                         const int nu = nu0 + 8 * b8 + k;
-                        f64[k] = nu < nbf ? phi[(size_t)nu * npad + p] : 0.0;
+                        // streamed once: evict-first, so the A slices of the tile stay in L2
+                        f64[k] = nu < nbf ? __ldcs(phi + (size_t)nu * npad + p) : 0.0;
                     }
                     float dh[8], dl[8];
                     tmem_ld8(ta + 8u * b8, dh);
