@@ -604,6 +604,9 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
     run(); run()
     for o in outs:
         o.zero_()
+    # the fill runs on torch's stream; the batch on the contexts' non-blocking
+    # streams, which do not wait for it
+    torch.cuda.synchronize(dev)
     run()
     torch.cuda.synchronize(dev)
     got = [o.clone() for o in outs]

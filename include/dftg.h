@@ -235,7 +235,10 @@ int dftg_batch_destroy(dftg_batch *b);
 /* dftg_fock_build_device for every context i with P_devs[i], J_devs[i],
  * XC_devs[i], scalars_devs[i] (arrays of n device pointers; J, XC and scalars
  * entries may be NULL).  stream: a cudaStream_t the batch is ordered on (NULL:
- * the first context's stream); the call returns without synchronising. */
+ * the first context's stream); the call returns without synchronising.  The
+ * contexts' own streams are non-blocking: work queued on the legacy default
+ * stream (a fill of the outputs, a copy of P) is not ordered before the batch
+ * unless the caller synchronises it or passes the stream it used. */
 int dftg_batch_fock_build_device(dftg_batch *b, const double *const *P_devs, double *const *J_devs,
                                  double *const *XC_devs, double *const *scalars_devs, void *stream);
 /* Batch autotuner: scales every context's CTA counts by 1, 1/2, 1/4 and 1/8

@@ -205,6 +205,9 @@ def test_batched_builds_match_single_builds(gpu_lib):
     for _ in range(3):                      # eager, captured, replayed
         for j in Jd + Xd:
             j.zero_()
+        # the batch runs on the contexts' non-blocking streams, which do not
+        # wait for torch's stream: the fills and the copies of P finish first
+        torch.cuda.synchronize()
         b.build(Pd, Jd, Xd, Sd)
         torch.cuda.synchronize()
         for (J0, X0, e0, ej0), P, j, x, sc in zip(ref, Ps, Jd, Xd, Sd):
