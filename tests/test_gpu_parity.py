@@ -295,6 +295,23 @@ def _synthetic_grid(npts, nbf, nocc, precision, seed=20261203):
     return g, (pts, w, lmn, alpha, centres, P)
 
 
+@pytest.mark.parametrize("nbf", [1024, 1025])
+def test_points_context_basis_limits(gpu_lib, oracle_mod, nbf):
+    """The largest basis of the tiled tensor-core density and contraction (1024
+    functions: eight row blocks, 36 contraction tiles, integer leading sums of
+    the density up to 2^24) and the first one past it (1025: the FP32 CUDA-core
+    kernels) on 8192 points: mixed rho, E_xc and XC within the tolerances of the
+    smaller sets against the oracle."""
+    g, (pts, w, lmn, alpha, centres, P) = _synthetic_grid(8192, nbf, nbf // 4, "mixed")
+    e_o, rho_o, xc_o = oracle_mod.points_xc(pts, w, centres, np.arange(nbf), lmn, np.ones(nbf, np.int32), alpha,
+                                            np.ones(nbf), P)
+    rm = g.xc_build(P)
+    assert np.abs(g.get_densities() - rho_o).max() <= 1e-6 * np.abs(rho_o).max()
+    assert abs(rm["Exc"] - e_o) <= 1e-7 * abs(e_o)
+    assert np.abs(rm["XC"] - xc_o).max() <= 1e-6 * np.abs(xc_o).max()
+    g.close()
+
+
 @pytest.mark.parametrize("nbf", [48, 133, 160, 200, 300, 512])
 def test_points_context_matches_oracle(gpu_lib, oracle_mod, nbf):
     """Synthetic contraction workload (explicit points and function centres, no
