@@ -279,16 +279,28 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
     if (mx > 0.0) frexp(mx, &e);                 // mx < 2^e
     row_exp[p] = e;
     const int tile = (int)(p / kTcTile), r = (int)(p % kTcTile);
-    const size_t slice = (size_t)ntiles * kTcTile * KP;
-    for (int mu = 0; mu < KP; ++mu) {
-        double x = mu < nbf ? ldexp(phi[(size_t)mu * npad + p], -e) : 0.0;
-        const size_t o = (size_t)tile * kTcTile * KP + core_off(r, mu, KP / 8) / 2;
-        for (int i = 0; i < kTcSlices; ++i) {
-            x *= 256.0;
-            const double m = rint(x);
-            x -= m;
-            A[(size_t)i * slice + o] = __float2bfloat16_rn((float)ldexp(m, -8 * i));
+    const size_t slice16 = (size_t)ntiles * kTcTile * KP / 8;     // one slice in 16-byte units
+    uint4 *A16 = reinterpret_cast<uint4 *>(A);
+    // eight consecutive functions (one core-matrix row) per step: one 16-byte store per slice
+    for (int mu0 = 0; mu0 < KP; mu0 += 8) {
+        uint32_t w[kTcSlices][4];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int mu = mu0 + k;
+            double x = mu < nbf ? ldexp(phi[(size_t)mu * npad + p], -e) : 0.0;
+#pragma unroll
+            for (int i = 0; i < kTcSlices; ++i) {
+                x *= 256.0;
+                const double m = rint(x);
+                x -= m;
+                const uint32_t h = __bfloat16_as_ushort(__float2bfloat16_rn((float)ldexp(m, -8 * i)));
+                if (k & 1) w[i][k >> 1] |= h << 16;
+                else w[i][k >> 1] = h;
+            }
         }
+        const size_t o16 = ((size_t)tile * kTcTile * KP * 2 + core_off(r, mu0, KP / 8)) / 16;
+#pragma unroll
+        for (int i = 0; i < kTcSlices; ++i) A16[(size_t)i * slice16 + o16] = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
     }
 }
 
