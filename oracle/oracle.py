@@ -24,10 +24,11 @@ _lib = None
 _ref = None
 
 
-def build(ref_src="/root/reference/src"):
-    """Compile the oracle (and oracle/_ref when the reference sources exist)."""
+def build(ref_src=None):
+    """Compile the oracle; with ref_src (the reference's src/ folder), also the
+    reference's dependency-free units into oracle/_ref."""
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
-    if os.path.isdir(ref_src):
+    if ref_src and os.path.isdir(ref_src):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REFSRC=" + ref_src])
 
 

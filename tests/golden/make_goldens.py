@@ -10,9 +10,26 @@ compiled from their sources) and records
   * ref_fgamma.npz    -- (m, x) grid and the reference's GammaInc::Fgamma;
   * ref_basis.json    -- SHA-256 of each reference basis file's parsed numbers;
   * oracle_h2o_scf.json -- oracle SCF energies of H2O/STO-3G/32x110 (a
-                          regression record of the oracle, not a reference pin).
+                          regression record of the oracle, not a reference pin);
+and, from the reference PROGRAM's own code (oracle/_ref/ref_dump*: its
+unmodified grid, Hartree, XC, energy and SCF translation units compiled
+against the Eigen/Boost API subset of oracle/shim):
+  * ref_h2o_sto3g_32x110.npz -- the reference's SCF from its core guess to
+                          |dE| <= 1e-10 (history rows E, 2tr(PH), 2tr(PJ),
+                          E_xc, N; final P), and one build at that P: J, XC,
+                          scalars (E_xc, E_J, 2tr(PH), E_nuc, E_tot, N before
+                          and after the correction), S, T, V, H, and per point
+                          w, Becke weight, rho, V_H; per atom rho_lm and U_lm;
+  * ref_benzene_p631_75x302.npz -- benzene / 6-31G: the reference's SCF at
+                          30 x 110 (lmax 8, |dE| <= 1e-9) gives P; one build at
+                          that P on the 75 x 302 grid (ref_dump302: the 302-point
+                          rule added to the reference's table) gives J, XC,
+                          scalars, S, T, V, H, the per-point arrays at every
+                          101st point, their full FP64 sums and the reference's
+                          own phase timings on this host.
+ref_dump302 is also checked to reproduce ref_dump bit for bit on H2O / 32 x 110.
 
-Usage: python tests/golden/make_goldens.py [/path/to/reference]
+Usage: python tests/golden/make_goldens.py /path/to/reference
 """
 import ctypes
 import hashlib
@@ -26,8 +43,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from oracle import oracle  # noqa: E402
-from dftcxx_gb300.molecule import Molecule, h2o, parse_basis_dat  # noqa: E402
+from oracle import oracle, refprog  # noqa: E402
+from dftcxx_gb300.molecule import Molecule, benzene, h2o, parse_basis_dat  # noqa: E402
 
 _dp = ctypes.POINTER(ctypes.c_double)
 
@@ -84,5 +101,53 @@ def main(ref_root):
                    "enuc": mats["enuc"]}, f, indent=1)
 
 
+    reference_program(ref_root)
+
+
+def _grid_keys(r, idx=None):
+    out = {}
+    for k, name in (("weights", "w"), ("becke", "becke"), ("rho", "rho"), ("potential", "V")):
+        out[name] = r[k] if idx is None else r[k][idx]
+    return out
+
+
+def reference_program(ref_root):
+    refprog.build(ref_root)
+    Z, xyz = h2o()
+    mol = Molecule(Z, xyz, "sto3g", "water")
+    s = refprog.scf(mol, 32, 7, 8, max_iter=200, tol=1e-10)
+    P = s["P"]
+    r = refprog.fock_build(mol, 32, 7, 8, P, amp=True)
+    r302 = refprog._run(mol.basis_name, refprog.input_text("water", "sto3g", mol.Z, mol.xyz, 32, 7, 8),
+                        ["build", lambda tmp: _pfile(tmp, P)], 11)
+    for k in ("J", "XC", "scalars", "rho", "potential", "weights", "becke"):
+        assert np.array_equal(r[k], r302[k]), ("ref_dump302 differs from ref_dump", k)
+    np.savez_compressed(os.path.join(HERE, "ref_h2o_sto3g_32x110.npz"),
+                        history=s["history"], P=P, J=r["J"], XC=r["XC"], scalars=r["scalars"],
+                        S=r["S"], T=r["T"], Vnuc=r["Vnuc"], H=r["H"], rho_lm=r["rho_lm"], U_lm=r["U_lm"],
+                        **_grid_keys(r))
+
+    Z, xyz = benzene()
+    mol = Molecule(Z, xyz, "p631", "benzene")
+    s = refprog.scf(mol, 30, 7, 8, max_iter=200, tol=1e-9)
+    P = s["P"]
+    r = refprog.fock_build(mol, 75, 11, 8, P)
+    idx = np.arange(0, r["rho"].size, 101)
+    sums = np.array([r["weights"].sum(), (r["weights"] * r["rho"]).sum(), (r["weights"] * r["potential"]).sum(),
+                     (r["weights"] * r["rho"] * r["potential"]).sum(), r["becke"].sum()])
+    np.savez_compressed(os.path.join(HERE, "ref_benzene_p631_75x302.npz"),
+                        scf_history_30x110=s["history"], P=P, J=r["J"], XC=r["XC"], scalars=r["scalars"],
+                        S=r["S"], T=r["T"], Vnuc=r["Vnuc"], H=r["H"], idx=idx, sums=sums,
+                        timings_ms=r["timings_ms"], threads=np.array([os.cpu_count()]), **_grid_keys(r, idx))
+
+
+def _pfile(tmp, P):
+    path = os.path.join(tmp, "P.bin")
+    np.asfortranarray(P).ravel(order="F").tofile(path)
+    return path
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_goldens.py /path/to/reference")
+    main(sys.argv[1])
