@@ -4,18 +4,23 @@
 Workload (the headline configuration): benzene D6h (C-C 2.640, C-H 2.040
 bohr), 6-31G (66 basis functions), 75 radial x 302 Lebedev points per atom,
 lmax 8: 271,800 grid points.  A step is one grid Fock build at a fixed density
-matrix P (the converged FP64 SCF density): rho on the grid, density
-correction, Slater+VWN point kernel, Becke-Poisson Hartree potential, J and XC.
+matrix P: rho on the grid, density correction, Slater+VWN point kernel,
+Becke-Poisson Hartree potential, J and XC.  P is the density of the reference
+program's own SCF (tests/golden/ref_benzene_p631_75x302.npz), the same in both
+arms.
 
   value     ms per build in mixed precision, P already in HBM, device-timed with
             CUDA events on the library's stream, L2 flushed before every step
   e2e       the same metric through dftg_fock_build (host buffers: P copied in,
             J, XC, E_xc, N copied out, all inside the timed region)
   fp64      the same build with every step in FP64 (the metric's comparison)
-  accuracy  |dE_tot| between mixed and FP64 SCF energies at convergence, and
-            max|dJ|, max|dXC| at the converged P
-  roofline  dominant kernel of the mixed build, algorithmic bytes / measured
-            duration, against the measured HBM copy bandwidth
+  accuracy  |dE_tot| between mixed and FP64 SCF energies at convergence,
+            max|dJ|, max|dXC| at the converged P, and both builds against the
+            reference program's own J, XC, E_xc and E_J at the fixed P
+  roofline  dominant kernel of the mixed build: its algorithmic bytes (the
+            per-point operand bytes of the contraction or density formula)
+            over its measured duration, against the measured HBM copy
+            bandwidth; the layout bytes it actually streams as a second field
   adjoint   alkanes CnH2n+2 / 6-31G / 50 x 194: mixed forward and backward
             (dE/dP, forces) times and force errors (outside the headline)
   batched   64 jittered small molecules in one CUDA graph vs per-molecule
@@ -23,8 +28,11 @@ correction, Slater+VWN point kernel, Becke-Poisson Hartree potential, J and XC.
   synthetic 2M points x 512 primitives: rho, LDA and XC in FP64 and mixed
             (outside the headline)
 
---impl reference times the reference algorithm on the host cores (the C port
-under oracle/, OpenMP on all cores) for the same workload.
+--impl reference times the reference algorithm on the host cores for the same
+workload: every step one whole, unsampled build by the C port of the
+reference's path under oracle/ (OpenMP on all cores).  The reference program
+itself builds only where its sources are (oracle/_ref); its outputs pin the
+port to 1e-12 (tests/test_reference_pin.py).
 """
 import argparse
 import ctypes
@@ -44,7 +52,17 @@ sys.path.insert(0, ROOT)
 
 METRIC = "ms per SCF grid Fock build, mixed vs FP64 on one GB300 at |\u0394E_tot|\u22641e-6 Ha"
 WORKLOAD = {"workload": "benzene/6-31G grid Fock build", "molecule": "C6H6 D6h", "basis": "6-31G", "nbf": 66,
-            "radial_points": 75, "lebedev_points": 302, "lmax": 8, "grid_points": 271800}
+            "radial_points": 75, "lebedev_points": 302, "lmax": 8, "grid_points": 271800,
+            "density_matrix": "the reference program's SCF density (30 x 110 grid, |dE| <= 1e-9)",
+            "l2": "GPU arm: flushed (256 MB write) before every step"}
+DTYPE = "bf16 slices (3 contraction / 4 density) + fp32 accumulate, fp64 reductions"
+REF_FIXTURE = os.path.join(ROOT, "tests", "golden", "ref_benzene_p631_75x302.npz")
+
+
+def _fixed_density():
+    """The workload's fixed density matrix (the reference program's SCF P) and
+    the reference program's outputs at it."""
+    return dict(np.load(REF_FIXTURE))
 
 # kernels launched per phase of one mixed-precision build (dftg_fock_build_device)
 KERNELS_PER_PHASE = {"density": 2, "charge": 1, "lda": 1, "rholm": 2, "poisson": 1, "vown": 1,
@@ -141,18 +159,15 @@ def _benzene_mol():
 
 
 def run_reference(args, rank):
-    """Reference algorithm (C port, oracle/) on all host cores."""
+    """Reference algorithm (C port, oracle/) on all host cores: every step one
+    whole, unsampled build at the workload's fixed P."""
     if rank != 0:
         return None
     from oracle import oracle
     oracle.build()
     mol = _benzene_mol()
     g = oracle.OracleGrid(mol, 75, 11, 8)
-    rng = np.random.default_rng(0)
-    C = rng.normal(0, 0.1, size=(mol.nbf, mol.nelec // 2))
-    P = C @ C.T
-    stride = 4
-    g.set_sample_stride(stride)
+    P = _fixed_density()["P"]
     cores = oracle.lib().orc_num_threads()
 
     def step():
@@ -160,23 +175,19 @@ def run_reference(args, rank):
         g.set_density(P)
         g.correct_densities()
         g.hartree()
-        t1 = time.perf_counter()
         g.xc()
-        t2 = time.perf_counter()
-        tm = g.timings()     # [multipole+Poisson, cross-V, J, XC matrix] (sampled: cross-V, J, XC)
-        fixed = (t1 - t0) - tm[1] - tm[2] + (t2 - t1) - tm[3]
-        return (fixed + stride * (tm[1] + tm[2] + tm[3])) * 1e3
+        return (time.perf_counter() - t0) * 1e3
 
     for _ in range(args.warmup):
         step()
     times = [step() for _ in range(args.steps)]
     ms = float(np.mean(times))
-    sample = ("benzene/6-31G/75x302 Fock build per step; cross-atom potential, J and XC point loops "
-              "on every %d-th point, their wall time scaled by %d" % (stride, stride))
+    sample = ("benzene/6-31G/75x302 grid Fock build, whole (every point, every phase), "
+              "one build per step at the reference program's SCF density")
     return {"metric": METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic geometry (no dataset)",
-            "config": dict(WORKLOAD, parallelism="host OpenMP"), "impl": "reference",
+            "config": dict(WORKLOAD), "impl": "reference", "parallelism": "host OpenMP, %d threads" % cores,
             "cpu_baseline": {"value": ms, "unit": "ms", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -285,11 +296,25 @@ def run_ours(args, rank, world):
                 "dExc_Ha": abs(rmx["Exc"] - r64["Exc"]), "dE_2trPdJ_Ha": dE_Jmatrix,
                 "dE_J_grid_fp64_vs_2trPJ_Ha": abs(r64["EJ"] - 2 * np.trace(P64 @ r64["J"])),
                 "per_step": ablation}
+    # both builds against the reference program's own outputs at the fixed P
+    fx = _fixed_density()
+    Pfix = fx["P"]
+    vs_ref = {}
+    for prec in ("fp64", "mixed"):
+        grid.set_precision(prec)
+        rr = grid.fock_build(Pfix)
+        vs_ref[prec] = {"dE_tot_Ha": float((rr["EJ"] - fx["scalars"][1]) + (rr["Exc"] - fx["scalars"][0])),
+                        "dE_xc_Ha": float(rr["Exc"] - fx["scalars"][0]),
+                        "dE_J_Ha": float(rr["EJ"] - fx["scalars"][1]),
+                        "max_dJ": float(np.abs(rr["J"] - fx["J"]).max()),
+                        "max_dXC": float(np.abs(rr["XC"] - fx["XC"]).max())}
+    accuracy["vs_reference_program_fixed_P"] = vs_ref
+    grid.set_precision("mixed")
 
     stream = torch.cuda.Stream(device=dev)
     grid.set_stream(stream.cuda_stream)
     nn = mol.nbf * mol.nbf
-    dP = torch.from_numpy(np.asfortranarray(P64).ravel(order="F").copy()).to(f"cuda:{dev}")
+    dP = torch.from_numpy(np.asfortranarray(Pfix).ravel(order="F").copy()).to(f"cuda:{dev}")
     dJ = torch.zeros(nn, dtype=torch.float64, device=f"cuda:{dev}")
     dXC = torch.zeros_like(dJ)
     dS = torch.zeros(2, dtype=torch.float64, device=f"cuda:{dev}")
@@ -350,7 +375,7 @@ def run_ours(args, rank, world):
     # end to end through the public host-buffer call
     grid.set_precision("mixed")
     grid.set_stream(0)
-    hP = torch.from_numpy(np.asfortranarray(P64).ravel(order="F").copy()).pin_memory()
+    hP = torch.from_numpy(np.asfortranarray(Pfix).ravel(order="F").copy()).pin_memory()
     hJ = torch.zeros(nn, dtype=torch.float64).pin_memory()
     hXC = torch.zeros(nn, dtype=torch.float64).pin_memory()
     e_, n_ = ctypes.c_double(), ctypes.c_double()
@@ -377,22 +402,29 @@ def run_ours(args, rank, world):
     if world > 1:
         ms_mx, ms_e2e, ms_64 = max_over_ranks([ms_mx, ms_e2e, ms_64], f"cuda:{dev}")
 
-    # roofline of the dominant mixed-precision kernel: algorithmic bytes per
-    # launch (the operands each kernel must stream) over the per-phase CUDA-event
-    # time of that kernel; DRAM traffic per launch from the committed ncu summary
+    # roofline of the dominant mixed-precision kernel: its algorithmic bytes per
+    # launch (the operand bytes of the formula, 6 bytes per amplitude: three
+    # BF16 planes) over the per-phase CUDA-event time of that kernel; the
+    # layout bytes it actually streams (padded rows and tiles, a fourth plane
+    # for the density) as a second figure; DRAM traffic per launch from the
+    # committed ncu summary
     hbm, _, peak_src = _peaks()
     npts, nbf = grid.grid_size, mol.nbf
     npad = (npts + 127) // 128 * 128
     kp, ar = (nbf + 15) // 16 * 16, (nbf + 7) // 8 * 8
     npairs = npts * (mol.natoms - 1)
     alg_bytes = {
-        # four BF16 slices of phi per point (tile layout), rho written
-        "density": 4 * npad * kp * 2 + 8 * npad,
-        # three BF16 slices of phi per point (chunk layout), c_xc and c_j (FP32), CTA partials
-        "contract": 3 * npad * ar * 2 + 2 * 4 * npad,
+        # rho = 2 phi^T P phi: Npts nbf amplitudes in, rho out, P in
+        "density": 6 * npts * nbf + 8 * npts + 8 * nbf * nbf,
+        # V_xc and J in one pass: Npts nbf amplitudes, two point coefficients
+        "contract": 6 * npts * nbf + 16 * npts,
         # per pair: direction and 1/r (16 B), offset and bin (8 B) in, contribution (8 B) out
         "vcross": 32 * npairs,
-        "lda": npad * (8 + 8 + 8) + npad * (8 + 4),
+        "lda": npts * (8 + 8 + 8) + npts * (8 + 4),
+    }
+    layout_bytes = {
+        "density": 4 * npad * kp * 2 + 8 * npad,
+        "contract": 3 * npad * ar * 2 + 2 * 4 * npad,
     }
     dom = max(prof_mx, key=lambda k: prof_mx[k])
     dom_ms = prof_mx[dom]
@@ -406,7 +438,12 @@ def run_ours(args, rank, world):
             "traffic": traffic}
     if dom in alg_bytes:
         ach = alg_bytes[dom] / (dom_ms * 1e-3) / 1e9
-        roof.update(achieved=ach, frac=ach / hbm, bytes_per_launch=alg_bytes[dom])
+        roof.update(achieved=ach, frac=ach / hbm, bytes_per_launch=alg_bytes[dom], ms_per_launch=dom_ms)
+        if dom in layout_bytes:
+            roof["layout_bytes_per_launch"] = layout_bytes[dom]
+            roof["layout_GBps"] = layout_bytes[dom] / (dom_ms * 1e-3) / 1e9
+        if traffic:
+            roof["traffic_over_alg_bytes"] = traffic / alg_bytes[dom]
     else:
         roof.update(achieved=None, frac=None)
     launches_per_step = sum(KERNELS_PER_PHASE.get(k, 1) for k in prof_mx)
@@ -415,9 +452,10 @@ def run_ours(args, rank, world):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         ref_args = argparse.Namespace(**vars(args))
-        ref_args.steps, ref_args.warmup = 1, 0
+        ref_args.steps, ref_args.warmup = 2, 0
         r = run_reference(ref_args, 0)
         cpu = r["cpu_baseline"]
+        cpu["sample"] = "2 whole builds (" + cpu["sample"] + ")"
 
     adjoint = batched = synthetic = None
     if rank == 0 and world == 1:
@@ -430,10 +468,9 @@ def run_ours(args, rank, world):
 
     return {"metric": METRIC, "value": ms_mx, "unit": "ms",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mx,
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32-split/f64",
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": DTYPE,
             "data": "synthetic geometry (no dataset)",
-            "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single GPU",
-                           l2="flushed (256 MB write) before every step"),
+            "config": dict(WORKLOAD), "parallelism": "replicas" if world > 1 else "single GPU",
             "fp64_ms_per_step": ms_64, "speedup_vs_fp64": ms_64 / ms_mx, "accuracy": accuracy,
             "phases_ms_mixed": prof_mx, "phases_ms_fp64": prof_64,
             "e2e": {"value": ms_e2e, "unit": "ms", "h2d_bytes_per_step": 8 * nn,
@@ -553,6 +590,7 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
     rng = np.random.default_rng(seed)
     grids, dPs, outs = [], [], []
     natoms = nbfs = npts = 0
+    cross_evals = 0
     t0 = time.perf_counter()
     for i in range(nmol):
         name = names[i % len(names)]
@@ -569,15 +607,20 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
         natoms += mol.natoms
         nbfs += mol.nbf
         npts += g.grid_size
+        cross_evals += g.grid_size * (mol.natoms - 1) * 81
     setup_s = time.perf_counter() - t0
     vp = lambda t: ctypes.c_void_p(t.data_ptr())
-    stream = torch.cuda.current_stream(dev)
+    # every leg is timed with events on this stream: the sequential builds run
+    # on it, and the batch graph is launched on it (its branches fork from it
+    # and join back into it)
+    stream = torch.cuda.Stream(device=dev)
 
     def sequential():
         for g, P, o in zip(grids, dPs, outs):
             nn = g.nbf * g.nbf
             _lib.check(L.dftg_fock_build_device(g.handle, vp(P), vp(o[:nn]), vp(o[nn:2 * nn]), vp(o[2 * nn:])))
 
+    torch.cuda.synchronize(dev)
     for g in grids:
         g.set_stream(stream.cuda_stream)
     sequential(); sequential()
@@ -586,6 +629,7 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
         g.set_precision("mixed")
     sequential(); sequential()
     seqmx = _event_ms(sequential, reps, stream)
+    torch.cuda.synchronize(dev)
     for g in grids:   # every context back on its own stream: the graph's branches run concurrently
         g.set_stream(0)
     b = Batch(grids)
@@ -595,17 +639,22 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
     run = lambda: b.build(dPs, Js, XCs, Ss, stream=stream.cuda_stream)
     run(); run()
     bat = _event_ms(run, reps, stream)
+    # one replay with host wall-clock around it (synchronised on both sides)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    run()
+    stream.synchronize()
+    bat_wall = (time.perf_counter() - t0) * 1e3
     t_tune = time.perf_counter()
-    b.autotune(reps=5)
+    tune_ms = b.autotune(reps=5)
     tune_s = time.perf_counter() - t_tune
     # the tuned batch does the work: after its graph is captured, outputs
     # zeroed, one replay, then per-molecule builds of the same launch shapes
     # must reproduce them bit for bit
     run(); run()
+    torch.cuda.synchronize(dev)
     for o in outs:
         o.zero_()
-    # the fill runs on torch's stream; the batch on the contexts' non-blocking
-    # streams, which do not wait for it
     torch.cuda.synchronize(dev)
     run()
     torch.cuda.synchronize(dev)
@@ -620,6 +669,7 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
         g.set_stream(0)
     run(); run()   # the contexts' streams are part of the graph key: recapture
     bat_t = _event_ms(run, reps, stream)
+    torch.cuda.synchronize(dev)
     shapes = sorted({g.launch_shape for g in grids})
     b.close()
     for g in grids:
@@ -631,7 +681,9 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
             "mixed_batched_graph_builds_per_s": nmol / (bat * 1e-3),
             "mixed_batched_autotuned_builds_per_s": nmol / (bat_t * 1e-3),
             "ms_per_batch": {"fp64_sequential": seq64, "mixed_sequential": seqmx, "mixed_graph": bat,
-                             "mixed_graph_autotuned": bat_t},
+                             "mixed_graph_autotuned": bat_t, "mixed_graph_host_wall_one_replay": bat_wall,
+                             "autotuner_best": tune_ms},
+            "cross_atom_evaluations": cross_evals,
             "max_rel_diff_batch_vs_single": diff, "batch_outputs_nonzero": nonzero,
             "autotuned_shapes": [list(s) for s in shapes], "autotune_s": tune_s, "setup_s": setup_s}
 

@@ -695,6 +695,10 @@ int dftg_set_precision_mask(dftg_ctx *c, unsigned mask)
 int dftg_set_stream(dftg_ctx *c, void *s)
 {
     CHECK_CTX(c);
+    if (s == reinterpret_cast<void *>(cudaStreamLegacy) || s == reinterpret_cast<void *>(cudaStreamPerThread)) {
+        set_error("the default streams cannot be captured into the build's CUDA graph: pass a created stream");
+        return DFTG_ERR_ARG;
+    }
     c->stream = s ? reinterpret_cast<cudaStream_t>(s) : c->own_stream;
     return DFTG_OK;
 }
@@ -1161,6 +1165,10 @@ extern "C" int dftg_batch_fock_build_device(dftg_batch *b, const double *const *
     const int n = (int)b->ctx.size();
     for (int i = 0; i < n; ++i)
         if (!P_devs[i]) { set_error("P_devs[%d] NULL", i); return DFTG_ERR_ARG; }
+    if (stream == reinterpret_cast<void *>(cudaStreamLegacy) || stream == reinterpret_cast<void *>(cudaStreamPerThread)) {
+        set_error("the default streams cannot be captured into the batch's CUDA graph: pass a created stream");
+        return DFTG_ERR_ARG;
+    }
     DFTG_CUDA(cudaSetDevice(b->ctx[0]->device));
     cudaStream_t s0 = stream ? reinterpret_cast<cudaStream_t>(stream) : b->ctx[0]->stream;
     std::vector<const void *> key;

@@ -11,13 +11,14 @@
 // loads the library holds DFTG_NOALLOC_SCRATCH_BYTES of device memory for it
 // until the process exits.
 //
-// Set-up: the first call on a device (with that device current) looks up the
-// array's device address with cudaGetSymbolAddress and caches it; make that
-// first call before any stream capture.  Calls share the array: two calls that
-// overlap on the GPU (different streams, or different host threads) race.
+// Set-up: every call looks up the array's device address on the current
+// device with cudaGetSymbolAddress (a host-side lookup that allocates nothing),
+// so the address stays right when the device's context is torn down and made
+// again.  The first call on a device also loads the library's device code
+// there; make it before any stream capture.  Calls share the array: two calls
+// that overlap on the GPU (different streams, or different host threads) race.
 // Every partial sum a call reads is written earlier by the same call, so no
 // part of the array needs clearing between calls.
-#include <mutex>
 #include "dftg_internal.cuh"
 
 namespace dftg {
@@ -25,7 +26,7 @@ namespace dftg {
 constexpr size_t kNoallocScratchDoubles = DFTG_NOALLOC_SCRATCH_BYTES / sizeof(double);
 static __device__ __align__(256) double g_noalloc_scratch[kNoallocScratchDoubles];
 
-constexpr int kNaR = 4, kNaTile = 16 * kNaR, kNaKB = 32, kNaMaxDevices = 64;
+constexpr int kNaR = 4, kNaTile = 16 * kNaR, kNaKB = 32;
 
 // upper-triangular block index -> (row block, column block)
 __device__ __forceinline__ void tile_of(int t, int nt, int &a, int &b)
@@ -127,25 +128,12 @@ __global__ void k_contract_na_reduce(int nbf, int nchunk, const double *__restri
     }
 }
 
-static std::mutex g_na_mutex;
-static double *g_na_ptr[kNaMaxDevices] = {};
-
-// once per device, with that device current
+// device address of the scratch array on the current device
 static int noalloc_scratch(double **out)
 {
-    int dev = 0;
-    DFTG_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNaMaxDevices) {
-        set_error("device ordinal %d beyond %d", dev, kNaMaxDevices);
-        return DFTG_ERR_ARG;
-    }
-    std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_ptr[dev]) {
-        void *p = nullptr;
-        DFTG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_na_ptr[dev] = static_cast<double *>(p);
-    }
-    *out = g_na_ptr[dev];
+    void *p = nullptr;
+    DFTG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    *out = static_cast<double *>(p);
     return DFTG_OK;
 }
 

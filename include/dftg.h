@@ -102,7 +102,14 @@ int dftg_set_precision(dftg_ctx *ctx, int precision);
 #define DFTG_MIX_CROSS 8u       /* cross-atom Hartree potential */
 #define DFTG_MIX_CONTRACT 16u   /* XC and J contractions */
 int dftg_set_precision_mask(dftg_ctx *ctx, unsigned mask);
-/* Run on a caller-owned cudaStream_t (NULL restores the context's stream). */
+/* Run on a caller-owned cudaStream_t (one the caller created).  NULL does NOT
+ * mean the legacy default stream here: it restores the context's own stream,
+ * which is non-blocking, so it is not ordered with work on the legacy default
+ * stream.  The builds are replayed as CUDA graphs captured on the stream, and
+ * the legacy and per-thread default streams cannot be captured, so
+ * cudaStreamLegacy and cudaStreamPerThread are rejected (DFTG_ERR_ARG).  A
+ * caller whose work is on a default stream synchronises it first, or moves it
+ * to a stream it created and passes that one. */
 int dftg_set_stream(dftg_ctx *ctx, void *cuda_stream);
 
 /* MolecularGrid::set_density(P) (moleculargrid.cpp:48-53): rho = 2 phi^T P phi
@@ -234,11 +241,14 @@ int dftg_batch_create(dftg_ctx *const *ctxs, int n, dftg_batch **out);
 int dftg_batch_destroy(dftg_batch *b);
 /* dftg_fock_build_device for every context i with P_devs[i], J_devs[i],
  * XC_devs[i], scalars_devs[i] (arrays of n device pointers; J, XC and scalars
- * entries may be NULL).  stream: a cudaStream_t the batch is ordered on (NULL:
- * the first context's stream); the call returns without synchronising.  The
- * contexts' own streams are non-blocking: work queued on the legacy default
- * stream (a fill of the outputs, a copy of P) is not ordered before the batch
- * unless the caller synchronises it or passes the stream it used. */
+ * entries may be NULL).  stream: a cudaStream_t the batch is ordered on: its
+ * branches start after the work queued there before the call, and the stream
+ * waits for all of them, so events recorded on it bracket the whole batch.
+ * NULL does NOT mean the legacy default stream: it selects the first context's
+ * own (non-blocking) stream, which is not ordered after legacy-stream work (a
+ * fill of the outputs, a copy of P); the default streams themselves cannot be
+ * captured and are rejected (DFTG_ERR_ARG), as in dftg_set_stream.  The call
+ * returns without synchronising. */
 int dftg_batch_fock_build_device(dftg_batch *b, const double *const *P_devs, double *const *J_devs,
                                  double *const *XC_devs, double *const *scalars_devs, void *stream);
 /* Batch autotuner: scales every context's CTA counts by 1, 1/2, 1/4 and 1/8
@@ -276,10 +286,12 @@ int dftg_selftest_wait(dftg_ctx *ctx, double limit_ms);
  * coefficients; XC and J (nbf x nbf, either may be NULL) are written.  Its
  * scratch is a static device array of DFTG_NOALLOC_SCRATCH_BYTES that every GPU
  * loading the library holds until exit; nbf above DFTG_NOALLOC_MAX_NBF is
- * rejected with DFTG_ERR_ARG.  The first call on a device looks up that array
- * (make it before any stream capture).  Calls that overlap on the GPU race on
- * the shared array.  stream: a cudaStream_t, NULL for the legacy stream; the
- * call returns without synchronising. */
+ * rejected with DFTG_ERR_ARG.  Every call looks up that array's address on the
+ * current device (no allocation); the first call on a device also loads the
+ * library's device code there, so make it before any stream capture.  Calls
+ * that overlap on the GPU race on the shared array.  stream: a cudaStream_t,
+ * NULL for the legacy default stream (as in the CUDA runtime); the call
+ * returns without synchronising. */
 #define DFTG_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
 #define DFTG_NOALLOC_MAX_NBF 1024
 int dftg_contract_noalloc(const double *phi, size_t ld, size_t npts, int nbf,
