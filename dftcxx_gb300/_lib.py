@@ -66,6 +66,12 @@ class DftgError(RuntimeError):
 SIGNATURES = {
     "dftg_create": [ctypes.POINTER(Molecule), ctypes.POINTER(Basis), ctypes.POINTER(GridParams),
                     ctypes.POINTER(ctypes.c_void_p)],
+    "dftg_create_cells": [ctypes.POINTER(Molecule), ctypes.POINTER(Basis), ctypes.POINTER(GridParams), ctypes.c_int,
+                          ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)],
+    "dftg_shard_blob_size": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t), _ip, _ip],
+    "dftg_shard_density": [ctypes.c_void_p, _dp, _dp],
+    "dftg_shard_multipoles": [ctypes.c_void_p, ctypes.c_double, _dp, ctypes.c_size_t],
+    "dftg_shard_finish": [ctypes.c_void_p, _dp, ctypes.c_size_t, _dp, _dp, _dp],
     "dftg_destroy": [ctypes.c_void_p],
     "dftg_grid_size": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)],
     "dftg_nbf": [ctypes.c_void_p, _ip],

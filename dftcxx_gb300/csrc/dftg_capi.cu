@@ -118,7 +118,8 @@ struct SetupTrace {
     }
 };
 
-static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *basis, const dftg_grid_params *g)
+static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *basis, const dftg_grid_params *g,
+                     int cell0 = 0, int ncell = -1)
 {
     SetupTrace tr;
     c->device = g->device;
@@ -153,7 +154,9 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     c->nang = dftg_lebedev_npts[c->leb];
     c->lmax = g->lmax;
     c->nlm = (c->lmax + 1) * (c->lmax + 1);
-    c->npts = (size_t)c->natoms * c->nrad * c->nang;
+    c->cell0 = cell0;
+    c->ncell = ncell < 0 ? c->natoms : ncell;
+    c->npts = (size_t)c->ncell * c->nrad * c->nang;
     c->npad = (c->npts + kPtsAlign - 1) / kPtsAlign * kPtsAlign;
     c->r_n.resize(c->nrad);
     c->w_rad.resize(c->nrad);
@@ -393,11 +396,42 @@ using namespace dftg;
         if (!(c)) { set_error("null context"); return DFTG_ERR_ARG; }  \
     } while (0)
 
+// a context over part of the molecule's cells builds only through dftg_shard_*
+#define CHECK_WHOLE(c)                                                                                         \
+    do {                                                                                                       \
+        if ((c)->cell0 != 0 || (c)->ncell != (c)->natoms) {                                                    \
+            set_error("the context holds cells [%d, %d) of %d atoms: build it with the dftg_shard_* calls",     \
+                      (c)->cell0, (c)->cell0 + (c)->ncell, (c)->natoms);                                        \
+            return DFTG_ERR_STATE;                                                                             \
+        }                                                                                                      \
+    } while (0)
+
 extern "C" {
 
 const char *dftg_last_error(void) { return g_err; }
 
+static int create_checked(const dftg_molecule *mol, const dftg_basis *basis, const dftg_grid_params *g, int cell0,
+                          int ncell, dftg_ctx **out);
+
 int dftg_create(const dftg_molecule *mol, const dftg_basis *basis, const dftg_grid_params *g, dftg_ctx **out)
+{
+    return create_checked(mol, basis, g, 0, -1, out);
+}
+
+int dftg_create_cells(const dftg_molecule *mol, const dftg_basis *basis, const dftg_grid_params *g, int first_cell,
+                      int ncells, dftg_ctx **out)
+{
+    if (out) *out = nullptr;
+    if (!mol) { set_error("NULL argument"); return DFTG_ERR_ARG; }
+    if (first_cell < 0 || ncells < 1 || first_cell + ncells > mol->natoms) {
+        set_error("cells [%d, %d) outside the molecule's %d atoms", first_cell, first_cell + ncells, mol->natoms);
+        return DFTG_ERR_ARG;
+    }
+    return create_checked(mol, basis, g, first_cell, ncells, out);
+}
+
+static int create_checked(const dftg_molecule *mol, const dftg_basis *basis, const dftg_grid_params *g, int cell0,
+                          int ncell, dftg_ctx **out)
 {
     if (!out) { set_error("out is NULL"); return DFTG_ERR_ARG; }
     *out = nullptr;
@@ -440,7 +474,7 @@ int dftg_create(const dftg_molecule *mol, const dftg_basis *basis, const dftg_gr
         }
     dftg_ctx *c = new (std::nothrow) dftg_ctx();
     if (!c) { set_error("host allocation failed"); return DFTG_ERR_NOMEM; }
-    int rc = build_ctx(c, mol, basis, g);
+    int rc = build_ctx(c, mol, basis, g, cell0, ncell);
     if (rc != DFTG_OK) { free_ctx(c); return rc; }
     *out = c;
     return DFTG_OK;
@@ -723,6 +757,7 @@ int dftg_set_density(dftg_ctx *c, const double *P)
 int dftg_correct_densities(dftg_ctx *c, double *scale)
 {
     CHECK_CTX(c);
+    CHECK_WHOLE(c);
     if (c->points_only) { set_error("a point-set context has no atoms: no Hartree step or density correction"); return DFTG_ERR_STATE; }
     if (!c->have_density) { set_error("correct_densities before set_density"); return DFTG_ERR_STATE; }
     DFTG_CUDA(cudaSetDevice(c->device));
@@ -748,6 +783,7 @@ int dftg_calculate_density(dftg_ctx *c, double *nelec)
 int dftg_calculate_hartree_potential(dftg_ctx *c, double *J)
 {
     CHECK_CTX(c);
+    CHECK_WHOLE(c);
     if (c->points_only) { set_error("a point-set context has no atoms: no Hartree step or density correction"); return DFTG_ERR_STATE; }
     if (!c->have_density) { set_error("calculate_hartree_potential before set_density"); return DFTG_ERR_STATE; }
     DFTG_CUDA(cudaSetDevice(c->device));
@@ -776,6 +812,7 @@ int dftg_calculate_xc(dftg_ctx *c, double *XC, double *exc)
 int dftg_fock_build_device(dftg_ctx *c, const double *P_dev, double *J_dev, double *XC_dev, double *scalars_dev)
 {
     CHECK_CTX(c);
+    CHECK_WHOLE(c);
     if (c->points_only) { set_error("a point-set context has no atoms: no Hartree step or density correction"); return DFTG_ERR_STATE; }
     if (!P_dev) { set_error("P_dev NULL"); return DFTG_ERR_ARG; }
     DFTG_CUDA(cudaSetDevice(c->device));
@@ -800,6 +837,7 @@ int dftg_fock_build_profile(dftg_ctx *c, const double *P_dev, double *phase_ms, 
                             int *nphase)
 {
     CHECK_CTX(c);
+    if (!c->points_only) CHECK_WHOLE(c);
     if (!P_dev || !phase_ms || !nphase) { set_error("NULL argument"); return DFTG_ERR_ARG; }
     DFTG_CUDA(cudaSetDevice(c->device));
     const size_t nn = (size_t)c->nbf * c->nbf;
@@ -832,6 +870,7 @@ int dftg_fock_build_profile(dftg_ctx *c, const double *P_dev, double *phase_ms, 
 int dftg_fock_build(dftg_ctx *c, const double *P, double *J, double *XC, double *exc, double *nelec)
 {
     CHECK_CTX(c);
+    CHECK_WHOLE(c);
     if (c->points_only) { set_error("a point-set context has no atoms: no Hartree step or density correction"); return DFTG_ERR_STATE; }
     if (!P) { set_error("P NULL"); return DFTG_ERR_ARG; }
     DFTG_TRY(check_matrix(P, c->nbf));
@@ -848,6 +887,118 @@ int dftg_fock_build(dftg_ctx *c, const double *P, double *J, double *XC, double 
     c->have_hartree = true;
     c->have_build = true;
     c->fwd_mask = c->prec_mask;
+    return DFTG_OK;
+}
+
+// ------------------------------------------------------------------ atom-cell shards
+// A build split by fuzzy cell over the contexts of a partition (one per rank),
+// with three exchanges between the calls: the sum of w rho, every cell's
+// spline data, and J, XC and the energies (moleculargrid.cpp:132-146, 336-389).
+static int shard_check(dftg_ctx *c, int phase)
+{
+    CHECK_CTX(c);
+    if (c->points_only) { set_error("a point-set context has no cells"); return DFTG_ERR_STATE; }
+    if (c->shard_phase < phase) { set_error("shard call out of order (phase %d before %d)", phase, c->shard_phase + 1); return DFTG_ERR_STATE; }
+    return DFTG_OK;
+}
+
+size_t shard_blob_doubles(const dftg_ctx *c)
+{
+    // FP64 spline coefficients [nlm][nrad][4], then the split FP32 table [nlm][nrad][8]
+    return (size_t)c->nlm * c->nrad * 4 + (size_t)c->nlm * c->nrad * 4;
+}
+
+int dftg_shard_blob_size(const dftg_ctx *c, size_t *doubles_per_cell, int *first_cell, int *ncells)
+{
+    CHECK_CTX(c);
+    if (c->points_only) { set_error("a point-set context has no cells"); return DFTG_ERR_STATE; }
+    if (doubles_per_cell) *doubles_per_cell = shard_blob_doubles(c);
+    if (first_cell) *first_cell = c->cell0;
+    if (ncells) *ncells = c->ncell;
+    return DFTG_OK;
+}
+
+int dftg_shard_density(dftg_ctx *c, const double *P, double *sum_wrho)
+{
+    DFTG_TRY(shard_check(c, 0));
+    if (!P || !sum_wrho) { set_error("NULL argument"); return DFTG_ERR_ARG; }
+    DFTG_TRY(check_matrix(P, c->nbf));
+    DFTG_CUDA(cudaSetDevice(c->device));
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    DFTG_CUDA(cudaMemcpyAsync(c->d_P, P, sizeof(double) * nn, cudaMemcpyHostToDevice, c->stream));
+    DFTG_TRY(launch_density(c));
+    DFTG_TRY(launch_atom_sums(c, kSumsOnly));   // per cell: kScalAtomQ + local index; total in kScalNelec
+    DFTG_TRY(sync_scalars(c));
+    *sum_wrho = c->h_scal[kScalNelec];
+    c->rho_scaled = false;
+    c->have_build = false;
+    c->shard_phase = 1;
+    return DFTG_OK;
+}
+
+int dftg_shard_multipoles(dftg_ctx *c, double total_wrho, double *blob, size_t cap)
+{
+    DFTG_TRY(shard_check(c, 1));
+    const size_t per = shard_blob_doubles(c);
+    if (!blob || cap < per * c->ncell) { set_error("blob capacity %zu < %zu", cap, per * c->ncell); return DFTG_ERR_ARG; }
+    if (!(total_wrho > 0.0) || !std::isfinite(total_wrho)) { set_error("total %g is not a positive number", total_wrho); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    // correction factor over the whole molecule (every atom's charge), charges of
+    // this context's cells at their atoms' slots
+    double charge = 0.0;
+    for (int a = 0; a < c->natoms; ++a) charge += (double)c->Z[a];
+    const double cf = charge / total_wrho;
+    const size_t ns = scal_elems(c->natoms);
+    std::vector<double> sc(c->h_scal, c->h_scal + ns);
+    std::vector<double> raw(c->h_scal + kScalAtomQ, c->h_scal + kScalAtomQ + c->ncell);
+    double n = 0.0;
+    for (int t = 0; t < c->ncell; ++t) {
+        sc[kScalAtomQ + c->cell0 + t] = raw[t] * cf;
+        n += raw[t] * cf;
+    }
+    sc[kScalSum] = total_wrho;
+    sc[kScalScale] = cf;
+    sc[kScalNelec] = n;
+    std::copy(sc.begin(), sc.end(), c->h_scal);
+    DFTG_CUDA(cudaMemcpyAsync(c->d_scal, c->h_scal, sizeof(double) * ns, cudaMemcpyHostToDevice, c->stream));
+    DFTG_TRY(launch_xc_points(c, true));        // rho *= cf, point kernel, this shard's E_xc
+    c->rho_scaled = true;
+    DFTG_TRY(launch_hartree_multipoles(c));
+    const size_t n4 = (size_t)c->nlm * c->nrad * 4, n8 = (size_t)c->nlm * c->nrad * 8;
+    DFTG_CUDA(cudaMemcpy2DAsync(blob, sizeof(double) * per, c->d_spl + (size_t)c->cell0 * n4, sizeof(double) * n4,
+                                sizeof(double) * n4, (size_t)c->ncell, cudaMemcpyDeviceToHost, c->stream));
+    DFTG_CUDA(cudaMemcpy2DAsync(blob + n4, sizeof(double) * per, c->d_splm + (size_t)c->cell0 * n8, sizeof(float) * n8,
+                                sizeof(float) * n8, (size_t)c->ncell, cudaMemcpyDeviceToHost, c->stream));
+    DFTG_TRY(sync_scalars(c));
+    c->shard_phase = 2;
+    return DFTG_OK;
+}
+
+int dftg_shard_finish(dftg_ctx *c, const double *blob_all, size_t cap, double *J, double *XC, double *scalars)
+{
+    DFTG_TRY(shard_check(c, 2));
+    const size_t per = shard_blob_doubles(c);
+    if (!blob_all || cap < per * c->natoms) { set_error("blob capacity %zu < %zu", cap, per * c->natoms); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(c->device));
+    const size_t n4 = (size_t)c->nlm * c->nrad * 4, n8 = (size_t)c->nlm * c->nrad * 8;
+    DFTG_CUDA(cudaMemcpy2DAsync(c->d_spl, sizeof(double) * n4, blob_all, sizeof(double) * per, sizeof(double) * n4,
+                                (size_t)c->natoms, cudaMemcpyHostToDevice, c->stream));
+    DFTG_CUDA(cudaMemcpy2DAsync(c->d_splm, sizeof(float) * n8, blob_all + n4, sizeof(double) * per, sizeof(float) * n8,
+                                (size_t)c->natoms, cudaMemcpyHostToDevice, c->stream));
+    DFTG_TRY(launch_hartree_cross(c));
+    DFTG_TRY(launch_contract(c, true, true));
+    const size_t nn = (size_t)c->nbf * c->nbf;
+    if (J) DFTG_CUDA(cudaMemcpyAsync(J, c->d_J, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream));
+    if (XC) DFTG_CUDA(cudaMemcpyAsync(XC, c->d_XC, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream));
+    DFTG_TRY(sync_scalars(c));
+    if (scalars) {
+        scalars[0] = c->h_scal[kScalExc];
+        scalars[1] = c->h_scal[kScalNelec];
+        scalars[2] = c->h_scal[kScalEJ];
+    }
+    c->have_density = true;
+    c->have_hartree = true;
+    c->shard_phase = 0;
     return DFTG_OK;
 }
 
@@ -913,6 +1064,7 @@ int dftg_get_energies(dftg_ctx *c, double *exc, double *ej, double *nelec)
 int dftg_backward_device(dftg_ctx *c, double seed_exc, double seed_ej, double *dEdP_dev, double *dEdR_dev)
 {
     CHECK_CTX(c);
+    CHECK_WHOLE(c);
     if (!c->have_build) { set_error("backward before a complete Fock build"); return DFTG_ERR_STATE; }
     if (!std::isfinite(seed_exc) || !std::isfinite(seed_ej)) { set_error("non-finite seed"); return DFTG_ERR_ARG; }
     DFTG_CUDA(cudaSetDevice(c->device));
@@ -922,6 +1074,7 @@ int dftg_backward_device(dftg_ctx *c, double seed_exc, double seed_ej, double *d
 int dftg_backward(dftg_ctx *c, double seed_exc, double seed_ej, double *dEdP, double *dEdR)
 {
     CHECK_CTX(c);
+    CHECK_WHOLE(c);
     if (!c->have_build) { set_error("backward before a complete Fock build"); return DFTG_ERR_STATE; }
     if (!std::isfinite(seed_exc) || !std::isfinite(seed_ej)) { set_error("non-finite seed"); return DFTG_ERR_ARG; }
     DFTG_CUDA(cudaSetDevice(c->device));
@@ -1031,6 +1184,7 @@ static void shape_candidates(int mx, std::vector<int> &out)
 int dftg_autotune(dftg_ctx *c, int reps, double *best_ms)
 {
     CHECK_CTX(c);
+    CHECK_WHOLE(c);
     if (reps < 1) { set_error("reps < 1"); return DFTG_ERR_ARG; }
     if (!c->have_build) { set_error("autotune before a complete Fock build (it times builds of that P)"); return DFTG_ERR_STATE; }
     DFTG_CUDA(cudaSetDevice(c->device));
@@ -1135,6 +1289,7 @@ extern "C" int dftg_batch_create(dftg_ctx *const *ctxs, int n, dftg_batch **out)
             if (ctxs[j] == ctxs[i]) { set_error("context %d repeated", i); return DFTG_ERR_ARG; }
         if (ctxs[i]->device != ctxs[0]->device) { set_error("contexts on different devices"); return DFTG_ERR_ARG; }
         if (ctxs[i]->points_only) { set_error("context %d is a point-set context (no Fock build)", i); return DFTG_ERR_ARG; }
+        if (ctxs[i]->cell0 != 0 || ctxs[i]->ncell != ctxs[i]->natoms) { set_error("context %d holds part of its molecule's cells", i); return DFTG_ERR_ARG; }
     }
     dftg_batch *b = new (std::nothrow) dftg_batch();
     if (!b) { set_error("host allocation failed"); return DFTG_ERR_NOMEM; }

@@ -132,7 +132,9 @@ struct dftg_ctx {
     std::vector<int> bf_atom, bf_lmn, bf_off;
     std::vector<double> alpha, coef, norm;
 
-    // grid
+    // grid: the fuzzy cells of atoms cell0 .. cell0 + ncell - 1 (every atom's
+    // cell unless the context is one shard of an atom-cell partition)
+    int cell0 = 0, ncell = 0;
     int nrad = 0, leb = 0, nang = 0, lmax = 0, nlm = 0;
     size_t npts = 0, npad = 0;
     std::vector<double> r_n, w_rad;
@@ -261,6 +263,7 @@ struct dftg_ctx {
     unsigned fwd_mask = 0;        // precision mask of that build (the backward follows it)
 
     bool points_only = false;     // built from explicit points and function centres: no cells, no Hartree
+    int shard_phase = 0;          // atom-cell shard build: 1 after the density, 2 after the multipoles
 
     // call-order state
     bool have_density = false;
@@ -340,6 +343,8 @@ int hartree_setup(dftg_ctx *c);
 int cross_pairs_setup(dftg_ctx *c);
 size_t hartree_splf_elems(int nrad);
 int launch_hartree(dftg_ctx *c);
+int launch_hartree_multipoles(dftg_ctx *c);
+int launch_hartree_cross(dftg_ctx *c);
 // k_adjoint.cu
 int launch_backward(dftg_ctx *c, double sxc, double sj, double *dEdP_dev, double *dEdR_dev);
 // k_integrals.cu

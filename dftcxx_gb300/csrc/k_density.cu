@@ -373,7 +373,7 @@ int launch_atom_sums(dftg_ctx *c, int mode)
 {
     // a point-set context has one cell (all points) and no density correction
     if (c->points_only) mode = kSumsOnly;
-    const int ncell = c->points_only ? 1 : c->natoms;
+    const int ncell = c->points_only ? 1 : c->ncell;
     const size_t per_atom = c->points_only ? c->npts : (size_t)c->nrad * c->nang;
     const int cpa = (int)((per_atom + kRedChunk - 1) / kRedChunk);
     const int nb = cpa * ncell;
@@ -384,7 +384,7 @@ int launch_atom_sums(dftg_ctx *c, int mode)
     if (mode == kSumsCorrect) {
         k_scale<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, c->d_scal, c->d_rho);
         DFTG_LAUNCH_CHECK();
-        k_atom_sums<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, c->natoms, c->d_w, c->d_rho, c->d_red, c->d_atoms,
+        k_atom_sums<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, ncell, c->d_w, c->d_rho, c->d_red, c->d_atoms,
                                                      c->d_scal, 1, cnt);
         DFTG_LAUNCH_CHECK();
     }

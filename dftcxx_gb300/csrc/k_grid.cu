@@ -11,7 +11,7 @@
 
 namespace dftg {
 
-__global__ void k_grid_points(int natoms, const double *__restrict__ atoms, const double *__restrict__ rab,
+__global__ void k_grid_points(int natoms, int cell0, const double *__restrict__ atoms, const double *__restrict__ rab,
                               int nrad, int nang, const double *__restrict__ rn, const double *__restrict__ wrad,
                               const double *__restrict__ leb, size_t npts, size_t npad,
                               double *X, double *Y, double *Zc, double *W, double *WB)
@@ -23,7 +23,7 @@ __global__ void k_grid_points(int natoms, const double *__restrict__ atoms, cons
         return;
     }
     const int per_atom = nrad * nang;
-    const int a = (int)(p / per_atom);
+    const int a = cell0 + (int)(p / per_atom);   // the cell (atom) that owns the point
     const int rem = (int)(p % per_atom);
     const int i = rem / nang;
     const int j = rem % nang;
@@ -89,7 +89,7 @@ int launch_grid(dftg_ctx *c)
 {
     const int bs = 128;
     const unsigned nb = (unsigned)((c->npad + bs - 1) / bs);
-    k_grid_points<<<nb, bs, 0, c->stream>>>(c->natoms, c->d_atoms, c->d_rab, c->nrad, c->nang, c->d_rn, c->d_wrad,
+    k_grid_points<<<nb, bs, 0, c->stream>>>(c->natoms, c->cell0, c->d_atoms, c->d_rab, c->nrad, c->nang, c->d_rn, c->d_wrad,
                                             c->d_leb, c->npts, c->npad, c->d_x, c->d_y, c->d_z, c->d_w, c->d_wb);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;

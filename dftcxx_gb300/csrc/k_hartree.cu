@@ -403,12 +403,12 @@ int hartree_setup(dftg_ctx *c)
 // ------------------------------------------------------------------ kernels
 
 // K5a (FP64): CTA per (atom, shell)
-__global__ void k_rholm(int nrad, int nang, int nlm, const double *__restrict__ rho, const double *__restrict__ wb,
-                        const double *__restrict__ Yw, double *__restrict__ rholm)
+__global__ void k_rholm(int nrad, int nang, int nlm, int cell0, const double *__restrict__ rho,
+                        const double *__restrict__ wb, const double *__restrict__ Yw, double *__restrict__ rholm)
 {
     extern __shared__ double s_rw[];   // [nang]
-    const int a = blockIdx.x / nrad, i = blockIdx.x % nrad;
-    const size_t base = ((size_t)a * nrad + i) * nang;
+    const int al = blockIdx.x / nrad, i = blockIdx.x % nrad, a = cell0 + al;
+    const size_t base = ((size_t)al * nrad + i) * nang;
     for (int j = threadIdx.x; j < nang; j += blockDim.x) s_rw[j] = rho[base + j] * wb[base + j];
     __syncthreads();
     for (int lm = threadIdx.x; lm < nlm; lm += blockDim.x) {
@@ -485,16 +485,17 @@ __global__ void __launch_bounds__(128) k_dfgemm(int M, int N, int K, const float
         }
 }
 
-// rho_lm[a][lm][i] = 4 pi sum_j (rho w_becke)[a, i, j] (w_leb Y_lm)[j]: rows m = a N + i.
+// rho_lm[a][lm][i] = 4 pi sum_j (rho w_becke)[a, i, j] (w_leb Y_lm)[j]: rows m = (a - cell0) N + i
+// (the context's points start at cell cell0).
 // K is split in kRholmSlices slices (parallelism); each goes to its own plane and
 // the Poisson kernel adds the planes in order.
 struct EpiRholm {
-    int nrad, nlm;
+    int nrad, nlm, cell0;
     size_t plane;
     double *out;
     __device__ void operator()(int m, int n, int z, dfl v) const
     {
-        const int a = m / nrad, i = m % nrad;
+        const int a = cell0 + m / nrad, i = m % nrad;
         out[z * plane + ((size_t)a * nlm + n) * nrad + i] = df_to(v) * (4.0 * kPi);
     }
 };
@@ -525,13 +526,13 @@ __global__ void k_split_rhow(size_t npts, const double *__restrict__ rho, const 
 // K5b: U_lm = G_l rho_lm (+ the l = 0 boundary column times q_a): one block per
 // (atom, lm), one thread per radial point, four partial sums per dot product.
 // Writes U (FP64) and its hi/lo FP32 split.
-__global__ void k_poisson(int natoms, int nrad, int lmax, const double *__restrict__ Gt,
+__global__ void k_poisson(int natoms, int cell0, int nrad, int lmax, const double *__restrict__ Gt,
                           const double *__restrict__ Gb, const double *__restrict__ rholm,
                           const double *__restrict__ scal, double *__restrict__ U, float *__restrict__ U32)
 {
     extern __shared__ double s_r[];     // [nrad]
     const int nlm = (lmax + 1) * (lmax + 1);
-    const int id = blockIdx.x, a = id / nlm, lm = id % nlm, N = nrad;
+    const int id = blockIdx.x + cell0 * nlm, a = id / nlm, lm = id % nlm, N = nrad;
     int l = 0;
     while ((l + 1) * (l + 1) <= lm) ++l;
     const double *R = rholm + (size_t)id * N;
@@ -560,13 +561,13 @@ __global__ void k_poisson(int natoms, int nrad, int lmax, const double *__restri
 
 // K5b (mixed): the same map in double-float arithmetic.  maps: the double-float
 // copies laid out as in hartree_setup.
-__global__ void k_poisson_split(int natoms, int nrad, int lmax, const float *__restrict__ maps,
+__global__ void k_poisson_split(int natoms, int cell0, int nrad, int lmax, const float *__restrict__ maps,
                                 const double *__restrict__ rholm, size_t rplane, const double *__restrict__ scal,
                                 double *__restrict__ U, float *__restrict__ U32, float *__restrict__ U32T)
 {
     extern __shared__ float s_r2[];     // [2][nrad] rho_lm hi, lo
     const int nlm = (lmax + 1) * (lmax + 1);
-    const int id = blockIdx.x, a = id / nlm, lm = id % nlm, N = nrad;
+    const int id = blockIdx.x + cell0 * nlm, a = id / nlm, lm = id % nlm, N = nrad;
     int l = 0;
     while ((l + 1) * (l + 1) <= lm) ++l;
     const size_t ng = (size_t)(lmax + 1) * N * N;
@@ -601,14 +602,14 @@ __global__ void k_poisson_split(int natoms, int nrad, int lmax, const float *__r
 }
 
 // K5c (FP64): own-cell potential for every point
-__global__ void k_vown(size_t npts, int nrad, int nang, int nlm, const double *__restrict__ rn,
+__global__ void k_vown(size_t npts, int nrad, int nang, int nlm, int cell0, const double *__restrict__ rn,
                        const double *__restrict__ leb, const double *__restrict__ Y, const double *__restrict__ U,
                        double *__restrict__ Vown)
 {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npts) return;
     const int per_atom = nrad * nang;
-    const int a = (int)(p / per_atom), rem = (int)(p % per_atom), i = rem / nang, j = rem % nang;
+    const int a = cell0 + (int)(p / per_atom), rem = (int)(p % per_atom), i = rem / nang, j = rem % nang;
     const double ri = rn[i];
     const double px = leb[4 * j] * ri, py = leb[4 * j + 1] * ri, pz = leb[4 * j + 2] * ri;
     const double inv_r = 1.0 / sqrt(px * px + py * py + pz * pz);
@@ -624,12 +625,12 @@ __global__ void k_vown(size_t npts, int nrad, int nang, int nlm, const double *_
 // cubic coefficients.  One block per (atom, lm).  Writes the FP64 table
 // [atom][lm][interval][4] and the mixed table [atom][lm][interval][8] =
 // fold_lm * (c0..c3) split into FP32 hi and lo.
-__global__ void k_splines(int natoms, int nrad, int nlm, const double *__restrict__ splf,
+__global__ void k_splines(int natoms, int cell0, int nrad, int nlm, const double *__restrict__ splf,
                           const double *__restrict__ Kt, const double *__restrict__ U,
                           const double *__restrict__ fold, double *__restrict__ spl, float *__restrict__ splm)
 {
     extern __shared__ double s_spl[];   // y [n], D [n]
-    const int id = blockIdx.x, n = nrad;
+    const int id = blockIdx.x + cell0 * nlm, n = nrad;
     double *y = s_spl, *D = s_spl + n;
     const double *u = U + (size_t)id * n;      // u[i] at r_n[i] (decreasing r)
     for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = u[n - 1 - i];
@@ -674,12 +675,12 @@ __global__ void k_splines(int natoms, int nrad, int nlm, const double *__restric
 
 // K5d (mixed): the same spline fit in double-float arithmetic from the split U;
 // the FP64 table is written only when want64 (an FP64 cross-atom step follows).
-__global__ void k_splines_split(int natoms, int nrad, int nlm, int lmax, const float *__restrict__ maps,
+__global__ void k_splines_split(int natoms, int cell0, int nrad, int nlm, int lmax, const float *__restrict__ maps,
                                 const float *__restrict__ U32, int want64, double *__restrict__ spl,
                                 float *__restrict__ splm)
 {
     extern __shared__ float s_y2[];    // y hi [n], y lo [n], D hi [n], D lo [n]
-    const int id = blockIdx.x, n = nrad;
+    const int id = blockIdx.x + cell0 * nlm, n = nrad;
     const size_t ng = (size_t)(lmax + 1) * n * n;
     const float *Kh = maps + 2 * ng + 2 * (size_t)n, *Kl = Kh + (size_t)n * n;
     const float *ih = Kl + (size_t)n * n, *il = ih + n;
@@ -748,7 +749,8 @@ __device__ __forceinline__ void spline_interval(double rd, const double *__restr
 }
 
 // K5e (FP64): total potential on every point; writes V and cj = w V / 2
-__global__ void __launch_bounds__(128) k_vcross64(size_t npts, size_t npad, int natoms, int nrad, int nang, int lmax,
+__global__ void __launch_bounds__(128) k_vcross64(size_t npts, size_t npad, int natoms, int cell0, int nrad, int nang,
+                                                  int lmax,
                                                   const double *__restrict__ atoms, const double *__restrict__ X,
                                                   const double *__restrict__ Yc, const double *__restrict__ Zc,
                                                   const double *__restrict__ W, const double *__restrict__ sx,
@@ -762,7 +764,7 @@ __global__ void __launch_bounds__(128) k_vcross64(size_t npts, size_t npad, int 
     if (p >= npts) { V[p] = 0.0; cj[p] = 0.0; cj32[p] = 0.f; return; }
     const int nlm = (lmax + 1) * (lmax + 1);
     const int N = nrad;
-    const int a = (int)(p / ((size_t)nrad * nang));
+    const int a = cell0 + (int)(p / ((size_t)nrad * nang));
     const double px = X[p], py = Yc[p], pz = Zc[p];
     const double fscale = (double)(N + 1) / kPi;
     double Vt = 0.0;
@@ -932,7 +934,7 @@ __global__ void __launch_bounds__(128) k_vcross_bins(int nrad, int lmax_rt,
 
 // total potential per point: own cell (FP64) plus the pair contributions in
 // atom order, summed with TwoSum; writes V and cj = w V / 2
-__global__ void k_vcross_gather(size_t npts, size_t npad, int natoms, int nrad, int nang,
+__global__ void k_vcross_gather(size_t npts, size_t npad, int natoms, int cell0, int nrad, int nang,
                                 const int *__restrict__ pos, const float2 *__restrict__ pairv,
                                 const double *__restrict__ Vown, const double *__restrict__ W,
                                 double *__restrict__ V, double *__restrict__ cj, float *__restrict__ cj32)
@@ -940,7 +942,7 @@ __global__ void k_vcross_gather(size_t npts, size_t npad, int natoms, int nrad, 
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npad) return;
     if (p >= npts) { V[p] = 0.0; cj[p] = 0.0; cj32[p] = 0.f; return; }
-    const int a = (int)(p / ((size_t)nrad * nang));
+    const int a = cell0 + (int)(p / ((size_t)nrad * nang));
     float vh = 0.f, vl = 0.f;
     for (int k = 0; k < natoms; ++k) {
         if (k == a) continue;
@@ -963,11 +965,11 @@ __global__ void k_vcross_gather(size_t npts, size_t npad, int natoms, int nrad, 
 // the enumeration index as payload, then the per-pair geometry at its sorted
 // place.  The runs of at most kCrossTask pairs inside one bin (the tasks of
 // k_vcross_bins) are formed on the host from the bin counts.
-__device__ __forceinline__ void pair_of_enum(size_t e, int na, int per_atom, size_t &p, int &k)
+__device__ __forceinline__ void pair_of_enum(size_t e, int na, int cell0, int per_atom, size_t &p, int &k)
 {
     p = e / (size_t)(na - 1);
     const int j = (int)(e - p * (size_t)(na - 1));
-    const int a = (int)(p / per_atom);
+    const int a = cell0 + (int)(p / per_atom);
     k = j < a ? j : j + 1;          // every atom but the point's own
 }
 
@@ -986,7 +988,7 @@ __device__ __forceinline__ void pair_interval(double r, const double *__restrict
     t = r - sx[iv];
 }
 
-__global__ void k_pair_keys(size_t npairs, int na, int per_atom, int N, const double *__restrict__ X,
+__global__ void k_pair_keys(size_t npairs, int na, int cell0, int per_atom, int N, const double *__restrict__ X,
                             const double *__restrict__ Y, const double *__restrict__ Z,
                             const double *__restrict__ atoms, const double *__restrict__ sx, int *__restrict__ key,
                             int *__restrict__ idx, unsigned *__restrict__ count)
@@ -995,7 +997,7 @@ __global__ void k_pair_keys(size_t npairs, int na, int per_atom, int N, const do
     if (e >= npairs) return;
     size_t p;
     int k;
-    pair_of_enum(e, na, per_atom, p, k);
+    pair_of_enum(e, na, cell0, per_atom, p, k);
     const double dx = X[p] - atoms[4 * k], dy = Y[p] - atoms[4 * k + 1], dz = Z[p] - atoms[4 * k + 2];
     int iv;
     double t;
@@ -1006,7 +1008,7 @@ __global__ void k_pair_keys(size_t npairs, int na, int per_atom, int N, const do
     atomicAdd(count + kk, 1u);
 }
 
-__global__ void k_pair_place(size_t npairs, int na, int per_atom, int N, const double *__restrict__ X,
+__global__ void k_pair_place(size_t npairs, int na, int cell0, int per_atom, int N, const double *__restrict__ X,
                              const double *__restrict__ Y, const double *__restrict__ Z,
                              const double *__restrict__ atoms, const double *__restrict__ sx,
                              const int *__restrict__ order, float4 *__restrict__ geo, float2 *__restrict__ tk,
@@ -1017,7 +1019,7 @@ __global__ void k_pair_place(size_t npairs, int na, int per_atom, int N, const d
     const size_t e = (size_t)order[dst];
     size_t p;
     int k;
-    pair_of_enum(e, na, per_atom, p, k);
+    pair_of_enum(e, na, cell0, per_atom, p, k);
     // the geometry of a pair is fixed for the grid: direction, 1/r and the
     // spline offset are formed in FP64 and rounded once to FP32
     const double dx = X[p] - atoms[4 * k], dy = Y[p] - atoms[4 * k + 1], dz = Z[p] - atoms[4 * k + 2];
@@ -1067,7 +1069,7 @@ int cross_pairs_setup(dftg_ctx *c)
     if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(unsigned) * nkeys, c->stream);
     const unsigned nb = (unsigned)((npairs + 255) / 256);
     if (e == cudaSuccess) {
-        k_pair_keys<<<nb, 256, 0, c->stream>>>(npairs, na, per_atom, N, c->d_x, c->d_y, c->d_z, c->d_atoms, sx, kin,
+        k_pair_keys<<<nb, 256, 0, c->stream>>>(npairs, na, c->cell0, per_atom, N, c->d_x, c->d_y, c->d_z, c->d_atoms, sx, kin,
                                               iin, cnt);
         e = cudaGetLastError();
     }
@@ -1080,7 +1082,7 @@ int cross_pairs_setup(dftg_ctx *c)
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_pairpos, 0, sizeof(int) * n * (size_t)na, c->stream);
     if (e == cudaSuccess) {
         char *base = static_cast<char *>(c->d_pairs);
-        k_pair_place<<<nb, 256, 0, c->stream>>>(npairs, na, per_atom, N, c->d_x, c->d_y, c->d_z, c->d_atoms, sx, iout,
+        k_pair_place<<<nb, 256, 0, c->stream>>>(npairs, na, c->cell0, per_atom, N, c->d_x, c->d_y, c->d_z, c->d_atoms, sx, iout,
                                                reinterpret_cast<float4 *>(base),
                                                reinterpret_cast<float2 *>(base + sizeof(float4) * npairs),
                                                c->d_pairpos);
@@ -1150,72 +1152,82 @@ static int launch_vcross_bins(dftg_ctx *c)
     return DFTG_OK;
 }
 
-int launch_hartree(dftg_ctx *c)
+// multipole part of the Hartree step for the context's cells (atoms cell0 ..
+// cell0 + ncell - 1, whose points the context holds): rho_lm, the radial
+// Poisson maps, the own-cell potential and the spline coefficients of U_lm
+int launch_hartree_multipoles(dftg_ctx *c)
 {
-    const int N = c->nrad, S = N + 2, nlm = c->nlm;
+    const int N = c->nrad, nlm = c->nlm, nc = c->ncell, c0 = c->cell0;
     // the mixed multipole kernels keep radial vectors per block in shared
     // memory: up to 256 radial points (the FP64 kernels take any)
     const bool mp = (c->prec_mask & kPrecMultipole) != 0 && N <= 256;
     const size_t rplane = (size_t)c->natoms * nlm * N;
     if (mp) {
-        // rho_lm as a double-float GEMM [(a, i) x j] x [j x lm], K split in two planes
+        // rho_lm as a double-float GEMM [(a, i) x j] x [j x lm], K split in planes
         float *S32 = reinterpret_cast<float *>(c->d_red2);
         k_split_rhow<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, c->d_rho, c->d_wb, S32);
         DFTG_LAUNCH_CHECK();
-        const int M = c->natoms * N;
+        const int M = nc * N;
         dim3 grid((unsigned)((nlm + kDgBN - 1) / kDgBN), (unsigned)((M + kDgBM - 1) / kDgBM), kRholmSlices);
         k_dfgemm<EpiRholm><<<grid, 128, 0, c->stream>>>(M, nlm, c->nang, S32, S32 + c->npts, c->nang, c->d_Ywt32,
                                                         c->d_Ywt32 + (size_t)nlm * c->nang, nlm,
-                                                        EpiRholm{N, nlm, rplane, c->d_rholm});
+                                                        EpiRholm{N, nlm, c0, rplane, c->d_rholm});
     } else
-        k_rholm<<<c->natoms * N, 96, sizeof(double) * c->nang, c->stream>>>(N, c->nang, nlm, c->d_rho, c->d_wb,
-                                                                            c->d_Yw, c->d_rholm);
+        k_rholm<<<nc * N, 96, sizeof(double) * c->nang, c->stream>>>(N, c->nang, nlm, c0, c->d_rho, c->d_wb, c->d_Yw,
+                                                                    c->d_rholm);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "rholm");
-    const int nrhs = c->natoms * nlm;
-    (void)S;
+    const int nrhs = nc * nlm;
     if (mp)
-        k_poisson_split<<<nrhs, 128, sizeof(float) * 2 * N, c->stream>>>(
-            c->natoms, N, c->lmax, c->d_maps32,
+        k_poisson_split<<<nrhs, 128, sizeof(float) * 2 * N, c->stream>>>(c->natoms, c0, N, c->lmax, c->d_maps32,
                                                                          c->d_rholm, rplane, c->d_scal, c->d_U,
                                                                          c->d_U32, c->d_U32T);
     else
-        k_poisson<<<nrhs, 128, sizeof(double) * N, c->stream>>>(c->natoms, N, c->lmax, c->d_Gt, c->d_Gb, c->d_rholm,
-                                                                c->d_scal, c->d_U, c->d_U32);
+        k_poisson<<<nrhs, 128, sizeof(double) * N, c->stream>>>(c->natoms, c0, N, c->lmax, c->d_Gt, c->d_Gb,
+                                                                c->d_rholm, c->d_scal, c->d_U, c->d_U32);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "poisson");
     const unsigned npb = (unsigned)((c->npts + 127) / 128);
     if (mp) {
         // own-cell potential as a double-float GEMM [(a, i) x lm] x [lm x j]
-        const int M = c->natoms * N;
+        const int M = nc * N;
+        const size_t off = (size_t)c0 * N * nlm;
         dim3 grid((unsigned)((c->nang + kDgBN - 1) / kDgBN), (unsigned)((M + kDgBM - 1) / kDgBM), 1);
-        k_dfgemm<EpiVown><<<grid, 128, 0, c->stream>>>(M, c->nang, nlm, c->d_U32T, c->d_U32T + rplane, nlm, c->d_Y32,
-                                                       c->d_Y32 + (size_t)nlm * c->nang, c->nang,
+        k_dfgemm<EpiVown><<<grid, 128, 0, c->stream>>>(M, c->nang, nlm, c->d_U32T + off, c->d_U32T + rplane + off, nlm,
+                                                       c->d_Y32, c->d_Y32 + (size_t)nlm * c->nang, c->nang,
                                                        EpiVown{c->nang, c->d_invr, c->d_Vown});
     } else
-        k_vown<<<npb, 128, 0, c->stream>>>(c->npts, N, c->nang, nlm, c->d_rn, c->d_leb, c->d_Y, c->d_U, c->d_Vown);
+        k_vown<<<npb, 128, 0, c->stream>>>(c->npts, N, c->nang, nlm, c0, c->d_rn, c->d_leb, c->d_Y, c->d_U, c->d_Vown);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "vown");
     if (mp)
         k_splines_split<<<nrhs, 128, sizeof(float) * 4 * N, c->stream>>>(
-            c->natoms, N, nlm, c->lmax, c->d_maps32, c->d_U32, (c->prec_mask & kPrecCross) ? 0 : 1, c->d_spl,
+            c->natoms, c0, N, nlm, c->lmax, c->d_maps32, c->d_U32, (c->prec_mask & kPrecCross) ? 0 : 1, c->d_spl,
             c->d_splm);
     else
-        k_splines<<<nrhs, 128, sizeof(double) * 2 * N, c->stream>>>(c->natoms, N, nlm, c->d_splf, c->d_Kt, c->d_U,
+        k_splines<<<nrhs, 128, sizeof(double) * 2 * N, c->stream>>>(c->natoms, c0, N, nlm, c->d_splf, c->d_Kt, c->d_U,
                                                                     c->d_fold, c->d_spl, c->d_splm);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "splines");
+    return DFTG_OK;
+}
+
+// cross-atom part: the potential of every other atom's spline expansion on the
+// context's points, the total V, cj = w V / 2 and E_J
+int launch_hartree_cross(dftg_ctx *c)
+{
+    const int N = c->nrad;
     const unsigned nb = (unsigned)(c->npad / 128);
     if (c->prec_mask & kPrecCross) {
         if (c->npairs > 0) {
             DFTG_TRY_L(launch_vcross_bins(c));
         }
         k_vcross_gather<<<(unsigned)((c->npad + 127) / 128), 128, 0, c->stream>>>(
-            c->npts, c->npad, c->natoms, N, c->nang, c->d_pairpos, reinterpret_cast<const float2 *>(c->d_pairv),
+            c->npts, c->npad, c->natoms, c->cell0, N, c->nang, c->d_pairpos, reinterpret_cast<const float2 *>(c->d_pairv),
             c->d_Vown, c->d_w, c->d_V, c->d_cj, c->d_cj32);
     } else
-        k_vcross64<<<nb, 128, 0, c->stream>>>(c->npts, c->npad, c->natoms, N, c->nang, c->lmax, c->d_atoms, c->d_x,
-                                              c->d_y, c->d_z, c->d_w, c->d_sx, c->d_spl, c->d_pre, c->d_rec,
+        k_vcross64<<<nb, 128, 0, c->stream>>>(c->npts, c->npad, c->natoms, c->cell0, N, c->nang, c->lmax, c->d_atoms,
+                                              c->d_x, c->d_y, c->d_z, c->d_w, c->d_sx, c->d_spl, c->d_pre, c->d_rec,
                                               c->d_Vown, c->d_V, c->d_cj, c->d_cj32);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "vcross");
@@ -1225,6 +1237,12 @@ int launch_hartree(dftg_ctx *c)
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "hartree_energy");
     return DFTG_OK;
+}
+
+int launch_hartree(dftg_ctx *c)
+{
+    DFTG_TRY_L(launch_hartree_multipoles(c));
+    return launch_hartree_cross(c);
 }
 
 }  // namespace dftg

@@ -648,6 +648,7 @@ extern "C" int dftg_scf_init(dftg_ctx *c, const dftg_scf_params *prm)
 {
     if (!c || !prm) { set_error("NULL argument"); return DFTG_ERR_ARG; }
     if (c->points_only) { set_error("a point-set context has no nuclei: no SCF"); return DFTG_ERR_STATE; }
+    if (c->cell0 != 0 || c->ncell != c->natoms) { set_error("a context over part of the cells has no whole build: no SCF"); return DFTG_ERR_STATE; }
     const int n = c->nbf;
     if (n > kScfMaxN) {
         set_error("device SCF supports nbf <= %d (got %d)", kScfMaxN, n);

@@ -26,7 +26,9 @@ class MolecularGrid:
     ``precision``: "fp64" (every step in FP64) or "mixed" (split-precision
     contractions, FP64 reductions)."""
 
-    def __init__(self, mol, radial_points=15, lebedev_order=7, lmax=8, precision="fp64", device=0):
+    def __init__(self, mol, radial_points=15, lebedev_order=7, lmax=8, precision="fp64", device=0, cells=None):
+        """cells: (first_cell, ncells) for a context over part of the molecule's
+        fuzzy cells (an atom-cell shard, built with dftcxx_gb300.shard)."""
         L = _lib.load()
         self.mol = mol
         self._arrays = [np.ascontiguousarray(mol.Z, dtype=np.int32),
@@ -42,7 +44,11 @@ class MolecularGrid:
         b = _lib.Basis(mol.nbf, ba.ctypes.data_as(ip), bl.ctypes.data_as(ip), bn.ctypes.data_as(ip), _ptr(pa), _ptr(pc))
         g = _lib.GridParams(radial_points, lebedev_order, lmax, device)
         h = ctypes.c_void_p()
-        check(L.dftg_create(ctypes.byref(m), ctypes.byref(b), ctypes.byref(g), ctypes.byref(h)))
+        if cells is None:
+            check(L.dftg_create(ctypes.byref(m), ctypes.byref(b), ctypes.byref(g), ctypes.byref(h)))
+        else:
+            check(L.dftg_create_cells(ctypes.byref(m), ctypes.byref(b), ctypes.byref(g), int(cells[0]), int(cells[1]),
+                                      ctypes.byref(h)))
         self._h = h
         n = ctypes.c_size_t()
         check(L.dftg_grid_size(h, ctypes.byref(n)))

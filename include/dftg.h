@@ -177,6 +177,39 @@ int dftg_create_points(const dftg_points *pts, const dftg_molecule *centres, con
 int dftg_xc_build(dftg_ctx *ctx, const double *P, double *XC, double *exc, double *nelec);
 int dftg_xc_build_device(dftg_ctx *ctx, const double *P_dev, double *XC_dev, double *scalars_dev);
 
+/* Atom-cell shards (no counterpart in the reference, which keeps one
+ * AtomicGrid per atom in one process: moleculargrid.cpp:193-261, 336-389).
+ * For several GPUs, or several processes, the build is split by fuzzy cell:
+ * every rank creates a context over the cells of atoms [first_cell,
+ * first_cell + ncells) of the same molecule (the grid points of those cells;
+ * Becke weights, basis functions and the cross-atom potential still see every
+ * atom) and runs the three calls below, with three exchanges between them:
+ *   1. dftg_shard_density: rho on the shard's points (P: host nbf x nbf);
+ *      *sum_wrho = the shard's integral of w rho.  Exchange: all-reduce (sum)
+ *      of sum_wrho over the ranks = the molecule's integral.
+ *   2. dftg_shard_multipoles(total): the correction factor sum(Z) / total
+ *      (moleculargrid.cpp:132-146), the LDA point kernel, and rho_lm, the
+ *      Poisson solve, the own-cell potential and the spline data of the
+ *      shard's cells, written to blob [ncells][per-cell doubles] (see
+ *      dftg_shard_blob_size).  Exchange: all-gather of the blobs in cell order
+ *      = [natoms][per-cell doubles].
+ *   3. dftg_shard_finish(blob_all): the cross-atom potential on the shard's
+ *      points from every cell's splines, and the shard's parts of J, XC (host
+ *      nbf x nbf, either may be NULL) and scalars = {E_xc, integral of the
+ *      corrected rho, E_J}.  Exchange: all-reduce (sum) of J, XC and scalars =
+ *      the whole build's.
+ * The blobs are opaque doubles (FP64 and split FP32 spline tables) that must
+ * travel bit for bit.  The whole-molecule build calls (dftg_fock_build*,
+ * dftg_correct_densities, dftg_calculate_hartree_potential, backward, SCF,
+ * batches) return DFTG_ERR_STATE on a shard context; dftg_set_density,
+ * dftg_calculate_density and the getters act on the shard's points. */
+int dftg_create_cells(const dftg_molecule *mol, const dftg_basis *basis, const dftg_grid_params *grid,
+                      int first_cell, int ncells, dftg_ctx **out);
+int dftg_shard_blob_size(const dftg_ctx *ctx, size_t *doubles_per_cell, int *first_cell, int *ncells);
+int dftg_shard_density(dftg_ctx *ctx, const double *P, double *sum_wrho);
+int dftg_shard_multipoles(dftg_ctx *ctx, double total_wrho, double *blob, size_t cap);
+int dftg_shard_finish(dftg_ctx *ctx, const double *blob_all, size_t cap, double *J, double *XC, double *scalars);
+
 /* Getters (copies): MolecularGrid::get_weights / get_densities /
  * get_amplitudes (moleculargrid.cpp:61-127).  cap is the element capacity of
  * out.  Amplitudes are nbf x npts column-major (the reference's layout). */

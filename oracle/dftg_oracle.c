@@ -1126,3 +1126,135 @@ double orc_points_xc(long npts, const double *xyz, const double *w, int nbf, con
     free(off);
     return exc;
 }
+
+/* ------------------------------------------------ atom-cell shards
+ * The same build split by fuzzy cell (MolecularGrid keeps one AtomicGrid per
+ * atom and sums their J blocks, moleculargrid.cpp:336-389), for checking the
+ * exchange pattern of a sharded build on CPU ranks: each rank holds the cells
+ * [c0, c0 + nc) and, between the calls below, the ranks exchange
+ *   (1) the sum of w rho over all cells (all-reduce), for the correction factor
+ *       of moleculargrid.cpp:132-146;
+ *   (2) every cell's spline data (all-gather), for the cross-atom potential of
+ *       moleculargrid.cpp:342-380;
+ *   (3) J, XC and the energies (all-reduce). */
+
+/* rho on the points of cells [c0, c0 + nc); returns their sum of w rho */
+double orc_shard_density(orc_t *o, const double *P, int c0, int nc)
+{
+    const int nbf = o->nbf;
+    const size_t per = (size_t)o->nrad * o->nang, p0 = (size_t)c0 * per, p1 = (size_t)(c0 + nc) * per;
+    #pragma omp parallel
+    {
+        double *t = malloc(sizeof(double) * nbf);
+        #pragma omp for schedule(static)
+        for (long i = (long)p0; i < (long)p1; ++i) {
+            const double *f = o->phi + (size_t)i * nbf;
+            for (int r = 0; r < nbf; ++r) {
+                double s = 0.0;
+                for (int c = 0; c < nbf; ++c) s += P[r + (size_t)c * nbf] * f[c];
+                t[r] = s;
+            }
+            double d = 0.0;
+            for (int r = 0; r < nbf; ++r) d += f[r] * t[r];
+            o->rho[i] = 2.0 * d;
+        }
+        free(t);
+    }
+    double s = 0.0;
+    for (int a = c0; a < c0 + nc; ++a) s += atom_density(o, a);
+    return s;
+}
+
+/* doubles of spline data per cell: ordinates [nlm][nrad], coefficients [nlm][nrad-1][4] */
+long orc_shard_blob_doubles(const orc_t *o)
+{
+    return (long)o->nlm * o->nrad + (long)o->nlm * (o->nrad - 1) * 4;
+}
+
+/* correction factor cf = sum(Z over every atom) / total, applied to the
+ * cells' rho; then rho_lm, the Poisson solve, the own-cell potential and the
+ * splines of those cells; their spline data into blob [nc][blob doubles] */
+void orc_shard_multipoles(orc_t *o, double total, int c0, int nc, double *blob)
+{
+    double charge = 0.0;
+    for (int a = 0; a < o->natoms; ++a) charge += o->Z[a];
+    const double cf = charge / total;
+    const size_t per = (size_t)o->nrad * o->nang;
+    for (size_t i = (size_t)c0 * per; i < (size_t)(c0 + nc) * per; ++i) o->rho[i] *= cf;
+    const size_t ny = (size_t)o->nlm * o->nrad, nsc = (size_t)o->nlm * (o->nrad - 1) * 4;
+    for (int a = c0; a < c0 + nc; ++a) {
+        calc_rho_lm(o, a);
+        calc_U_lm(o, a);
+        double *b = blob + (size_t)(a - c0) * (ny + nsc);
+        memcpy(b, o->sy + (size_t)a * ny, sizeof(double) * ny);
+        memcpy(b + ny, o->sc + (size_t)a * nsc, sizeof(double) * nsc);
+    }
+}
+
+/* with every cell's spline data (blob_all [natoms][blob doubles]): the total
+ * potential on the cells' points, their J block (atomicgrid.cpp:471-488), their
+ * part of XC and E_xc (dft.cpp:394-433); scal = {E_xc, sum w rho, 2 tr(P J_part)} */
+void orc_shard_finish(orc_t *o, const double *blob_all, const double *P, int c0, int nc, double *J, double *XC,
+                      double *scal)
+{
+    const int N = o->nrad, nlm = o->nlm, nang = o->nang, nbf = o->nbf;
+    const size_t ny = (size_t)nlm * N, nsc = (size_t)nlm * (N - 1) * 4;
+    for (int a = 0; a < o->natoms; ++a) {
+        memcpy(o->sy + (size_t)a * ny, blob_all + (size_t)a * (ny + nsc), sizeof(double) * ny);
+        memcpy(o->sc + (size_t)a * nsc, blob_all + (size_t)a * (ny + nsc) + ny, sizeof(double) * nsc);
+    }
+    for (int i = c0; i < c0 + nc; ++i) {
+        size_t base = (size_t)i * N * nang;
+        #pragma omp parallel for schedule(static)
+        for (long j = 0; j < (long)N * nang; ++j) {
+            double V = 0.0;
+            const double *pp = o->pos + 3 * (base + j);
+            for (int k = 0; k < o->natoms; ++k) {
+                if (i == k) { V += o->Vown[base + j]; continue; }
+                int lm = 0;
+                for (int l = 0; l <= o->lmax; ++l)
+                    for (int m = -l; m <= l; ++m) {
+                        double d[3] = {pp[0] - o->xyz[3 * k], pp[1] - o->xyz[3 * k + 1], pp[2] - o->xyz[3 * k + 2]};
+                        double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                        double y = ylm_dir(l, m, d);
+                        const double *sy = o->sy + ((size_t)k * nlm + lm) * N;
+                        const double *sc = o->sc + ((size_t)k * nlm + lm) * (N - 1) * 4;
+                        V += 1.0 / r * y * spline_eval(N, o->sx, sy, sc, r);
+                        lm++;
+                    }
+            }
+            o->V[base + j] = V;
+        }
+    }
+    memset(J, 0, sizeof(double) * nbf * nbf);
+    memset(XC, 0, sizeof(double) * nbf * nbf);
+    const size_t p0 = (size_t)c0 * N * nang, p1 = (size_t)(c0 + nc) * N * nang;
+    double exc = 0.0, nel = 0.0;
+    double *wv = malloc(sizeof(double) * (p1 - p0));
+    for (size_t p = p0; p < p1; ++p) {
+        double e, v;
+        orc_lda_point(o->rho[p], &e, &v);
+        exc += o->w[p] * e;
+        nel += o->w[p] * o->rho[p];
+        wv[p - p0] = o->w[p] * v;
+    }
+    #pragma omp parallel for schedule(dynamic)
+    for (int i = 0; i < nbf; ++i)
+        for (int j = i; j < nbf; ++j) {
+            double sj = 0.0, sx = 0.0;
+            for (size_t p = p0; p < p1; ++p) {
+                const double f = o->phi[p * nbf + i] * o->phi[p * nbf + j];
+                sj += o->w[p] * o->V[p] * f;
+                sx += wv[p - p0] * f;
+            }
+            J[i + (size_t)j * nbf] = J[j + (size_t)i * nbf] = 0.5 * sj;
+            XC[i + (size_t)j * nbf] = XC[j + (size_t)i * nbf] = sx;
+        }
+    free(wv);
+    double ej = 0.0;
+    for (int i = 0; i < nbf; ++i)
+        for (int j = 0; j < nbf; ++j) ej += P[i + (size_t)j * nbf] * J[j + (size_t)i * nbf];
+    scal[0] = exc;
+    scal[1] = nel;
+    scal[2] = 2.0 * ej;
+}

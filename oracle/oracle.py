@@ -78,6 +78,12 @@ def lib():
                                     ctypes.c_int, _dp, _dp]
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_set_sample_stride.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_shard_density.restype = ctypes.c_double
+        L.orc_shard_density.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int]
+        L.orc_shard_blob_doubles.restype = ctypes.c_long
+        L.orc_shard_blob_doubles.argtypes = [ctypes.c_void_p]
+        L.orc_shard_multipoles.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp]
+        L.orc_shard_finish.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
         L.orc_get_timings.argtypes = [ctypes.c_void_p, _dp]
         _lib = L
     return _lib
@@ -227,6 +233,37 @@ class OracleGrid:
         J = self.hartree()
         XC, exc = self.xc()
         return {"J": J, "XC": XC, "Exc": exc, "scale": c, "nelec": self.calculate_density()}
+
+
+class OracleShard:
+    """The cells [first_cell, first_cell + ncells) of an oracle grid, with the
+    interface of dftcxx_gb300.shard's backends (density / multipoles /
+    finish): the CPU stand-in of one rank in checks of the sharded build."""
+
+    def __init__(self, mol, nrad, lebedev_order, lmax, first_cell, ncells):
+        self.grid = OracleGrid(mol, nrad, lebedev_order, lmax)
+        self.first_cell, self.ncells = first_cell, ncells
+        self.blob_per_cell = int(lib().orc_shard_blob_doubles(self.grid.h))
+        self.nbf = mol.nbf
+
+    def density(self, P):
+        P = np.asfortranarray(P, dtype=np.float64)
+        return lib().orc_shard_density(self.grid.h, _p(P), self.first_cell, self.ncells)
+
+    def multipoles(self, total):
+        blob = np.zeros(self.blob_per_cell * self.ncells)
+        lib().orc_shard_multipoles(self.grid.h, float(total), self.first_cell, self.ncells, _p(blob))
+        return blob
+
+    def finish(self, blob_all, P):
+        n = self.nbf
+        blob_all = np.ascontiguousarray(blob_all, dtype=np.float64)
+        P = np.asfortranarray(P, dtype=np.float64)
+        J = np.zeros((n, n), order="F")
+        XC = np.zeros((n, n), order="F")
+        sc = np.zeros(3)
+        lib().orc_shard_finish(self.grid.h, _p(blob_all), _p(P), self.first_cell, self.ncells, _p(J), _p(XC), _p(sc))
+        return np.ascontiguousarray(J), np.ascontiguousarray(XC), sc
 
 
 def energy(P, H, J, enuc, exc):
