@@ -127,7 +127,9 @@ def test_contract_noalloc_three_blocks_padded_rows(gpu_lib, oracle_mod):
         assert _rel(XC, XC_ref) <= 1e-10
         assert _rel(XC, (phi * cxc) @ phi.T) <= 1e-10
         assert _rel(J, (phi * cj) @ phi.T) <= 1e-10
-        assert np.array_equal(XC, XC.T) and np.array_equal(J, J.T)
+        # off-diagonal blocks are written once and mirrored; diagonal blocks are
+        # summed in both orders, so they agree to rounding
+        assert _rel(XC, XC.T) <= 1e-14 and _rel(J, J.T) <= 1e-14
     g.close()
 
 
