@@ -64,8 +64,11 @@ def _fixed_density():
     the reference program's outputs at it."""
     return dict(np.load(REF_FIXTURE))
 
-# kernels launched per phase of one mixed-precision build (dftg_fock_build_device)
-KERNELS_PER_PHASE = {"density": 2, "charge": 1, "lda": 1, "rholm": 2, "poisson": 1, "vown": 1,
+# kernels launched per phase of one mixed-precision build (dftg_fock_build_device):
+# density = P slicing with the correction factor + the tensor-core density with
+# the LDA point kernel; multipole = rho_lm, Poisson and splines; vcross = the
+# pair evaluation + the own-cell / total potential with E_J
+KERNELS_PER_PHASE = {"density": 2, "charge": 1, "lda": 1, "multipole": 1, "rholm": 1, "poisson": 1, "vown": 1,
                      "splines": 1, "vcross": 2, "hartree_energy": 1, "contract_bounds": 1, "contract": 1,
                      "contract_reduce": 1}
 

@@ -23,7 +23,6 @@ constexpr double kPiTrunc = 3.14159265359;          // cgf.cpp:103, integrals.cp
 constexpr int kLmaxCap = 16;
 constexpr int kMaxAtoms = 256;
 constexpr int kPtsAlign = 128;
-constexpr int kRholmSlices = 6;      // K slices of the mixed rho_lm GEMM (planes of d_rholm)
 
 void set_error(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
@@ -183,11 +182,10 @@ struct dftg_ctx {
     float *d_pre32 = nullptr;
     double *d_rec = nullptr;      // [nlm][2] associated-Legendre recursion coefficients
     float *d_rec32 = nullptr;
-    double *d_rholm = nullptr;    // [natoms][nlm][nrad]
+    double *d_rholm = nullptr;    // [natoms][nlm][nrad] (FP64 path)
     double *d_U = nullptr;        // [natoms][nlm][nrad]
     float *d_U32 = nullptr;       // [2][natoms][nlm][nrad] U split into FP32 hi, lo
     float *d_U32T = nullptr;      // [2][natoms][nrad][nlm] the same, transposed
-    double *d_red2 = nullptr;     // [npts] work plane (rho w_becke split for the rho_lm GEMM)
     float *d_Y32 = nullptr;       // [2][nlm][nang] Y_lm split into FP32 hi, lo
     float *d_Ywt32 = nullptr;     // [2][nang][nlm] w_leb Y_lm split, transposed
     double *d_fold = nullptr;     // [nlm] Y_lm normalisation of the integer recursion
@@ -214,6 +212,7 @@ struct dftg_ctx {
     void *d_tcB = nullptr;        // [4][NP x KP] BF16 slices of P
     int *d_tc_rowexp = nullptr;   // [npad] per-point scale exponents
     int *d_tc_colexp = nullptr;   // [NP] per-column scale exponents of P
+    double *d_Sgrid = nullptr;    // [nbf][nbf] Phi^T diag(w) Phi (FP64), for the fused density + LDA pass
     int *d_flag = nullptr;        // device error flag (bounded waits that expired)
 
     // device: tensor-core density for 81 <= nbf <= 1024 (128-point tiles x 128-column blocks)
@@ -328,11 +327,11 @@ int mark(dftg_ctx *c, const char *name);
 int launch_grid(dftg_ctx *c);
 int launch_amplitudes(dftg_ctx *c);
 // k_density.cu
-int launch_density(dftg_ctx *c);
+int launch_density(dftg_ctx *c, bool fuse_lda = false);
 enum { kSumsOnly = 0, kSumsCorrect = 1, kSumsFactor = 2 };
 // k_density_tc.cu
 int density_tc_setup(dftg_ctx *c);
-int launch_density_tc(dftg_ctx *c);
+int launch_density_tc(dftg_ctx *c, bool fuse_lda);
 // k_density_tt.cu
 int density_tt_setup(dftg_ctx *c);
 int launch_density_tt(dftg_ctx *c);

@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
 
 // ---------------------------------------------------------------- launchers
 
-int launch_density(dftg_ctx *c)
+int launch_density(dftg_ctx *c, bool fuse_lda)
 {
     if (!(c->prec_mask & kPrecDensity)) {
         const unsigned nb = (unsigned)(c->npad / 128);
@@ -350,7 +350,7 @@ int launch_density(dftg_ctx *c)
         if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_density<double>), c->device));
         k_density<double><<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi, c->d_P, c->d_rho);
     } else if (c->tc_ready) {
-        DFTG_TRY_L(launch_density_tc(c));
+        DFTG_TRY_L(launch_density_tc(c, fuse_lda));
     } else if (c->dt_ready) {
         DFTG_TRY_L(launch_density_tt(c));
     } else {

@@ -23,6 +23,13 @@
 //   A slices in HBM: [slice][tile][128/8][KP/8][8][8] BF16, one contiguous
 //     128 x KP block per slice and tile, copied with cp.async.bulk;
 //   B slices: [slice][NP/8][KP/8][8][8] BF16 (rows nu, K = mu).
+// With the LDA fused in (the whole-molecule mixed build), the density
+// correction factor cf = sum Z / (2 tr(P S_grid)), S_grid = Phi^T diag(w) Phi,
+// is known before the pass (k_slice_P forms it), so the epilogue finishes each
+// point: rho = cf rho_raw (moleculargrid.cpp:132-146), the Slater + VWN point
+// kernel in double-float (functionals.cpp:24-114), c_xc = w v_xc, and the
+// CTA's sums of w e_xc and w rho_raw; the last CTA adds the CTA sums in order
+// (E_xc and the integrated density, dft.cpp:417).
 // CTA: warp 0 producer (bulk copies), warp 1 TMEM owner + MMA issuer,
 // warps 2-9 epilogue: TMEM lanes 32 (w % 4) ..., the two warps of a lane quarter
 // take alternate 16-column blocks and meet in shared memory per tile.  Persistent over tiles, two
@@ -32,6 +39,7 @@
 #include <cuda_bf16.h>
 #include <cstdint>
 #include "dftg_internal.cuh"
+#include "lda_point.cuh"
 #include "tc_common.cuh"
 
 namespace dftg {
@@ -65,7 +73,9 @@ struct TcShared {
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restrict__ Aslices,
              const int *__restrict__ row_exp, const unsigned char *__restrict__ Bslices,
-             const int *__restrict__ col_exp, double *__restrict__ rho, int *__restrict__ err)
+             const int *__restrict__ col_exp, double *__restrict__ rho, int *__restrict__ err, int fuse,
+             const double *__restrict__ wt, double *__restrict__ scal, double *__restrict__ cxc,
+             float *__restrict__ cxc32, int want64, double *__restrict__ part, int *__restrict__ counter)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const uint32_t a_slice_bytes = (uint32_t)kTcTile * KP * 2;
@@ -77,6 +87,8 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
     __shared__ int s_texp[kTcMaxK];
     __shared__ int s_fail;
     __shared__ float2 s_half[kTcTile];            // (S, E) of the second column half, per row
+    __shared__ float2 s_exc[kTcTile];             // fused LDA: per-row sums of w e_xc (double-float)
+    __shared__ double s_nraw[kTcTile];            // fused LDA: per-row sums of w rho_raw
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -178,6 +190,9 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
         const int half = (warp - 2) >> 2;       // column blocks half, half + 2, ...
         const int r = q * 32 + lane;            // row of the tile = TMEM lane
         const int kc = KP / 8;
+        const double cf = fuse ? scal[kScalScale] : 1.0;
+        dfl exc_acc{0.f, 0.f};
+        double nraw_acc = 0.0;
         for (int it = 0; it < my_tiles; ++it) {
             const int s = it & 1, n = it >> 1;
             bool ok = mbar_wait(&sh->tmem_full[s], (uint32_t)(n & 1));
@@ -253,7 +268,53 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
                 const float bq = w - St;
                 const float e = Et + o.y + (St - (w - bq)) + (o.x - bq);
                 const int ep = row_exp[p];
-                rho[p] = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
+                const double raw = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
+                if (fuse) {
+                    const double wp = wt[p];
+                    nraw_acc += wp * raw;
+                    const double rc = raw * cf;
+                    rho[p] = rc;
+                    dfl ex;
+                    float v;
+                    lda_point_df(df_from(rc), ex, v);
+                    const dfl wd = df_from(wp);
+                    exc_acc = df_add(exc_acc, df_mul(wd, ex));
+                    cxc32[p] = (wd.h + wd.l) * v;
+                    if (want64) cxc[p] = wp * (double)v;
+                } else {
+                    rho[p] = raw;
+                }
+            }
+        }
+        if (fuse) {
+            // CTA sums of the fused point kernel: rows in order, then CTAs in order
+            if (half == 0) {
+                s_exc[r] = make_float2(exc_acc.h, exc_acc.l);
+                s_nraw[r] = nraw_acc;
+            }
+            epi8_bar_sync();
+            if (threadIdx.x == 64) {
+                dfl te{0.f, 0.f};
+                double tn = 0.0;
+                for (int i = 0; i < kTcTile; ++i) {
+                    te = df_add(te, dfl{s_exc[i].x, s_exc[i].y});
+                    tn += s_nraw[i];
+                }
+                part[2 * blockIdx.x] = df_to(te);
+                part[2 * blockIdx.x + 1] = tn;
+                __threadfence();
+                const int t = atomicAdd(counter, 1);
+                if (t == (int)gridDim.x - 1) {
+                    __threadfence();
+                    double se = 0.0, sn = 0.0;
+                    for (int b = 0; b < (int)gridDim.x; ++b) {
+                        se += __ldcg(part + 2 * b);
+                        sn += __ldcg(part + 2 * b + 1);
+                    }
+                    scal[kScalExc] = se;
+                    scal[kScalNelec] = sn * cf;
+                    *counter = 0;
+                }
             }
         }
     }
@@ -305,29 +366,52 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
 }
 
 // P (FP64, nbf x nbf, symmetric) -> 4 pre-scaled integer slices per column in
-// the B layout: one warp per column, lanes over the rows
+// the B layout: one warp per column, lanes over the rows.  With S (S_grid =
+// Phi^T diag(w) Phi, FP64) it also forms the integral of w rho_raw as
+// 2 tr(P S_grid) (warp, block and block-order sums; the last block finishes)
+// and the density correction factor charge / integral (moleculargrid.cpp:132-146).
 __global__ void k_slice_P(int nbf, int KP, int NP, const double *__restrict__ P, __nv_bfloat16 *__restrict__ B,
-                          int *__restrict__ col_exp)
+                          int *__restrict__ col_exp, const double *__restrict__ S, double charge,
+                          double *__restrict__ part, double *__restrict__ scal, int *__restrict__ counter)
 {
+    __shared__ double s_w[32];
+    __shared__ int s_last;
     const int nu = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (nu >= NP) return;
-    double mx = 0.0;
-    if (nu < nbf)
-        for (int mu = lane; mu < nbf; mu += 32) mx = fmax(mx, fabs(P[(size_t)nu * nbf + mu]));
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    int e = 0;
-    if (mx > 0.0) frexp(mx, &e);
-    if (nu < nbf && lane == 0) col_exp[nu] = e;
-    const size_t slice = (size_t)NP * KP;
-    for (int mu = lane; mu < KP; mu += 32) {
-        double x = (nu < nbf && mu < nbf) ? ldexp(P[(size_t)nu * nbf + mu], -e) : 0.0;
-        const size_t o = core_off(nu, mu, KP / 8) / 2;
-        for (int i = 0; i < kTcSlices; ++i) {
-            x *= 256.0;
-            const double m = rint(x);
-            x -= m;
-            B[(size_t)i * slice + o] = __float2bfloat16_rn((float)ldexp(m, -8 * i));
+    double tr = 0.0;
+    if (nu < NP) {
+        double mx = 0.0;
+        if (nu < nbf)
+            for (int mu = lane; mu < nbf; mu += 32) {
+                const double pv = P[(size_t)nu * nbf + mu];
+                mx = fmax(mx, fabs(pv));
+                if (S) tr += pv * S[(size_t)nu * nbf + mu];
+            }
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        int e = 0;
+        if (mx > 0.0) frexp(mx, &e);
+        if (nu < nbf && lane == 0) col_exp[nu] = e;
+        const size_t slice = (size_t)NP * KP;
+        for (int mu = lane; mu < KP; mu += 32) {
+            double x = (nu < nbf && mu < nbf) ? ldexp(P[(size_t)nu * nbf + mu], -e) : 0.0;
+            const size_t o = core_off(nu, mu, KP / 8) / 2;
+            for (int i = 0; i < kTcSlices; ++i) {
+                x *= 256.0;
+                const double m = rint(x);
+                x -= m;
+                B[(size_t)i * slice + o] = __float2bfloat16_rn((float)ldexp(m, -8 * i));
+            }
         }
+    }
+    if (!S) return;                     // block-uniform
+    const double t = block_sum(tr, s_w);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+    if (!last_block(counter, &s_last)) return;
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int b = 0; b < (int)gridDim.x; ++b) sum += __ldcg(part + b);
+        const double total = 2.0 * sum;
+        scal[kScalSum] = total;
+        scal[kScalScale] = charge / total;
     }
 }
 
@@ -364,18 +448,32 @@ int density_tc_setup(dftg_ctx *c)
     c->tc_grid = nsm < ntiles ? nsm : ntiles;
     c->tc_grid_max = c->tc_grid;
     c->tc_ready = true;
+    // S_grid = Phi^T diag(w) Phi in FP64 (the grid overlap), for the correction
+    // factor of the fused density + LDA pass: integral of w rho_raw = 2 tr(P S_grid)
+    if (!c->points_only) {
+        DFTG_CUDA(cudaMalloc(&c->d_Sgrid, sizeof(double) * (size_t)c->nbf * c->nbf));
+        DFTG_TRY_L(launch_contract_coef(c, c->d_w, c->d_Sgrid));
+    }
     return DFTG_OK;
 }
 
-int launch_density_tc(dftg_ctx *c)
+int launch_density_tc(dftg_ctx *c, bool fuse_lda)
 {
+    // the fused LDA needs the correction factor from 2 tr(P S_grid) up front
+    const bool fuse = fuse_lda && c->d_Sgrid;
+    double charge = 0.0;
+    for (int a = 0; a < c->natoms; ++a) charge += (double)c->Z[a];
     k_slice_P<<<(c->tc_NP + 3) / 4, 128, 0, c->stream>>>(c->nbf, c->tc_KP, c->tc_NP, c->d_P,
-                                                         reinterpret_cast<__nv_bfloat16 *>(c->d_tcB), c->d_tc_colexp);
+                                                         reinterpret_cast<__nv_bfloat16 *>(c->d_tcB), c->d_tc_colexp,
+                                                         fuse ? c->d_Sgrid : nullptr, charge, c->d_red, c->d_scal,
+                                                         c->d_counters + kCntAtoms);
     DFTG_LAUNCH_CHECK();
     const int ntiles = (int)(c->npad / kTcTile);
+    const int want64 = (c->prec_mask & kPrecContract) && c->ct_ready ? 0 : 1;
     k_density_tc<<<c->tc_grid, kTcThreads, density_tc_smem(c->tc_KP, c->tc_NP), c->stream>>>(
         c->nbf, c->tc_KP, c->tc_NP, ntiles, reinterpret_cast<const unsigned char *>(c->d_tcA), c->d_tc_rowexp,
-        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag);
+        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag, fuse ? 1 : 0, c->d_w,
+        c->d_scal, c->d_cxc, c->d_cxc32, want64, c->d_red, c->d_counters + kCntLda);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }

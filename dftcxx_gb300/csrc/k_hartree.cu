@@ -419,10 +419,8 @@ __global__ void k_rholm(int nrad, int nang, int nlm, int cell0, const double *__
     }
 }
 
-// K5a (mixed): split-FP32 products (hi*hi + hi*lo + lo*hi), FP32 partial sums of
-// 16 terms added in FP64
 // ------------------------------------------------------------------
-// Double-float GEMM for the mixed multipole steps: C = A B with A (M x K) and
+// Double-float GEMM for the own-cell potential of the mixed multipole step: C = A B with A (M x K) and
 // B (K x N) given as FP32 hi + lo planes (row-major, leading dimensions lda /
 // ldb), every product formed exactly (TwoProd) and accumulated with TwoSum, so
 // C carries ~2^-44 relative error.  Tile 16 x 32 per block of 128 threads, 2 x 2
@@ -485,21 +483,6 @@ __global__ void __launch_bounds__(128) k_dfgemm(int M, int N, int K, const float
         }
 }
 
-// rho_lm[a][lm][i] = 4 pi sum_j (rho w_becke)[a, i, j] (w_leb Y_lm)[j]: rows m = (a - cell0) N + i
-// (the context's points start at cell cell0).
-// K is split in kRholmSlices slices (parallelism); each goes to its own plane and
-// the Poisson kernel adds the planes in order.
-struct EpiRholm {
-    int nrad, nlm, cell0;
-    size_t plane;
-    double *out;
-    __device__ void operator()(int m, int n, int z, dfl v) const
-    {
-        const int a = cell0 + m / nrad, i = m % nrad;
-        out[z * plane + ((size_t)a * nlm + n) * nrad + i] = df_to(v) * (4.0 * kPi);
-    }
-};
-
 // V_own[p] = (1 / r_p) sum_lm U[a][lm][i] Y_lm[j], p = (a N + i) nang + j
 struct EpiVown {
     int nang;
@@ -511,17 +494,6 @@ struct EpiVown {
         Vown[p] = df_to(v) * invr[p];
     }
 };
-
-// rho w_becke split into FP32 hi / lo planes [2][npts]
-__global__ void k_split_rhow(size_t npts, const double *__restrict__ rho, const double *__restrict__ wb,
-                             float *__restrict__ out)
-{
-    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npts) return;
-    const dfl v = df_from(rho[p] * wb[p]);
-    out[p] = v.h;
-    out[npts + p] = v.l;
-}
 
 // K5b: U_lm = G_l rho_lm (+ the l = 0 boundary column times q_a): one block per
 // (atom, lm), one thread per radial point, four partial sums per dot product.
@@ -556,48 +528,6 @@ __global__ void k_poisson(int natoms, int cell0, int nrad, int lmax, const doubl
         const float hi = (float)v;
         U32[(size_t)id * N + i] = hi;
         U32[(size_t)natoms * nlm * N + (size_t)id * N + i] = (float)(v - (double)hi);
-    }
-}
-
-// K5b (mixed): the same map in double-float arithmetic.  maps: the double-float
-// copies laid out as in hartree_setup.
-__global__ void k_poisson_split(int natoms, int cell0, int nrad, int lmax, const float *__restrict__ maps,
-                                const double *__restrict__ rholm, size_t rplane, const double *__restrict__ scal,
-                                double *__restrict__ U, float *__restrict__ U32, float *__restrict__ U32T)
-{
-    extern __shared__ float s_r2[];     // [2][nrad] rho_lm hi, lo
-    const int nlm = (lmax + 1) * (lmax + 1);
-    const int id = blockIdx.x + cell0 * nlm, a = id / nlm, lm = id % nlm, N = nrad;
-    int l = 0;
-    while ((l + 1) * (l + 1) <= lm) ++l;
-    const size_t ng = (size_t)(lmax + 1) * N * N;
-    const float *Gh = maps + (size_t)l * N * N, *Gl = Gh + ng;
-    const float *Gbh = maps + 2 * ng, *Gbl = Gbh + N;
-    for (int k = threadIdx.x; k < N; k += blockDim.x) {     // the two K slices of the projection
-        dfl r = df_from(rholm[(size_t)id * N + k]);
-        for (int z = 1; z < kRholmSlices; ++z) r = df_add(r, df_from(rholm[z * rplane + (size_t)id * N + k]));
-        s_r2[k] = r.h;
-        s_r2[N + k] = r.l;
-    }
-    __syncthreads();
-    const dfl q = lm == 0 ? df_from(scal[kScalAtomQ + a]) : dfl{0.f, 0.f};
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        dfl acc0{0.f, 0.f}, acc1{0.f, 0.f};
-        int k = 0;
-        for (; k + 1 < N; k += 2) {
-            acc0 = df_fma(acc0, dfl{Gh[(size_t)k * N + i], Gl[(size_t)k * N + i]}, dfl{s_r2[k], s_r2[N + k]});
-            acc1 = df_fma(acc1, dfl{Gh[(size_t)(k + 1) * N + i], Gl[(size_t)(k + 1) * N + i]},
-                          dfl{s_r2[k + 1], s_r2[N + k + 1]});
-        }
-        if (k < N) acc0 = df_fma(acc0, dfl{Gh[(size_t)k * N + i], Gl[(size_t)k * N + i]}, dfl{s_r2[k], s_r2[N + k]});
-        dfl v = df_add(acc0, acc1);
-        if (lm == 0) v = df_fma(v, dfl{Gbh[i], Gbl[i]}, q);
-        U[(size_t)id * N + i] = df_to(v);
-        U32[(size_t)id * N + i] = v.h;
-        U32[(size_t)natoms * nlm * N + (size_t)id * N + i] = v.l;
-        // transposed copy [2][(a, i)][lm] for the own-cell GEMM
-        U32T[((size_t)a * N + i) * nlm + lm] = v.h;
-        U32T[(size_t)natoms * nlm * N + ((size_t)a * N + i) * nlm + lm] = v.l;
     }
 }
 
@@ -673,46 +603,142 @@ __global__ void k_splines(int natoms, int cell0, int nrad, int nlm, const double
     }
 }
 
-// K5d (mixed): the same spline fit in double-float arithmetic from the split U;
-// the FP64 table is written only when want64 (an FP64 cross-atom step follows).
-__global__ void k_splines_split(int natoms, int cell0, int nrad, int nlm, int lmax, const float *__restrict__ maps,
-                                const float *__restrict__ U32, int want64, double *__restrict__ spl,
-                                float *__restrict__ splm)
+// K5a-d (mixed, one launch): the multipole chain of one atom cell for a group
+// of kMpLG (l, m) rows per CTA: rho_lm (atomicgrid.cpp:241-296), the radial
+// Poisson map with the l = 0 boundary value sqrt(4 pi) q_a (atomicgrid.cpp:
+// 301-432), and the spline fit of U_lm (atomicgrid.cpp:535-556), all in
+// double-float arithmetic with exact products.  The CTA stages the cell's
+// rho w_becke shell by shell (kMpSC shells per pass) and each thread forms one
+// rho_lm(i) as a 302-term dot product against the group's w_leb Y_lm rows, so
+// nothing is reduced across threads; the Poisson and spline maps are read from
+// L2 once per (l, m) row.  The CTA holding lm = 0 also sums q_a = sum w rho
+// over the cell (FP64, fixed order) for the boundary value.
+// Writes U (FP64 and split FP32, both radial orders) and the spline tables.
+constexpr int kMpLG = 7;          // (l, m) rows per CTA
+constexpr int kMpSC = 32;         // radial shells staged per pass
+constexpr int kMpThreads = 256;
+
+size_t multipole_smem(int nrad, int nang)
 {
-    extern __shared__ float s_y2[];    // y hi [n], y lo [n], D hi [n], D lo [n]
-    const int id = blockIdx.x + cell0 * nlm, n = nrad;
-    const size_t ng = (size_t)(lmax + 1) * n * n;
-    const float *Kh = maps + 2 * ng + 2 * (size_t)n, *Kl = Kh + (size_t)n * n;
-    const float *ih = Kl + (size_t)n * n, *il = ih + n;
-    const float *fh = il + n, *fl = fh + nlm;
-    const size_t uhalf = (size_t)natoms * nlm * n;
-    float *yh = s_y2, *yl = s_y2 + n, *Dh = s_y2 + 2 * n, *Dl = s_y2 + 3 * n;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {   // increasing r: reverse the radial order
-        yh[i] = U32[(size_t)id * n + n - 1 - i];
-        yl[i] = U32[uhalf + (size_t)id * n + n - 1 - i];
+    const size_t row = (size_t)(nang | 1);                  // odd row length: no bank aliasing across shells
+    return sizeof(dfl) * ((size_t)kMpSC * row + (size_t)kMpLG * nang + 3 * (size_t)kMpLG * nrad) + 64 * sizeof(double);
+}
+
+__global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0, int N, int nang, int lmax, int ngroup,
+                                                          const double *__restrict__ rho, const double *__restrict__ wb,
+                                                          const double *__restrict__ w, const float *__restrict__ Ywt32,
+                                                          const float *__restrict__ maps, double *__restrict__ scal,
+                                                          double *__restrict__ U, float *__restrict__ U32,
+                                                          float *__restrict__ U32T, int want64,
+                                                          double *__restrict__ spl, float *__restrict__ splm)
+{
+    extern __shared__ __align__(16) unsigned char mp_smem[];
+    const int nlm = (lmax + 1) * (lmax + 1);
+    const int row = nang | 1;
+    dfl *sRW = reinterpret_cast<dfl *>(mp_smem);                 // [kMpSC][row] rho w_becke
+    dfl *sY = sRW + (size_t)kMpSC * row;                         // [kMpLG][nang] w_leb Y_lm
+    dfl *sR = sY + (size_t)kMpLG * nang;                         // [kMpLG][N] rho_lm
+    dfl *sU = sR + (size_t)kMpLG * N;                            // [kMpLG][N] U_lm
+    dfl *sD = sU + (size_t)kMpLG * N;                            // [kMpLG][N] spline derivatives
+    double *sred = reinterpret_cast<double *>(sD + (size_t)kMpLG * N);
+    const int tid = threadIdx.x;
+    const int al = blockIdx.x / ngroup, g = blockIdx.x % ngroup, a = cell0 + al;
+    const int lm0 = g * kMpLG, nl = min(kMpLG, nlm - lm0);
+    const size_t base = (size_t)al * N * nang;
+    const size_t uhalf = (size_t)natoms * nlm * N;
+    for (int e = tid; e < nl * nang; e += kMpThreads) {
+        const int r = e / nang, j = e % nang;
+        sY[e] = dfl{Ywt32[(size_t)j * nlm + lm0 + r], Ywt32[(size_t)nang * nlm + (size_t)j * nlm + lm0 + r]};
+    }
+    // q_a for the boundary row of lm = 0
+    double q = 0.0;
+    if (lm0 == 0) {
+        double t = 0.0;
+        for (int e = tid; e < N * nang; e += kMpThreads) t += w[base + e] * rho[base + e];
+        q = block_sum(t, sred);
+        if (tid == 0) {
+            sred[32] = q;
+            scal[kScalAtomQ + a] = q;
+        }
+    }
+    const dfl four_pi = df_from(4.0 * kPi);
+    for (int i0 = 0; i0 < N; i0 += kMpSC) {
+        const int ns = min(kMpSC, N - i0);
+        __syncthreads();                                          // the previous pass is done with sRW
+        for (int e = tid; e < ns * nang; e += kMpThreads) {
+            const int ii = e / nang, j = e % nang;
+            const size_t p = base + (size_t)(i0 + ii) * nang + j;
+            sRW[(size_t)ii * row + j] = df_from(rho[p] * wb[p]);
+        }
+        __syncthreads();
+        for (int o = tid; o < nl * ns; o += kMpThreads) {
+            const int r = o % nl, ii = o / nl;
+            const dfl *x = sRW + (size_t)ii * row, *y = sY + (size_t)r * nang;
+            float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f;
+            int j = 0;
+            for (; j + 1 < nang; j += 2) {
+                const dfl x0 = x[j], y0 = y[j], x1 = x[j + 1], y1 = y[j + 1];
+                df_mac(s0, e0, x0.h, x0.l, y0.h, y0.l);
+                df_mac(s1, e1, x1.h, x1.l, y1.h, y1.l);
+            }
+            if (j < nang) df_mac(s0, e0, x[j].h, x[j].l, y[j].h, y[j].l);
+            sR[r * N + i0 + ii] = df_mul(df_add(df_norm(s0, e0), df_norm(s1, e1)), four_pi);
+        }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    if (lm0 == 0) q = sred[32];
+    // Poisson: U = G_l rho_lm (+ Gb q for lm = 0)
+    const size_t ng = (size_t)(lmax + 1) * N * N;
+    const float *Gbh = maps + 2 * ng, *Gbl = Gbh + N;
+    for (int o = tid; o < nl * N; o += kMpThreads) {
+        const int r = o / N, i = o % N, lm = lm0 + r;
+        int l = 0;
+        while ((l + 1) * (l + 1) <= lm) ++l;
+        const float *Gh = maps + (size_t)l * N * N, *Gl = Gh + ng;
+        const dfl *R = sR + r * N;
+        dfl acc0{0.f, 0.f}, acc1{0.f, 0.f};
+        int k = 0;
+        for (; k + 1 < N; k += 2) {
+            acc0 = df_fma(acc0, dfl{Gh[(size_t)k * N + i], Gl[(size_t)k * N + i]}, R[k]);
+            acc1 = df_fma(acc1, dfl{Gh[(size_t)(k + 1) * N + i], Gl[(size_t)(k + 1) * N + i]}, R[k + 1]);
+        }
+        if (k < N) acc0 = df_fma(acc0, dfl{Gh[(size_t)k * N + i], Gl[(size_t)k * N + i]}, R[k]);
+        dfl v = df_add(acc0, acc1);
+        if (lm == 0) v = df_fma(v, dfl{Gbh[i], Gbl[i]}, df_from(q));
+        sU[r * N + i] = v;
+        const size_t id = (size_t)a * nlm + lm;
+        U[id * N + i] = df_to(v);
+        U32[id * N + i] = v.h;
+        U32[uhalf + id * N + i] = v.l;
+        U32T[((size_t)a * N + i) * nlm + lm] = v.h;
+        U32T[uhalf + ((size_t)a * N + i) * nlm + lm] = v.l;
+    }
+    __syncthreads();
+    // spline derivatives over increasing r: D = K y, y[i] = U[N - 1 - i]
+    const float *Kh = maps + 2 * ng + 2 * (size_t)N, *Kl = Kh + (size_t)N * N;
+    const float *ih = Kl + (size_t)N * N, *il = ih + N;
+    const float *fh = il + N, *fl = fh + nlm;
+    for (int o = tid; o < nl * N; o += kMpThreads) {
+        const int r = o / N, i = o % N;
+        const dfl *u = sU + r * N;
         dfl a0{0.f, 0.f}, a1{0.f, 0.f};
         int j = 0;
-        for (; j + 1 < n; j += 2) {
-            a0 = df_fma(a0, dfl{Kh[(size_t)j * n + i], Kl[(size_t)j * n + i]}, dfl{yh[j], yl[j]});
-            a1 = df_fma(a1, dfl{Kh[(size_t)(j + 1) * n + i], Kl[(size_t)(j + 1) * n + i]}, dfl{yh[j + 1], yl[j + 1]});
+        for (; j + 1 < N; j += 2) {
+            a0 = df_fma(a0, dfl{Kh[(size_t)j * N + i], Kl[(size_t)j * N + i]}, u[N - 1 - j]);
+            a1 = df_fma(a1, dfl{Kh[(size_t)(j + 1) * N + i], Kl[(size_t)(j + 1) * N + i]}, u[N - 2 - j]);
         }
-        if (j < n) a0 = df_fma(a0, dfl{Kh[(size_t)j * n + i], Kl[(size_t)j * n + i]}, dfl{yh[j], yl[j]});
-        const dfl d = df_add(a0, a1);
-        Dh[i] = d.h;
-        Dl[i] = d.l;
+        if (j < N) a0 = df_fma(a0, dfl{Kh[(size_t)j * N + i], Kl[(size_t)j * N + i]}, u[N - 1 - j]);
+        sD[r * N + i] = df_add(a0, a1);
     }
     __syncthreads();
-    const int lm = id % nlm;
-    const dfl F{fh[lm], fl[lm]};
-    float *o32 = splm + (size_t)id * n * 8;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int o = tid; o < nl * N; o += kMpThreads) {
+        const int r = o / N, i = o % N, lm = lm0 + r;
+        const dfl *u = sU + r * N, *D = sD + r * N;
+        const dfl F{fh[lm], fl[lm]};
         dfl cc[4];
-        if (i < n - 1) {
-            const dfl dx{ih[i], il[i]}, y0{yh[i], yl[i]}, y1{yh[i + 1], yl[i + 1]};
-            const dfl D0{Dh[i], Dl[i]}, D1{Dh[i + 1], Dl[i + 1]};
+        if (i < N - 1) {
+            const dfl dx{ih[i], il[i]}, y0 = u[N - 1 - i], y1 = u[N - 2 - i];
+            const dfl D0 = D[i], D1 = D[i + 1];
             const dfl dy = df_mul(df_sub(y1, y0), dx);
             const dfl three{3.f, 0.f}, two{2.f, 0.f};
             cc[0] = y0;
@@ -720,14 +746,16 @@ __global__ void k_splines_split(int natoms, int cell0, int nrad, int nlm, int lm
             cc[2] = df_mul(dx, df_sub(df_sub(df_mul(three, dy), df_mul(two, D0)), D1));
             cc[3] = df_mul(df_mul(dx, dx), df_add(df_add(df_mul(dfl{-2.f, 0.f}, dy), D0), D1));
         } else {                     // clamp value of the last knot
-            cc[0] = dfl{yh[n - 1], yl[n - 1]};
+            cc[0] = u[0];
             cc[1] = cc[2] = cc[3] = dfl{0.f, 0.f};
         }
+        const size_t id = (size_t)a * nlm + lm;
+        float *o32 = splm + (id * N + i) * 8;
         for (int k = 0; k < 4; ++k) {
             const dfl v = df_mul(F, cc[k]);
-            o32[8 * i + k] = v.h;
-            o32[8 * i + 4 + k] = v.l;
-            if (want64) spl[((size_t)id * n + i) * 4 + k] = df_to(cc[k]);
+            o32[k] = v.h;
+            o32[4 + k] = v.l;
+            if (want64) spl[(id * N + i) * 4 + k] = df_to(cc[k]);
         }
     }
 }
@@ -957,6 +985,60 @@ __global__ void k_vcross_gather(size_t npts, size_t npad, int natoms, int cell0,
     cj32[p] = (float)c;
 }
 
+// K5c+K5e+E_J (mixed, one launch): per point the own-cell potential
+// V_own = (1 / r) sum_lm U_lm(r_i) Y_lm(j) in double-float with exact products
+// (the products and order of the own-cell GEMM), plus the pair contributions
+// in atom order summed with TwoSum; writes V and cj = w V / 2, and sums
+// E_J = sum_p cj rho_raw: block partials, the last block adds them in order.
+__global__ void __launch_bounds__(128) k_vcross_gather_own(size_t npts, size_t npad, int natoms, int cell0, int nrad,
+                                                           int nang, int nlm, const int *__restrict__ pos,
+                                                           const float2 *__restrict__ pairv,
+                                                           const float *__restrict__ U32T, size_t uhalf,
+                                                           const float *__restrict__ Y32, const double *__restrict__ invr,
+                                                           const double *__restrict__ W, const double *__restrict__ rho,
+                                                           int scaled, double *__restrict__ V, double *__restrict__ cj,
+                                                           float *__restrict__ cj32, double *__restrict__ part,
+                                                           double *scal, int *counter)
+{
+    __shared__ double sh[32];
+    __shared__ int s_last;
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double ej = 0.0;
+    if (p < npts) {
+        const int per = nrad * nang;
+        const int al = (int)(p / per), rem = (int)(p % per), i = rem / nang, j = rem % nang, a = cell0 + al;
+        const float *uh = U32T + ((size_t)a * nrad + i) * nlm, *ul = uh + uhalf;
+        const float *yh = Y32 + j, *yl = Y32 + (size_t)nlm * nang + j;
+        float s = 0.f, e = 0.f;
+        for (int lm = 0; lm < nlm; ++lm) df_mac(s, e, uh[lm], ul[lm], yh[(size_t)lm * nang], yl[(size_t)lm * nang]);
+        const double vown = df_to(df_norm(s, e)) * invr[p];
+        float vh = 0.f, vl = 0.f;
+        for (int k = 0; k < natoms; ++k) {
+            if (k == a) continue;
+            const float2 v = pairv[pos[p * natoms + k]];
+            two_sum_acc(vh, vl, v.x);
+            vl += v.y;
+        }
+        const double Vt = vown + ((double)vh + (double)vl);
+        V[p] = Vt;
+        const double c = 0.5 * (W[p] * Vt);
+        cj[p] = c;
+        cj32[p] = (float)c;
+        ej = c * rho[p];
+    } else if (p < npad) {
+        V[p] = 0.0;
+        cj[p] = 0.0;
+        cj32[p] = 0.f;
+    }
+    ej = block_sum(ej, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = ej;
+    if (!last_block(counter, &s_last)) return;
+    double t = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) t += __ldcg(part + b);
+    t = block_sum(t, sh);
+    if (threadIdx.x == 0) scal[kScalEJ] = scaled ? t / scal[kScalScale] : t;
+}
+
 // Order the (point, other atom) pairs by (atom, spline interval of their
 // distance), stably in the enumeration order (point, then atom): pos[p][k] is
 // the place of pair (p, k).  On the device: the pairs' keys (FP64 distance,
@@ -1162,51 +1244,45 @@ int launch_hartree_multipoles(dftg_ctx *c)
     // memory: up to 256 radial points (the FP64 kernels take any)
     const bool mp = (c->prec_mask & kPrecMultipole) != 0 && N <= 256;
     const size_t rplane = (size_t)c->natoms * nlm * N;
+    const int nrhs = nc * nlm;
     if (mp) {
-        // rho_lm as a double-float GEMM [(a, i) x j] x [j x lm], K split in planes
-        float *S32 = reinterpret_cast<float *>(c->d_red2);
-        k_split_rhow<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, c->d_rho, c->d_wb, S32);
+        // rho_lm, Poisson and splines in one launch per (cell, group of l, m rows)
+        const int ngroup = (nlm + kMpLG - 1) / kMpLG;
+        const size_t sm = multipole_smem(N, c->nang);
+        if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_multipole), c->device));
+        k_multipole<<<(unsigned)(nc * ngroup), kMpThreads, sm, c->stream>>>(
+            c->natoms, c0, N, c->nang, c->lmax, ngroup, c->d_rho, c->d_wb, c->d_w, c->d_Ywt32, c->d_maps32, c->d_scal,
+            c->d_U, c->d_U32, c->d_U32T, (c->prec_mask & kPrecCross) ? 0 : 1, c->d_spl, c->d_splm);
         DFTG_LAUNCH_CHECK();
-        const int M = nc * N;
-        dim3 grid((unsigned)((nlm + kDgBN - 1) / kDgBN), (unsigned)((M + kDgBM - 1) / kDgBM), kRholmSlices);
-        k_dfgemm<EpiRholm><<<grid, 128, 0, c->stream>>>(M, nlm, c->nang, S32, S32 + c->npts, c->nang, c->d_Ywt32,
-                                                        c->d_Ywt32 + (size_t)nlm * c->nang, nlm,
-                                                        EpiRholm{N, nlm, c0, rplane, c->d_rholm});
-    } else
-        k_rholm<<<nc * N, 96, sizeof(double) * c->nang, c->stream>>>(N, c->nang, nlm, c0, c->d_rho, c->d_wb, c->d_Yw,
-                                                                    c->d_rholm);
+        DFTG_MARK(c, "multipole");
+        if (!(c->prec_mask & kPrecCross)) {
+            // the FP64 cross-atom step takes the own-cell potential from memory:
+            // a double-float GEMM [(a, i) x lm] x [lm x j]
+            const int M = nc * N;
+            const size_t off = (size_t)c0 * N * nlm;
+            dim3 grid((unsigned)((c->nang + kDgBN - 1) / kDgBN), (unsigned)((M + kDgBM - 1) / kDgBM), 1);
+            k_dfgemm<EpiVown><<<grid, 128, 0, c->stream>>>(M, c->nang, nlm, c->d_U32T + off, c->d_U32T + rplane + off,
+                                                           nlm, c->d_Y32, c->d_Y32 + (size_t)nlm * c->nang, c->nang,
+                                                           EpiVown{c->nang, c->d_invr, c->d_Vown});
+            DFTG_LAUNCH_CHECK();
+            DFTG_MARK(c, "vown");
+        }
+        return DFTG_OK;
+    }
+    k_rholm<<<nc * N, 96, sizeof(double) * c->nang, c->stream>>>(N, c->nang, nlm, c0, c->d_rho, c->d_wb, c->d_Yw,
+                                                                c->d_rholm);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "rholm");
-    const int nrhs = nc * nlm;
-    if (mp)
-        k_poisson_split<<<nrhs, 128, sizeof(float) * 2 * N, c->stream>>>(c->natoms, c0, N, c->lmax, c->d_maps32,
-                                                                         c->d_rholm, rplane, c->d_scal, c->d_U,
-                                                                         c->d_U32, c->d_U32T);
-    else
-        k_poisson<<<nrhs, 128, sizeof(double) * N, c->stream>>>(c->natoms, c0, N, c->lmax, c->d_Gt, c->d_Gb,
-                                                                c->d_rholm, c->d_scal, c->d_U, c->d_U32);
+    k_poisson<<<nrhs, 128, sizeof(double) * N, c->stream>>>(c->natoms, c0, N, c->lmax, c->d_Gt, c->d_Gb, c->d_rholm,
+                                                            c->d_scal, c->d_U, c->d_U32);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "poisson");
     const unsigned npb = (unsigned)((c->npts + 127) / 128);
-    if (mp) {
-        // own-cell potential as a double-float GEMM [(a, i) x lm] x [lm x j]
-        const int M = nc * N;
-        const size_t off = (size_t)c0 * N * nlm;
-        dim3 grid((unsigned)((c->nang + kDgBN - 1) / kDgBN), (unsigned)((M + kDgBM - 1) / kDgBM), 1);
-        k_dfgemm<EpiVown><<<grid, 128, 0, c->stream>>>(M, c->nang, nlm, c->d_U32T + off, c->d_U32T + rplane + off, nlm,
-                                                       c->d_Y32, c->d_Y32 + (size_t)nlm * c->nang, c->nang,
-                                                       EpiVown{c->nang, c->d_invr, c->d_Vown});
-    } else
-        k_vown<<<npb, 128, 0, c->stream>>>(c->npts, N, c->nang, nlm, c0, c->d_rn, c->d_leb, c->d_Y, c->d_U, c->d_Vown);
+    k_vown<<<npb, 128, 0, c->stream>>>(c->npts, N, c->nang, nlm, c0, c->d_rn, c->d_leb, c->d_Y, c->d_U, c->d_Vown);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "vown");
-    if (mp)
-        k_splines_split<<<nrhs, 128, sizeof(float) * 4 * N, c->stream>>>(
-            c->natoms, c0, N, nlm, c->lmax, c->d_maps32, c->d_U32, (c->prec_mask & kPrecCross) ? 0 : 1, c->d_spl,
-            c->d_splm);
-    else
-        k_splines<<<nrhs, 128, sizeof(double) * 2 * N, c->stream>>>(c->natoms, c0, N, nlm, c->d_splf, c->d_Kt, c->d_U,
-                                                                    c->d_fold, c->d_spl, c->d_splm);
+    k_splines<<<nrhs, 128, sizeof(double) * 2 * N, c->stream>>>(c->natoms, c0, N, nlm, c->d_splf, c->d_Kt, c->d_U,
+                                                                c->d_fold, c->d_spl, c->d_splm);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "splines");
     return DFTG_OK;
@@ -1217,10 +1293,22 @@ int launch_hartree_multipoles(dftg_ctx *c)
 int launch_hartree_cross(dftg_ctx *c)
 {
     const int N = c->nrad;
+    const bool mp = (c->prec_mask & kPrecMultipole) != 0 && N <= 256;
     const unsigned nb = (unsigned)(c->npad / 128);
     if (c->prec_mask & kPrecCross) {
         if (c->npairs > 0) {
             DFTG_TRY_L(launch_vcross_bins(c));
+        }
+        if (mp) {
+            // own-cell potential, total potential and E_J in one pass
+            const size_t uhalf = (size_t)c->natoms * c->nlm * N;
+            k_vcross_gather_own<<<(unsigned)((c->npad + 255) / 256), 256, 0, c->stream>>>(
+                c->npts, c->npad, c->natoms, c->cell0, N, c->nang, c->nlm, c->d_pairpos,
+                reinterpret_cast<const float2 *>(c->d_pairv), c->d_U32T, uhalf, c->d_Y32, c->d_invr, c->d_w, c->d_rho,
+                c->rho_scaled ? 1 : 0, c->d_V, c->d_cj, c->d_cj32, c->d_red, c->d_scal, c->d_counters + kCntEJ);
+            DFTG_LAUNCH_CHECK();
+            DFTG_MARK(c, "vcross");
+            return DFTG_OK;
         }
         k_vcross_gather<<<(unsigned)((c->npad + 127) / 128), 128, 0, c->stream>>>(
             c->npts, c->npad, c->natoms, c->cell0, N, c->nang, c->d_pairpos, reinterpret_cast<const float2 *>(c->d_pairv),
