@@ -990,7 +990,7 @@ __global__ void k_vcross_gather(size_t npts, size_t npad, int natoms, int cell0,
 // (the products and order of the own-cell GEMM), plus the pair contributions
 // in atom order summed with TwoSum; writes V and cj = w V / 2, and sums
 // E_J = sum_p cj rho_raw: block partials, the last block adds them in order.
-__global__ void __launch_bounds__(128) k_vcross_gather_own(size_t npts, size_t npad, int natoms, int cell0, int nrad,
+__global__ void __launch_bounds__(256) k_vcross_gather_own(size_t npts, size_t npad, int natoms, int cell0, int nrad,
                                                            int nang, int nlm, const int *__restrict__ pos,
                                                            const float2 *__restrict__ pairv,
                                                            const float *__restrict__ U32T, size_t uhalf,
