@@ -23,6 +23,7 @@ constexpr double kPiTrunc = 3.14159265359;          // cgf.cpp:103, integrals.cp
 constexpr int kLmaxCap = 16;
 constexpr int kMaxAtoms = 256;
 constexpr int kPtsAlign = 128;
+constexpr int kMaxRedCtas = 1024;    // CTAs of a persistent kernel that writes per-CTA reduction partials
 
 void set_error(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
@@ -212,7 +213,9 @@ struct dftg_ctx {
     void *d_tcB = nullptr;        // [4][NP x KP] BF16 slices of P
     int *d_tc_rowexp = nullptr;   // [npad] per-point scale exponents
     int *d_tc_colexp = nullptr;   // [NP] per-column scale exponents of P
-    double *d_Sgrid = nullptr;    // [nbf][nbf] Phi^T diag(w) Phi (FP64), for the fused density + LDA pass
+    double *d_Sgrid = nullptr;    // [nbf][nbf] Phi^T diag(w) Phi (FP64): correction factor from 2 tr(P S_grid)
+    float *d_rw32 = nullptr;      // [2][npad] rho w_becke split into FP32 hi, lo (mixed multipole input)
+    bool rw_ready = false;        // d_rw32 holds the current corrected rho (written by the point kernel)
     int *d_flag = nullptr;        // device error flag (bounded waits that expired)
 
     // device: tensor-core density for 81 <= nbf <= 1024 (128-point tiles x 128-column blocks)
@@ -327,16 +330,16 @@ int mark(dftg_ctx *c, const char *name);
 int launch_grid(dftg_ctx *c);
 int launch_amplitudes(dftg_ctx *c);
 // k_density.cu
-int launch_density(dftg_ctx *c, bool fuse_lda = false);
+int launch_density(dftg_ctx *c, bool with_scale = false);
 enum { kSumsOnly = 0, kSumsCorrect = 1, kSumsFactor = 2 };
 // k_density_tc.cu
 int density_tc_setup(dftg_ctx *c);
-int launch_density_tc(dftg_ctx *c, bool fuse_lda);
+int launch_density_tc(dftg_ctx *c, bool with_scale);
 // k_density_tt.cu
 int density_tt_setup(dftg_ctx *c);
 int launch_density_tt(dftg_ctx *c);
 int launch_atom_sums(dftg_ctx *c, int mode);
-int launch_xc_points(dftg_ctx *c, bool apply_scale);
+int launch_xc_points(dftg_ctx *c, bool apply_scale, bool with_n = false);
 // k_hartree.cu
 int hartree_setup(dftg_ctx *c);
 int cross_pairs_setup(dftg_ctx *c);

@@ -264,12 +264,19 @@ __global__ void k_scale(size_t npts, const double *__restrict__ scal, double *rh
 
 // ---------------------------------------------------------------- LDA
 
+// Slater + VWN point kernel (functionals.cpp:24-114) with the density
+// correction applied first when apply_scale (moleculargrid.cpp:132-146), E_xc
+// summed per block and then over the blocks in order by the last one.  The
+// mixed form with want_n also sums the integral of the corrected rho (the
+// build's N, dft.cpp:111) and, with rw32, writes rho w_becke split into FP32
+// hi / lo planes [2][npad] for the multipole kernel.
 template <bool MIXED>
 __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restrict__ rho,
                                                    const double *__restrict__ w, double *__restrict__ scal,
                                                    int apply_scale, double *__restrict__ cxc,
                                                    float *__restrict__ cxc32, double *__restrict__ part, int *counter,
-                                                   int want64)
+                                                   int want64, int want_n, const double *__restrict__ wb,
+                                                   float *__restrict__ rw32)
 {
     __shared__ double sh[32];
     __shared__ float shf[2][32];
@@ -280,6 +287,7 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
         // double-float point kernel and block sum; FP64 only for the density
         // correction, the weight split and the block partial
         dfl ewd{0.f, 0.f};
+        double wr = 0.0;
         if (p < npad) {
             double r = rho[p];
             if (apply_scale) {
@@ -289,11 +297,18 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
             dfl e;
             float v;
             lda_point_df(df_from(r), e, v);
-            const dfl wd = df_from(w[p]);
+            const double wp = w[p];
+            const dfl wd = df_from(wp);
             ewd = df_mul(wd, e);
             const float c32 = (wd.h + wd.l) * v;
             cxc32[p] = c32;
-            if (want64) cxc[p] = w[p] * (double)v;
+            if (want64) cxc[p] = wp * (double)v;
+            wr = wp * r;
+            if (rw32) {
+                const dfl x = df_from(r * wb[p]);
+                rw32[p] = x.h;
+                rw32[npad + p] = x.l;
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
@@ -302,17 +317,26 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
             shf[0][threadIdx.x >> 5] = ewd.h;
             shf[1][threadIdx.x >> 5] = ewd.l;
         }
-        __syncthreads();
+        const double wrs = want_n ? block_sum(wr, sh) : 0.0;   // block-uniform; synchronises the posts above
+        if (!want_n) __syncthreads();
         if (threadIdx.x == 0) {
             dfl t{0.f, 0.f};
             for (int i = 0; i < kRedBlock / 32; ++i) t = df_add(t, dfl{shf[0][i], shf[1][i]});
             part[blockIdx.x] = df_to(t);
+            if (want_n) part[gridDim.x + blockIdx.x] = wrs;
         }
         if (!last_block(counter, &s_last)) return;
-        double t = 0.0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += kRedBlock) t += __ldcg(part + i);
+        double t = 0.0, tn = 0.0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += kRedBlock) {
+            t += __ldcg(part + i);
+            if (want_n) tn += __ldcg(part + gridDim.x + i);
+        }
         t = block_sum(t, sh);
-        if (threadIdx.x == 0) scal[kScalExc] = t;
+        if (want_n) tn = block_sum(tn, sh);
+        if (threadIdx.x == 0) {
+            scal[kScalExc] = t;
+            if (want_n) scal[kScalNelec] = tn;
+        }
         return;
     }
     if (p < npad) {
@@ -342,15 +366,16 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
 
 // ---------------------------------------------------------------- launchers
 
-int launch_density(dftg_ctx *c, bool fuse_lda)
+int launch_density(dftg_ctx *c, bool with_scale)
 {
+    c->rw_ready = false;             // a new density: the rho w_becke planes are stale
     if (!(c->prec_mask & kPrecDensity)) {
         const unsigned nb = (unsigned)(c->npad / 128);
         const size_t sm = (size_t)c->nbf * 32 * sizeof(double);
         if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_density<double>), c->device));
         k_density<double><<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi, c->d_P, c->d_rho);
     } else if (c->tc_ready) {
-        DFTG_TRY_L(launch_density_tc(c, fuse_lda));
+        DFTG_TRY_L(launch_density_tc(c, with_scale));
     } else if (c->dt_ready) {
         DFTG_TRY_L(launch_density_tt(c));
     } else {
@@ -382,6 +407,7 @@ int launch_atom_sums(dftg_ctx *c, int mode)
                                                  c->d_scal, mode == kSumsOnly ? 1 : 0, cnt);
     DFTG_LAUNCH_CHECK();
     if (mode == kSumsCorrect) {
+        c->rw_ready = false;         // rho is rescaled below
         k_scale<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, c->d_scal, c->d_rho);
         DFTG_LAUNCH_CHECK();
         k_atom_sums<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, ncell, c->d_w, c->d_rho, c->d_red, c->d_atoms,
@@ -392,28 +418,41 @@ int launch_atom_sums(dftg_ctx *c, int mode)
     return DFTG_OK;
 }
 
-int launch_xc_points(dftg_ctx *c, bool apply_scale)
+int launch_xc_points(dftg_ctx *c, bool apply_scale, bool with_n)
 {
     const unsigned nb = (unsigned)((c->npad + kRedBlock - 1) / kRedBlock);
     const int sc = apply_scale ? 1 : 0;
+    if (2 * (size_t)nb > c->red_elems) { set_error("reduction buffer too small for %u blocks", nb); return DFTG_ERR_STATE; }
+    // with_n: the build's N from the corrected rho (no per-atom sums ran), and
+    // the rho w_becke planes for the mixed multipole kernel
+    const int wn = with_n ? 1 : 0;
+    float *rw32 = (with_n && c->d_rw32 && (c->prec_mask & kPrecMultipole)) ? c->d_rw32 : nullptr;
+    c->rw_ready = rw32 != nullptr;
     if (c->prec_mask & kPrecLda)
         k_lda<true><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_scal, sc, c->d_cxc, c->d_cxc32,
                                                      c->d_red, c->d_counters + kCntLda,
-                                                     (c->prec_mask & kPrecContract) && c->ct_ready ? 0 : 1);
+                                                     (c->prec_mask & kPrecContract) && c->ct_ready ? 0 : 1, wn,
+                                                     c->d_wb, rw32);
     else
         k_lda<false><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_scal, sc, c->d_cxc,
-                                                      c->d_cxc32, c->d_red, c->d_counters + kCntLda, 1);
+                                                      c->d_cxc32, c->d_red, c->d_counters + kCntLda, 1, 0, nullptr,
+                                                      nullptr);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "lda");
     return DFTG_OK;
 }
 
+// partials of the block reductions: two per 256-point block (LDA: E_xc and N;
+// E_J: one), one per
+// stage-1 chunk of the per-atom sums, two per CTA of the fused density + LDA
+// pass (at most one CTA per SM; kMaxRedCtas bounds the SM count)
 size_t reduction_elems(size_t npad, int natoms, int nrad, int nang)
 {
     size_t a = (npad + kRedBlock - 1) / kRedBlock;
     size_t per_atom = (size_t)nrad * nang;
     size_t b = (size_t)natoms * ((per_atom + kRedChunk - 1) / kRedChunk);
-    return a > b ? a : b;
+    size_t m = 2 * a > b ? 2 * a : b;      // two partials per block in the point kernel
+    return m > 2 * (size_t)kMaxRedCtas ? m : 2 * (size_t)kMaxRedCtas;
 }
 
 }  // namespace dftg

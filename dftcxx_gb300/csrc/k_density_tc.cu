@@ -23,13 +23,6 @@
 //   A slices in HBM: [slice][tile][128/8][KP/8][8][8] BF16, one contiguous
 //     128 x KP block per slice and tile, copied with cp.async.bulk;
 //   B slices: [slice][NP/8][KP/8][8][8] BF16 (rows nu, K = mu).
-// With the LDA fused in (the whole-molecule mixed build), the density
-// correction factor cf = sum Z / (2 tr(P S_grid)), S_grid = Phi^T diag(w) Phi,
-// is known before the pass (k_slice_P forms it), so the epilogue finishes each
-// point: rho = cf rho_raw (moleculargrid.cpp:132-146), the Slater + VWN point
-// kernel in double-float (functionals.cpp:24-114), c_xc = w v_xc, and the
-// CTA's sums of w e_xc and w rho_raw; the last CTA adds the CTA sums in order
-// (E_xc and the integrated density, dft.cpp:417).
 // CTA: warp 0 producer (bulk copies), warp 1 TMEM owner + MMA issuer,
 // warps 2-9 epilogue: TMEM lanes 32 (w % 4) ..., the two warps of a lane quarter
 // take alternate 16-column blocks and meet in shared memory per tile.  Persistent over tiles, two
@@ -39,7 +32,6 @@
 #include <cuda_bf16.h>
 #include <cstdint>
 #include "dftg_internal.cuh"
-#include "lda_point.cuh"
 #include "tc_common.cuh"
 
 namespace dftg {
@@ -73,9 +65,7 @@ struct TcShared {
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restrict__ Aslices,
              const int *__restrict__ row_exp, const unsigned char *__restrict__ Bslices,
-             const int *__restrict__ col_exp, double *__restrict__ rho, int *__restrict__ err, int fuse,
-             const double *__restrict__ wt, double *__restrict__ scal, double *__restrict__ cxc,
-             float *__restrict__ cxc32, int want64, double *__restrict__ part, int *__restrict__ counter)
+             const int *__restrict__ col_exp, double *__restrict__ rho, int *__restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const uint32_t a_slice_bytes = (uint32_t)kTcTile * KP * 2;
@@ -87,8 +77,6 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
     __shared__ int s_texp[kTcMaxK];
     __shared__ int s_fail;
     __shared__ float2 s_half[kTcTile];            // (S, E) of the second column half, per row
-    __shared__ float2 s_exc[kTcTile];             // fused LDA: per-row sums of w e_xc (double-float)
-    __shared__ double s_nraw[kTcTile];            // fused LDA: per-row sums of w rho_raw
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -190,9 +178,6 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
         const int half = (warp - 2) >> 2;       // column blocks half, half + 2, ...
         const int r = q * 32 + lane;            // row of the tile = TMEM lane
         const int kc = KP / 8;
-        const double cf = fuse ? scal[kScalScale] : 1.0;
-        dfl exc_acc{0.f, 0.f};
-        double nraw_acc = 0.0;
         for (int it = 0; it < my_tiles; ++it) {
             const int s = it & 1, n = it >> 1;
             bool ok = mbar_wait(&sh->tmem_full[s], (uint32_t)(n & 1));
@@ -268,53 +253,7 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
                 const float bq = w - St;
                 const float e = Et + o.y + (St - (w - bq)) + (o.x - bq);
                 const int ep = row_exp[p];
-                const double raw = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
-                if (fuse) {
-                    const double wp = wt[p];
-                    nraw_acc += wp * raw;
-                    const double rc = raw * cf;
-                    rho[p] = rc;
-                    dfl ex;
-                    float v;
-                    lda_point_df(df_from(rc), ex, v);
-                    const dfl wd = df_from(wp);
-                    exc_acc = df_add(exc_acc, df_mul(wd, ex));
-                    cxc32[p] = (wd.h + wd.l) * v;
-                    if (want64) cxc[p] = wp * (double)v;
-                } else {
-                    rho[p] = raw;
-                }
-            }
-        }
-        if (fuse) {
-            // CTA sums of the fused point kernel: rows in order, then CTAs in order
-            if (half == 0) {
-                s_exc[r] = make_float2(exc_acc.h, exc_acc.l);
-                s_nraw[r] = nraw_acc;
-            }
-            epi8_bar_sync();
-            if (threadIdx.x == 64) {
-                dfl te{0.f, 0.f};
-                double tn = 0.0;
-                for (int i = 0; i < kTcTile; ++i) {
-                    te = df_add(te, dfl{s_exc[i].x, s_exc[i].y});
-                    tn += s_nraw[i];
-                }
-                part[2 * blockIdx.x] = df_to(te);
-                part[2 * blockIdx.x + 1] = tn;
-                __threadfence();
-                const int t = atomicAdd(counter, 1);
-                if (t == (int)gridDim.x - 1) {
-                    __threadfence();
-                    double se = 0.0, sn = 0.0;
-                    for (int b = 0; b < (int)gridDim.x; ++b) {
-                        se += __ldcg(part + 2 * b);
-                        sn += __ldcg(part + 2 * b + 1);
-                    }
-                    scal[kScalExc] = se;
-                    scal[kScalNelec] = sn * cf;
-                    *counter = 0;
-                }
+                rho[p] = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
             }
         }
     }
@@ -448,8 +387,9 @@ int density_tc_setup(dftg_ctx *c)
     c->tc_grid = nsm < ntiles ? nsm : ntiles;
     c->tc_grid_max = c->tc_grid;
     c->tc_ready = true;
-    // S_grid = Phi^T diag(w) Phi in FP64 (the grid overlap), for the correction
-    // factor of the fused density + LDA pass: integral of w rho_raw = 2 tr(P S_grid)
+    // S_grid = Phi^T diag(w) Phi in FP64 (the grid overlap): the integral of
+    // w rho_raw is 2 tr(P S_grid), so the correction factor is known when the
+    // density is formed and the point kernel needs no per-atom sums first
     if (!c->points_only) {
         DFTG_CUDA(cudaMalloc(&c->d_Sgrid, sizeof(double) * (size_t)c->nbf * c->nbf));
         DFTG_TRY_L(launch_contract_coef(c, c->d_w, c->d_Sgrid));
@@ -457,23 +397,25 @@ int density_tc_setup(dftg_ctx *c)
     return DFTG_OK;
 }
 
-int launch_density_tc(dftg_ctx *c, bool fuse_lda)
+int launch_density_tc(dftg_ctx *c, bool with_scale)
 {
-    // the fused LDA needs the correction factor from 2 tr(P S_grid) up front
-    const bool fuse = fuse_lda && c->d_Sgrid;
+    // the correction factor from 2 tr(P S_grid), for the point kernel that follows
+    const bool fuse = with_scale && c->d_Sgrid;
     double charge = 0.0;
     for (int a = 0; a < c->natoms; ++a) charge += (double)c->Z[a];
+    if (fuse && (size_t)((c->tc_NP + 3) / 4) > c->red_elems) {
+        set_error("reduction buffer too small for %d column blocks", (c->tc_NP + 3) / 4);
+        return DFTG_ERR_STATE;
+    }
     k_slice_P<<<(c->tc_NP + 3) / 4, 128, 0, c->stream>>>(c->nbf, c->tc_KP, c->tc_NP, c->d_P,
                                                          reinterpret_cast<__nv_bfloat16 *>(c->d_tcB), c->d_tc_colexp,
                                                          fuse ? c->d_Sgrid : nullptr, charge, c->d_red, c->d_scal,
                                                          c->d_counters + kCntAtoms);
     DFTG_LAUNCH_CHECK();
     const int ntiles = (int)(c->npad / kTcTile);
-    const int want64 = (c->prec_mask & kPrecContract) && c->ct_ready ? 0 : 1;
     k_density_tc<<<c->tc_grid, kTcThreads, density_tc_smem(c->tc_KP, c->tc_NP), c->stream>>>(
         c->nbf, c->tc_KP, c->tc_NP, ntiles, reinterpret_cast<const unsigned char *>(c->d_tcA), c->d_tc_rowexp,
-        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag, fuse ? 1 : 0, c->d_w,
-        c->d_scal, c->d_cxc, c->d_cxc32, want64, c->d_red, c->d_counters + kCntLda);
+        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }

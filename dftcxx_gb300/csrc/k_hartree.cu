@@ -608,23 +608,48 @@ __global__ void k_splines(int natoms, int cell0, int nrad, int nlm, const double
 // Poisson map with the l = 0 boundary value sqrt(4 pi) q_a (atomicgrid.cpp:
 // 301-432), and the spline fit of U_lm (atomicgrid.cpp:535-556), all in
 // double-float arithmetic with exact products.  The CTA stages the cell's
-// rho w_becke shell by shell (kMpSC shells per pass) and each thread forms one
-// rho_lm(i) as a 302-term dot product against the group's w_leb Y_lm rows, so
-// nothing is reduced across threads; the Poisson and spline maps are read from
-// L2 once per (l, m) row.  The CTA holding lm = 0 also sums q_a = sum w rho
-// over the cell (FP64, fixed order) for the boundary value.
-// Writes U (FP64 and split FP32, both radial orders) and the spline tables.
-constexpr int kMpLG = 7;          // (l, m) rows per CTA
+// rho w_becke (the FP32 hi / lo planes of the point kernel when given, else
+// formed from the FP64 arrays) kMpSC shells per pass, and each thread forms
+// one rho_lm(i) as a dot product over the Lebedev points against the group's
+// w_leb Y_lm rows, so nothing is reduced across threads.  The Poisson map of
+// each l and the spline derivative map are then staged in the same shared
+// memory (when an N x N double-float map fits) and applied a row per thread.
+// The CTA holding lm = 0 also sums q_a = sum w rho over the cell (FP64, fixed
+// order) for the boundary value.  Writes U (FP64 and split FP32, both radial
+// orders) and the spline tables.
+constexpr int kMpLG = 4;          // (l, m) rows per CTA
 constexpr int kMpSC = 32;         // radial shells staged per pass
-constexpr int kMpThreads = 256;
+constexpr int kMpThreads = 320;
+
+static size_t mp_stage_bytes(int nang) { return sizeof(dfl) * (size_t)kMpSC * (size_t)(nang | 1); }
 
 size_t multipole_smem(int nrad, int nang)
 {
-    const size_t row = (size_t)(nang | 1);                  // odd row length: no bank aliasing across shells
-    return sizeof(dfl) * ((size_t)kMpSC * row + (size_t)kMpLG * nang + 3 * (size_t)kMpLG * nrad) + 64 * sizeof(double);
+    return mp_stage_bytes(nang) + sizeof(dfl) * ((size_t)kMpLG * nang + 3 * (size_t)kMpLG * nrad) +
+           64 * sizeof(double);
+}
+
+// acc = sum_k M[k][i] x[k] over k < N (M given as hi / lo planes with row
+// stride N), four independent double-float accumulators
+__device__ __forceinline__ dfl mp_matvec(const float *__restrict__ Mh, const float *__restrict__ Ml, int N, int i,
+                                         const dfl *__restrict__ x, bool reverse_x)
+{
+    dfl a0{0.f, 0.f}, a1{0.f, 0.f}, a2{0.f, 0.f}, a3{0.f, 0.f};
+    int k = 0;
+    for (; k + 3 < N; k += 4) {
+        const dfl x0 = reverse_x ? x[N - 1 - k] : x[k], x1 = reverse_x ? x[N - 2 - k] : x[k + 1];
+        const dfl x2 = reverse_x ? x[N - 3 - k] : x[k + 2], x3 = reverse_x ? x[N - 4 - k] : x[k + 3];
+        a0 = df_fma(a0, dfl{Mh[(size_t)k * N + i], Ml[(size_t)k * N + i]}, x0);
+        a1 = df_fma(a1, dfl{Mh[(size_t)(k + 1) * N + i], Ml[(size_t)(k + 1) * N + i]}, x1);
+        a2 = df_fma(a2, dfl{Mh[(size_t)(k + 2) * N + i], Ml[(size_t)(k + 2) * N + i]}, x2);
+        a3 = df_fma(a3, dfl{Mh[(size_t)(k + 3) * N + i], Ml[(size_t)(k + 3) * N + i]}, x3);
+    }
+    for (; k < N; ++k) a0 = df_fma(a0, dfl{Mh[(size_t)k * N + i], Ml[(size_t)k * N + i]}, reverse_x ? x[N - 1 - k] : x[k]);
+    return df_add(df_add(a0, a1), df_add(a2, a3));
 }
 
 __global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0, int N, int nang, int lmax, int ngroup,
+                                                          const float *__restrict__ rw32, size_t npad,
                                                           const double *__restrict__ rho, const double *__restrict__ wb,
                                                           const double *__restrict__ w, const float *__restrict__ Ywt32,
                                                           const float *__restrict__ maps, double *__restrict__ scal,
@@ -635,8 +660,11 @@ __global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0,
     extern __shared__ __align__(16) unsigned char mp_smem[];
     const int nlm = (lmax + 1) * (lmax + 1);
     const int row = nang | 1;
+    const size_t stage_bytes = sizeof(dfl) * (size_t)kMpSC * row;
     dfl *sRW = reinterpret_cast<dfl *>(mp_smem);                 // [kMpSC][row] rho w_becke
-    dfl *sY = sRW + (size_t)kMpSC * row;                         // [kMpLG][nang] w_leb Y_lm
+    float *sMap = reinterpret_cast<float *>(mp_smem);            // the same space: a map's hi, lo planes
+    const bool stage_maps = (size_t)2 * N * N * sizeof(float) <= stage_bytes;
+    dfl *sY = reinterpret_cast<dfl *>(mp_smem + stage_bytes);    // [kMpLG][nang] w_leb Y_lm
     dfl *sR = sY + (size_t)kMpLG * nang;                         // [kMpLG][N] rho_lm
     dfl *sU = sR + (size_t)kMpLG * N;                            // [kMpLG][N] U_lm
     dfl *sD = sU + (size_t)kMpLG * N;                            // [kMpLG][N] spline derivatives
@@ -668,67 +696,76 @@ __global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0,
         for (int e = tid; e < ns * nang; e += kMpThreads) {
             const int ii = e / nang, j = e % nang;
             const size_t p = base + (size_t)(i0 + ii) * nang + j;
-            sRW[(size_t)ii * row + j] = df_from(rho[p] * wb[p]);
+            sRW[(size_t)ii * row + j] = rw32 ? dfl{rw32[p], rw32[npad + p]} : df_from(rho[p] * wb[p]);
         }
         __syncthreads();
         for (int o = tid; o < nl * ns; o += kMpThreads) {
             const int r = o % nl, ii = o / nl;
             const dfl *x = sRW + (size_t)ii * row, *y = sY + (size_t)r * nang;
-            float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f;
+            float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f, s2 = 0.f, e2 = 0.f, s3 = 0.f, e3 = 0.f;
             int j = 0;
-            for (; j + 1 < nang; j += 2) {
-                const dfl x0 = x[j], y0 = y[j], x1 = x[j + 1], y1 = y[j + 1];
-                df_mac(s0, e0, x0.h, x0.l, y0.h, y0.l);
-                df_mac(s1, e1, x1.h, x1.l, y1.h, y1.l);
+            for (; j + 3 < nang; j += 4) {
+                df_mac(s0, e0, x[j].h, x[j].l, y[j].h, y[j].l);
+                df_mac(s1, e1, x[j + 1].h, x[j + 1].l, y[j + 1].h, y[j + 1].l);
+                df_mac(s2, e2, x[j + 2].h, x[j + 2].l, y[j + 2].h, y[j + 2].l);
+                df_mac(s3, e3, x[j + 3].h, x[j + 3].l, y[j + 3].h, y[j + 3].l);
             }
-            if (j < nang) df_mac(s0, e0, x[j].h, x[j].l, y[j].h, y[j].l);
-            sR[r * N + i0 + ii] = df_mul(df_add(df_norm(s0, e0), df_norm(s1, e1)), four_pi);
+            for (; j < nang; ++j) df_mac(s0, e0, x[j].h, x[j].l, y[j].h, y[j].l);
+            const dfl t = df_add(df_add(df_norm(s0, e0), df_norm(s1, e1)), df_add(df_norm(s2, e2), df_norm(s3, e3)));
+            sR[r * N + i0 + ii] = df_mul(t, four_pi);
         }
     }
     __syncthreads();
     if (lm0 == 0) q = sred[32];
-    // Poisson: U = G_l rho_lm (+ Gb q for lm = 0)
+    // Poisson: U = G_l rho_lm (+ Gb q for lm = 0), one l of the group at a time
     const size_t ng = (size_t)(lmax + 1) * N * N;
     const float *Gbh = maps + 2 * ng, *Gbl = Gbh + N;
-    for (int o = tid; o < nl * N; o += kMpThreads) {
-        const int r = o / N, i = o % N, lm = lm0 + r;
-        int l = 0;
-        while ((l + 1) * (l + 1) <= lm) ++l;
+    int lfirst = 0, llast = 0;
+    while ((lfirst + 1) * (lfirst + 1) <= lm0) ++lfirst;
+    while ((llast + 1) * (llast + 1) <= lm0 + nl - 1) ++llast;
+    for (int l = lfirst; l <= llast; ++l) {
         const float *Gh = maps + (size_t)l * N * N, *Gl = Gh + ng;
-        const dfl *R = sR + r * N;
-        dfl acc0{0.f, 0.f}, acc1{0.f, 0.f};
-        int k = 0;
-        for (; k + 1 < N; k += 2) {
-            acc0 = df_fma(acc0, dfl{Gh[(size_t)k * N + i], Gl[(size_t)k * N + i]}, R[k]);
-            acc1 = df_fma(acc1, dfl{Gh[(size_t)(k + 1) * N + i], Gl[(size_t)(k + 1) * N + i]}, R[k + 1]);
+        if (stage_maps) {
+            __syncthreads();                                      // sMap free (rho w planes or the previous l)
+            for (int e = tid; e < N * N; e += kMpThreads) {
+                sMap[e] = Gh[e];
+                sMap[(size_t)N * N + e] = Gl[e];
+            }
+            __syncthreads();
+            Gh = sMap;
+            Gl = sMap + (size_t)N * N;
         }
-        if (k < N) acc0 = df_fma(acc0, dfl{Gh[(size_t)k * N + i], Gl[(size_t)k * N + i]}, R[k]);
-        dfl v = df_add(acc0, acc1);
-        if (lm == 0) v = df_fma(v, dfl{Gbh[i], Gbl[i]}, df_from(q));
-        sU[r * N + i] = v;
-        const size_t id = (size_t)a * nlm + lm;
-        U[id * N + i] = df_to(v);
-        U32[id * N + i] = v.h;
-        U32[uhalf + id * N + i] = v.l;
-        U32T[((size_t)a * N + i) * nlm + lm] = v.h;
-        U32T[uhalf + ((size_t)a * N + i) * nlm + lm] = v.l;
+        for (int o = tid; o < nl * N; o += kMpThreads) {
+            const int r = o / N, i = o % N, lm = lm0 + r;
+            if (lm < l * l || lm > l * l + 2 * l) continue;
+            dfl v = mp_matvec(Gh, Gl, N, i, sR + r * N, false);
+            if (lm == 0) v = df_fma(v, dfl{Gbh[i], Gbl[i]}, df_from(q));
+            sU[r * N + i] = v;
+            const size_t id = (size_t)a * nlm + lm;
+            U[id * N + i] = df_to(v);
+            U32[id * N + i] = v.h;
+            U32[uhalf + id * N + i] = v.l;
+            U32T[((size_t)a * N + i) * nlm + lm] = v.h;
+            U32T[uhalf + ((size_t)a * N + i) * nlm + lm] = v.l;
+        }
     }
-    __syncthreads();
     // spline derivatives over increasing r: D = K y, y[i] = U[N - 1 - i]
     const float *Kh = maps + 2 * ng + 2 * (size_t)N, *Kl = Kh + (size_t)N * N;
     const float *ih = Kl + (size_t)N * N, *il = ih + N;
     const float *fh = il + N, *fl = fh + nlm;
+    __syncthreads();                                              // sU complete; sMap free
+    if (stage_maps) {
+        for (int e = tid; e < N * N; e += kMpThreads) {
+            sMap[e] = Kh[e];
+            sMap[(size_t)N * N + e] = Kl[e];
+        }
+        __syncthreads();
+        Kh = sMap;
+        Kl = sMap + (size_t)N * N;
+    }
     for (int o = tid; o < nl * N; o += kMpThreads) {
         const int r = o / N, i = o % N;
-        const dfl *u = sU + r * N;
-        dfl a0{0.f, 0.f}, a1{0.f, 0.f};
-        int j = 0;
-        for (; j + 1 < N; j += 2) {
-            a0 = df_fma(a0, dfl{Kh[(size_t)j * N + i], Kl[(size_t)j * N + i]}, u[N - 1 - j]);
-            a1 = df_fma(a1, dfl{Kh[(size_t)(j + 1) * N + i], Kl[(size_t)(j + 1) * N + i]}, u[N - 2 - j]);
-        }
-        if (j < N) a0 = df_fma(a0, dfl{Kh[(size_t)j * N + i], Kl[(size_t)j * N + i]}, u[N - 1 - j]);
-        sD[r * N + i] = df_add(a0, a1);
+        sD[r * N + i] = mp_matvec(Kh, Kl, N, i, sU + r * N, true);
     }
     __syncthreads();
     for (int o = tid; o < nl * N; o += kMpThreads) {
@@ -1009,13 +1046,24 @@ __global__ void __launch_bounds__(256) k_vcross_gather_own(size_t npts, size_t n
         const int al = (int)(p / per), rem = (int)(p % per), i = rem / nang, j = rem % nang, a = cell0 + al;
         const float *uh = U32T + ((size_t)a * nrad + i) * nlm, *ul = uh + uhalf;
         const float *yh = Y32 + j, *yl = Y32 + (size_t)nlm * nang + j;
-        float s = 0.f, e = 0.f;
-        for (int lm = 0; lm < nlm; ++lm) df_mac(s, e, uh[lm], ul[lm], yh[(size_t)lm * nang], yl[(size_t)lm * nang]);
-        const double vown = df_to(df_norm(s, e)) * invr[p];
+        // four independent accumulators so the loads of several (l, m) are in flight
+        float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f, s2 = 0.f, e2 = 0.f, s3 = 0.f, e3 = 0.f;
+        int lm = 0;
+        for (; lm + 3 < nlm; lm += 4) {
+            df_mac(s0, e0, uh[lm], ul[lm], yh[(size_t)lm * nang], yl[(size_t)lm * nang]);
+            df_mac(s1, e1, uh[lm + 1], ul[lm + 1], yh[(size_t)(lm + 1) * nang], yl[(size_t)(lm + 1) * nang]);
+            df_mac(s2, e2, uh[lm + 2], ul[lm + 2], yh[(size_t)(lm + 2) * nang], yl[(size_t)(lm + 2) * nang]);
+            df_mac(s3, e3, uh[lm + 3], ul[lm + 3], yh[(size_t)(lm + 3) * nang], yl[(size_t)(lm + 3) * nang]);
+        }
+        for (; lm < nlm; ++lm) df_mac(s0, e0, uh[lm], ul[lm], yh[(size_t)lm * nang], yl[(size_t)lm * nang]);
+        const dfl vs = df_add(df_add(df_norm(s0, e0), df_norm(s1, e1)), df_add(df_norm(s2, e2), df_norm(s3, e3)));
+        const double vown = df_to(vs) * invr[p];
         float vh = 0.f, vl = 0.f;
+        const int *pp = pos + p * natoms;
+#pragma unroll 4
         for (int k = 0; k < natoms; ++k) {
             if (k == a) continue;
-            const float2 v = pairv[pos[p * natoms + k]];
+            const float2 v = pairv[pp[k]];
             two_sum_acc(vh, vl, v.x);
             vl += v.y;
         }
@@ -1251,8 +1299,9 @@ int launch_hartree_multipoles(dftg_ctx *c)
         const size_t sm = multipole_smem(N, c->nang);
         if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_multipole), c->device));
         k_multipole<<<(unsigned)(nc * ngroup), kMpThreads, sm, c->stream>>>(
-            c->natoms, c0, N, c->nang, c->lmax, ngroup, c->d_rho, c->d_wb, c->d_w, c->d_Ywt32, c->d_maps32, c->d_scal,
-            c->d_U, c->d_U32, c->d_U32T, (c->prec_mask & kPrecCross) ? 0 : 1, c->d_spl, c->d_splm);
+            c->natoms, c0, N, c->nang, c->lmax, ngroup, c->rw_ready ? c->d_rw32 : nullptr, c->npad, c->d_rho, c->d_wb,
+            c->d_w, c->d_Ywt32, c->d_maps32, c->d_scal, c->d_U, c->d_U32, c->d_U32T, (c->prec_mask & kPrecCross) ? 0 : 1,
+            c->d_spl, c->d_splm);
         DFTG_LAUNCH_CHECK();
         DFTG_MARK(c, "multipole");
         if (!(c->prec_mask & kPrecCross)) {
