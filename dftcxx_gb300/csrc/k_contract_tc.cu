@@ -7,14 +7,15 @@
 //   A = phi                         rows mu < nbf of M = 128
 //   B = [c_xc o phi ; c_j o phi]    rows n < 2 nbf of N = NP (2 nbf rounded up to 16)
 //
-// Number format (per point chunk of at most 512 points).  Row mu of A is scaled
+// Number format (per point chunk of at most 1024 points).  Row mu of A is scaled
 // by 2^(7 - e_mu), e_mu the exponent bound of max |phi_mu| over the chunk, and
 // split into three BF16 slices: a_1 = rint(x) (an integer, |a_1| <= 128),
 // a_2 = bf16(x - a_1), a_3 = bf16(x - a_1 - a_2).  B row nu is scaled by
 // 2^(7 - s_nu - v), s_nu the bound of max |w phi_nu| over the chunk (fixed for
 // the grid) and v the bound of max |c / w| (per build), and split likewise.  The
-// leading products a_1 b_1 are integers below 2^14, so their sum over a chunk
-// (< 2^23) is exact in the FP32 accumulator whatever the accumulator's
+// leading products a_1 b_1 are integers of magnitude at most 2^14, so every
+// partial sum over a chunk is an integer of magnitude at most 2^24, exact in the
+// FP32 accumulator whatever the accumulator's
 // rounding; the five correction products (a_1 b_2, a_2 b_1, a_1 b_3, a_2 b_2,
 // a_3 b_1) go to a second accumulator, about 2^-8 of the first.  The epilogue
 // scales D_hi and D_lo back by exact powers of two and adds them to the CTA's
@@ -55,7 +56,7 @@ constexpr int kCtEpiWarps = 16;           // four per TMEM lane quarter
 constexpr int kCtThreads = (kCtEpi0 + kCtEpiWarps + 1) * 32;
 constexpr int kCtLoaderWarp = kCtEpi0 + kCtEpiWarps;
 constexpr int kCtMaxStages = 8;
-constexpr int kCtMaxKbPerChunk = 16;       // <= 512 points per exact integer accumulation (sums < 2^23)
+constexpr int kCtMaxKbPerChunk = 32;       // <= 1024 points per exact integer accumulation (|sums| <= 2^24)
 constexpr uint32_t kCtTmemCols = 512;      // D_hi at column 0, D_lo at column 256
 constexpr int kCtSlices = 3;
 constexpr int kCtExpMin = -100;            // exponent bounds are clamped to [-100, 100]
