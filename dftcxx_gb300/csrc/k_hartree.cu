@@ -648,6 +648,20 @@ __device__ __forceinline__ dfl mp_matvec(const float *__restrict__ Mh, const flo
     return df_add(df_add(a0, a1), df_add(a2, a3));
 }
 
+// n floats global -> shared with eight loads in flight per thread
+__device__ __forceinline__ void mp_copy(float *__restrict__ dst, const float *__restrict__ src, int n)
+{
+    int e = threadIdx.x;
+    for (; e + 7 * kMpThreads < n; e += 8 * kMpThreads) {
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = src[e + u * kMpThreads];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) dst[e + u * kMpThreads] = v[u];
+    }
+    for (; e < n; e += kMpThreads) dst[e] = src[e];
+}
+
 __global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0, int N, int nang, int lmax, int ngroup,
                                                           const float *__restrict__ rw32, size_t npad,
                                                           const double *__restrict__ rho, const double *__restrict__ wb,
@@ -678,12 +692,20 @@ __global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0,
         const int r = e / nang, j = e % nang;
         sY[e] = dfl{Ywt32[(size_t)j * nlm + lm0 + r], Ywt32[(size_t)nang * nlm + (size_t)j * nlm + lm0 + r]};
     }
-    // q_a for the boundary row of lm = 0
+    // q_a for the boundary row of lm = 0 (four loads in flight per thread)
     double q = 0.0;
     if (lm0 == 0) {
-        double t = 0.0;
-        for (int e = tid; e < N * nang; e += kMpThreads) t += w[base + e] * rho[base + e];
-        q = block_sum(t, sred);
+        const int n = N * nang;
+        double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+        int e = tid;
+        for (; e + 3 * kMpThreads < n; e += 4 * kMpThreads) {
+            t0 += w[base + e] * rho[base + e];
+            t1 += w[base + e + kMpThreads] * rho[base + e + kMpThreads];
+            t2 += w[base + e + 2 * kMpThreads] * rho[base + e + 2 * kMpThreads];
+            t3 += w[base + e + 3 * kMpThreads] * rho[base + e + 3 * kMpThreads];
+        }
+        for (; e < n; e += kMpThreads) t0 += w[base + e] * rho[base + e];
+        q = block_sum((t0 + t1) + (t2 + t3), sred);
         if (tid == 0) {
             sred[32] = q;
             scal[kScalAtomQ + a] = q;
@@ -693,11 +715,19 @@ __global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0,
     for (int i0 = 0; i0 < N; i0 += kMpSC) {
         const int ns = min(kMpSC, N - i0);
         __syncthreads();                                          // the previous pass is done with sRW
-        for (int e = tid; e < ns * nang; e += kMpThreads) {
-            const int ii = e / nang, j = e % nang;
-            const size_t p = base + (size_t)(i0 + ii) * nang + j;
-            sRW[(size_t)ii * row + j] = rw32 ? dfl{rw32[p], rw32[npad + p]} : df_from(rho[p] * wb[p]);
-        }
+        // a thread per Lebedev direction, eight shells' loads in flight
+        for (int j = tid; j < nang; j += kMpThreads)
+            for (int ii0 = 0; ii0 < ns; ii0 += 8) {
+                dfl v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const size_t p = base + (size_t)(i0 + min(ii0 + u, ns - 1)) * nang + j;
+                    v[u] = rw32 ? dfl{rw32[p], rw32[npad + p]} : df_from(rho[p] * wb[p]);
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (ii0 + u < ns) sRW[(size_t)(ii0 + u) * row + j] = v[u];
+            }
         __syncthreads();
         // two threads per rho_lm(i), each over half of the Lebedev points, met
         // by a shuffle; every lane of a warp takes part (items past the end run
@@ -738,10 +768,8 @@ __global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0,
         const float *Gh = maps + (size_t)l * N * N, *Gl = Gh + ng;
         if (stage_maps) {
             __syncthreads();                                      // sMap free (rho w planes or the previous l)
-            for (int e = tid; e < N * N; e += kMpThreads) {
-                sMap[e] = Gh[e];
-                sMap[(size_t)N * N + e] = Gl[e];
-            }
+            mp_copy(sMap, Gh, N * N);
+            mp_copy(sMap + (size_t)N * N, Gl, N * N);
             __syncthreads();
             Gh = sMap;
             Gl = sMap + (size_t)N * N;
@@ -766,10 +794,8 @@ __global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0,
     const float *fh = il + N, *fl = fh + nlm;
     __syncthreads();                                              // sU complete; sMap free
     if (stage_maps) {
-        for (int e = tid; e < N * N; e += kMpThreads) {
-            sMap[e] = Kh[e];
-            sMap[(size_t)N * N + e] = Kl[e];
-        }
+        mp_copy(sMap, Kh, N * N);
+        mp_copy(sMap + (size_t)N * N, Kl, N * N);
         __syncthreads();
         Kh = sMap;
         Kl = sMap + (size_t)N * N;
