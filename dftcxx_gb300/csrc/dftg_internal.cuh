@@ -213,7 +213,6 @@ struct dftg_ctx {
     void *d_tcB = nullptr;        // [4][NP x KP] BF16 slices of P
     int *d_tc_rowexp = nullptr;   // [npad] per-point scale exponents
     int *d_tc_colexp = nullptr;   // [NP] per-column scale exponents of P
-    double *d_Sgrid = nullptr;    // [nbf][nbf] Phi^T diag(w) Phi (FP64): correction factor from 2 tr(P S_grid)
     float *d_rw32 = nullptr;      // [2][npad] rho w_becke split into FP32 hi, lo (mixed multipole input)
     bool rw_ready = false;        // d_rw32 holds the current corrected rho (written by the point kernel)
     int *d_flag = nullptr;        // device error flag (bounded waits that expired)

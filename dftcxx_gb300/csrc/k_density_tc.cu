@@ -65,7 +65,9 @@ struct TcShared {
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restrict__ Aslices,
              const int *__restrict__ row_exp, const unsigned char *__restrict__ Bslices,
-             const int *__restrict__ col_exp, double *__restrict__ rho, int *__restrict__ err)
+             const int *__restrict__ col_exp, double *__restrict__ rho, int *__restrict__ err,
+             const double *__restrict__ wt, double charge, double *__restrict__ part,
+             double *__restrict__ scal, int *__restrict__ counter)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const uint32_t a_slice_bytes = (uint32_t)kTcTile * KP * 2;
@@ -77,6 +79,7 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
     __shared__ int s_texp[kTcMaxK];
     __shared__ int s_fail;
     __shared__ float2 s_half[kTcTile];            // (S, E) of the second column half, per row
+    __shared__ double s_nraw[kTcTile];            // with wt: per-row sums of w rho_raw
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -178,6 +181,7 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
         const int half = (warp - 2) >> 2;       // column blocks half, half + 2, ...
         const int r = q * 32 + lane;            // row of the tile = TMEM lane
         const int kc = KP / 8;
+        double nraw = 0.0;                      // with wt: this row's sum of w rho_raw over the CTA's tiles
         for (int it = 0; it < my_tiles; ++it) {
             const int s = it & 1, n = it >> 1;
             bool ok = mbar_wait(&sh->tmem_full[s], (uint32_t)(n & 1));
@@ -253,7 +257,29 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
                 const float bq = w - St;
                 const float e = Et + o.y + (St - (w - bq)) + (o.x - bq);
                 const int ep = row_exp[p];
-                rho[p] = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
+                const double raw = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
+                rho[p] = raw;
+                if (wt) nraw += wt[p] * raw;
+            }
+        }
+        if (wt) {                          // every epilogue warp, also after an expired wait
+            // the integral of w rho_raw: rows in order per CTA, CTAs in order by the
+            // last one, which also forms the correction factor charge / integral
+            if (half == 0) s_nraw[r] = nraw;
+            epi8_bar_sync();
+            if (threadIdx.x == 64) {
+                double t = 0.0;
+                for (int i = 0; i < kTcTile; ++i) t += s_nraw[i];
+                part[blockIdx.x] = t;
+                __threadfence();
+                if (atomicAdd(counter, 1) == (int)gridDim.x - 1) {
+                    __threadfence();
+                    double total = 0.0;
+                    for (int b = 0; b < (int)gridDim.x; ++b) total += __ldcg(part + b);
+                    scal[kScalSum] = total;
+                    scal[kScalScale] = charge / total;
+                    *counter = 0;
+                }
             }
         }
     }
@@ -305,52 +331,29 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
 }
 
 // P (FP64, nbf x nbf, symmetric) -> 4 pre-scaled integer slices per column in
-// the B layout: one warp per column, lanes over the rows.  With S (S_grid =
-// Phi^T diag(w) Phi, FP64) it also forms the integral of w rho_raw as
-// 2 tr(P S_grid) (warp, block and block-order sums; the last block finishes)
-// and the density correction factor charge / integral (moleculargrid.cpp:132-146).
+// the B layout: one warp per column, lanes over the rows
 __global__ void k_slice_P(int nbf, int KP, int NP, const double *__restrict__ P, __nv_bfloat16 *__restrict__ B,
-                          int *__restrict__ col_exp, const double *__restrict__ S, double charge,
-                          double *__restrict__ part, double *__restrict__ scal, int *__restrict__ counter)
+                          int *__restrict__ col_exp)
 {
-    __shared__ double s_w[32];
-    __shared__ int s_last;
     const int nu = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    double tr = 0.0;
-    if (nu < NP) {
-        double mx = 0.0;
-        if (nu < nbf)
-            for (int mu = lane; mu < nbf; mu += 32) {
-                const double pv = P[(size_t)nu * nbf + mu];
-                mx = fmax(mx, fabs(pv));
-                if (S) tr += pv * S[(size_t)nu * nbf + mu];
-            }
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        int e = 0;
-        if (mx > 0.0) frexp(mx, &e);
-        if (nu < nbf && lane == 0) col_exp[nu] = e;
-        const size_t slice = (size_t)NP * KP;
-        for (int mu = lane; mu < KP; mu += 32) {
-            double x = (nu < nbf && mu < nbf) ? ldexp(P[(size_t)nu * nbf + mu], -e) : 0.0;
-            const size_t o = core_off(nu, mu, KP / 8) / 2;
-            for (int i = 0; i < kTcSlices; ++i) {
-                x *= 256.0;
-                const double m = rint(x);
-                x -= m;
-                B[(size_t)i * slice + o] = __float2bfloat16_rn((float)ldexp(m, -8 * i));
-            }
+    if (nu >= NP) return;
+    double mx = 0.0;
+    if (nu < nbf)
+        for (int mu = lane; mu < nbf; mu += 32) mx = fmax(mx, fabs(P[(size_t)nu * nbf + mu]));
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = 0;
+    if (mx > 0.0) frexp(mx, &e);
+    if (nu < nbf && lane == 0) col_exp[nu] = e;
+    const size_t slice = (size_t)NP * KP;
+    for (int mu = lane; mu < KP; mu += 32) {
+        double x = (nu < nbf && mu < nbf) ? ldexp(P[(size_t)nu * nbf + mu], -e) : 0.0;
+        const size_t o = core_off(nu, mu, KP / 8) / 2;
+        for (int i = 0; i < kTcSlices; ++i) {
+            x *= 256.0;
+            const double m = rint(x);
+            x -= m;
+            B[(size_t)i * slice + o] = __float2bfloat16_rn((float)ldexp(m, -8 * i));
         }
-    }
-    if (!S) return;                     // block-uniform
-    const double t = block_sum(tr, s_w);
-    if (threadIdx.x == 0) part[blockIdx.x] = t;
-    if (!last_block(counter, &s_last)) return;
-    if (threadIdx.x == 0) {
-        double sum = 0.0;
-        for (int b = 0; b < (int)gridDim.x; ++b) sum += __ldcg(part + b);
-        const double total = 2.0 * sum;
-        scal[kScalSum] = total;
-        scal[kScalScale] = charge / total;
     }
 }
 
@@ -387,35 +390,27 @@ int density_tc_setup(dftg_ctx *c)
     c->tc_grid = nsm < ntiles ? nsm : ntiles;
     c->tc_grid_max = c->tc_grid;
     c->tc_ready = true;
-    // S_grid = Phi^T diag(w) Phi in FP64 (the grid overlap): the integral of
-    // w rho_raw is 2 tr(P S_grid), so the correction factor is known when the
-    // density is formed and the point kernel needs no per-atom sums first
-    if (!c->points_only) {
-        DFTG_CUDA(cudaMalloc(&c->d_Sgrid, sizeof(double) * (size_t)c->nbf * c->nbf));
-        DFTG_TRY_L(launch_contract_coef(c, c->d_w, c->d_Sgrid));
-    }
     return DFTG_OK;
 }
 
 int launch_density_tc(dftg_ctx *c, bool with_scale)
 {
-    // the correction factor from 2 tr(P S_grid), for the point kernel that follows
-    const bool fuse = with_scale && c->d_Sgrid;
+    k_slice_P<<<(c->tc_NP + 3) / 4, 128, 0, c->stream>>>(c->nbf, c->tc_KP, c->tc_NP, c->d_P,
+                                                         reinterpret_cast<__nv_bfloat16 *>(c->d_tcB), c->d_tc_colexp);
+    DFTG_LAUNCH_CHECK();
+    // with_scale: the integral of w rho_raw and the correction factor, summed in
+    // the epilogue, for the point kernel that follows
     double charge = 0.0;
     for (int a = 0; a < c->natoms; ++a) charge += (double)c->Z[a];
-    if (fuse && (size_t)((c->tc_NP + 3) / 4) > c->red_elems) {
-        set_error("reduction buffer too small for %d column blocks", (c->tc_NP + 3) / 4);
+    if (with_scale && (size_t)c->tc_grid > c->red_elems) {
+        set_error("reduction buffer too small for %d density CTAs", c->tc_grid);
         return DFTG_ERR_STATE;
     }
-    k_slice_P<<<(c->tc_NP + 3) / 4, 128, 0, c->stream>>>(c->nbf, c->tc_KP, c->tc_NP, c->d_P,
-                                                         reinterpret_cast<__nv_bfloat16 *>(c->d_tcB), c->d_tc_colexp,
-                                                         fuse ? c->d_Sgrid : nullptr, charge, c->d_red, c->d_scal,
-                                                         c->d_counters + kCntAtoms);
-    DFTG_LAUNCH_CHECK();
     const int ntiles = (int)(c->npad / kTcTile);
     k_density_tc<<<c->tc_grid, kTcThreads, density_tc_smem(c->tc_KP, c->tc_NP), c->stream>>>(
         c->nbf, c->tc_KP, c->tc_NP, ntiles, reinterpret_cast<const unsigned char *>(c->d_tcA), c->d_tc_rowexp,
-        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag);
+        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag,
+        with_scale ? c->d_w : nullptr, charge, c->d_red, c->d_scal, c->d_counters + kCntAtoms);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }
