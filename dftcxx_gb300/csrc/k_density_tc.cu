@@ -184,13 +184,17 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
         double nraw = 0.0;                      // with wt: this row's sum of w rho_raw over the CTA's tiles
         for (int it = 0; it < my_tiles; ++it) {
             const int s = it & 1, n = it >> 1;
+            const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+            const size_t p = (size_t)tile * kTcTile + r;
+            // the row's scale exponent and weight are loaded before the wait, so
+            // their latency overlaps it
+            const int ep = half == 0 ? row_exp[p] : 0;
+            const double wp = (wt && half == 0) ? __ldcs(wt + p) : 0.0;
             bool ok = mbar_wait(&sh->tmem_full[s], (uint32_t)(n & 1));
             if (!ok) { atomicExch(err, 4); s_fail = 1; }
             epi8_bar_sync();
             if (s_fail) break;
             tc_fence_after();
-            const int tile = (int)blockIdx.x + it * (int)gridDim.x;
-            const size_t p = (size_t)tile * kTcTile + r;
             const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
             const uint32_t ta0 = tmem + (uint32_t)(s * 256) + ((uint32_t)(q * 32) << 16);
             // two independent compensated accumulators (even / odd columns)
@@ -256,10 +260,9 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
                 const float w = St + o.x;
                 const float bq = w - St;
                 const float e = Et + o.y + (St - (w - bq)) + (o.x - bq);
-                const int ep = row_exp[p];
                 const double raw = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
                 rho[p] = raw;
-                if (wt) nraw += wt[p] * raw;
+                nraw += wp * raw;
             }
         }
         if (wt) {                          // every epilogue warp, also after an expired wait

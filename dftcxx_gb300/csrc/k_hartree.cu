@@ -1084,18 +1084,29 @@ __global__ void __launch_bounds__(kGoThreads) k_vcross_gather_own(size_t npts, s
                                                                   float *__restrict__ cj32, double *__restrict__ part,
                                                                   double *scal, int *counter)
 {
-    extern __shared__ float go_smem[];                       // [2][nlm][kGoSlab] Y_lm hi, lo
+    extern __shared__ float go_smem[];                       // [2][nlm][kGoSlab] Y_lm, [2][kGoShells][nlm] U_lm
     __shared__ double sh[32];
     __shared__ int s_last;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int b = blockIdx.x;
     const int al = b / (nslab * nsplit), rest = b % (nslab * nsplit), slab = rest / nsplit, sp = rest % nsplit;
     const int a = cell0 + al, j0 = slab * kGoSlab;
+    const int i_beg = sp * kGoShells, i_end = min(nrad, i_beg + kGoShells);
     float *syh = go_smem, *syl = go_smem + (size_t)nlm * kGoSlab;
+    float *suh = syl + (size_t)nlm * kGoSlab, *sul = suh + (size_t)kGoShells * nlm;
     for (int e = tid; e < nlm * kGoSlab; e += kGoThreads) {
         const int lm = e / kGoSlab, jj = e % kGoSlab, j = j0 + jj;
         syh[e] = j < nang ? Y32[(size_t)lm * nang + j] : 0.f;
         syl[e] = j < nang ? Y32[(size_t)nlm * nang + (size_t)lm * nang + j] : 0.f;
+    }
+    // the block's shells of U_lm (rows (a, i) of the transposed split table are contiguous)
+    {
+        const size_t u0 = ((size_t)a * nrad + i_beg) * nlm;
+        const int nu = (i_end - i_beg) * nlm;
+        for (int e = tid; e < nu; e += kGoThreads) {
+            suh[e] = U32T[u0 + e];
+            sul[e] = U32T[uhalf + u0 + e];
+        }
     }
     if (b == 0)                                              // the padded tail of the point arrays
         for (size_t p = npts + tid; p < npad; p += kGoThreads) {
@@ -1105,10 +1116,9 @@ __global__ void __launch_bounds__(kGoThreads) k_vcross_gather_own(size_t npts, s
         }
     __syncthreads();
     const int j = j0 + lane;
-    const int i_beg = sp * kGoShells, i_end = min(nrad, i_beg + kGoShells);
     double ej = 0.0;
     for (int i = i_beg + warp; i < i_end; i += kGoThreads / 32) {
-        const float *uh = U32T + ((size_t)a * nrad + i) * nlm, *ul = uh + uhalf;
+        const float *uh = suh + (size_t)(i - i_beg) * nlm, *ul = sul + (size_t)(i - i_beg) * nlm;
         float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f, s2 = 0.f, e2 = 0.f, s3 = 0.f, e3 = 0.f;
         int lm = 0;
         for (; lm + 3 < nlm; lm += 4) {
@@ -1124,12 +1134,21 @@ __global__ void __launch_bounds__(kGoThreads) k_vcross_gather_own(size_t npts, s
         const double vown = df_to(vs) * invr[p];
         float vh = 0.f, vl = 0.f;
         const int *pp = pos + p * natoms;
-#pragma unroll 4
-        for (int k = 0; k < natoms; ++k) {
-            if (k == a) continue;
-            const float2 v = pairv[pp[k]];
-            two_sum_acc(vh, vl, v.x);
-            vl += v.y;
+        // eight atoms at a time: their places, then their contributions, then
+        // the sum in atom order
+        for (int k0 = 0; k0 < natoms; k0 += 8) {
+            int q[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) q[u] = (k0 + u < natoms && k0 + u != a) ? pp[k0 + u] : -1;
+            float2 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = q[u] >= 0 ? pairv[q[u]] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (q[u] >= 0) {
+                    two_sum_acc(vh, vl, v[u].x);
+                    vl += v[u].y;
+                }
         }
         const double Vt = vown + ((double)vh + (double)vl);
         V[p] = Vt;
@@ -1414,7 +1433,7 @@ int launch_hartree_cross(dftg_ctx *c)
             const int nslab = (c->nang + kGoSlab - 1) / kGoSlab, nsplit = (N + kGoShells - 1) / kGoShells;
             const size_t nblk = (size_t)c->ncell * nslab * nsplit;
             if (nblk > c->red_elems) { set_error("reduction buffer too small for %zu blocks", nblk); return DFTG_ERR_STATE; }
-            const size_t sm = sizeof(float) * 2 * (size_t)c->nlm * kGoSlab;
+            const size_t sm = sizeof(float) * 2 * (size_t)c->nlm * (kGoSlab + kGoShells);
             if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_vcross_gather_own), c->device));
             k_vcross_gather_own<<<(unsigned)nblk, kGoThreads, sm, c->stream>>>(
                 c->npts, c->npad, c->natoms, c->cell0, N, c->nang, c->nlm, nslab, nsplit, c->d_pairpos,
