@@ -79,7 +79,8 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
     __shared__ int s_texp[kTcMaxK];
     __shared__ int s_fail;
     __shared__ float2 s_half[kTcTile];            // (S, E) of the second column half, per row
-    __shared__ double s_nraw[kTcTile];            // with wt: per-row sums of w rho_raw
+    __shared__ double s_nraw[2 * kTcTile];        // with wt: per-row sums of w rho_raw, then the CTA sums
+    __shared__ int s_lastcta;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -266,8 +267,8 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
             }
         }
         if (wt) {                          // every epilogue warp, also after an expired wait
-            // the integral of w rho_raw: rows in order per CTA, CTAs in order by the
-            // last one, which also forms the correction factor charge / integral
+            // the integral of w rho_raw: rows in order per CTA, CTAs in order in
+            // the last one, which also forms the correction factor charge / integral
             if (half == 0) s_nraw[r] = nraw;
             epi8_bar_sync();
             if (threadIdx.x == 64) {
@@ -275,10 +276,17 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
                 for (int i = 0; i < kTcTile; ++i) t += s_nraw[i];
                 part[blockIdx.x] = t;
                 __threadfence();
-                if (atomicAdd(counter, 1) == (int)gridDim.x - 1) {
-                    __threadfence();
+                s_lastcta = atomicAdd(counter, 1) == (int)gridDim.x - 1;
+            }
+            epi8_bar_sync();
+            if (s_lastcta) {
+                __threadfence();
+                const int e = threadIdx.x - 64;                     // 0 .. 255 over the epilogue warps
+                for (int b = e; b < (int)gridDim.x; b += 256) s_nraw[b] = __ldcg(part + b);
+                epi8_bar_sync();
+                if (threadIdx.x == 64) {
                     double total = 0.0;
-                    for (int b = 0; b < (int)gridDim.x; ++b) total += __ldcg(part + b);
+                    for (int b = 0; b < (int)gridDim.x; ++b) total += s_nraw[b];
                     scal[kScalSum] = total;
                     scal[kScalScale] = charge / total;
                     *counter = 0;
@@ -405,7 +413,7 @@ int launch_density_tc(dftg_ctx *c, bool with_scale)
     // the epilogue, for the point kernel that follows
     double charge = 0.0;
     for (int a = 0; a < c->natoms; ++a) charge += (double)c->Z[a];
-    if (with_scale && (size_t)c->tc_grid > c->red_elems) {
+    if (with_scale && ((size_t)c->tc_grid > c->red_elems || c->tc_grid > 2 * kTcTile)) {
         set_error("reduction buffer too small for %d density CTAs", c->tc_grid);
         return DFTG_ERR_STATE;
     }
