@@ -330,24 +330,13 @@ int sync_scalars(dftg_ctx *c)
 }
 
 // device part of one Fock build; P already in c->d_P
-// the mixed density forms the integral of w rho_raw and the correction factor
-// in its epilogue, so the point kernel follows it directly and no per-atom sums
-// run: both steps mixed, the tensor-core density ready
-static bool scaled_density_lda(const dftg_ctx *c)
-{
-    return (c->prec_mask & kPrecDensity) && (c->prec_mask & kPrecLda) && c->tc_ready;
-}
-
 int fock_pipeline(dftg_ctx *c)
 {
-    if (scaled_density_lda(c)) {
-        DFTG_TRY(launch_density(c, true));      // rho_raw, its integral, the correction factor
-        DFTG_TRY(launch_xc_points(c, true, true));  // rho *= c, point kernel, E_xc, N, rho w_becke planes
-    } else {
-        DFTG_TRY(launch_density(c));
-        DFTG_TRY(launch_atom_sums(c, kSumsFactor));
-        DFTG_TRY(launch_xc_points(c, true));    // rescales rho by the correction factor
-    }
+    DFTG_TRY(launch_density(c));
+    DFTG_TRY(launch_atom_sums(c, kSumsFactor));
+    // rescales rho by the correction factor; with the mixed point kernel it also
+    // sums the corrected N and writes the rho w_becke planes of the multipoles
+    DFTG_TRY(launch_xc_points(c, true, (c->prec_mask & kPrecLda) != 0));
     c->rho_scaled = true;
     DFTG_TRY(launch_hartree(c));
     DFTG_TRY(launch_contract(c, true, true));

@@ -329,11 +329,11 @@ int mark(dftg_ctx *c, const char *name);
 int launch_grid(dftg_ctx *c);
 int launch_amplitudes(dftg_ctx *c);
 // k_density.cu
-int launch_density(dftg_ctx *c, bool with_scale = false);
+int launch_density(dftg_ctx *c);
 enum { kSumsOnly = 0, kSumsCorrect = 1, kSumsFactor = 2 };
 // k_density_tc.cu
 int density_tc_setup(dftg_ctx *c);
-int launch_density_tc(dftg_ctx *c, bool with_scale);
+int launch_density_tc(dftg_ctx *c);
 // k_density_tt.cu
 int density_tt_setup(dftg_ctx *c);
 int launch_density_tt(dftg_ctx *c);

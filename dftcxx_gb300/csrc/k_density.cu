@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
 
 // ---------------------------------------------------------------- launchers
 
-int launch_density(dftg_ctx *c, bool with_scale)
+int launch_density(dftg_ctx *c)
 {
     c->rw_ready = false;             // a new density: the rho w_becke planes are stale
     if (!(c->prec_mask & kPrecDensity)) {
@@ -375,7 +375,7 @@ int launch_density(dftg_ctx *c, bool with_scale)
         if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_density<double>), c->device));
         k_density<double><<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi, c->d_P, c->d_rho);
     } else if (c->tc_ready) {
-        DFTG_TRY_L(launch_density_tc(c, with_scale));
+        DFTG_TRY_L(launch_density_tc(c));
     } else if (c->dt_ready) {
         DFTG_TRY_L(launch_density_tt(c));
     } else {

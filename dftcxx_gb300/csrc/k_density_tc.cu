@@ -65,9 +65,7 @@ struct TcShared {
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restrict__ Aslices,
              const int *__restrict__ row_exp, const unsigned char *__restrict__ Bslices,
-             const int *__restrict__ col_exp, double *__restrict__ rho, int *__restrict__ err,
-             const double *__restrict__ wt, double charge, double *__restrict__ part,
-             double *__restrict__ scal, int *__restrict__ counter)
+             const int *__restrict__ col_exp, double *__restrict__ rho, int *__restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const uint32_t a_slice_bytes = (uint32_t)kTcTile * KP * 2;
@@ -79,8 +77,6 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
     __shared__ int s_texp[kTcMaxK];
     __shared__ int s_fail;
     __shared__ float2 s_half[kTcTile];            // (S, E) of the second column half, per row
-    __shared__ double s_nraw[2 * kTcTile];        // with wt: per-row sums of w rho_raw, then the CTA sums
-    __shared__ int s_lastcta;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -182,20 +178,15 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
         const int half = (warp - 2) >> 2;       // column blocks half, half + 2, ...
         const int r = q * 32 + lane;            // row of the tile = TMEM lane
         const int kc = KP / 8;
-        double nraw = 0.0;                      // with wt: this row's sum of w rho_raw over the CTA's tiles
         for (int it = 0; it < my_tiles; ++it) {
             const int s = it & 1, n = it >> 1;
-            const int tile = (int)blockIdx.x + it * (int)gridDim.x;
-            const size_t p = (size_t)tile * kTcTile + r;
-            // the row's scale exponent and weight are loaded before the wait, so
-            // their latency overlaps it
-            const int ep = half == 0 ? row_exp[p] : 0;
-            const double wp = (wt && half == 0) ? __ldcs(wt + p) : 0.0;
             bool ok = mbar_wait(&sh->tmem_full[s], (uint32_t)(n & 1));
             if (!ok) { atomicExch(err, 4); s_fail = 1; }
             epi8_bar_sync();
             if (s_fail) break;
             tc_fence_after();
+            const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+            const size_t p = (size_t)tile * kTcTile + r;
             const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
             const uint32_t ta0 = tmem + (uint32_t)(s * 256) + ((uint32_t)(q * 32) << 16);
             // two independent compensated accumulators (even / odd columns)
@@ -261,36 +252,8 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
                 const float w = St + o.x;
                 const float bq = w - St;
                 const float e = Et + o.y + (St - (w - bq)) + (o.x - bq);
-                const double raw = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
-                rho[p] = raw;
-                nraw += wp * raw;
-            }
-        }
-        if (wt) {                          // every epilogue warp, also after an expired wait
-            // the integral of w rho_raw: rows in order per CTA, CTAs in order in
-            // the last one, which also forms the correction factor charge / integral
-            if (half == 0) s_nraw[r] = nraw;
-            epi8_bar_sync();
-            if (threadIdx.x == 64) {
-                double t = 0.0;
-                for (int i = 0; i < kTcTile; ++i) t += s_nraw[i];
-                part[blockIdx.x] = t;
-                __threadfence();
-                s_lastcta = atomicAdd(counter, 1) == (int)gridDim.x - 1;
-            }
-            epi8_bar_sync();
-            if (s_lastcta) {
-                __threadfence();
-                const int e = threadIdx.x - 64;                     // 0 .. 255 over the epilogue warps
-                for (int b = e; b < (int)gridDim.x; b += 256) s_nraw[b] = __ldcg(part + b);
-                epi8_bar_sync();
-                if (threadIdx.x == 64) {
-                    double total = 0.0;
-                    for (int b = 0; b < (int)gridDim.x; ++b) total += s_nraw[b];
-                    scal[kScalSum] = total;
-                    scal[kScalScale] = charge / total;
-                    *counter = 0;
-                }
+                const int ep = row_exp[p];
+                rho[p] = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
             }
         }
     }
@@ -404,24 +367,15 @@ int density_tc_setup(dftg_ctx *c)
     return DFTG_OK;
 }
 
-int launch_density_tc(dftg_ctx *c, bool with_scale)
+int launch_density_tc(dftg_ctx *c)
 {
     k_slice_P<<<(c->tc_NP + 3) / 4, 128, 0, c->stream>>>(c->nbf, c->tc_KP, c->tc_NP, c->d_P,
                                                          reinterpret_cast<__nv_bfloat16 *>(c->d_tcB), c->d_tc_colexp);
     DFTG_LAUNCH_CHECK();
-    // with_scale: the integral of w rho_raw and the correction factor, summed in
-    // the epilogue, for the point kernel that follows
-    double charge = 0.0;
-    for (int a = 0; a < c->natoms; ++a) charge += (double)c->Z[a];
-    if (with_scale && ((size_t)c->tc_grid > c->red_elems || c->tc_grid > 2 * kTcTile)) {
-        set_error("reduction buffer too small for %d density CTAs", c->tc_grid);
-        return DFTG_ERR_STATE;
-    }
     const int ntiles = (int)(c->npad / kTcTile);
     k_density_tc<<<c->tc_grid, kTcThreads, density_tc_smem(c->tc_KP, c->tc_NP), c->stream>>>(
         c->nbf, c->tc_KP, c->tc_NP, ntiles, reinterpret_cast<const unsigned char *>(c->d_tcA), c->d_tc_rowexp,
-        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag,
-        with_scale ? c->d_w : nullptr, charge, c->d_red, c->d_scal, c->d_counters + kCntAtoms);
+        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }
