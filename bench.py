@@ -23,8 +23,9 @@ arms.
             bandwidth; the layout bytes it actually streams as a second field
   adjoint   alkanes CnH2n+2 / 6-31G / 50 x 194: mixed forward and backward
             (dE/dP, forces) times and force errors (outside the headline)
-  batched   64 jittered small molecules in one CUDA graph vs per-molecule
-            builds, with the batch autotuner (outside the headline)
+  batched   64 jittered small molecules: one persistent launch per step over
+            all molecules, and one CUDA graph of per-molecule branches, vs
+            per-molecule builds, with the batch autotuner (outside the headline)
   synthetic 2M points x 512 primitives: rho, LDA and XC in FP64 and mixed
             (outside the headline)
 
@@ -583,7 +584,8 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
     STO-3G and 6-31G alternating by round, 50 x 194 grid, each at its own
     core-Hamiltonian density.  Throughput in grid builds (SCF iterations) per
     second: the per-molecule FP64 build, the per-molecule mixed build, and the
-    whole batch in one graph, before and after the batch autotuner."""
+    whole batch as persistent launches (one per step) and as one graph of
+    per-molecule branches, before and after the batch autotuner."""
     import torch
     from dftcxx_gb300 import _lib
     from dftcxx_gb300.grid import MolecularGrid, Batch
@@ -635,32 +637,47 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
     torch.cuda.synchronize(dev)
     for g in grids:   # every context back on its own stream: the graph's branches run concurrently
         g.set_stream(0)
-    b = Batch(grids)
+    b = Batch(grids, mode="graph")
     Js = [o[:g.nbf * g.nbf] for g, o in zip(grids, outs)]
     XCs = [o[g.nbf * g.nbf:2 * g.nbf * g.nbf] for g, o in zip(grids, outs)]
     Ss = [o[2 * g.nbf * g.nbf:] for g, o in zip(grids, outs)]
     run = lambda: b.build(dPs, Js, XCs, Ss, stream=stream.cuda_stream)
+    # graph of branches, then the persistent launches, at the set-up launch shapes
     run(); run()
-    bat = _event_ms(run, reps, stream)
+    bat_g = _event_ms(run, reps, stream)
+    b.set_mode("persistent")
+    run(); run()
+    bat_p = _event_ms(run, reps, stream)
+    b.status()
+    persistent = b.persistent_active()
+    # each form autotuned (the persistent form last, so its shapes stay)
+    b.set_mode("graph")
+    run()
+    tune_g = b.autotune(reps=5)
+    run(); run()
+    bat_gt = _event_ms(run, reps, stream)
+    b.set_mode("persistent")
+    run()
+    t_tune = time.perf_counter()
+    tune_p = b.autotune(reps=5)
+    tune_s = time.perf_counter() - t_tune
+    run(); run()
+    bat_pt = _event_ms(run, reps, stream)
     # one replay with host wall-clock around it (synchronised on both sides)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     run()
     stream.synchronize()
     bat_wall = (time.perf_counter() - t0) * 1e3
-    t_tune = time.perf_counter()
-    tune_ms = b.autotune(reps=5)
-    tune_s = time.perf_counter() - t_tune
-    # the tuned batch does the work: after its graph is captured, outputs
-    # zeroed, one replay, then per-molecule builds of the same launch shapes
-    # must reproduce them bit for bit
-    run(); run()
+    b.status()
+    # the tuned persistent batch does the work: outputs zeroed, one replay, then
+    # per-molecule builds of the same launch shapes must reproduce it bit for bit
     torch.cuda.synchronize(dev)
     for o in outs:
         o.zero_()
     torch.cuda.synchronize(dev)
     run()
-    torch.cuda.synchronize(dev)
+    b.status()
     got = [o.clone() for o in outs]
     nonzero = all(bool(o.abs().max() > 0) for o in got)
     for g in grids:
@@ -668,11 +685,6 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
     sequential()
     torch.cuda.synchronize(dev)
     diff = max(float((a - b_).abs().max() / max(b_.abs().max(), 1e-300)) for a, b_ in zip(got, outs))
-    for g in grids:
-        g.set_stream(0)
-    run(); run()   # the contexts' streams are part of the graph key: recapture
-    bat_t = _event_ms(run, reps, stream)
-    torch.cuda.synchronize(dev)
     shapes = sorted({g.launch_shape for g in grids})
     b.close()
     for g in grids:
@@ -681,11 +693,14 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
             "atoms": natoms, "basis_functions": nbfs, "grid_points": npts,
             "fp64_per_molecule_builds_per_s": nmol / (seq64 * 1e-3),
             "mixed_per_molecule_builds_per_s": nmol / (seqmx * 1e-3),
-            "mixed_batched_graph_builds_per_s": nmol / (bat * 1e-3),
-            "mixed_batched_autotuned_builds_per_s": nmol / (bat_t * 1e-3),
-            "ms_per_batch": {"fp64_sequential": seq64, "mixed_sequential": seqmx, "mixed_graph": bat,
-                             "mixed_graph_autotuned": bat_t, "mixed_graph_host_wall_one_replay": bat_wall,
-                             "autotuner_best": tune_ms},
+            "mixed_batched_persistent_builds_per_s": nmol / (bat_pt * 1e-3),
+            "mixed_batched_graph_builds_per_s": nmol / (bat_gt * 1e-3),
+            "persistent_launches_ran": persistent,
+            "launches_per_batch": {"persistent": 10, "graph": "about 10 per molecule"},
+            "ms_per_batch": {"fp64_sequential": seq64, "mixed_sequential": seqmx, "mixed_graph": bat_g,
+                             "mixed_graph_autotuned": bat_gt, "mixed_persistent": bat_p,
+                             "mixed_persistent_autotuned": bat_pt, "mixed_persistent_host_wall_one_replay": bat_wall,
+                             "autotuner_best_graph": tune_g, "autotuner_best_persistent": tune_p},
             "cross_atom_evaluations": cross_evals,
             "max_rel_diff_batch_vs_single": diff, "batch_outputs_nonzero": nonzero,
             "autotuned_shapes": [list(s) for s in shapes], "autotune_s": tune_s, "setup_s": setup_s}

@@ -112,6 +112,10 @@ SIGNATURES = {
     "dftg_batch_autotune": [ctypes.c_void_p, ctypes.c_int, _dp],
     "dftg_batch_create": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)],
     "dftg_batch_destroy": [ctypes.c_void_p],
+    "dftg_batch_set_mode": [ctypes.c_void_p, ctypes.c_int],
+    "dftg_batch_get_mode": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)],
+    "dftg_batch_status": [ctypes.c_void_p],
+    "dftg_batch_selftest_wait": [ctypes.c_void_p, ctypes.c_double],
     "dftg_batch_fock_build_device": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.c_void_p],

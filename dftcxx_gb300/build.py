@@ -20,7 +20,7 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-rela
            "-I" + os.path.join(os.path.dirname(HERE), "include")]
 SOURCES = ["dftg_capi.cu", "k_grid.cu", "k_density.cu", "k_hartree.cu", "k_contract.cu", "k_integrals.cu",
            "k_contract_noalloc.cu", "k_density_tc.cu", "k_contract_tc.cu", "k_contract_tt.cu", "k_density_tt.cu", "k_adjoint.cu",
-           "k_scf.cu"]
+           "k_scf.cu", "k_batch.cu"]
 
 
 def nvcc():

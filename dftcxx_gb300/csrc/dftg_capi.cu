@@ -1242,18 +1242,25 @@ int dftg_nuclear_repulsion(const dftg_ctx *c, double *enuc)
 
 // ------------------------------------------------------------------ batches
 
+constexpr unsigned long long kBatchWaitNs = 2000000000ull;   // limit of the persistent launches' waits: 2 s
+
 struct dftg_batch {
     std::vector<dftg_ctx *> ctx;
-    std::vector<cudaEvent_t> join;      // per context: end of its branch
+    std::vector<cudaEvent_t> join;      // per context: end of its branch (graph of branches)
     cudaEvent_t fork = nullptr;
     cudaGraphExec_t exec = nullptr;
-    std::vector<const void *> key;      // buffers, masks and stream the graph was captured with
+    std::vector<const void *> key;      // buffers, masks, shapes, mode and stream the graph was captured with
     bool warm = false;
+    int mode = DFTG_BATCH_PERSISTENT;
+    dftg::BatchPlan *plan = nullptr;    // persistent launches: device records of the current key
+    cudaStream_t last = nullptr;        // stream of the last launch
 };
 
 static void batch_free(dftg_batch *b)
 {
     if (!b) return;
+    if (b->last) cudaStreamSynchronize(b->last);
+    dftg::batch_plan_free(b->plan);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->fork) cudaEventDestroy(b->fork);
     for (cudaEvent_t e : b->join)
@@ -1329,8 +1336,11 @@ extern "C" int dftg_batch_fock_build_device(dftg_batch *b, const double *const *
     }
     DFTG_CUDA(cudaSetDevice(b->ctx[0]->device));
     cudaStream_t s0 = stream ? reinterpret_cast<cudaStream_t>(stream) : b->ctx[0]->stream;
+    bool persist = b->mode == DFTG_BATCH_PERSISTENT;
+    for (int i = 0; i < n && persist; ++i) persist = dftg::batch_group_eligible(b->ctx[i]);
     std::vector<const void *> key;
     key.push_back(s0);
+    key.push_back(reinterpret_cast<const void *>((uintptr_t)(persist ? 1 : 0)));
     for (int i = 0; i < n; ++i) {
         key.push_back(P_devs[i]);
         key.push_back(J_devs ? J_devs[i] : nullptr);
@@ -1342,12 +1352,39 @@ extern "C" int dftg_batch_fock_build_device(dftg_batch *b, const double *const *
         key.push_back(reinterpret_cast<const void *>((uintptr_t)b->ctx[i]->ct_grid));
         key.push_back(reinterpret_cast<const void *>((uintptr_t)b->ctx[i]->ct_nst));
     }
-    if (b->exec && key != b->key) {
-        cudaGraphExecDestroy(b->exec);
+    if (key != b->key) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
         b->warm = false;
+        if (b->plan) {                  // its device records may still be read by a running batch
+            if (b->last) DFTG_CUDA(cudaStreamSynchronize(b->last));
+            dftg::batch_plan_free(b->plan);
+            b->plan = nullptr;
+        }
     }
+    if (persist && !b->plan)
+        DFTG_TRY(dftg::batch_plan_create(b->ctx.data(), n, P_devs, J_devs, XC_devs, scalars_devs, &b->plan));
+    // the persistent launches run on s0 alone: s0 first waits for the work queued
+    // on the contexts' own streams (set-up, earlier builds), and those streams
+    // wait for the batch afterwards (outside any capture)
+    auto order_before = [&]() -> int {
+        if (!persist) return DFTG_OK;
+        for (int i = 0; i < n; ++i)
+            if (b->ctx[i]->stream != s0) {
+                DFTG_CUDA(cudaEventRecord(b->join[i], b->ctx[i]->stream));
+                DFTG_CUDA(cudaStreamWaitEvent(s0, b->join[i], 0));
+            }
+        return DFTG_OK;
+    };
+    auto order_after = [&]() -> int {
+        if (!persist) return DFTG_OK;
+        DFTG_CUDA(cudaEventRecord(b->fork, s0));
+        for (dftg_ctx *c : b->ctx)
+            if (c->stream != s0) DFTG_CUDA(cudaStreamWaitEvent(c->stream, b->fork, 0));
+        return DFTG_OK;
+    };
     auto enqueue = [&]() -> int {
+        if (persist) return dftg::batch_plan_enqueue(b->plan, s0, -1, kBatchWaitNs, false);
         // fork: every branch waits for s0, s0 waits for every branch
         DFTG_CUDA(cudaEventRecord(b->fork, s0));
         for (int i = 0; i < n; ++i) {
@@ -1362,11 +1399,26 @@ extern "C" int dftg_batch_fock_build_device(dftg_batch *b, const double *const *
         }
         return DFTG_OK;
     };
+    auto mark_built = [&]() {
+        for (dftg_ctx *c : b->ctx) {
+            c->rho_scaled = true;
+            if (persist) c->rw_ready = true;
+            c->have_density = true;
+            c->have_hartree = true;
+            c->have_build = true;
+            c->fwd_mask = c->prec_mask;
+        }
+        b->last = s0;
+    };
     if (!b->exec) {
-        if (!b->warm || key != b->key) {
+        if (!b->warm) {
             b->warm = true;
             b->key = key;
-            return enqueue();
+            DFTG_TRY(order_before());
+            const int rc = enqueue();
+            if (rc != DFTG_OK) return rc;
+            mark_built();
+            return order_after();
         }
         cudaGraph_t g = nullptr;
         DFTG_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
@@ -1384,13 +1436,69 @@ extern "C" int dftg_batch_fock_build_device(dftg_batch *b, const double *const *
             return cuda_fail(ei, "cudaGraphInstantiate", __FILE__, __LINE__);
         }
     }
+    DFTG_TRY(order_before());
     DFTG_CUDA(cudaGraphLaunch(b->exec, s0));
+    mark_built();
+    return order_after();
+}
+
+extern "C" int dftg_batch_set_mode(dftg_batch *b, int mode)
+{
+    if (!b) { set_error("null batch"); return DFTG_ERR_ARG; }
+    if (mode != DFTG_BATCH_PERSISTENT && mode != DFTG_BATCH_GRAPH) { set_error("unknown batch mode %d", mode); return DFTG_ERR_ARG; }
+    b->mode = mode;
+    return DFTG_OK;
+}
+
+extern "C" int dftg_batch_get_mode(const dftg_batch *b, int *persistent_active)
+{
+    if (!b) { set_error("null batch"); return DFTG_ERR_ARG; }
+    if (persistent_active) *persistent_active = b->plan != nullptr && b->mode == DFTG_BATCH_PERSISTENT ? 1 : 0;
+    return b->mode;
+}
+
+// A CTA whose wait gave up stops, leaving the last-block counters of the
+// reductions it skipped part-way: zero them all (the stream is synchronised)
+static int reset_counters(dftg_batch *b)
+{
+    for (dftg_ctx *c : b->ctx) DFTG_CUDA(cudaMemset(c->d_counters, 0, sizeof(int) * dftg::kNumCounters));
+    return DFTG_OK;
+}
+
+extern "C" int dftg_batch_status(dftg_batch *b)
+{
+    if (!b) { set_error("null batch"); return DFTG_ERR_ARG; }
+    DFTG_CUDA(cudaSetDevice(b->ctx[0]->device));
+    int code = 0;
+    if (b->plan && b->last) DFTG_TRY(dftg::batch_plan_take_error(b->plan, b->last, &code));
+    int rc = DFTG_OK;
     for (dftg_ctx *c : b->ctx) {
-        c->rho_scaled = true;
-        c->have_density = true;
-        c->have_hartree = true;
-        c->have_build = true;
-    c->fwd_mask = c->prec_mask;
+        const int r = sync_scalars(c);      // also reads and clears the context's bounded-wait flag
+        if (r != DFTG_OK && rc == DFTG_OK) rc = r;
+    }
+    if (code) {
+        DFTG_TRY(reset_counters(b));
+        set_error("a bounded wait of the batch's persistent launches expired (code %d); results of this batch are invalid",
+                  code);
+        return DFTG_ERR_TIMEOUT;
+    }
+    return rc;
+}
+
+extern "C" int dftg_batch_selftest_wait(dftg_batch *b, double limit_ms)
+{
+    if (!b) { set_error("null batch"); return DFTG_ERR_ARG; }
+    if (!(limit_ms > 0.0 && limit_ms <= 2000.0)) { set_error("limit_ms %g out of (0, 2000]", limit_ms); return DFTG_ERR_ARG; }
+    if (!b->plan || !b->last) { set_error("self-test before a persistent batch build"); return DFTG_ERR_STATE; }
+    DFTG_CUDA(cudaSetDevice(b->ctx[0]->device));
+    DFTG_TRY(dftg::batch_plan_enqueue(b->plan, b->last, 0, (unsigned long long)(limit_ms * 1e6), true));
+    int code = 0;
+    DFTG_TRY(dftg::batch_plan_take_error(b->plan, b->last, &code));
+    for (dftg_ctx *c : b->ctx) c->have_build = c->have_hartree = false;   // the self-test left partial results
+    if (code) {
+        DFTG_TRY(reset_counters(b));
+        set_error("a bounded wait of the batch's persistent launches expired (code %d)", code);
+        return DFTG_ERR_TIMEOUT;
     }
     return DFTG_OK;
 }

@@ -96,21 +96,112 @@ __device__ __forceinline__ double block_sum(double v, double *sh)
     return s;
 }
 
-// True in exactly one block: the last to get here.  Every block's global writes
-// made before the call are visible to that block (read them with __ldcg).  The
-// counter is reset for the next launch.
-__device__ __forceinline__ bool last_block(int *counter, int *s_flag)
+// True in exactly one of nblocks blocks: the last to get here.  Every block's
+// global writes made before the call are visible to that block (read them with
+// __ldcg).  The counter is reset for the next launch.
+__device__ __forceinline__ bool last_block_of(int *counter, int nblocks, int *s_flag)
 {
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         const int t = atomicAdd(counter, 1);
-        *s_flag = (t == (int)gridDim.x - 1) ? 1 : 0;
+        *s_flag = (t == nblocks - 1) ? 1 : 0;
         if (*s_flag) *counter = 0;
     }
     __syncthreads();
     if (*s_flag) __threadfence();
     return *s_flag != 0;
+}
+
+// ---------------------------------------------------------------- grouped launches
+// A batch of molecules runs each step of the build as one persistent launch.
+// The launch's work items 0 .. nitems - 1 are the blocks of the molecules' own
+// launches, molecule-major: item i belongs to molecule m with prefix[m] <= i <
+// prefix[m + 1] and is its block vb = i - prefix[m] of nvb = prefix[m + 1] -
+// prefix[m].  Every CTA takes `take` consecutive items at a time from a device
+// counter (zero at the start of the launch) until none are left, and runs each
+// item as that block of the molecule's own launch, so each molecule's
+// arithmetic and reduction order are those of its single build.
+struct GroupQueue {
+    const int *prefix;    // [nmol + 1], non-decreasing, prefix[0] = 0, prefix[nmol] = nitems
+    int nmol, nitems, take;
+    int *head;            // items handed out so far
+};
+
+// molecule of item i: the largest m < nmol with prefix[m] <= i (its range holds i)
+__device__ __forceinline__ int gq_molecule(const GroupQueue &q, int i)
+{
+    int lo = 0, hi = q.nmol - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(q.prefix + mid) <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The CTA's item loop: f(m, vb, nvb) runs one item with every thread of the
+// CTA and returns false to stop the CTA (a bounded wait that gave up).  s_item:
+// one int of shared memory.
+template <typename F>
+__device__ __forceinline__ void gq_run(const GroupQueue &q, int *s_item, F &&f)
+{
+    for (;;) {
+        __syncthreads();                        // the previous item is done with shared memory and s_item
+        if (threadIdx.x == 0) *s_item = atomicAdd(q.head, q.take);
+        __syncthreads();
+        const int i0 = *s_item;
+        if (i0 >= q.nitems) return;
+        const int i1 = min(q.nitems, i0 + q.take);
+        for (int i = i0; i < i1; ++i) {
+            const int m = gq_molecule(q, i);
+            const int b0 = __ldg(q.prefix + m);
+            if (i > i0) __syncthreads();
+            if (!f(m, i - b0, __ldg(q.prefix + m + 1) - b0)) return;
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// *flag = v with release semantics at GPU scope (after the caller's writes)
+__device__ __forceinline__ void flag_release(int *flag, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(flag), "r"(v) : "memory");
+}
+
+// Bounded wait of the CTA until *flag >= v: thread 0 polls with acquire loads,
+// gives up after limit_ns of wall-clock time (or 2^26 polls whatever the
+// timer).  Block-uniform result; s_ok: one int of shared memory.
+__device__ __forceinline__ bool wait_flag_ge(const int *flag, int v, unsigned long long limit_ns, int *s_ok)
+{
+    if (threadIdx.x == 0) {
+        int ok = 0;
+        const unsigned long long t0 = globaltimer_ns();
+        for (unsigned it = 0; it < (1u << 26); ++it) {
+            int cur;
+            asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(cur) : "l"(flag) : "memory");
+            if (cur >= v) { ok = 1; break; }
+            if ((it & 15u) == 0u && globaltimer_ns() - t0 > limit_ns) break;
+            __nanosleep(128);
+        }
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+// True in exactly one block: the last to get here.  Every block's global writes
+// made before the call are visible to that block (read them with __ldcg).  The
+// counter is reset for the next launch.
+__device__ __forceinline__ bool last_block(int *counter, int *s_flag)
+{
+    return last_block_of(counter, (int)gridDim.x, s_flag);
 }
 
 // counters of the last-block reductions
@@ -316,6 +407,126 @@ enum {
 };
 inline size_t scal_elems(int natoms) { return 8 + (size_t)natoms; }
 
+// CTAs of a grouped launch: every CTA resident (occ per SM on nsm SMs), and no
+// more than the queue has runs of items
+inline int group_grid(const GroupQueue &q, int occ, int nsm)
+{
+    const int runs = (q.nitems + q.take - 1) / q.take;
+    const int resident = (occ > 0 ? occ : 1) * nsm;
+    return runs < resident ? runs : resident;
+}
+
+// ---------------------------------------------------------------- steps of the mixed build
+// The arguments of one molecule's launch of each step, as one record: the
+// single build passes it by value, a batch's grouped launch reads molecule m's
+// record from a device array (one per molecule).
+struct SlicePArgs {            // P -> BF16 slices (density operand)
+    int nbf, KP, NP;
+    const double *P;
+    double *Pcopy;             // also copies P here when not null (the context's own P)
+    void *B;
+    int *col_exp;
+};
+struct DensTcArgs {            // rho on the tensor cores
+    int nbf, KP, NP, ntiles;
+    const unsigned char *A;
+    const int *row_exp;
+    const unsigned char *B;
+    const int *col_exp;
+    double *rho;
+    int *err;
+};
+struct SumsArgs {              // per-atom sums of w rho, correction factor
+    size_t per_atom;
+    int cpa, natoms, mode;
+    const double *w, *rho;
+    double *part;
+    const double *atoms;
+    double *scal;
+    int *counter;
+    int *done;                 // set to 1 by the last block once scal is written (grouped launch), or null
+};
+struct LdaArgs {               // LDA point kernel
+    size_t npad;
+    double *rho;
+    const double *w;
+    double *scal;
+    int apply_scale, want64, want_n;
+    double *cxc;
+    float *cxc32;
+    double *part;
+    int *counter;
+    const double *wb;
+    float *rw32;
+};
+struct MpArgs {                // multipole chain of one atom cell per (cell, l group)
+    int natoms, cell0, N, nang, lmax, ngroup, want64;
+    const float *rw32;
+    size_t npad;
+    const double *rho, *wb, *w;
+    const float *Ywt32, *maps;
+    double *scal, *U;
+    float *U32, *U32T;
+    double *spl;
+    float *splm;
+};
+struct VcbArgs {               // cross-atom pair contributions, one block per bin task
+    int nrad, lmax;
+    const int4 *tasks;
+    const float4 *pgeo;
+    const float2 *ptk;
+    const float *splm;
+    float2 *out;
+};
+struct GoArgs {                // own-cell potential + pair sums per point, cj, E_J
+    size_t npts, npad, uhalf;
+    int natoms, cell0, nrad, nang, nlm, nslab, nsplit, scaled;
+    const int *pos;
+    const float2 *pairv;
+    const float *U32T, *Y32;
+    const double *invr, *W, *rho;
+    double *V, *cj;
+    float *cj32;
+    double *part, *scal;
+    int *counter;
+};
+struct CexpArgs {              // per-chunk exponent bounds of the point coefficients
+    int nkb, kbpc;
+    const float *cxc, *cj, *winv;
+    int2 *cexp;
+};
+struct CtArgs {                // XC and J contraction on the tensor cores
+    int nbf, AR, NP, nst, spart, nkb, kbpc, nchunk;
+    const unsigned char *aslices;
+    const int *rowexp, *swexp;
+    const int2 *cexp;
+    const float *cxc, *cj;
+    float2 *part;
+    int *err;
+};
+struct SumsLdaCtl {            // the batch's fused atom-sum + point-kernel launch
+    int *head;                 // one queue over both item ranges
+    int *done;                 // [nmol] set by each molecule's last atom-sum block
+    int *err;                  // code 21 when a wait gave up
+    unsigned long long limit_ns;
+    int stall_mol;             // -1, or the molecule whose waits cannot end (self-test)
+};
+// one molecule's launch of a step: its arguments, blocks and dynamic shared memory
+template <typename A>
+struct StepLaunch {
+    A args;
+    int blocks = 0;
+    size_t smem = 0;
+};
+struct RedArgs {               // sum of the contraction partials, symmetric XC and J
+    int nbf, nparts, want_xc, want_j;
+    const float2 *part;
+    double *XC, *J;
+    double *XC2, *J2;          // second copies (a batch's output buffers), or null
+    const double *scal;        // with sc: copy E_xc, N, E_J to sc[0..2] (block 0)
+    double *sc;
+};
+
 // Raise a kernel's dynamic shared-memory limit to the device maximum (minus
 // its static shared memory), once per kernel and device.  The limit is a
 // property of the function, shared by every context, so it is never lowered.
@@ -375,6 +586,39 @@ int ct_setup_tables(dftg_ctx *c, int AR, int nkb, int kbpc, int nchunk, int *row
                     void *A);
 int ct_launch_cexp(dftg_ctx *c, int nkb, int kbpc, int nchunk, const float *cx, const float *cy, const float *winv,
                    int2 *cexp);
+// One molecule's launch of each step of the mixed build (its arguments, blocks
+// and shared memory; the single build launches exactly these), and the batch's
+// grouped launch of each step over all molecules (device argument arrays, one
+// queue per launch).
+StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy);
+StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c);
+StepLaunch<SumsArgs> step_atom_sums(const dftg_ctx *c, int mode);
+StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n);
+StepLaunch<MpArgs> step_multipole(const dftg_ctx *c, bool rw_ready);
+StepLaunch<VcbArgs> step_vcross_bins(const dftg_ctx *c);
+StepLaunch<GoArgs> step_gather_own(const dftg_ctx *c, bool rho_scaled);
+StepLaunch<CexpArgs> step_cexp(const dftg_ctx *c, const float *cx, const float *cy);
+StepLaunch<CtArgs> step_contract_tc(const dftg_ctx *c, const float *cx, const float *cy);
+StepLaunch<RedArgs> step_contract_reduce(const dftg_ctx *c, bool want_xc, bool want_j, double *XC, double *J);
+int group_slice_P(const SlicePArgs *d_args, const GroupQueue &q, int nsm, cudaStream_t st);
+int group_density_tc(const DensTcArgs *d_args, const GroupQueue &q, size_t smem, int device, int nsm, cudaStream_t st);
+int group_sums_lda(const SumsArgs *d_sums, const GroupQueue &qs, const LdaArgs *d_lda, const GroupQueue &ql,
+                   const SumsLdaCtl &ctl, int nsm, cudaStream_t st);
+int group_multipole(const MpArgs *d_args, const GroupQueue &q, size_t smem, int device, int nsm, cudaStream_t st);
+int group_vcross_bins(const VcbArgs *d_args, const GroupQueue &q, int lmax, size_t smem, int nsm, cudaStream_t st);
+int group_gather_own(const GoArgs *d_args, const GroupQueue &q, size_t smem, int device, int nsm, cudaStream_t st);
+int group_cexp(const CexpArgs *d_args, const GroupQueue &q, int nsm, cudaStream_t st);
+int group_contract_tc(const CtArgs *d_args, const GroupQueue &q, size_t smem, int device, int nsm, cudaStream_t st);
+int group_contract_reduce(const RedArgs *d_args, const GroupQueue &q, int nsm, cudaStream_t st);
+// k_batch.cu: the persistent launches of a batch of mixed builds
+struct BatchPlan;
+bool batch_group_eligible(const dftg_ctx *c);
+int batch_plan_create(dftg_ctx *const *ctx, int n, const double *const *P, double *const *J, double *const *XC,
+                      double *const *sc, BatchPlan **out);
+void batch_plan_free(BatchPlan *bp);
+int batch_plan_enqueue(const BatchPlan *bp, cudaStream_t st, int stall_mol, unsigned long long limit_ns,
+                       bool sums_lda_only);
+int batch_plan_take_error(const BatchPlan *bp, cudaStream_t st, int *code);
 // k_contract_tt.cu
 int contract_tt_setup(dftg_ctx *c);
 int launch_contract_tt_bounds(dftg_ctx *c, const float *cx, const float *cy);

@@ -69,6 +69,7 @@ struct CtShared {
     uint64_t tmem_full, tmem_empty, drain;
     uint32_t tmem_base;
     int fail;
+    int item;                              // the grouped launch's queue position (broadcast)
 };
 
 __device__ __forceinline__ void ct_epi_bar()   // named barrier 1 over the epilogue warps
@@ -122,12 +123,12 @@ __device__ __forceinline__ void unpack8(uint4 u, float (&v)[8])
 }
 
 // per chunk: exponent bounds of max |c_xc / w| and max |c_j / w| (block per chunk)
-__global__ void __launch_bounds__(256) k_ct_cexp(int nkb, int kb_per_chunk, const float *__restrict__ cxc,
-                                                 const float *__restrict__ cj, const float *__restrict__ winv,
-                                                 int2 *__restrict__ cexp)
+__device__ __forceinline__ void ct_cexp_block(const CexpArgs A, int ch)
 {
+    const int nkb = A.nkb, kb_per_chunk = A.kbpc;
+    const float *__restrict__ cxc = A.cxc, *__restrict__ cj = A.cj, *__restrict__ winv = A.winv;
+    int2 *__restrict__ cexp = A.cexp;
     __shared__ float sx[8], sj[8];
-    const int ch = blockIdx.x;
     const size_t p0 = (size_t)ch * kb_per_chunk * kCtKS;
     const size_t p1 = (size_t)min(nkb, (ch + 1) * kb_per_chunk) * kCtKS;
     float mx = 0.f, mj = 0.f;
@@ -155,6 +156,20 @@ __global__ void __launch_bounds__(256) k_ct_cexp(int nkb, int kb_per_chunk, cons
     }
 }
 
+constexpr int kCexpThreads = 256;
+
+__global__ void __launch_bounds__(kCexpThreads) k_ct_cexp(const CexpArgs a) { ct_cexp_block(a, (int)blockIdx.x); }
+
+__global__ void __launch_bounds__(kCexpThreads) k_ct_cexp_group(const CexpArgs *__restrict__ args, GroupQueue q)
+{
+    __shared__ int s_item;
+    gq_run(q, &s_item, [&](int m, int vb, int) {
+        const CexpArgs a = args[m];
+        ct_cexp_block(a, vb);
+        return true;
+    });
+}
+
 // Stage layout in shared memory: the three A slices packed at a stride of AR
 // rows (AR = nbf rounded up to 8) -- the MMA reads 128 rows from each slice
 // start, and rows >= AR (the next slice, or the tail) only feed accumulator
@@ -171,13 +186,28 @@ __host__ __device__ constexpr uint32_t ct_stage_bytes(int NP, int AR)
     return ct_a_region_bytes(AR) + (uint32_t)kCtSlices * ct_b_slice_bytes(NP) + 2 * kCtKS * 4;
 }
 
-__global__ void __launch_bounds__(kCtThreads, 1)
-k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_chunk, int nchunk,
-              const unsigned char *__restrict__ aslices, const int *__restrict__ rowexp,
-              const int *__restrict__ swexp, const int2 *__restrict__ cexp, const float *__restrict__ cxc,
-              const float *__restrict__ cj, float2 *__restrict__ part, int *__restrict__ err)
+// One CTA's share of one molecule's chunks (vb, vb + nvb, ...): zeroes the
+// operand stages, initialises the mbarriers, runs the roles and invalidates the
+// mbarriers again; the caller owns the kCtTmemCols TMEM columns at tmem.
+// Returns false (block-uniform) when a bounded wait gave up.
+// the CTA's mbarriers and TMEM address (one instance in every kernel that uses them)
+__shared__ CtShared ct_sh;
+
+// G: a grouped launch's item (vb, nvb given); else the CTA of a single launch
+// (vb, nvb read from blockIdx / gridDim where used, so they hold no registers)
+template <bool G>
+__device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb_, uint32_t tmem)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
+    CtShared *sh = &ct_sh;
+    const int nbf = A.nbf, AR = A.AR, NP = A.NP, nst = A.nst, spart = A.spart, nkb = A.nkb;
+    const int kb_per_chunk = A.kbpc, nchunk = A.nchunk;
+    const unsigned char *__restrict__ aslices = A.aslices;
+    const int *__restrict__ rowexp = A.rowexp, *__restrict__ swexp = A.swexp;
+    const int2 *__restrict__ cexp = A.cexp;
+    const float *__restrict__ cxc = A.cxc, *__restrict__ cj = A.cj;
+    float2 *__restrict__ part = A.part;
+    int *__restrict__ err = A.err;
     const uint32_t a_slice = ct_a_slice_bytes(AR), b_slice = ct_b_slice_bytes(NP);
     const uint32_t a_region = ct_a_region_bytes(AR);
     const uint32_t stage = ct_stage_bytes(NP, AR);
@@ -186,8 +216,6 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
     // CTA partial: XC and J upper triangles, packed (element (mu, nu), mu <= nu, at
     // nu (nu + 1) / 2 + mu), double-float, in shared memory when spart (else in HBM / L2)
     float2 *s_part = reinterpret_cast<float2 *>(smem + (size_t)nst * stage);
-    CtShared *sh = reinterpret_cast<CtShared *>(smem + (size_t)nst * stage +
-                                                (spart ? 2 * ntri * sizeof(float2) : 0));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __shared__ float s_colf[2 * kCtMaxNbf];     // column scales of the current chunk (epilogue)
     __shared__ int s_coloff[2 * kCtMaxNbf];     // packed-triangle offset of column n, row 0
@@ -212,16 +240,9 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
         sh->fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == kCtMmaWarp) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem_base)),
-                     "r"(kCtTmemCols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = sh->tmem_base;
 
     if (warp < kCtProducers) {
         // ------------------------------------------------------------ producers
@@ -235,7 +256,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
         const int g = lane >> 3, mrow = lane & 7;
         int it = 0;
         bool ok = true;
-        for (int ch = blockIdx.x; ch < nchunk && ok; ch += gridDim.x) {
+        for (int ch = (G ? vb_ : (int)blockIdx.x); ch < nchunk && ok; ch += (G ? nvb_ : (int)gridDim.x)) {
             const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
             const int2 ce = cexp[ch];
             const float sx = pow2f(-ce.x), sj = pow2f(-ce.y);
@@ -332,7 +353,7 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
             const uint32_t d_hi = tmem, d_lo = tmem + 256;
             int it = 0, cc = 0;
             bool ok = true;
-            for (int ch = blockIdx.x; ch < nchunk && ok; ch += gridDim.x, ++cc) {
+            for (int ch = (G ? vb_ : (int)blockIdx.x); ch < nchunk && ok; ch += (G ? nvb_ : (int)gridDim.x), ++cc) {
                 if (!mbar_wait(&sh->tmem_empty, (uint32_t)((cc & 1) ^ 1))) { atomicExch(err, 12); sh->fail = 1; break; }
                 tc_fence_after();
                 const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
@@ -381,9 +402,9 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
         const int q = warp & 3;                  // TMEM lane quarter of this warp
         const int h = (warp - kCtEpi0) >> 2;     // column blocks h, h + kCtEpiWarps / 4, ...
         const int r = q * 32 + lane;             // accumulator row = basis function mu
-        float2 *gpart = part + (size_t)blockIdx.x * 2 * ntri;   // this CTA's partial in HBM
+        float2 *gpart = part + (size_t)(G ? vb_ : (int)blockIdx.x) * 2 * ntri;   // this CTA's partial in HBM
         int cc = 0;
-        for (int ch = blockIdx.x; ch < nchunk; ch += gridDim.x, ++cc) {
+        for (int ch = (G ? vb_ : (int)blockIdx.x); ch < nchunk; ch += (G ? nvb_ : (int)gridDim.x), ++cc) {
             const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
             // column scales 2^(s_nu + v - 14) of the chunk in shared memory, row scale 2^e_mu in a register
             {
@@ -466,11 +487,11 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
         if (lane == 0) {
             const uint32_t tx = kCtSlices * a_slice + 2 * kCtKS * 4;
             int it = 0, issued = 0;
-            for (int ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+            for (int ch = (G ? vb_ : (int)blockIdx.x); ch < nchunk; ch += (G ? nvb_ : (int)gridDim.x)) {
                 const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
                 bool ok = true;
                 // L2 prefetch: this chunk's A block (first chunk only) and the next chunk's
-                for (int pc = (ch == (int)blockIdx.x ? ch : ch + (int)gridDim.x); pc <= ch + (int)gridDim.x; pc += (int)gridDim.x) {
+                for (int pc = (ch == (G ? vb_ : (int)blockIdx.x) ? ch : ch + (G ? nvb_ : (int)gridDim.x)); pc <= ch + (G ? nvb_ : (int)gridDim.x); pc += (G ? nvb_ : (int)gridDim.x)) {
                     if (pc >= nchunk) break;
                     const int p0 = pc * kb_per_chunk, p1 = min(nkb, p0 + kb_per_chunk);
                     for (int kb = p0; kb < p1; ++kb)
@@ -501,10 +522,64 @@ k_contract_tc(int nbf, int AR, int NP, int nst, int spart, int nkb, int kb_per_c
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == kCtMmaWarp) {
+    const bool ok = sh->fail == 0;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < nst; ++s) {
+            mbar_inval(&sh->a_full[s]);
+            mbar_inval(&sh->full[s]);
+            mbar_inval(&sh->empty[s]);
+        }
+        mbar_inval(&sh->tmem_full);
+        mbar_inval(&sh->tmem_empty);
+        mbar_inval(&sh->drain);
+    }
+    return ok;
+}
+
+__device__ __forceinline__ void contract_tc_alloc()
+{
+    CtShared *sh = &ct_sh;
+    if ((threadIdx.x >> 5) == kCtMmaWarp) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem_base)),
+                     "r"(kCtTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+}
+
+// after the CTA's last __syncthreads
+__device__ __forceinline__ void contract_tc_free(uint32_t tmem)
+{
+    if ((threadIdx.x >> 5) == kCtMmaWarp) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCtTmemCols) : "memory");
     }
+}
+
+__global__ void __launch_bounds__(kCtThreads, 1) k_contract_tc(const CtArgs args)
+{
+    contract_tc_alloc();
+    const uint32_t tmem = ct_sh.tmem_base;
+    contract_tc_cta<false>(args, 0, 0, tmem);
+    contract_tc_free(tmem);
+}
+
+// the batch's grouped launch: items (molecule, virtual CTA) from the queue,
+// TMEM allocated once for all of them
+__global__ void __launch_bounds__(kCtThreads, 1) k_contract_tc_group(const CtArgs *__restrict__ args, GroupQueue q)
+{
+    contract_tc_alloc();
+    const uint32_t tmem = ct_sh.tmem_base;
+    gq_run(q, &ct_sh.item, [&](int m, int vb, int nvb) {
+        const CtArgs a = args[m];
+        return contract_tc_cta<true>(a, vb, nvb, tmem);
+    });
+    tc_fence_before();
+    __syncthreads();
+    contract_tc_free(tmem);
 }
 
 // ------------------------------------------------------------------ setup
@@ -576,25 +651,22 @@ __global__ void k_ct_slice_A(int nbf, int AR, size_t npad, int nkb, int kb_per_c
 
 static size_t ct_smem(int nst, int NP, int AR, int nbf, bool spart)
 {
-    return (size_t)nst * ct_stage_bytes(NP, AR) + (spart ? (size_t)nbf * (nbf + 1) * sizeof(float2) : 0) +
-           sizeof(CtShared);
+    return (size_t)nst * ct_stage_bytes(NP, AR) + (spart ? (size_t)nbf * (nbf + 1) * sizeof(float2) : 0);
 }
 
-// Sum the double-float CTA partials of every element on or above the diagonal
-// in CTA order (double-float, no FP64 until the final value) and write XC, J
-// symmetrically (column-major).  Block: 32 elements x 32 CTA groups; group g
-// sums CTAs g, g + 32, ...; the 32 group sums are added in a fixed order.
-__global__ void __launch_bounds__(1024) k_contract_tc_reduce(int nbf, int nparts, int want_xc, int want_j,
-                                                             const float2 *__restrict__ part,
-                                                             double *__restrict__ XC, double *__restrict__ J)
+__device__ __forceinline__ void contract_tc_reduce_block(const RedArgs A, int vb)
 {
     __shared__ float2 shx[32][33], shj[32][33];
+    const int nbf = A.nbf, nparts = A.nparts;
+    const float2 *__restrict__ part = A.part;
     const size_t nn = (size_t)nbf * nbf, ntri = (size_t)nbf * (nbf + 1) / 2;
     const int lx = threadIdx.x & 31, g = threadIdx.x >> 5;
-    const size_t e = (size_t)blockIdx.x * 32 + lx;          // element (mu, nu) = e % nbf, e / nbf
+    const size_t e = (size_t)vb * 32 + lx;                  // element (mu, nu) = e % nbf, e / nbf
     const int nu = (int)(e / nbf), mu = (int)(e % nbf);
     const bool act = e < nn && mu <= nu;
     const size_t t = (size_t)nu * (nu + 1) / 2 + mu;        // packed upper-triangle index
+    if (vb == 0 && A.sc && threadIdx.x < 3)                  // the build's E_xc, N, E_J
+        A.sc[threadIdx.x] = A.scal[threadIdx.x == 0 ? kScalExc : (threadIdx.x == 1 ? kScalNelec : kScalEJ)];
     dfl sx{0.f, 0.f}, sj{0.f, 0.f};
     if (act)
         for (int c = g; c < nparts; c += 32) {
@@ -612,14 +684,42 @@ __global__ void __launch_bounds__(1024) k_contract_tc_reduce(int nbf, int nparts
         sj = df_add(sj, dfl{shj[k][lx].x, shj[k][lx].y});
     }
     const double vx = df_to(sx), vj = df_to(sj);
-    if (want_xc) {
-        XC[(size_t)nu * nbf + mu] = vx;
-        XC[(size_t)mu * nbf + nu] = vx;
+    const size_t lo = (size_t)nu * nbf + mu, up = (size_t)mu * nbf + nu;
+    if (A.want_xc) {
+        A.XC[lo] = vx;
+        A.XC[up] = vx;
+        if (A.XC2) {
+            A.XC2[lo] = vx;
+            A.XC2[up] = vx;
+        }
     }
-    if (want_j) {
-        J[(size_t)nu * nbf + mu] = vj;
-        J[(size_t)mu * nbf + nu] = vj;
+    if (A.want_j) {
+        A.J[lo] = vj;
+        A.J[up] = vj;
+        if (A.J2) {
+            A.J2[lo] = vj;
+            A.J2[up] = vj;
+        }
     }
+}
+
+// Sum the double-float CTA partials of every element on or above the diagonal
+// in CTA order (double-float, no FP64 until the final value) and write XC, J
+// symmetrically (column-major).  Block: 32 elements x 32 CTA groups; group g
+// sums CTAs g, g + 32, ...; the 32 group sums are added in a fixed order.
+__global__ void __launch_bounds__(1024) k_contract_tc_reduce(const RedArgs a)
+{
+    contract_tc_reduce_block(a, (int)blockIdx.x);
+}
+
+__global__ void __launch_bounds__(1024) k_contract_tc_reduce_group(const RedArgs *__restrict__ args, GroupQueue q)
+{
+    __shared__ int s_item;
+    gq_run(q, &s_item, [&](int m, int vb, int) {
+        const RedArgs a = args[m];
+        contract_tc_reduce_block(a, vb);
+        return true;
+    });
 }
 
 // chunking of the point dimension for nsm CTAs: chunks per CTA is the smallest
@@ -706,19 +806,47 @@ int contract_tc_setup(dftg_ctx *c)
     return DFTG_OK;
 }
 
+StepLaunch<CexpArgs> step_cexp(const dftg_ctx *c, const float *cx, const float *cy)
+{
+    StepLaunch<CexpArgs> s;
+    s.args = CexpArgs{c->ct_nkb, c->ct_kbpc, cx, cy, c->d_ct_winv,
+                      reinterpret_cast<int2 *>(c->d_ct_rowexp + 2 * (size_t)c->ct_nchunk * c->nbf)};
+    s.blocks = c->ct_nchunk;
+    return s;
+}
+
+StepLaunch<CtArgs> step_contract_tc(const dftg_ctx *c, const float *cx, const float *cy)
+{
+    StepLaunch<CtArgs> s;
+    s.args = CtArgs{c->nbf, c->ct_AR, c->ct_NP, c->ct_nst, c->ct_spart, c->ct_nkb, c->ct_kbpc, c->ct_nchunk,
+                    reinterpret_cast<const unsigned char *>(c->d_ct_A), c->d_ct_rowexp,
+                    c->d_ct_rowexp + (size_t)c->ct_nchunk * c->nbf,
+                    reinterpret_cast<const int2 *>(c->d_ct_rowexp + 2 * (size_t)c->ct_nchunk * c->nbf), cx, cy,
+                    reinterpret_cast<float2 *>(c->d_part), c->d_flag};
+    s.blocks = c->ct_grid;
+    s.smem = ct_smem(c->ct_nst, c->ct_NP, c->ct_AR, c->nbf, c->ct_spart != 0);
+    return s;
+}
+
+StepLaunch<RedArgs> step_contract_reduce(const dftg_ctx *c, bool want_xc, bool want_j, double *XC, double *J)
+{
+    StepLaunch<RedArgs> s;
+    s.args = RedArgs{c->nbf, c->ct_grid, want_xc ? 1 : 0, want_j ? 1 : 0, reinterpret_cast<const float2 *>(c->d_part),
+                     XC, J, nullptr, nullptr, c->d_scal, nullptr};
+    s.blocks = (int)(((size_t)c->nbf * c->nbf + 31) / 32);
+    return s;
+}
+
 // XC = phi^T diag(cxc) phi and J = phi^T diag(cj) phi partials on the tensor
 // cores for any pair of FP32 point-coefficient arrays
 int launch_contract_tc_on(dftg_ctx *c, const float *cxc32, const float *cj32)
 {
-    int2 *cexp = reinterpret_cast<int2 *>(c->d_ct_rowexp + 2 * (size_t)c->ct_nchunk * c->nbf);
-    k_ct_cexp<<<c->ct_nchunk, 256, 0, c->stream>>>(c->ct_nkb, c->ct_kbpc, cxc32, cj32, c->d_ct_winv, cexp);
+    const StepLaunch<CexpArgs> ce = step_cexp(c, cxc32, cj32);
+    k_ct_cexp<<<ce.blocks, kCexpThreads, 0, c->stream>>>(ce.args);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "contract_bounds");
-    k_contract_tc<<<c->ct_grid, kCtThreads, ct_smem(c->ct_nst, c->ct_NP, c->ct_AR, c->nbf, c->ct_spart != 0), c->stream>>>(
-        c->nbf, c->ct_AR, c->ct_NP, c->ct_nst, c->ct_spart, c->ct_nkb, c->ct_kbpc, c->ct_nchunk,
-        reinterpret_cast<const unsigned char *>(c->d_ct_A), c->d_ct_rowexp,
-        c->d_ct_rowexp + (size_t)c->ct_nchunk * c->nbf, cexp, cxc32, cj32,
-        reinterpret_cast<float2 *>(c->d_part), c->d_flag);
+    const StepLaunch<CtArgs> ct = step_contract_tc(c, cxc32, cj32);
+    k_contract_tc<<<ct.blocks, kCtThreads, ct.smem, c->stream>>>(ct.args);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }
@@ -746,16 +874,45 @@ int ct_setup_tables(dftg_ctx *c, int AR, int nkb, int kbpc, int nchunk, int *row
 int ct_launch_cexp(dftg_ctx *c, int nkb, int kbpc, int nchunk, const float *cx, const float *cy, const float *winv,
                    int2 *cexp)
 {
-    k_ct_cexp<<<nchunk, 256, 0, c->stream>>>(nkb, kbpc, cx, cy, winv, cexp);
+    k_ct_cexp<<<nchunk, kCexpThreads, 0, c->stream>>>(CexpArgs{nkb, kbpc, cx, cy, winv, cexp});
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }
 
 int launch_contract_tc_reduce_to(dftg_ctx *c, bool want_xc, bool want_j, double *XC, double *J)
 {
-    const size_t nn = (size_t)c->nbf * c->nbf;
-    k_contract_tc_reduce<<<(unsigned)((nn + 31) / 32), 1024, 0, c->stream>>>(
-        c->nbf, c->ct_grid, want_xc ? 1 : 0, want_j ? 1 : 0, reinterpret_cast<const float2 *>(c->d_part), XC, J);
+    const StepLaunch<RedArgs> st = step_contract_reduce(c, want_xc, want_j, XC, J);
+    k_contract_tc_reduce<<<st.blocks, 1024, 0, c->stream>>>(st.args);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+int group_cexp(const CexpArgs *d_args, const GroupQueue &q, int nsm, cudaStream_t st)
+{
+    int occ = 0;
+    DFTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_ct_cexp_group, kCexpThreads, 0));
+    const int grid = group_grid(q, occ, nsm);
+    if (grid > 0) k_ct_cexp_group<<<grid, kCexpThreads, 0, st>>>(d_args, q);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+int group_contract_tc(const CtArgs *d_args, const GroupQueue &q, size_t smem, int device, int nsm, cudaStream_t st)
+{
+    DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_contract_tc_group), device));
+    // one CTA per SM: each holds all kCtTmemCols TMEM columns for its lifetime
+    const int grid = group_grid(q, 1, nsm);
+    if (grid > 0) k_contract_tc_group<<<grid, kCtThreads, smem, st>>>(d_args, q);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+int group_contract_reduce(const RedArgs *d_args, const GroupQueue &q, int nsm, cudaStream_t st)
+{
+    int occ = 0;
+    DFTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_contract_tc_reduce_group, 1024, 0));
+    const int grid = group_grid(q, occ, nsm);
+    if (grid > 0) k_contract_tc_reduce_group<<<grid, 1024, 0, st>>>(d_args, q);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }

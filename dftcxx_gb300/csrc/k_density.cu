@@ -207,16 +207,17 @@ __global__ void __launch_bounds__(kDtThreads) k_density_tiled(int nbf, int ldp, 
     if (tid < kDtPts) rho[p0 + tid] = 2.0 * rsum;
 }
 
-// stage 1: partial sums of w*rho over chunks that never straddle two atoms
-__global__ void __launch_bounds__(kRedBlock) k_atom_sums(size_t per_atom, int chunks_per_atom, int natoms,
-                                                          const double *__restrict__ w, const double *__restrict__ rho,
-                                                          double *__restrict__ part, const double *__restrict__ atoms,
-                                                          double *scal, int mode, int *counter)
+// stage 1: partial sums of w*rho over chunks that never straddle two atoms;
+// the last of the nb blocks sums them per atom and forms the correction factor
+__device__ __forceinline__ void atom_sums_block(const SumsArgs A, int b, int nb)
 {
     __shared__ double sh[32];
     __shared__ double sq[kMaxAtoms];
     __shared__ int s_last;
-    const int b = blockIdx.x;
+    const size_t per_atom = A.per_atom;
+    const int chunks_per_atom = A.cpa, natoms = A.natoms;
+    const double *__restrict__ w = A.w, *__restrict__ rho = A.rho;
+    double *__restrict__ part = A.part;
     const int a = b / chunks_per_atom, ch = b % chunks_per_atom;
     const size_t base = (size_t)a * per_atom;
     const size_t lo = (size_t)ch * kRedChunk, hi = min(per_atom, lo + kRedChunk);
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(kRedBlock) k_atom_sums(size_t per_atom, int ch
     for (size_t i = lo + threadIdx.x; i < hi; i += kRedBlock) s += w[base + i] * rho[base + i];
     s = block_sum(s, sh);
     if (threadIdx.x == 0) part[b] = s;
-    if (!last_block(counter, &s_last)) return;
+    if (!last_block_of(A.counter, nb, &s_last)) return;
     // last block: per-atom sums in chunk order, total, correction factor
     for (int t = threadIdx.x; t < natoms; t += kRedBlock) {
         double q = 0.0;
@@ -233,12 +234,13 @@ __global__ void __launch_bounds__(kRedBlock) k_atom_sums(size_t per_atom, int ch
     }
     __syncthreads();
     if (threadIdx.x == 0) {
+        double *scal = A.scal;
         double total = 0.0, charge = 0.0;
         for (int t = 0; t < natoms; ++t) {
             total += sq[t];
-            charge += atoms[4 * t + 3];
+            charge += A.atoms[4 * t + 3];
         }
-        if (mode == 0) {           // before correction; charges scaled to the corrected density
+        if (A.mode == 0) {         // before correction; charges scaled to the corrected density
             scal[kScalSum] = total;
             const double cf = charge / total;
             scal[kScalScale] = cf;
@@ -253,7 +255,16 @@ __global__ void __launch_bounds__(kRedBlock) k_atom_sums(size_t per_atom, int ch
             for (int t = 0; t < natoms; ++t) scal[kScalAtomQ + t] = sq[t];
             scal[kScalNelec] = total;
         }
+        if (A.done) {              // publish the factor to the grouped launch's point blocks
+            __threadfence();
+            flag_release(A.done, 1);
+        }
     }
+}
+
+__global__ void __launch_bounds__(kRedBlock) k_atom_sums(const SumsArgs a)
+{
+    atom_sums_block(a, (int)blockIdx.x, (int)gridDim.x);
 }
 
 __global__ void k_scale(size_t npts, const double *__restrict__ scal, double *rho)
@@ -271,17 +282,23 @@ __global__ void k_scale(size_t npts, const double *__restrict__ scal, double *rh
 // build's N, dft.cpp:111) and, with rw32, writes rho w_becke split into FP32
 // hi / lo planes [2][npad] for the multipole kernel.
 template <bool MIXED>
-__global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restrict__ rho,
-                                                   const double *__restrict__ w, double *__restrict__ scal,
-                                                   int apply_scale, double *__restrict__ cxc,
-                                                   float *__restrict__ cxc32, double *__restrict__ part, int *counter,
-                                                   int want64, int want_n, const double *__restrict__ wb,
-                                                   float *__restrict__ rw32)
+__device__ __forceinline__ void lda_block(const LdaArgs A, int vb, int nvb)
 {
+    const size_t npad = A.npad;
+    double *__restrict__ rho = A.rho;
+    const double *__restrict__ w = A.w;
+    double *__restrict__ scal = A.scal;
+    const int apply_scale = A.apply_scale, want64 = A.want64, want_n = A.want_n;
+    double *__restrict__ cxc = A.cxc;
+    float *__restrict__ cxc32 = A.cxc32;
+    double *__restrict__ part = A.part;
+    int *counter = A.counter;
+    const double *__restrict__ wb = A.wb;
+    float *__restrict__ rw32 = A.rw32;
     __shared__ double sh[32];
     __shared__ float shf[2][32];
     __shared__ int s_last;
-    const size_t p = (size_t)blockIdx.x * kRedBlock + threadIdx.x;
+    const size_t p = (size_t)vb * kRedBlock + threadIdx.x;
     double ew = 0.0;
     if (MIXED) {
         // double-float point kernel and block sum; FP64 only for the density
@@ -291,7 +308,7 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
         if (p < npad) {
             double r = rho[p];
             if (apply_scale) {
-                r *= scal[kScalScale];
+                r *= __ldcg(scal + kScalScale);
                 rho[p] = r;
             }
             dfl e;
@@ -322,14 +339,14 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
         if (threadIdx.x == 0) {
             dfl t{0.f, 0.f};
             for (int i = 0; i < kRedBlock / 32; ++i) t = df_add(t, dfl{shf[0][i], shf[1][i]});
-            part[blockIdx.x] = df_to(t);
-            if (want_n) part[gridDim.x + blockIdx.x] = wrs;
+            part[vb] = df_to(t);
+            if (want_n) part[nvb + vb] = wrs;
         }
-        if (!last_block(counter, &s_last)) return;
+        if (!last_block_of(counter, nvb, &s_last)) return;
         double t = 0.0, tn = 0.0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += kRedBlock) {
+        for (int i = threadIdx.x; i < nvb; i += kRedBlock) {
             t += __ldcg(part + i);
-            if (want_n) tn += __ldcg(part + gridDim.x + i);
+            if (want_n) tn += __ldcg(part + nvb + i);
         }
         t = block_sum(t, sh);
         if (want_n) tn = block_sum(tn, sh);
@@ -342,7 +359,7 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
     if (p < npad) {
         double r = rho[p];
         if (apply_scale) {        // density correction fused into the point kernel
-            r *= scal[kScalScale];
+            r *= __ldcg(scal + kScalScale);
             rho[p] = r;
         }
         double e;
@@ -355,13 +372,61 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(size_t npad, double *__restri
         cxc32[p] = (float)c;
     }
     ew = block_sum(ew, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = ew;
-    if (!last_block(counter, &s_last)) return;
+    if (threadIdx.x == 0) part[vb] = ew;
+    if (!last_block_of(counter, nvb, &s_last)) return;
     // last block: E_xc = sum of the block partials (fixed assignment and order)
     double t = 0.0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += kRedBlock) t += __ldcg(part + i);
+    for (int i = threadIdx.x; i < nvb; i += kRedBlock) t += __ldcg(part + i);
     t = block_sum(t, sh);
     if (threadIdx.x == 0) scal[kScalExc] = t;
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kRedBlock) k_lda(const LdaArgs a)
+{
+    lda_block<MIXED>(a, (int)blockIdx.x, (int)gridDim.x);
+}
+
+// The batch's per-atom sums and mixed point kernel in one persistent launch.
+// Items [0, qs.nitems) are the molecules' atom-sum blocks, the next ql.nitems
+// their point-kernel blocks, handed out from *head in that order.  A point block
+// of molecule m first waits (bounded) until m's last atom-sum block has
+// published the correction factor (done[m] = 1): every item it can wait on was
+// handed out before it, to a running CTA, so the wait ends.  A wait that gives
+// up records code 21 in *err and stops the CTA (the batch's results are then
+// invalid).  stall_mol >= 0 makes that molecule's point blocks wait for a value
+// nothing writes (the self-test of the bounded wait).
+__global__ void __launch_bounds__(kRedBlock) k_sums_lda_group(const SumsArgs *__restrict__ sa, GroupQueue qs,
+                                                              const LdaArgs *__restrict__ la, GroupQueue ql,
+                                                              SumsLdaCtl ctl)
+{
+    __shared__ int s_item, s_ok;
+    const int total = qs.nitems + ql.nitems, take = ql.take;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(ctl.head, take);
+        __syncthreads();
+        const int i0 = s_item;
+        if (i0 >= total) return;
+        const int i1 = min(total, i0 + take);
+        for (int i = i0; i < i1; ++i) {
+            if (i > i0) __syncthreads();
+            if (i < qs.nitems) {
+                const int m = gq_molecule(qs, i), b0 = __ldg(qs.prefix + m);
+                const SumsArgs a = sa[m];
+                atom_sums_block(a, i - b0, __ldg(qs.prefix + m + 1) - b0);
+            } else {
+                const int j = i - qs.nitems;
+                const int m = gq_molecule(ql, j), b0 = __ldg(ql.prefix + m);
+                if (!wait_flag_ge(ctl.done + m, m == ctl.stall_mol ? 2 : 1, ctl.limit_ns, &s_ok)) {
+                    if (threadIdx.x == 0) atomicExch(ctl.err, 21);
+                    return;
+                }
+                const LdaArgs a = la[m];
+                lda_block<true>(a, j - b0, __ldg(ql.prefix + m + 1) - b0);
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------- launchers
@@ -391,54 +456,77 @@ int launch_density(dftg_ctx *c)
     return DFTG_OK;
 }
 
+StepLaunch<SumsArgs> step_atom_sums(const dftg_ctx *c, int mode)
+{
+    // a point-set context has one cell (all points) and no density correction
+    const int ncell = c->points_only ? 1 : c->ncell;
+    const size_t per_atom = c->points_only ? c->npts : (size_t)c->nrad * c->nang;
+    const int cpa = (int)((per_atom + kRedChunk - 1) / kRedChunk);
+    StepLaunch<SumsArgs> s;
+    s.args = SumsArgs{per_atom, cpa, ncell, mode == kSumsOnly || c->points_only ? 1 : 0, c->d_w, c->d_rho, c->d_red,
+                      c->d_atoms, c->d_scal, c->d_counters + kCntAtoms, nullptr};
+    s.blocks = cpa * ncell;
+    return s;
+}
+
 // kSumsOnly: per-atom charges of the current rho.  kSumsCorrect: correction
 // factor, rho rescaled, charges recomputed (correct_densities).  kSumsFactor:
 // correction factor and rescaled charges only; the LDA kernel rescales rho.
 int launch_atom_sums(dftg_ctx *c, int mode)
 {
-    // a point-set context has one cell (all points) and no density correction
     if (c->points_only) mode = kSumsOnly;
-    const int ncell = c->points_only ? 1 : c->ncell;
-    const size_t per_atom = c->points_only ? c->npts : (size_t)c->nrad * c->nang;
-    const int cpa = (int)((per_atom + kRedChunk - 1) / kRedChunk);
-    const int nb = cpa * ncell;
-    int *cnt = c->d_counters + kCntAtoms;
-    k_atom_sums<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, ncell, c->d_w, c->d_rho, c->d_red, c->d_atoms,
-                                                 c->d_scal, mode == kSumsOnly ? 1 : 0, cnt);
+    StepLaunch<SumsArgs> st = step_atom_sums(c, mode);
+    k_atom_sums<<<st.blocks, kRedBlock, 0, c->stream>>>(st.args);
     DFTG_LAUNCH_CHECK();
     if (mode == kSumsCorrect) {
         c->rw_ready = false;         // rho is rescaled below
         k_scale<<<(unsigned)((c->npts + 255) / 256), 256, 0, c->stream>>>(c->npts, c->d_scal, c->d_rho);
         DFTG_LAUNCH_CHECK();
-        k_atom_sums<<<nb, kRedBlock, 0, c->stream>>>(per_atom, cpa, ncell, c->d_w, c->d_rho, c->d_red, c->d_atoms,
-                                                     c->d_scal, 1, cnt);
+        st.args.mode = 1;
+        k_atom_sums<<<st.blocks, kRedBlock, 0, c->stream>>>(st.args);
         DFTG_LAUNCH_CHECK();
     }
     DFTG_MARK(c, "charge");
     return DFTG_OK;
 }
 
-int launch_xc_points(dftg_ctx *c, bool apply_scale, bool with_n)
+StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n)
 {
-    const unsigned nb = (unsigned)((c->npad + kRedBlock - 1) / kRedBlock);
-    const int sc = apply_scale ? 1 : 0;
-    if (2 * (size_t)nb > c->red_elems) { set_error("reduction buffer too small for %u blocks", nb); return DFTG_ERR_STATE; }
     // with_n: the build's N from the corrected rho (no per-atom sums ran), and
     // the rho w_becke planes for the mixed multipole kernel
-    const int wn = with_n ? 1 : 0;
     float *rw32 = (with_n && c->d_rw32 && (c->prec_mask & kPrecMultipole)) ? c->d_rw32 : nullptr;
-    c->rw_ready = rw32 != nullptr;
-    if (c->prec_mask & kPrecLda)
-        k_lda<true><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_scal, sc, c->d_cxc, c->d_cxc32,
-                                                     c->d_red, c->d_counters + kCntLda,
-                                                     (c->prec_mask & kPrecContract) && c->ct_ready ? 0 : 1, wn,
-                                                     c->d_wb, rw32);
-    else
-        k_lda<false><<<nb, kRedBlock, 0, c->stream>>>(c->npad, c->d_rho, c->d_w, c->d_scal, sc, c->d_cxc,
-                                                      c->d_cxc32, c->d_red, c->d_counters + kCntLda, 1, 0, nullptr,
-                                                      nullptr);
+    const bool mixed = (c->prec_mask & kPrecLda) != 0;
+    StepLaunch<LdaArgs> s;
+    s.args = LdaArgs{c->npad, c->d_rho, c->d_w, c->d_scal, apply_scale ? 1 : 0,
+                     mixed ? ((c->prec_mask & kPrecContract) && c->ct_ready ? 0 : 1) : 1, mixed && with_n ? 1 : 0,
+                     c->d_cxc, c->d_cxc32, c->d_red, c->d_counters + kCntLda, mixed ? c->d_wb : nullptr,
+                     mixed ? rw32 : nullptr};
+    s.blocks = (int)((c->npad + kRedBlock - 1) / kRedBlock);
+    return s;
+}
+
+int launch_xc_points(dftg_ctx *c, bool apply_scale, bool with_n)
+{
+    const StepLaunch<LdaArgs> st = step_lda(c, apply_scale, with_n);
+    if (2 * (size_t)st.blocks > c->red_elems) { set_error("reduction buffer too small for %d blocks", st.blocks); return DFTG_ERR_STATE; }
+    c->rw_ready = st.args.rw32 != nullptr;
+    if (c->prec_mask & kPrecLda) k_lda<true><<<st.blocks, kRedBlock, 0, c->stream>>>(st.args);
+    else k_lda<false><<<st.blocks, kRedBlock, 0, c->stream>>>(st.args);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "lda");
+    return DFTG_OK;
+}
+
+int group_sums_lda(const SumsArgs *d_sums, const GroupQueue &qs, const LdaArgs *d_lda, const GroupQueue &ql,
+                   const SumsLdaCtl &ctl, int nsm, cudaStream_t st)
+{
+    int occ = 0;
+    DFTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sums_lda_group, kRedBlock, 0));
+    GroupQueue all = ql;
+    all.nitems = qs.nitems + ql.nitems;
+    const int grid = group_grid(all, occ, nsm);
+    if (grid > 0) k_sums_lda_group<<<grid, kRedBlock, 0, st>>>(d_sums, qs, d_lda, ql, ctl);
+    DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }
 

@@ -60,20 +60,32 @@ __device__ __forceinline__ void unpack8_bf16(uint4 u, float (&v)[8])
 struct TcShared {
     uint64_t full[2], empty[2], tmem_full[2], tmem_empty[2];
     uint32_t tmem_base;
+    int item;                              // the grouped launch's queue position (broadcast)
 };
 
-__global__ void __launch_bounds__(kTcThreads, 1)
-k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restrict__ Aslices,
-             const int *__restrict__ row_exp, const unsigned char *__restrict__ Bslices,
-             const int *__restrict__ col_exp, double *__restrict__ rho, int *__restrict__ err)
+// One CTA's share of one molecule's tiles (vb, vb + nvb, ...): initialises the
+// mbarriers, stages the B slices, runs the producer / MMA / epilogue roles and
+// invalidates the mbarriers again.  The caller owns the kTcTmemCols TMEM
+// columns at tmem.  Returns false (block-uniform) when a bounded wait gave up.
+// the CTA's mbarriers and TMEM address (one instance in every kernel that uses them)
+__shared__ TcShared tc_sh;
+
+__device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, int nvb, uint32_t tmem)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
+    TcShared *sh = &tc_sh;
+    const int nbf = args.nbf, KP = args.KP, NP = args.NP, ntiles = args.ntiles;
+    const unsigned char *__restrict__ Aslices = args.A;
+    const int *__restrict__ row_exp = args.row_exp;
+    const unsigned char *__restrict__ Bslices = args.B;
+    const int *__restrict__ col_exp = args.col_exp;
+    double *__restrict__ rho = args.rho;
+    int *__restrict__ err = args.err;
     const uint32_t a_slice_bytes = (uint32_t)kTcTile * KP * 2;
     const uint32_t a_stage_bytes = kTcSlices * a_slice_bytes;
     const uint32_t b_slice_bytes = (uint32_t)NP * KP * 2;
     unsigned char *sA = smem;                                   // [2][slices][tile block]
     unsigned char *sB = smem + 2 * a_stage_bytes;                // [slices][B block]
-    TcShared *sh = reinterpret_cast<TcShared *>(sB + kTcSlices * b_slice_bytes);
     __shared__ int s_texp[kTcMaxK];
     __shared__ int s_fail;
     __shared__ float2 s_half[kTcTile];            // (S, E) of the second column half, per row
@@ -98,17 +110,10 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
         for (int i = threadIdx.x; i < NP && i < kTcMaxK; i += kTcThreads) s_texp[i] = i < nbf ? col_exp[i] : 0;
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
-    if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem_base)),
-                     "r"(kTcTmemCols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = sh->tmem_base;
-    const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int my_tiles = (ntiles - vb + nvb - 1) / nvb;
 
     if (warp == 0) {
         // ------------------------------------------------------------ producer
@@ -117,16 +122,16 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
             // L2 prefetch two tiles ahead of the bulk copies
             for (int it = 0; it < 2 && it < my_tiles; ++it)
                 for (int i = 0; i < kTcSlices; ++i)
-                    prefetch_l2(Aslices + ((size_t)i * ntiles + blockIdx.x + it * gridDim.x) * a_slice_bytes, a_slice_bytes);
+                    prefetch_l2(Aslices + ((size_t)i * ntiles + vb + it * nvb) * a_slice_bytes, a_slice_bytes);
             for (int it = 0; it < my_tiles; ++it) {
                 const int s = it & 1, n = it >> 1;
                 if (it + 2 < my_tiles)
                     for (int i = 0; i < kTcSlices; ++i)
-                        prefetch_l2(Aslices + ((size_t)i * ntiles + blockIdx.x + (it + 2) * gridDim.x) * a_slice_bytes,
+                        prefetch_l2(Aslices + ((size_t)i * ntiles + vb + (it + 2) * nvb) * a_slice_bytes,
                                     a_slice_bytes);
                 if (!mbar_wait(&sh->empty[s], (uint32_t)((n & 1) ^ 1))) { atomicExch(err, 1); s_fail = 1; break; }
                 if (s_fail) break;
-                const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+                const int tile = vb + it * nvb;
                 mbar_arrive_expect_tx(&sh->full[s], a_stage_bytes);
                 for (int i = 0; i < kTcSlices; ++i)
                     bulk_g2s(sA + (size_t)s * a_stage_bytes + (size_t)i * a_slice_bytes,
@@ -185,7 +190,7 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
             epi8_bar_sync();
             if (s_fail) break;
             tc_fence_after();
-            const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+            const int tile = vb + it * nvb;
             const size_t p = (size_t)tile * kTcTile + r;
             const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
             const uint32_t ta0 = tmem + (uint32_t)(s * 256) + ((uint32_t)(q * 32) << 16);
@@ -259,10 +264,61 @@ k_density_tc(int nbf, int KP, int NP, int ntiles, const unsigned char *__restric
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 1) {
+    const bool ok = s_fail == 0;
+    if (threadIdx.x == 0)
+        for (int b = 0; b < 2; ++b) {
+            mbar_inval(&sh->full[b]);
+            mbar_inval(&sh->empty[b]);
+            mbar_inval(&sh->tmem_full[b]);
+            mbar_inval(&sh->tmem_empty[b]);
+        }
+    return ok;
+}
+
+__device__ __forceinline__ void density_tc_alloc()
+{
+    TcShared *sh = &tc_sh;
+    if ((threadIdx.x >> 5) == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem_base)),
+                     "r"(kTcTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+}
+
+// after the CTA's last __syncthreads
+__device__ __forceinline__ void density_tc_free(uint32_t tmem)
+{
+    if ((threadIdx.x >> 5) == 1) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
     }
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_density_tc(const DensTcArgs args)
+{
+    density_tc_alloc();
+    const uint32_t tmem = tc_sh.tmem_base;
+    density_tc_cta(args, (int)blockIdx.x, (int)gridDim.x, tmem);
+    density_tc_free(tmem);
+}
+
+// the batch's grouped launch: each CTA runs items (molecule, virtual CTA) from
+// the queue, TMEM allocated once for all of them
+__global__ void __launch_bounds__(kTcThreads, 1) k_density_tc_group(const DensTcArgs *__restrict__ args, GroupQueue q)
+{
+    density_tc_alloc();
+    const uint32_t tmem = tc_sh.tmem_base;
+    gq_run(q, &tc_sh.item, [&](int m, int vb, int nvb) {
+        const DensTcArgs a = args[m];
+        return density_tc_cta(a, vb, nvb, tmem);
+    });
+    tc_fence_before();
+    __syncthreads();
+    density_tc_free(tmem);
 }
 
 // ------------------------------------------------------------------ slicing
@@ -305,19 +361,26 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
 }
 
 // P (FP64, nbf x nbf, symmetric) -> 4 pre-scaled integer slices per column in
-// the B layout: one warp per column, lanes over the rows
-__global__ void k_slice_P(int nbf, int KP, int NP, const double *__restrict__ P, __nv_bfloat16 *__restrict__ B,
-                          int *__restrict__ col_exp)
+// the B layout: one warp per column, lanes over the rows; with Pcopy the warp
+// also copies its column of P there
+__device__ __forceinline__ void slice_P_block(const SlicePArgs a, int vb)
 {
-    const int nu = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int nbf = a.nbf, KP = a.KP, NP = a.NP;
+    const double *__restrict__ P = a.P;
+    __nv_bfloat16 *__restrict__ B = static_cast<__nv_bfloat16 *>(a.B);
+    const int nu = vb * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (nu >= NP) return;
     double mx = 0.0;
     if (nu < nbf)
-        for (int mu = lane; mu < nbf; mu += 32) mx = fmax(mx, fabs(P[(size_t)nu * nbf + mu]));
+        for (int mu = lane; mu < nbf; mu += 32) {
+            const double v = P[(size_t)nu * nbf + mu];
+            if (a.Pcopy) a.Pcopy[(size_t)nu * nbf + mu] = v;
+            mx = fmax(mx, fabs(v));
+        }
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     int e = 0;
     if (mx > 0.0) frexp(mx, &e);
-    if (nu < nbf && lane == 0) col_exp[nu] = e;
+    if (nu < nbf && lane == 0) a.col_exp[nu] = e;
     const size_t slice = (size_t)NP * KP;
     for (int mu = lane; mu < KP; mu += 32) {
         double x = (nu < nbf && mu < nbf) ? ldexp(P[(size_t)nu * nbf + mu], -e) : 0.0;
@@ -331,9 +394,23 @@ __global__ void k_slice_P(int nbf, int KP, int NP, const double *__restrict__ P,
     }
 }
 
+constexpr int kSlicePThreads = 128;
+
+__global__ void __launch_bounds__(kSlicePThreads) k_slice_P(const SlicePArgs a) { slice_P_block(a, (int)blockIdx.x); }
+
+__global__ void __launch_bounds__(kSlicePThreads) k_slice_P_group(const SlicePArgs *__restrict__ args, GroupQueue q)
+{
+    __shared__ int s_item;
+    gq_run(q, &s_item, [&](int m, int vb, int) {
+        const SlicePArgs a = args[m];
+        slice_P_block(a, vb);
+        return true;
+    });
+}
+
 size_t density_tc_smem(int KP, int NP)
 {
-    return 2 * (size_t)kTcSlices * kTcTile * KP * 2 + (size_t)kTcSlices * NP * KP * 2 + sizeof(TcShared) + 64;
+    return 2 * (size_t)kTcSlices * kTcTile * KP * 2 + (size_t)kTcSlices * NP * KP * 2 + 64;
 }
 
 bool density_tc_supported(int nbf) { return nbf <= kTcMaxK; }
@@ -367,15 +444,53 @@ int density_tc_setup(dftg_ctx *c)
     return DFTG_OK;
 }
 
+StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy)
+{
+    StepLaunch<SlicePArgs> s;
+    s.args = SlicePArgs{c->nbf, c->tc_KP, c->tc_NP, P, Pcopy, c->d_tcB, c->d_tc_colexp};
+    s.blocks = (c->tc_NP + kSlicePThreads / 32 - 1) / (kSlicePThreads / 32);
+    s.smem = 0;
+    return s;
+}
+
+StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c)
+{
+    StepLaunch<DensTcArgs> s;
+    s.args = DensTcArgs{c->nbf, c->tc_KP, c->tc_NP, (int)(c->npad / kTcTile),
+                        reinterpret_cast<const unsigned char *>(c->d_tcA), c->d_tc_rowexp,
+                        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag};
+    s.blocks = c->tc_grid;
+    s.smem = density_tc_smem(c->tc_KP, c->tc_NP);
+    return s;
+}
+
 int launch_density_tc(dftg_ctx *c)
 {
-    k_slice_P<<<(c->tc_NP + 3) / 4, 128, 0, c->stream>>>(c->nbf, c->tc_KP, c->tc_NP, c->d_P,
-                                                         reinterpret_cast<__nv_bfloat16 *>(c->d_tcB), c->d_tc_colexp);
+    const StepLaunch<SlicePArgs> sp = step_slice_P(c, c->d_P, nullptr);
+    k_slice_P<<<sp.blocks, kSlicePThreads, 0, c->stream>>>(sp.args);
     DFTG_LAUNCH_CHECK();
-    const int ntiles = (int)(c->npad / kTcTile);
-    k_density_tc<<<c->tc_grid, kTcThreads, density_tc_smem(c->tc_KP, c->tc_NP), c->stream>>>(
-        c->nbf, c->tc_KP, c->tc_NP, ntiles, reinterpret_cast<const unsigned char *>(c->d_tcA), c->d_tc_rowexp,
-        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag);
+    const StepLaunch<DensTcArgs> dn = step_density_tc(c);
+    k_density_tc<<<dn.blocks, kTcThreads, dn.smem, c->stream>>>(dn.args);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+int group_slice_P(const SlicePArgs *d_args, const GroupQueue &q, int nsm, cudaStream_t st)
+{
+    int occ = 0;
+    DFTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_slice_P_group, kSlicePThreads, 0));
+    const int grid = group_grid(q, occ, nsm);
+    if (grid > 0) k_slice_P_group<<<grid, kSlicePThreads, 0, st>>>(d_args, q);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+int group_density_tc(const DensTcArgs *d_args, const GroupQueue &q, size_t smem, int device, int nsm, cudaStream_t st)
+{
+    DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_density_tc_group), device));
+    // one CTA per SM: each holds all kTcTmemCols TMEM columns for its lifetime
+    const int grid = group_grid(q, 1, nsm);
+    if (grid > 0) k_density_tc_group<<<grid, kTcThreads, smem, st>>>(d_args, q);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }

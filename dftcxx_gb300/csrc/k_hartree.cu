@@ -662,15 +662,18 @@ __device__ __forceinline__ void mp_copy(float *__restrict__ dst, const float *__
     for (; e < n; e += kMpThreads) dst[e] = src[e];
 }
 
-__global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0, int N, int nang, int lmax, int ngroup,
-                                                          const float *__restrict__ rw32, size_t npad,
-                                                          const double *__restrict__ rho, const double *__restrict__ wb,
-                                                          const double *__restrict__ w, const float *__restrict__ Ywt32,
-                                                          const float *__restrict__ maps, double *__restrict__ scal,
-                                                          double *__restrict__ U, float *__restrict__ U32,
-                                                          float *__restrict__ U32T, int want64,
-                                                          double *__restrict__ spl, float *__restrict__ splm)
+__device__ __forceinline__ void multipole_block(const MpArgs A, int vb)
 {
+    const int natoms = A.natoms, cell0 = A.cell0, N = A.N, nang = A.nang, lmax = A.lmax, ngroup = A.ngroup;
+    const float *__restrict__ rw32 = A.rw32;
+    const size_t npad = A.npad;
+    const double *__restrict__ rho = A.rho, *__restrict__ wb = A.wb, *__restrict__ w = A.w;
+    const float *__restrict__ Ywt32 = A.Ywt32, *__restrict__ maps = A.maps;
+    double *__restrict__ scal = A.scal, *__restrict__ U = A.U;
+    float *__restrict__ U32 = A.U32, *__restrict__ U32T = A.U32T;
+    const int want64 = A.want64;
+    double *__restrict__ spl = A.spl;
+    float *__restrict__ splm = A.splm;
     extern __shared__ __align__(16) unsigned char mp_smem[];
     const int nlm = (lmax + 1) * (lmax + 1);
     const int row = nang | 1;
@@ -684,7 +687,7 @@ __global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0,
     dfl *sD = sU + (size_t)kMpLG * N;                            // [kMpLG][N] spline derivatives
     double *sred = reinterpret_cast<double *>(sD + (size_t)kMpLG * N);
     const int tid = threadIdx.x;
-    const int al = blockIdx.x / ngroup, g = blockIdx.x % ngroup, a = cell0 + al;
+    const int al = vb / ngroup, g = vb % ngroup, a = cell0 + al;
     const int lm0 = g * kMpLG, nl = min(kMpLG, nlm - lm0);
     const size_t base = (size_t)al * N * nang;
     const size_t uhalf = (size_t)natoms * nlm * N;
@@ -834,6 +837,18 @@ __global__ void __launch_bounds__(kMpThreads) k_multipole(int natoms, int cell0,
     }
 }
 
+__global__ void __launch_bounds__(kMpThreads, 2) k_multipole(const MpArgs a) { multipole_block(a, (int)blockIdx.x); }
+
+__global__ void __launch_bounds__(kMpThreads, 2) k_multipole_group(const MpArgs *__restrict__ args, GroupQueue q)
+{
+    __shared__ int s_item;
+    gq_run(q, &s_item, [&](int m, int vb, int) {
+        const MpArgs a = args[m];
+        multipole_block(a, vb);
+        return true;
+    });
+}
+
 // spline interval of r: smallest i >= 1 with r <= sx[i] (cspline.cpp:163-170),
 // from the analytic inverse of the radial map and an exact comparison fix-up
 __device__ __forceinline__ void spline_interval(double rd, const double *__restrict__ sx, int N, double fscale,
@@ -936,14 +951,16 @@ constexpr int kCrossLoLmax = 0;
 // halves for l <= kCrossLoLmax.  Writes each pair's contribution as an FP32 (hi, lo)
 // pair.
 template <int P, int LMAX>
-__global__ void __launch_bounds__(128) k_vcross_bins(int nrad, int lmax_rt,
-                                                     const int4 *__restrict__ tasks,
-                                                     const float4 *__restrict__ pgeo,
-                                                     const float2 *__restrict__ ptk,
-                                                     const float *__restrict__ splm, float2 *__restrict__ out)
+__device__ __forceinline__ void vcross_bins_block(const VcbArgs A, int vb)
 {
+    const int nrad = A.nrad, lmax_rt = A.lmax;
+    const int4 *__restrict__ tasks = A.tasks;
+    const float4 *__restrict__ pgeo = A.pgeo;
+    const float2 *__restrict__ ptk = A.ptk;
+    const float *__restrict__ splm = A.splm;
+    float2 *__restrict__ out = A.out;
     extern __shared__ float4 s_cf[];      // [nlm][2]: (c0..c3) high, (c0..c3) low
-    const int4 task = tasks[blockIdx.x];  // start, count, atom k, interval iv
+    const int4 task = tasks[vb];  // start, count, atom k, interval iv
     const int lmax = LMAX >= 0 ? LMAX : lmax_rt;   // compile-time for the common cut-offs
     const int nlm = (lmax + 1) * (lmax + 1);
     for (int i = threadIdx.x; i < 2 * nlm; i += blockDim.x) {
@@ -1034,6 +1051,23 @@ __global__ void __launch_bounds__(128) k_vcross_bins(int nrad, int lmax_rt,
     }
 }
 
+template <int P, int LMAX>
+__global__ void __launch_bounds__(128) k_vcross_bins(const VcbArgs a)
+{
+    vcross_bins_block<P, LMAX>(a, (int)blockIdx.x);
+}
+
+template <int P, int LMAX>
+__global__ void __launch_bounds__(128) k_vcross_bins_group(const VcbArgs *__restrict__ args, GroupQueue q)
+{
+    __shared__ int s_item;
+    gq_run(q, &s_item, [&](int m, int vb, int) {
+        const VcbArgs a = args[m];
+        vcross_bins_block<P, LMAX>(a, vb);
+        return true;
+    });
+}
+
 // total potential per point: own cell (FP64) plus the pair contributions in
 // atom order, summed with TwoSum; writes V and cj = w V / 2
 __global__ void k_vcross_gather(size_t npts, size_t npad, int natoms, int cell0, int nrad, int nang,
@@ -1071,24 +1105,24 @@ constexpr int kGoSlab = 32;
 constexpr int kGoShells = 16;
 constexpr int kGoThreads = 256;
 
-__global__ void __launch_bounds__(kGoThreads) k_vcross_gather_own(size_t npts, size_t npad, int natoms, int cell0,
-                                                                  int nrad, int nang, int nlm, int nslab, int nsplit,
-                                                                  const int *__restrict__ pos,
-                                                                  const float2 *__restrict__ pairv,
-                                                                  const float *__restrict__ U32T, size_t uhalf,
-                                                                  const float *__restrict__ Y32,
-                                                                  const double *__restrict__ invr,
-                                                                  const double *__restrict__ W,
-                                                                  const double *__restrict__ rho, int scaled,
-                                                                  double *__restrict__ V, double *__restrict__ cj,
-                                                                  float *__restrict__ cj32, double *__restrict__ part,
-                                                                  double *scal, int *counter)
+__device__ __forceinline__ void gather_own_block(const GoArgs A, int b, int nblk)
 {
+    const size_t npts = A.npts, npad = A.npad, uhalf = A.uhalf;
+    const int natoms = A.natoms, cell0 = A.cell0, nrad = A.nrad, nang = A.nang, nlm = A.nlm;
+    const int nslab = A.nslab, nsplit = A.nsplit, scaled = A.scaled;
+    const int *__restrict__ pos = A.pos;
+    const float2 *__restrict__ pairv = A.pairv;
+    const float *__restrict__ U32T = A.U32T, *__restrict__ Y32 = A.Y32;
+    const double *__restrict__ invr = A.invr, *__restrict__ W = A.W, *__restrict__ rho = A.rho;
+    double *__restrict__ V = A.V, *__restrict__ cj = A.cj;
+    float *__restrict__ cj32 = A.cj32;
+    double *__restrict__ part = A.part;
+    double *scal = A.scal;
+    int *counter = A.counter;
     extern __shared__ float go_smem[];                       // [2][nlm][kGoSlab] Y_lm, [2][kGoShells][nlm] U_lm
     __shared__ double sh[32];
     __shared__ int s_last;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int b = blockIdx.x;
     const int al = b / (nslab * nsplit), rest = b % (nslab * nsplit), slab = rest / nsplit, sp = rest % nsplit;
     const int a = cell0 + al, j0 = slab * kGoSlab;
     const int i_beg = sp * kGoShells, i_end = min(nrad, i_beg + kGoShells);
@@ -1159,11 +1193,26 @@ __global__ void __launch_bounds__(kGoThreads) k_vcross_gather_own(size_t npts, s
     }
     ej = block_sum(ej, sh);
     if (tid == 0) part[b] = ej;
-    if (!last_block(counter, &s_last)) return;
+    if (!last_block_of(counter, nblk, &s_last)) return;
     double t = 0.0;
-    for (int k = tid; k < (int)gridDim.x; k += kGoThreads) t += __ldcg(part + k);
+    for (int k = tid; k < nblk; k += kGoThreads) t += __ldcg(part + k);
     t = block_sum(t, sh);
-    if (tid == 0) scal[kScalEJ] = scaled ? t / scal[kScalScale] : t;
+    if (tid == 0) scal[kScalEJ] = scaled ? t / __ldcg(scal + kScalScale) : t;
+}
+
+__global__ void __launch_bounds__(kGoThreads) k_vcross_gather_own(const GoArgs a)
+{
+    gather_own_block(a, (int)blockIdx.x, (int)gridDim.x);
+}
+
+__global__ void __launch_bounds__(kGoThreads) k_vcross_gather_own_group(const GoArgs *__restrict__ args, GroupQueue q)
+{
+    __shared__ int s_item;
+    gq_run(q, &s_item, [&](int m, int vb, int nvb) {
+        const GoArgs a = args[m];
+        gather_own_block(a, vb, nvb);
+        return true;
+    });
 }
 
 // Order the (point, other atom) pairs by (atom, spline interval of their
@@ -1338,25 +1387,89 @@ __global__ void __launch_bounds__(256) k_ej(size_t npad, const double *__restric
     if (threadIdx.x == 0) scal[kScalEJ] = scaled ? t / scal[kScalScale] : t;
 }
 
-template <int LMAX>
-static void vcross_bins_launch(dftg_ctx *c)
+StepLaunch<VcbArgs> step_vcross_bins(const dftg_ctx *c)
 {
-    k_vcross_bins<kCrossPerThread, LMAX><<<(unsigned)c->ncross_tasks, 128, sizeof(float4) * 2 * c->nlm, c->stream>>>(
-        c->nrad, c->lmax, reinterpret_cast<const int4 *>(c->d_cross_tasks), reinterpret_cast<const float4 *>(c->d_pairs),
-        reinterpret_cast<const float2 *>(static_cast<const char *>(c->d_pairs) + sizeof(float4) * c->npairs),
-        c->d_splm, reinterpret_cast<float2 *>(c->d_pairv));
+    StepLaunch<VcbArgs> s;
+    s.args = VcbArgs{c->nrad, c->lmax, reinterpret_cast<const int4 *>(c->d_cross_tasks),
+                     reinterpret_cast<const float4 *>(c->d_pairs),
+                     reinterpret_cast<const float2 *>(static_cast<const char *>(c->d_pairs) + sizeof(float4) * c->npairs),
+                     c->d_splm, reinterpret_cast<float2 *>(c->d_pairv)};
+    s.blocks = c->npairs > 0 ? (int)c->ncross_tasks : 0;
+    s.smem = sizeof(float4) * 2 * c->nlm;
+    return s;
 }
+
+// the kernel variant of an lmax: fully unrolled for the grid presets' cut-offs
+template <int LMAX>
+struct VcbSingle {
+    static void run(const StepLaunch<VcbArgs> &s, cudaStream_t st)
+    {
+        k_vcross_bins<kCrossPerThread, LMAX><<<s.blocks, 128, s.smem, st>>>(s.args);
+    }
+};
+template <int LMAX>
+struct VcbGroup {
+    static int run(const VcbArgs *d, const GroupQueue &q, size_t smem, int nsm, cudaStream_t st)
+    {
+        int occ = 0;
+        DFTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_vcross_bins_group<kCrossPerThread, LMAX>, 128, smem));
+        const int grid = group_grid(q, occ, nsm);
+        if (grid > 0) k_vcross_bins_group<kCrossPerThread, LMAX><<<grid, 128, smem, st>>>(d, q);
+        return DFTG_OK;
+    }
+};
 
 static int launch_vcross_bins(dftg_ctx *c)
 {
-    switch (c->lmax) {   // fully unrolled variants for the grid presets' cut-offs
-    case 5: vcross_bins_launch<5>(c); break;
-    case 6: vcross_bins_launch<6>(c); break;
-    case 8: vcross_bins_launch<8>(c); break;
-    case 10: vcross_bins_launch<10>(c); break;
-    case 11: vcross_bins_launch<11>(c); break;
-    default: vcross_bins_launch<-1>(c); break;
+    const StepLaunch<VcbArgs> s = step_vcross_bins(c);
+    switch (c->lmax) {
+    case 5: VcbSingle<5>::run(s, c->stream); break;
+    case 6: VcbSingle<6>::run(s, c->stream); break;
+    case 8: VcbSingle<8>::run(s, c->stream); break;
+    case 10: VcbSingle<10>::run(s, c->stream); break;
+    case 11: VcbSingle<11>::run(s, c->stream); break;
+    default: VcbSingle<-1>::run(s, c->stream); break;
     }
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+// lmax: the molecules' common cut-off (the unrolled variant), or -1 when they differ
+int group_vcross_bins(const VcbArgs *d_args, const GroupQueue &q, int lmax, size_t smem, int nsm, cudaStream_t st)
+{
+    int rc = DFTG_OK;
+    switch (lmax) {
+    case 5: rc = VcbGroup<5>::run(d_args, q, smem, nsm, st); break;
+    case 6: rc = VcbGroup<6>::run(d_args, q, smem, nsm, st); break;
+    case 8: rc = VcbGroup<8>::run(d_args, q, smem, nsm, st); break;
+    case 10: rc = VcbGroup<10>::run(d_args, q, smem, nsm, st); break;
+    case 11: rc = VcbGroup<11>::run(d_args, q, smem, nsm, st); break;
+    default: rc = VcbGroup<-1>::run(d_args, q, smem, nsm, st); break;
+    }
+    if (rc != DFTG_OK) return rc;
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
+StepLaunch<MpArgs> step_multipole(const dftg_ctx *c, bool rw_ready)
+{
+    const int ngroup = (c->nlm + kMpLG - 1) / kMpLG;
+    StepLaunch<MpArgs> s;
+    s.args = MpArgs{c->natoms, c->cell0, c->nrad, c->nang, c->lmax, ngroup, (c->prec_mask & kPrecCross) ? 0 : 1,
+                    rw_ready ? c->d_rw32 : nullptr, c->npad, c->d_rho, c->d_wb, c->d_w, c->d_Ywt32, c->d_maps32,
+                    c->d_scal, c->d_U, c->d_U32, c->d_U32T, c->d_spl, c->d_splm};
+    s.blocks = c->ncell * ngroup;
+    s.smem = multipole_smem(c->nrad, c->nang);
+    return s;
+}
+
+int group_multipole(const MpArgs *d_args, const GroupQueue &q, size_t smem, int device, int nsm, cudaStream_t st)
+{
+    DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_multipole_group), device));
+    int occ = 0;
+    DFTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_multipole_group, kMpThreads, smem));
+    const int grid = group_grid(q, occ, nsm);
+    if (grid > 0) k_multipole_group<<<grid, kMpThreads, smem, st>>>(d_args, q);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }
@@ -1374,13 +1487,9 @@ int launch_hartree_multipoles(dftg_ctx *c)
     const int nrhs = nc * nlm;
     if (mp) {
         // rho_lm, Poisson and splines in one launch per (cell, group of l, m rows)
-        const int ngroup = (nlm + kMpLG - 1) / kMpLG;
-        const size_t sm = multipole_smem(N, c->nang);
-        if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_multipole), c->device));
-        k_multipole<<<(unsigned)(nc * ngroup), kMpThreads, sm, c->stream>>>(
-            c->natoms, c0, N, c->nang, c->lmax, ngroup, c->rw_ready ? c->d_rw32 : nullptr, c->npad, c->d_rho, c->d_wb,
-            c->d_w, c->d_Ywt32, c->d_maps32, c->d_scal, c->d_U, c->d_U32, c->d_U32T, (c->prec_mask & kPrecCross) ? 0 : 1,
-            c->d_spl, c->d_splm);
+        const StepLaunch<MpArgs> st = step_multipole(c, c->rw_ready);
+        if (st.smem > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_multipole), c->device));
+        k_multipole<<<st.blocks, kMpThreads, st.smem, c->stream>>>(st.args);
         DFTG_LAUNCH_CHECK();
         DFTG_MARK(c, "multipole");
         if (!(c->prec_mask & kPrecCross)) {
@@ -1416,6 +1525,31 @@ int launch_hartree_multipoles(dftg_ctx *c)
     return DFTG_OK;
 }
 
+StepLaunch<GoArgs> step_gather_own(const dftg_ctx *c, bool rho_scaled)
+{
+    const int N = c->nrad;
+    const int nslab = (c->nang + kGoSlab - 1) / kGoSlab, nsplit = (N + kGoShells - 1) / kGoShells;
+    StepLaunch<GoArgs> s;
+    s.args = GoArgs{c->npts, c->npad, (size_t)c->natoms * c->nlm * N, c->natoms, c->cell0, N, c->nang, c->nlm, nslab,
+                    nsplit, rho_scaled ? 1 : 0, c->d_pairpos, reinterpret_cast<const float2 *>(c->d_pairv), c->d_U32T,
+                    c->d_Y32, c->d_invr, c->d_w, c->d_rho, c->d_V, c->d_cj, c->d_cj32, c->d_red, c->d_scal,
+                    c->d_counters + kCntEJ};
+    s.blocks = c->ncell * nslab * nsplit;
+    s.smem = sizeof(float) * 2 * (size_t)c->nlm * (kGoSlab + kGoShells);
+    return s;
+}
+
+int group_gather_own(const GoArgs *d_args, const GroupQueue &q, size_t smem, int device, int nsm, cudaStream_t st)
+{
+    DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_vcross_gather_own_group), device));
+    int occ = 0;
+    DFTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_vcross_gather_own_group, kGoThreads, smem));
+    const int grid = group_grid(q, occ, nsm);
+    if (grid > 0) k_vcross_gather_own_group<<<grid, kGoThreads, smem, st>>>(d_args, q);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
 // cross-atom part: the potential of every other atom's spline expansion on the
 // context's points, the total V, cj = w V / 2 and E_J
 int launch_hartree_cross(dftg_ctx *c)
@@ -1429,16 +1563,10 @@ int launch_hartree_cross(dftg_ctx *c)
         }
         if (mp) {
             // own-cell potential, total potential and E_J in one pass
-            const size_t uhalf = (size_t)c->natoms * c->nlm * N;
-            const int nslab = (c->nang + kGoSlab - 1) / kGoSlab, nsplit = (N + kGoShells - 1) / kGoShells;
-            const size_t nblk = (size_t)c->ncell * nslab * nsplit;
-            if (nblk > c->red_elems) { set_error("reduction buffer too small for %zu blocks", nblk); return DFTG_ERR_STATE; }
-            const size_t sm = sizeof(float) * 2 * (size_t)c->nlm * (kGoSlab + kGoShells);
-            if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_vcross_gather_own), c->device));
-            k_vcross_gather_own<<<(unsigned)nblk, kGoThreads, sm, c->stream>>>(
-                c->npts, c->npad, c->natoms, c->cell0, N, c->nang, c->nlm, nslab, nsplit, c->d_pairpos,
-                reinterpret_cast<const float2 *>(c->d_pairv), c->d_U32T, uhalf, c->d_Y32, c->d_invr, c->d_w, c->d_rho,
-                c->rho_scaled ? 1 : 0, c->d_V, c->d_cj, c->d_cj32, c->d_red, c->d_scal, c->d_counters + kCntEJ);
+            const StepLaunch<GoArgs> st = step_gather_own(c, c->rho_scaled);
+            if ((size_t)st.blocks > c->red_elems) { set_error("reduction buffer too small for %d blocks", st.blocks); return DFTG_ERR_STATE; }
+            if (st.smem > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_vcross_gather_own), c->device));
+            k_vcross_gather_own<<<st.blocks, kGoThreads, st.smem, c->stream>>>(st.args);
             DFTG_LAUNCH_CHECK();
             DFTG_MARK(c, "vcross");
             return DFTG_OK;

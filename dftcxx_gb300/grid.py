@@ -398,18 +398,42 @@ class PointGrid(MolecularGrid):
 
 
 class Batch:
-    """Many MolecularGrid contexts built in one launch (dftg_batch_*): the
-    per-build kernel sequences are captured into one CUDA graph with a stream
-    branch per context and replayed.  Buffers are device tensors (torch), one
-    set per context; build() returns nothing and does not synchronise."""
+    """Many MolecularGrid contexts built together (dftg_batch_*).  mode
+    "persistent" (the default): every step of the mixed build is one persistent
+    launch over all contexts, taking (context, block) items from a device queue;
+    "graph": the per-build kernel sequences on one stream branch per context.
+    Either form is captured into a CUDA graph and replayed.  Buffers are device
+    tensors (torch), one set per context; build() returns nothing and does not
+    synchronise (status() does, and reports expired bounded waits)."""
 
-    def __init__(self, grids):
+    MODES = {"persistent": 0, "graph": 1}
+
+    def __init__(self, grids, mode="persistent"):
         self.grids = list(grids)
         n = len(self.grids)
         arr = (ctypes.c_void_p * n)(*[g.handle for g in self.grids])
         h = ctypes.c_void_p()
         check(_lib.load().dftg_batch_create(arr, n, ctypes.byref(h)))
         self._h = h.value
+        self.set_mode(mode)
+
+    def set_mode(self, mode):
+        check(_lib.load().dftg_batch_set_mode(self._h, self.MODES[mode]))
+
+    def persistent_active(self):
+        """True when the last build ran as the persistent launches."""
+        flag = ctypes.c_int()
+        _lib.load().dftg_batch_get_mode(self._h, ctypes.byref(flag))
+        return bool(flag.value)
+
+    def status(self):
+        """Synchronise the last batch; raises DftgError on an expired wait."""
+        check(_lib.load().dftg_batch_status(self._h))
+
+    def selftest_wait(self, limit_ms=20.0):
+        """Return code of the persistent launches' bounded-wait self-test
+        (DFTG_ERR_TIMEOUT expected)."""
+        return _lib.load().dftg_batch_selftest_wait(self._h, float(limit_ms))
 
     def close(self):
         if getattr(self, "_h", None):

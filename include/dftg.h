@@ -262,16 +262,44 @@ int dftg_backward_device(dftg_ctx *ctx, double seed_exc, double seed_ej, double 
 int dftg_backward_profile(dftg_ctx *ctx, double seed_exc, double seed_ej, double *phase_ms, const char **names,
                           int cap, int *nphase);
 
-/* Batched builds (no counterpart in the reference): many contexts -- molecules
- * or geometries of any size -- built in one launch.  The per-build kernel
- * sequences of all contexts are captured once into one CUDA graph, each
- * context on its own stream branch, and the graph is replayed; the first call
- * with a new set of buffers runs the builds one after another and the next one
+/* Batched builds (no counterpart in the reference; its driver builds one
+ * molecule at a time, dft.cpp:84-142): many contexts -- molecules or
+ * geometries of any size -- built together.  Two forms:
+ *   DFTG_BATCH_PERSISTENT (default): every step of the mixed build runs as ONE
+ *     persistent launch over all contexts (nine launches per batch); each CTA
+ *     takes (context, block) work items from a device queue and runs each as
+ *     that block of the context's own launch, so every context's results are
+ *     bit-identical to its single build.  The per-atom sums and the LDA point
+ *     kernel share one launch: a context's point blocks wait, bounded (2 s),
+ *     for its correction factor; a wait that gives up is reported by
+ *     dftg_batch_status.  Needs every context in mixed precision with the
+ *     tensor-core density and contraction (nbf <= 80) and <= 256 radial points;
+ *     otherwise the batch falls back to the graph of branches.
+ *   DFTG_BATCH_GRAPH: each context's kernel sequence on its own stream branch
+ *     of one CUDA graph (any precision, any size).
+ * Either way the launches are captured into a CUDA graph and replayed: the
+ * first call with a new set of buffers runs eagerly and the next one
  * captures.  The contexts must be distinct and stay alive while the batch
- * exists; each context keeps its own precision setting. */
+ * exists. */
+#define DFTG_BATCH_PERSISTENT 0
+#define DFTG_BATCH_GRAPH 1
 typedef struct dftg_batch dftg_batch;
 int dftg_batch_create(dftg_ctx *const *ctxs, int n, dftg_batch **out);
 int dftg_batch_destroy(dftg_batch *b);
+/* Select the form (takes effect at the next build).  dftg_batch_get_mode
+ * returns the selected form and sets *persistent_active (may be NULL) to 1 when
+ * the last build ran as persistent launches. */
+int dftg_batch_set_mode(dftg_batch *b, int mode);
+int dftg_batch_get_mode(const dftg_batch *b, int *persistent_active);
+/* Synchronise the batch's last launch and report its bounded waits:
+ * DFTG_ERR_TIMEOUT when one gave up (the flags are cleared), else DFTG_OK. */
+int dftg_batch_status(dftg_batch *b);
+/* Self-test of the persistent batch's bounded wait: runs the fused atom-sum +
+ * point launch with the first context's waits on a flag that nothing sets,
+ * limit limit_ms (0 < limit_ms <= 2000); returns DFTG_ERR_TIMEOUT.  The
+ * contexts' results are then incomplete until their next build (DFTG_ERR_STATE
+ * for calls that need one).  Needs a preceding persistent build. */
+int dftg_batch_selftest_wait(dftg_batch *b, double limit_ms);
 /* dftg_fock_build_device for every context i with P_devs[i], J_devs[i],
  * XC_devs[i], scalars_devs[i] (arrays of n device pointers; J, XC and scalars
  * entries may be NULL).  stream: a cudaStream_t the batch is ordered on: its
@@ -285,9 +313,10 @@ int dftg_batch_destroy(dftg_batch *b);
 int dftg_batch_fock_build_device(dftg_batch *b, const double *const *P_devs, double *const *J_devs,
                                  double *const *XC_devs, double *const *scalars_devs, void *stream);
 /* Batch autotuner: scales every context's CTA counts by 1, 1/2, 1/4 and 1/8
- * together (the graph's branches run concurrently), times reps replays of the
- * batch graph on the contexts' own last P and keeps the fastest scale; needs a
- * complete build of every context.  best_ms (per batch replay) may be NULL. */
+ * together (more work items per CTA in the persistent form; concurrent
+ * branches in the graph form), times reps replays of the batch on the
+ * contexts' own last P and keeps the fastest scale; needs a complete build of
+ * every context.  best_ms (per batch replay) may be NULL. */
 int dftg_batch_autotune(dftg_batch *b, int reps, double *best_ms);
 
 /* Launch-shape autotuner (no counterpart in the reference).  Shape =
