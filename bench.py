@@ -69,9 +69,9 @@ def _fixed_density():
 # density = P slicing with the correction factor + the tensor-core density with
 # the LDA point kernel; multipole = rho_lm, Poisson and splines; vcross = the
 # pair evaluation + the own-cell / total potential with E_J
-KERNELS_PER_PHASE = {"density": 2, "charge": 1, "lda": 1, "multipole": 1, "rholm": 1, "poisson": 1, "vown": 1,
-                     "splines": 1, "vcross": 2, "hartree_energy": 1, "contract_bounds": 1, "contract": 1,
-                     "contract_reduce": 1}
+KERNELS_PER_PHASE = {"density_slices": 1, "density": 1, "charge": 1, "lda": 1, "multipole": 1, "rholm": 1,
+                     "poisson": 1, "vown": 1, "splines": 1, "vcross_bins": 1, "vcross": 1, "hartree_energy": 1,
+                     "contract_bounds": 1, "contract": 1, "contract_reduce": 1}
 
 
 def _env_int(name, default):
@@ -423,7 +423,10 @@ def run_ours(args, rank, world):
         # V_xc and J in one pass: Npts nbf amplitudes, two point coefficients
         "contract": 6 * npts * nbf + 16 * npts,
         # per pair: direction and 1/r (16 B), offset and bin (8 B) in, contribution (8 B) out
-        "vcross": 32 * npairs,
+        "vcross_bins": 32 * npairs,
+        # per point: pair places (4 B per atom), pair contributions (8 B per other
+        # atom), w, rho, 1/r in; V, cj (FP64) and cj (FP32) out
+        "vcross": npts * (12 * mol.natoms + 36),
         "lda": npts * (8 + 8 + 8) + npts * (8 + 4),
     }
     layout_bytes = {

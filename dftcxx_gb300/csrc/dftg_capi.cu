@@ -1504,8 +1504,9 @@ extern "C" int dftg_batch_selftest_wait(dftg_batch *b, double limit_ms)
 }
 
 // Autotuner of a batch: the contexts' CTA counts scaled together by 1, 1/2,
-// 1/4 and 1/8 (branches of the graph run concurrently, so smaller grids per
-// build can raise the throughput); the graph of every candidate is timed on the
+// 1/4 and 1/8 (and 1/16, 1/32 in the persistent form: fewer, longer work items
+// per molecule; in the graph form the branches run concurrently, so smaller
+// grids per build can raise the throughput); every candidate is timed on the
 // contexts' own density matrices and the fastest scale is kept.
 extern "C" int dftg_batch_autotune(dftg_batch *b, int reps, double *best_ms)
 {
@@ -1551,10 +1552,13 @@ extern "C" int dftg_batch_autotune(dftg_batch *b, int reps, double *best_ms)
     double best = 0.0;
     int best_div = 1;
     DFTG_TRY(run(1, &best));
-    for (int div : {2, 4, 8}) {
+    // the persistent form also tries fewer, longer work items per molecule
+    const int ndiv = b->mode == DFTG_BATCH_PERSISTENT ? 5 : 3;
+    const int divs[5] = {2, 4, 8, 16, 32};
+    for (int k = 0; k < ndiv; ++k) {
         double t = 0.0;
-        DFTG_TRY(run(div, &t));
-        if (t < best) { best = t; best_div = div; }
+        DFTG_TRY(run(divs[k], &t));
+        if (t < best) { best = t; best_div = divs[k]; }
     }
     double t = 0.0;
     DFTG_TRY(run(best_div, &t));   // leave the chosen shapes and their outputs

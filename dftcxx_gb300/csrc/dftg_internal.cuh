@@ -300,8 +300,8 @@ struct dftg_ctx {
     // device: tensor-core density (integer-slice split of phi and P)
     bool tc_ready = false;
     int tc_KP = 0, tc_NP = 0, tc_grid = 0;
-    void *d_tcA = nullptr;        // [4][tiles][128 x KP] BF16 slices of phi
-    void *d_tcB = nullptr;        // [4][NP x KP] BF16 slices of P
+    void *d_tcA = nullptr;        // [3][tiles][128 x KP] FP16 slices of phi
+    void *d_tcB = nullptr;        // [3][NP x KP] FP16 slices of P
     int *d_tc_rowexp = nullptr;   // [npad] per-point scale exponents
     int *d_tc_colexp = nullptr;   // [NP] per-column scale exponents of P
     float *d_rw32 = nullptr;      // [2][npad] rho w_becke split into FP32 hi, lo (mixed multipole input)

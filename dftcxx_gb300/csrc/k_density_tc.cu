@@ -4,71 +4,81 @@
 // The energy depends on rho at first order, so rho must carry near-FP64
 // accuracy; FP32 or 3xTF32 arithmetic leaves ~1e-7 random errors per point,
 // about 3e-6 Ha on benzene.  The GEMM T = Phi P is therefore done as an
-// integer-slice product (Ozaki's error-free splitting) on the BF16 tensor cores:
+// integer-slice product (Ozaki's error-free splitting) on the FP16 tensor cores,
+// with three fixed-point slices per operand:
 //
-//   Phi[p, mu] = 2^e_p  sum_{i=1..4} a_i[p, mu] 2^(-8 i)      (per point e_p)
-//   P[mu, nu]  = 2^t_nu sum_{j=1..4} b_j[mu, nu] 2^(-8 j)     (per column t_nu)
+//   Phi[p, mu] 2^(8 - e_p) = A_1 + A_2 + 2^-11 A_3      (per point e_p, |Phi| < 2^e_p)
+//   P[mu, nu]  2^(8 - t_nu) = B_1 + B_2 + 2^-11 B_3     (per column t_nu)
 //
-// with integers |a_1|, |b_1| <= 256 and |a_i|, |b_j| <= 128.  Slice i is
-// stored pre-scaled, A_i = a_i 2^(-8(i-1)) (exact in BF16), so every pair
-// (i, j) contributes A_i B_j with the same weight 2^-16 2^(e_p + t_nu):
-//   D_hi = A_1 B_1           integer products, exact in the FP32 accumulator
-//   D_lo = the other 9 pairs with i + j <= 5, about 2^-8 of D_hi; its FP32
-//          rounding stays near 2^-32 of D_hi, the size of the dropped pairs.
-// The epilogue forms T = D_hi + D_lo with TwoSum and rho = 2 sum_nu T_nu phi_nu
-// in compensated FP32, phi rebuilt exactly from the slices in shared memory.
+// A_1 an integer (|A_1| <= 256), A_2 and A_3 multiples of 2^-11 (|.| <= 1/2):
+// every slice is exact in FP16, and together they hold the operand to 2^-31
+// of its row maximum.  Three accumulators per tile:
+//   D_hi  = A_1 B_1                               integer products, exact in FP32
+//   D_lo  = A_1 B_2 + A_2 B_1 + A_2 B_2            about 2^-9 of D_hi
+//   D_lo2 = A_1 B_3 + A_3 B_1 + A_2 B_3 + A_3 B_2  weight 2^-11
+// (A_3 B_3, 2^-22 x 2^-22 of the head, is dropped): eight MMAs per K step.  The
+// epilogue forms T = D_hi + D_lo + 2^-11 D_lo2 with TwoSum and rho = 2 sum_nu
+// T_nu phi_nu in compensated FP32, phi rebuilt exactly from the slices in
+// shared memory (A_1 + A_2 is exact in FP32).  Six bytes per operand element.
 //
 // Layouts (canonical no-swizzle K-major core matrices, 8 rows x 16 bytes,
 // cores ordered row group by row group: LBO 128 B, SBO (KP/8) 128 B):
-//   A slices in HBM: [slice][tile][128/8][KP/8][8][8] BF16, one contiguous
+//   A slices in HBM: [slice][tile][128/8][KP/8][8][8] FP16, one contiguous
 //     128 x KP block per slice and tile, copied with cp.async.bulk;
-//   B slices: [slice][NP/8][KP/8][8][8] BF16 (rows nu, K = mu).
+//   B slices: [slice][NP/8][KP/8][8][8] FP16 (rows nu, K = mu).
 // CTA: warp 0 producer (bulk copies), warp 1 TMEM owner + MMA issuer,
 // warps 2-9 epilogue: TMEM lanes 32 (w % 4) ..., the two warps of a lane quarter
-// take alternate 16-column blocks and meet in shared memory per tile.  Persistent over tiles, two
-// A stages and two TMEM accumulator pairs, so the MMAs of one tile overlap the
-// epilogue of the previous one.  Every mbarrier wait is bounded: on expiry the
-// CTA records an error code, drains its copies, frees TMEM and exits.
+// take alternate 16-column blocks and meet in shared memory per tile.
+// Persistent over tiles: three A stages and two TMEM accumulator sets, so the
+// copies of the next tiles and the MMAs of one tile overlap the epilogue of the
+// previous one.  Every mbarrier wait is bounded: on expiry the CTA records an
+// error code, drains its copies, frees TMEM and exits.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cstdint>
 #include "dftg_internal.cuh"
 #include "tc_common.cuh"
 
 namespace dftg {
 
-constexpr int kTcSlices = 4;
+constexpr int kTcSlices = 3;
+constexpr int kTcStages = 3;                  // A stages (copies in flight + the tile in use)
+constexpr int kTcAcc = 80;                    // TMEM column stride of the three accumulators of a set
 constexpr int kTcTile = 128;
 constexpr int kTcMaxK = 80;                   // nbf <= 80 for this kernel
-constexpr int kTcThreads = 320;
+constexpr int kTcEpiWarps = 16;               // four per TMEM lane quarter
+constexpr int kTcThreads = (2 + kTcEpiWarps) * 32;
 constexpr uint32_t kTcTmemCols = 512;
-// named barrier 1 over the 8 epilogue warps
-__device__ __forceinline__ void epi8_bar_sync()
+// named barrier 1 over the epilogue warps
+__device__ __forceinline__ void epi_bar_sync_tc()
 {
-    asm volatile("bar.sync 1, 256;" ::: "memory");
+    asm volatile("bar.sync 1, %0;" ::"n"(kTcEpiWarps * 32) : "memory");
 }
 
-__device__ __forceinline__ void unpack8_bf16(uint4 u, float (&v)[8])
+__device__ __forceinline__ void unpack8_f16(uint4 u, float (&v)[8])
 {
     const uint32_t w[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        v[2 * j] = __uint_as_float(w[j] << 16);
-        v[2 * j + 1] = __uint_as_float(w[j] & 0xffff0000u);
+        const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&w[j]));
+        v[2 * j] = f.x;
+        v[2 * j + 1] = f.y;
     }
 }
 
 struct TcShared {
-    uint64_t full[2], empty[2], tmem_full[2], tmem_empty[2];
+    uint64_t full[kTcStages], empty[kTcStages], tmem_full[2], tmem_empty[2];
     uint32_t tmem_base;
     int item;                              // the grouped launch's queue position (broadcast)
 };
+
+// the CTA's mbarriers and TMEM address (one instance in every kernel that uses them)
+__shared__ TcShared tc_sh;
 
 // One CTA's share of one molecule's tiles (vb, vb + nvb, ...): initialises the
 // mbarriers, stages the B slices, runs the producer / MMA / epilogue roles and
 // invalidates the mbarriers again.  The caller owns the kTcTmemCols TMEM
 // columns at tmem.  Returns false (block-uniform) when a bounded wait gave up.
-// the CTA's mbarriers and TMEM address (one instance in every kernel that uses them)
-__shared__ TcShared tc_sh;
 
 __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, int nvb, uint32_t tmem)
 {
@@ -84,17 +94,19 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
     const uint32_t a_slice_bytes = (uint32_t)kTcTile * KP * 2;
     const uint32_t a_stage_bytes = kTcSlices * a_slice_bytes;
     const uint32_t b_slice_bytes = (uint32_t)NP * KP * 2;
-    unsigned char *sA = smem;                                   // [2][slices][tile block]
-    unsigned char *sB = smem + 2 * a_stage_bytes;                // [slices][B block]
-    __shared__ int s_texp[kTcMaxK];
+    unsigned char *sA = smem;                                   // [stages][slices][tile block]
+    unsigned char *sB = smem + kTcStages * a_stage_bytes;        // [slices][B block]
+    __shared__ __align__(16) int s_texp[kTcMaxK];
     __shared__ int s_fail;
-    __shared__ float2 s_half[kTcTile];            // (S, E) of the second column half, per row
+    __shared__ float2 s_part[3][kTcTile];         // (S, E) of column parts 1-3, per row
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < kTcStages; ++b) {
             mbar_init(&sh->full[b], 1);
             mbar_init(&sh->empty[b], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
             mbar_init(&sh->tmem_full[b], 1);
             mbar_init(&sh->tmem_empty[b], 1);
         }
@@ -119,15 +131,15 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
         // ------------------------------------------------------------ producer
         int issued = 0;
         if (lane == 0) {
-            // L2 prefetch two tiles ahead of the bulk copies
-            for (int it = 0; it < 2 && it < my_tiles; ++it)
+            // L2 prefetch a ring's depth ahead of the bulk copies
+            for (int it = 0; it < kTcStages && it < my_tiles; ++it)
                 for (int i = 0; i < kTcSlices; ++i)
                     prefetch_l2(Aslices + ((size_t)i * ntiles + vb + it * nvb) * a_slice_bytes, a_slice_bytes);
             for (int it = 0; it < my_tiles; ++it) {
-                const int s = it & 1, n = it >> 1;
-                if (it + 2 < my_tiles)
+                const int s = it % kTcStages, n = it / kTcStages;
+                if (it + kTcStages < my_tiles)
                     for (int i = 0; i < kTcSlices; ++i)
-                        prefetch_l2(Aslices + ((size_t)i * ntiles + vb + (it + 2) * nvb) * a_slice_bytes,
+                        prefetch_l2(Aslices + ((size_t)i * ntiles + vb + (it + kTcStages) * nvb) * a_slice_bytes,
                                     a_slice_bytes);
                 if (!mbar_wait(&sh->empty[s], (uint32_t)((n & 1) ^ 1))) { atomicExch(err, 1); s_fail = 1; break; }
                 if (s_fail) break;
@@ -139,102 +151,103 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
                 issued = it + 1;
             }
             // drain: every issued stage must have landed before the CTA exits
-            for (int it = (issued > 2 ? issued - 2 : 0); it < issued; ++it)
-                mbar_wait(&sh->full[it & 1], (uint32_t)((it >> 1) & 1));
+            for (int it = (issued > kTcStages ? issued - kTcStages : 0); it < issued; ++it)
+                mbar_wait(&sh->full[it % kTcStages], (uint32_t)((it / kTcStages) & 1));
         }
         __syncwarp();
     } else if (warp == 1) {
         // ------------------------------------------------------------ MMA issuer
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16(kTcTile, NP);
+            const uint32_t idesc = idesc_f16(kTcTile, NP);
             const uint32_t lbo = 128, sbo = (uint32_t)(KP / 8) * 128;
             // descriptors built once; every operand is a fixed byte offset from these
             const uint64_t a_desc0 = smem_desc(sA, lbo, sbo), b_desc0 = smem_desc(sB, lbo, sbo);
             const int ksteps = KP / 16;
             for (int it = 0; it < my_tiles; ++it) {
-                const int s = it & 1, n = it >> 1;   // A stage and TMEM buffer share the index
-                if (!mbar_wait(&sh->full[s], (uint32_t)(n & 1))) { atomicExch(err, 2); s_fail = 1; break; }
-                if (!mbar_wait(&sh->tmem_empty[s], (uint32_t)((n & 1) ^ 1))) { atomicExch(err, 3); s_fail = 1; break; }
+                const int s = it % kTcStages, ns = it / kTcStages;   // A stage
+                const int bset = it & 1, nb = it >> 1;               // TMEM accumulator set
+                if (!mbar_wait(&sh->full[s], (uint32_t)(ns & 1))) { atomicExch(err, 2); s_fail = 1; break; }
+                if (!mbar_wait(&sh->tmem_empty[bset], (uint32_t)((nb & 1) ^ 1))) { atomicExch(err, 3); s_fail = 1; break; }
                 if (s_fail) break;
                 tc_fence_after();
                 const uint64_t a_st = desc_add(a_desc0, (uint32_t)s * a_stage_bytes);
-                const uint32_t d_hi = tmem + (uint32_t)(s * 256), d_lo = d_hi + 128;
-                // K step outermost (the tensor core reuses the K block's operands): the
-                // leading product A_1 B_1 into D_hi, the nine correction pairs into D_lo
+                const uint32_t d_hi = tmem + (uint32_t)(bset * 256), d_lo = d_hi + kTcAcc, d_lo2 = d_hi + 2 * kTcAcc;
+                // K step outermost (the tensor core reuses the K block's operands)
                 for (int kk = 0; kk < ksteps; ++kk) {
                     const uint64_t ak = desc_add(a_st, kk * 2 * lbo), bk = desc_add(b_desc0, kk * 2 * lbo);
-#pragma unroll
-                    for (int i = 1; i <= 4; ++i)
-#pragma unroll
-                        for (int j = 1; i + j <= 5; ++j) {
-                            const uint64_t ad = desc_add(ak, (uint32_t)(i - 1) * a_slice_bytes);
-                            const uint64_t bd = desc_add(bk, (uint32_t)(j - 1) * b_slice_bytes);
-                            if (i == 1 && j == 1) mma_bf16(d_hi, ad, bd, idesc, kk > 0 ? 1u : 0u);
-                            else mma_bf16(d_lo, ad, bd, idesc, (kk == 0 && i == 1 && j == 2) ? 0u : 1u);
-                        }
+                    const uint64_t a1 = ak, a2 = desc_add(ak, a_slice_bytes), a3 = desc_add(ak, 2 * a_slice_bytes);
+                    const uint64_t b1 = bk, b2 = desc_add(bk, b_slice_bytes), b3 = desc_add(bk, 2 * b_slice_bytes);
+                    const uint32_t acc = kk > 0 ? 1u : 0u;
+                    mma_bf16(d_hi, a1, b1, idesc, acc);
+                    mma_bf16(d_lo, a1, b2, idesc, acc);
+                    mma_bf16(d_lo, a2, b1, idesc, 1u);
+                    mma_bf16(d_lo, a2, b2, idesc, 1u);
+                    mma_bf16(d_lo2, a1, b3, idesc, acc);
+                    mma_bf16(d_lo2, a3, b1, idesc, 1u);
+                    mma_bf16(d_lo2, a2, b3, idesc, 1u);
+                    mma_bf16(d_lo2, a3, b2, idesc, 1u);
                 }
-                mma_commit(&sh->tmem_full[s]);
+                mma_commit(&sh->tmem_full[bset]);
             }
         }
         __syncwarp();
     } else {
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3;                 // TMEM lane quarter of this warp
-        const int half = (warp - 2) >> 2;       // column blocks half, half + 2, ...
+        const int part = (warp - 2) >> 2;       // 8-column groups part, part + 4, ...
         const int r = q * 32 + lane;            // row of the tile = TMEM lane
         const int kc = KP / 8;
         for (int it = 0; it < my_tiles; ++it) {
-            const int s = it & 1, n = it >> 1;
-            bool ok = mbar_wait(&sh->tmem_full[s], (uint32_t)(n & 1));
+            const int s = it % kTcStages;
+            const int bset = it & 1, nb = it >> 1;
+            bool ok = mbar_wait(&sh->tmem_full[bset], (uint32_t)(nb & 1));
             if (!ok) { atomicExch(err, 4); s_fail = 1; }
-            epi8_bar_sync();
+            epi_bar_sync_tc();
             if (s_fail) break;
             tc_fence_after();
             const int tile = vb + it * nvb;
             const size_t p = (size_t)tile * kTcTile + r;
             const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
-            const uint32_t ta0 = tmem + (uint32_t)(s * 256) + ((uint32_t)(q * 32) << 16);
+            const uint32_t ta0 = tmem + (uint32_t)(bset * 256) + ((uint32_t)(q * 32) << 16);
             // two independent compensated accumulators (even / odd columns)
             float S[2] = {0.f, 0.f}, E[2] = {0.f, 0.f};
-            for (int c0 = 16 * half; c0 < NP; c0 += 32) {
-                float dh[16], dl[16];
-                tmem_ld16(ta0 + (uint32_t)c0, dh);
-                tmem_ld16(ta0 + 128u + (uint32_t)c0, dl);
+            // columns nu >= nbf hold T = 0 and phi = 0 (zero rows of B, zero slices
+            // of A) and contribute exactly nothing, so every group is done whole
+            for (int nb8 = 8 * part; nb8 < nbf; nb8 += 32) {
+                float dh[8], dl[8], dl2[8];
+                tmem_ld8(ta0 + (uint32_t)nb8, dh);
+                tmem_ld8(ta0 + (uint32_t)(kTcAcc + nb8), dl);
+                tmem_ld8(ta0 + (uint32_t)(2 * kTcAcc + nb8), dl2);
+                // phi 2^(8 - e_p) of columns nb8..nb8+7 from the three slices (16 B each)
+                const uint32_t off = core_off(r, nb8, kc);
+                float m1[8], m2[8], m3[8];
+                unpack8_f16(*reinterpret_cast<const uint4 *>(a0 + off), m1);
+                unpack8_f16(*reinterpret_cast<const uint4 *>(a0 + a_slice_bytes + off), m2);
+                unpack8_f16(*reinterpret_cast<const uint4 *>(a0 + 2 * a_slice_bytes + off), m3);
+                const int4 e0 = *reinterpret_cast<const int4 *>(s_texp + nb8);
+                const int4 e1 = *reinterpret_cast<const int4 *>(s_texp + nb8 + 4);
+                const int ex[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
                 tmem_wait_ld();
 #pragma unroll
-                for (int g8 = 0; g8 < 2; ++g8) {
-                    const int nb = c0 + 8 * g8;
-                    if (nb >= nbf) break;
-                    // phi~ 2^8 of columns nb..nb+7 from the four pre-scaled slices (16 B each)
-                    const uint32_t off = core_off(r, nb, kc);
-                    float m1[8], m2[8], m3[8], m4[8];
-                    unpack8_bf16(*reinterpret_cast<const uint4 *>(a0 + off), m1);
-                    unpack8_bf16(*reinterpret_cast<const uint4 *>(a0 + a_slice_bytes + off), m2);
-                    unpack8_bf16(*reinterpret_cast<const uint4 *>(a0 + 2 * a_slice_bytes + off), m3);
-                    unpack8_bf16(*reinterpret_cast<const uint4 *>(a0 + 3 * a_slice_bytes + off), m4);
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) {
-                        const int nu = nb + k;
-                        if (nu >= nbf) continue;
-                        const int j = 8 * g8 + k;
-                        // T~_nu 2^16 = D_hi + D_lo: exact head by TwoSum
-                        const float u = dh[j] + dl[j];
-                        const float bp = u - dh[j];
-                        float te = (dh[j] - (u - bp)) + (dl[j] - bp);
-                        const float sc = __int_as_float((127 - 16 + s_texp[nu]) << 23);
-                        const float t = u * sc;
-                        te *= sc;
-                        const float fh = (m1[k] + m2[k]) * 0x1p-8f;
-                        const float fl = (m3[k] + m4[k]) * 0x1p-8f;
-                        // S + E += (t + te)(fh + fl)
-                        const int a = k & 1;
-                        const float pr = t * fh;
-                        const float pe = fmaf(t, fh, -pr);
-                        const float w = S[a] + pr;
-                        const float bq = w - S[a];
-                        E[a] += (S[a] - (w - bq)) + (pr - bq) + pe + fmaf(t, fl, te * fh);
-                        S[a] = w;
-                    }
+                for (int k = 0; k < 8; ++k) {
+                    // T~_nu 2^16 = D_hi + D_lo + 2^-11 D_lo2 as u + te (TwoSum of the
+                    // first two), scaled by 2^(t_nu - 24); phi~ 2^8 = fh + fl
+                    const float u = dh[k] + dl[k];
+                    const float bp = u - dh[k];
+                    float te = (dh[k] - (u - bp)) + (dl[k] - bp) + dl2[k] * 0x1p-11f;
+                    const float sc = __int_as_float((127 - 24 + ex[k]) << 23);
+                    const float t = u * sc;
+                    te *= sc;
+                    const float fh = m1[k] + m2[k];                      // exact: multiples of 2^-11 below 2^9
+                    const float fl = m3[k] * 0x1p-11f;
+                    // S + E += (t + te)(fh + fl)
+                    const int a = k & 1;
+                    const float pr = t * fh;
+                    const float pe = fmaf(t, fh, -pr);
+                    const float w = S[a] + pr;
+                    const float bq = w - S[a];
+                    E[a] += ((S[a] - (w - bq)) + (pr - bq)) + (pe + fmaf(t, fl, te * fh));
+                    S[a] = w;
                 }
             }
             // fold the two accumulators (TwoSum)
@@ -246,17 +259,23 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
                 St = w;
             }
             tc_fence_before();
-            if (half == 1) s_half[r] = make_float2(St, Et);
-            epi8_bar_sync();                     // TMEM and A-stage reads of this tile done, halves posted
+            if (part > 0) s_part[part - 1][r] = make_float2(St, Et);
+            epi_bar_sync_tc();                   // TMEM and A-stage reads of this tile done, parts posted
             if (threadIdx.x == 64) {
-                mbar_arrive(&sh->tmem_empty[s]);
+                mbar_arrive(&sh->tmem_empty[bset]);
                 mbar_arrive(&sh->empty[s]);
             }
-            if (half == 0) {
-                const float2 o = s_half[r];
-                const float w = St + o.x;
-                const float bq = w - St;
-                const float e = Et + o.y + (St - (w - bq)) + (o.x - bq);
+            if (part == 0) {
+                // the four column parts in a fixed order (TwoSum)
+                float w = St, e = Et;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float2 o = s_part[k][r];
+                    const float t2 = w + o.x;
+                    const float bq = t2 - w;
+                    e += o.y + (w - (t2 - bq)) + (o.x - bq);
+                    w = t2;
+                }
                 const int ep = row_exp[p];
                 rho[p] = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
             }
@@ -265,13 +284,16 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
     tc_fence_before();
     __syncthreads();
     const bool ok = s_fail == 0;
-    if (threadIdx.x == 0)
-        for (int b = 0; b < 2; ++b) {
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < kTcStages; ++b) {
             mbar_inval(&sh->full[b]);
             mbar_inval(&sh->empty[b]);
+        }
+        for (int b = 0; b < 2; ++b) {
             mbar_inval(&sh->tmem_full[b]);
             mbar_inval(&sh->tmem_empty[b]);
         }
+    }
     return ok;
 }
 
@@ -323,9 +345,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_density_tc_group(const DensTc
 
 // ------------------------------------------------------------------ slicing
 
-// Phi (FP64, [nbf][npad]) -> 4 pre-scaled integer slices per element in the tile layout
+// x with |x| < 1 -> the three FP16 slices of x 2^8 = A_1 + A_2 + 2^-11 A_3: A_1 =
+// rint(x 2^8), A_2 the remainder rounded to a multiple of 2^-11, A_3 the next
+// remainder times 2^11, rounded likewise (FP64 steps, all exact)
+__device__ __forceinline__ void slice3_f16(double x, uint16_t (&h)[kTcSlices])
+{
+    x *= 256.0;
+    const double a1 = rint(x);
+    x -= a1;                                     // |x| <= 1/2
+    const double a2 = rint(x * 2048.0) * 0x1p-11;
+    x -= a2;                                     // |x| <= 2^-12
+    const double a3 = rint(x * 0x1p22) * 0x1p-11;
+    h[0] = __half_as_ushort(__float2half_rn((float)a1));
+    h[1] = __half_as_ushort(__float2half_rn((float)a2));
+    h[2] = __half_as_ushort(__float2half_rn((float)a3));
+}
+
+// Phi (FP64, [nbf][npad]) -> three FP16 slices per element in the tile layout
 __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const double *__restrict__ phi,
-                            __nv_bfloat16 *__restrict__ A, int *__restrict__ row_exp)
+                            __half *__restrict__ A, int *__restrict__ row_exp)
 {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npad) return;
@@ -343,15 +381,12 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const int mu = mu0 + k;
-            double x = mu < nbf ? ldexp(phi[(size_t)mu * npad + p], -e) : 0.0;
+            uint16_t h[kTcSlices];
+            slice3_f16(mu < nbf ? ldexp(phi[(size_t)mu * npad + p], -e) : 0.0, h);
 #pragma unroll
             for (int i = 0; i < kTcSlices; ++i) {
-                x *= 256.0;
-                const double m = rint(x);
-                x -= m;
-                const uint32_t h = __bfloat16_as_ushort(__float2bfloat16_rn((float)ldexp(m, -8 * i)));
-                if (k & 1) w[i][k >> 1] |= h << 16;
-                else w[i][k >> 1] = h;
+                if (k & 1) w[i][k >> 1] |= (uint32_t)h[i] << 16;
+                else w[i][k >> 1] = h[i];
             }
         }
         const size_t o16 = ((size_t)tile * kTcTile * KP * 2 + core_off(r, mu0, KP / 8)) / 16;
@@ -360,14 +395,14 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
     }
 }
 
-// P (FP64, nbf x nbf, symmetric) -> 4 pre-scaled integer slices per column in
-// the B layout: one warp per column, lanes over the rows; with Pcopy the warp
-// also copies its column of P there
+// P (FP64, nbf x nbf, symmetric) -> three FP16 slices per column in the B
+// layout: one warp per column, lanes over the rows; with Pcopy the warp also
+// copies its column of P there
 __device__ __forceinline__ void slice_P_block(const SlicePArgs a, int vb)
 {
     const int nbf = a.nbf, KP = a.KP, NP = a.NP;
     const double *__restrict__ P = a.P;
-    __nv_bfloat16 *__restrict__ B = static_cast<__nv_bfloat16 *>(a.B);
+    uint16_t *__restrict__ B = static_cast<uint16_t *>(a.B);
     const int nu = vb * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (nu >= NP) return;
     double mx = 0.0;
@@ -383,14 +418,10 @@ __device__ __forceinline__ void slice_P_block(const SlicePArgs a, int vb)
     if (nu < nbf && lane == 0) a.col_exp[nu] = e;
     const size_t slice = (size_t)NP * KP;
     for (int mu = lane; mu < KP; mu += 32) {
-        double x = (nu < nbf && mu < nbf) ? ldexp(P[(size_t)nu * nbf + mu], -e) : 0.0;
+        uint16_t h[kTcSlices];
+        slice3_f16((nu < nbf && mu < nbf) ? ldexp(P[(size_t)nu * nbf + mu], -e) : 0.0, h);
         const size_t o = core_off(nu, mu, KP / 8) / 2;
-        for (int i = 0; i < kTcSlices; ++i) {
-            x *= 256.0;
-            const double m = rint(x);
-            x -= m;
-            B[(size_t)i * slice + o] = __float2bfloat16_rn((float)ldexp(m, -8 * i));
-        }
+        for (int i = 0; i < kTcSlices; ++i) B[(size_t)i * slice + o] = h[i];
     }
 }
 
@@ -410,7 +441,7 @@ __global__ void __launch_bounds__(kSlicePThreads) k_slice_P_group(const SlicePAr
 
 size_t density_tc_smem(int KP, int NP)
 {
-    return 2 * (size_t)kTcSlices * kTcTile * KP * 2 + (size_t)kTcSlices * NP * KP * 2 + 64;
+    return (size_t)kTcStages * kTcSlices * kTcTile * KP * 2 + (size_t)kTcSlices * NP * KP * 2 + 64;
 }
 
 bool density_tc_supported(int nbf) { return nbf <= kTcMaxK; }
@@ -422,16 +453,16 @@ int density_tc_setup(dftg_ctx *c)
     c->tc_NP = c->tc_KP;
     const int ntiles = (int)(c->npad / kTcTile);
     const size_t aslice = (size_t)ntiles * kTcTile * c->tc_KP;
-    DFTG_CUDA(cudaMalloc(&c->d_tcA, sizeof(__nv_bfloat16) * kTcSlices * aslice));
+    DFTG_CUDA(cudaMalloc(&c->d_tcA, sizeof(__half) * kTcSlices * aslice));
     DFTG_CUDA(cudaMalloc(&c->d_tc_rowexp, sizeof(int) * c->npad));
-    DFTG_CUDA(cudaMalloc(&c->d_tcB, sizeof(__nv_bfloat16) * kTcSlices * c->tc_NP * c->tc_KP));
+    DFTG_CUDA(cudaMalloc(&c->d_tcB, sizeof(__half) * kTcSlices * c->tc_NP * c->tc_KP));
     DFTG_CUDA(cudaMalloc(&c->d_tc_colexp, sizeof(int) * c->tc_NP));
     if (!c->d_flag) {
         DFTG_CUDA(cudaMalloc(&c->d_flag, sizeof(int)));
         DFTG_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
     }
     k_slice_phi<<<(unsigned)((c->npad + 127) / 128), 128, 0, c->stream>>>(
-        c->nbf, c->tc_KP, c->npad, ntiles, c->d_phi, reinterpret_cast<__nv_bfloat16 *>(c->d_tcA), c->d_tc_rowexp);
+        c->nbf, c->tc_KP, c->npad, ntiles, c->d_phi, reinterpret_cast<__half *>(c->d_tcA), c->d_tc_rowexp);
     DFTG_LAUNCH_CHECK();
     const size_t sm = density_tc_smem(c->tc_KP, c->tc_NP);
     (void)sm;
@@ -469,6 +500,7 @@ int launch_density_tc(dftg_ctx *c)
     const StepLaunch<SlicePArgs> sp = step_slice_P(c, c->d_P, nullptr);
     k_slice_P<<<sp.blocks, kSlicePThreads, 0, c->stream>>>(sp.args);
     DFTG_LAUNCH_CHECK();
+    DFTG_MARK(c, "density_slices");
     const StepLaunch<DensTcArgs> dn = step_density_tc(c);
     k_density_tc<<<dn.blocks, kTcThreads, dn.smem, c->stream>>>(dn.args);
     DFTG_LAUNCH_CHECK();

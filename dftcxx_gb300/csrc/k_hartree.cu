@@ -837,9 +837,9 @@ __device__ __forceinline__ void multipole_block(const MpArgs A, int vb)
     }
 }
 
-__global__ void __launch_bounds__(kMpThreads, 2) k_multipole(const MpArgs a) { multipole_block(a, (int)blockIdx.x); }
+__global__ void __launch_bounds__(kMpThreads, 3) k_multipole(const MpArgs a) { multipole_block(a, (int)blockIdx.x); }
 
-__global__ void __launch_bounds__(kMpThreads, 2) k_multipole_group(const MpArgs *__restrict__ args, GroupQueue q)
+__global__ void __launch_bounds__(kMpThreads, 3) k_multipole_group(const MpArgs *__restrict__ args, GroupQueue q)
 {
     __shared__ int s_item;
     gq_run(q, &s_item, [&](int m, int vb, int) {
@@ -1560,6 +1560,7 @@ int launch_hartree_cross(dftg_ctx *c)
     if (c->prec_mask & kPrecCross) {
         if (c->npairs > 0) {
             DFTG_TRY_L(launch_vcross_bins(c));
+            DFTG_MARK(c, "vcross_bins");
         }
         if (mp) {
             // own-cell potential, total potential and E_J in one pass

@@ -13,6 +13,10 @@ SCF driver's set-up and N iterations (one conditional-graph launch; with
 --scf-step one graph launch per iteration, for profilers).
 --workload synthetic: the seeded point-set workload (--points, --nbf; default
 2,000,000 x 512) through dftg_xc_build_device.
+--workload batch: --nmol jittered small molecules (H2 .. C6H6, STO-3G and
+6-31G, 50 x 194, lmax 8, mixed) built --builds times as one batch
+(--batch-mode persistent or graph; the first build runs eagerly, the second
+captures the graph, the rest replay it).
 """
 import argparse
 import ctypes
@@ -23,7 +27,9 @@ import numpy as np
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="benzene", choices=["benzene", "h2o", "decane", "synthetic"])
+    ap.add_argument("--workload", default="benzene", choices=["benzene", "h2o", "decane", "synthetic", "batch"])
+    ap.add_argument("--nmol", type=int, default=64)
+    ap.add_argument("--batch-mode", default="persistent", choices=["persistent", "graph"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--builds", type=int, default=2)
     ap.add_argument("--backward", type=int, default=0)
@@ -42,6 +48,8 @@ def main(argv=None):
     build()
     if args.workload == "synthetic":
         return _synthetic(args)
+    if args.workload == "batch":
+        return _batch(args)
     if args.workload == "benzene":
         Z, xyz = benzene()
         mol, grid = Molecule(Z, xyz, "p631"), (75, 11, 8)
@@ -109,6 +117,32 @@ def _synthetic(args):
                                           ctypes.c_void_p(sc.data_ptr())))
     torch.cuda.synchronize()
     print("synthetic builds %d  npts %d  nbf %d  Exc %.10f" % (args.builds, args.points, n, float(sc[0])))
+    return 0
+
+
+def _batch(args):
+    import torch
+    from .grid import Batch, MolecularGrid
+    from .molecule import Molecule, small_molecule
+    names = ["H2", "LiH", "H2O", "NH3", "CH4", "N2", "CO", "C2H6", "C6H6"]
+    rng = np.random.default_rng(20261204)
+    grids, Ps = [], []
+    for i in range(args.nmol):
+        Z, xyz = small_molecule(names[i % len(names)])
+        xyz = np.asarray(xyz, dtype=float) + rng.normal(0.0, 0.05, size=(len(Z), 3))
+        mol = Molecule(Z, xyz, "sto3g" if (i // len(names)) % 2 == 0 else "p631")
+        grids.append(MolecularGrid(mol, 50, 10, 8, precision="mixed"))
+        C = rng.normal(0, 0.2, size=(mol.nbf, max(1, mol.nelec // 2)))
+        Ps.append(torch.from_numpy(np.asfortranarray(C @ C.T).ravel(order="F").copy()).cuda())
+    outs = [torch.zeros(g.nbf * g.nbf, dtype=torch.float64, device="cuda") for g in grids]
+    b = Batch(grids, mode=args.batch_mode)
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    for _ in range(args.builds):
+        b.build(Ps, outs, None, None, stream=stream.cuda_stream)
+    b.status()
+    print("batch builds %d  molecules %d  persistent %s" % (args.builds, args.nmol, b.persistent_active()))
+    b.close()
     return 0
 
 

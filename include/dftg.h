@@ -313,8 +313,8 @@ int dftg_batch_selftest_wait(dftg_batch *b, double limit_ms);
 int dftg_batch_fock_build_device(dftg_batch *b, const double *const *P_devs, double *const *J_devs,
                                  double *const *XC_devs, double *const *scalars_devs, void *stream);
 /* Batch autotuner: scales every context's CTA counts by 1, 1/2, 1/4 and 1/8
- * together (more work items per CTA in the persistent form; concurrent
- * branches in the graph form), times reps replays of the batch on the
+ * together, and 1/16 and 1/32 in the persistent form (fewer, longer work items
+ * per molecule there; concurrent branches in the graph form), times reps replays of the batch on the
  * contexts' own last P and keeps the fastest scale; needs a complete build of
  * every context.  best_ms (per batch replay) may be NULL. */
 int dftg_batch_autotune(dftg_batch *b, int reps, double *best_ms);
