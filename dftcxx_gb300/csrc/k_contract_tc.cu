@@ -622,7 +622,10 @@ __global__ void k_ct_winv(size_t npad, const double *__restrict__ W, float *__re
 }
 
 // A slices in HBM, [nkb][slice][AR x 32 core layout]: thread per (kb, row, 8-point group)
-__global__ void k_ct_slice_A(int nbf, int AR, size_t npad, int nkb, int kb_per_chunk, const double *__restrict__ phi,
+// the three BF16 slices of the FP32 amplitudes (the ones the B operand and the
+// CUDA-core path use), in FP32 arithmetic: x = phi 2^(7 - e) and every remainder
+// are exact in FP32, so the slices are those of the exact values
+__global__ void k_ct_slice_A(int nbf, int AR, size_t npad, int nkb, int kb_per_chunk, const float *__restrict__ phi,
                              const int *__restrict__ rowexp, __nv_bfloat16 *__restrict__ A)
 {
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -636,16 +639,15 @@ __global__ void k_ct_slice_A(int nbf, int AR, size_t npad, int nkb, int kb_per_c
     const int e = row < nbf ? rowexp[(size_t)(kb / kb_per_chunk) * nbf + row] : 0;
     for (int k = 0; k < 8; ++k) {
         const size_t p = (size_t)kb * kCtKS + 8 * g + k;
-        // the FP32 amplitudes are the ones the CUDA-core path and the B operand use
-        const double x = row < nbf ? ldexp((double)(float)phi[(size_t)row * npad + p], 7 - e) : 0.0;
-        const double a1 = rint(x);
-        const double r1 = x - a1;
-        const __nv_bfloat16 h2 = __float2bfloat16_rn((float)r1);
-        const double r2 = r1 - (double)__bfloat162float(h2);
+        const float x = row < nbf ? phi[(size_t)row * npad + p] * pow2f(7 - e) : 0.f;   // |7 - e| <= 107
+        const float a1 = rintf(x);
+        const float r1 = x - a1;
+        const __nv_bfloat16 h2 = __float2bfloat16_rn(r1);
+        const float r2 = r1 - __bfloat162float(h2);
         const size_t base = (size_t)kb * kCtSlices * blk + o + k;
-        A[base] = __float2bfloat16_rn((float)a1);
+        A[base] = __float2bfloat16_rn(a1);
         A[base + blk] = h2;
-        A[base + 2 * blk] = __float2bfloat16_rn((float)r2);
+        A[base + 2 * blk] = __float2bfloat16_rn(r2);
     }
 }
 
@@ -784,7 +786,7 @@ int contract_tc_setup(dftg_ctx *c)
     DFTG_LAUNCH_CHECK();
     const size_t threads = (size_t)nkb * AR * 4;
     k_ct_slice_A<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-        c->nbf, AR, c->npad, nkb, kbpc, c->d_phi, c->d_ct_rowexp, reinterpret_cast<__nv_bfloat16 *>(c->d_ct_A));
+        c->nbf, AR, c->npad, nkb, kbpc, c->d_phi32, c->d_ct_rowexp, reinterpret_cast<__nv_bfloat16 *>(c->d_ct_A));
     DFTG_LAUNCH_CHECK();
     c->ct_NP = NP;
     c->ct_AR = AR;
@@ -865,7 +867,7 @@ int ct_setup_tables(dftg_ctx *c, int AR, int nkb, int kbpc, int nchunk, int *row
     DFTG_LAUNCH_CHECK();
     const size_t threads = (size_t)nkb * AR * 4;
     k_ct_slice_A<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-        c->nbf, AR, c->npad, nkb, kbpc, c->d_phi, rowexp, reinterpret_cast<__nv_bfloat16 *>(A));
+        c->nbf, AR, c->npad, nkb, kbpc, c->d_phi32, rowexp, reinterpret_cast<__nv_bfloat16 *>(A));
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
 }

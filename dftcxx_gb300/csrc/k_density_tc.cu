@@ -11,8 +11,8 @@
 //   P[mu, nu]  2^(8 - t_nu) = B_1 + B_2 + 2^-11 B_3     (per column t_nu)
 //
 // A_1 an integer (|A_1| <= 256), A_2 and A_3 multiples of 2^-11 (|.| <= 1/2):
-// every slice is exact in FP16, and together they hold the operand to 2^-31
-// of its row maximum.  Three accumulators per tile:
+// balanced base-2^11 digits of the operand rounded to 2^-30 of 2^e, every
+// slice exact in FP16 (formed with integer operations on the IEEE bits).  Three accumulators per tile:
 //   D_hi  = A_1 B_1                               integer products, exact in FP32
 //   D_lo  = A_1 B_2 + A_2 B_1 + A_2 B_2            about 2^-9 of D_hi
 //   D_lo2 = A_1 B_3 + A_3 B_1 + A_2 B_3 + A_3 B_2  weight 2^-11
@@ -345,20 +345,45 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_density_tc_group(const DensTc
 
 // ------------------------------------------------------------------ slicing
 
-// x with |x| < 1 -> the three FP16 slices of x 2^8 = A_1 + A_2 + 2^-11 A_3: A_1 =
-// rint(x 2^8), A_2 the remainder rounded to a multiple of 2^-11, A_3 the next
-// remainder times 2^11, rounded likewise (FP64 steps, all exact)
-__device__ __forceinline__ void slice3_f16(double x, uint16_t (&h)[kTcSlices])
+// The slicing works on the IEEE bits with integer operations (no FP64
+// arithmetic, slow on this GPU).  For x with |x| < 2^e, N = |x| 2^(30 - e)
+// rounded to an integer (half away from zero), with x's sign; |N| <= 2^30.
+__device__ __forceinline__ long long fixed30(unsigned long long bits, int e)
 {
-    x *= 256.0;
-    const double a1 = rint(x);
-    x -= a1;                                     // |x| <= 1/2
-    const double a2 = rint(x * 2048.0) * 0x1p-11;
-    x -= a2;                                     // |x| <= 2^-12
-    const double a3 = rint(x * 0x1p22) * 0x1p-11;
-    h[0] = __half_as_ushort(__float2half_rn((float)a1));
-    h[1] = __half_as_ushort(__float2half_rn((float)a2));
-    h[2] = __half_as_ushort(__float2half_rn((float)a3));
+    const int ef = (int)((bits >> 52) & 0x7ffu);
+    unsigned long long m = bits & 0xfffffffffffffull;
+    int E = -1022;                               // subnormal
+    if (ef != 0) {
+        m |= 1ull << 52;
+        E = ef - 1023;
+    }
+    // |x| = m 2^(E - 52), so N = m 2^-s with s = 22 + e - E >= 23 (E <= e - 1)
+    const int s = 22 + e - E;
+    const unsigned long long n = s > 64 ? 0ull : ((m >> (s - 1)) + 1ull) >> 1;
+    return (bits >> 63) ? -(long long)n : (long long)n;
+}
+
+// exponent e with |x| < 2^e for the largest |x| given by its magnitude bits
+// (frexp's exponent; 0 for zero)
+__device__ __forceinline__ int exp_above(unsigned long long magbits)
+{
+    if (magbits == 0ull) return 0;
+    const int ef = (int)(magbits >> 52);
+    return ef == 0 ? -1021 : ef - 1022;
+}
+
+// N (|N| <= 2^30) -> the three FP16 slices of N 2^-22 = A_1 + A_2 + 2^-11 A_3:
+// balanced digits N = d1 2^22 + d2 2^11 + d3 with |d2|, |d3| <= 2^10, so A_1 =
+// d1 (|d1| <= 256), A_2 = d2 2^-11, A_3 = d3 2^-11, each exact in FP16
+__device__ __forceinline__ void slice3_f16(long long N, uint16_t (&h)[kTcSlices])
+{
+    const long long d1 = (N + (1ll << 21)) >> 22;
+    const long long r1 = N - (d1 << 22);         // [-2^21, 2^21)
+    const long long d2 = (r1 + (1ll << 10)) >> 11;
+    const long long d3 = r1 - (d2 << 11);        // [-2^10, 2^10)
+    h[0] = __half_as_ushort(__float2half_rn((float)d1));
+    h[1] = __half_as_ushort(__float2half_rn((float)d2 * 0x1p-11f));
+    h[2] = __half_as_ushort(__float2half_rn((float)d3 * 0x1p-11f));
 }
 
 // Phi (FP64, [nbf][npad]) -> three FP16 slices per element in the tile layout
@@ -367,10 +392,10 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
 {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npad) return;
-    double mx = 0.0;
-    for (int mu = 0; mu < nbf; ++mu) mx = fmax(mx, fabs(phi[(size_t)mu * npad + p]));
-    int e = 0;
-    if (mx > 0.0) frexp(mx, &e);                 // mx < 2^e
+    const unsigned long long *__restrict__ pb = reinterpret_cast<const unsigned long long *>(phi);
+    unsigned long long mx = 0ull;
+    for (int mu = 0; mu < nbf; ++mu) mx = max(mx, pb[(size_t)mu * npad + p] & 0x7fffffffffffffffull);
+    const int e = exp_above(mx);                 // every |phi| < 2^e
     row_exp[p] = e;
     const int tile = (int)(p / kTcTile), r = (int)(p % kTcTile);
     const size_t slice16 = (size_t)ntiles * kTcTile * KP / 8;     // one slice in 16-byte units
@@ -382,7 +407,7 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
         for (int k = 0; k < 8; ++k) {
             const int mu = mu0 + k;
             uint16_t h[kTcSlices];
-            slice3_f16(mu < nbf ? ldexp(phi[(size_t)mu * npad + p], -e) : 0.0, h);
+            slice3_f16(mu < nbf ? fixed30(pb[(size_t)mu * npad + p], e) : 0ll, h);
 #pragma unroll
             for (int i = 0; i < kTcSlices; ++i) {
                 if (k & 1) w[i][k >> 1] |= (uint32_t)h[i] << 16;
@@ -405,21 +430,21 @@ __device__ __forceinline__ void slice_P_block(const SlicePArgs a, int vb)
     uint16_t *__restrict__ B = static_cast<uint16_t *>(a.B);
     const int nu = vb * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (nu >= NP) return;
-    double mx = 0.0;
+    const unsigned long long *__restrict__ Pb = reinterpret_cast<const unsigned long long *>(P);
+    unsigned long long mx = 0ull;
     if (nu < nbf)
         for (int mu = lane; mu < nbf; mu += 32) {
-            const double v = P[(size_t)nu * nbf + mu];
-            if (a.Pcopy) a.Pcopy[(size_t)nu * nbf + mu] = v;
-            mx = fmax(mx, fabs(v));
+            const unsigned long long v = Pb[(size_t)nu * nbf + mu];
+            if (a.Pcopy) reinterpret_cast<unsigned long long *>(a.Pcopy)[(size_t)nu * nbf + mu] = v;
+            mx = max(mx, v & 0x7fffffffffffffffull);
         }
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    int e = 0;
-    if (mx > 0.0) frexp(mx, &e);
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const int e = exp_above(mx);
     if (nu < nbf && lane == 0) a.col_exp[nu] = e;
     const size_t slice = (size_t)NP * KP;
     for (int mu = lane; mu < KP; mu += 32) {
         uint16_t h[kTcSlices];
-        slice3_f16((nu < nbf && mu < nbf) ? ldexp(P[(size_t)nu * nbf + mu], -e) : 0.0, h);
+        slice3_f16((nu < nbf && mu < nbf) ? fixed30(Pb[(size_t)nu * nbf + mu], e) : 0ll, h);
         const size_t o = core_off(nu, mu, KP / 8) / 2;
         for (int i = 0; i < kTcSlices; ++i) B[(size_t)i * slice + o] = h[i];
     }
