@@ -80,7 +80,7 @@ static void free_ctx(dftg_ctx *c)
                     c->d_XC, c->d_part, c->d_red, c->d_scal, c->d_Y, c->d_Yw, c->d_pre, c->d_pre32, c->d_rec,
                     c->d_rec32, c->d_rholm, c->d_U, c->d_U32, c->d_Y32, c->d_Ywt32, c->d_fold, c->d_Gt,
                     c->d_Gb, c->d_Kt, c->d_sx, c->d_splf, c->d_spl, c->d_splm, c->d_tiles,
-                    c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_rw32, c->d_flag,
+                    c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_rw32, c->d_wsplit, c->d_flag,
                     c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32, c->d_U32T,
                     c->d_bw_pt, c->d_bw_lm, c->d_bw_fpart, c->d_bw_out, c->d_bw_counter, c->d_bw_pairp,
                     c->d_bw_binfirst, c->d_bw_cpart, c->d_bw_geo, c->d_bw_geo64, c->d_bw_prim32,
@@ -188,6 +188,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     DFTG_TRY(dalloc(&c->d_wb, np));
     DFTG_TRY(dalloc(&c->d_rho, np));
     DFTG_CUDA(cudaMalloc(&c->d_rw32, sizeof(float) * 2 * np));
+    DFTG_CUDA(cudaMalloc(&c->d_wsplit, sizeof(float) * 4 * np));
     DFTG_TRY(dalloc(&c->d_V, np));
     DFTG_TRY(dalloc(&c->d_Vown, np));
     DFTG_TRY(dalloc(&c->d_cxc, np));
@@ -259,6 +260,7 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
 
     tr.mark(c->stream, "copies");
     DFTG_TRY(launch_grid(c));
+    DFTG_TRY(launch_weight_planes(c));
     tr.mark(c->stream, "grid and Becke weights");
     DFTG_TRY(launch_amplitudes(c));
     tr.mark(c->stream, "amplitudes");
@@ -533,6 +535,7 @@ static int build_points_ctx(dftg_ctx *c, const dftg_points *pts, const dftg_mole
     DFTG_TRY(dalloc(&c->d_wb, np));
     DFTG_TRY(dalloc(&c->d_rho, np));
     DFTG_CUDA(cudaMalloc(&c->d_rw32, sizeof(float) * 2 * np));
+    DFTG_CUDA(cudaMalloc(&c->d_wsplit, sizeof(float) * 4 * np));
     DFTG_TRY(dalloc(&c->d_V, np));
     DFTG_TRY(dalloc(&c->d_cxc, np));
     DFTG_TRY(dalloc(&c->d_cj, np));
@@ -575,6 +578,7 @@ static int build_points_ctx(dftg_ctx *c, const dftg_points *pts, const dftg_mole
     DFTG_CUDA(cudaMemcpy(c->d_z, Zc.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
     DFTG_CUDA(cudaMemcpy(c->d_w, W.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
     DFTG_CUDA(cudaMemcpy(c->d_wb, WB.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
+    DFTG_TRY(launch_weight_planes(c));
     DFTG_CUDA(cudaMemset(c->d_cj, 0, sizeof(double) * np));
     DFTG_CUDA(cudaMemset(c->d_cj32, 0, sizeof(float) * np));
     DFTG_CUDA(cudaMemcpy(c->d_bf_lmn, c->bf_lmn.data(), sizeof(int) * 3 * c->nbf, cudaMemcpyHostToDevice));

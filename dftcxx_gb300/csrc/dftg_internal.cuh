@@ -80,6 +80,25 @@ __host__ __device__ __forceinline__ dfl df_from(double x)
 }
 __device__ __forceinline__ double df_to(dfl a) { return (double)a.h + (double)a.l; }
 
+// x as a double-float from its IEEE bits with integer operations (no FP64
+// arithmetic): h = x rounded to 24 bits (half away from zero), l = the
+// remainder rounded to FP32.  |x| < 2^-100 gives 0; |x| < 2^127.
+__device__ __forceinline__ dfl df_from_bits(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int ef = (int)((b >> 52) & 0x7ffu);
+    if (ef < 1023 - 100) return {0.f, 0.f};
+    const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+    const long long m = (long long)((b & 0xfffffffffffffull) | (1ull << 52));   // x = m 2^(E - 52)
+    const long long mh = (m + (1ll << 28)) >> 29;                               // [2^23, 2^24]
+    const int rem = (int)(m - (mh << 29));                                      // [-2^28, 2^28]
+    const int E = ef - 1023;
+    // h = mh 2^(E - 23); mh = 2^24 is 2^(E + 1)
+    const float h = __uint_as_float(sgn | ((unsigned)(E + 127 + (int)(mh >> 24)) << 23) | ((unsigned)mh & 0x7fffffu));
+    const float l = (float)rem * 0x1p-52f * __int_as_float((127 + E) << 23);
+    return {h, sgn ? -l : l};
+}
+
 // Deterministic sum of v over the block (blockDim.x a multiple of 32, at most
 // 1024): butterfly shuffles inside each warp, then warp totals in warp order.
 // The result is valid in thread 0.  sh: 32 doubles of shared memory.
@@ -265,6 +284,7 @@ struct dftg_ctx {
     size_t red_elems = 0;
     double *d_scal = nullptr;     // scalars, see kScal* below
     int *d_counters = nullptr;    // [kNumCounters] last-block counters (zero between launches)
+    float *d_wsplit = nullptr;    // [4][npad] w and w_becke as FP32 hi / lo planes (mixed point kernel)
     double *h_scal = nullptr;     // pinned host mirror of d_scal
 
     // device: Hartree
@@ -458,6 +478,7 @@ struct LdaArgs {               // LDA point kernel
     int *counter;
     const double *wb;
     float *rw32;
+    const float *w2, *wb2;     // w and w_becke as FP32 hi / lo planes [2][npad] (mixed kernel)
 };
 struct MpArgs {                // multipole chain of one atom cell per (cell, l group)
     int natoms, cell0, N, nang, lmax, ngroup, want64;
@@ -550,6 +571,7 @@ int density_tt_setup(dftg_ctx *c);
 int launch_density_tt(dftg_ctx *c);
 int launch_atom_sums(dftg_ctx *c, int mode);
 int launch_xc_points(dftg_ctx *c, bool apply_scale, bool with_n = false);
+int launch_weight_planes(dftg_ctx *c);
 // k_hartree.cu
 int hartree_setup(dftg_ctx *c);
 int cross_pairs_setup(dftg_ctx *c);

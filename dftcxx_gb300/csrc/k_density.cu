@@ -226,11 +226,17 @@ __device__ __forceinline__ void atom_sums_block(const SumsArgs A, int b, int nb)
     s = block_sum(s, sh);
     if (threadIdx.x == 0) part[b] = s;
     if (!last_block_of(A.counter, nb, &s_last)) return;
-    // last block: per-atom sums in chunk order, total, correction factor
-    for (int t = threadIdx.x; t < natoms; t += kRedBlock) {
-        double q = 0.0;
-        for (int c = 0; c < chunks_per_atom; ++c) q += __ldcg(part + (size_t)t * chunks_per_atom + c);
-        sq[t] = q;
+    // last block: per-atom sums (a warp per atom: the lanes take every 32nd
+    // chunk, then a fixed shuffle tree), total, correction factor
+    {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int t = warp; t < natoms; t += kRedBlock / 32) {
+            double q = 0.0;
+            for (int c = lane; c < chunks_per_atom; c += 32) q += __ldcg(part + (size_t)t * chunks_per_atom + c);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+            if (lane == 0) sq[t] = q;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -296,51 +302,57 @@ __device__ __forceinline__ void lda_block(const LdaArgs A, int vb, int nvb)
     const double *__restrict__ wb = A.wb;
     float *__restrict__ rw32 = A.rw32;
     __shared__ double sh[32];
-    __shared__ float shf[2][32];
+    __shared__ float shf[2][32], shn[2][32];
     __shared__ int s_last;
     const size_t p = (size_t)vb * kRedBlock + threadIdx.x;
     double ew = 0.0;
     if (MIXED) {
-        // double-float point kernel and block sum; FP64 only for the density
-        // correction, the weight split and the block partial
-        dfl ewd{0.f, 0.f};
-        double wr = 0.0;
+        // double-float point kernel and block sums; FP64 only for the density
+        // correction (one product per point) and the block partials: rho is
+        // split into FP32 hi / lo with integer operations, w and w_becke come as
+        // FP32 hi / lo planes made at set-up
+        dfl ewd{0.f, 0.f}, wrd{0.f, 0.f};
         if (p < npad) {
             double r = rho[p];
             if (apply_scale) {
                 r *= __ldcg(scal + kScalScale);
                 rho[p] = r;
             }
+            const dfl rd = df_from_bits(r);
             dfl e;
             float v;
-            lda_point_df(df_from(r), e, v);
-            const double wp = w[p];
-            const dfl wd = df_from(wp);
+            lda_point_df(rd, e, v);
+            const dfl wd{A.w2[p], A.w2[npad + p]};
             ewd = df_mul(wd, e);
-            const float c32 = (wd.h + wd.l) * v;
-            cxc32[p] = c32;
-            if (want64) cxc[p] = wp * (double)v;
-            wr = wp * r;
+            cxc32[p] = (wd.h + wd.l) * v;
+            if (want64) cxc[p] = w[p] * (double)v;
+            wrd = df_mul(wd, rd);
             if (rw32) {
-                const dfl x = df_from(r * wb[p]);
+                const dfl x = df_mul(rd, dfl{A.wb2[p], A.wb2[npad + p]});
                 rw32[p] = x.h;
                 rw32[npad + p] = x.l;
             }
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
+        for (int o = 16; o > 0; o >>= 1) {
             ewd = df_add(ewd, dfl{__shfl_xor_sync(0xffffffffu, ewd.h, o), __shfl_xor_sync(0xffffffffu, ewd.l, o)});
+            wrd = df_add(wrd, dfl{__shfl_xor_sync(0xffffffffu, wrd.h, o), __shfl_xor_sync(0xffffffffu, wrd.l, o)});
+        }
         if ((threadIdx.x & 31) == 0) {
             shf[0][threadIdx.x >> 5] = ewd.h;
             shf[1][threadIdx.x >> 5] = ewd.l;
+            shn[0][threadIdx.x >> 5] = wrd.h;
+            shn[1][threadIdx.x >> 5] = wrd.l;
         }
-        const double wrs = want_n ? block_sum(wr, sh) : 0.0;   // block-uniform; synchronises the posts above
-        if (!want_n) __syncthreads();
+        __syncthreads();
         if (threadIdx.x == 0) {
-            dfl t{0.f, 0.f};
-            for (int i = 0; i < kRedBlock / 32; ++i) t = df_add(t, dfl{shf[0][i], shf[1][i]});
+            dfl t{0.f, 0.f}, tn{0.f, 0.f};
+            for (int i = 0; i < kRedBlock / 32; ++i) {
+                t = df_add(t, dfl{shf[0][i], shf[1][i]});
+                tn = df_add(tn, dfl{shn[0][i], shn[1][i]});
+            }
             part[vb] = df_to(t);
-            if (want_n) part[nvb + vb] = wrs;
+            if (want_n) part[nvb + vb] = df_to(tn);
         }
         if (!last_block_of(counter, nvb, &s_last)) return;
         double t = 0.0, tn = 0.0;
@@ -490,6 +502,26 @@ int launch_atom_sums(dftg_ctx *c, int mode)
     return DFTG_OK;
 }
 
+// w and w_becke as FP32 hi / lo planes [2][npad] each (once per grid)
+__global__ void k_weight_planes(size_t npad, const double *__restrict__ w, const double *__restrict__ wb,
+                                float *__restrict__ out)
+{
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npad) return;
+    const dfl a = df_from(w[p]), b = df_from(wb[p]);
+    out[p] = a.h;
+    out[npad + p] = a.l;
+    out[2 * npad + p] = b.h;
+    out[3 * npad + p] = b.l;
+}
+
+int launch_weight_planes(dftg_ctx *c)
+{
+    k_weight_planes<<<(unsigned)((c->npad + 255) / 256), 256, 0, c->stream>>>(c->npad, c->d_w, c->d_wb, c->d_wsplit);
+    DFTG_LAUNCH_CHECK();
+    return DFTG_OK;
+}
+
 StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n)
 {
     // with_n: the build's N from the corrected rho (no per-atom sums ran), and
@@ -500,7 +532,7 @@ StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n)
     s.args = LdaArgs{c->npad, c->d_rho, c->d_w, c->d_scal, apply_scale ? 1 : 0,
                      mixed ? ((c->prec_mask & kPrecContract) && c->ct_ready ? 0 : 1) : 1, mixed && with_n ? 1 : 0,
                      c->d_cxc, c->d_cxc32, c->d_red, c->d_counters + kCntLda, mixed ? c->d_wb : nullptr,
-                     mixed ? rw32 : nullptr};
+                     mixed ? rw32 : nullptr, c->d_wsplit, c->d_wsplit + 2 * c->npad};
     s.blocks = (int)((c->npad + kRedBlock - 1) / kRedBlock);
     return s;
 }
