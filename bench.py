@@ -56,7 +56,7 @@ WORKLOAD = {"workload": "benzene/6-31G grid Fock build", "molecule": "C6H6 D6h",
             "radial_points": 75, "lebedev_points": 302, "lmax": 8, "grid_points": 271800,
             "density_matrix": "the reference program's SCF density (30 x 110 grid, |dE| <= 1e-9)",
             "l2": "GPU arm: flushed (256 MB write) before every step"}
-DTYPE = "bf16 slices (3 contraction / 4 density) + fp32 accumulate, fp64 reductions"
+DTYPE = "fp16 fixed-point slices (3, density) and bf16 slices (3, contraction) + fp32 accumulate, fp64 reductions"
 REF_FIXTURE = os.path.join(ROOT, "tests", "golden", "ref_benzene_p631_75x302.npz")
 
 
