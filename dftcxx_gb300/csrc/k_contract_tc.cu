@@ -25,17 +25,17 @@
 // in the shared-memory operand layout; B is formed every build from A and c.
 //
 // CTA (persistent over chunks, 832 threads):
-//   warps 0-7  producers in two groups of four: group g builds the B slices of
-//              the stages in ring slots of parity g (the ring depth is even, so
-//              a group sees each of its slots' phases in order), every warp of
-//              the group its rows (w, w + 4, ... in groups of eight), from the A
-//              slices and c values of the stage (shared memory), then a proxy
-//              fence and an mbarrier arrive (the full barrier counts four);
-//   warp 8     TMEM owner and MMA issuer (one thread);
-//   warps 9-24 epilogue: TMEM -> double-float partial (TMEM lane quarter =
-//              warp % 4, the four warps of a quarter take every fourth
-//              16-column block);
-//   warp 25    loader: bulk copies of the A slices and c values of each stage.
+//   warps 0-11  producers in two groups of six: group g builds the B slices of
+//               the stages in ring slots of parity g (the ring depth is even, so
+//               a group sees each of its slots' phases in order), every warp of
+//               the group its rows (w, w + 6, ... in groups of eight), from the A
+//               slices and c values of the stage (shared memory), then a proxy
+//               fence and an mbarrier arrive (the full barrier counts six);
+//   warp 12     TMEM owner and MMA issuer (one thread);
+//   warps 13-24 epilogue: TMEM -> double-float partial (TMEM lane quarter =
+//               warp % 4, the three warps of a quarter take every third
+//               16-column block);
+//   warp 25     loader: bulk copies of the A slices and c values of each stage.
 // Every mbarrier wait is bounded: on expiry the CTA records an error code, lets
 // its copies and MMAs complete, frees TMEM and exits.
 #include <cuda_bf16.h>
@@ -49,10 +49,12 @@ constexpr int kCtKS = 32;                  // points per stage
 constexpr int kCtKcores = kCtKS / 8;       // core matrices along K per stage
 constexpr int kCtM = 128;
 constexpr int kCtMaxNbf = 128;             // 2 nbf <= 256 columns per accumulator
-constexpr int kCtProducers = 8;           // producer warps 0..7
+constexpr int kCtProducers = 12;          // producer warps 0..11, two groups of six
+constexpr int kCtGroupWarps = kCtProducers / 2;
+constexpr int kCtRowSteps = (kCtMaxNbf + 8 * kCtGroupWarps - 1) / (8 * kCtGroupWarps);   // rows per lane
 constexpr int kCtMmaWarp = kCtProducers;   // TMEM owner and MMA issuer
-constexpr int kCtEpi0 = kCtMmaWarp + 1;    // epilogue warps kCtEpi0 .. kCtEpi0 + 7
-constexpr int kCtEpiWarps = 16;           // four per TMEM lane quarter
+constexpr int kCtEpi0 = kCtMmaWarp + 1;    // epilogue warps kCtEpi0 .. kCtEpi0 + kCtEpiWarps - 1
+constexpr int kCtEpiWarps = 12;           // three per TMEM lane quarter
 constexpr int kCtThreads = (kCtEpi0 + kCtEpiWarps + 1) * 32;
 constexpr int kCtLoaderWarp = kCtEpi0 + kCtEpiWarps;
 constexpr int kCtMaxStages = 8;
@@ -231,7 +233,7 @@ __device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb
     if (threadIdx.x == 0) {
         for (int s = 0; s < nst; ++s) {
             mbar_init(&sh->a_full[s], 1);
-            mbar_init(&sh->full[s], kCtProducers / 2);   // the four warps of the slot's group
+            mbar_init(&sh->full[s], kCtGroupWarps);      // the warps of the slot's group
             mbar_init(&sh->empty[s], 1);
         }
         mbar_init(&sh->tmem_full, 1);
@@ -246,13 +248,13 @@ __device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb
 
     if (warp < kCtProducers) {
         // ------------------------------------------------------------ producers
-        // two groups of four warps own the even and the odd ring slots (nst is
+        // two groups of six warps own the even and the odd ring slots (nst is
         // even, so each group sees its slots' phases in order); in a group, warp
-        // w takes row groups w, w + 4, ...; lane = (8-point group g) x (row within
+        // w takes row groups w, w + 6, ...; lane = (8-point group g) x (row within
         // the group of 8).  The eight lanes of one 16-byte shared-memory phase
         // share g and cover the eight rows of one core matrix, 128 contiguous
         // bytes, so the slice loads and stores are free of bank conflicts.
-        const int grp = warp >> 2, wg = warp & 3;
+        const int grp = warp / kCtGroupWarps, wg = warp % kCtGroupWarps;
         const int g = lane >> 3, mrow = lane & 7;
         int it = 0;
         bool ok = true;
@@ -261,12 +263,12 @@ __device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb
             const int2 ce = cexp[ch];
             const float sx = pow2f(-ce.x), sj = pow2f(-ce.y);
             // B row scales of this lane's rows for the chunk, in registers
-            float rfr[kCtMaxNbf / 32];
+            float rfr[kCtRowSteps];
             {
                 const int *ea = rowexp + (size_t)ch * nbf, *es = swexp + (size_t)ch * nbf;
 #pragma unroll
-                for (int j = 0; j < kCtMaxNbf / 32; ++j) {
-                    const int mu = 32 * j + 8 * wg + mrow;
+                for (int j = 0; j < kCtRowSteps; ++j) {
+                    const int mu = 8 * kCtGroupWarps * j + 8 * wg + mrow;
                     rfr[j] = mu < nbf ? pow2f(max(-126, min(127, ea[mu] - es[mu]))) : 0.f;
                 }
             }
@@ -293,11 +295,11 @@ __device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb
                 // the lane's rows one at a time: its slice loads first, then the
                 // arithmetic (predicated, no early exit)
 #pragma unroll
-                for (int j0 = 0; j0 < kCtMaxNbf / 32; j0 += 1) {
+                for (int j0 = 0; j0 < kCtRowSteps; j0 += 1) {
                     uint4 q0[1], q1[1], q2[1];
 #pragma unroll
                     for (int jj = 0; jj < 1; ++jj) {
-                        const int mu = 32 * (j0 + jj) + 8 * wg + mrow;
+                        const int mu = 8 * kCtGroupWarps * (j0 + jj) + 8 * wg + mrow;
                         if (mu < nbf) {
                             const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
                             q0[jj] = *reinterpret_cast<const uint4 *>(sA + oa);
@@ -307,7 +309,7 @@ __device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb
                     }
 #pragma unroll
                     for (int jj = 0; jj < 1; ++jj) {
-                        const int mu = 32 * (j0 + jj) + 8 * wg + mrow;
+                        const int mu = 8 * kCtGroupWarps * (j0 + jj) + 8 * wg + mrow;
                         if (mu < nbf) {
                             const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
                             // B row scale: phi 2^(7 - e_mu) -> phi 2^(7 - s_mu)
