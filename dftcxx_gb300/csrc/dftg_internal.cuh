@@ -285,6 +285,8 @@ struct dftg_ctx {
     double *d_scal = nullptr;     // scalars, see kScal* below
     int *d_counters = nullptr;    // [kNumCounters] last-block counters (zero between launches)
     float *d_wsplit = nullptr;    // [4][npad] w and w_becke as FP32 hi / lo planes (mixed point kernel)
+    int2 *d_lebpair = nullptr;    // [nang / 2] Lebedev directions paired with their antipodes
+    int nlebpair = 0;
     double *h_scal = nullptr;     // pinned host mirror of d_scal
 
     // device: Hartree
@@ -490,6 +492,8 @@ struct MpArgs {                // multipole chain of one atom cell per (cell, l 
     float *U32, *U32T;
     double *spl;
     float *splm;
+    const int2 *pairs;         // [npair] Lebedev directions (j, antipode of j), j < antipode
+    int npair;
 };
 struct VcbArgs {               // cross-atom pair contributions, one block per bin task
     int nrad, lmax;
@@ -510,6 +514,8 @@ struct GoArgs {                // own-cell potential + pair sums per point, cj, 
     float *cj32;
     double *part, *scal;
     int *counter;
+    const int2 *pairs;         // [npair] Lebedev directions (j, antipode of j)
+    int npair;
 };
 struct CexpArgs {              // per-chunk exponent bounds of the point coefficients
     int nkb, kbpc;

@@ -49,7 +49,7 @@ struct BatchPlan {
 bool batch_group_eligible(const dftg_ctx *c)
 {
     return !c->points_only && c->cell0 == 0 && c->ncell == c->natoms && (c->prec_mask & kPrecAll) == kPrecAll &&
-           c->tc_ready && c->ct_ready && c->nrad <= 256 && c->d_rw32 != nullptr;
+           c->tc_ready && c->ct_ready && c->nrad <= 256 && c->nlebpair > 0 && c->d_rw32 != nullptr;
 }
 
 void batch_plan_free(BatchPlan *bp)

@@ -239,7 +239,30 @@ __global__ void k_inv_radius(size_t npts, int nrad, int nang, const double *__re
 struct HartreeTables {
     std::vector<double> Y, Yw, pre, fold, Gt, Gb, Kt, rec, sx, f;
     std::vector<float> Y32, Ywt32, pre32, rec32, m32;
+    std::vector<int> pairs;        // (j, antipode of j) for j < antipode; empty if a direction has none
 };
+
+// Lebedev rules are invariant under inversion: every direction j has an antipode
+// -j with the same weight.  Pairs (j, antipode) with j < antipode, or nothing
+// when some direction has no antipode.
+static std::vector<int> antipode_pairs(int nang, const std::vector<double> &leb)
+{
+    std::vector<int> pairs;
+    for (int j = 0; j < nang; ++j) {
+        int a = -1;
+        for (int k = 0; k < nang && a < 0; ++k)
+            if (std::fabs(leb[4 * k] + leb[4 * j]) + std::fabs(leb[4 * k + 1] + leb[4 * j + 1]) +
+                        std::fabs(leb[4 * k + 2] + leb[4 * j + 2]) < 1e-12 &&
+                std::fabs(leb[4 * k + 3] - leb[4 * j + 3]) <= 1e-15 * std::fabs(leb[4 * j + 3]))
+                a = k;
+        if (a < 0 || a == j) return {};
+        if (j < a) {
+            pairs.push_back(j);
+            pairs.push_back(a);
+        }
+    }
+    return (int)pairs.size() == nang ? pairs : std::vector<int>{};
+}
 
 static std::shared_ptr<const HartreeTables> build_hartree_tables(int N, int nang, int lmax, const std::vector<double> &r_n,
                                                                  const std::vector<double> &leb)
@@ -349,6 +372,7 @@ static std::shared_ptr<const HartreeTables> build_hartree_tables(int N, int nang
     T->sx = std::move(sx); T->f = std::move(f);
     T->Y32 = std::move(Y32); T->Ywt32 = std::move(Ywt32); T->pre32 = std::move(pre32); T->rec32 = std::move(rec32);
     T->m32 = std::move(m32);
+    T->pairs = antipode_pairs(nang, leb);
     return T;
 }
 
@@ -397,6 +421,11 @@ int hartree_setup(dftg_ctx *c)
     DFTG_TRY_L(up(c->d_sx, T->sx.data(), sizeof(double) * N));
     DFTG_TRY_L(up(c->d_splf, T->f.data(), sizeof(double) * T->f.size()));
     DFTG_TRY_L(up(c->d_maps32, T->m32.data(), sizeof(float) * T->m32.size()));
+    c->nlebpair = (int)T->pairs.size() / 2;
+    if (c->nlebpair > 0) {
+        DFTG_CUDA(cudaMalloc(&c->d_lebpair, sizeof(int2) * c->nlebpair));
+        DFTG_TRY_L(up(c->d_lebpair, T->pairs.data(), sizeof(int) * T->pairs.size()));
+    }
     return DFTG_OK;
 }
 
@@ -630,22 +659,27 @@ size_t multipole_smem(int nrad, int nang)
 }
 
 // acc = sum_k M[k][i] x[k] over k < N (M given as hi / lo planes with row
-// stride N), four independent double-float accumulators
+// stride N): four independent compensated accumulators (exact leading
+// products by TwoProd, the cross terms and the roundings gathered in the error
+// part), normalised once at the end
 __device__ __forceinline__ dfl mp_matvec(const float *__restrict__ Mh, const float *__restrict__ Ml, int N, int i,
                                          const dfl *__restrict__ x, bool reverse_x)
 {
-    dfl a0{0.f, 0.f}, a1{0.f, 0.f}, a2{0.f, 0.f}, a3{0.f, 0.f};
+    float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f, s2 = 0.f, e2 = 0.f, s3 = 0.f, e3 = 0.f;
     int k = 0;
     for (; k + 3 < N; k += 4) {
         const dfl x0 = reverse_x ? x[N - 1 - k] : x[k], x1 = reverse_x ? x[N - 2 - k] : x[k + 1];
         const dfl x2 = reverse_x ? x[N - 3 - k] : x[k + 2], x3 = reverse_x ? x[N - 4 - k] : x[k + 3];
-        a0 = df_fma(a0, dfl{Mh[(size_t)k * N + i], Ml[(size_t)k * N + i]}, x0);
-        a1 = df_fma(a1, dfl{Mh[(size_t)(k + 1) * N + i], Ml[(size_t)(k + 1) * N + i]}, x1);
-        a2 = df_fma(a2, dfl{Mh[(size_t)(k + 2) * N + i], Ml[(size_t)(k + 2) * N + i]}, x2);
-        a3 = df_fma(a3, dfl{Mh[(size_t)(k + 3) * N + i], Ml[(size_t)(k + 3) * N + i]}, x3);
+        df_mac(s0, e0, Mh[(size_t)k * N + i], Ml[(size_t)k * N + i], x0.h, x0.l);
+        df_mac(s1, e1, Mh[(size_t)(k + 1) * N + i], Ml[(size_t)(k + 1) * N + i], x1.h, x1.l);
+        df_mac(s2, e2, Mh[(size_t)(k + 2) * N + i], Ml[(size_t)(k + 2) * N + i], x2.h, x2.l);
+        df_mac(s3, e3, Mh[(size_t)(k + 3) * N + i], Ml[(size_t)(k + 3) * N + i], x3.h, x3.l);
     }
-    for (; k < N; ++k) a0 = df_fma(a0, dfl{Mh[(size_t)k * N + i], Ml[(size_t)k * N + i]}, reverse_x ? x[N - 1 - k] : x[k]);
-    return df_add(df_add(a0, a1), df_add(a2, a3));
+    for (; k < N; ++k) {
+        const dfl xk = reverse_x ? x[N - 1 - k] : x[k];
+        df_mac(s0, e0, Mh[(size_t)k * N + i], Ml[(size_t)k * N + i], xk.h, xk.l);
+    }
+    return df_add(df_add(df_norm(s0, e0), df_norm(s1, e1)), df_add(df_norm(s2, e2), df_norm(s3, e3)));
 }
 
 // n floats global -> shared with eight loads in flight per thread
@@ -691,8 +725,11 @@ __device__ __forceinline__ void multipole_block(const MpArgs A, int vb)
     const int lm0 = g * kMpLG, nl = min(kMpLG, nlm - lm0);
     const size_t base = (size_t)al * N * nang;
     const size_t uhalf = (size_t)natoms * nlm * N;
-    for (int e = tid; e < nl * nang; e += kMpThreads) {
-        const int r = e / nang, j = e % nang;
+    // w_leb Y_lm at the first direction of every antipodal pair: [row][pair]
+    const int npair = A.npair;
+    const int2 *__restrict__ pairs = A.pairs;
+    for (int e = tid; e < nl * npair; e += kMpThreads) {
+        const int r = e / npair, j = __ldg(&pairs[e % npair].x);
         sY[e] = dfl{Ywt32[(size_t)j * nlm + lm0 + r], Ywt32[(size_t)nang * nlm + (size_t)j * nlm + lm0 + r]};
     }
     // q_a for the boundary row of lm = 0 (four loads in flight per thread)
@@ -718,32 +755,43 @@ __device__ __forceinline__ void multipole_block(const MpArgs A, int vb)
     for (int i0 = 0; i0 < N; i0 += kMpSC) {
         const int ns = min(kMpSC, N - i0);
         __syncthreads();                                          // the previous pass is done with sRW
-        // a thread per Lebedev direction, eight shells' loads in flight
-        for (int j = tid; j < nang; j += kMpThreads)
+        // a thread per antipodal pair (j, a), eight shells' loads in flight: the
+        // even and odd combinations rho w(j) +- rho w(a) (Y_lm(a) = (-1)^l Y_lm(j))
+        for (int k = tid; k < npair; k += kMpThreads) {
+            const int2 ja = __ldg(&pairs[k]);
             for (int ii0 = 0; ii0 < ns; ii0 += 8) {
-                dfl v[8];
+                dfl v[8], w[8];
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
-                    const size_t p = base + (size_t)(i0 + min(ii0 + u, ns - 1)) * nang + j;
-                    v[u] = rw32 ? dfl{rw32[p], rw32[npad + p]} : df_from(rho[p] * wb[p]);
+                    const size_t p = base + (size_t)(i0 + min(ii0 + u, ns - 1)) * nang;
+                    const size_t pj = p + ja.x, pa = p + ja.y;
+                    v[u] = rw32 ? dfl{rw32[pj], rw32[npad + pj]} : df_from(rho[pj] * wb[pj]);
+                    w[u] = rw32 ? dfl{rw32[pa], rw32[npad + pa]} : df_from(rho[pa] * wb[pa]);
                 }
 #pragma unroll
                 for (int u = 0; u < 8; ++u)
-                    if (ii0 + u < ns) sRW[(size_t)(ii0 + u) * row + j] = v[u];
+                    if (ii0 + u < ns) {
+                        sRW[(size_t)(ii0 + u) * row + k] = df_add(v[u], w[u]);
+                        sRW[(size_t)(ii0 + u) * row + npair + k] = df_sub(v[u], w[u]);
+                    }
             }
+        }
         __syncthreads();
-        // two threads per rho_lm(i), each over half of the Lebedev points, met
-        // by a shuffle; every lane of a warp takes part (items past the end run
-        // on empty ranges)
+        // two threads per rho_lm(i), each over half of the pairs, met by a
+        // shuffle; every lane of a warp takes part (items past the end run on
+        // empty ranges).  Row lm of degree l takes the even combinations for
+        // even l, the odd ones for odd l.
         const int nitem = 2 * nl * ns;
-        const int half_ang = (nang + 1) / 2;
+        const int half_pair = (npair + 1) / 2;
         for (int o0 = (tid & ~31); o0 < nitem; o0 += kMpThreads) {
             const int o = o0 + (tid & 31);
             const bool valid = o < nitem;
             const int out = o >> 1, hf = o & 1;
             const int r = valid ? out % nl : 0, ii = valid ? out / nl : 0;
-            const int j0 = hf ? half_ang : 0, j1 = valid ? (hf ? nang : half_ang) : 0;
-            const dfl *x = sRW + (size_t)ii * row, *y = sY + (size_t)r * nang;
+            const int j0 = hf ? half_pair : 0, j1 = valid ? (hf ? npair : half_pair) : 0;
+            int l = 0;
+            while ((l + 1) * (l + 1) <= lm0 + r) ++l;
+            const dfl *x = sRW + (size_t)ii * row + ((l & 1) ? npair : 0), *y = sY + (size_t)r * npair;
             float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f, s2 = 0.f, e2 = 0.f, s3 = 0.f, e3 = 0.f;
             int j = j0;
             for (; j + 3 < j1; j += 4) {
@@ -1097,12 +1145,15 @@ __global__ void k_vcross_gather(size_t npts, size_t npad, int natoms, int cell0,
 // V_own = (1 / r) sum_lm U_lm(r_i) Y_lm(j) in double-float with exact products,
 // plus the pair contributions in atom order summed with TwoSum; writes V and
 // cj = w V / 2, and sums E_J = sum_p cj rho_raw (block partials, the last block
-// adds them in order).  A block takes one cell, a slab of kGoSlab Lebedev
-// directions and kGoShells radial shells: the slab's Y_lm (hi, lo) is staged in
-// shared memory once, a warp takes a shell at a time with a lane per direction,
-// and the shell's U_lm row is one broadcast load per (l, m).
+// adds them in order).  A block takes one cell, a slab of kGoSlab antipodal
+// pairs of Lebedev directions and kGoShells radial shells: the Y_lm (hi, lo) of
+// the slab's first directions are staged in shared memory once, a warp takes a
+// shell at a time with a lane per pair, and the shell's U_lm row is one
+// broadcast load per (l, m).  Since Y_lm(-r) = (-1)^l Y_lm(r), a lane sums the
+// even-l and the odd-l terms once and has V_own at both points of its pair
+// (even + odd, even - odd): half the products of a lane per direction.
 constexpr int kGoSlab = 32;
-constexpr int kGoShells = 16;
+constexpr int kGoShells = 8;
 constexpr int kGoThreads = 256;
 
 __device__ __forceinline__ void gather_own_block(const GoArgs A, int b, int nblk)
@@ -1119,19 +1170,24 @@ __device__ __forceinline__ void gather_own_block(const GoArgs A, int b, int nblk
     double *__restrict__ part = A.part;
     double *scal = A.scal;
     int *counter = A.counter;
+    const int npair = A.npair;
+    const int2 *__restrict__ pairs = A.pairs;
     extern __shared__ float go_smem[];                       // [2][nlm][kGoSlab] Y_lm, [2][kGoShells][nlm] U_lm
     __shared__ double sh[32];
     __shared__ int s_last;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int al = b / (nslab * nsplit), rest = b % (nslab * nsplit), slab = rest / nsplit, sp = rest % nsplit;
-    const int a = cell0 + al, j0 = slab * kGoSlab;
+    const int a = cell0 + al, k0 = slab * kGoSlab;          // the slab's first antipodal pair
     const int i_beg = sp * kGoShells, i_end = min(nrad, i_beg + kGoShells);
     float *syh = go_smem, *syl = go_smem + (size_t)nlm * kGoSlab;
     float *suh = syl + (size_t)nlm * kGoSlab, *sul = suh + (size_t)kGoShells * nlm;
+    // Y_lm at the first direction of each of the slab's pairs (Y_lm at the
+    // antipode is (-1)^l times it)
     for (int e = tid; e < nlm * kGoSlab; e += kGoThreads) {
-        const int lm = e / kGoSlab, jj = e % kGoSlab, j = j0 + jj;
-        syh[e] = j < nang ? Y32[(size_t)lm * nang + j] : 0.f;
-        syl[e] = j < nang ? Y32[(size_t)nlm * nang + (size_t)lm * nang + j] : 0.f;
+        const int lm = e / kGoSlab, k = k0 + e % kGoSlab;
+        const int j = k < npair ? __ldg(&pairs[k].x) : 0;
+        syh[e] = k < npair ? Y32[(size_t)lm * nang + j] : 0.f;
+        syl[e] = k < npair ? Y32[(size_t)nlm * nang + (size_t)lm * nang + j] : 0.f;
     }
     // the block's shells of U_lm (rows (a, i) of the transposed split table are contiguous)
     {
@@ -1149,47 +1205,64 @@ __device__ __forceinline__ void gather_own_block(const GoArgs A, int b, int nblk
             cj32[p] = 0.f;
         }
     __syncthreads();
-    const int j = j0 + lane;
+    const int k = k0 + lane;
+    const int2 ja = k < npair ? __ldg(&pairs[k]) : make_int2(0, 0);
+    const int lmax = (int)sqrtf((float)nlm + 0.5f) - 1;
     double ej = 0.0;
     for (int i = i_beg + warp; i < i_end; i += kGoThreads / 32) {
         const float *uh = suh + (size_t)(i - i_beg) * nlm, *ul = sul + (size_t)(i - i_beg) * nlm;
+        // even-l and odd-l parts of the own-cell sum, two accumulators each
         float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f, s2 = 0.f, e2 = 0.f, s3 = 0.f, e3 = 0.f;
-        int lm = 0;
-        for (; lm + 3 < nlm; lm += 4) {
-            df_mac(s0, e0, uh[lm], ul[lm], syh[lm * kGoSlab + lane], syl[lm * kGoSlab + lane]);
-            df_mac(s1, e1, uh[lm + 1], ul[lm + 1], syh[(lm + 1) * kGoSlab + lane], syl[(lm + 1) * kGoSlab + lane]);
-            df_mac(s2, e2, uh[lm + 2], ul[lm + 2], syh[(lm + 2) * kGoSlab + lane], syl[(lm + 2) * kGoSlab + lane]);
-            df_mac(s3, e3, uh[lm + 3], ul[lm + 3], syh[(lm + 3) * kGoSlab + lane], syl[(lm + 3) * kGoSlab + lane]);
-        }
-        for (; lm < nlm; ++lm) df_mac(s0, e0, uh[lm], ul[lm], syh[lm * kGoSlab + lane], syl[lm * kGoSlab + lane]);
-        if (j >= nang) continue;
-        const size_t p = ((size_t)al * nrad + i) * nang + j;
-        const dfl vs = df_add(df_add(df_norm(s0, e0), df_norm(s1, e1)), df_add(df_norm(s2, e2), df_norm(s3, e3)));
-        const double vown = df_to(vs) * invr[p];
-        float vh = 0.f, vl = 0.f;
-        const int *pp = pos + p * natoms;
-        // eight atoms at a time: their places, then their contributions, then
-        // the sum in atom order
-        for (int k0 = 0; k0 < natoms; k0 += 8) {
-            int q[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) q[u] = (k0 + u < natoms && k0 + u != a) ? pp[k0 + u] : -1;
-            float2 v[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = q[u] >= 0 ? pairv[q[u]] : make_float2(0.f, 0.f);
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (q[u] >= 0) {
-                    two_sum_acc(vh, vl, v[u].x);
-                    vl += v[u].y;
+        for (int l = 0; l <= lmax; ++l) {
+            int lm = l * l;
+            const int lm1 = lm + 2 * l + 1;
+            if (l & 1) {
+                for (; lm + 1 < lm1; lm += 2) {
+                    df_mac(s2, e2, uh[lm], ul[lm], syh[lm * kGoSlab + lane], syl[lm * kGoSlab + lane]);
+                    df_mac(s3, e3, uh[lm + 1], ul[lm + 1], syh[(lm + 1) * kGoSlab + lane], syl[(lm + 1) * kGoSlab + lane]);
                 }
+                if (lm < lm1) df_mac(s2, e2, uh[lm], ul[lm], syh[lm * kGoSlab + lane], syl[lm * kGoSlab + lane]);
+            } else {
+                for (; lm + 1 < lm1; lm += 2) {
+                    df_mac(s0, e0, uh[lm], ul[lm], syh[lm * kGoSlab + lane], syl[lm * kGoSlab + lane]);
+                    df_mac(s1, e1, uh[lm + 1], ul[lm + 1], syh[(lm + 1) * kGoSlab + lane], syl[(lm + 1) * kGoSlab + lane]);
+                }
+                if (lm < lm1) df_mac(s0, e0, uh[lm], ul[lm], syh[lm * kGoSlab + lane], syl[lm * kGoSlab + lane]);
+            }
         }
-        const double Vt = vown + ((double)vh + (double)vl);
-        V[p] = Vt;
-        const double c = 0.5 * (W[p] * Vt);
-        cj[p] = c;
-        cj32[p] = (float)c;
-        ej += c * rho[p];
+        if (k >= npair) continue;
+        const dfl ev = df_add(df_norm(s0, e0), df_norm(s1, e1)), od = df_add(df_norm(s2, e2), df_norm(s3, e3));
+        // the pair's two points: V_own = even + odd at j, even - odd at its antipode
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            const size_t p = ((size_t)al * nrad + i) * nang + (t ? ja.y : ja.x);
+            const dfl vs = t ? df_sub(ev, od) : df_add(ev, od);
+            const double vown = df_to(vs) * invr[p];
+            float vh = 0.f, vl = 0.f;
+            const int *pp = pos + p * natoms;
+            // eight atoms at a time: their places, then their contributions, then
+            // the sum in atom order
+            for (int q0 = 0; q0 < natoms; q0 += 8) {
+                int q[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) q[u] = (q0 + u < natoms && q0 + u != a) ? pp[q0 + u] : -1;
+                float2 v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) v[u] = q[u] >= 0 ? pairv[q[u]] : make_float2(0.f, 0.f);
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (q[u] >= 0) {
+                        two_sum_acc(vh, vl, v[u].x);
+                        vl += v[u].y;
+                    }
+            }
+            const double Vt = vown + ((double)vh + (double)vl);
+            V[p] = Vt;
+            const double c = 0.5 * (W[p] * Vt);
+            cj[p] = c;
+            cj32[p] = (float)c;
+            ej += c * rho[p];
+        }
     }
     ej = block_sum(ej, sh);
     if (tid == 0) part[b] = ej;
@@ -1457,7 +1530,7 @@ StepLaunch<MpArgs> step_multipole(const dftg_ctx *c, bool rw_ready)
     StepLaunch<MpArgs> s;
     s.args = MpArgs{c->natoms, c->cell0, c->nrad, c->nang, c->lmax, ngroup, (c->prec_mask & kPrecCross) ? 0 : 1,
                     rw_ready ? c->d_rw32 : nullptr, c->npad, c->d_rho, c->d_wb, c->d_w, c->d_Ywt32, c->d_maps32,
-                    c->d_scal, c->d_U, c->d_U32, c->d_U32T, c->d_spl, c->d_splm};
+                    c->d_scal, c->d_U, c->d_U32, c->d_U32T, c->d_spl, c->d_splm, c->d_lebpair, c->nlebpair};
     s.blocks = c->ncell * ngroup;
     s.smem = multipole_smem(c->nrad, c->nang);
     return s;
@@ -1482,7 +1555,7 @@ int launch_hartree_multipoles(dftg_ctx *c)
     const int N = c->nrad, nlm = c->nlm, nc = c->ncell, c0 = c->cell0;
     // the mixed multipole kernels keep radial vectors per block in shared
     // memory: up to 256 radial points (the FP64 kernels take any)
-    const bool mp = (c->prec_mask & kPrecMultipole) != 0 && N <= 256;
+    const bool mp = (c->prec_mask & kPrecMultipole) != 0 && N <= 256 && c->nlebpair > 0;
     const size_t rplane = (size_t)c->natoms * nlm * N;
     const int nrhs = nc * nlm;
     if (mp) {
@@ -1528,12 +1601,12 @@ int launch_hartree_multipoles(dftg_ctx *c)
 StepLaunch<GoArgs> step_gather_own(const dftg_ctx *c, bool rho_scaled)
 {
     const int N = c->nrad;
-    const int nslab = (c->nang + kGoSlab - 1) / kGoSlab, nsplit = (N + kGoShells - 1) / kGoShells;
+    const int nslab = (c->nlebpair + kGoSlab - 1) / kGoSlab, nsplit = (N + kGoShells - 1) / kGoShells;
     StepLaunch<GoArgs> s;
     s.args = GoArgs{c->npts, c->npad, (size_t)c->natoms * c->nlm * N, c->natoms, c->cell0, N, c->nang, c->nlm, nslab,
                     nsplit, rho_scaled ? 1 : 0, c->d_pairpos, reinterpret_cast<const float2 *>(c->d_pairv), c->d_U32T,
                     c->d_Y32, c->d_invr, c->d_w, c->d_rho, c->d_V, c->d_cj, c->d_cj32, c->d_red, c->d_scal,
-                    c->d_counters + kCntEJ};
+                    c->d_counters + kCntEJ, c->d_lebpair, c->nlebpair};
     s.blocks = c->ncell * nslab * nsplit;
     s.smem = sizeof(float) * 2 * (size_t)c->nlm * (kGoSlab + kGoShells);
     return s;
@@ -1555,7 +1628,7 @@ int group_gather_own(const GoArgs *d_args, const GroupQueue &q, size_t smem, int
 int launch_hartree_cross(dftg_ctx *c)
 {
     const int N = c->nrad;
-    const bool mp = (c->prec_mask & kPrecMultipole) != 0 && N <= 256;
+    const bool mp = (c->prec_mask & kPrecMultipole) != 0 && N <= 256 && c->nlebpair > 0;
     const unsigned nb = (unsigned)(c->npad / 128);
     if (c->prec_mask & kPrecCross) {
         if (c->npairs > 0) {
