@@ -27,8 +27,10 @@
 //     128 x KP block per slice and tile, copied with cp.async.bulk;
 //   B slices: [slice][NP/8][KP/8][8][8] FP16 (rows nu, K = mu).
 // CTA: warp 0 producer (bulk copies), warp 1 TMEM owner + MMA issuer,
-// warps 2-9 epilogue: TMEM lanes 32 (w % 4) ..., the two warps of a lane quarter
-// take alternate 16-column blocks and meet in shared memory per tile.
+// warps 2-17 epilogue in two groups of eight that take alternate tiles (group g
+// the tiles of TMEM accumulator set g); TMEM lanes 32 (w % 4) ..., the two warps
+// of a lane quarter in a group take alternate 8-column groups and meet in shared
+// memory per tile.
 // Persistent over tiles: three A stages and two TMEM accumulator sets, so the
 // copies of the next tiles and the MMAs of one tile overlap the epilogue of the
 // previous one.  Every mbarrier wait is bounded: on expiry the CTA records an
@@ -49,10 +51,10 @@ constexpr int kTcMaxK = 80;                   // nbf <= 80 for this kernel
 constexpr int kTcEpiWarps = 16;               // four per TMEM lane quarter
 constexpr int kTcThreads = (2 + kTcEpiWarps) * 32;
 constexpr uint32_t kTcTmemCols = 512;
-// named barrier 1 over the epilogue warps
-__device__ __forceinline__ void epi_bar_sync_tc()
+// named barriers 1 and 2 over the eight warps of epilogue group 0 and 1
+__device__ __forceinline__ void epi_group_bar(int g)
 {
-    asm volatile("bar.sync 1, %0;" ::"n"(kTcEpiWarps * 32) : "memory");
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "n"(kTcEpiWarps * 16) : "memory");
 }
 
 __device__ __forceinline__ void unpack8_f16(uint4 u, float (&v)[8])
@@ -98,7 +100,7 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
     unsigned char *sB = smem + kTcStages * a_stage_bytes;        // [slices][B block]
     __shared__ __align__(16) int s_texp[kTcMaxK];
     __shared__ int s_fail;
-    __shared__ float2 s_part[3][kTcTile];         // (S, E) of column parts 1-3, per row
+    __shared__ float2 s_part[2][kTcTile];         // (S, E) of the second column half of each epilogue group
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -193,27 +195,31 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
         __syncwarp();
     } else {
         // ------------------------------------------------------------ epilogue
+        // two groups of eight warps take alternate tiles (group g the tiles of
+        // TMEM accumulator set g), so two tiles' epilogues are in flight; in a
+        // group, the two warps of a lane quarter take alternate 8-column groups
         const int q = warp & 3;                 // TMEM lane quarter of this warp
-        const int part = (warp - 2) >> 2;       // 8-column groups part, part + 4, ...
+        const int eg = (warp - 2) >> 3;         // epilogue group = accumulator set
+        const int half = ((warp - 2) >> 2) & 1; // 8-column groups 8 half, 8 half + 16, ...
         const int r = q * 32 + lane;            // row of the tile = TMEM lane
         const int kc = KP / 8;
-        for (int it = 0; it < my_tiles; ++it) {
+        for (int it = eg; it < my_tiles; it += 2) {
             const int s = it % kTcStages;
-            const int bset = it & 1, nb = it >> 1;
-            bool ok = mbar_wait(&sh->tmem_full[bset], (uint32_t)(nb & 1));
+            const int nb = it >> 1;
+            bool ok = mbar_wait(&sh->tmem_full[eg], (uint32_t)(nb & 1));
             if (!ok) { atomicExch(err, 4); s_fail = 1; }
-            epi_bar_sync_tc();
+            epi_group_bar(eg);
             if (s_fail) break;
             tc_fence_after();
             const int tile = vb + it * nvb;
             const size_t p = (size_t)tile * kTcTile + r;
             const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
-            const uint32_t ta0 = tmem + (uint32_t)(bset * 256) + ((uint32_t)(q * 32) << 16);
+            const uint32_t ta0 = tmem + (uint32_t)(eg * 256) + ((uint32_t)(q * 32) << 16);
             // two independent compensated accumulators (even / odd columns)
             float S[2] = {0.f, 0.f}, E[2] = {0.f, 0.f};
             // columns nu >= nbf hold T = 0 and phi = 0 (zero rows of B, zero slices
             // of A) and contribute exactly nothing, so every group is done whole
-            for (int nb8 = 8 * part; nb8 < nbf; nb8 += 32) {
+            for (int nb8 = 8 * half; nb8 < nbf; nb8 += 16) {
                 float dh[8], dl[8], dl2[8];
                 tmem_ld8(ta0 + (uint32_t)nb8, dh);
                 tmem_ld8(ta0 + (uint32_t)(kTcAcc + nb8), dl);
@@ -259,23 +265,17 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
                 St = w;
             }
             tc_fence_before();
-            if (part > 0) s_part[part - 1][r] = make_float2(St, Et);
-            epi_bar_sync_tc();                   // TMEM and A-stage reads of this tile done, parts posted
-            if (threadIdx.x == 64) {
-                mbar_arrive(&sh->tmem_empty[bset]);
+            if (half == 1) s_part[eg][r] = make_float2(St, Et);
+            epi_group_bar(eg);                   // TMEM and A-stage reads of this tile done, halves posted
+            if (threadIdx.x == 64 + 256 * eg) {
+                mbar_arrive(&sh->tmem_empty[eg]);
                 mbar_arrive(&sh->empty[s]);
             }
-            if (part == 0) {
-                // the four column parts in a fixed order (TwoSum)
-                float w = St, e = Et;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const float2 o = s_part[k][r];
-                    const float t2 = w + o.x;
-                    const float bq = t2 - w;
-                    e += o.y + (w - (t2 - bq)) + (o.x - bq);
-                    w = t2;
-                }
+            if (half == 0) {
+                const float2 o = s_part[eg][r];
+                const float w = St + o.x;
+                const float bq = w - St;
+                const float e = Et + o.y + (St - (w - bq)) + (o.x - bq);
                 const int ep = row_exp[p];
                 rho[p] = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
             }
