@@ -91,21 +91,18 @@ __device__ __forceinline__ int exp_bound(uint32_t absbits)
     return e < kCtExpMin ? kCtExpMin : (e > kCtExpMax ? kCtExpMax : e);
 }
 
-// eight consecutive K values (scaled, |x| < 128) -> three BF16 slices, the
-// first an integer
-__device__ __forceinline__ void slice8_fixed(const float (&v)[8], uint4 (&out)[kCtSlices])
+// eight consecutive K values as four packed pairs (scaled, |x| < 128) -> three
+// BF16 slices, the first an integer
+__device__ __forceinline__ void slice8_fixed(const float2 (&v)[4], uint4 (&out)[kCtSlices])
 {
     uint32_t w[kCtSlices][4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        float x0 = v[2 * j], x1 = v[2 * j + 1];
-        const float i0 = rintf(x0), i1 = rintf(x1);
-        const __nv_bfloat162 h1 = __floats2bfloat162_rn(i0, i1);   // exact: integers <= 128
-        x0 -= i0;                                                  // exact
-        x1 -= i1;
-        const __nv_bfloat162 h2 = __floats2bfloat162_rn(x0, x1);
-        const float2 f2 = __bfloat1622float2(h2);
-        const __nv_bfloat162 h3 = __floats2bfloat162_rn(x0 - f2.x, x1 - f2.y);
+        const float2 i = make_float2(rintf(v[j].x), rintf(v[j].y));
+        const __nv_bfloat162 h1 = __float22bfloat162_rn(i);        // exact: integers <= 128
+        const float2 x = f2sub(v[j], i);                           // exact
+        const __nv_bfloat162 h2 = __float22bfloat162_rn(x);
+        const __nv_bfloat162 h3 = __float22bfloat162_rn(f2sub(x, __bfloat1622float2(h2)));
         w[0][j] = *reinterpret_cast<const uint32_t *>(&h1);
         w[1][j] = *reinterpret_cast<const uint32_t *>(&h2);
         w[2][j] = *reinterpret_cast<const uint32_t *>(&h3);
@@ -114,14 +111,12 @@ __device__ __forceinline__ void slice8_fixed(const float (&v)[8], uint4 (&out)[k
     for (int i = 0; i < kCtSlices; ++i) out[i] = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
 }
 
-__device__ __forceinline__ void unpack8(uint4 u, float (&v)[8])
+// eight BF16 values (16 bytes) -> four packed FP32 pairs
+__device__ __forceinline__ void unpack8(uint4 u, float2 (&v)[4])
 {
     const uint32_t w[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        v[2 * j] = __uint_as_float(w[j] << 16);
-        v[2 * j + 1] = __uint_as_float(w[j] & 0xffff0000u);
-    }
+    for (int j = 0; j < 4; ++j) v[j] = make_float2(__uint_as_float(w[j] << 16), __uint_as_float(w[j] & 0xffff0000u));
 }
 
 // per chunk: exponent bounds of max |c_xc / w| and max |c_j / w| (block per chunk)
@@ -286,11 +281,11 @@ __device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb
                 unsigned char *sA = smem + (size_t)s * stage;
                 unsigned char *sB = sA + a_region;
                 const float *sc = reinterpret_cast<const float *>(sA + c_off);
-                float cx[8], cy[8];
+                float2 cx[4], cy[4];
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    cx[k] = sc[8 * g + k] * sx;
-                    cy[k] = sc[kCtKS + 8 * g + k] * sj;
+                for (int k = 0; k < 4; ++k) {
+                    cx[k] = f2mul(*reinterpret_cast<const float2 *>(sc + 8 * g + 2 * k), make_float2(sx, sx));
+                    cy[k] = f2mul(*reinterpret_cast<const float2 *>(sc + kCtKS + 8 * g + 2 * k), make_float2(sj, sj));
                 }
                 // the lane's rows one at a time: its slice loads first, then the
                 // arithmetic (predicated, no early exit)
@@ -313,20 +308,20 @@ __device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb
                         if (mu < nbf) {
                             const uint32_t oa = core_off(mu, 8 * g, kCtKcores);
                             // B row scale: phi 2^(7 - e_mu) -> phi 2^(7 - s_mu)
-                            const float rf = rfr[j0 + jj];
-                            float v[8], t[8];
+                            const float2 rf = make_float2(rfr[j0 + jj], rfr[j0 + jj]);
+                            float2 v[4], t[4];
                             unpack8(q0[jj], v);
                             unpack8(q1[jj], t);
 #pragma unroll
-                            for (int k = 0; k < 8; ++k) v[k] += t[k];
+                            for (int k = 0; k < 4; ++k) v[k] = f2add(v[k], t[k]);
                             unpack8(q2[jj], t);
-                            float bx[8], by[8];
+                            float2 bx[4], by[4];
 #pragma unroll
-                            for (int k = 0; k < 8; ++k) {
-                                v[k] += t[k];                          // phi 2^(7 - e_mu), |v| < 128
-                                const float u = v[k] * rf;
-                                bx[k] = cx[k] * u;                     // c phi 2^(7 - s_mu - v), |bx| < 128
-                                by[k] = cy[k] * u;
+                            for (int k = 0; k < 4; ++k) {
+                                v[k] = f2add(v[k], t[k]);              // phi 2^(7 - e_mu), |v| < 128
+                                const float2 u = f2mul(v[k], rf);
+                                bx[k] = f2mul(cx[k], u);               // c phi 2^(7 - s_mu - v), |bx| < 128
+                                by[k] = f2mul(cy[k], u);
                             }
                             uint4 sbx[kCtSlices], sby[kCtSlices];
                             slice8_fixed(bx, sbx);

@@ -215,8 +215,11 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
             const size_t p = (size_t)tile * kTcTile + r;
             const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
             const uint32_t ta0 = tmem + (uint32_t)(eg * 256) + ((uint32_t)(q * 32) << 16);
-            // two independent compensated accumulators (even / odd columns)
-            float S[2] = {0.f, 0.f}, E[2] = {0.f, 0.f};
+            // two independent compensated accumulators (even / odd columns), the
+            // two lanes of packed FP32 pairs: every step below is one packed
+            // instruction for an (even, odd) column pair
+            float2 S = make_float2(0.f, 0.f), E = make_float2(0.f, 0.f);
+            const float2 k2m11 = make_float2(0x1p-11f, 0x1p-11f);
             // columns nu >= nbf hold T = 0 and phi = 0 (zero rows of B, zero slices
             // of A) and contribute exactly nothing, so every group is done whole
             for (int nb8 = 8 * half; nb8 < nbf; nb8 += 16) {
@@ -235,33 +238,37 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
                 const int ex[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
                 tmem_wait_ld();
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
+                for (int k = 0; k < 8; k += 2) {
                     // T~_nu 2^16 = D_hi + D_lo + 2^-11 D_lo2 as u + te (TwoSum of the
                     // first two), scaled by 2^(t_nu - 24); phi~ 2^8 = fh + fl
-                    const float u = dh[k] + dl[k];
-                    const float bp = u - dh[k];
-                    float te = (dh[k] - (u - bp)) + (dl[k] - bp) + dl2[k] * 0x1p-11f;
-                    const float sc = __int_as_float((127 - 24 + ex[k]) << 23);
-                    const float t = u * sc;
-                    te *= sc;
-                    const float fh = m1[k] + m2[k];                      // exact: multiples of 2^-11 below 2^9
-                    const float fl = m3[k] * 0x1p-11f;
+                    const float2 h = make_float2(dh[k], dh[k + 1]), l = make_float2(dl[k], dl[k + 1]);
+                    const float2 u = f2add(h, l);
+                    const float2 bp = f2sub(u, h);
+                    float2 te = f2fma(make_float2(dl2[k], dl2[k + 1]), k2m11,
+                                      f2add(f2sub(h, f2sub(u, bp)), f2sub(l, bp)));
+                    const float2 sc = make_float2(__int_as_float((127 - 24 + ex[k]) << 23),
+                                                  __int_as_float((127 - 24 + ex[k + 1]) << 23));
+                    const float2 t = f2mul(u, sc);
+                    te = f2mul(te, sc);
+                    // exact: multiples of 2^-11 below 2^9
+                    const float2 fh = f2add(make_float2(m1[k], m1[k + 1]), make_float2(m2[k], m2[k + 1]));
+                    const float2 fl = f2mul(make_float2(m3[k], m3[k + 1]), k2m11);
                     // S + E += (t + te)(fh + fl)
-                    const int a = k & 1;
-                    const float pr = t * fh;
-                    const float pe = fmaf(t, fh, -pr);
-                    const float w = S[a] + pr;
-                    const float bq = w - S[a];
-                    E[a] += ((S[a] - (w - bq)) + (pr - bq)) + (pe + fmaf(t, fl, te * fh));
-                    S[a] = w;
+                    const float2 pr = f2mul(t, fh);
+                    const float2 pe = f2fma(t, fh, make_float2(-pr.x, -pr.y));
+                    const float2 w = f2add(S, pr);
+                    const float2 bq = f2sub(w, S);
+                    E = f2add(E, f2add(f2add(f2sub(S, f2sub(w, bq)), f2sub(pr, bq)),
+                                       f2add(pe, f2fma(t, fl, f2mul(te, fh)))));
+                    S = w;
                 }
             }
             // fold the two accumulators (TwoSum)
             float St, Et;
             {
-                const float w = S[0] + S[1];
-                const float bq = w - S[0];
-                Et = E[0] + E[1] + (S[0] - (w - bq)) + (S[1] - bq);
+                const float w = S.x + S.y;
+                const float bq = w - S.x;
+                Et = E.x + E.y + (S.x - (w - bq)) + (S.y - bq);
                 St = w;
             }
             tc_fence_before();
