@@ -80,7 +80,7 @@ static void free_ctx(dftg_ctx *c)
                     c->d_XC, c->d_part, c->d_red, c->d_scal, c->d_Y, c->d_Yw, c->d_pre, c->d_pre32, c->d_rec,
                     c->d_rec32, c->d_rholm, c->d_U, c->d_U32, c->d_Y32, c->d_Ywt32, c->d_fold, c->d_Gt,
                     c->d_Gb, c->d_Kt, c->d_sx, c->d_splf, c->d_spl, c->d_splm, c->d_tiles,
-                    c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_rw32, c->d_wsplit, c->d_lebpair, c->d_flag,
+                    c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_sgrid, c->d_rw32, c->d_wsplit, c->d_lebpair, c->d_flag,
                     c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32, c->d_U32T,
                     c->d_bw_pt, c->d_bw_lm, c->d_bw_fpart, c->d_bw_out, c->d_bw_counter, c->d_bw_pairp,
                     c->d_bw_binfirst, c->d_bw_cpart, c->d_bw_geo, c->d_bw_geo64, c->d_bw_prim32,
@@ -334,8 +334,11 @@ int sync_scalars(dftg_ctx *c)
 // device part of one Fock build; P already in c->d_P
 int fock_pipeline(dftg_ctx *c)
 {
-    DFTG_TRY(launch_density(c));
-    DFTG_TRY(launch_atom_sums(c, kSumsFactor));
+    const bool fused = sgrid_route(c);
+    DFTG_TRY(launch_density(c, fused));
+    // the whole build's form takes the correction factor from the P-slicing
+    // step (2 tr(P S_grid)); otherwise the per-atom sums give it
+    if (!fused) DFTG_TRY(launch_atom_sums(c, kSumsFactor));
     // rescales rho by the correction factor; with the mixed point kernel it also
     // sums the corrected N and writes the rho w_becke planes of the multipoles
     DFTG_TRY(launch_xc_points(c, true, (c->prec_mask & kPrecLda) != 0));

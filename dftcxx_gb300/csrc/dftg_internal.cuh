@@ -46,6 +46,21 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &e, float x)
     s = t;
 }
 
+// Packed FP32 pairs: one instruction for two independent lanes, each rounded to
+// nearest exactly as the scalar operation (and, being explicit roundings, never
+// contracted into an FMA, so error-free transformations keep their meaning).
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;"
+        : "=l"(d)
+        : "l"(*reinterpret_cast<const unsigned long long *>(&a)), "l"(*reinterpret_cast<const unsigned long long *>(&b)));
+    return *reinterpret_cast<const float2 *>(&d);
+}
+
 // Double-float arithmetic (value = h + l, |l| <= ulp(h) / 2): about 48-bit
 // precision from FP32 operations, for per-build loops that would otherwise run
 // in FP64 (slow on this GPU).  TwoSum / TwoProd with fmaf (Dekker, Knuth).
@@ -224,7 +239,7 @@ __device__ __forceinline__ bool last_block(int *counter, int *s_flag)
 }
 
 // counters of the last-block reductions
-enum { kCntAtoms = 0, kCntLda = 1, kCntEJ = 2, kNumCounters = 4 };
+enum { kCntAtoms = 0, kCntLda = 1, kCntEJ = 2, kCntTrace = 3, kNumCounters = 4 };
 
 }  // namespace dftg
 
@@ -280,6 +295,7 @@ struct dftg_ctx {
     int nchunk = 0;               // point chunks of the contraction
     int ntiles = 0;               // output blocks on or above the diagonal
     void *d_tiles = nullptr;      // [ntiles] int2 block coordinates
+    double *d_sgrid = nullptr;    // [nbf][nbf] S_grid = Phi^T diag(w) Phi (FP64), for the correction factor
     double *d_red = nullptr;      // reduction partials
     size_t red_elems = 0;
     double *d_scal = nullptr;     // scalars, see kScal* below
@@ -442,12 +458,20 @@ inline int group_grid(const GroupQueue &q, int occ, int nsm)
 // The arguments of one molecule's launch of each step, as one record: the
 // single build passes it by value, a batch's grouped launch reads molecule m's
 // record from a device array (one per molecule).
-struct SlicePArgs {            // P -> BF16 slices (density operand)
+struct SlicePArgs {            // P -> FP16 slices (density operand)
     int nbf, KP, NP;
     const double *P;
     double *Pcopy;             // also copies P here when not null (the context's own P)
     void *B;
     int *col_exp;
+    // when S is not null: sum_p w rho = 2 tr(P S_grid) and the correction factor
+    // into scal, from per-column partials and the last block
+    const double *S;           // S_grid [nbf][nbf]
+    const double *atoms;       // [natoms][4]: x, y, z, Z
+    int natoms;
+    double *part;              // [nbf] column partials
+    int *counter;
+    double *scal;
 };
 struct DensTcArgs {            // rho on the tensor cores
     int nbf, KP, NP, ntiles;
@@ -567,11 +591,16 @@ int mark(dftg_ctx *c, const char *name);
 int launch_grid(dftg_ctx *c);
 int launch_amplitudes(dftg_ctx *c);
 // k_density.cu
-int launch_density(dftg_ctx *c);
+// fused: the whole build's form on the S_grid route (the correction factor
+// from the P-slicing step, no atom-sum pass)
+int launch_density(dftg_ctx *c, bool fused = false);
 enum { kSumsOnly = 0, kSumsCorrect = 1, kSumsFactor = 2 };
 // k_density_tc.cu
 int density_tc_setup(dftg_ctx *c);
-int launch_density_tc(dftg_ctx *c);
+// the mixed build takes the density correction's total from 2 tr(P S_grid)
+// in the P-slicing step (no atom-sum pass)
+bool sgrid_route(const dftg_ctx *c);
+int launch_density_tc(dftg_ctx *c, bool fused);
 // k_density_tt.cu
 int density_tt_setup(dftg_ctx *c);
 int launch_density_tt(dftg_ctx *c);
@@ -618,7 +647,7 @@ int ct_launch_cexp(dftg_ctx *c, int nkb, int kbpc, int nchunk, const float *cx, 
 // and shared memory; the single build launches exactly these), and the batch's
 // grouped launch of each step over all molecules (device argument arrays, one
 // queue per launch).
-StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy);
+StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy, bool fused);
 StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c);
 StepLaunch<SumsArgs> step_atom_sums(const dftg_ctx *c, int mode);
 StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n);

@@ -9,12 +9,15 @@
 // single launch (GroupQueue in dftg_internal.cuh), so every molecule's results
 // are bit-identical to its own build.  Per batch: one memset of the queue
 // counters, then nine launches --
-//   P slices (and the copy of P into the context), density (tensor cores),
-//   per-atom sums + LDA point kernel (one launch: a molecule's point blocks
-//   wait, bounded, until its last atom-sum block has published the correction
-//   factor), multipole chain, cross-atom bins, potential gather + E_J,
+//   P slices (with the copy of P into the context and the correction factor
+//   from 2 tr(P S_grid)), density (tensor cores), LDA point kernel (with the
+//   correction), multipole chain, cross-atom bins, potential gather + E_J,
 //   coefficient bounds, XC / J contraction (tensor cores), partial reduction
 //   (which also writes the caller's output buffers and scalars).
+// The point-kernel launch also takes per-atom sum items for molecules without
+// S_grid; their point blocks wait (bounded) for the molecule's factor.  Every
+// context a batch accepts has S_grid, so no block waits but in the self-test of
+// the bounded wait.
 // The launch records of every molecule (arguments, block counts, shared memory)
 // come from the same step functions the single build launches with, and are
 // copied to the device once per set of buffers.
@@ -40,6 +43,7 @@ struct BatchPlan {
     int *d_heads = nullptr;                  // [kNumSteps] counters, then done[nmol]
     int *d_done = nullptr;
     int *d_err = nullptr;
+    const int *d_self_prefix = nullptr;      // [nmol + 1] one point item, of molecule 0 (the wait self-test)
     size_t zero_bytes = 0;                   // counters and done flags, cleared before every batch
     GroupQueue q[kNumSteps];
     size_t smem[kNumSteps] = {};
@@ -80,10 +84,11 @@ int batch_plan_create(dftg_ctx *const *ctx, int n, const double *const *P, doubl
         const dftg_ctx *c = ctx[i];
         if (!batch_group_eligible(c)) { set_error("context %d cannot join a persistent batch", i); return DFTG_ERR_STATE; }
         if (c->lmax != lmax) lmax = -1;
-        s0[i] = step_slice_P(c, P[i], P[i] != c->d_P ? c->d_P : nullptr);
+        s0[i] = step_slice_P(c, P[i], P[i] != c->d_P ? c->d_P : nullptr, true);
         s1[i] = step_density_tc(c);
         s2[i] = step_atom_sums(c, kSumsFactor);
         s3[i] = step_lda(c, true, true);
+        if (sgrid_route(c)) s2[i].blocks = 0;   // the P-slicing step writes the factor
         s4[i] = step_multipole(c, s3[i].args.rw32 != nullptr);
         s5[i] = step_vcross_bins(c);
         s6[i] = step_gather_own(c, true);
@@ -101,7 +106,8 @@ int batch_plan_create(dftg_ctx *const *ctx, int n, const double *const *P, doubl
     }
     // device layout: counters + done flags, error flag, prefix arrays, argument records
     const size_t off_err = sizeof(int) * ((size_t)kCtlInts + n);
-    const size_t off_prefix = align16(off_err + sizeof(int));
+    const size_t off_self = align16(off_err + sizeof(int));
+    const size_t off_prefix = align16(off_self + sizeof(int) * (size_t)(n + 1));
     const size_t prefix_bytes = sizeof(int) * (size_t)kNumSteps * (n + 1);
     const size_t rec[kNumSteps] = {sizeof(SlicePArgs), sizeof(DensTcArgs), sizeof(SumsArgs), sizeof(LdaArgs),
                                    sizeof(MpArgs),     sizeof(VcbArgs),    sizeof(GoArgs),   sizeof(CexpArgs),
@@ -131,6 +137,9 @@ int batch_plan_create(dftg_ctx *const *ctx, int n, const double *const *P, doubl
     for (int i = 0; i < n; ++i) s2[i].args.done = bp->d_done + i;
 
     std::vector<unsigned char> h(total, 0);
+    int *hself = reinterpret_cast<int *>(h.data() + off_self);
+    for (int i = 0; i <= n; ++i) hself[i] = i > 0 ? 1 : 0;
+    bp->d_self_prefix = reinterpret_cast<const int *>(base + off_self);
     int *hp = reinterpret_cast<int *>(h.data() + off_prefix);
     auto fill = [&](int st, auto &steps) {
         int *pre = hp + (size_t)st * (n + 1);
@@ -179,14 +188,23 @@ int batch_plan_enqueue(const BatchPlan *bp, cudaStream_t st, int stall_mol, unsi
     const int nsm = bp->nsm, dev = bp->device;
     DFTG_CUDA(cudaMemsetAsync(bp->d_heads, 0, bp->zero_bytes, st));
     const SumsLdaCtl ctl{bp->q[kStLda].head, bp->d_done, bp->d_err, limit_ns, stall_mol};
-    if (sums_lda_only)
-        return group_sums_lda(static_cast<const SumsArgs *>(bp->args[kStSums]), bp->q[kStSums],
-                              static_cast<const LdaArgs *>(bp->args[kStLda]), bp->q[kStLda], ctl, nsm, st);
+    if (sums_lda_only) {
+        // the self-test: one point item of molecule 0, which waits for a flag
+        // that nothing sets (no atom-sum items run)
+        GroupQueue qs = bp->q[kStSums], ql = bp->q[kStLda];
+        qs.nitems = 0;
+        ql.prefix = bp->d_self_prefix;
+        ql.nitems = 1;
+        ql.take = 1;
+        return group_sums_lda(static_cast<const SumsArgs *>(bp->args[kStSums]), qs,
+                              static_cast<const LdaArgs *>(bp->args[kStLda]), ql, ctl, nsm, st);
+    }
     DFTG_TRY_L(group_slice_P(static_cast<const SlicePArgs *>(bp->args[kStSliceP]), bp->q[kStSliceP], nsm, st));
     DFTG_TRY_L(group_density_tc(static_cast<const DensTcArgs *>(bp->args[kStDensity]), bp->q[kStDensity],
                                 bp->smem[kStDensity], dev, nsm, st));
-    DFTG_TRY_L(group_sums_lda(static_cast<const SumsArgs *>(bp->args[kStSums]), bp->q[kStSums],
-                              static_cast<const LdaArgs *>(bp->args[kStLda]), bp->q[kStLda], ctl, nsm, st));
+    if (bp->q[kStSums].nitems + bp->q[kStLda].nitems > 0)
+        DFTG_TRY_L(group_sums_lda(static_cast<const SumsArgs *>(bp->args[kStSums]), bp->q[kStSums],
+                                  static_cast<const LdaArgs *>(bp->args[kStLda]), bp->q[kStLda], ctl, nsm, st));
     DFTG_TRY_L(group_multipole(static_cast<const MpArgs *>(bp->args[kStMultipole]), bp->q[kStMultipole],
                                bp->smem[kStMultipole], dev, nsm, st));
     if (bp->q[kStVcb].nitems > 0)

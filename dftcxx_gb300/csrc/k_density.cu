@@ -406,8 +406,9 @@ __global__ void __launch_bounds__(kRedBlock) k_lda(const LdaArgs a)
 // published the correction factor (done[m] = 1): every item it can wait on was
 // handed out before it, to a running CTA, so the wait ends.  A wait that gives
 // up records code 21 in *err and stops the CTA (the batch's results are then
-// invalid).  stall_mol >= 0 makes that molecule's point blocks wait for a value
-// nothing writes (the self-test of the bounded wait).
+// invalid).  A molecule without atom-sum items (its factor came from the
+// P-slicing step) does not wait.  stall_mol >= 0 makes that molecule's point
+// blocks wait for a value nothing writes (the self-test of the bounded wait).
 __global__ void __launch_bounds__(kRedBlock) k_sums_lda_group(const SumsArgs *__restrict__ sa, GroupQueue qs,
                                                               const LdaArgs *__restrict__ la, GroupQueue ql,
                                                               SumsLdaCtl ctl)
@@ -430,7 +431,10 @@ __global__ void __launch_bounds__(kRedBlock) k_sums_lda_group(const SumsArgs *__
             } else {
                 const int j = i - qs.nitems;
                 const int m = gq_molecule(ql, j), b0 = __ldg(ql.prefix + m);
-                if (!wait_flag_ge(ctl.done + m, m == ctl.stall_mol ? 2 : 1, ctl.limit_ns, &s_ok)) {
+                // a molecule without atom-sum items has its factor already
+                // (the P-slicing step); the self-test's molecule waits regardless
+                const bool wait = m == ctl.stall_mol || __ldg(qs.prefix + m + 1) > __ldg(qs.prefix + m);
+                if (wait && !wait_flag_ge(ctl.done + m, m == ctl.stall_mol ? 2 : 1, ctl.limit_ns, &s_ok)) {
                     if (threadIdx.x == 0) atomicExch(ctl.err, 21);
                     return;
                 }
@@ -443,7 +447,7 @@ __global__ void __launch_bounds__(kRedBlock) k_sums_lda_group(const SumsArgs *__
 
 // ---------------------------------------------------------------- launchers
 
-int launch_density(dftg_ctx *c)
+int launch_density(dftg_ctx *c, bool fused)
 {
     c->rw_ready = false;             // a new density: the rho w_becke planes are stale
     if (!(c->prec_mask & kPrecDensity)) {
@@ -452,7 +456,7 @@ int launch_density(dftg_ctx *c)
         if (sm > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_density<double>), c->device));
         k_density<double><<<nb, 128, sm, c->stream>>>(c->nbf, c->npad, c->d_phi, c->d_P, c->d_rho);
     } else if (c->tc_ready) {
-        DFTG_TRY_L(launch_density_tc(c));
+        DFTG_TRY_L(launch_density_tc(c, fused));
     } else if (c->dt_ready) {
         DFTG_TRY_L(launch_density_tt(c));
     } else {

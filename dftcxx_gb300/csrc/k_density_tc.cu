@@ -31,6 +31,9 @@
 // the tiles of TMEM accumulator set g); TMEM lanes 32 (w % 4) ..., the two warps
 // of a lane quarter in a group take alternate 8-column groups and meet in shared
 // memory per tile.
+// Whole-build form: the density correction's total is known before this pass,
+// sum_p w rho = 2 tr(P S_grid) with S_grid = Phi^T diag(w) Phi made once per
+// grid, so the P-slicing step forms the trace and the factor (no atom-sum pass).
 // Persistent over tiles: three A stages and two TMEM accumulator sets, so the
 // copies of the next tiles and the MMAs of one tile overlap the epilogue of the
 // previous one.  Every mbarrier wait is bounded: on expiry the CTA records an
@@ -430,43 +433,77 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
 // P (FP64, nbf x nbf, symmetric) -> three FP16 slices per column in the B
 // layout: one warp per column, lanes over the rows; with Pcopy the warp also
 // copies its column of P there
-__device__ __forceinline__ void slice_P_block(const SlicePArgs a, int vb)
+// One block of the P slicing (a warp per column nu of B): the column's
+// exponent and FP16 slices, and with a.S its share of tr(P S_grid); the
+// molecule's last block (of nvb) then writes sum_p w rho = 2 tr(P S_grid) and
+// the correction factor sum Z / sum_p w rho (moleculargrid.cpp:132-146), the
+// per-column partials summed in column order.
+__device__ __forceinline__ void slice_P_block(const SlicePArgs a, int vb, int nvb)
 {
+    __shared__ int s_last;
     const int nbf = a.nbf, KP = a.KP, NP = a.NP;
     const double *__restrict__ P = a.P;
     uint16_t *__restrict__ B = static_cast<uint16_t *>(a.B);
     const int nu = vb * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (nu >= NP) return;
-    const unsigned long long *__restrict__ Pb = reinterpret_cast<const unsigned long long *>(P);
-    unsigned long long mx = 0ull;
-    if (nu < nbf)
-        for (int mu = lane; mu < nbf; mu += 32) {
-            const unsigned long long v = Pb[(size_t)nu * nbf + mu];
-            if (a.Pcopy) reinterpret_cast<unsigned long long *>(a.Pcopy)[(size_t)nu * nbf + mu] = v;
-            mx = max(mx, v & 0x7fffffffffffffffull);
+    if (nu < NP) {
+        const unsigned long long *__restrict__ Pb = reinterpret_cast<const unsigned long long *>(P);
+        unsigned long long mx = 0ull;
+        double tr = 0.0;
+        if (nu < nbf)
+            for (int mu = lane; mu < nbf; mu += 32) {
+                const unsigned long long v = Pb[(size_t)nu * nbf + mu];
+                if (a.Pcopy) reinterpret_cast<unsigned long long *>(a.Pcopy)[(size_t)nu * nbf + mu] = v;
+                mx = max(mx, v & 0x7fffffffffffffffull);
+                if (a.S) tr = fma(__longlong_as_double((long long)v), a.S[(size_t)nu * nbf + mu], tr);
+            }
+        for (int o = 16; o > 0; o >>= 1) {
+            mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            tr += __shfl_xor_sync(0xffffffffu, tr, o);
         }
-    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    const int e = exp_above(mx);
-    if (nu < nbf && lane == 0) a.col_exp[nu] = e;
-    const size_t slice = (size_t)NP * KP;
-    for (int mu = lane; mu < KP; mu += 32) {
-        uint16_t h[kTcSlices];
-        slice3_f16((nu < nbf && mu < nbf) ? fixed30(Pb[(size_t)nu * nbf + mu], e) : 0ll, h);
-        const size_t o = core_off(nu, mu, KP / 8) / 2;
-        for (int i = 0; i < kTcSlices; ++i) B[(size_t)i * slice + o] = h[i];
+        const int e = exp_above(mx);
+        if (nu < nbf && lane == 0) {
+            a.col_exp[nu] = e;
+            if (a.S) a.part[nu] = tr;
+        }
+        const size_t slice = (size_t)NP * KP;
+        for (int mu = lane; mu < KP; mu += 32) {
+            uint16_t h[kTcSlices];
+            slice3_f16((nu < nbf && mu < nbf) ? fixed30(Pb[(size_t)nu * nbf + mu], e) : 0ll, h);
+            const size_t o = core_off(nu, mu, KP / 8) / 2;
+            for (int i = 0; i < kTcSlices; ++i) B[(size_t)i * slice + o] = h[i];
+        }
+    }
+    if (!a.S || !last_block_of(a.counter, nvb, &s_last)) return;
+    if (threadIdx.x < 32) {
+        // lane l: columns l, l + 32, ..., then a fixed shuffle tree (lane 0's order)
+        double t = 0.0, charge = 0.0;
+        for (int n = lane; n < nbf; n += 32) t += __ldcg(a.part + n);
+        for (int i = lane; i < a.natoms; i += 32) charge += a.atoms[4 * i + 3];
+        for (int o = 16; o > 0; o >>= 1) {
+            t += __shfl_xor_sync(0xffffffffu, t, o);
+            charge += __shfl_xor_sync(0xffffffffu, charge, o);
+        }
+        if (lane == 0) {
+            const double total = 2.0 * t;
+            a.scal[kScalSum] = total;
+            a.scal[kScalScale] = charge / total;
+        }
     }
 }
 
 constexpr int kSlicePThreads = 128;
 
-__global__ void __launch_bounds__(kSlicePThreads) k_slice_P(const SlicePArgs a) { slice_P_block(a, (int)blockIdx.x); }
+__global__ void __launch_bounds__(kSlicePThreads) k_slice_P(const SlicePArgs a)
+{
+    slice_P_block(a, (int)blockIdx.x, (int)gridDim.x);
+}
 
 __global__ void __launch_bounds__(kSlicePThreads) k_slice_P_group(const SlicePArgs *__restrict__ args, GroupQueue q)
 {
     __shared__ int s_item;
-    gq_run(q, &s_item, [&](int m, int vb, int) {
+    gq_run(q, &s_item, [&](int m, int vb, int nvb) {
         const SlicePArgs a = args[m];
-        slice_P_block(a, vb);
+        slice_P_block(a, vb, nvb);
         return true;
     });
 }
@@ -477,6 +514,79 @@ size_t density_tc_smem(int KP, int NP)
 }
 
 bool density_tc_supported(int nbf) { return nbf <= kTcMaxK; }
+
+// S_grid = Phi^T diag(w) Phi over the grid points, FP64, once per grid: with it
+// sum_p w_p rho_p = 2 tr(P S_grid) is known from P before the density pass.
+// Block b sums the pairs (mu <= nu) over points [b kSgChunk, (b + 1) kSgChunk)
+// into part[b][pair]; k_sgrid_sum adds the blocks in order and mirrors.
+constexpr int kSgThreads = 256, kSgPts = 32, kSgChunk = 1024;
+constexpr int kSgPairsMax = kTcMaxK * (kTcMaxK + 1) / 2;
+constexpr int kSgPerThread = (kSgPairsMax + kSgThreads - 1) / kSgThreads;
+
+__global__ void __launch_bounds__(kSgThreads) k_sgrid_part(int nbf, size_t npts, size_t npad,
+                                                           const double *__restrict__ phi,
+                                                           const double *__restrict__ w, double *__restrict__ part)
+{
+    __shared__ double sphi[kTcMaxK][kSgPts + 1];
+    __shared__ double sw[kSgPts];
+    __shared__ short2 spair[kSgPairsMax];
+    const int npair = nbf * (nbf + 1) / 2, tid = threadIdx.x;
+    for (int k = tid; k < npair; k += kSgThreads) {      // k = nu (nu + 1) / 2 + mu, mu <= nu
+        int nu = (int)((sqrtf(8.f * (float)k + 1.f) - 1.f) * 0.5f);
+        while (nu * (nu + 1) / 2 > k) --nu;
+        while ((nu + 1) * (nu + 2) / 2 <= k) ++nu;
+        spair[k] = make_short2((short)(k - nu * (nu + 1) / 2), (short)nu);
+    }
+    double acc[kSgPerThread];
+#pragma unroll
+    for (int q = 0; q < kSgPerThread; ++q) acc[q] = 0.0;
+    const size_t p0 = (size_t)blockIdx.x * kSgChunk, p1 = min(npts, p0 + kSgChunk);
+    for (size_t s0 = p0; s0 < p1; s0 += kSgPts) {
+        __syncthreads();
+        for (int e = tid; e < nbf * kSgPts; e += kSgThreads) {
+            const int mu = e / kSgPts, j = e % kSgPts;
+            sphi[mu][j] = s0 + j < p1 ? phi[(size_t)mu * npad + s0 + j] : 0.0;
+        }
+        if (tid < kSgPts) sw[tid] = s0 + tid < p1 ? w[s0 + tid] : 0.0;
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kSgPerThread; ++q) {
+            const int k = tid + q * kSgThreads;
+            if (k < npair) {
+                const short2 mn = spair[k];
+                double t = acc[q];
+                for (int j = 0; j < kSgPts; ++j) t = fma(sw[j] * sphi[mn.x][j], sphi[mn.y][j], t);
+                acc[q] = t;
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kSgPerThread; ++q) {
+        const int k = tid + q * kSgThreads;
+        if (k < npair) part[(size_t)blockIdx.x * npair + k] = acc[q];
+    }
+}
+
+__global__ void k_sgrid_sum(int nbf, int nblk, const double *__restrict__ part, double *__restrict__ S)
+{
+    const int npair = nbf * (nbf + 1) / 2;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= npair) return;
+    int nu = (int)((sqrtf(8.f * (float)k + 1.f) - 1.f) * 0.5f);
+    while (nu * (nu + 1) / 2 > k) --nu;
+    while ((nu + 1) * (nu + 2) / 2 <= k) ++nu;
+    const int mu = k - nu * (nu + 1) / 2;
+    double t = 0.0;
+    for (int b = 0; b < nblk; ++b) t += part[(size_t)b * npair + k];
+    S[(size_t)mu * nbf + nu] = t;
+    S[(size_t)nu * nbf + mu] = t;
+}
+
+bool sgrid_route(const dftg_ctx *c)
+{
+    return c->d_sgrid && c->tc_ready && !c->points_only && c->cell0 == 0 && c->ncell == c->natoms &&
+           (c->prec_mask & kPrecDensity) && (c->prec_mask & kPrecLda);
+}
 
 int density_tc_setup(dftg_ctx *c)
 {
@@ -499,6 +609,21 @@ int density_tc_setup(dftg_ctx *c)
     const size_t sm = density_tc_smem(c->tc_KP, c->tc_NP);
     (void)sm;
     DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_density_tc), c->device));
+    if (!c->points_only) {
+        const int nblk = (int)((c->npts + kSgChunk - 1) / kSgChunk), npair = c->nbf * (c->nbf + 1) / 2;
+        double *part = nullptr;
+        DFTG_CUDA(cudaMalloc(&c->d_sgrid, sizeof(double) * (size_t)c->nbf * c->nbf));
+        DFTG_CUDA(cudaMalloc(&part, sizeof(double) * (size_t)nblk * npair));
+        k_sgrid_part<<<nblk, kSgThreads, 0, c->stream>>>(c->nbf, c->npts, c->npad, c->d_phi, c->d_w, part);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) {
+            k_sgrid_sum<<<(npair + 127) / 128, 128, 0, c->stream>>>(c->nbf, nblk, part, c->d_sgrid);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        cudaFree(part);
+        if (e != cudaSuccess) return cuda_fail(e, "S_grid", __FILE__, __LINE__);
+    }
     int nsm = 0;
     DFTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     c->tc_grid = nsm < ntiles ? nsm : ntiles;
@@ -507,10 +632,13 @@ int density_tc_setup(dftg_ctx *c)
     return DFTG_OK;
 }
 
-StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy)
+StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy, bool fused)
 {
     StepLaunch<SlicePArgs> s;
-    s.args = SlicePArgs{c->nbf, c->tc_KP, c->tc_NP, P, Pcopy, c->d_tcB, c->d_tc_colexp};
+    const bool tr = fused && sgrid_route(c);
+    s.args = SlicePArgs{c->nbf, c->tc_KP, c->tc_NP, P, Pcopy, c->d_tcB, c->d_tc_colexp,
+                        tr ? c->d_sgrid : nullptr, c->d_atoms, c->natoms, c->d_red, c->d_counters + kCntTrace,
+                        c->d_scal};
     s.blocks = (c->tc_NP + kSlicePThreads / 32 - 1) / (kSlicePThreads / 32);
     s.smem = 0;
     return s;
@@ -527,9 +655,9 @@ StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c)
     return s;
 }
 
-int launch_density_tc(dftg_ctx *c)
+int launch_density_tc(dftg_ctx *c, bool fused)
 {
-    const StepLaunch<SlicePArgs> sp = step_slice_P(c, c->d_P, nullptr);
+    const StepLaunch<SlicePArgs> sp = step_slice_P(c, c->d_P, nullptr, fused);
     k_slice_P<<<sp.blocks, kSlicePThreads, 0, c->stream>>>(sp.args);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "density_slices");

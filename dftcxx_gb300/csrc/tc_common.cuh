@@ -157,21 +157,6 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// Packed FP32 pairs: one instruction for two independent lanes, each rounded to
-// nearest exactly as the scalar operation (and, being explicit roundings, never
-// contracted into an FMA, so error-free transformations keep their meaning).
-__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 f2sub(float2 a, float2 b)
-{
-    unsigned long long d;
-    asm("sub.rn.f32x2 %0, %1, %2;"
-        : "=l"(d)
-        : "l"(*reinterpret_cast<const unsigned long long *>(&a)), "l"(*reinterpret_cast<const unsigned long long *>(&b)));
-    return *reinterpret_cast<const float2 *>(&d);
-}
-
 // named barrier 1 over the 4 epilogue warps (128 threads)
 __device__ __forceinline__ void epi_bar_sync()
 {
