@@ -94,6 +94,9 @@ static void free_ctx(dftg_ctx *c)
     for (cudaEvent_t ev : c->prof_ev)
         if (ev) cudaEventDestroy(ev);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    if (c->aux_stream) cudaStreamDestroy(c->aux_stream);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     delete c;
 }
 
@@ -209,7 +212,8 @@ static int build_ctx(dftg_ctx *c, const dftg_molecule *mol, const dftg_basis *ba
     const size_t spline_work = 2 * (size_t)c->natoms * nlm * N;
     c->part_elems = part > spline_work ? part : spline_work;
     DFTG_TRY(dalloc(&c->d_part, c->part_elems));
-    c->red_elems = reduction_elems(c->npad, c->natoms, c->nrad, c->nang) + 64;
+    c->red_lda_off = reduction_elems(c->npad, c->natoms, c->nrad, c->nang) + 64;
+    c->red_elems = c->red_lda_off + 2 * lda_blocks(c->npad);
     DFTG_TRY(dalloc(&c->d_red, c->red_elems));
     DFTG_TRY(dalloc(&c->d_scal, scal_elems(c->natoms)));
     DFTG_CUDA(cudaMalloc(&c->d_counters, sizeof(int) * kNumCounters));
@@ -336,14 +340,44 @@ int fock_pipeline(dftg_ctx *c)
 {
     const bool fused = sgrid_route(c);
     DFTG_TRY(launch_density(c, fused));
-    // the whole build's form takes the correction factor from the P-slicing
-    // step (2 tr(P S_grid)); otherwise the per-atom sums give it
-    if (!fused) DFTG_TRY(launch_atom_sums(c, kSumsFactor));
-    // rescales rho by the correction factor; with the mixed point kernel it also
-    // sums the corrected N and writes the rho w_becke planes of the multipoles
-    DFTG_TRY(launch_xc_points(c, true, (c->prec_mask & kPrecLda) != 0));
-    c->rho_scaled = true;
-    DFTG_TRY(launch_hartree(c));
+    if (!fused) {
+        DFTG_TRY(launch_atom_sums(c, kSumsFactor));
+        // rescales rho by the correction factor; with the mixed point kernel it also
+        // sums the corrected N and writes the rho w_becke planes of the multipoles
+        DFTG_TRY(launch_xc_points(c, true, (c->prec_mask & kPrecLda) != 0));
+        c->rho_scaled = true;
+        DFTG_TRY(launch_hartree(c));
+    } else {
+        // the correction factor came from the P-slicing step (2 tr(P S_grid)) and
+        // the density epilogue applied it and wrote the rho w_becke planes, so the
+        // LDA point kernel and the Hartree steps are independent: the Hartree
+        // steps (the longer branch) run on a second stream of the greatest
+        // priority beside the point kernel (not when the phases are being timed)
+        c->rho_scaled = true;
+        const bool fork = !c->prof_on;
+        const cudaStream_t main = c->stream;
+        if (fork) {
+            if (!c->aux_stream) {
+                int least = 0, greatest = 0;
+                DFTG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+                DFTG_CUDA(cudaStreamCreateWithPriority(&c->aux_stream, cudaStreamNonBlocking, greatest));
+            }
+            if (!c->ev_fork) DFTG_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+            if (!c->ev_join) DFTG_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+            DFTG_CUDA(cudaEventRecord(c->ev_fork, main));
+            DFTG_CUDA(cudaStreamWaitEvent(c->aux_stream, c->ev_fork, 0));
+        }
+        DFTG_TRY(launch_xc_points(c, false, true, false));
+        c->rw_ready = rw_planes(c);
+        if (fork) c->stream = c->aux_stream;
+        const int rc = launch_hartree(c);
+        c->stream = main;
+        DFTG_TRY(rc);
+        if (fork) {
+            DFTG_CUDA(cudaEventRecord(c->ev_join, c->aux_stream));
+            DFTG_CUDA(cudaStreamWaitEvent(main, c->ev_join, 0));
+        }
+    }
     DFTG_TRY(launch_contract(c, true, true));
     return DFTG_OK;
 }
@@ -382,7 +416,8 @@ int fock_pipeline_graph(dftg_ctx *c)
             return rc;
         }
         if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
-        const cudaError_t ei = cudaGraphInstantiate(&c->pipe_exec, g, 0);
+        // node priorities: the Hartree branch's stream priority is kept
+        const cudaError_t ei = cudaGraphInstantiate(&c->pipe_exec, g, cudaGraphInstantiateFlagUseNodePriority);
         cudaGraphDestroy(g);
         if (ei != cudaSuccess) {
             c->pipe_exec = nullptr;
@@ -556,7 +591,8 @@ static int build_points_ctx(dftg_ctx *c, const dftg_points *pts, const dftg_mole
     const size_t part_tc = contract_tc_part_elems(c->nbf, c->npad, nsm);
     c->part_elems = part > part_tc ? part : part_tc;
     DFTG_TRY(dalloc(&c->d_part, c->part_elems));
-    c->red_elems = reduction_elems(c->npad, 1, 1, (int)std::min<size_t>(c->npts, 0x7fffffff)) + 64;
+    c->red_lda_off = reduction_elems(c->npad, 1, 1, (int)std::min<size_t>(c->npts, 0x7fffffff)) + 64;
+    c->red_elems = c->red_lda_off + 2 * lda_blocks(c->npad);
     DFTG_TRY(dalloc(&c->d_red, c->red_elems));
     DFTG_TRY(dalloc(&c->d_scal, scal_elems(c->natoms)));
     DFTG_CUDA(cudaMalloc(&c->d_counters, sizeof(int) * kNumCounters));
@@ -1436,7 +1472,7 @@ extern "C" int dftg_batch_fock_build_device(dftg_batch *b, const double *const *
             return rc;
         }
         if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
-        const cudaError_t ei = cudaGraphInstantiate(&b->exec, g, 0);
+        const cudaError_t ei = cudaGraphInstantiate(&b->exec, g, cudaGraphInstantiateFlagUseNodePriority);
         cudaGraphDestroy(g);
         if (ei != cudaSuccess) {
             b->exec = nullptr;

@@ -298,6 +298,9 @@ struct dftg_ctx {
     double *d_sgrid = nullptr;    // [nbf][nbf] S_grid = Phi^T diag(w) Phi (FP64), for the correction factor
     double *d_red = nullptr;      // reduction partials
     size_t red_elems = 0;
+    size_t red_lda_off = 0;       // the LDA point kernel's partials start here (it may run beside the Hartree steps)
+    cudaStream_t aux_stream = nullptr;          // the second branch of the whole build
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double *d_scal = nullptr;     // scalars, see kScal* below
     int *d_counters = nullptr;    // [kNumCounters] last-block counters (zero between launches)
     float *d_wsplit = nullptr;    // [4][npad] w and w_becke as FP32 hi / lo planes (mixed point kernel)
@@ -481,6 +484,13 @@ struct DensTcArgs {            // rho on the tensor cores
     const int *col_exp;
     double *rho;
     int *err;
+    // correct: rho times the correction factor scal[kScalScale] (written by the
+    // P-slicing step), and the rho w_becke hi / lo planes into rw32 when not null
+    int correct;
+    size_t npad;
+    const double *scal;
+    const float *wb2;          // [2][npad] FP32 hi / lo planes of w_becke
+    float *rw32;
 };
 struct SumsArgs {              // per-atom sums of w rho, correction factor
     size_t per_atom;
@@ -592,7 +602,8 @@ int launch_grid(dftg_ctx *c);
 int launch_amplitudes(dftg_ctx *c);
 // k_density.cu
 // fused: the whole build's form on the S_grid route (the correction factor
-// from the P-slicing step, no atom-sum pass)
+// from the P-slicing step, no atom-sum pass; the density epilogue applies it
+// and writes the rho w_becke planes)
 int launch_density(dftg_ctx *c, bool fused = false);
 enum { kSumsOnly = 0, kSumsCorrect = 1, kSumsFactor = 2 };
 // k_density_tc.cu
@@ -605,7 +616,11 @@ int launch_density_tc(dftg_ctx *c, bool fused);
 int density_tt_setup(dftg_ctx *c);
 int launch_density_tt(dftg_ctx *c);
 int launch_atom_sums(dftg_ctx *c, int mode);
-int launch_xc_points(dftg_ctx *c, bool apply_scale, bool with_n = false);
+// write_rw: the point kernel also writes the rho w_becke planes (when the
+// multipoles take them)
+int launch_xc_points(dftg_ctx *c, bool apply_scale, bool with_n = false, bool write_rw = true);
+// the rho w_becke planes exist and the multipole step takes them
+bool rw_planes(const dftg_ctx *c);
 int launch_weight_planes(dftg_ctx *c);
 // k_hartree.cu
 int hartree_setup(dftg_ctx *c);
@@ -629,6 +644,7 @@ void scf_free(dftg_ctx *c);
 int contract_setup(dftg_ctx *c);
 size_t contract_part_elems(int nbf, size_t npad);
 size_t reduction_elems(size_t npad, int natoms, int nrad, int nang);
+size_t lda_blocks(size_t npad);   // blocks of the LDA point kernel
 int launch_contract(dftg_ctx *c, bool want_xc, bool want_j);
 int launch_contract_coef(dftg_ctx *c, const double *coef, double *out);
 int launch_contract_coef32(dftg_ctx *c, const float *coef, double *out);
@@ -648,9 +664,9 @@ int ct_launch_cexp(dftg_ctx *c, int nkb, int kbpc, int nchunk, const float *cx, 
 // grouped launch of each step over all molecules (device argument arrays, one
 // queue per launch).
 StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy, bool fused);
-StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c);
+StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c, bool fused);
 StepLaunch<SumsArgs> step_atom_sums(const dftg_ctx *c, int mode);
-StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n);
+StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n, bool write_rw);
 StepLaunch<MpArgs> step_multipole(const dftg_ctx *c, bool rw_ready);
 StepLaunch<VcbArgs> step_vcross_bins(const dftg_ctx *c);
 StepLaunch<GoArgs> step_gather_own(const dftg_ctx *c, bool rho_scaled);

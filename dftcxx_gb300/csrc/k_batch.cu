@@ -85,11 +85,14 @@ int batch_plan_create(dftg_ctx *const *ctx, int n, const double *const *P, doubl
         if (!batch_group_eligible(c)) { set_error("context %d cannot join a persistent batch", i); return DFTG_ERR_STATE; }
         if (c->lmax != lmax) lmax = -1;
         s0[i] = step_slice_P(c, P[i], P[i] != c->d_P ? c->d_P : nullptr, true);
-        s1[i] = step_density_tc(c);
+        s1[i] = step_density_tc(c, true);
         s2[i] = step_atom_sums(c, kSumsFactor);
-        s3[i] = step_lda(c, true, true);
-        if (sgrid_route(c)) s2[i].blocks = 0;   // the P-slicing step writes the factor
-        s4[i] = step_multipole(c, s3[i].args.rw32 != nullptr);
+        const bool route = sgrid_route(c);
+        // on the S_grid route the P-slicing step writes the factor and the density
+        // epilogue corrects rho and writes the rho w_becke planes
+        s3[i] = route ? step_lda(c, false, true, false) : step_lda(c, true, true, true);
+        if (route) s2[i].blocks = 0;
+        s4[i] = step_multipole(c, route ? rw_planes(c) : s3[i].args.rw32 != nullptr);
         s5[i] = step_vcross_bins(c);
         s6[i] = step_gather_own(c, true);
         s7[i] = step_cexp(c, c->d_cxc32, c->d_cj32);

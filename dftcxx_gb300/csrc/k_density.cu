@@ -526,25 +526,30 @@ int launch_weight_planes(dftg_ctx *c)
     return DFTG_OK;
 }
 
-StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n)
+bool rw_planes(const dftg_ctx *c) { return c->d_rw32 && (c->prec_mask & kPrecMultipole); }
+
+StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n, bool write_rw)
 {
     // with_n: the build's N from the corrected rho (no per-atom sums ran), and
-    // the rho w_becke planes for the mixed multipole kernel
-    float *rw32 = (with_n && c->d_rw32 && (c->prec_mask & kPrecMultipole)) ? c->d_rw32 : nullptr;
+    // (write_rw) the rho w_becke planes for the mixed multipole kernel
+    float *rw32 = (with_n && write_rw && rw_planes(c)) ? c->d_rw32 : nullptr;
     const bool mixed = (c->prec_mask & kPrecLda) != 0;
     StepLaunch<LdaArgs> s;
     s.args = LdaArgs{c->npad, c->d_rho, c->d_w, c->d_scal, apply_scale ? 1 : 0,
                      mixed ? ((c->prec_mask & kPrecContract) && c->ct_ready ? 0 : 1) : 1, mixed && with_n ? 1 : 0,
-                     c->d_cxc, c->d_cxc32, c->d_red, c->d_counters + kCntLda, mixed ? c->d_wb : nullptr,
+                     c->d_cxc, c->d_cxc32, c->d_red + c->red_lda_off, c->d_counters + kCntLda, mixed ? c->d_wb : nullptr,
                      mixed ? rw32 : nullptr, c->d_wsplit, c->d_wsplit + 2 * c->npad};
     s.blocks = (int)((c->npad + kRedBlock - 1) / kRedBlock);
     return s;
 }
 
-int launch_xc_points(dftg_ctx *c, bool apply_scale, bool with_n)
+int launch_xc_points(dftg_ctx *c, bool apply_scale, bool with_n, bool write_rw)
 {
-    const StepLaunch<LdaArgs> st = step_lda(c, apply_scale, with_n);
-    if (2 * (size_t)st.blocks > c->red_elems) { set_error("reduction buffer too small for %d blocks", st.blocks); return DFTG_ERR_STATE; }
+    const StepLaunch<LdaArgs> st = step_lda(c, apply_scale, with_n, write_rw);
+    if (c->red_lda_off + 2 * (size_t)st.blocks > c->red_elems) {
+        set_error("reduction buffer too small for %d blocks", st.blocks);
+        return DFTG_ERR_STATE;
+    }
     c->rw_ready = st.args.rw32 != nullptr;
     if (c->prec_mask & kPrecLda) k_lda<true><<<st.blocks, kRedBlock, 0, c->stream>>>(st.args);
     else k_lda<false><<<st.blocks, kRedBlock, 0, c->stream>>>(st.args);
@@ -570,6 +575,8 @@ int group_sums_lda(const SumsArgs *d_sums, const GroupQueue &qs, const LdaArgs *
 // E_J: one), one per
 // stage-1 chunk of the per-atom sums, two per CTA of the fused density + LDA
 // pass (at most one CTA per SM; kMaxRedCtas bounds the SM count)
+size_t lda_blocks(size_t npad) { return (npad + kRedBlock - 1) / kRedBlock; }
+
 size_t reduction_elems(size_t npad, int natoms, int nrad, int nang)
 {
     size_t a = (npad + kRedBlock - 1) / kRedBlock;

@@ -206,16 +206,28 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
         const int half = ((warp - 2) >> 2) & 1; // 8-column groups 8 half, 8 half + 16, ...
         const int r = q * 32 + lane;            // row of the tile = TMEM lane
         const int kc = KP / 8;
+        const double cf = args.correct ? __ldcg(args.scal + kScalScale) : 1.0;
         for (int it = eg; it < my_tiles; it += 2) {
             const int s = it % kTcStages;
             const int nb = it >> 1;
+            const int tile = vb + it * nvb;
+            const size_t p = (size_t)tile * kTcTile + r;
+            // the point's exponent and w_becke planes, loaded now and used at the
+            // tile's end (their latency hidden behind the column loop)
+            int ep = 0;
+            float wbh = 0.f, wbl = 0.f;
+            if (half == 0) {
+                ep = row_exp[p];
+                if (args.rw32) {
+                    wbh = args.wb2[p];
+                    wbl = args.wb2[args.npad + p];
+                }
+            }
             bool ok = mbar_wait(&sh->tmem_full[eg], (uint32_t)(nb & 1));
             if (!ok) { atomicExch(err, 4); s_fail = 1; }
             epi_group_bar(eg);
             if (s_fail) break;
             tc_fence_after();
-            const int tile = vb + it * nvb;
-            const size_t p = (size_t)tile * kTcTile + r;
             const unsigned char *a0 = sA + (size_t)s * a_stage_bytes;
             const uint32_t ta0 = tmem + (uint32_t)(eg * 256) + ((uint32_t)(q * 32) << 16);
             // two independent compensated accumulators (even / odd columns), the
@@ -286,8 +298,18 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
                 const float w = St + o.x;
                 const float bq = w - St;
                 const float e = Et + o.y + (St - (w - bq)) + (o.x - bq);
-                const int ep = row_exp[p];
-                rho[p] = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
+                double rv = 2.0 * ((double)w + (double)e) * ldexp(1.0, 2 * ep);
+                if (args.correct) {
+                    // the density correction, and rho w_becke for the multipoles
+                    // (the point kernel's arithmetic)
+                    rv *= cf;
+                    if (args.rw32) {
+                        const dfl x = df_mul(df_from_bits(rv), dfl{wbh, wbl});
+                        args.rw32[p] = x.h;
+                        args.rw32[args.npad + p] = x.l;
+                    }
+                }
+                rho[p] = rv;
             }
         }
     }
@@ -644,12 +666,15 @@ StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *
     return s;
 }
 
-StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c)
+StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c, bool fused)
 {
     StepLaunch<DensTcArgs> s;
+    const bool correct = fused && sgrid_route(c);
     s.args = DensTcArgs{c->nbf, c->tc_KP, c->tc_NP, (int)(c->npad / kTcTile),
                         reinterpret_cast<const unsigned char *>(c->d_tcA), c->d_tc_rowexp,
-                        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag};
+                        reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag,
+                        correct ? 1 : 0, c->npad, c->d_scal, c->d_wsplit + 2 * c->npad,
+                        correct && rw_planes(c) ? c->d_rw32 : nullptr};
     s.blocks = c->tc_grid;
     s.smem = density_tc_smem(c->tc_KP, c->tc_NP);
     return s;
@@ -661,7 +686,7 @@ int launch_density_tc(dftg_ctx *c, bool fused)
     k_slice_P<<<sp.blocks, kSlicePThreads, 0, c->stream>>>(sp.args);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "density_slices");
-    const StepLaunch<DensTcArgs> dn = step_density_tc(c);
+    const StepLaunch<DensTcArgs> dn = step_density_tc(c, fused);
     k_density_tc<<<dn.blocks, kTcThreads, dn.smem, c->stream>>>(dn.args);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
