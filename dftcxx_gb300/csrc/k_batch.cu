@@ -13,7 +13,9 @@
 //   from 2 tr(P S_grid)), density (tensor cores), LDA point kernel (with the
 //   correction), multipole chain, cross-atom bins, potential gather + E_J,
 //   coefficient bounds, XC / J contraction (tensor cores), partial reduction
-//   (which also writes the caller's output buffers and scalars).
+//   (which also writes the caller's output buffers and scalars).  The point
+//   kernel and the three Hartree launches are independent and run on two
+//   branches (the Hartree ones on a stream of the greatest priority).
 // The point-kernel launch also takes per-atom sum items for molecules without
 // S_grid; their point blocks wait (bounded) for the molecule's factor.  Every
 // context a batch accepts has S_grid, so no block waits but in the self-test of
@@ -48,6 +50,9 @@ struct BatchPlan {
     GroupQueue q[kNumSteps];
     size_t smem[kNumSteps] = {};
     const void *args[kNumSteps] = {};
+    // the Hartree steps' branch (greatest priority) beside the point-kernel launch
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 bool batch_group_eligible(const dftg_ctx *c)
@@ -60,6 +65,9 @@ void batch_plan_free(BatchPlan *bp)
 {
     if (!bp) return;
     if (bp->d_mem) cudaFree(bp->d_mem);
+    if (bp->aux) cudaStreamDestroy(bp->aux);
+    if (bp->ev_fork) cudaEventDestroy(bp->ev_fork);
+    if (bp->ev_join) cudaEventDestroy(bp->ev_join);
     delete bp;
 }
 
@@ -128,6 +136,11 @@ int batch_plan_create(dftg_ctx *const *ctx, int n, const double *const *P, doubl
     bp->lmax = lmax;
     cudaError_t e = cudaDeviceGetAttribute(&bp->nsm, cudaDevAttrMultiProcessorCount, bp->device);
     if (e == cudaSuccess) e = cudaMalloc(&bp->d_mem, total);
+    int least = 0, greatest = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&bp->aux, cudaStreamNonBlocking, greatest);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bp->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bp->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         batch_plan_free(bp);
         return cuda_fail(e, "batch plan", __FILE__, __LINE__);
@@ -205,16 +218,29 @@ int batch_plan_enqueue(const BatchPlan *bp, cudaStream_t st, int stall_mol, unsi
     DFTG_TRY_L(group_slice_P(static_cast<const SlicePArgs *>(bp->args[kStSliceP]), bp->q[kStSliceP], nsm, st));
     DFTG_TRY_L(group_density_tc(static_cast<const DensTcArgs *>(bp->args[kStDensity]), bp->q[kStDensity],
                                 bp->smem[kStDensity], dev, nsm, st));
+    // with no atom-sum items the point kernel and the Hartree steps are
+    // independent (the density launch corrected rho and wrote the rho w_becke
+    // planes): the Hartree steps run on the greatest-priority branch beside it
+    const bool fork = bp->q[kStSums].nitems == 0;
+    const cudaStream_t sh = fork ? bp->aux : st;
+    if (fork) {
+        DFTG_CUDA(cudaEventRecord(bp->ev_fork, st));
+        DFTG_CUDA(cudaStreamWaitEvent(bp->aux, bp->ev_fork, 0));
+    }
     if (bp->q[kStSums].nitems + bp->q[kStLda].nitems > 0)
         DFTG_TRY_L(group_sums_lda(static_cast<const SumsArgs *>(bp->args[kStSums]), bp->q[kStSums],
                                   static_cast<const LdaArgs *>(bp->args[kStLda]), bp->q[kStLda], ctl, nsm, st));
     DFTG_TRY_L(group_multipole(static_cast<const MpArgs *>(bp->args[kStMultipole]), bp->q[kStMultipole],
-                               bp->smem[kStMultipole], dev, nsm, st));
+                               bp->smem[kStMultipole], dev, nsm, sh));
     if (bp->q[kStVcb].nitems > 0)
         DFTG_TRY_L(group_vcross_bins(static_cast<const VcbArgs *>(bp->args[kStVcb]), bp->q[kStVcb], bp->lmax,
-                                     bp->smem[kStVcb], nsm, st));
+                                     bp->smem[kStVcb], nsm, sh));
     DFTG_TRY_L(group_gather_own(static_cast<const GoArgs *>(bp->args[kStGather]), bp->q[kStGather],
-                                bp->smem[kStGather], dev, nsm, st));
+                                bp->smem[kStGather], dev, nsm, sh));
+    if (fork) {
+        DFTG_CUDA(cudaEventRecord(bp->ev_join, bp->aux));
+        DFTG_CUDA(cudaStreamWaitEvent(st, bp->ev_join, 0));
+    }
     DFTG_TRY_L(group_cexp(static_cast<const CexpArgs *>(bp->args[kStCexp]), bp->q[kStCexp], nsm, st));
     DFTG_TRY_L(group_contract_tc(static_cast<const CtArgs *>(bp->args[kStContract]), bp->q[kStContract],
                                  bp->smem[kStContract], dev, nsm, st));
