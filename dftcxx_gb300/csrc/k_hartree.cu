@@ -682,19 +682,17 @@ __device__ __forceinline__ dfl mp_matvec(const float *__restrict__ Mh, const flo
     return df_add(df_add(df_norm(s0, e0), df_norm(s1, e1)), df_add(df_norm(s2, e2), df_norm(s3, e3)));
 }
 
-// n floats global -> shared with eight loads in flight per thread
+// n floats global -> shared as asynchronous 4-byte copies, all in flight at
+// once (no register staging); complete after mp_copy_wait
 __device__ __forceinline__ void mp_copy(float *__restrict__ dst, const float *__restrict__ src, int n)
 {
-    int e = threadIdx.x;
-    for (; e + 7 * kMpThreads < n; e += 8 * kMpThreads) {
-        float v[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = src[e + u * kMpThreads];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) dst[e + u * kMpThreads] = v[u];
-    }
-    for (; e < n; e += kMpThreads) dst[e] = src[e];
+    for (int e = threadIdx.x; e < n; e += kMpThreads)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + e)),
+                     "l"(src + e)
+                     : "memory");
 }
+// this thread's copies landed (then a __syncthreads for the others')
+__device__ __forceinline__ void mp_copy_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 __device__ __forceinline__ void multipole_block(const MpArgs A, int vb)
 {
@@ -755,11 +753,14 @@ __device__ __forceinline__ void multipole_block(const MpArgs A, int vb)
     for (int i0 = 0; i0 < N; i0 += kMpSC) {
         const int ns = min(kMpSC, N - i0);
         __syncthreads();                                          // the previous pass is done with sRW
-        // a thread per antipodal pair (j, a), eight shells' loads in flight: the
-        // even and odd combinations rho w(j) +- rho w(a) (Y_lm(a) = (-1)^l Y_lm(j))
-        for (int k = tid; k < npair; k += kMpThreads) {
+        // a thread per (antipodal pair (j, a), eight shells), the shells' loads in
+        // flight: the even and odd combinations rho w(j) +- rho w(a)
+        // (Y_lm(a) = (-1)^l Y_lm(j))
+        const int nb8 = (ns + 7) / 8;
+        for (int item = tid; item < npair * nb8; item += kMpThreads) {
+            const int k = item % npair, ii0 = (item / npair) * 8;
             const int2 ja = __ldg(&pairs[k]);
-            for (int ii0 = 0; ii0 < ns; ii0 += 8) {
+            {
                 dfl v[8], w[8];
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
@@ -821,6 +822,7 @@ __device__ __forceinline__ void multipole_block(const MpArgs A, int vb)
             __syncthreads();                                      // sMap free (rho w planes or the previous l)
             mp_copy(sMap, Gh, N * N);
             mp_copy(sMap + (size_t)N * N, Gl, N * N);
+            mp_copy_wait();
             __syncthreads();
             Gh = sMap;
             Gl = sMap + (size_t)N * N;
@@ -847,6 +849,7 @@ __device__ __forceinline__ void multipole_block(const MpArgs A, int vb)
     if (stage_maps) {
         mp_copy(sMap, Kh, N * N);
         mp_copy(sMap + (size_t)N * N, Kl, N * N);
+        mp_copy_wait();
         __syncthreads();
         Kh = sMap;
         Kl = sMap + (size_t)N * N;
