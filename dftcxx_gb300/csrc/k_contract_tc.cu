@@ -667,30 +667,13 @@ __device__ __forceinline__ void contract_tc_reduce_block(const RedArgs A, int vb
     if (vb == 0 && A.sc && threadIdx.x < 3)                  // the build's E_xc, N, E_J
         A.sc[threadIdx.x] = A.scal[threadIdx.x == 0 ? kScalExc : (threadIdx.x == 1 ? kScalNelec : kScalEJ)];
     dfl sx{0.f, 0.f}, sj{0.f, 0.f};
-    if (act) {
-        // partials g, g + 32, ... in order, four partials' loads in flight at a time
-        int c = g;
-        for (; c + 96 < nparts; c += 128) {
-            float2 a[4], b[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const float2 *p = part + (size_t)(c + 32 * u) * 2 * ntri;
-                a[u] = p[t];
-                b[u] = p[ntri + t];
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                sx = df_add(sx, dfl{a[u].x, a[u].y});
-                sj = df_add(sj, dfl{b[u].x, b[u].y});
-            }
-        }
-        for (; c < nparts; c += 32) {
+    if (act)
+        for (int c = g; c < nparts; c += 32) {
             const float2 *p = part + (size_t)c * 2 * ntri;
             const float2 a = p[t], b = p[ntri + t];
             sx = df_add(sx, dfl{a.x, a.y});
             sj = df_add(sj, dfl{b.x, b.y});
         }
-    }
     shx[g][lx] = make_float2(sx.h, sx.l);
     shj[g][lx] = make_float2(sj.h, sj.l);
     __syncthreads();

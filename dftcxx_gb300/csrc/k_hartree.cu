@@ -720,7 +720,17 @@ __device__ __forceinline__ void multipole_block(const MpArgs A, int vb)
     double *sred = reinterpret_cast<double *>(sD + (size_t)kMpLG * N);
     const int tid = threadIdx.x;
     const int al = vb / ngroup, g = vb % ngroup, a = cell0 + al;
-    const int lm0 = g * kMpLG, nl = min(kMpLG, nlm - lm0);
+    // group g: rows lm0 .. lm0 + nl - 1 of one degree l (at most kMpLG of them)
+    int lm0 = 0, nl = 0;
+    for (int l = 0, gg = g; l <= lmax; ++l) {
+        const int nrow = 2 * l + 1, ngl = (nrow + kMpLG - 1) / kMpLG;
+        if (gg < ngl) {
+            lm0 = l * l + gg * kMpLG;
+            nl = min(kMpLG, nrow - gg * kMpLG);
+            break;
+        }
+        gg -= ngl;
+    }
     const size_t base = (size_t)al * N * nang;
     const size_t uhalf = (size_t)natoms * nlm * N;
     // w_leb Y_lm at the first direction of every antipodal pair: [row][pair]
@@ -1529,7 +1539,8 @@ int group_vcross_bins(const VcbArgs *d_args, const GroupQueue &q, int lmax, size
 
 StepLaunch<MpArgs> step_multipole(const dftg_ctx *c, bool rw_ready)
 {
-    const int ngroup = (c->nlm + kMpLG - 1) / kMpLG;
+    int ngroup = 0;                          // groups of at most kMpLG rows of one degree l
+    for (int l = 0; l <= c->lmax; ++l) ngroup += (2 * l + 1 + kMpLG - 1) / kMpLG;
     StepLaunch<MpArgs> s;
     s.args = MpArgs{c->natoms, c->cell0, c->nrad, c->nang, c->lmax, ngroup, (c->prec_mask & kPrecCross) ? 0 : 1,
                     rw_ready ? c->d_rw32 : nullptr, c->npad, c->d_rho, c->d_wb, c->d_w, c->d_Ywt32, c->d_maps32,
