@@ -81,7 +81,7 @@ static void free_ctx(dftg_ctx *c)
                     c->d_rec32, c->d_rholm, c->d_U, c->d_U32, c->d_Y32, c->d_Ywt32, c->d_fold, c->d_Gt,
                     c->d_Gb, c->d_Kt, c->d_sx, c->d_splf, c->d_spl, c->d_splm, c->d_tiles,
                     c->d_ints_work, c->d_tcA, c->d_tcB, c->d_tc_rowexp, c->d_tc_colexp, c->d_sgrid, c->d_rw32, c->d_wsplit, c->d_lebpair, c->d_flag,
-                    c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_counters, c->d_invr, c->d_maps32, c->d_U32T,
+                    c->d_pairs, c->d_pairpos, c->d_pairv, c->d_cross_tasks, c->d_ct_rowexp, c->d_ct_A, c->d_ct_winv, c->d_ct_cmax, c->d_counters, c->d_invr, c->d_maps32, c->d_U32T,
                     c->d_bw_pt, c->d_bw_lm, c->d_bw_fpart, c->d_bw_out, c->d_bw_counter, c->d_bw_pairp,
                     c->d_bw_binfirst, c->d_bw_cpart, c->d_bw_geo, c->d_bw_geo64, c->d_bw_prim32,
                     c->d_tt_exp, c->d_tt_winv, c->d_tt_A, c->d_tt_B, c->d_tt_part,
@@ -338,6 +338,12 @@ int sync_scalars(dftg_ctx *c)
 // device part of one Fock build; P already in c->d_P
 int fock_pipeline(dftg_ctx *c)
 {
+    // the steps made inside take the whole build's forms (cmax_route)
+    struct WholeBuild {
+        dftg_ctx *c;
+        ~WholeBuild() { c->whole_build = false; }
+    } whole{c};
+    c->whole_build = true;
     const bool fused = sgrid_route(c);
     DFTG_TRY(launch_density(c, fused));
     if (!fused) {

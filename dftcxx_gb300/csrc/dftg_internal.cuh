@@ -46,6 +46,18 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &e, float x)
     s = t;
 }
 
+// Fold the maximum of non-negative v over the lanes of a warp that share a
+// chunk into cmax[chunk], one atomicMax per (warp, chunk): the IEEE bits of
+// non-negative floats order like their values, and a maximum is exact and
+// independent of order.  Every lane of the warp calls it; chunk < 0 for a lane
+// without a value.
+__device__ __forceinline__ void warp_chunk_max(unsigned *cmax, int chunk, float v)
+{
+    const unsigned grp = __match_any_sync(0xffffffffu, chunk);
+    const unsigned m = __reduce_max_sync(grp, __float_as_uint(v));
+    if (chunk >= 0 && (int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(cmax + chunk, m);
+}
+
 // Packed FP32 pairs: one instruction for two independent lanes, each rounded to
 // nearest exactly as the scalar operation (and, being explicit roundings, never
 // contracted into an FMA, so error-free transformations keep their meaning).
@@ -300,6 +312,8 @@ struct dftg_ctx {
     size_t red_elems = 0;
     size_t red_lda_off = 0;       // the LDA point kernel's partials start here (it may run beside the Hartree steps)
     cudaStream_t aux_stream = nullptr;          // the second branch of the whole build
+    bool whole_build = false;     // set while the whole build's launches (or a batch's records) are made
+    unsigned *d_ct_cmax = nullptr;   // [2][nchunk] max |c / w| bits per contraction chunk (XC, J), zero between builds
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double *d_scal = nullptr;     // scalars, see kScal* below
     int *d_counters = nullptr;    // [kNumCounters] last-block counters (zero between launches)
@@ -515,6 +529,11 @@ struct LdaArgs {               // LDA point kernel
     const double *wb;
     float *rw32;
     const float *w2, *wb2;     // w and w_becke as FP32 hi / lo planes [2][npad] (mixed kernel)
+    // when cmax is not null: max |cxc32 / w| per contraction chunk of chunk_pts
+    // points into cmax (the contraction's coefficient bounds, no separate pass)
+    unsigned *cmax;
+    const float *winv;
+    int chunk_pts;
 };
 struct MpArgs {                // multipole chain of one atom cell per (cell, l group)
     int natoms, cell0, N, nang, lmax, ngroup, want64;
@@ -550,6 +569,9 @@ struct GoArgs {                // own-cell potential + pair sums per point, cj, 
     int *counter;
     const int2 *pairs;         // [npair] Lebedev directions (j, antipode of j)
     int npair;
+    unsigned *cmax;            // max |cj32 / w| per contraction chunk, or null
+    const float *winv;
+    int chunk_pts;
 };
 struct CexpArgs {              // per-chunk exponent bounds of the point coefficients
     int nkb, kbpc;
@@ -564,6 +586,7 @@ struct CtArgs {                // XC and J contraction on the tensor cores
     const float *cxc, *cj;
     float2 *part;
     int *err;
+    const unsigned *cmax;      // when not null: [2][nchunk] max |c / w| bits (the bounds' source instead of cexp)
 };
 struct SumsLdaCtl {            // the batch's fused atom-sum + point-kernel launch
     int *head;                 // one queue over both item ranges
@@ -586,6 +609,8 @@ struct RedArgs {               // sum of the contraction partials, symmetric XC 
     double *XC2, *J2;          // second copies (a batch's output buffers), or null
     const double *scal;        // with sc: copy E_xc, N, E_J to sc[0..2] (block 0)
     double *sc;
+    unsigned *cmax;            // when not null: block 0 clears [ncmax] for the next build
+    int ncmax;
 };
 
 // Raise a kernel's dynamic shared-memory limit to the device maximum (minus
@@ -611,6 +636,9 @@ int density_tc_setup(dftg_ctx *c);
 // the mixed build takes the density correction's total from 2 tr(P S_grid)
 // in the P-slicing step (no atom-sum pass)
 bool sgrid_route(const dftg_ctx *c);
+// the whole mixed build takes the contraction's coefficient bounds from the
+// point kernel and the potential gather (atomic chunk maxima), no bounds pass
+bool cmax_route(const dftg_ctx *c);
 int launch_density_tc(dftg_ctx *c, bool fused);
 // k_density_tt.cu
 int density_tt_setup(dftg_ctx *c);

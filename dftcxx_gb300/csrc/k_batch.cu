@@ -89,6 +89,12 @@ int batch_plan_create(dftg_ctx *const *ctx, int n, const double *const *P, doubl
     std::vector<StepLaunch<RedArgs>> s9(n);
     int lmax = ctx[0]->lmax;
     for (int i = 0; i < n; ++i) {
+        // the launch records take the whole build's forms (cmax_route)
+        struct WholeBuild {
+            dftg_ctx *c;
+            ~WholeBuild() { c->whole_build = false; }
+        } whole{ctx[i]};
+        ctx[i]->whole_build = true;
         const dftg_ctx *c = ctx[i];
         if (!batch_group_eligible(c)) { set_error("context %d cannot join a persistent batch", i); return DFTG_ERR_STATE; }
         if (c->lmax != lmax) lmax = -1;
@@ -104,6 +110,7 @@ int batch_plan_create(dftg_ctx *const *ctx, int n, const double *const *P, doubl
         s5[i] = step_vcross_bins(c);
         s6[i] = step_gather_own(c, true);
         s7[i] = step_cexp(c, c->d_cxc32, c->d_cj32);
+        if (cmax_route(c)) s7[i].blocks = 0;   // the point kernel and the gather keep the chunk maxima
         s8[i] = step_contract_tc(c, c->d_cxc32, c->d_cj32);
         s9[i] = step_contract_reduce(c, true, true, c->d_XC, c->d_J);
         s9[i].args.XC2 = (XC && XC[i] && XC[i] != c->d_XC) ? XC[i] : nullptr;

@@ -202,6 +202,12 @@ __device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb
     const unsigned char *__restrict__ aslices = A.aslices;
     const int *__restrict__ rowexp = A.rowexp, *__restrict__ swexp = A.swexp;
     const int2 *__restrict__ cexp = A.cexp;
+    const unsigned *__restrict__ cmax = A.cmax;
+    // exponent bounds of max |c_xc / w| and max |c_j / w| over chunk ch: from the
+    // bounds pass, or from the chunk maxima the point kernel and the gather kept
+    auto chunk_bounds = [&](int ch) {
+        return cmax ? make_int2(exp_bound(cmax[ch]), exp_bound(cmax[nchunk + ch])) : cexp[ch];
+    };
     const float *__restrict__ cxc = A.cxc, *__restrict__ cj = A.cj;
     float2 *__restrict__ part = A.part;
     int *__restrict__ err = A.err;
@@ -255,7 +261,7 @@ __device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb
         bool ok = true;
         for (int ch = (G ? vb_ : (int)blockIdx.x); ch < nchunk && ok; ch += (G ? nvb_ : (int)gridDim.x)) {
             const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
-            const int2 ce = cexp[ch];
+            const int2 ce = chunk_bounds(ch);
             const float sx = pow2f(-ce.x), sj = pow2f(-ce.y);
             // B row scales of this lane's rows for the chunk, in registers
             float rfr[kCtRowSteps];
@@ -405,7 +411,7 @@ __device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb
             const int kb0 = ch * kb_per_chunk, kb1 = min(nkb, kb0 + kb_per_chunk);
             // column scales 2^(s_nu + v - 14) of the chunk in shared memory, row scale 2^e_mu in a register
             {
-                const int2 ce = cexp[ch];
+                const int2 ce = chunk_bounds(ch);
                 const int *es = swexp + (size_t)ch * nbf;
                 for (int n = threadIdx.x - 32 * kCtEpi0; n < 2 * nbf; n += 32 * kCtEpiWarps) {
                     const int nu = n < nbf ? n : n - nbf;
@@ -666,6 +672,8 @@ __device__ __forceinline__ void contract_tc_reduce_block(const RedArgs A, int vb
     const size_t t = (size_t)nu * (nu + 1) / 2 + mu;        // packed upper-triangle index
     if (vb == 0 && A.sc && threadIdx.x < 3)                  // the build's E_xc, N, E_J
         A.sc[threadIdx.x] = A.scal[threadIdx.x == 0 ? kScalExc : (threadIdx.x == 1 ? kScalNelec : kScalEJ)];
+    if (vb == 0 && A.cmax)                                   // chunk maxima start from zero next build
+        for (int i = threadIdx.x; i < A.ncmax; i += blockDim.x) A.cmax[i] = 0u;
     dfl sx{0.f, 0.f}, sj{0.f, 0.f};
     if (act)
         for (int c = g; c < nparts; c += 32) {
@@ -785,6 +793,8 @@ int contract_tc_setup(dftg_ctx *c)
     k_ct_slice_A<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
         c->nbf, AR, c->npad, nkb, kbpc, c->d_phi32, c->d_ct_rowexp, reinterpret_cast<__nv_bfloat16 *>(c->d_ct_A));
     DFTG_LAUNCH_CHECK();
+    DFTG_CUDA(cudaMalloc(&c->d_ct_cmax, sizeof(unsigned) * 2 * (size_t)nchunk));
+    DFTG_CUDA(cudaMemsetAsync(c->d_ct_cmax, 0, sizeof(unsigned) * 2 * (size_t)nchunk, c->stream));
     c->ct_NP = NP;
     c->ct_AR = AR;
     c->ct_nst = nst;
@@ -821,7 +831,8 @@ StepLaunch<CtArgs> step_contract_tc(const dftg_ctx *c, const float *cx, const fl
                     reinterpret_cast<const unsigned char *>(c->d_ct_A), c->d_ct_rowexp,
                     c->d_ct_rowexp + (size_t)c->ct_nchunk * c->nbf,
                     reinterpret_cast<const int2 *>(c->d_ct_rowexp + 2 * (size_t)c->ct_nchunk * c->nbf), cx, cy,
-                    reinterpret_cast<float2 *>(c->d_part), c->d_flag};
+                    reinterpret_cast<float2 *>(c->d_part), c->d_flag,
+                    cmax_route(c) && cx == c->d_cxc32 && cy == c->d_cj32 ? c->d_ct_cmax : nullptr};
     s.blocks = c->ct_grid;
     s.smem = ct_smem(c->ct_nst, c->ct_NP, c->ct_AR, c->nbf, c->ct_spart != 0);
     return s;
@@ -831,7 +842,8 @@ StepLaunch<RedArgs> step_contract_reduce(const dftg_ctx *c, bool want_xc, bool w
 {
     StepLaunch<RedArgs> s;
     s.args = RedArgs{c->nbf, c->ct_grid, want_xc ? 1 : 0, want_j ? 1 : 0, reinterpret_cast<const float2 *>(c->d_part),
-                     XC, J, nullptr, nullptr, c->d_scal, nullptr};
+                     XC, J, nullptr, nullptr, c->d_scal, nullptr, cmax_route(c) ? c->d_ct_cmax : nullptr,
+                     2 * c->ct_nchunk};
     s.blocks = (int)(((size_t)c->nbf * c->nbf + 31) / 32);
     return s;
 }
@@ -840,11 +852,13 @@ StepLaunch<RedArgs> step_contract_reduce(const dftg_ctx *c, bool want_xc, bool w
 // cores for any pair of FP32 point-coefficient arrays
 int launch_contract_tc_on(dftg_ctx *c, const float *cxc32, const float *cj32)
 {
-    const StepLaunch<CexpArgs> ce = step_cexp(c, cxc32, cj32);
-    k_ct_cexp<<<ce.blocks, kCexpThreads, 0, c->stream>>>(ce.args);
-    DFTG_LAUNCH_CHECK();
-    DFTG_MARK(c, "contract_bounds");
     const StepLaunch<CtArgs> ct = step_contract_tc(c, cxc32, cj32);
+    if (!ct.args.cmax) {                 // the bounds pass (the whole build keeps chunk maxima instead)
+        const StepLaunch<CexpArgs> ce = step_cexp(c, cxc32, cj32);
+        k_ct_cexp<<<ce.blocks, kCexpThreads, 0, c->stream>>>(ce.args);
+        DFTG_LAUNCH_CHECK();
+        DFTG_MARK(c, "contract_bounds");
+    }
     k_contract_tc<<<ct.blocks, kCtThreads, ct.smem, c->stream>>>(ct.args);
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;

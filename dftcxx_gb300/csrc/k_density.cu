@@ -312,6 +312,7 @@ __device__ __forceinline__ void lda_block(const LdaArgs A, int vb, int nvb)
         // split into FP32 hi / lo with integer operations, w and w_becke come as
         // FP32 hi / lo planes made at set-up
         dfl ewd{0.f, 0.f}, wrd{0.f, 0.f};
+        float cbound = 0.f;                // |cxc32 / w| for the contraction's chunk bound
         if (p < npad) {
             double r = rho[p];
             if (apply_scale) {
@@ -324,7 +325,9 @@ __device__ __forceinline__ void lda_block(const LdaArgs A, int vb, int nvb)
             lda_point_df(rd, e, v);
             const dfl wd{A.w2[p], A.w2[npad + p]};
             ewd = df_mul(wd, e);
-            cxc32[p] = (wd.h + wd.l) * v;
+            const float cv = (wd.h + wd.l) * v;
+            cxc32[p] = cv;
+            if (A.cmax) cbound = fabsf(cv) * A.winv[p];
             if (want64) cxc[p] = w[p] * (double)v;
             wrd = df_mul(wd, rd);
             if (rw32) {
@@ -333,6 +336,7 @@ __device__ __forceinline__ void lda_block(const LdaArgs A, int vb, int nvb)
                 rw32[npad + p] = x.l;
             }
         }
+        if (A.cmax) warp_chunk_max(A.cmax, p < npad ? (int)(p / A.chunk_pts) : -1, cbound);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             ewd = df_add(ewd, dfl{__shfl_xor_sync(0xffffffffu, ewd.h, o), __shfl_xor_sync(0xffffffffu, ewd.l, o)});
@@ -538,7 +542,8 @@ StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n, b
     s.args = LdaArgs{c->npad, c->d_rho, c->d_w, c->d_scal, apply_scale ? 1 : 0,
                      mixed ? ((c->prec_mask & kPrecContract) && c->ct_ready ? 0 : 1) : 1, mixed && with_n ? 1 : 0,
                      c->d_cxc, c->d_cxc32, c->d_red + c->red_lda_off, c->d_counters + kCntLda, mixed ? c->d_wb : nullptr,
-                     mixed ? rw32 : nullptr, c->d_wsplit, c->d_wsplit + 2 * c->npad};
+                     mixed ? rw32 : nullptr, c->d_wsplit, c->d_wsplit + 2 * c->npad,
+                     mixed && cmax_route(c) ? c->d_ct_cmax : nullptr, c->d_ct_winv, c->ct_kbpc * 32};
     s.blocks = (int)((c->npad + kRedBlock - 1) / kRedBlock);
     return s;
 }

@@ -604,6 +604,11 @@ __global__ void k_sgrid_sum(int nbf, int nblk, const double *__restrict__ part, 
     S[(size_t)nu * nbf + mu] = t;
 }
 
+bool cmax_route(const dftg_ctx *c)
+{
+    return c->whole_build && c->d_ct_cmax && batch_group_eligible(c) && sgrid_route(c);
+}
+
 bool sgrid_route(const dftg_ctx *c)
 {
     return c->d_sgrid && c->tc_ready && !c->points_only && c->cell0 == 0 && c->ncell == c->natoms &&

@@ -1243,38 +1243,50 @@ __device__ __forceinline__ void gather_own_block(const GoArgs A, int b, int nblk
                 if (lm < lm1) df_mac(s0, e0, uh[lm], ul[lm], syh[lm * kGoSlab + lane], syl[lm * kGoSlab + lane]);
             }
         }
-        if (k >= npair) continue;
-        const dfl ev = df_add(df_norm(s0, e0), df_norm(s1, e1)), od = df_add(df_norm(s2, e2), df_norm(s3, e3));
-        // the pair's two points: V_own = even + odd at j, even - odd at its antipode
+        float cbound[2] = {0.f, 0.f};      // |cj32 / w| of the pair's points (chunk bounds)
+        int cchunk[2] = {-1, -1};
+        if (k < npair) {
+            const dfl ev = df_add(df_norm(s0, e0), df_norm(s1, e1)), od = df_add(df_norm(s2, e2), df_norm(s3, e3));
+            // the pair's two points: V_own = even + odd at j, even - odd at its antipode
 #pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            const size_t p = ((size_t)al * nrad + i) * nang + (t ? ja.y : ja.x);
-            const dfl vs = t ? df_sub(ev, od) : df_add(ev, od);
-            const double vown = df_to(vs) * invr[p];
-            float vh = 0.f, vl = 0.f;
-            const int *pp = pos + p * natoms;
-            // eight atoms at a time: their places, then their contributions, then
-            // the sum in atom order
-            for (int q0 = 0; q0 < natoms; q0 += 8) {
-                int q[8];
+            for (int t = 0; t < 2; ++t) {
+                const size_t p = ((size_t)al * nrad + i) * nang + (t ? ja.y : ja.x);
+                const dfl vs = t ? df_sub(ev, od) : df_add(ev, od);
+                const double vown = df_to(vs) * invr[p];
+                float vh = 0.f, vl = 0.f;
+                const int *pp = pos + p * natoms;
+                // eight atoms at a time: their places, then their contributions, then
+                // the sum in atom order
+                for (int q0 = 0; q0 < natoms; q0 += 8) {
+                    int q[8];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) q[u] = (q0 + u < natoms && q0 + u != a) ? pp[q0 + u] : -1;
-                float2 v[8];
+                    for (int u = 0; u < 8; ++u) q[u] = (q0 + u < natoms && q0 + u != a) ? pp[q0 + u] : -1;
+                    float2 v[8];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) v[u] = q[u] >= 0 ? pairv[q[u]] : make_float2(0.f, 0.f);
+                    for (int u = 0; u < 8; ++u) v[u] = q[u] >= 0 ? pairv[q[u]] : make_float2(0.f, 0.f);
 #pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    if (q[u] >= 0) {
-                        two_sum_acc(vh, vl, v[u].x);
-                        vl += v[u].y;
-                    }
+                    for (int u = 0; u < 8; ++u)
+                        if (q[u] >= 0) {
+                            two_sum_acc(vh, vl, v[u].x);
+                            vl += v[u].y;
+                        }
+                }
+                const double Vt = vown + ((double)vh + (double)vl);
+                V[p] = Vt;
+                const double c = 0.5 * (W[p] * Vt);
+                cj[p] = c;
+                const float cf = (float)c;
+                cj32[p] = cf;
+                if (A.cmax) {
+                    cbound[t] = fabsf(cf) * A.winv[p];
+                    cchunk[t] = (int)(p / A.chunk_pts);
+                }
+                ej += c * rho[p];
             }
-            const double Vt = vown + ((double)vh + (double)vl);
-            V[p] = Vt;
-            const double c = 0.5 * (W[p] * Vt);
-            cj[p] = c;
-            cj32[p] = (float)c;
-            ej += c * rho[p];
+        }
+        if (A.cmax) {                       // every lane of the warp, valid pair or not
+            warp_chunk_max(A.cmax, cchunk[0], cbound[0]);
+            warp_chunk_max(A.cmax, cchunk[1], cbound[1]);
         }
     }
     ej = block_sum(ej, sh);
@@ -1620,7 +1632,8 @@ StepLaunch<GoArgs> step_gather_own(const dftg_ctx *c, bool rho_scaled)
     s.args = GoArgs{c->npts, c->npad, (size_t)c->natoms * c->nlm * N, c->natoms, c->cell0, N, c->nang, c->nlm, nslab,
                     nsplit, rho_scaled ? 1 : 0, c->d_pairpos, reinterpret_cast<const float2 *>(c->d_pairv), c->d_U32T,
                     c->d_Y32, c->d_invr, c->d_w, c->d_rho, c->d_V, c->d_cj, c->d_cj32, c->d_red, c->d_scal,
-                    c->d_counters + kCntEJ, c->d_lebpair, c->nlebpair};
+                    c->d_counters + kCntEJ, c->d_lebpair, c->nlebpair,
+                    cmax_route(c) ? c->d_ct_cmax + c->ct_nchunk : nullptr, c->d_ct_winv, c->ct_kbpc * 32};
     s.blocks = c->ncell * nslab * nsplit;
     s.smem = sizeof(float) * 2 * (size_t)c->nlm * (kGoSlab + kGoShells);
     return s;
