@@ -699,7 +699,7 @@ def run_batched(dev, nmol=64, reps=10, seed=20261204):
             "mixed_batched_persistent_builds_per_s": nmol / (bat_pt * 1e-3),
             "mixed_batched_graph_builds_per_s": nmol / (bat_gt * 1e-3),
             "persistent_launches_ran": persistent,
-            "launches_per_batch": {"persistent": 10, "graph": "about 10 per molecule"},
+            "launches_per_batch": {"persistent": "8 kernels + 1 memset", "graph": "8 kernels per molecule"},
             "ms_per_batch": {"fp64_sequential": seq64, "mixed_sequential": seqmx, "mixed_graph": bat_g,
                              "mixed_graph_autotuned": bat_gt, "mixed_persistent": bat_p,
                              "mixed_persistent_autotuned": bat_pt, "mixed_persistent_host_wall_one_replay": bat_wall,

@@ -100,6 +100,18 @@ __device__ __forceinline__ dfl df_mul(dfl a, dfl b)
     return df_norm(p, e);
 }
 __device__ __forceinline__ dfl df_fma(dfl acc, dfl a, dfl b) { return df_add(acc, df_mul(a, b)); }
+// s + e += (ah + al)(bh + bl): the leading product exact (TwoProd), the sum
+// compensated (TwoSum), the cross terms and roundings gathered in e
+__device__ __forceinline__ void df_mac(float &s, float &e, float ah, float al, float bh, float bl)
+{
+    const float p = ah * bh;
+    const float pe = fmaf(ah, bh, -p);
+    const float t = s + p;
+    const float bp = t - s;
+    e += ((s - (t - bp)) + (p - bp)) + fmaf(ah, bl, fmaf(al, bh, pe));
+    s = t;
+}
+
 __host__ __device__ __forceinline__ dfl df_from(double x)
 {
     const float h = (float)x;
@@ -251,7 +263,7 @@ __device__ __forceinline__ bool last_block(int *counter, int *s_flag)
 }
 
 // counters of the last-block reductions
-enum { kCntAtoms = 0, kCntLda = 1, kCntEJ = 2, kCntTrace = 3, kNumCounters = 4 };
+enum { kCntAtoms = 0, kCntLda = 1, kCntEJ = 2, kNumCounters = 4 };
 
 }  // namespace dftg
 
@@ -481,14 +493,6 @@ struct SlicePArgs {            // P -> FP16 slices (density operand)
     double *Pcopy;             // also copies P here when not null (the context's own P)
     void *B;
     int *col_exp;
-    // when S is not null: sum_p w rho = 2 tr(P S_grid) and the correction factor
-    // into scal, from per-column partials and the last block
-    const double *S;           // S_grid [nbf][nbf]
-    const double *atoms;       // [natoms][4]: x, y, z, Z
-    int natoms;
-    double *part;              // [nbf] column partials
-    int *counter;
-    double *scal;
 };
 struct DensTcArgs {            // rho on the tensor cores
     int nbf, KP, NP, ntiles;
@@ -498,13 +502,18 @@ struct DensTcArgs {            // rho on the tensor cores
     const int *col_exp;
     double *rho;
     int *err;
-    // correct: rho times the correction factor scal[kScalScale] (written by the
-    // P-slicing step), and the rho w_becke hi / lo planes into rw32 when not null
+    // correct: rho times the correction factor sum Z / (2 tr(P S_grid)), formed by
+    // the epilogue warps of every CTA before their first tile (block 0 writes it
+    // and the total to scal), and the rho w_becke hi / lo planes into rw32 when
+    // not null
     int correct;
     size_t npad;
-    const double *scal;
+    double *scal;
     const float *wb2;          // [2][npad] FP32 hi / lo planes of w_becke
     float *rw32;
+    const double *P, *S;       // the context's P and S_grid [nbf][nbf]
+    const double *atoms;       // [natoms][4]: x, y, z, Z
+    int natoms;
 };
 struct SumsArgs {              // per-atom sums of w rho, correction factor
     size_t per_atom;
@@ -626,15 +635,15 @@ int mark(dftg_ctx *c, const char *name);
 int launch_grid(dftg_ctx *c);
 int launch_amplitudes(dftg_ctx *c);
 // k_density.cu
-// fused: the whole build's form on the S_grid route (the correction factor
-// from the P-slicing step, no atom-sum pass; the density epilogue applies it
-// and writes the rho w_becke planes)
+// fused: the whole build's form on the S_grid route (the density epilogue forms
+// the correction factor from 2 tr(P S_grid), applies it and writes the rho
+// w_becke planes; no atom-sum pass)
 int launch_density(dftg_ctx *c, bool fused = false);
 enum { kSumsOnly = 0, kSumsCorrect = 1, kSumsFactor = 2 };
 // k_density_tc.cu
 int density_tc_setup(dftg_ctx *c);
 // the mixed build takes the density correction's total from 2 tr(P S_grid)
-// in the P-slicing step (no atom-sum pass)
+// in the density pass (no atom-sum pass)
 bool sgrid_route(const dftg_ctx *c);
 // the whole mixed build takes the contraction's coefficient bounds from the
 // point kernel and the potential gather (atomic chunk maxima), no bounds pass
@@ -691,7 +700,7 @@ int ct_launch_cexp(dftg_ctx *c, int nkb, int kbpc, int nchunk, const float *cx, 
 // and shared memory; the single build launches exactly these), and the batch's
 // grouped launch of each step over all molecules (device argument arrays, one
 // queue per launch).
-StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy, bool fused);
+StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy);
 StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c, bool fused);
 StepLaunch<SumsArgs> step_atom_sums(const dftg_ctx *c, int mode);
 StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n, bool write_rw);

@@ -33,7 +33,10 @@
 // memory per tile.
 // Whole-build form: the density correction's total is known before this pass,
 // sum_p w rho = 2 tr(P S_grid) with S_grid = Phi^T diag(w) Phi made once per
-// grid, so the P-slicing step forms the trace and the factor (no atom-sum pass).
+// grid, so the epilogue warps form the factor while the first tile's copies
+// and products run, apply it, and write the rho w_becke planes for the
+// multipoles (no atom-sum pass; the LDA point kernel then runs beside the
+// Hartree steps).
 // Persistent over tiles: three A stages and two TMEM accumulator sets, so the
 // copies of the next tiles and the MMAs of one tile overlap the epilogue of the
 // previous one.  Every mbarrier wait is bounded: on expiry the CTA records an
@@ -79,6 +82,36 @@ struct TcShared {
 
 // the CTA's mbarriers and TMEM address (one instance in every kernel that uses them)
 __shared__ TcShared tc_sh;
+
+// The density correction factor sum Z / sum_p w rho with sum_p w rho =
+// 2 tr(P S_grid) (moleculargrid.cpp:132-146), by the epilogue warps (named
+// barrier 3) in a fixed order, so every CTA forms the same value; block 0 writes
+// the total and the factor to scal.
+__device__ __forceinline__ double density_factor(const DensTcArgs &a, int vb)
+{
+    __shared__ double s_tr[kTcEpiWarps];
+    __shared__ double s_cf;
+    const int et = (int)threadIdx.x - 64, lane = threadIdx.x & 31;   // epilogue thread 0 .. 32 kTcEpiWarps - 1
+    const int nn = a.nbf * a.nbf;
+    double t = 0.0;
+    for (int i = et; i < nn; i += kTcEpiWarps * 32) t = fma(a.P[i], a.S[i], t);
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) s_tr[et >> 5] = t;
+    asm volatile("bar.sync 3, %0;" ::"n"(kTcEpiWarps * 32) : "memory");
+    if (et == 0) {
+        double tr = 0.0, charge = 0.0;
+        for (int i = 0; i < kTcEpiWarps; ++i) tr += s_tr[i];
+        for (int i = 0; i < a.natoms; ++i) charge += a.atoms[4 * i + 3];
+        const double total = 2.0 * tr;
+        s_cf = charge / total;
+        if (vb == 0) {
+            a.scal[kScalSum] = total;
+            a.scal[kScalScale] = s_cf;
+        }
+    }
+    asm volatile("bar.sync 3, %0;" ::"n"(kTcEpiWarps * 32) : "memory");
+    return s_cf;
+}
 
 // One CTA's share of one molecule's tiles (vb, vb + nvb, ...): initialises the
 // mbarriers, stages the B slices, runs the producer / MMA / epilogue roles and
@@ -206,7 +239,7 @@ __device__ __forceinline__ bool density_tc_cta(const DensTcArgs args, int vb, in
         const int half = ((warp - 2) >> 2) & 1; // 8-column groups 8 half, 8 half + 16, ...
         const int r = q * 32 + lane;            // row of the tile = TMEM lane
         const int kc = KP / 8;
-        const double cf = args.correct ? __ldcg(args.scal + kScalScale) : 1.0;
+        const double cf = args.correct ? density_factor(args, vb) : 1.0;
         for (int it = eg; it < my_tiles; it += 2) {
             const int s = it % kTcStages;
             const int nb = it >> 1;
@@ -456,76 +489,44 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
 // layout: one warp per column, lanes over the rows; with Pcopy the warp also
 // copies its column of P there
 // One block of the P slicing (a warp per column nu of B): the column's
-// exponent and FP16 slices, and with a.S its share of tr(P S_grid); the
-// molecule's last block (of nvb) then writes sum_p w rho = 2 tr(P S_grid) and
-// the correction factor sum Z / sum_p w rho (moleculargrid.cpp:132-146), the
-// per-column partials summed in column order.
-__device__ __forceinline__ void slice_P_block(const SlicePArgs a, int vb, int nvb)
+// exponent and FP16 slices (and the copy of P into the context when Pcopy).
+__device__ __forceinline__ void slice_P_block(const SlicePArgs a, int vb)
 {
-    __shared__ int s_last;
     const int nbf = a.nbf, KP = a.KP, NP = a.NP;
     const double *__restrict__ P = a.P;
     uint16_t *__restrict__ B = static_cast<uint16_t *>(a.B);
     const int nu = vb * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (nu < NP) {
-        const unsigned long long *__restrict__ Pb = reinterpret_cast<const unsigned long long *>(P);
-        unsigned long long mx = 0ull;
-        double tr = 0.0;
-        if (nu < nbf)
-            for (int mu = lane; mu < nbf; mu += 32) {
-                const unsigned long long v = Pb[(size_t)nu * nbf + mu];
-                if (a.Pcopy) reinterpret_cast<unsigned long long *>(a.Pcopy)[(size_t)nu * nbf + mu] = v;
-                mx = max(mx, v & 0x7fffffffffffffffull);
-                if (a.S) tr = fma(__longlong_as_double((long long)v), a.S[(size_t)nu * nbf + mu], tr);
-            }
-        for (int o = 16; o > 0; o >>= 1) {
-            mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    if (nu >= NP) return;
+    const unsigned long long *__restrict__ Pb = reinterpret_cast<const unsigned long long *>(P);
+    unsigned long long mx = 0ull;
+    if (nu < nbf)
+        for (int mu = lane; mu < nbf; mu += 32) {
+            const unsigned long long v = Pb[(size_t)nu * nbf + mu];
+            if (a.Pcopy) reinterpret_cast<unsigned long long *>(a.Pcopy)[(size_t)nu * nbf + mu] = v;
+            mx = max(mx, v & 0x7fffffffffffffffull);
         }
-        const int e = exp_above(mx);
-        if (nu < nbf && lane == 0) {
-            a.col_exp[nu] = e;
-            if (a.S) a.part[nu] = tr;
-        }
-        const size_t slice = (size_t)NP * KP;
-        for (int mu = lane; mu < KP; mu += 32) {
-            uint16_t h[kTcSlices];
-            slice3_f16((nu < nbf && mu < nbf) ? fixed30(Pb[(size_t)nu * nbf + mu], e) : 0ll, h);
-            const size_t o = core_off(nu, mu, KP / 8) / 2;
-            for (int i = 0; i < kTcSlices; ++i) B[(size_t)i * slice + o] = h[i];
-        }
-    }
-    if (!a.S || !last_block_of(a.counter, nvb, &s_last)) return;
-    if (threadIdx.x < 32) {
-        // lane l: columns l, l + 32, ..., then a fixed shuffle tree (lane 0's order)
-        double t = 0.0, charge = 0.0;
-        for (int n = lane; n < nbf; n += 32) t += __ldcg(a.part + n);
-        for (int i = lane; i < a.natoms; i += 32) charge += a.atoms[4 * i + 3];
-        for (int o = 16; o > 0; o >>= 1) {
-            t += __shfl_xor_sync(0xffffffffu, t, o);
-            charge += __shfl_xor_sync(0xffffffffu, charge, o);
-        }
-        if (lane == 0) {
-            const double total = 2.0 * t;
-            a.scal[kScalSum] = total;
-            a.scal[kScalScale] = charge / total;
-        }
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const int e = exp_above(mx);
+    if (nu < nbf && lane == 0) a.col_exp[nu] = e;
+    const size_t slice = (size_t)NP * KP;
+    for (int mu = lane; mu < KP; mu += 32) {
+        uint16_t h[kTcSlices];
+        slice3_f16((nu < nbf && mu < nbf) ? fixed30(Pb[(size_t)nu * nbf + mu], e) : 0ll, h);
+        const size_t o = core_off(nu, mu, KP / 8) / 2;
+        for (int i = 0; i < kTcSlices; ++i) B[(size_t)i * slice + o] = h[i];
     }
 }
 
 constexpr int kSlicePThreads = 128;
 
-__global__ void __launch_bounds__(kSlicePThreads) k_slice_P(const SlicePArgs a)
-{
-    slice_P_block(a, (int)blockIdx.x, (int)gridDim.x);
-}
+__global__ void __launch_bounds__(kSlicePThreads) k_slice_P(const SlicePArgs a) { slice_P_block(a, (int)blockIdx.x); }
 
 __global__ void __launch_bounds__(kSlicePThreads) k_slice_P_group(const SlicePArgs *__restrict__ args, GroupQueue q)
 {
     __shared__ int s_item;
-    gq_run(q, &s_item, [&](int m, int vb, int nvb) {
+    gq_run(q, &s_item, [&](int m, int vb, int) {
         const SlicePArgs a = args[m];
-        slice_P_block(a, vb, nvb);
+        slice_P_block(a, vb);
         return true;
     });
 }
@@ -537,11 +538,13 @@ size_t density_tc_smem(int KP, int NP)
 
 bool density_tc_supported(int nbf) { return nbf <= kTcMaxK; }
 
-// S_grid = Phi^T diag(w) Phi over the grid points, FP64, once per grid: with it
+// S_grid = Phi^T diag(w) Phi over the grid points, once per grid: with it
 // sum_p w_p rho_p = 2 tr(P S_grid) is known from P before the density pass.
 // Block b sums the pairs (mu <= nu) over points [b kSgChunk, (b + 1) kSgChunk)
-// into part[b][pair]; k_sgrid_sum adds the blocks in order and mirrors.
-constexpr int kSgThreads = 256, kSgPts = 32, kSgChunk = 1024;
+// in double-float arithmetic (FP32 TwoProd / TwoSum, about 2^-44 relative; the
+// FP64 pipe of this GPU is narrow) into part[b][pair] as FP64; k_sgrid_sum adds
+// the blocks in order and mirrors.
+constexpr int kSgThreads = 256, kSgPts = 16, kSgChunk = 1024;
 constexpr int kSgPairsMax = kTcMaxK * (kTcMaxK + 1) / 2;
 constexpr int kSgPerThread = (kSgPairsMax + kSgThreads - 1) / kSgThreads;
 
@@ -549,8 +552,8 @@ __global__ void __launch_bounds__(kSgThreads) k_sgrid_part(int nbf, size_t npts,
                                                            const double *__restrict__ phi,
                                                            const double *__restrict__ w, double *__restrict__ part)
 {
-    __shared__ double sphi[kTcMaxK][kSgPts + 1];
-    __shared__ double sw[kSgPts];
+    __shared__ float2 sph[kTcMaxK][kSgPts + 1];     // phi as (hi, lo)
+    __shared__ float2 swph[kTcMaxK][kSgPts + 1];    // w phi as (hi, lo)
     __shared__ short2 spair[kSgPairsMax];
     const int npair = nbf * (nbf + 1) / 2, tid = threadIdx.x;
     for (int k = tid; k < npair; k += kSgThreads) {      // k = nu (nu + 1) / 2 + mu, mu <= nu
@@ -559,33 +562,42 @@ __global__ void __launch_bounds__(kSgThreads) k_sgrid_part(int nbf, size_t npts,
         while ((nu + 1) * (nu + 2) / 2 <= k) ++nu;
         spair[k] = make_short2((short)(k - nu * (nu + 1) / 2), (short)nu);
     }
-    double acc[kSgPerThread];
+    float as[kSgPerThread], ae[kSgPerThread];
 #pragma unroll
-    for (int q = 0; q < kSgPerThread; ++q) acc[q] = 0.0;
+    for (int q = 0; q < kSgPerThread; ++q) as[q] = ae[q] = 0.f;
     const size_t p0 = (size_t)blockIdx.x * kSgChunk, p1 = min(npts, p0 + kSgChunk);
     for (size_t s0 = p0; s0 < p1; s0 += kSgPts) {
         __syncthreads();
         for (int e = tid; e < nbf * kSgPts; e += kSgThreads) {
             const int mu = e / kSgPts, j = e % kSgPts;
-            sphi[mu][j] = s0 + j < p1 ? phi[(size_t)mu * npad + s0 + j] : 0.0;
+            const bool in = s0 + j < p1;
+            // hi / lo split of the FP64 values with integer operations
+            const dfl f = df_from_bits(in ? phi[(size_t)mu * npad + s0 + j] : 0.0);
+            const dfl wf = df_mul(df_from_bits(in ? w[s0 + j] : 0.0), f);
+            sph[mu][j] = make_float2(f.h, f.l);
+            swph[mu][j] = make_float2(wf.h, wf.l);
         }
-        if (tid < kSgPts) sw[tid] = s0 + tid < p1 ? w[s0 + tid] : 0.0;
         __syncthreads();
 #pragma unroll
         for (int q = 0; q < kSgPerThread; ++q) {
             const int k = tid + q * kSgThreads;
             if (k < npair) {
                 const short2 mn = spair[k];
-                double t = acc[q];
-                for (int j = 0; j < kSgPts; ++j) t = fma(sw[j] * sphi[mn.x][j], sphi[mn.y][j], t);
-                acc[q] = t;
+                float s = as[q], e = ae[q];
+#pragma unroll 4
+                for (int j = 0; j < kSgPts; ++j) {
+                    const float2 a = swph[mn.x][j], b = sph[mn.y][j];
+                    df_mac(s, e, a.x, a.y, b.x, b.y);
+                }
+                as[q] = s;
+                ae[q] = e;
             }
         }
     }
 #pragma unroll
     for (int q = 0; q < kSgPerThread; ++q) {
         const int k = tid + q * kSgThreads;
-        if (k < npair) part[(size_t)blockIdx.x * npair + k] = acc[q];
+        if (k < npair) part[(size_t)blockIdx.x * npair + k] = df_to(df_norm(as[q], ae[q]));
     }
 }
 
@@ -659,13 +671,10 @@ int density_tc_setup(dftg_ctx *c)
     return DFTG_OK;
 }
 
-StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy, bool fused)
+StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy)
 {
     StepLaunch<SlicePArgs> s;
-    const bool tr = fused && sgrid_route(c);
-    s.args = SlicePArgs{c->nbf, c->tc_KP, c->tc_NP, P, Pcopy, c->d_tcB, c->d_tc_colexp,
-                        tr ? c->d_sgrid : nullptr, c->d_atoms, c->natoms, c->d_red, c->d_counters + kCntTrace,
-                        c->d_scal};
+    s.args = SlicePArgs{c->nbf, c->tc_KP, c->tc_NP, P, Pcopy, c->d_tcB, c->d_tc_colexp};
     s.blocks = (c->tc_NP + kSlicePThreads / 32 - 1) / (kSlicePThreads / 32);
     s.smem = 0;
     return s;
@@ -679,7 +688,7 @@ StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c, bool fused)
                         reinterpret_cast<const unsigned char *>(c->d_tcA), c->d_tc_rowexp,
                         reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag,
                         correct ? 1 : 0, c->npad, c->d_scal, c->d_wsplit + 2 * c->npad,
-                        correct && rw_planes(c) ? c->d_rw32 : nullptr};
+                        correct && rw_planes(c) ? c->d_rw32 : nullptr, c->d_P, c->d_sgrid, c->d_atoms, c->natoms};
     s.blocks = c->tc_grid;
     s.smem = density_tc_smem(c->tc_KP, c->tc_NP);
     return s;
@@ -687,7 +696,7 @@ StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c, bool fused)
 
 int launch_density_tc(dftg_ctx *c, bool fused)
 {
-    const StepLaunch<SlicePArgs> sp = step_slice_P(c, c->d_P, nullptr, fused);
+    const StepLaunch<SlicePArgs> sp = step_slice_P(c, c->d_P, nullptr);
     k_slice_P<<<sp.blocks, kSlicePThreads, 0, c->stream>>>(sp.args);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "density_slices");

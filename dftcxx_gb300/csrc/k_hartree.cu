@@ -457,16 +457,6 @@ __global__ void k_rholm(int nrad, int nang, int nlm, int cell0, const double *__
 // epilogue functor receives with their slice index.
 constexpr int kDgBM = 16, kDgBN = 32, kDgBK = 16;
 
-__device__ __forceinline__ void df_mac(float &s, float &e, float ah, float al, float bh, float bl)
-{
-    const float p = ah * bh;
-    const float pe = fmaf(ah, bh, -p);
-    const float t = s + p;
-    const float bp = t - s;
-    e += ((s - (t - bp)) + (p - bp)) + fmaf(ah, bl, fmaf(al, bh, pe));
-    s = t;
-}
-
 template <class Epi>
 __global__ void __launch_bounds__(128) k_dfgemm(int M, int N, int K, const float *__restrict__ Ah,
                                                 const float *__restrict__ Al, int lda, const float *__restrict__ Bh,
