@@ -493,6 +493,8 @@ struct SlicePArgs {            // P -> FP16 slices (density operand)
     double *Pcopy;             // also copies P here when not null (the context's own P)
     void *B;
     int *col_exp;
+    const double *S;           // when not null: tr[nu] = sum_mu P[nu][mu] S_grid[nu][mu]
+    double *tr;
 };
 struct DensTcArgs {            // rho on the tensor cores
     int nbf, KP, NP, ntiles;
@@ -503,15 +505,15 @@ struct DensTcArgs {            // rho on the tensor cores
     double *rho;
     int *err;
     // correct: rho times the correction factor sum Z / (2 tr(P S_grid)), formed by
-    // the epilogue warps of every CTA before their first tile (block 0 writes it
-    // and the total to scal), and the rho w_becke hi / lo planes into rw32 when
-    // not null
+    // the epilogue warps of every CTA before their first tile from the P-slicing
+    // step's column partials (block 0 writes it and the total to scal), and the
+    // rho w_becke hi / lo planes into rw32 when not null
     int correct;
     size_t npad;
     double *scal;
     const float *wb2;          // [2][npad] FP32 hi / lo planes of w_becke
     float *rw32;
-    const double *P, *S;       // the context's P and S_grid [nbf][nbf]
+    const double *tr;          // [nbf] column partials of tr(P S_grid) (the P-slicing step)
     const double *atoms;       // [natoms][4]: x, y, z, Z
     int natoms;
 };
@@ -700,7 +702,7 @@ int ct_launch_cexp(dftg_ctx *c, int nkb, int kbpc, int nchunk, const float *cx, 
 // and shared memory; the single build launches exactly these), and the batch's
 // grouped launch of each step over all molecules (device argument arrays, one
 // queue per launch).
-StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy);
+StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy, bool fused);
 StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c, bool fused);
 StepLaunch<SumsArgs> step_atom_sums(const dftg_ctx *c, int mode);
 StepLaunch<LdaArgs> step_lda(const dftg_ctx *c, bool apply_scale, bool with_n, bool write_rw);

@@ -98,7 +98,7 @@ int batch_plan_create(dftg_ctx *const *ctx, int n, const double *const *P, doubl
         const dftg_ctx *c = ctx[i];
         if (!batch_group_eligible(c)) { set_error("context %d cannot join a persistent batch", i); return DFTG_ERR_STATE; }
         if (c->lmax != lmax) lmax = -1;
-        s0[i] = step_slice_P(c, P[i], P[i] != c->d_P ? c->d_P : nullptr);
+        s0[i] = step_slice_P(c, P[i], P[i] != c->d_P ? c->d_P : nullptr, true);
         s1[i] = step_density_tc(c, true);
         s2[i] = step_atom_sums(c, kSumsFactor);
         const bool route = sgrid_route(c);

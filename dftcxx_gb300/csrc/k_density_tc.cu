@@ -33,8 +33,9 @@
 // memory per tile.
 // Whole-build form: the density correction's total is known before this pass,
 // sum_p w rho = 2 tr(P S_grid) with S_grid = Phi^T diag(w) Phi made once per
-// grid, so the epilogue warps form the factor while the first tile's copies
-// and products run, apply it, and write the rho w_becke planes for the
+// grid: the P-slicing step forms the column partials of the trace, the epilogue
+// warps sum them (in a fixed order, before their first tile) into the factor,
+// apply it, and write the rho w_becke planes for the
 // multipoles (no atom-sum pass; the LDA point kernel then runs beside the
 // Hartree steps).
 // Persistent over tiles: three A stages and two TMEM accumulator sets, so the
@@ -84,29 +85,30 @@ struct TcShared {
 __shared__ TcShared tc_sh;
 
 // The density correction factor sum Z / sum_p w rho with sum_p w rho =
-// 2 tr(P S_grid) (moleculargrid.cpp:132-146), by the epilogue warps (named
-// barrier 3) in a fixed order, so every CTA forms the same value; block 0 writes
-// the total and the factor to scal.
+// 2 tr(P S_grid) (moleculargrid.cpp:132-146), from the P-slicing step's column
+// partials summed in a fixed order by the first epilogue warp (lanes over
+// columns, then a fixed shuffle tree), so every CTA forms the same value;
+// block 0 writes the total and the factor to scal.  Named barrier 3 over the
+// epilogue warps.
 __device__ __forceinline__ double density_factor(const DensTcArgs &a, int vb)
 {
-    __shared__ double s_tr[kTcEpiWarps];
     __shared__ double s_cf;
     const int et = (int)threadIdx.x - 64, lane = threadIdx.x & 31;   // epilogue thread 0 .. 32 kTcEpiWarps - 1
-    const int nn = a.nbf * a.nbf;
-    double t = 0.0;
-    for (int i = et; i < nn; i += kTcEpiWarps * 32) t = fma(a.P[i], a.S[i], t);
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (lane == 0) s_tr[et >> 5] = t;
-    asm volatile("bar.sync 3, %0;" ::"n"(kTcEpiWarps * 32) : "memory");
-    if (et == 0) {
-        double tr = 0.0, charge = 0.0;
-        for (int i = 0; i < kTcEpiWarps; ++i) tr += s_tr[i];
-        for (int i = 0; i < a.natoms; ++i) charge += a.atoms[4 * i + 3];
-        const double total = 2.0 * tr;
-        s_cf = charge / total;
-        if (vb == 0) {
-            a.scal[kScalSum] = total;
-            a.scal[kScalScale] = s_cf;
+    if (et < 32) {
+        double t = 0.0, charge = 0.0;
+        for (int n = lane; n < a.nbf; n += 32) t += a.tr[n];
+        for (int i = lane; i < a.natoms; i += 32) charge += a.atoms[4 * i + 3];
+        for (int o = 16; o > 0; o >>= 1) {
+            t += __shfl_xor_sync(0xffffffffu, t, o);
+            charge += __shfl_xor_sync(0xffffffffu, charge, o);
+        }
+        if (et == 0) {
+            const double total = 2.0 * t;
+            s_cf = charge / total;
+            if (vb == 0) {
+                a.scal[kScalSum] = total;
+                a.scal[kScalScale] = s_cf;
+            }
         }
     }
     asm volatile("bar.sync 3, %0;" ::"n"(kTcEpiWarps * 32) : "memory");
@@ -489,7 +491,8 @@ __global__ void k_slice_phi(int nbf, int KP, size_t npad, int ntiles, const doub
 // layout: one warp per column, lanes over the rows; with Pcopy the warp also
 // copies its column of P there
 // One block of the P slicing (a warp per column nu of B): the column's
-// exponent and FP16 slices (and the copy of P into the context when Pcopy).
+// exponent and FP16 slices (and the copy of P into the context when Pcopy), and
+// with S the column's share of tr(P S_grid).
 __device__ __forceinline__ void slice_P_block(const SlicePArgs a, int vb)
 {
     const int nbf = a.nbf, KP = a.KP, NP = a.NP;
@@ -499,15 +502,23 @@ __device__ __forceinline__ void slice_P_block(const SlicePArgs a, int vb)
     if (nu >= NP) return;
     const unsigned long long *__restrict__ Pb = reinterpret_cast<const unsigned long long *>(P);
     unsigned long long mx = 0ull;
+    double t = 0.0;
     if (nu < nbf)
         for (int mu = lane; mu < nbf; mu += 32) {
             const unsigned long long v = Pb[(size_t)nu * nbf + mu];
             if (a.Pcopy) reinterpret_cast<unsigned long long *>(a.Pcopy)[(size_t)nu * nbf + mu] = v;
             mx = max(mx, v & 0x7fffffffffffffffull);
+            if (a.S) t = fma(__longlong_as_double((long long)v), a.S[(size_t)nu * nbf + mu], t);
         }
-    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
     const int e = exp_above(mx);
-    if (nu < nbf && lane == 0) a.col_exp[nu] = e;
+    if (nu < nbf && lane == 0) {
+        a.col_exp[nu] = e;
+        if (a.S) a.tr[nu] = t;
+    }
     const size_t slice = (size_t)NP * KP;
     for (int mu = lane; mu < KP; mu += 32) {
         uint16_t h[kTcSlices];
@@ -545,32 +556,45 @@ bool density_tc_supported(int nbf) { return nbf <= kTcMaxK; }
 // FP64 pipe of this GPU is narrow) into part[b][pair] as FP64; k_sgrid_sum adds
 // the blocks in order and mirrors.
 constexpr int kSgThreads = 256, kSgPts = 16, kSgChunk = 1024;
-constexpr int kSgPairsMax = kTcMaxK * (kTcMaxK + 1) / 2;
-constexpr int kSgPerThread = (kSgPairsMax + kSgThreads - 1) / kSgThreads;
+constexpr int kSgTilesMax = (kTcMaxK / 2) * (kTcMaxK / 2 + 1) / 2;   // 2 x 2 tiles (I <= J)
+constexpr int kSgPerThread = (kSgTilesMax + kSgThreads - 1) / kSgThreads;
 
+// k = j (j + 1) / 2 + i, i <= j
+__device__ __forceinline__ short2 tri_index(int k)
+{
+    int j = (int)((sqrtf(8.f * (float)k + 1.f) - 1.f) * 0.5f);
+    while (j * (j + 1) / 2 > k) --j;
+    while ((j + 1) * (j + 2) / 2 <= k) ++j;
+    return make_short2((short)(k - j * (j + 1) / 2), (short)j);
+}
+
+// A thread takes 2 x 2 tiles (rows 2I, 2I + 1 against columns 2J, 2J + 1,
+// I <= J): four loads serve four products per point.
 __global__ void __launch_bounds__(kSgThreads) k_sgrid_part(int nbf, size_t npts, size_t npad,
                                                            const double *__restrict__ phi,
                                                            const double *__restrict__ w, double *__restrict__ part)
 {
-    __shared__ float2 sph[kTcMaxK][kSgPts + 1];     // phi as (hi, lo)
+    __shared__ float2 sph[kTcMaxK][kSgPts + 1];     // phi as (hi, lo); rows >= nbf zero
     __shared__ float2 swph[kTcMaxK][kSgPts + 1];    // w phi as (hi, lo)
-    __shared__ short2 spair[kSgPairsMax];
     const int npair = nbf * (nbf + 1) / 2, tid = threadIdx.x;
-    for (int k = tid; k < npair; k += kSgThreads) {      // k = nu (nu + 1) / 2 + mu, mu <= nu
-        int nu = (int)((sqrtf(8.f * (float)k + 1.f) - 1.f) * 0.5f);
-        while (nu * (nu + 1) / 2 > k) --nu;
-        while ((nu + 1) * (nu + 2) / 2 <= k) ++nu;
-        spair[k] = make_short2((short)(k - nu * (nu + 1) / 2), (short)nu);
-    }
-    float as[kSgPerThread], ae[kSgPerThread];
+    const int nb2 = (nbf + 1) / 2, ntile = nb2 * (nb2 + 1) / 2;
+    short2 tl[kSgPerThread];
 #pragma unroll
-    for (int q = 0; q < kSgPerThread; ++q) as[q] = ae[q] = 0.f;
+    for (int q = 0; q < kSgPerThread; ++q) {
+        const int t = tid + q * kSgThreads;
+        tl[q] = t < ntile ? tri_index(t) : make_short2(0, 0);
+    }
+    float as[kSgPerThread][4], ae[kSgPerThread][4];
+#pragma unroll
+    for (int q = 0; q < kSgPerThread; ++q)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) as[q][u] = ae[q][u] = 0.f;
     const size_t p0 = (size_t)blockIdx.x * kSgChunk, p1 = min(npts, p0 + kSgChunk);
     for (size_t s0 = p0; s0 < p1; s0 += kSgPts) {
         __syncthreads();
-        for (int e = tid; e < nbf * kSgPts; e += kSgThreads) {
+        for (int e = tid; e < 2 * nb2 * kSgPts; e += kSgThreads) {
             const int mu = e / kSgPts, j = e % kSgPts;
-            const bool in = s0 + j < p1;
+            const bool in = s0 + j < p1 && mu < nbf;
             // hi / lo split of the FP64 values with integer operations
             const dfl f = df_from_bits(in ? phi[(size_t)mu * npad + s0 + j] : 0.0);
             const dfl wf = df_mul(df_from_bits(in ? w[s0 + j] : 0.0), f);
@@ -580,24 +604,28 @@ __global__ void __launch_bounds__(kSgThreads) k_sgrid_part(int nbf, size_t npts,
         __syncthreads();
 #pragma unroll
         for (int q = 0; q < kSgPerThread; ++q) {
-            const int k = tid + q * kSgThreads;
-            if (k < npair) {
-                const short2 mn = spair[k];
-                float s = as[q], e = ae[q];
+            if (tid + q * kSgThreads < ntile) {
+                const int r0 = 2 * tl[q].x, c0 = 2 * tl[q].y;
 #pragma unroll 4
                 for (int j = 0; j < kSgPts; ++j) {
-                    const float2 a = swph[mn.x][j], b = sph[mn.y][j];
-                    df_mac(s, e, a.x, a.y, b.x, b.y);
+                    const float2 a0 = swph[r0][j], a1 = swph[r0 + 1][j], b0 = sph[c0][j], b1 = sph[c0 + 1][j];
+                    df_mac(as[q][0], ae[q][0], a0.x, a0.y, b0.x, b0.y);
+                    df_mac(as[q][1], ae[q][1], a0.x, a0.y, b1.x, b1.y);
+                    df_mac(as[q][2], ae[q][2], a1.x, a1.y, b0.x, b0.y);
+                    df_mac(as[q][3], ae[q][3], a1.x, a1.y, b1.x, b1.y);
                 }
-                as[q] = s;
-                ae[q] = e;
             }
         }
     }
 #pragma unroll
     for (int q = 0; q < kSgPerThread; ++q) {
-        const int k = tid + q * kSgThreads;
-        if (k < npair) part[(size_t)blockIdx.x * npair + k] = df_to(df_norm(as[q], ae[q]));
+        if (tid + q * kSgThreads >= ntile) continue;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int mu = 2 * tl[q].x + (u >> 1), nu = 2 * tl[q].y + (u & 1);
+            if (mu <= nu && nu < nbf)
+                part[(size_t)blockIdx.x * npair + nu * (nu + 1) / 2 + mu] = df_to(df_norm(as[q][u], ae[q][u]));
+        }
     }
 }
 
@@ -671,10 +699,12 @@ int density_tc_setup(dftg_ctx *c)
     return DFTG_OK;
 }
 
-StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy)
+StepLaunch<SlicePArgs> step_slice_P(const dftg_ctx *c, const double *P, double *Pcopy, bool fused)
 {
     StepLaunch<SlicePArgs> s;
-    s.args = SlicePArgs{c->nbf, c->tc_KP, c->tc_NP, P, Pcopy, c->d_tcB, c->d_tc_colexp};
+    const bool tr = fused && sgrid_route(c);
+    s.args = SlicePArgs{c->nbf, c->tc_KP, c->tc_NP, P, Pcopy, c->d_tcB, c->d_tc_colexp, tr ? c->d_sgrid : nullptr,
+                        c->d_red};
     s.blocks = (c->tc_NP + kSlicePThreads / 32 - 1) / (kSlicePThreads / 32);
     s.smem = 0;
     return s;
@@ -688,7 +718,7 @@ StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c, bool fused)
                         reinterpret_cast<const unsigned char *>(c->d_tcA), c->d_tc_rowexp,
                         reinterpret_cast<const unsigned char *>(c->d_tcB), c->d_tc_colexp, c->d_rho, c->d_flag,
                         correct ? 1 : 0, c->npad, c->d_scal, c->d_wsplit + 2 * c->npad,
-                        correct && rw_planes(c) ? c->d_rw32 : nullptr, c->d_P, c->d_sgrid, c->d_atoms, c->natoms};
+                        correct && rw_planes(c) ? c->d_rw32 : nullptr, c->d_red, c->d_atoms, c->natoms};
     s.blocks = c->tc_grid;
     s.smem = density_tc_smem(c->tc_KP, c->tc_NP);
     return s;
@@ -696,7 +726,7 @@ StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c, bool fused)
 
 int launch_density_tc(dftg_ctx *c, bool fused)
 {
-    const StepLaunch<SlicePArgs> sp = step_slice_P(c, c->d_P, nullptr);
+    const StepLaunch<SlicePArgs> sp = step_slice_P(c, c->d_P, nullptr, fused);
     k_slice_P<<<sp.blocks, kSlicePThreads, 0, c->stream>>>(sp.args);
     DFTG_LAUNCH_CHECK();
     DFTG_MARK(c, "density_slices");
