@@ -1036,9 +1036,11 @@ __device__ __forceinline__ void vcross_bins_block(const VcbArgs A, int vb)
     for (int j = 0; j < P; ++j) { ah[j] = 0.f; al[j] = 0.f; cm[j] = 1.f; sm[j] = 0.f; }
 #pragma unroll
     for (int m = 0; m <= lmax; ++m) {
-        float r1[P], r2[P];
+        // for m > 0: sum_l q_l s_lm and sum_l q_l s_l,-m first, then times cos m phi
+        // and sin m phi once per m
+        float r1[P], r2[P], am[P], bm[P];
 #pragma unroll
-        for (int j = 0; j < P; ++j) { r1[j] = 1.f; r2[j] = 0.f; }
+        for (int j = 0; j < P; ++j) { r1[j] = 1.f; r2[j] = 0.f; am[j] = 0.f; bm[j] = 0.f; }
 #pragma unroll
         for (int l = m; l <= lmax; ++l) {
             float q[P];
@@ -1074,15 +1076,20 @@ __device__ __forceinline__ void vcross_bins_block(const VcbArgs A, int vb)
                 for (int j = 0; j < P; ++j) {
                     const float sh = fmaf(t[j], fmaf(t[j], fmaf(t[j], ch.w, ch.z), ch.y), ch.x);
                     const float nh = fmaf(t[j], fmaf(t[j], fmaf(t[j], dh.w, dh.z), dh.y), dh.x);
-                    const float qc = q[j] * cm[j], qs = q[j] * sm[j];
-                    ah[j] = fmaf(qc, sh, fmaf(qs, nh, ah[j]));
+                    am[j] = fmaf(q[j], sh, am[j]);
+                    bm[j] = fmaf(q[j], nh, bm[j]);
                     if (lo) {
+                        const float qc = q[j] * cm[j], qs = q[j] * sm[j];
                         const float sl = fmaf(t[j], fmaf(t[j], fmaf(t[j], cl.w, cl.z), cl.y), cl.x);
                         const float nl = fmaf(t[j], fmaf(t[j], fmaf(t[j], dl.w, dl.z), dl.y), dl.x);
                         al[j] = fmaf(qc, sl, fmaf(qs, nl, al[j]));
                     }
                 }
             }
+        }
+        if (m > 0) {
+#pragma unroll
+            for (int j = 0; j < P; ++j) ah[j] = fmaf(cm[j], am[j], fmaf(sm[j], bm[j], ah[j]));
         }
 #pragma unroll
         for (int j = 0; j < P; ++j) {
