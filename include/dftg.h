@@ -266,13 +266,16 @@ int dftg_backward_profile(dftg_ctx *ctx, double seed_exc, double seed_ej, double
  * molecule at a time, dft.cpp:84-142): many contexts -- molecules or
  * geometries of any size -- built together.  Two forms:
  *   DFTG_BATCH_PERSISTENT (default): every step of the mixed build runs as ONE
- *     persistent launch over all contexts (nine launches per batch); each CTA
+ *     persistent launch over all contexts (eight launches per batch, the LDA
+ *     point kernel on a second branch beside the Hartree launches); each CTA
  *     takes (context, block) work items from a device queue and runs each as
  *     that block of the context's own launch, so every context's results are
- *     bit-identical to its single build.  The per-atom sums and the LDA point
- *     kernel share one launch: a context's point blocks wait, bounded (2 s),
- *     for its correction factor; a wait that gives up is reported by
- *     dftg_batch_status.  Needs every context in mixed precision with the
+ *     bit-identical to its single build.  The point-kernel launch can also
+ *     take per-atom sum items, whose context's point blocks then wait,
+ *     bounded (2 s), for the correction factor; every context a batch accepts
+ *     gets its factor from the density launch instead, so no block waits in a
+ *     build.  A wait that gives up is reported by dftg_batch_status.  Needs
+ *     every context in mixed precision with the
  *     tensor-core density and contraction (nbf <= 80) and <= 256 radial points;
  *     otherwise the batch falls back to the graph of branches.
  *   DFTG_BATCH_GRAPH: each context's kernel sequence on its own stream branch
@@ -294,9 +297,9 @@ int dftg_batch_get_mode(const dftg_batch *b, int *persistent_active);
 /* Synchronise the batch's last launch and report its bounded waits:
  * DFTG_ERR_TIMEOUT when one gave up (the flags are cleared), else DFTG_OK. */
 int dftg_batch_status(dftg_batch *b);
-/* Self-test of the persistent batch's bounded wait: runs the fused atom-sum +
- * point launch with the first context's waits on a flag that nothing sets,
- * limit limit_ms (0 < limit_ms <= 2000); returns DFTG_ERR_TIMEOUT.  The
+/* Self-test of the persistent batch's bounded wait: runs the atom-sum + point
+ * launch with one point item of the first context, which waits on a flag that
+ * nothing sets, limit limit_ms (0 < limit_ms <= 2000); returns DFTG_ERR_TIMEOUT.  The
  * contexts' results are then incomplete until their next build (DFTG_ERR_STATE
  * for calls that need one).  Needs a preceding persistent build. */
 int dftg_batch_selftest_wait(dftg_batch *b, double limit_ms);
