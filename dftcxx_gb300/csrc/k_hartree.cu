@@ -888,9 +888,9 @@ __device__ __forceinline__ void multipole_block(const MpArgs A, int vb)
     }
 }
 
-__global__ void __launch_bounds__(kMpThreads, 3) k_multipole(const MpArgs a) { multipole_block(a, (int)blockIdx.x); }
+__global__ void __launch_bounds__(kMpThreads, 2) k_multipole(const MpArgs a) { multipole_block(a, (int)blockIdx.x); }
 
-__global__ void __launch_bounds__(kMpThreads, 3) k_multipole_group(const MpArgs *__restrict__ args, GroupQueue q)
+__global__ void __launch_bounds__(kMpThreads, 2) k_multipole_group(const MpArgs *__restrict__ args, GroupQueue q)
 {
     __shared__ int s_item;
     gq_run(q, &s_item, [&](int m, int vb, int) {
