@@ -983,7 +983,7 @@ __global__ void __launch_bounds__(128) k_vcross64(size_t npts, size_t npad, int 
     cj32[p] = (float)c;
 }
 
-constexpr int kCrossPerThread = 4;               // pairs per thread of k_vcross_bins
+constexpr int kCrossPerThread = 2;               // pairs per thread of k_vcross_bins
 constexpr int kCrossTask = 128 * kCrossPerThread;  // pairs per block
 // low halves of the spline coefficients are evaluated for l <= kCrossLoLmax:
 // beyond l = 0 they change E_tot of benzene / 6-31G by < 1e-9 Ha
