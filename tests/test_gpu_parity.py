@@ -180,6 +180,27 @@ def test_mixed_contraction_tensor_core_accuracy(gpu_lib, name, basis, nrad, leb)
     assert np.abs(b["J"] - b["J"].T).max() == 0.0 and np.abs(b["XC"] - b["XC"].T).max() == 0.0
 
 
+@pytest.mark.parametrize("name,basis,nrad,leb", [("H2O", "sto3g", 32, 7), ("C6H6", "p631", 20, 8)])
+def test_mixed_correction_factor_from_sgrid(gpu_lib, name, basis, nrad, leb):
+    """The whole mixed build takes the density correction's total from
+    2 tr(P S_grid), S_grid = Phi^T diag(w) Phi made at set-up
+    (moleculargrid.cpp:132-146).  Its corrected density then integrates to
+    sum Z exactly when that total equals sum_p w rho of the same density: the
+    reported N over sum Z is the ratio of the staged sequence's per-atom total
+    to the S_grid total."""
+    from dftcxx_gb300.grid import MolecularGrid
+    Z, xyz = small_molecule(name)
+    mol = Molecule(Z, xyz, basis)
+    g = MolecularGrid(mol, nrad, leb, 6, precision="mixed")
+    P = _density(mol, 5)
+    r = g.fock_build(P)
+    g.set_density(P)
+    total = g.calculate_density()            # sum_p w rho of the mixed density, per-atom sums
+    assert abs(total / mol.nelec - 1.0) > 1e-6   # a density that needs the correction
+    assert abs(r["nelec"] - mol.nelec) < 1e-8 * mol.nelec, (r["nelec"], mol.nelec, total)
+    g.close()
+
+
 def test_batched_builds_match_single_builds(gpu_lib):
     """Four molecules of different sizes and precisions built in one captured
     launch give the same J, XC and energies as their single builds."""
