@@ -983,6 +983,61 @@ __global__ void __launch_bounds__(128) k_vcross64(size_t npts, size_t npad, int 
     cj32[p] = (float)c;
 }
 
+// S_lm = prod_{j = |m| + 1}^{l} (2 j - 1) at lm = l^2 + l + m, l <= kLmaxCap: the
+// scale between the integer recursion R_l^|m| and its monic form (exact in FP32
+// up to l = 8, rounded once above)
+__constant__ float kLegScale[(kLmaxCap + 1) * (kLmaxCap + 1)] = {
+    1.f, 1.f, 1.f, 1.f, 1.f, 3.f,
+    3.f, 3.f, 1.f, 1.f, 5.f, 15.f,
+    15.f, 15.f, 5.f, 1.f, 1.f, 7.f,
+    35.f, 105.f, 105.f, 105.f, 35.f, 7.f,
+    1.f, 1.f, 9.f, 63.f, 315.f, 945.f,
+    945.f, 945.f, 315.f, 63.f, 9.f, 1.f,
+    1.f, 11.f, 99.f, 693.f, 3465.f, 10395.f,
+    10395.f, 10395.f, 3465.f, 693.f, 99.f, 11.f,
+    1.f, 1.f, 13.f, 143.f, 1287.f, 9009.f,
+    45045.f, 135135.f, 135135.f, 135135.f, 45045.f, 9009.f,
+    1287.f, 143.f, 13.f, 1.f, 1.f, 15.f,
+    195.f, 2145.f, 19305.f, 135135.f, 675675.f, 2027025.f,
+    2027025.f, 2027025.f, 675675.f, 135135.f, 19305.f, 2145.f,
+    195.f, 15.f, 1.f, 1.f, 17.f, 255.f,
+    3315.f, 36465.f, 328185.f, 2297295.f, 11486475.f, 3.445942500e+07f,
+    3.445942500e+07f, 3.445942500e+07f, 11486475.f, 2297295.f, 328185.f, 36465.f,
+    3315.f, 255.f, 17.f, 1.f, 1.f, 19.f,
+    323.f, 4845.f, 62985.f, 692835.f, 6235515.f, 4.364860500e+07f,
+    2.182430250e+08f, 6.547290750e+08f, 6.547290750e+08f, 6.547290750e+08f, 2.182430250e+08f, 4.364860500e+07f,
+    6235515.f, 692835.f, 62985.f, 4845.f, 323.f, 19.f,
+    1.f, 1.f, 21.f, 399.f, 6783.f, 101745.f,
+    1322685.f, 14549535.f, 1.309458150e+08f, 9.166207050e+08f, 4.583103525e+09f, 1.374931058e+10f,
+    1.374931058e+10f, 1.374931058e+10f, 4.583103525e+09f, 9.166207050e+08f, 1.309458150e+08f, 14549535.f,
+    1322685.f, 101745.f, 6783.f, 399.f, 21.f, 1.f,
+    1.f, 23.f, 483.f, 9177.f, 156009.f, 2340135.f,
+    3.042175500e+07f, 3.346393050e+08f, 3.011753745e+09f, 2.108227622e+10f, 1.054113811e+11f, 3.162341432e+11f,
+    3.162341432e+11f, 3.162341432e+11f, 1.054113811e+11f, 2.108227622e+10f, 3.011753745e+09f, 3.346393050e+08f,
+    3.042175500e+07f, 2340135.f, 156009.f, 9177.f, 483.f, 23.f,
+    1.f, 1.f, 25.f, 575.f, 12075.f, 229425.f,
+    3900225.f, 5.850337500e+07f, 7.605438750e+08f, 8.365982625e+09f, 7.529384362e+10f, 5.270569054e+11f,
+    2.635284527e+12f, 7.905853581e+12f, 7.905853581e+12f, 7.905853581e+12f, 2.635284527e+12f, 5.270569054e+11f,
+    7.529384362e+10f, 8.365982625e+09f, 7.605438750e+08f, 5.850337500e+07f, 3900225.f, 229425.f,
+    12075.f, 575.f, 25.f, 1.f, 1.f, 27.f,
+    675.f, 15525.f, 326025.f, 6194475.f, 1.053060750e+08f, 1.579591125e+09f,
+    2.053468462e+10f, 2.258815309e+11f, 2.032933778e+12f, 1.423053645e+13f, 7.115268223e+13f, 2.134580467e+14f,
+    2.134580467e+14f, 2.134580467e+14f, 7.115268223e+13f, 1.423053645e+13f, 2.032933778e+12f, 2.258815309e+11f,
+    2.053468462e+10f, 1.579591125e+09f, 1.053060750e+08f, 6194475.f, 326025.f, 15525.f,
+    675.f, 27.f, 1.f, 1.f, 29.f, 783.f,
+    19575.f, 450225.f, 9454725.f, 1.796397750e+08f, 3.053876175e+09f, 4.580814262e+10f,
+    5.955058541e+11f, 6.550564395e+12f, 5.895507956e+13f, 4.126855569e+14f, 2.063427785e+15f, 6.190283354e+15f,
+    6.190283354e+15f, 6.190283354e+15f, 2.063427785e+15f, 4.126855569e+14f, 5.895507956e+13f, 6.550564395e+12f,
+    5.955058541e+11f, 4.580814262e+10f, 3.053876175e+09f, 1.796397750e+08f, 9454725.f, 450225.f,
+    19575.f, 783.f, 29.f, 1.f, 1.f, 31.f,
+    899.f, 24273.f, 606825.f, 13956975.f, 2.930964750e+08f, 5.568833025e+09f,
+    9.467016142e+10f, 1.420052421e+12f, 1.846068148e+13f, 2.030674963e+14f, 1.827607466e+15f, 1.279325226e+16f,
+    6.396626132e+16f, 1.918987840e+17f, 1.918987840e+17f, 1.918987840e+17f, 6.396626132e+16f, 1.279325226e+16f,
+    1.827607466e+15f, 2.030674963e+14f, 1.846068148e+13f, 1.420052421e+12f, 9.467016142e+10f, 5.568833025e+09f,
+    2.930964750e+08f, 13956975.f, 606825.f, 24273.f, 899.f, 31.f,
+    1.f,
+};
+
 constexpr int kCrossPerThread = 2;               // pairs per thread of k_vcross_bins
 constexpr int kCrossTask = 128 * kCrossPerThread;  // pairs per block
 // low halves of the spline coefficients are evaluated for l <= kCrossLoLmax:
@@ -1014,9 +1069,17 @@ __device__ __forceinline__ void vcross_bins_block(const VcbArgs A, int vb)
     const int4 task = tasks[vb];  // start, count, atom k, interval iv
     const int lmax = LMAX >= 0 ? LMAX : lmax_rt;   // compile-time for the common cut-offs
     const int nlm = (lmax + 1) * (lmax + 1);
+    // the high halves scaled by S_lm = prod_{j = |m| + 1}^{l} (2 j - 1), the
+    // scale of the recursion below (one rounding; the low halves are used for
+    // l = 0 only, where S = 1)
     for (int i = threadIdx.x; i < 2 * nlm; i += blockDim.x) {
         const int lm = i >> 1;
-        s_cf[i] = reinterpret_cast<const float4 *>(splm + (((size_t)task.z * nlm + lm) * nrad + task.w) * 8)[i & 1];
+        float4 c = reinterpret_cast<const float4 *>(splm + (((size_t)task.z * nlm + lm) * nrad + task.w) * 8)[i & 1];
+        if ((i & 1) == 0) {
+            const float sc = kLegScale[lm];
+            c = make_float4(c.x * sc, c.y * sc, c.z * sc, c.w * sc);
+        }
+        s_cf[i] = c;
     }
     float ux[P], uy[P], uz[P], ir[P], t[P];
 #pragma unroll
@@ -1044,14 +1107,23 @@ __device__ __forceinline__ void vcross_bins_block(const VcbArgs A, int vb)
 #pragma unroll
         for (int l = m; l <= lmax; ++l) {
             float q[P];
+            // the recursion R_l = (2l-1) z R_{l-1} - (l+m-1)(l-m-1) R_{l-2} divided by
+            // S_l = prod (2j-1): Q_l = z Q_{l-1} - beta_l Q_{l-2}, Q_m = 1, Q_{m+1} = z
             if (l == m) {
 #pragma unroll
                 for (int j = 0; j < P; ++j) q[j] = 1.f;
-            } else {
-                const float fa = (float)(2 * l - 1), fb = (float)((l + m - 1) * (l - m - 1));
+            } else if (l == m + 1) {
 #pragma unroll
                 for (int j = 0; j < P; ++j) {
-                    q[j] = fa * uz[j] * r1[j] - fb * r2[j];
+                    q[j] = uz[j];
+                    r2[j] = r1[j];
+                    r1[j] = q[j];
+                }
+            } else {
+                const float beta = (float)((double)((l + m - 1) * (l - m - 1)) / ((double)(2 * l - 1) * (double)(2 * l - 3)));
+#pragma unroll
+                for (int j = 0; j < P; ++j) {
+                    q[j] = fmaf(uz[j], r1[j], -beta * r2[j]);
                     r2[j] = r1[j];
                     r1[j] = q[j];
                 }
