@@ -95,15 +95,24 @@ __device__ __forceinline__ int exp_bound(uint32_t absbits)
 // BF16 slices, the first an integer
 __device__ __forceinline__ void slice8_fixed(const float2 (&v)[4], uint4 (&out)[kCtSlices])
 {
+    // rint by the shift 1.5 * 2^23: for |x| < 2^22 the FP32 sums x + 1.5 * 2^23 are
+    // spaced by one, so the round-to-nearest-even add rounds x to an integer as
+    // rintf does (a packed add and subtract per pair in place of two rounding
+    // conversions; the byte permute below replaces the leading slice's conversion)
+    const float2 kRint = make_float2(12582912.f, 12582912.f);
     uint32_t w[kCtSlices][4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        const float2 i = make_float2(rintf(v[j].x), rintf(v[j].y));
-        const __nv_bfloat162 h1 = __float22bfloat162_rn(i);        // exact: integers <= 128
+        // i = +0 where rintf gives -0 (x from -0.5 to -0): the MMA's sums are not
+        // invariant to the sign of a zero operand, so the results differ from the
+        // rintf form in the last bits of the correction accumulator
+        const float2 i = f2sub(f2add(v[j], kRint), kRint);
         const float2 x = f2sub(v[j], i);                           // exact
         const __nv_bfloat162 h2 = __float22bfloat162_rn(x);
         const __nv_bfloat162 h3 = __float22bfloat162_rn(f2sub(x, __bfloat1622float2(h2)));
-        w[0][j] = *reinterpret_cast<const uint32_t *>(&h1);
+        // integers of magnitude <= 128 have at most eight significant bits, so their
+        // BF16 encodings are the high halves of their FP32 encodings
+        w[0][j] = __byte_perm(__float_as_uint(i.x), __float_as_uint(i.y), 0x7632);
         w[1][j] = *reinterpret_cast<const uint32_t *>(&h2);
         w[2][j] = *reinterpret_cast<const uint32_t *>(&h3);
     }
