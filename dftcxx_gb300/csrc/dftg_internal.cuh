@@ -37,6 +37,31 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
 #define DFTG_LAUNCH_CHECK() DFTG_CUDA(cudaGetLastError())
 #define DFTG_TRY_L(x) do { int rc_l_ = (x); if (rc_l_ != DFTG_OK) return rc_l_; } while (0)
 
+// Programmatic dependent launch between the kernels of one build: each kernel
+// waits for its predecessors' completion and memory first (griddepcontrol.wait,
+// a no-op for a launch without a programmatic dependency) and signals at its end,
+// so the successor's launch overlaps the tail of the predecessor.
+#if defined(__CUDACC__)
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_signal() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+#endif
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*k)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+                              const Args &...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // compensated FP32 accumulation (Knuth's TwoSum): s + e is the running sum
 __device__ __forceinline__ void two_sum_acc(float &s, float &e, float x)
 {

@@ -573,10 +573,12 @@ __device__ __forceinline__ void contract_tc_free(uint32_t tmem)
 
 __global__ void __launch_bounds__(kCtThreads, 1) k_contract_tc(const CtArgs args)
 {
+    pdl_wait();
     contract_tc_alloc();
     const uint32_t tmem = ct_sh.tmem_base;
     contract_tc_cta<false>(args, 0, 0, tmem);
     contract_tc_free(tmem);
+    pdl_signal();
 }
 
 // the batch's grouped launch: items (molecule, virtual CTA) from the queue,
@@ -725,7 +727,9 @@ __device__ __forceinline__ void contract_tc_reduce_block(const RedArgs A, int vb
 // sums CTAs g, g + 32, ...; the 32 group sums are added in a fixed order.
 __global__ void __launch_bounds__(1024) k_contract_tc_reduce(const RedArgs a)
 {
+    pdl_wait();
     contract_tc_reduce_block(a, (int)blockIdx.x);
+    pdl_signal();
 }
 
 __global__ void __launch_bounds__(1024) k_contract_tc_reduce_group(const RedArgs *__restrict__ args, GroupQueue q)
@@ -868,8 +872,7 @@ int launch_contract_tc_on(dftg_ctx *c, const float *cxc32, const float *cj32)
         DFTG_LAUNCH_CHECK();
         DFTG_MARK(c, "contract_bounds");
     }
-    k_contract_tc<<<ct.blocks, kCtThreads, ct.smem, c->stream>>>(ct.args);
-    DFTG_LAUNCH_CHECK();
+    DFTG_CUDA(launch_pdl(k_contract_tc, ct.blocks, kCtThreads, ct.smem, c->stream, ct.args));
     return DFTG_OK;
 }
 
@@ -904,8 +907,7 @@ int ct_launch_cexp(dftg_ctx *c, int nkb, int kbpc, int nchunk, const float *cx, 
 int launch_contract_tc_reduce_to(dftg_ctx *c, bool want_xc, bool want_j, double *XC, double *J)
 {
     const StepLaunch<RedArgs> st = step_contract_reduce(c, want_xc, want_j, XC, J);
-    k_contract_tc_reduce<<<st.blocks, 1024, 0, c->stream>>>(st.args);
-    DFTG_LAUNCH_CHECK();
+    DFTG_CUDA(launch_pdl(k_contract_tc_reduce, st.blocks, 1024, 0, c->stream, st.args));
     return DFTG_OK;
 }
 

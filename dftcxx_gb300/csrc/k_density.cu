@@ -400,7 +400,9 @@ __device__ __forceinline__ void lda_block(const LdaArgs A, int vb, int nvb)
 template <bool MIXED>
 __global__ void __launch_bounds__(kRedBlock) k_lda(const LdaArgs a)
 {
+    pdl_wait();
     lda_block<MIXED>(a, (int)blockIdx.x, (int)gridDim.x);
+    pdl_signal();
 }
 
 // The batch's per-atom sums and mixed point kernel in one persistent launch.
@@ -556,9 +558,8 @@ int launch_xc_points(dftg_ctx *c, bool apply_scale, bool with_n, bool write_rw)
         return DFTG_ERR_STATE;
     }
     c->rw_ready = st.args.rw32 != nullptr;
-    if (c->prec_mask & kPrecLda) k_lda<true><<<st.blocks, kRedBlock, 0, c->stream>>>(st.args);
-    else k_lda<false><<<st.blocks, kRedBlock, 0, c->stream>>>(st.args);
-    DFTG_LAUNCH_CHECK();
+    if (c->prec_mask & kPrecLda) DFTG_CUDA(launch_pdl(k_lda<true>, st.blocks, kRedBlock, 0, c->stream, st.args));
+    else DFTG_CUDA(launch_pdl(k_lda<false>, st.blocks, kRedBlock, 0, c->stream, st.args));
     DFTG_MARK(c, "lda");
     return DFTG_OK;
 }

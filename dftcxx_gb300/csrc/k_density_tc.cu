@@ -389,10 +389,12 @@ __device__ __forceinline__ void density_tc_free(uint32_t tmem)
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_density_tc(const DensTcArgs args)
 {
+    pdl_wait();
     density_tc_alloc();
     const uint32_t tmem = tc_sh.tmem_base;
     density_tc_cta(args, (int)blockIdx.x, (int)gridDim.x, tmem);
     density_tc_free(tmem);
+    pdl_signal();
 }
 
 // the batch's grouped launch: each CTA runs items (molecule, virtual CTA) from
@@ -530,7 +532,12 @@ __device__ __forceinline__ void slice_P_block(const SlicePArgs a, int vb)
 
 constexpr int kSlicePThreads = 128;
 
-__global__ void __launch_bounds__(kSlicePThreads) k_slice_P(const SlicePArgs a) { slice_P_block(a, (int)blockIdx.x); }
+__global__ void __launch_bounds__(kSlicePThreads) k_slice_P(const SlicePArgs a)
+{
+    pdl_wait();
+    slice_P_block(a, (int)blockIdx.x);
+    pdl_signal();
+}
 
 __global__ void __launch_bounds__(kSlicePThreads) k_slice_P_group(const SlicePArgs *__restrict__ args, GroupQueue q)
 {
@@ -727,12 +734,10 @@ StepLaunch<DensTcArgs> step_density_tc(const dftg_ctx *c, bool fused)
 int launch_density_tc(dftg_ctx *c, bool fused)
 {
     const StepLaunch<SlicePArgs> sp = step_slice_P(c, c->d_P, nullptr, fused);
-    k_slice_P<<<sp.blocks, kSlicePThreads, 0, c->stream>>>(sp.args);
-    DFTG_LAUNCH_CHECK();
+    DFTG_CUDA(launch_pdl(k_slice_P, sp.blocks, kSlicePThreads, 0, c->stream, sp.args));
     DFTG_MARK(c, "density_slices");
     const StepLaunch<DensTcArgs> dn = step_density_tc(c, fused);
-    k_density_tc<<<dn.blocks, kTcThreads, dn.smem, c->stream>>>(dn.args);
-    DFTG_LAUNCH_CHECK();
+    DFTG_CUDA(launch_pdl(k_density_tc, dn.blocks, kTcThreads, dn.smem, c->stream, dn.args));
     return DFTG_OK;
 }
 

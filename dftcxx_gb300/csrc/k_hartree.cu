@@ -888,7 +888,12 @@ __device__ __forceinline__ void multipole_block(const MpArgs A, int vb)
     }
 }
 
-__global__ void __launch_bounds__(kMpThreads, 2) k_multipole(const MpArgs a) { multipole_block(a, (int)blockIdx.x); }
+__global__ void __launch_bounds__(kMpThreads, 2) k_multipole(const MpArgs a)
+{
+    pdl_wait();
+    multipole_block(a, (int)blockIdx.x);
+    pdl_signal();
+}
 
 __global__ void __launch_bounds__(kMpThreads, 2) k_multipole_group(const MpArgs *__restrict__ args, GroupQueue q)
 {
@@ -1184,7 +1189,9 @@ __device__ __forceinline__ void vcross_bins_block(const VcbArgs A, int vb)
 template <int P, int LMAX>
 __global__ void __launch_bounds__(128) k_vcross_bins(const VcbArgs a)
 {
+    pdl_wait();
     vcross_bins_block<P, LMAX>(a, (int)blockIdx.x);
+    pdl_signal();
 }
 
 template <int P, int LMAX>
@@ -1369,7 +1376,9 @@ __device__ __forceinline__ void gather_own_block(const GoArgs A, int b, int nblk
 
 __global__ void __launch_bounds__(kGoThreads) k_vcross_gather_own(const GoArgs a)
 {
+    pdl_wait();
     gather_own_block(a, (int)blockIdx.x, (int)gridDim.x);
+    pdl_signal();
 }
 
 __global__ void __launch_bounds__(kGoThreads) k_vcross_gather_own_group(const GoArgs *__restrict__ args, GroupQueue q)
@@ -1569,9 +1578,9 @@ StepLaunch<VcbArgs> step_vcross_bins(const dftg_ctx *c)
 // the kernel variant of an lmax: fully unrolled for the grid presets' cut-offs
 template <int LMAX>
 struct VcbSingle {
-    static void run(const StepLaunch<VcbArgs> &s, cudaStream_t st)
+    static cudaError_t run(const StepLaunch<VcbArgs> &s, cudaStream_t st)
     {
-        k_vcross_bins<kCrossPerThread, LMAX><<<s.blocks, 128, s.smem, st>>>(s.args);
+        return launch_pdl(k_vcross_bins<kCrossPerThread, LMAX>, s.blocks, 128, s.smem, st, s.args);
     }
 };
 template <int LMAX>
@@ -1590,12 +1599,12 @@ static int launch_vcross_bins(dftg_ctx *c)
 {
     const StepLaunch<VcbArgs> s = step_vcross_bins(c);
     switch (c->lmax) {
-    case 5: VcbSingle<5>::run(s, c->stream); break;
-    case 6: VcbSingle<6>::run(s, c->stream); break;
-    case 8: VcbSingle<8>::run(s, c->stream); break;
-    case 10: VcbSingle<10>::run(s, c->stream); break;
-    case 11: VcbSingle<11>::run(s, c->stream); break;
-    default: VcbSingle<-1>::run(s, c->stream); break;
+    case 5: DFTG_CUDA(VcbSingle<5>::run(s, c->stream)); break;
+    case 6: DFTG_CUDA(VcbSingle<6>::run(s, c->stream)); break;
+    case 8: DFTG_CUDA(VcbSingle<8>::run(s, c->stream)); break;
+    case 10: DFTG_CUDA(VcbSingle<10>::run(s, c->stream)); break;
+    case 11: DFTG_CUDA(VcbSingle<11>::run(s, c->stream)); break;
+    default: DFTG_CUDA(VcbSingle<-1>::run(s, c->stream)); break;
     }
     DFTG_LAUNCH_CHECK();
     return DFTG_OK;
@@ -1657,8 +1666,7 @@ int launch_hartree_multipoles(dftg_ctx *c)
         // rho_lm, Poisson and splines in one launch per (cell, group of l, m rows)
         const StepLaunch<MpArgs> st = step_multipole(c, c->rw_ready);
         if (st.smem > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_multipole), c->device));
-        k_multipole<<<st.blocks, kMpThreads, st.smem, c->stream>>>(st.args);
-        DFTG_LAUNCH_CHECK();
+        DFTG_CUDA(launch_pdl(k_multipole, st.blocks, kMpThreads, st.smem, c->stream, st.args));
         DFTG_MARK(c, "multipole");
         if (!(c->prec_mask & kPrecCross)) {
             // the FP64 cross-atom step takes the own-cell potential from memory:
@@ -1736,8 +1744,7 @@ int launch_hartree_cross(dftg_ctx *c)
             const StepLaunch<GoArgs> st = step_gather_own(c, c->rho_scaled);
             if ((size_t)st.blocks > c->red_elems) { set_error("reduction buffer too small for %d blocks", st.blocks); return DFTG_ERR_STATE; }
             if (st.smem > 48 * 1024) DFTG_TRY_L(allow_max_dyn_smem(reinterpret_cast<const void *>(k_vcross_gather_own), c->device));
-            k_vcross_gather_own<<<st.blocks, kGoThreads, st.smem, c->stream>>>(st.args);
-            DFTG_LAUNCH_CHECK();
+            DFTG_CUDA(launch_pdl(k_vcross_gather_own, st.blocks, kGoThreads, st.smem, c->stream, st.args));
             DFTG_MARK(c, "vcross");
             return DFTG_OK;
         }
