@@ -255,6 +255,7 @@ __device__ __forceinline__ bool contract_tc_cta(const CtArgs A, int vb_, int nvb
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
+    pdl_wait();      // the set-up above reads nothing the preceding kernels write
 
     if (warp < kCtProducers) {
         // ------------------------------------------------------------ producers
@@ -573,7 +574,6 @@ __device__ __forceinline__ void contract_tc_free(uint32_t tmem)
 
 __global__ void __launch_bounds__(kCtThreads, 1) k_contract_tc(const CtArgs args)
 {
-    pdl_wait();
     contract_tc_alloc();
     const uint32_t tmem = ct_sh.tmem_base;
     contract_tc_cta<false>(args, 0, 0, tmem);

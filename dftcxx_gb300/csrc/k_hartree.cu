@@ -1074,18 +1074,6 @@ __device__ __forceinline__ void vcross_bins_block(const VcbArgs A, int vb)
     const int4 task = tasks[vb];  // start, count, atom k, interval iv
     const int lmax = LMAX >= 0 ? LMAX : lmax_rt;   // compile-time for the common cut-offs
     const int nlm = (lmax + 1) * (lmax + 1);
-    // the high halves scaled by S_lm = prod_{j = |m| + 1}^{l} (2 j - 1), the
-    // scale of the recursion below (one rounding; the low halves are used for
-    // l = 0 only, where S = 1)
-    for (int i = threadIdx.x; i < 2 * nlm; i += blockDim.x) {
-        const int lm = i >> 1;
-        float4 c = reinterpret_cast<const float4 *>(splm + (((size_t)task.z * nlm + lm) * nrad + task.w) * 8)[i & 1];
-        if ((i & 1) == 0) {
-            const float sc = kLegScale[lm];
-            c = make_float4(c.x * sc, c.y * sc, c.z * sc, c.w * sc);
-        }
-        s_cf[i] = c;
-    }
     float ux[P], uy[P], uz[P], ir[P], t[P];
 #pragma unroll
     for (int j = 0; j < P; ++j) {
@@ -1097,6 +1085,21 @@ __device__ __forceinline__ void vcross_bins_block(const VcbArgs A, int vb)
         } else {
             ux[j] = 0.f; uy[j] = 0.f; uz[j] = 1.f; ir[j] = 0.f; t[j] = 0.f;
         }
+    }
+    // the pair geometry above is fixed per grid; the coefficients come from the
+    // multipole kernel
+    pdl_wait();
+    // the high halves scaled by S_lm = prod_{j = |m| + 1}^{l} (2 j - 1), the
+    // scale of the recursion below (one rounding; the low halves are used for
+    // l = 0 only, where S = 1)
+    for (int i = threadIdx.x; i < 2 * nlm; i += blockDim.x) {
+        const int lm = i >> 1;
+        float4 c = reinterpret_cast<const float4 *>(splm + (((size_t)task.z * nlm + lm) * nrad + task.w) * 8)[i & 1];
+        if ((i & 1) == 0) {
+            const float sc = kLegScale[lm];
+            c = make_float4(c.x * sc, c.y * sc, c.z * sc, c.w * sc);
+        }
+        s_cf[i] = c;
     }
     __syncthreads();
     float ah[P], al[P], cm[P], sm[P];
@@ -1189,7 +1192,6 @@ __device__ __forceinline__ void vcross_bins_block(const VcbArgs A, int vb)
 template <int P, int LMAX>
 __global__ void __launch_bounds__(128) k_vcross_bins(const VcbArgs a)
 {
-    pdl_wait();
     vcross_bins_block<P, LMAX>(a, (int)blockIdx.x);
     pdl_signal();
 }
